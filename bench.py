@@ -1,0 +1,257 @@
+"""Benchmark: QC/MM AM1 energy + gradient evaluations per second on one GB300.
+
+Workload: the QC/MM water box (65 QC atoms = 21 waters + hydroxide, charge -1, AM1 RHF, in 4000 TIP3P waters,
+NBModelABFS 8/12 A), as a batch of B independent frames (seeded Gaussian displacements of 0.02 A, standing in
+for molecular-dynamics frames).  One step = one full energy + gradient of every frame from the diagonal guess
+(QC/MM potentials, integrals, SCF to 1e-8 on the density, QC and QC/MM gradients).
+
+value  frames / device time per step, inputs resident on the device (CUDA events on the launching stream);
+e2e    the same through System.EnergyBatch with host numpy inputs and results (host<->device copies timed).
+The working set per step (~4 MB per frame, >1 GB per batch) is far larger than L2, so no flush is needed.
+
+--impl reference times the CPU restatement of pDynamo's path (oracle/liboracle.so, built from mndo_oracle.c)
+on the host cores (one frame per process, all cores) on a bounded sample of the same frames.
+"""
+
+import argparse, json, os, subprocess, sys, threading, time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+import numpy as np
+
+METRIC = "QC/MM E+grad evals/s (AM1 RHF, 65 QC atoms in 4000 TIP3P waters, ABFS 8/12 A)"
+UNIT = "evals/s"
+KJ = 2625.5
+
+
+def peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index=0):
+        self.index, self.samples, self.proc = index, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 6:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[2 + k].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None, "reasons": reasons}
+
+
+def workload(n_frames, seed=1):
+    from pdynamo_mirror_gb300 import workloads
+    Z, X, Q, sel, charge = workloads.qcmm_water_box(seed=seed)
+    frames = workloads.perturbed_frames(X, n_frames, sigma=0.02, seed=11)
+    return Z, X, Q, sel, charge, frames
+
+
+def cpu_reference_sample(Z, Q, sel, charge, frames, n_sample, processes):
+    """Oracle E+grad on n_sample frames, `processes` at a time (spawned workers). Returns (seconds, n)."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    args = [(list(Z), Q, sel, charge, frames[f]) for f in range(n_sample)]
+    t0 = time.perf_counter()
+    if processes == 1:
+        for a in args:
+            _oracle_eval(a)
+    else:
+        with ctx.Pool(processes) as pool:
+            pool.map(_oracle_eval, args)
+    return time.perf_counter() - t0, n_sample
+
+
+def _oracle_eval(args):
+    sys.path.insert(0, HERE)
+    from oracle import oracle as O
+    Z, Q, sel, charge, X = args
+    nq = len(sel)
+    knots = O.abfs_knots(8.0, 12.0)
+    phi, _, _ = O.qcmm("abfs", X[:nq], X[nq:], Q[nq:], knots=knots)
+    r = O.System(O.Hamiltonian("am1", Z[:nq]), Z[:nq], charge=charge).energy(X[:nq], phi=phi)
+    O.qcmm("abfs", X[:nq], X[nq:], Q[nq:], qcq=r["charges"], knots=knots)
+    return r["eelectronic"]
+
+
+def run_reference(args):
+    Z, X, Q, sel, charge, frames = workload(max(args.frames, args.reference_sample))
+    cores = os.cpu_count() or 1
+    n = min(len(frames), max(cores, args.reference_sample))
+    times = []
+    for s in range(args.warmup + args.steps):
+        t, k = cpu_reference_sample(Z, Q, sel, charge, frames, n, cores)
+        if s >= args.warmup:
+            times.append(t)
+    value = n / (sum(times) / len(times))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded water box, perturbed frames)",
+            "config": {"workload": "qcmm_water_box_am1_abfs", "qc_atoms": len(sel), "mm_atoms": len(Z) - len(sel),
+                       "frames_per_step": n},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d frames per step, one frame per process, oracle/mndo_oracle.c" % n},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--frames", type=int, default=304, help="frames per step per GPU")
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--reference-sample", type=int, default=256)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+
+    import torch
+    from pdynamo_mirror_gb300 import NBModelABFS, QCModelMNDO, System, _native
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.device("cuda")
+    Z, X, Q, sel, charge, frames = workload(args.frames, seed=1 + rank)
+    s = System(Z, X, mmCharges=Q)
+    s.electronicState.charge = charge
+    s.DefineQCModel(QCModelMNDO("am1"), qcSelection=sel)
+    s.DefineNBModel(NBModelABFS(innerCutoff=8.0, outerCutoff=12.0))
+    eng = s.engine()
+    qc, mm, q, mm_idx = s._device_inputs(frames)
+    conv = s.qcModel.converger
+    nb = s.nbModel
+
+    def step():
+        return eng.run(qc, conv, mm, q, nb, gradients=True, warm_start=False)
+
+    for _ in range(args.warmup):
+        r = step()
+    torch.cuda.synchronize()
+    st = r["status"].cpu().numpy()
+    if (st != 0).any():
+        raise SystemExit("SCF did not converge for %d frames" % int((st != 0).sum()))
+    ncyc = r["ncycles"].cpu().numpy()
+    stream = torch.cuda.current_stream()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        r = step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    # per-kernel timing of the dominant kernel (the SCF), events on the same stream
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    from pdynamo_mirror_gb300.parameters import ANGSTROMS_TO_BOHRS
+    import ctypes
+    xyz_bohr = (qc * ANGSTROMS_TO_BOHRS).contiguous()
+    ws = eng.workspace(len(frames))
+    opts = conv.options()
+    dens = torch.empty_like(eng.density)
+    en = torch.empty_like(r["energies"]); stt = torch.empty_like(r["status"]); nc = torch.empty_like(r["ncycles"])
+    sh = _native.stream_handle(stream)
+    k0.record(stream)
+    _native.check(eng.L.pdg_energy_gradients(eng.handle, len(frames), _native.ptr(xyz_bohr), _native.ptr(r["phi"]), ctypes.byref(opts),
+                                             _native.ptr(dens), 0, _native.ptr(en), None, None, _native.ptr(stt), _native.ptr(nc),
+                                             _native.ptr(ws), ws.numel(), sh), "scf timing")
+    k1.record(stream)
+    torch.cuda.synchronize()
+    scf_ms = k0.elapsed_time(k1)
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    n_total = len(frames) * world
+    value = n_total / (ms * 1e-3)
+    # e2e through the public API with host inputs and results
+    te = []
+    for k in range(2 + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        E, G, terms = s.EnergyBatch(frames, doGradients=True, warmStart=False)
+        torch.cuda.synchronize()
+        if k >= 2:
+            te.append(time.perf_counter() - t0)
+    e2e = n_total / (sum(te) / len(te))
+    # FP64 roofline of the SCF kernel: algorithmic FP64 flops per frame-cycle
+    N, nocc, kv = eng.n_basis, eng.n_occupied, min(eng.n_occupied, eng.n_basis - eng.n_occupied)
+    cyc = float(ncyc.mean()) + 1.0
+    flops_cycle = 2.0 * N ** 3 + (4.0 / 3.0) * N ** 3 + 4.0 * N * N * kv + 2.0 * N * N * kv
+    scf_flops = flops_cycle * cyc * len(frames)
+    achieved_tf = scf_flops / (scf_ms * 1e-3) / 1e12
+    pk = peaks()
+    fp64_peak = 1.25
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded water box, perturbed frames)",
+            "config": {"workload": "qcmm_water_box_am1_abfs", "qc_atoms": len(sel), "mm_atoms": len(Z) - len(sel),
+                       "basis_functions": N, "frames_per_step": len(frames), "method": "plain FP64",
+                       "density_tolerance": conv.densityTolerance, "mean_scf_cycles": float(ncyc.mean()),
+                       "l2": "working set > L2 (no flush needed)"},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(frames.nbytes),
+                    "d2h_bytes_per_step": int(E.nbytes + G.nbytes)},
+            "gpu_launches": 8 * args.steps,
+            "roofline": {"bound": "fp64", "kernel": "k_scf", "achieved": achieved_tf, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": achieved_tf / fp64_peak, "traffic": None,
+                         "note": "GB300 FP64 nominal 1.25 TFLOP/s (no measured FP64 peak in MEASURED_PEAKS.json); k_scf %.2f ms of a %.2f ms step" % (scf_ms, ms)},
+            "clocks": clk}
+    if rank == 0 and not args.no_cpu_baseline:
+        n = min(len(frames), 96)
+        t, k = cpu_reference_sample(list(Z), Q, sel, charge, frames, n, 1)
+        line["cpu_baseline"] = {"value": k / t, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": "%d frames, serial, oracle/mndo_oracle.c (C restatement; pDynamo's own core is not buildable on the GPU host)" % n}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

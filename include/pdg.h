@@ -1,0 +1,158 @@
+/*
+ * pdg.h - C ABI of the GB300 (sm_103a) NDDO QC/MM energy + gradient library (libpdg.so).
+ *
+ * The library replaces pDynamo 1.9.0's C compute core for one path: closed-shell RHF
+ * MNDO/AM1/PM3/PDDG/RM1 energy + analytic gradient with Lowdin-charge QC/MM embedding, as driven by
+ * QCModel.Energy (pMolecule-1.9.0/extensions/pyrex/pMolecule.QCModel.pyx:146-185) and System.Energy
+ * (pMolecule-1.9.0/pMolecule/System.py:272-318).  One call evaluates a whole batch of configurations
+ * ("frames") of the same QC region: integrals, the complete SCF loop, and gradients, on the device.
+ *
+ * Conventions
+ *   - All pointers named d_* are device pointers (cudaMalloc / torch CUDA tensors); h_* are host.
+ *   - The library never allocates or frees caller memory.  Scratch lives in a caller-provided
+ *     workspace whose size pdg_workspace_bytes() reports.
+ *   - Every function returns a pdg_status.  No exception or C++ type crosses this boundary.
+ *   - Work is queued on the stream passed in; functions return before it completes unless stated.
+ *   - A pdg_system may be used from one host thread at a time.
+ *   - Units: coordinates Bohr, energies Hartree, gradients Hartree/Bohr, potentials Hartree/e.
+ *   - Matrices are dense row-major N x N doubles per frame (N = basis functions); basis order per atom
+ *     is s, pz, px, py as in pDynamo (pMolecule-1.9.0/extensions/cinclude/MNDODefinitions.h:16-19).
+ */
+#ifndef PDG_H
+#define PDG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    PDG_OK             = 0,   /* converged / success */
+    PDG_NOT_CONVERGED  = 1,   /* SCF hit maximumSCFCycles (pMolecule.QCModel.pyx:177 raises ValueError) */
+    PDG_NAN            = 2,   /* non-finite energy or density */
+    PDG_DIIS_SINGULAR  = 3,   /* reserved: DIIS never recovered a well-conditioned subspace */
+    PDG_BAD_ARGUMENT   = 4,
+    PDG_CUDA_ERROR     = 5,
+    PDG_TOO_LARGE      = 6    /* a size exceeds a compiled limit */
+} pdg_status;
+
+/* Per-element parameter record: PDG_ELEMENT_STRIDE doubles, all in atomic units, filled by the host
+ * from pDynamo's parameter files (restating pMolecule.MNDOParameters.pyx:309-370 and
+ * MNDOParameters.c:155-930).  Offsets: */
+#define PDG_ELEMENT_STRIDE 96
+enum {
+    PDG_E_Z = 0, PDG_E_NORB = 1, PDG_E_ZCORE = 2, PDG_E_ALP = 3, PDG_E_GPHOT = 4, PDG_E_NG = 5, PDG_E_NPDDG = 6,
+    PDG_E_DD = 7, PDG_E_QQ = 8, PDG_E_PO = 9 /* 9 values */, PDG_E_GSS = 18, PDG_E_GSP = 19, PDG_E_GPP = 20,
+    PDG_E_GP2 = 21, PDG_E_HSP = 22, PDG_E_HPP = 23, PDG_E_BETA = 24 /* 4 */, PDG_E_USPD = 28 /* 4 */,
+    PDG_E_FN1 = 32 /* 4 */, PDG_E_FN2 = 36 /* 4 */, PDG_E_FN3 = 40 /* 4 */, PDG_E_PDDGC = 44 /* 4 */,
+    PDG_E_PDDGE = 48 /* 4 */, PDG_E_EHEAT = 52, PDG_E_EISOL = 53, PDG_E_NSHELL = 54, PDG_E_NPRIM_S = 55,
+    PDG_E_NPRIM_P = 56, PDG_E_EXP_S = 57 /* 6 */, PDG_E_CCBF_S = 63 /* 6 */, PDG_E_EXP_P = 69 /* 6 */,
+    PDG_E_CCBF_P = 75 /* 6 */
+};
+
+#define PDG_MAX_ELEMENTS 16
+#define PDG_MAX_ATOMS    1024
+#define PDG_MAX_BASIS    2048
+
+/* SCF options: the DIISSCFConverger keywords (pMolecule.DIISSCFConverger.pyx:140-150;
+ * defaults DIISSCFConverger.c:27-32). */
+typedef struct {
+    double density_tolerance;   /* 1e-8 */
+    double energy_tolerance;    /* 2e-4 */
+    double diis_onset;          /* 0.2  */
+    int    maximum_scf_cycles;  /* 100  */
+    int    history;             /* 10, at most 16 */
+    int    use_rca;             /* 1: ODA/RCA before DIIS, as the reference default */
+    int    reserved;
+} pdg_scf_options;
+
+/* Energy terms returned per frame (PDG_NENERGY doubles). */
+#define PDG_NENERGY 8
+enum {
+    PDG_EN_TOTAL_ELECTRONIC = 0,   /* QC electronic + QC/MM (what the SCF minimises) */
+    PDG_EN_ELECTRONIC = 1,         /* QCModelMNDOState eelectronic: tr(PH) + tr(PG)/2 */
+    PDG_EN_NUCLEAR = 2,            /* core-core */
+    PDG_EN_BASELINE = 3,           /* sum (eheat - eisol) */
+    PDG_EN_QCMM = 4,               /* q . phi */
+    PDG_EN_ONE_ELECTRON = 5,
+    PDG_EN_TWO_ELECTRON = 6,
+    PDG_EN_RMS_DENSITY = 7         /* final RMS density change */
+};
+
+typedef struct pdg_system pdg_system;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int pdg_version(void);
+
+/* Create a QC region.  Replaces the set-up that pDynamo performs in QCModelMNDO.SetUp
+ * (pMolecule.QCModelMNDO.pyx:623-672 -> QCModelMNDOState_Setup, QCModelMNDOState.c:477) and
+ * QCAtomContainer assignment (pMolecule.QCAtomContainer.pyx:218-278).
+ *   h_elements     n_elements * PDG_ELEMENT_STRIDE doubles
+ *   h_atom_element n_atoms indices into h_elements
+ *   charge         total QC charge (closed shell: nuclear charge - charge must be even) */
+int pdg_system_create(const double *h_elements, int n_elements, int n_atoms, const int *h_atom_element,
+                      int charge, pdg_system **out);
+int pdg_system_destroy(pdg_system *sys);
+
+/* Basis functions, occupied orbitals and atom-pair count of a system. */
+int pdg_system_info(const pdg_system *sys, int *n_basis, int *n_occupied, int *n_pairs);
+
+/* Workspace bytes needed for a batch of n_frames. */
+size_t pdg_workspace_bytes(const pdg_system *sys, int n_frames);
+
+/* Energy and gradient for a batch of frames.  One call does what one System.Energy(doGradients=True)
+ * does for the QC part of each frame: QCModelMNDO_Integrals (QCModelMNDO.c:1032), the SCF loop of
+ * QCModel.Energy with QCModelMNDO_Fock (:700), QCModelMNDO_QCMMFockLowdin (:1808) and the
+ * DIISSCFConverger (DIISSCFConverger.c:147-770), then QCModelMNDO_Gradients (:732).
+ *   d_xyz        n_frames * n_atoms * 3 (Bohr)
+ *   d_phi        n_frames * n_atoms QC/MM potentials at the QC atoms, or NULL (no QC/MM)
+ *   d_density    n_frames * N * N: in = start density when use_density != 0 (the reference keeps the
+ *                previous density on the configuration, pMolecule.QCModel.pyx:153), else the diagonal
+ *                guess (QCOnePDM.c:280); out = converged density
+ *   d_energies   n_frames * PDG_NENERGY
+ *   d_gradients  n_frames * n_atoms * 3 (Eh/Bohr) or NULL
+ *   d_charges    n_frames * n_atoms Lowdin charges of the final density, or NULL
+ *   d_status     n_frames pdg_status values (PDG_OK or PDG_NOT_CONVERGED / PDG_NAN)
+ *   d_ncycles    n_frames SCF cycle counts, or NULL */
+int pdg_energy_gradients(pdg_system *sys, int n_frames, const double *d_xyz, const double *d_phi,
+                         const pdg_scf_options *options, double *d_density, int use_density,
+                         double *d_energies, double *d_gradients, double *d_charges, int *d_status,
+                         int *d_ncycles, void *d_workspace, size_t workspace_bytes, void *stream);
+
+/* Diagnostics for parity tests: the one-electron matrix H (n_frames * N * N) and the Fock matrix
+ * F = H + G(P) - phi for given densities (QCModelMNDO_Fock + QCMMFockLowdin on one density), with
+ * the energies of that density in d_energies. */
+int pdg_one_electron(pdg_system *sys, int n_frames, const double *d_xyz, double *d_h,
+                     void *d_workspace, size_t workspace_bytes, void *stream);
+int pdg_fock(pdg_system *sys, int n_frames, const double *d_xyz, const double *d_phi, const double *d_density,
+             double *d_fock, double *d_energies, void *d_workspace, size_t workspace_bytes, void *stream);
+/* Gradients (Eh/Bohr) for given densities, no SCF (QCModelMNDO_Gradients on a fixed density). */
+int pdg_gradients(pdg_system *sys, int n_frames, const double *d_xyz, const double *d_density,
+                  double *d_gradients, void *d_workspace, size_t workspace_bytes, void *stream);
+
+/* QC/MM electrostatics with MM point charges.
+ * model 0: NBModelFull, plain 1/r over all pairs (NBModelFull.c:604 potentials, :392 gradients).
+ * model 1: NBModelABFS Delta/Gaussian spline in r^2 with outer cutoff (PairwiseInteraction.c:612, :542);
+ *          the spline is given by n_knots knots d_knots = [x (A^2) | y (a.u.) | y'' (second derivatives)].
+ * Coordinates here are in Angstrom, as the reference evaluates these pair terms in Angstrom.
+ *   d_qc_xyz  n_frames * n_qc * 3,  d_mm_xyz n_frames * n_mm * 3,  d_mm_charges n_mm (shared by frames)
+ *   d_phi     out n_frames * n_qc potentials (a.u.) */
+int pdg_qcmm_potentials(int model, int n_frames, int n_qc, int n_mm, const double *d_qc_xyz,
+                        const double *d_mm_xyz, const double *d_mm_charges, int n_knots, const double *d_knots,
+                        double outer_cutoff, double *d_phi, void *stream);
+/* Gradients (Eh/Bohr) of q_A phi_A with respect to QC and MM coordinates for given QC charges.
+ * d_qc_grad (n_frames*n_qc*3) and d_mm_grad (n_frames*n_mm*3) are overwritten. */
+int pdg_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const double *d_qc_xyz,
+                       const double *d_mm_xyz, const double *d_mm_charges, const double *d_qc_charges,
+                       int n_knots, const double *d_knots, double outer_cutoff,
+                       double *d_qc_grad, double *d_mm_grad, void *stream);
+
+/* Text of the last error on this host thread (never NULL). */
+const char *pdg_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -483,24 +483,28 @@ int ref_abfs_spline ( void *vp, const int n, const double *x, double *f, double 
 int ref_abfs_qcmm ( void *vp, void *vs, const double *qcxyz, const int nMM, const double *mmxyz, const double *mmCharges,
                     const double *qcCharges, double *potentials, double *qcGradients, double *mmGradients )
 {
+    /* . The pair list indexes MM atoms after the QC atoms, as system-wide atom indices do in pDynamo
+       (PairList_FromIntegerPairArray drops pairs with equal indices). */
     PairwiseInteractionABFS *p = ( PairwiseInteractionABFS * ) vp ;
     RefSystem *s = ( RefSystem * ) vs ;
-    Coordinates3 *crd1 = Coordinates3_Allocate ( s->nAtoms ), *crd2 = Coordinates3_Allocate ( nMM ) ;
-    Coordinates3 *grd1 = Coordinates3_Allocate ( s->nAtoms ), *grd2 = Coordinates3_Allocate ( nMM ) ;
-    Real1DArray *q = Real1DArray_Allocate ( nMM, NULL ), *phi = Real1DArray_Allocate ( s->nAtoms, NULL ), *qc = Real1DArray_Allocate ( s->nAtoms, NULL ) ;
-    Integer *indices = ( Integer * ) malloc ( sizeof ( Integer ) * 2 * ( size_t ) s->nAtoms * nMM ) ;
+    int nq = s->nAtoms, nt = s->nAtoms + nMM ;
+    Coordinates3 *crd1 = Coordinates3_Allocate ( nq ), *crd2 = Coordinates3_Allocate ( nt ) ;
+    Coordinates3 *grd1 = Coordinates3_Allocate ( nq ), *grd2 = Coordinates3_Allocate ( nt ) ;
+    Real1DArray *q = Real1DArray_Allocate ( nt, NULL ), *phi = Real1DArray_Allocate ( nq, NULL ), *qc = Real1DArray_Allocate ( nq, NULL ) ;
+    Integer *indices = ( Integer * ) malloc ( sizeof ( Integer ) * 2 * ( size_t ) nq * nMM ) ;
     PairList *list ;
     int i, m, n = 0 ;
-    for ( i = 0 ; i < s->nAtoms ; i++ ) { Coordinates3_SetRow ( crd1, i, qcxyz[3*i], qcxyz[3*i+1], qcxyz[3*i+2] ) ; Real1DArray_Item ( qc, i ) = qcCharges[i] ; }
-    for ( m = 0 ; m < nMM ; m++ ) { Coordinates3_SetRow ( crd2, m, mmxyz[3*m], mmxyz[3*m+1], mmxyz[3*m+2] ) ; Real1DArray_Item ( q, m ) = mmCharges[m] ; }
-    for ( i = 0 ; i < s->nAtoms ; i++ ) for ( m = 0 ; m < nMM ; m++ ) { indices[n++] = i ; indices[n++] = m ; }
-    list = PairList_FromIntegerPairArray ( False, s->nAtoms * nMM, indices ) ;
+    Coordinates3_Set ( crd2, 0.0 ) ; Real1DArray_Set ( q, 0.0 ) ;
+    for ( i = 0 ; i < nq ; i++ ) { Coordinates3_SetRow ( crd1, i, qcxyz[3*i], qcxyz[3*i+1], qcxyz[3*i+2] ) ; Real1DArray_Item ( qc, i ) = qcCharges[i] ; }
+    for ( m = 0 ; m < nMM ; m++ ) { Coordinates3_SetRow ( crd2, nq + m, mmxyz[3*m], mmxyz[3*m+1], mmxyz[3*m+2] ) ; Real1DArray_Item ( q, nq + m ) = mmCharges[m] ; }
+    for ( i = 0 ; i < nq ; i++ ) for ( m = 0 ; m < nMM ; m++ ) { indices[n++] = i ; indices[n++] = nq + m ; }
+    list = PairList_FromIntegerPairArray ( False, nq * nMM, indices ) ;
     Real1DArray_Set ( phi, 0.0 ) ;
     Coordinates3_Set ( grd1, 0.0 ) ; Coordinates3_Set ( grd2, 0.0 ) ;
     PairwiseInteractionABFS_QCMMPotentials ( p, q, s->qcAtoms, list, 1.0, crd1, crd2, phi ) ;
     PairwiseInteractionABFS_QCMMGradients  ( p, q, s->qcAtoms, list, 1.0, crd1, crd2, qc, grd1, grd2 ) ;
-    for ( i = 0 ; i < s->nAtoms ; i++ ) { potentials[i] = Real1DArray_Item ( phi, i ) ; Coordinates3_GetRow ( grd1, i, qcGradients[3*i], qcGradients[3*i+1], qcGradients[3*i+2] ) ; }
-    for ( m = 0 ; m < nMM ; m++ ) Coordinates3_GetRow ( grd2, m, mmGradients[3*m], mmGradients[3*m+1], mmGradients[3*m+2] ) ;
+    for ( i = 0 ; i < nq ; i++ ) { potentials[i] = Real1DArray_Item ( phi, i ) ; Coordinates3_GetRow ( grd1, i, qcGradients[3*i], qcGradients[3*i+1], qcGradients[3*i+2] ) ; }
+    for ( m = 0 ; m < nMM ; m++ ) Coordinates3_GetRow ( grd2, nq + m, mmGradients[3*m], mmGradients[3*m+1], mmGradients[3*m+2] ) ;
     PairList_Deallocate ( &list ) ;
     free ( indices ) ;
     Coordinates3_Deallocate ( &crd1 ) ; Coordinates3_Deallocate ( &crd2 ) ;

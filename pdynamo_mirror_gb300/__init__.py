@@ -1,0 +1,13 @@
+"""pdynamo_mirror_gb300: GB300-native (sm_103a) NDDO QC/MM energy + gradient for pDynamo's QCModelMNDO path.
+
+Public surface (mirroring pDynamo 1.9.0's names):
+    QCModelMNDO, DIISSCFConverger, NBModelABFS, NBModelFull, System, ElectronicState
+The compute path is libpdg.so (CUDA, include/pdg.h); nothing here computes on the CPU.
+"""
+
+from .converger import DIISSCFConverger
+from .nbmodel import NBModelABFS, NBModelFull
+from .qcmodel import QCModelMNDO
+from .system import ElectronicState, SCFNotConverged, System
+
+__all__ = ["DIISSCFConverger", "ElectronicState", "NBModelABFS", "NBModelFull", "QCModelMNDO", "SCFNotConverged", "System"]

@@ -1,0 +1,76 @@
+"""ctypes binding of libpdg.so (include/pdg.h).
+
+The CUDA library is the only compute path: importing the energy functions on a machine without the
+built library or without a CUDA device raises, there is no CPU fallback.
+"""
+
+import ctypes, os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libpdg.so")
+
+PDG_OK, PDG_NOT_CONVERGED, PDG_NAN, PDG_DIIS_SINGULAR, PDG_BAD_ARGUMENT, PDG_CUDA_ERROR, PDG_TOO_LARGE = range(7)
+NENERGY = 8
+EN_TOTAL_ELECTRONIC, EN_ELECTRONIC, EN_NUCLEAR, EN_BASELINE, EN_QCMM, EN_ONE_ELECTRON, EN_TWO_ELECTRON, EN_RMS_DENSITY = range(8)
+MAX_HISTORY = 16
+
+EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system_info", "pdg_workspace_bytes",
+           "pdg_energy_gradients", "pdg_one_electron", "pdg_fock", "pdg_gradients", "pdg_qcmm_potentials",
+           "pdg_qcmm_gradients", "pdg_last_error")
+
+
+class SCFOptions(ctypes.Structure):
+    _fields_ = [("density_tolerance", ctypes.c_double), ("energy_tolerance", ctypes.c_double),
+                ("diis_onset", ctypes.c_double), ("maximum_scf_cycles", ctypes.c_int),
+                ("history", ctypes.c_int), ("use_rca", ctypes.c_int), ("reserved", ctypes.c_int)]
+
+
+class NativeError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load libpdg.so and declare its signatures (no GPU needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise NativeError("libpdg.so is not built (%s); run __graft_entry__.build()" % path)
+    L = ctypes.CDLL(path)
+    P, I, D, S = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_size_t
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    L.pdg_version.restype = I
+    L.pdg_last_error.restype = ctypes.c_char_p
+    L.pdg_system_create.argtypes = [P, I, I, P, I, PP]
+    L.pdg_system_destroy.argtypes = [P]
+    L.pdg_system_info.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]
+    L.pdg_workspace_bytes.argtypes = [P, I]
+    L.pdg_workspace_bytes.restype = S
+    L.pdg_energy_gradients.argtypes = [P, I, P, P, ctypes.POINTER(SCFOptions), P, I, P, P, P, P, P, P, S, P]
+    L.pdg_one_electron.argtypes = [P, I, P, P, P, S, P]
+    L.pdg_fock.argtypes = [P, I, P, P, P, P, P, P, S, P]
+    L.pdg_gradients.argtypes = [P, I, P, P, P, P, S, P]
+    L.pdg_qcmm_potentials.argtypes = [I, I, I, I, P, P, P, I, P, D, P, P]
+    L.pdg_qcmm_gradients.argtypes = [I, I, I, I, P, P, P, P, I, P, D, P, P, P]
+    for name in EXPORTS:
+        getattr(L, name).restype = getattr(L, name).restype or I
+    _lib = L
+    return L
+
+
+def check(rc, what):
+    if rc != PDG_OK:
+        msg = load().pdg_last_error().decode()
+        raise NativeError("%s failed (status %d): %s" % (what, rc, msg))
+
+
+def ptr(t):
+    """Device (or host) address of a torch tensor or None."""
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def stream_handle(torch_stream):
+    return ctypes.c_void_p(torch_stream.cuda_stream)

@@ -1,0 +1,229 @@
+// api.cu - the extern "C" boundary of libpdg.so (declared in include/pdg.h).
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "multipole.cuh"
+
+static thread_local std::string g_error;
+
+static int fail(int code, const std::string &msg)
+{
+    g_error = msg;
+    return code;
+}
+
+static int cuda_check(cudaError_t e, const char *what)
+{
+    if (e != cudaSuccess) return fail(PDG_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+    return PDG_OK;
+}
+
+struct pdg_system {
+    DeviceSystem d;
+    std::vector<double> elements;
+    int charge;
+    // device allocations owned by the system (tables only; no per-frame data)
+    double *d_elements = nullptr, *d_terms = nullptr;
+    int *d_ints = nullptr;
+};
+
+extern "C" int pdg_version(void) { return 100; }
+
+extern "C" const char *pdg_last_error(void) { return g_error.c_str(); }
+
+extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n_atoms, const int *h_atom_element,
+                                 int charge, pdg_system **out)
+{
+    if (!out || !h_elements || !h_atom_element) return fail(PDG_BAD_ARGUMENT, "null argument");
+    *out = nullptr;
+    if (n_elements <= 0 || n_elements > PDG_MAX_ELEMENTS) return fail(PDG_TOO_LARGE, "element count outside 1..16");
+    if (n_atoms <= 0 || n_atoms > PDG_MAX_ATOMS) return fail(PDG_TOO_LARGE, "atom count outside 1..1024");
+    std::vector<int> elem(n_atoms), start(n_atoms), norb(n_atoms);
+    int nb = 0, zsum = 0;
+    for (int a = 0; a < n_atoms; a++) {
+        int e = h_atom_element[a];
+        if (e < 0 || e >= n_elements) return fail(PDG_BAD_ARGUMENT, "atom element index out of range");
+        int no = (int)h_elements[e * PDG_ELEMENT_STRIDE + PDG_E_NORB];
+        if (no != 1 && no != 4) return fail(PDG_BAD_ARGUMENT, "only s and sp elements are supported");
+        elem[a] = e; start[a] = nb; norb[a] = no; nb += no;
+        zsum += (int)llround(h_elements[e * PDG_ELEMENT_STRIDE + PDG_E_ZCORE]);
+    }
+    if (nb > PDG_MAX_BASIS) return fail(PDG_TOO_LARGE, "more than 2048 basis functions");
+    int nel = zsum - charge;
+    if (nel < 0 || nel % 2 != 0 || nel / 2 > nb) return fail(PDG_BAD_ARGUMENT, "closed-shell RHF needs an even electron count that fits the basis");
+    int npairs = n_atoms * (n_atoms - 1) / 2;
+    std::vector<int> pi(npairs), pj(npairs), pt(npairs);
+    int tei = 0;
+    for (int i = 0, p = 0; i < n_atoms; i++)
+        for (int j = 0; j < i; j++, p++) {
+            pi[p] = i; pj[p] = j; pt[p] = tei;
+            tei += (norb[i] * (norb[i] + 1) / 2) * (norb[j] * (norb[j] + 1) / 2);
+        }
+    // multipole term tables per ordered element pair
+    std::vector<double> terms((size_t)n_elements * n_elements * 2 * MP_NTERMS);
+    for (int a = 0; a < n_elements; a++)
+        for (int b = 0; b < n_elements; b++) {
+            double *o = &terms[(size_t)(a * n_elements + b) * 2 * MP_NTERMS];
+            multipole_terms(h_elements + a * PDG_ELEMENT_STRIDE, h_elements + b * PDG_ELEMENT_STRIDE, o, o + MP_NTERMS);
+        }
+    pdg_system *s = new pdg_system();
+    s->elements.assign(h_elements, h_elements + (size_t)n_elements * PDG_ELEMENT_STRIDE);
+    s->charge = charge;
+    std::vector<int> ints;
+    ints.insert(ints.end(), elem.begin(), elem.end());
+    ints.insert(ints.end(), start.begin(), start.end());
+    ints.insert(ints.end(), norb.begin(), norb.end());
+    ints.insert(ints.end(), pi.begin(), pi.end());
+    ints.insert(ints.end(), pj.begin(), pj.end());
+    ints.insert(ints.end(), pt.begin(), pt.end());
+    int rc = PDG_OK;
+    if ((rc = cuda_check(cudaMalloc(&s->d_elements, sizeof(double) * s->elements.size()), "cudaMalloc elements")) ||
+        (rc = cuda_check(cudaMalloc(&s->d_terms, sizeof(double) * terms.size()), "cudaMalloc terms")) ||
+        (rc = cuda_check(cudaMalloc(&s->d_ints, sizeof(int) * ints.size()), "cudaMalloc tables")) ||
+        (rc = cuda_check(cudaMemcpy(s->d_elements, s->elements.data(), sizeof(double) * s->elements.size(), cudaMemcpyHostToDevice), "copy elements")) ||
+        (rc = cuda_check(cudaMemcpy(s->d_terms, terms.data(), sizeof(double) * terms.size(), cudaMemcpyHostToDevice), "copy terms")) ||
+        (rc = cuda_check(cudaMemcpy(s->d_ints, ints.data(), sizeof(int) * ints.size(), cudaMemcpyHostToDevice), "copy tables"))) {
+        pdg_system_destroy(s);
+        return rc;
+    }
+    DeviceSystem &d = s->d;
+    d.n_atoms = n_atoms; d.n_basis = nb; d.n_occ = nel / 2; d.n_pairs = npairs; d.n_elements = n_elements;
+    d.n_electrons = nel; d.tei_total = tei;
+    d.vec_occupied = (d.n_occ <= nb - d.n_occ) ? 1 : 0;
+    d.n_vec = d.vec_occupied ? d.n_occ : nb - d.n_occ;
+    d.elements = s->d_elements; d.terms = s->d_terms;
+    const int *b = s->d_ints;
+    d.atom_elem = b; d.atom_start = b + n_atoms; d.atom_norb = b + 2 * n_atoms;
+    d.pair_i = b + 3 * n_atoms; d.pair_j = d.pair_i + npairs; d.pair_tei = d.pair_j + npairs;
+    *out = s;
+    return PDG_OK;
+}
+
+extern "C" int pdg_system_destroy(pdg_system *s)
+{
+    if (!s) return PDG_OK;
+    cudaFree(s->d_elements); cudaFree(s->d_terms); cudaFree(s->d_ints);
+    delete s;
+    return PDG_OK;
+}
+
+extern "C" int pdg_system_info(const pdg_system *s, int *n_basis, int *n_occupied, int *n_pairs)
+{
+    if (!s) return fail(PDG_BAD_ARGUMENT, "null system");
+    if (n_basis) *n_basis = s->d.n_basis;
+    if (n_occupied) *n_occupied = s->d.n_occ;
+    if (n_pairs) *n_pairs = s->d.n_pairs;
+    return PDG_OK;
+}
+
+static FramePlan plan_for(const pdg_system *s, int history) { return make_plan(s->d, history < 1 ? 1 : history); }
+
+extern "C" size_t pdg_workspace_bytes(const pdg_system *s, int n_frames)
+{
+    if (!s || n_frames <= 0) return 0;
+    return sizeof(double) * plan_for(s, PDG_MAX_HISTORY).stride * (size_t)n_frames;
+}
+
+static int check_workspace(const pdg_system *s, int n_frames, void *ws, size_t bytes)
+{
+    if (!s) return fail(PDG_BAD_ARGUMENT, "null system");
+    if (n_frames <= 0) return fail(PDG_BAD_ARGUMENT, "n_frames must be positive");
+    if (!ws || bytes < pdg_workspace_bytes(s, n_frames)) return fail(PDG_BAD_ARGUMENT, "workspace missing or too small");
+    return PDG_OK;
+}
+
+static int integrals(pdg_system *s, const FramePlan &p, int n_frames, const double *xyz, double *ws, cudaStream_t st)
+{
+    launch_pair_integrals(s->d, p, n_frames, xyz, ws, st);
+    launch_assemble_h(s->d, p, n_frames, ws, st);
+    return cuda_check(cudaGetLastError(), "integral kernels");
+}
+
+extern "C" int pdg_energy_gradients(pdg_system *s, int n_frames, const double *d_xyz, const double *d_phi,
+                                    const pdg_scf_options *o, double *d_density, int use_density,
+                                    double *d_energies, double *d_gradients, double *d_charges, int *d_status,
+                                    int *d_ncycles, void *ws, size_t bytes, void *stream)
+{
+    int rc = check_workspace(s, n_frames, ws, bytes);
+    if (rc) return rc;
+    if (!o || !d_xyz || !d_density || !d_energies || !d_status) return fail(PDG_BAD_ARGUMENT, "null argument");
+    if (o->history < 1 || o->history > PDG_MAX_HISTORY) return fail(PDG_BAD_ARGUMENT, "history must be 1..16");
+    if (o->maximum_scf_cycles < 0) return fail(PDG_BAD_ARGUMENT, "maximum_scf_cycles must be >= 0");
+    cudaStream_t st = (cudaStream_t)stream;
+    FramePlan p = plan_for(s, PDG_MAX_HISTORY);
+    double *w = (double *)ws;
+    if ((rc = integrals(s, p, n_frames, d_xyz, w, st))) return rc;
+    launch_scf(s->d, p, n_frames, d_phi, *o, d_density, use_density, d_energies, d_charges, d_status, d_ncycles, w, 0, nullptr, st);
+    if ((rc = cuda_check(cudaGetLastError(), "scf kernel"))) return rc;
+    if (d_gradients) {
+        launch_pair_gradients(s->d, p, n_frames, d_xyz, d_density, w, st);
+        launch_reduce_gradients(s->d, p, n_frames, w, d_gradients, st);
+        if ((rc = cuda_check(cudaGetLastError(), "gradient kernels"))) return rc;
+    }
+    return PDG_OK;
+}
+
+extern "C" int pdg_one_electron(pdg_system *s, int n_frames, const double *d_xyz, double *d_h, void *ws, size_t bytes, void *stream)
+{
+    int rc = check_workspace(s, n_frames, ws, bytes);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    FramePlan p = plan_for(s, PDG_MAX_HISTORY);
+    double *w = (double *)ws;
+    if ((rc = integrals(s, p, n_frames, d_xyz, w, st))) return rc;
+    size_t NN = (size_t)s->d.n_basis * s->d.n_basis;
+    for (int f = 0; f < n_frames; f++)
+        if ((rc = cuda_check(cudaMemcpyAsync(d_h + f * NN, w + f * p.stride + p.H, sizeof(double) * NN, cudaMemcpyDeviceToDevice, st), "copy H"))) return rc;
+    return PDG_OK;
+}
+
+extern "C" int pdg_fock(pdg_system *s, int n_frames, const double *d_xyz, const double *d_phi, const double *d_density,
+                        double *d_fock, double *d_energies, void *ws, size_t bytes, void *stream)
+{
+    int rc = check_workspace(s, n_frames, ws, bytes);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    FramePlan p = plan_for(s, PDG_MAX_HISTORY);
+    double *w = (double *)ws;
+    if ((rc = integrals(s, p, n_frames, d_xyz, w, st))) return rc;
+    pdg_scf_options o = { 1e-8, 2e-4, 0.2, 0, 10, 1, 0 };
+    launch_scf(s->d, p, n_frames, d_phi, o, const_cast<double *>(d_density), 1, d_energies, nullptr, nullptr, nullptr, w, 1, d_fock, st);
+    return cuda_check(cudaGetLastError(), "fock kernel");
+}
+
+extern "C" int pdg_gradients(pdg_system *s, int n_frames, const double *d_xyz, const double *d_density,
+                             double *d_gradients, void *ws, size_t bytes, void *stream)
+{
+    int rc = check_workspace(s, n_frames, ws, bytes);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    FramePlan p = plan_for(s, PDG_MAX_HISTORY);
+    double *w = (double *)ws;
+    launch_pair_gradients(s->d, p, n_frames, d_xyz, d_density, w, st);
+    launch_reduce_gradients(s->d, p, n_frames, w, d_gradients, st);
+    return cuda_check(cudaGetLastError(), "gradient kernels");
+}
+
+extern "C" int pdg_qcmm_potentials(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,
+                                   const double *q, int n_knots, const double *knots, double cutoff, double *phi, void *stream)
+{
+    if (model != 0 && model != 1) return fail(PDG_BAD_ARGUMENT, "model must be 0 (full) or 1 (ABFS)");
+    if (n_frames <= 0 || n_qc <= 0 || n_mm < 0 || !qc || !phi || (n_mm > 0 && (!mm || !q))) return fail(PDG_BAD_ARGUMENT, "bad sizes or null pointers");
+    if (model == 1 && (n_knots < 2 || !knots || cutoff <= 0.0)) return fail(PDG_BAD_ARGUMENT, "ABFS needs spline knots and a cutoff");
+    launch_qcmm_potentials(model, n_frames, n_qc, n_mm, qc, mm, q, n_knots, knots, cutoff, phi, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "qcmm potentials");
+}
+
+extern "C" int pdg_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,
+                                  const double *q, const double *qcq, int n_knots, const double *knots, double cutoff,
+                                  double *gqc, double *gmm, void *stream)
+{
+    if (model != 0 && model != 1) return fail(PDG_BAD_ARGUMENT, "model must be 0 (full) or 1 (ABFS)");
+    if (n_frames <= 0 || n_qc <= 0 || n_mm < 0 || !qc || !qcq || !gqc || (n_mm > 0 && (!mm || !q || !gmm))) return fail(PDG_BAD_ARGUMENT, "bad sizes or null pointers");
+    if (model == 1 && (n_knots < 2 || !knots || cutoff <= 0.0)) return fail(PDG_BAD_ARGUMENT, "ABFS needs spline knots and a cutoff");
+    launch_qcmm_gradients(model, n_frames, n_qc, n_mm, qc, mm, q, qcq, n_knots, knots, cutoff, gqc, gmm, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "qcmm gradients");
+}

@@ -1,0 +1,122 @@
+// common.cuh - shared definitions of the GB300 NDDO QC/MM energy + gradient library.
+//
+// Layout in HBM (one batch of n_frames configurations of one QC region):
+//   element table      n_elements * PDG_ELEMENT_STRIDE doubles (atomic units), read through L1
+//   atom tables        element index, first basis function, orbital count per atom
+//   pair tables        (i, j) for every atom pair i > j, in pDynamo's loop order (QCModelMNDO.c:1047-1063),
+//                      and the offset of the pair's two-electron block in the compact per-frame TEI array
+//   per-frame arrays   frame-major: everything one frame needs is contiguous, so that the CTA that runs
+//                      a frame's SCF streams its own data and nothing else.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "../../include/pdg.h"
+
+#define PDG_BLOCK 512
+#define PDG_WARPS (PDG_BLOCK / 32)
+#define PDG_MAX_HISTORY 16
+#define PDG_PAIR_E_STRIDE 24   // e1b[10] | e2a[10] | enuc | spare
+#define PDG_TEI_UNDERFLOW 1.0e-12
+
+struct DeviceSystem {
+    int n_atoms, n_basis, n_occ, n_pairs, n_elements, n_electrons, tei_total;
+    int n_vec, vec_occupied;       // eigenvectors computed per density step: min(n_occ, N - n_occ)
+    const double *elements;        // n_elements * PDG_ELEMENT_STRIDE
+    const int *atom_elem, *atom_start, *atom_norb;
+    const int *pair_i, *pair_j, *pair_tei;   // n_pairs
+    const double *terms;           // multipole (o, a) tables per ordered element pair (multipole.cuh)
+};
+
+// Per-frame workspace plan (all offsets in doubles from the frame's base).
+struct FramePlan {
+    size_t tei, pair_e, pair_g, H, F, P0, A, HV, Z, LU, hP, hF, hE, rP, rF, misc, stride;
+    int hist_len;   // packed history vector length N(N+1)/2 (errors use N(N-1)/2 within the same slot)
+};
+
+__host__ __device__ inline size_t align32(size_t x) { return (x + 31) & ~size_t(31); }
+
+__host__ inline FramePlan make_plan(const DeviceSystem &s, int history)
+{
+    FramePlan p;
+    size_t N = s.n_basis, NN = N * N, o = 0;
+    p.hist_len = (int)(N * (N + 1) / 2);
+    p.tei = o;    o += align32(s.tei_total);
+    p.pair_e = o; o += align32((size_t)s.n_pairs * PDG_PAIR_E_STRIDE);
+    p.pair_g = o; o += align32((size_t)s.n_pairs * 3);
+    p.H = o;      o += align32(NN);
+    p.F = o;      o += align32(NN);
+    p.P0 = o;     o += align32(NN);          // previous density (for the RMS change)
+    p.A = o;      o += align32(NN);          // work matrix: F P product, tridiagonalisation
+    p.HV = o;     o += align32(NN);          // Householder vectors, one row per reflector
+    p.Z = o;      o += align32(N * (size_t)(s.n_vec > 0 ? s.n_vec : 1));
+    p.LU = o;     o += align32((size_t)PDG_WARPS * 8 * N);
+    p.hP = o;     o += align32((size_t)history * p.hist_len);
+    p.hF = o;     o += align32((size_t)history * p.hist_len);
+    p.hE = o;     o += align32((size_t)history * p.hist_len);
+    p.rP = o;     o += align32(NN);
+    p.rF = o;     o += align32(NN);
+    p.misc = o;   o += align32(PDG_MAX_HISTORY * PDG_MAX_HISTORY + 64);
+    p.stride = align32(o);
+    return p;
+}
+
+__device__ __forceinline__ const double *elem(const DeviceSystem &s, int e) { return s.elements + e * PDG_ELEMENT_STRIDE; }
+__device__ __forceinline__ int pk(int i, int j) { return i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i; }
+
+// Deterministic reductions: fixed thread-to-element assignment, fixed shuffle tree, fixed warp order.
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Block-wide sum; every thread gets the result.  red must hold blockDim.x / 32 doubles.
+__device__ __forceinline__ double block_sum(double v, double *red)
+{
+    v = warp_sum(v);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int i = 0; i < nw; i++) t += red[i];
+    __syncthreads();
+    return t;
+}
+__device__ __forceinline__ double block_max(double v, double *red)
+{
+    v = warp_max(v);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double t = red[0];
+    for (int i = 1; i < nw; i++) t = fmax(t, red[i]);
+    __syncthreads();
+    return t;
+}
+
+// Units (pCore-1.9.0/extensions/cinclude/Units.h:21,55-58).
+#define PDG_BOHRS_TO_ANGSTROMS (5.291772083e-11 / 1.0e-10)
+#define PDG_ANGSTROMS_TO_BOHRS (1.0e-10 / 5.291772083e-11)
+
+// Kernel launchers (defined in the .cu files, called by api.cu).
+void launch_pair_integrals(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *xyz, double *ws, cudaStream_t st);
+void launch_assemble_h(const DeviceSystem &s, const FramePlan &p, int n_frames, double *ws, cudaStream_t st);
+void launch_scf(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *phi, const pdg_scf_options &o,
+                double *density, int use_density, double *energies, double *charges, int *status, int *ncycles,
+                double *ws, int fock_only, double *fock_out, cudaStream_t st);
+void launch_pair_gradients(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *xyz,
+                           const double *density, double *ws, cudaStream_t st);
+void launch_reduce_gradients(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *ws,
+                             double *gradients, cudaStream_t st);
+int launch_qcmm_potentials(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,
+                           const double *q, int n_knots, const double *knots, double cutoff, double *phi, cudaStream_t st);
+int launch_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,
+                          const double *q, const double *qcq, int n_knots, const double *knots, double cutoff,
+                          double *gqc, double *gmm, cudaStream_t st);

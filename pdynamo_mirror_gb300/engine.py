@@ -1,0 +1,144 @@
+"""Device orchestration of one QC region: the call sequence of one System.Energy(doGradients=True).
+
+For a batch of frames (configurations of the same QC region and MM environment) the engine queues, on one
+CUDA stream:
+  1. QC/MM potentials at the QC atoms              pdg_qcmm_potentials   (NBModel.QCMMPotentials)
+  2. integrals, the complete SCF, QC gradients     pdg_energy_gradients  (QCModel.Energy + EnergyGradients)
+  3. QC/MM gradients with the final Lowdin charges pdg_qcmm_gradients    (NBModel.QCMMGradients)
+(pMolecule/System.py:309-312).  Torch supplies device memory and the stream only.
+"""
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native
+from .parameters import ANGSTROMS_TO_BOHRS, HARTREES_TO_KJ, element_table
+
+GRADIENT_TO_KJ_PER_A = ANGSTROMS_TO_BOHRS * HARTREES_TO_KJ   # QCAtomContainer.c:632 CONVERSION_FACTOR
+
+
+def require_cuda():
+    if not torch.cuda.is_available():
+        raise _native.NativeError("a CUDA device is required: the GB300 kernels are the only compute path")
+
+
+class QCEngine:
+    """A pdg_system plus the device buffers of a batch."""
+
+    def __init__(self, hamiltonian, atomic_numbers, charge, device=None):
+        require_cuda()
+        self.L = _native.load()
+        self.device = torch.device(device or "cuda")
+        self.atomic_numbers = [int(z) for z in atomic_numbers]
+        self.elements, records, index = element_table(hamiltonian, self.atomic_numbers)
+        self._records = np.ascontiguousarray(records)
+        self._index = np.ascontiguousarray(index)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _native.check(self.L.pdg_system_create(self._records.ctypes.data_as(ctypes.c_void_p), len(self.elements),
+                                                   len(self.atomic_numbers), self._index.ctypes.data_as(ctypes.c_void_p),
+                                                   int(charge), ctypes.byref(h)), "pdg_system_create")
+        self.handle = h
+        nb, no, npair = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _native.check(self.L.pdg_system_info(h, ctypes.byref(nb), ctypes.byref(no), ctypes.byref(npair)), "pdg_system_info")
+        self.n_atoms, self.n_basis, self.n_occupied, self.n_pairs = len(self.atomic_numbers), nb.value, no.value, npair.value
+        self._ws, self._ws_frames = None, 0
+        self.density = None          # device [F, N, N], kept between calls as the reference keeps its state
+        self._knots = {}
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                self.L.pdg_system_destroy(self.handle)
+        except Exception:
+            pass
+
+    def workspace(self, n_frames):
+        if self._ws is None or self._ws_frames < n_frames:
+            nbytes = int(self.L.pdg_workspace_bytes(self.handle, n_frames))
+            self._ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+            self._ws_frames = n_frames
+        return self._ws
+
+    def knots(self, nbmodel):
+        k = id(nbmodel)
+        if k not in self._knots:
+            self._knots[k] = torch.as_tensor(nbmodel.knots(), dtype=torch.float64, device=self.device)
+        return self._knots[k]
+
+    def run(self, qc_xyz, converger, mm_xyz=None, mm_charges=None, nbmodel=None, gradients=True, warm_start=True):
+        """qc_xyz [F, n, 3] and mm_xyz [F, m, 3] in Angstrom (device float64), mm_charges [m].
+        Returns a dict of device tensors in Hartree / Hartree per Bohr."""
+        F = qc_xyz.shape[0]
+        n, N = self.n_atoms, self.n_basis
+        dev = self.device
+        stream = torch.cuda.current_stream(dev)
+        sh = _native.stream_handle(stream)
+        ws = self.workspace(F)
+        out = {}
+        phi = None
+        qcmm = nbmodel is not None and mm_xyz is not None and mm_xyz.shape[1] > 0
+        if qcmm:
+            knots = self.knots(nbmodel) if nbmodel.model_id == 1 else None
+            nk = 0 if knots is None else knots.numel() // 3
+            phi = torch.empty((F, n), dtype=torch.float64, device=dev)
+            _native.check(self.L.pdg_qcmm_potentials(nbmodel.model_id, F, n, mm_xyz.shape[1], _native.ptr(qc_xyz), _native.ptr(mm_xyz),
+                                                     _native.ptr(mm_charges), nk, _native.ptr(knots), float(nbmodel.outerCutoff),
+                                                     _native.ptr(phi), sh), "pdg_qcmm_potentials")
+        xyz_bohr = (qc_xyz * ANGSTROMS_TO_BOHRS).contiguous()
+        use = 1 if (warm_start and self.density is not None and self.density.shape[0] == F) else 0
+        if not use:
+            self.density = torch.empty((F, N, N), dtype=torch.float64, device=dev)
+        energies = torch.empty((F, _native.NENERGY), dtype=torch.float64, device=dev)
+        grad = torch.empty((F, n, 3), dtype=torch.float64, device=dev) if gradients else None
+        charges = torch.empty((F, n), dtype=torch.float64, device=dev)
+        status = torch.empty(F, dtype=torch.int32, device=dev)
+        ncycles = torch.empty(F, dtype=torch.int32, device=dev)
+        opts = converger.options()
+        _native.check(self.L.pdg_energy_gradients(self.handle, F, _native.ptr(xyz_bohr), _native.ptr(phi), ctypes.byref(opts),
+                                                  _native.ptr(self.density), use, _native.ptr(energies), _native.ptr(grad),
+                                                  _native.ptr(charges), _native.ptr(status), _native.ptr(ncycles),
+                                                  _native.ptr(ws), ws.numel(), sh), "pdg_energy_gradients")
+        out.update(energies=energies, qc_gradients=grad, charges=charges, status=status, ncycles=ncycles, phi=phi)
+        if qcmm and gradients:
+            gqc = torch.empty((F, n, 3), dtype=torch.float64, device=dev)
+            gmm = torch.empty((F, mm_xyz.shape[1], 3), dtype=torch.float64, device=dev)
+            _native.check(self.L.pdg_qcmm_gradients(nbmodel.model_id, F, n, mm_xyz.shape[1], _native.ptr(qc_xyz), _native.ptr(mm_xyz),
+                                                    _native.ptr(mm_charges), _native.ptr(charges), nk, _native.ptr(knots),
+                                                    float(nbmodel.outerCutoff), _native.ptr(gqc), _native.ptr(gmm), sh),
+                          "pdg_qcmm_gradients")
+            out.update(qcmm_qc_gradients=gqc, qcmm_mm_gradients=gmm)
+        return out
+
+    # diagnostics used by the parity tests
+    def one_electron(self, qc_xyz):
+        F = qc_xyz.shape[0]
+        ws = self.workspace(F)
+        H = torch.empty((F, self.n_basis, self.n_basis), dtype=torch.float64, device=self.device)
+        xyz_bohr = (qc_xyz * ANGSTROMS_TO_BOHRS).contiguous()
+        _native.check(self.L.pdg_one_electron(self.handle, F, _native.ptr(xyz_bohr), _native.ptr(H), _native.ptr(ws), ws.numel(),
+                                              _native.stream_handle(torch.cuda.current_stream(self.device))), "pdg_one_electron")
+        return H
+
+    def fock(self, qc_xyz, density, phi=None):
+        F = qc_xyz.shape[0]
+        ws = self.workspace(F)
+        Fm = torch.empty((F, self.n_basis, self.n_basis), dtype=torch.float64, device=self.device)
+        en = torch.empty((F, _native.NENERGY), dtype=torch.float64, device=self.device)
+        xyz_bohr = (qc_xyz * ANGSTROMS_TO_BOHRS).contiguous()
+        _native.check(self.L.pdg_fock(self.handle, F, _native.ptr(xyz_bohr), _native.ptr(phi), _native.ptr(density.contiguous()),
+                                      _native.ptr(Fm), _native.ptr(en), _native.ptr(ws), ws.numel(),
+                                      _native.stream_handle(torch.cuda.current_stream(self.device))), "pdg_fock")
+        return Fm, en
+
+    def gradients(self, qc_xyz, density):
+        F = qc_xyz.shape[0]
+        ws = self.workspace(F)
+        g = torch.empty((F, self.n_atoms, 3), dtype=torch.float64, device=self.device)
+        xyz_bohr = (qc_xyz * ANGSTROMS_TO_BOHRS).contiguous()
+        _native.check(self.L.pdg_gradients(self.handle, F, _native.ptr(xyz_bohr), _native.ptr(density.contiguous()), _native.ptr(g),
+                                           _native.ptr(ws), ws.numel(), _native.stream_handle(torch.cuda.current_stream(self.device))),
+                      "pdg_gradients")
+        return g

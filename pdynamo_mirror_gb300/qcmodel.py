@@ -1,0 +1,51 @@
+"""QCModelMNDO: closed-shell RHF MNDO-family QC model on the GB300 path.
+
+Mirrors the keyword surface of pDynamo's QCModelMNDO (pMolecule.QCModelMNDO.pyx:511-621): the first
+positional argument or ``mndoModel`` names the Hamiltonian; ``converger`` takes a DIISSCFConverger.
+Only the closed-shell, spin-restricted, cardinal-occupancy case is on this path; other occupancy or
+spin options raise ValueError, as unknown options do in the reference.
+"""
+
+from .converger import DIISSCFConverger
+from .parameters import HAMILTONIANS, available_elements
+
+
+class QCModelMNDO:
+    def __init__(self, *arguments, **options):
+        self.mndoModel = "am1"
+        self.converger = None
+        self.label = None
+        self.isSpinRestricted = True
+        self.keepOrbitalData = False
+        if len(arguments) > 1:
+            raise ValueError("QCModelMNDO takes at most one positional argument.")
+        if arguments:
+            self.mndoModel = arguments[0]
+        self.SetOptions(**options)
+
+    def SetOptions(self, **options):
+        if "converger" in options: self.converger = options.pop("converger")
+        if "mndoModel" in options: self.mndoModel = options.pop("mndoModel")
+        if "label" in options: self.label = options.pop("label")
+        if "keepOrbitalData" in options: self.keepOrbitalData = bool(options.pop("keepOrbitalData"))
+        if "isSpinRestricted" in options:
+            if not options.pop("isSpinRestricted"):
+                raise ValueError("Only spin-restricted (RHF) models are on this path.")
+        if "occupancyType" in options:
+            if options.pop("occupancyType") != "Cardinal":
+                raise ValueError("Only cardinal occupancies are on this path.")
+        if options:
+            raise ValueError("Invalid options: " + ", ".join(sorted(options)) + ".")
+        self.mndoModel = str(self.mndoModel).lower()
+        if self.mndoModel not in HAMILTONIANS:
+            raise ValueError("Unknown MNDO Hamiltonian: %s." % self.mndoModel)
+        if self.converger is None:
+            self.converger = DIISSCFConverger()
+        if self.label is None:
+            self.label = self.mndoModel.upper()
+
+    def CheckElements(self, atomic_numbers):
+        have = set(available_elements(self.mndoModel))
+        missing = sorted(set(int(z) for z in atomic_numbers) - have)
+        if missing:
+            raise ValueError("Error processing some QC parameter files: %s has no parameters for %s." % (self.mndoModel, missing))

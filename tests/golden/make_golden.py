@@ -112,6 +112,58 @@ def main(root):
                 h, label, r["converged"], r["ncycles"], r["pure_qc_kj"], pk[h][label]["value"],
                 r["pure_qc_kj"] - pk[h][label]["value"]))
     json.dump(ref, open(os.path.join(HERE, "mndo_rhf_reference.json"), "w"), indent=0, sort_keys=True)
+    qcmm_fixtures(root)
+
+
+def qcmm_fixtures(root):
+    """QC/MM fixtures.  example8: the book's AM1 water dimer (QC = first water, OPLS/TIP3P charges on the
+    second, NBModelFull) with its published values (book/logs/Example8.log:75-85) and the reference core's
+    results.  abfs: a 4-water AM1 QC cluster in 300 TIP3P waters with NBModelABFS 8/12 A through the
+    reference's ABFS pair routines; the spline knots are the C restatement's (oracle.abfs_knots) because
+    the reference tabulates them in Python-2 Pyrex that cannot run here."""
+    sys.path.insert(0, os.path.join(HERE, "..", ".."))
+    from oracle import oracle as O
+    from pdynamo_mirror_gb300 import workloads as W
+    out = {}
+    lines = open(os.path.join(root, "book", "data", "mol", "waterDimer_cs.mol")).read().splitlines()
+    X = np.array([[float(v) for v in l.split()[:3]] for l in lines[4:10]])
+    Zq, q = [8, 1, 1], np.array([-0.834, 0.417, 0.417])
+    phi, _, _ = O.qcmm("full", X[:3], X[3:], q)
+    rs = R.RefSystem(R.RefHamiltonian("am1", Zq), Zq, qcmm=True)
+    r = rs.energy(X[:3], phi=phi)
+    gfull = np.zeros((6, 3))
+    _, gq, gm = O.qcmm("full", X[:3], X[3:], q, qcq=r["charges"])
+    out["example8"] = {"Z": [8, 1, 1, 8, 1, 1], "xyz": X.tolist(), "mm_charges": [0, 0, 0] + q.tolist(), "qc": [0, 1, 2],
+                       "model": "full", "book": {"pure_qc_kj": -244.1191, "qcmm_kj": -23.7448, "electronic_with_qcmm": -18.121115,
+                                                 "nuclear": 5.3040515, "ncycles": 8},
+                       "pure_qc_kj": r["pure_qc_kj"], "qcmm_kj": 2625.5 * r["eqcmm"], "ncycles": r["ncycles"],
+                       "qc_gradients": (r["gradients"] + gq).tolist(), "mm_gradients": gm.tolist()}
+    Zc, Xc = W.water_cluster(4, seed=11, centre=[10.0, 10.0, 10.0])
+    rng = np.random.default_rng(5)
+    mmX, mmZ, mmq = [], [], []
+    grid = W._Grid(np.zeros(3) - 5.0, 30.0, 2.6)
+    for o in Xc[Zc == 8]:
+        grid.add(o)
+    for o in W._place(rng, 300, np.zeros(3), 20.0, grid):
+        Rm = W._random_rotation(rng)
+        mmX.extend(o + W._water_local() @ Rm.T); mmZ.extend([8, 1, 1]); mmq.extend([W.TIP3P_O, W.TIP3P_H, W.TIP3P_H])
+    mmX, mmq = np.array(mmX), np.array(mmq)
+    kx, ky = O.abfs_knots(8.0, 12.0)
+    ab = R.RefABFS(8.0, 12.0, kx, ky)
+    Zl = [int(z) for z in Zc]
+    rs = R.RefSystem(R.RefHamiltonian("am1", Zl), Zl, qcmm=True)
+    phi, _, _ = ab.qcmm(rs, Xc, mmX, mmq, np.zeros(len(Zl)))
+    r = rs.energy(Xc, phi=phi)
+    _, gq, gm = ab.qcmm(rs, Xc, mmX, mmq, r["charges"])
+    conv = 1.0 / ((1.0e-10 / 5.291772083e-11) * 2625.5)   # kJ/mol/A -> Eh/Bohr
+    out["abfs"] = {"Z": Zl + mmZ, "xyz": np.concatenate([Xc, mmX]).tolist(), "mm_charges": [0.0] * len(Zl) + mmq.tolist(),
+                   "qc": list(range(len(Zl))), "model": "abfs", "inner": 8.0, "outer": 12.0,
+                   "pure_qc_kj": r["pure_qc_kj"], "qcmm_kj": 2625.5 * r["eqcmm"], "ncycles": r["ncycles"], "phi": phi.tolist(),
+                   "qc_gradients": (r["gradients"] + gq * conv).tolist(), "mm_gradients": (gm * conv).tolist()}
+    json.dump(out, open(os.path.join(HERE, "qcmm_reference.json"), "w"), indent=0)
+    print("example8 pure %.4f qcmm %.4f cycles %d; abfs pure %.4f qcmm %.4f cycles %d" % (
+        out["example8"]["pure_qc_kj"], out["example8"]["qcmm_kj"], out["example8"]["ncycles"],
+        out["abfs"]["pure_qc_kj"], out["abfs"]["qcmm_kj"], out["abfs"]["ncycles"]))
 
 
 if __name__ == "__main__":

@@ -1,0 +1,76 @@
+"""Host-side logic without a GPU: parameter processing, ABFS spline tabulation, the C ABI's exports."""
+import os, re
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pdynamo_mirror_gb300 import DIISSCFConverger, NBModelABFS, QCModelMNDO, nbmodel, parameters
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize("h", parameters.HAMILTONIANS)
+def test_parameters_match_oracle(h):
+    for z in parameters.available_elements(h):
+        try:
+            p = parameters.ElementParameters(h, z)
+        except ValueError:
+            continue   # no STO-6G basis for this element in the reference either
+        d = O.Hamiltonian(h, [z]).derived(z)
+        np.testing.assert_allclose(p.po, d["po"], rtol=1e-13, atol=1e-15)
+        np.testing.assert_allclose(p.ddp, d["ddp"], rtol=1e-13, atol=1e-15)
+        for k in ("am", "ad", "aq", "alp", "zcore", "eheat", "eisol", "gss", "gsp", "gpp", "gp2", "hsp", "hpp"):
+            assert abs(getattr(p, k) - d[k]) <= 1e-13 * max(1.0, abs(d[k])), (h, z, k)
+        np.testing.assert_allclose(p.beta + [0.0] * (4 - len(p.beta)), d["beta"], rtol=1e-13)
+        np.testing.assert_allclose(p.uspd + [0.0] * (4 - len(p.uspd)), d["uspd"], rtol=1e-13)
+
+
+def test_parameters_match_reference_core():
+    R = pytest.importorskip("oracle.refdriver")
+    try:
+        R.lib()
+    except R.RefUnavailable:
+        pytest.skip("reference core not built here")
+    for h in parameters.HAMILTONIANS:
+        for z in (1, 6, 7, 8):
+            if z not in parameters.available_elements(h):
+                continue
+            p = parameters.ElementParameters(h, z)
+            d = R.RefHamiltonian(h, [z]).derived(z)
+            np.testing.assert_allclose(p.po, d["po"], rtol=1e-14)
+            ex, cc = R.RefHamiltonian(h, [z]).basis(z)
+            for s, (l, e, c) in enumerate(p.shells):
+                np.testing.assert_allclose(e, ex[s, :len(e)], rtol=1e-15)
+                np.testing.assert_allclose(c, cc[s, :len(c)], rtol=1e-12)
+
+
+def test_abfs_knots_match_oracle():
+    x, y = nbmodel.abfs_knots(8.0, 12.0)
+    ox, oy = O.abfs_knots(8.0, 12.0)
+    assert len(x) == len(ox) == 601
+    np.testing.assert_array_equal(x, ox)
+    np.testing.assert_allclose(y, oy, rtol=0, atol=1e-15)
+    assert y[-1] == 0.0 and abs(y[0] - y[1]) < 1e-3
+
+
+def test_option_errors_match_reference_behaviour():
+    with pytest.raises(ValueError):
+        DIISSCFConverger(notAnOption=1)
+    with pytest.raises(ValueError):
+        QCModelMNDO("am1", isSpinRestricted=False)
+    with pytest.raises(ValueError):
+        QCModelMNDO("pm6")
+    with pytest.raises(ValueError):
+        NBModelABFS(innerCutoff=12.0, outerCutoff=8.0)
+
+
+def test_library_exports_every_declared_symbol():
+    from pdynamo_mirror_gb300 import _native
+    header = open(os.path.join(ROOT, "include", "pdg.h")).read()
+    declared = set(re.findall(r"\b(pdg_[a-z_0-9]+)\s*\(", header))
+    assert declared == set(_native.EXPORTS)
+    lib = _native.load()
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert lib.pdg_version() == 100
