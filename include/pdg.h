@@ -65,7 +65,7 @@ typedef struct {
     int    maximum_scf_cycles;  /* 100  */
     int    history;             /* 10, at most 16 */
     int    use_rca;             /* 1: ODA/RCA before DIIS, as the reference default */
-    int    reserved;
+    int    reserved;            /* must be 0 */
 } pdg_scf_options;
 
 /* Energy terms returned per frame (PDG_NENERGY doubles). */
@@ -131,6 +131,18 @@ int pdg_fock(pdg_system *sys, int n_frames, const double *d_xyz, const double *d
 /* Gradients (Eh/Bohr) for given densities, no SCF (QCModelMNDO_Gradients on a fixed density). */
 int pdg_gradients(pdg_system *sys, int n_frames, const double *d_xyz, const double *d_density,
                   double *d_gradients, void *d_workspace, size_t workspace_bytes, void *stream);
+
+/* Per-phase SCF timings of the last pdg_energy_gradients call that used this workspace: for every frame
+ * PDG_NTIMERS GPU clock-cycle counts (clock64 of the frame's CTA), the device counterpart of the phase
+ * timings of pMolecule.QCModel.pyx:208-275 (EnergyWithTimings: QC Fock, QC Converger Iterate,
+ * QC Converger Densities), with the density step split into its parts.  d_out: n_frames * PDG_NTIMERS. */
+#define PDG_NTIMERS 10
+enum {
+    PDG_T_FOCK = 0, PDG_T_DIIS_SAVE = 1, PDG_T_ITERATE = 2, PDG_T_TRIDIAGONAL = 3, PDG_T_EIGENVALUES = 4,
+    PDG_T_EIGENVECTORS = 5, PDG_T_BACKTRANSFORM = 6, PDG_T_DENSITY = 7, PDG_T_TOTAL = 8, PDG_T_CYCLES = 9
+};
+int pdg_scf_timings(const pdg_system *sys, int n_frames, const void *d_workspace, size_t workspace_bytes,
+                    double *d_out, void *stream);
 
 /* QC/MM electrostatics with MM point charges.
  * model 0: NBModelFull, plain 1/r over all pairs (NBModelFull.c:604 potentials, :392 gradients).

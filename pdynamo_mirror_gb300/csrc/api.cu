@@ -207,6 +207,20 @@ extern "C" int pdg_gradients(pdg_system *s, int n_frames, const double *d_xyz, c
     return cuda_check(cudaGetLastError(), "gradient kernels");
 }
 
+extern "C" int pdg_scf_timings(const pdg_system *s, int n_frames, const void *ws, size_t bytes, double *d_out, void *stream)
+{
+    int rc = check_workspace(s, n_frames, const_cast<void *>(ws), bytes);
+    if (rc) return rc;
+    if (!d_out) return fail(PDG_BAD_ARGUMENT, "null output");
+    FramePlan p = plan_for(s, PDG_MAX_HISTORY);
+    const double *w = (const double *)ws;
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int f = 0; f < n_frames; f++)
+        if ((rc = cuda_check(cudaMemcpyAsync(d_out + (size_t)f * PDG_NTIMERS, w + f * p.stride + p.misc + PDG_MAX_HISTORY * PDG_MAX_HISTORY,
+                                             sizeof(double) * PDG_NTIMERS, cudaMemcpyDeviceToDevice, st), "copy timings"))) return rc;
+    return PDG_OK;
+}
+
 extern "C" int pdg_qcmm_potentials(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,
                                    const double *q, int n_knots, const double *knots, double cutoff, double *phi, void *stream)
 {

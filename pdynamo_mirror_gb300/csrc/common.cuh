@@ -55,7 +55,7 @@ __host__ inline FramePlan make_plan(const DeviceSystem &s, int history)
     p.hE = o;     o += align32((size_t)history * p.hist_len);
     p.rP = o;     o += align32(NN);
     p.rF = o;     o += align32(NN);
-    p.misc = o;   o += align32(PDG_MAX_HISTORY * PDG_MAX_HISTORY + 64);
+    p.misc = o;   o += align32(PDG_MAX_HISTORY * PDG_MAX_HISTORY + 64);   // DIIS B matrix, then PDG_NTIMERS phase timers
     p.stride = align32(o);
     return p;
 }

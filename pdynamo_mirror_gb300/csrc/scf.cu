@@ -235,7 +235,15 @@ __device__ int sturm_count(int N, const double *d, const double *e2, double x, d
     return c;
 }
 
-__device__ double density_step(const SCFArgs &a, double *wsf, const double *F, double *P, Smem &sm)
+// Phase timers: thread 0 accumulates clock64() deltas between block-wide barriers into the frame's
+// timer slots (workspace misc area, after the DIIS B matrix).
+struct Timer {
+    double *slot; long long t;
+    __device__ void start() { if (threadIdx.x == 0) t = clock64(); }
+    __device__ void lap(int k) { if (threadIdx.x == 0) { long long n = clock64(); slot[k] += (double)(n - t); t = n; } }
+};
+
+__device__ double density_step(const SCFArgs &a, double *wsf, const double *F, double *P, Smem &sm, Timer &tm)
 {
     const DeviceSystem &s = a.s;
     const FramePlan &pl = a.plan;
@@ -294,6 +302,7 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
         sm.e[N - 1] = 0.0;
     }
     __syncthreads();
+    tm.lap(PDG_T_TRIDIAGONAL);
     // --- eigenvalues by bisection, one thread per wanted index (ascending)
     double gl = 1e300, gu = -1e300, emax2 = 0.0;
     for (int i = tid; i < N; i += PDG_BLOCK) {
@@ -317,6 +326,7 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
         sm.eig[t] = 0.5 * (lo + hi);
     }
     __syncthreads();
+    tm.lap(PDG_T_EIGENVALUES);
     // --- clusters (dstein-style): gaps below ortol share re-orthogonalisation; equal values are split
     if (tid == 0) {
         double onenrm = 0.0;
@@ -395,6 +405,7 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
         }
     }
     __syncthreads();
+    tm.lap(PDG_T_EIGENVECTORS);
     // --- back-transformation z <- Q z (reflectors applied last to first), one warp per vector
     for (int t = w; t < kv; t += PDG_WARPS) {
         double *zt = Z + (size_t)t * N;
@@ -411,6 +422,7 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
         }
     }
     __syncthreads();
+    tm.lap(PDG_T_BACKTRANSFORM);
     // --- P = 2 Z^T Z (occupied) or 2 (1 - Z^T Z) (virtual); lower triangle then mirrored
     const bool occ = s.vec_occupied;
     double rms = 0.0;
@@ -422,7 +434,9 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
         P[(size_t)i * N + j] = pn;
         if (i != j) P[(size_t)j * N + i] = pn;
     });
-    return sqrt(block_sum(rms, sm.red)) / (double)N;
+    double out = sqrt(block_sum(rms, sm.red)) / (double)N;
+    tm.lap(PDG_T_DENSITY);
+    return out;
 }
 
 // ----------------------------------------------------------------------------------------------------
@@ -438,6 +452,12 @@ __global__ void __launch_bounds__(PDG_BLOCK, 1) k_scf(SCFArgs a)
     double *H = wsf + pl.H, *F = wsf + pl.F, *P = a.density + (size_t)f * NN;
     const double *tei = wsf + pl.tei;
     double *Bm = wsf + pl.misc;   // DIIS B matrix, PDG_MAX_HISTORY^2
+    Timer tm;
+    tm.slot = wsf + pl.misc + PDG_MAX_HISTORY * PDG_MAX_HISTORY;
+    long long t_begin = clock64();
+    if (tid < PDG_NTIMERS) tm.slot[tid] = 0.0;
+    __syncthreads();
+    tm.start();
     // nuclear energy: sum of the pair terms in pair order
     double en = 0.0;
     for (int p = tid; p < s.n_pairs; p += PDG_BLOCK) en += wsf[pl.pair_e + (size_t)p * PDG_PAIR_E_STRIDE + 20];
@@ -469,8 +489,11 @@ __global__ void __launch_bounds__(PDG_BLOCK, 1) k_scf(SCFArgs a)
     int iteration = 0, converged = 0, qdiis = 0, qrca = o.use_rca ? 1 : 0, st = PDG_NOT_CONVERGED;
     double eold = 0.0, deltaeold = 0.0, rms = 0.0, eel = 0.0;
     __syncthreads();
+    int ncyc = 0;
     while (iteration < o.maximum_scf_cycles && !converged) {
         fock_build(a, f, H, P, F, tei, sm, &e1, &e2, &eq);
+        tm.lap(PDG_T_FOCK);
+        ncyc++;
         eel = e1 + e2 + eq;
         if (!isfinite(eel)) { st = PDG_NAN; break; }
         converged = (iteration > 0) && (rms <= o.density_tolerance) && (deltaeold <= o.energy_tolerance);
@@ -512,6 +535,7 @@ __global__ void __launch_bounds__(PDG_BLOCK, 1) k_scf(SCFArgs a)
                 if (tid == 0) { int n = ctl[2 + m]; Bm[n * PDG_MAX_HISTORY + newest] = b; Bm[newest * PDG_MAX_HISTORY + n] = b; }
             }
             __syncthreads();
+            tm.lap(PDG_T_DIIS_SAVE);
             if (iteration > 0) {
                 if (o.use_rca) {
                     if (qdiis && maxerr > 0.8) { qdiis = 0; qrca = 1; }
@@ -592,7 +616,8 @@ __global__ void __launch_bounds__(PDG_BLOCK, 1) k_scf(SCFArgs a)
         }
         deltaeold = deltae; eold = etemp;
         __syncthreads();
-        rms = density_step(a, wsf, F, P, sm);
+        tm.lap(PDG_T_ITERATE);
+        rms = density_step(a, wsf, F, P, sm, tm);
         valid = true;
     }
     if (converged) st = PDG_OK;
@@ -601,6 +626,8 @@ __global__ void __launch_bounds__(PDG_BLOCK, 1) k_scf(SCFArgs a)
         E[0] = eel; E[1] = e1 + e2; E[2] = en; E[3] = base; E[4] = eq; E[5] = e1; E[6] = e2; E[7] = rms;
         a.status[f] = st;
         if (a.ncycles) a.ncycles[f] = iteration;
+        tm.slot[PDG_T_TOTAL] = (double)(clock64() - t_begin);
+        tm.slot[PDG_T_CYCLES] = (double)ncyc;
     }
 }
 

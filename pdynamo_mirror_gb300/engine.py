@@ -112,6 +112,15 @@ class QCEngine:
             out.update(qcmm_qc_gradients=gqc, qcmm_mm_gradients=gmm)
         return out
 
+    def timings(self, n_frames):
+        """Per-frame SCF phase timings (GPU clock cycles) of the last run, as {name: array}."""
+        out = torch.empty((n_frames, len(_native.TIMERS)), dtype=torch.float64, device=self.device)
+        ws = self.workspace(n_frames)
+        _native.check(self.L.pdg_scf_timings(self.handle, n_frames, _native.ptr(ws), ws.numel(), _native.ptr(out),
+                                             _native.stream_handle(torch.cuda.current_stream(self.device))), "pdg_scf_timings")
+        t = out.cpu().numpy()
+        return {name: t[:, k] for k, name in enumerate(_native.TIMERS)}
+
     # diagnostics used by the parity tests
     def one_electron(self, qc_xyz):
         F = qc_xyz.shape[0]
