@@ -29,7 +29,7 @@ struct DeviceSystem {
 
 // Per-frame workspace plan (all offsets in doubles from the frame's base).
 struct FramePlan {
-    size_t tei, pair_e, pair_g, H, F, P0, A, HV, Z, LU, hP, hF, hE, rP, rF, misc, stride;
+    size_t tei, pair_e, pair_g, H, F, P0, A, G, Z, LU, hP, hF, hE, rP, rF, misc, stride;
     int hist_len;   // packed history vector length N(N+1)/2 (errors use N(N-1)/2 within the same slot)
 };
 
@@ -47,9 +47,10 @@ __host__ inline FramePlan make_plan(const DeviceSystem &s, int history)
     p.F = o;      o += align32(NN);
     p.P0 = o;     o += align32(NN);          // previous density (for the RMS change)
     p.A = o;      o += align32(NN);          // work matrix: F P product, tridiagonalisation
-    p.HV = o;     o += align32(NN);          // Householder vectors, one row per reflector
-    p.Z = o;      o += align32(N * (size_t)(s.n_vec > 0 ? s.n_vec : 1));
-    p.LU = o;     o += align32((size_t)PDG_WARPS * 8 * N);
+    const size_t kv = s.n_vec > 0 ? s.n_vec : 1, kvp = (kv + 31) & ~size_t(31);
+    p.G = o;      o += align32(kv * N);      // DIIS: the vectors times F
+    p.Z = o;      o += align32(kv * (N | 1)); // wanted eigenvectors when they do not fit in shared memory
+    p.LU = o;     o += align32(5 * N * kvp + (N * kvp + 7) / 8);   // inverse iteration factors + iterates
     p.hP = o;     o += align32((size_t)history * p.hist_len);
     p.hF = o;     o += align32((size_t)history * p.hist_len);
     p.hE = o;     o += align32((size_t)history * p.hist_len);

@@ -15,8 +15,6 @@
 // shared-memory GEMMs and everything sequential is confined to O(N) or O(N^2) work.
 #include "common.cuh"
 
-#define TILE 64
-#define KCH 16
 
 struct SCFArgs {
     DeviceSystem s; FramePlan plan; int n_frames;
@@ -26,59 +24,101 @@ struct SCFArgs {
     double *ws; int fock_only; double *fock_out;
 };
 
-// Shared scratch layout (doubles): red[32] | gemm tiles 2*TILE*KCH | small[256] | d,e,e2,tau,eig (5N) | v,p (2N)
 struct Smem {
-    double *red, *ta, *tb, *small, *d, *e, *e2, *tau, *eig, *v, *p;
-    int *iv;   // ints: [0..63] control, [64..] cluster starts
+    double *red, *small, *d, *e, *e2, *tau, *eig, *v, *v2, *p, *w, *dot;
+    double *ta, *tb;   // GEMM staging
+    double *amat;      // packed lower triangle of the matrix being tridiagonalised (null: in the workspace)
+    double *zs;        // the wanted eigenvectors, one row of ldz per vector (null: in the workspace)
+    int ldz;
+    int *iv;           // ints: [0..63] control, [64..64+N) per-vector cluster starts
 };
 
-__device__ __forceinline__ Smem carve(double *base, int N)
+// GEMM tile: GM x GN outputs per pass, GK-deep staged chunks (padded rows against bank conflicts).
+#define GM 32
+#define GN 64
+#define GK 16
+#define GA_LD (GM + 1)
+#define GB_LD (GN + 1)
+
+// Shared memory plan: red | small | d e e2 tau eig v v2 p w (9N) | dot | ints | GEMM staging | amat | zs.
+// The packed matrix goes to shared memory when it fits, then the eigenvectors.
+struct SmemPlan { size_t head, work, amat, zs, bytes; int ldz; };
+
+__host__ __device__ inline SmemPlan smem_plan(int N, int kv)
+{
+    SmemPlan p;
+    p.head = 32 + 256 + 9 * (size_t)N + 64 + ((64 + (size_t)N + 2) * sizeof(int) + 7) / 8;
+    p.work = (size_t)GK * GA_LD + (size_t)GK * GB_LD;
+    p.ldz = N | 1;
+    const size_t limit = 220 * 1024 / 8, packed = (size_t)N * (N + 1) / 2, zsz = (size_t)(kv > 0 ? kv : 1) * p.ldz;
+    p.amat = (p.head + p.work + packed <= limit) ? packed : 0;
+    p.zs = (p.amat && p.head + p.work + packed + zsz <= limit) ? zsz : 0;
+    p.bytes = 8 * (p.head + p.work + p.amat + p.zs);
+    return p;
+}
+
+__device__ __forceinline__ Smem carve(double *base, int N, int kv)
 {
     Smem m;
-    m.red = base; m.ta = base + 32; m.tb = m.ta + TILE * KCH; m.small = m.tb + TILE * KCH;
-    m.d = m.small + 256; m.e = m.d + N; m.e2 = m.e + N; m.tau = m.e2 + N; m.eig = m.tau + N; m.v = m.eig + N; m.p = m.v + N;
-    m.iv = (int *)(m.p + N);
+    SmemPlan sp = smem_plan(N, kv);
+    m.red = base; m.small = base + 32;
+    m.d = m.small + 256; m.e = m.d + N; m.e2 = m.e + N; m.tau = m.e2 + N; m.eig = m.tau + N;
+    m.v = m.eig + N; m.v2 = m.v + N; m.p = m.v2 + N; m.w = m.p + N; m.dot = m.w + N;
+    m.iv = (int *)(m.dot + 64);
+    double *work = base + sp.head;
+    m.ta = work; m.tb = work + GK * GA_LD;
+    m.amat = sp.amat ? work + sp.work : nullptr;
+    m.zs = sp.zs ? work + sp.work + sp.amat : nullptr;
+    m.ldz = sp.ldz;
     return m;
 }
 
-// C = A * B over M x Nc outputs with inner dimension K; element accessors are strided.  Each thread owns
-// a 2 x 4 register tile of a TILE x TILE output tile.  lower_only skips tiles strictly above the diagonal.
-// The epilogue receives (i, j, value).
-template <typename Epi>
-__device__ void block_gemm(int M, int Nc, int K, const double *A, int a_r, int a_c, const double *B, int b_r, int b_c,
-                           bool lower_only, Smem &sm, Epi epi)
+// C = A B over M x Nc outputs with inner dimension K; fa(i, k) and fb(k, j) fetch the operands (AK / BK: k is
+// the contiguous index of that operand, which picks the coalesced staging order).  Each warp owns an
+// 8 x 16 sub-tile of the GM x GN pass (2 x 2 outputs per lane) and skips the FMA loop when the sub-tile lies
+// outside the output, or above the diagonal when lower_only; warp (wr, wc) sits on FP64 unit (wr + wc) % 4,
+// so the partial warps of edge tiles stay spread over all four.  The epilogue receives every (i, j) < (M, Nc)
+// of an active sub-tile; lower_only callers filter j > i there.
+template <bool AK, bool BK, typename FA, typename FB, typename Epi>
+__device__ void tgemm(int M, int Nc, int K, FA fa, FB fb, bool lower_only, Smem &sm, Epi epi)
 {
-    const int tid = threadIdx.x;
-    const int tr = tid / 16, tc = tid % 16;   // 32 x 16 threads -> rows tr*2 + {0,1}, cols tc*4 + {0..3}
-    for (int i0 = 0; i0 < M; i0 += TILE)
-        for (int j0 = 0; j0 < Nc; j0 += TILE) {
-            if (lower_only && j0 > i0 + TILE - 1) continue;
-            double acc[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
-            for (int k0 = 0; k0 < K; k0 += KCH) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int wr = w >> 2, wc = ((w & 3) - wr) & 3;
+    const int r0 = wr * 8 + (lane >> 3) * 2, c0 = wc * 16 + (lane & 7) * 2;
+    double *ga = sm.ta, *gb = sm.tb;
+    for (int i0 = 0; i0 < M; i0 += GM)
+        for (int j0 = 0; j0 < Nc; j0 += GN) {
+            if (lower_only && j0 > i0 + GM - 1) continue;
+            const bool active = (i0 + wr * 8 < M) && (j0 + wc * 16 < Nc) && !(lower_only && j0 + wc * 16 > i0 + wr * 8 + 7);
+            double a00 = 0.0, a01 = 0.0, a10 = 0.0, a11 = 0.0;
+            for (int k0 = 0; k0 < K; k0 += GK) {
+                const int kc = min(GK, K - k0);
                 __syncthreads();
-                for (int t = tid; t < TILE * KCH; t += PDG_BLOCK) {
-                    int r = t / KCH, kk = t % KCH, gi = i0 + r, gk = k0 + kk;
-                    sm.ta[kk * TILE + r] = (gi < M && gk < K) ? A[(size_t)gi * a_r + (size_t)gk * a_c] : 0.0;
-                    int c = t % TILE, kb = t / TILE, gj = j0 + c, gk2 = k0 + kb;
-                    sm.tb[kb * TILE + c] = (gj < Nc && gk2 < K) ? B[(size_t)gk2 * b_r + (size_t)gj * b_c] : 0.0;
+                {
+                    const int r = AK ? tid / GK : tid % GM, kk = AK ? tid % GK : tid / GM, gi = i0 + r;
+                    ga[kk * GA_LD + r] = (kk < kc && gi < M) ? fa(gi, k0 + kk) : 0.0;
+                }
+                for (int t = tid; t < GK * GN; t += PDG_BLOCK) {
+                    const int c = BK ? t / GK : t % GN, kk = BK ? t % GK : t / GN, gj = j0 + c;
+                    gb[kk * GB_LD + c] = (kk < kc && gj < Nc) ? fb(k0 + kk, gj) : 0.0;
                 }
                 __syncthreads();
-#pragma unroll
-                for (int kk = 0; kk < KCH; kk++) {
-                    double a0 = sm.ta[kk * TILE + tr * 2], a1 = sm.ta[kk * TILE + tr * 2 + 1];
-#pragma unroll
-                    for (int c = 0; c < 4; c++) {
-                        double b = sm.tb[kk * TILE + tc * 4 + c];
-                        acc[0][c] = fma(a0, b, acc[0][c]);
-                        acc[1][c] = fma(a1, b, acc[1][c]);
+                if (active) {
+#pragma unroll 4
+                    for (int kk = 0; kk < kc; kk++) {
+                        const double x0 = ga[kk * GA_LD + r0], x1 = ga[kk * GA_LD + r0 + 1];
+                        const double y0 = gb[kk * GB_LD + c0], y1 = gb[kk * GB_LD + c0 + 1];
+                        a00 = fma(x0, y0, a00); a01 = fma(x0, y1, a01); a10 = fma(x1, y0, a10); a11 = fma(x1, y1, a11);
                     }
                 }
             }
-            for (int r = 0; r < 2; r++)
-                for (int c = 0; c < 4; c++) {
-                    int gi = i0 + tr * 2 + r, gj = j0 + tc * 4 + c;
-                    if (gi < M && gj < Nc) epi(gi, gj, acc[r][c]);
-                }
+            if (active) {
+                const int gi = i0 + r0, gj = j0 + c0;
+                if (gi < M && gj < Nc) epi(gi, gj, a00);
+                if (gi < M && gj + 1 < Nc) epi(gi, gj + 1, a01);
+                if (gi + 1 < M && gj < Nc) epi(gi + 1, gj, a10);
+                if (gi + 1 < M && gj + 1 < Nc) epi(gi + 1, gj + 1, a11);
+            }
         }
     __syncthreads();
 }
@@ -221,16 +261,18 @@ __device__ unsigned int hash2(unsigned int a, unsigned int b)
     return h;
 }
 
-__device__ int sturm_count(int N, const double *d, const double *e2, double x, double pivmin)
+// Sturm count in FP32: number of eigenvalues of T below x (LDL^T pivots, pivmin guard).  The counts only
+// locate shifts for inverse iteration, which then converges in FP64 on the FP64 matrix.
+__device__ int sturm_count32(int N, const float *d, const float *e2, float x, float pivmin)
 {
     int c = 0;
-    double q = d[0] - x;
-    if (fabs(q) < pivmin) q = -pivmin;
-    if (q < 0.0) c++;
+    float q = d[0] - x;
+    if (fabsf(q) < pivmin) q = -pivmin;
+    c += (q < 0.0f);
     for (int i = 1; i < N; i++) {
-        q = d[i] - x - e2[i - 1] / q;
-        if (fabs(q) < pivmin) q = -pivmin;
-        if (q < 0.0) c++;
+        q = (d[i] - x) - __fdividef(e2[i - 1], q);
+        if (fabsf(q) < pivmin) q = -pivmin;
+        c += (q < 0.0f);
     }
     return c;
 }
@@ -243,181 +285,280 @@ struct Timer {
     __device__ void lap(int k) { if (threadIdx.x == 0) { long long n = clock64(); slot[k] += (double)(n - t); t = n; } }
 };
 
+// Packed lower-triangle element (i >= j) of the matrix being tridiagonalised.
+__device__ __forceinline__ int plo(int i, int j) { return i * (i + 1) / 2 + j; }
+
+// Householder reflector for column c (rows c+1 .. N-1) of the packed matrix, by one warp (dlarfg): writes
+// v (v[0] = 1) to vout and into the column below the subdiagonal, tau and the subdiagonal beta.
+__device__ void make_reflector(double *A, int N, int c, double *vout, Smem &sm)
+{
+    const int lane = threadIdx.x & 31, m = N - c - 1, r0 = c + 1;
+    const double alpha = A[plo(r0, c)];
+    double part = 0.0;
+    for (int i = 1 + lane; i < m; i += 32) { const double x = A[plo(r0 + i, c)]; part = fma(x, x, part); }
+    const double xn2 = warp_sum(part);
+    double tau = 0.0, e = alpha, scal = 0.0;
+    if (xn2 != 0.0) {
+        const double beta = -copysign(sqrt(fma(alpha, alpha, xn2)), alpha);
+        tau = (beta - alpha) / beta; e = beta; scal = 1.0 / (alpha - beta);
+    }
+    for (int i = lane; i < m; i += 32) {
+        const double vi = (i == 0) ? 1.0 : A[plo(r0 + i, c)] * scal;
+        vout[i] = vi;
+        if (i > 0 && tau != 0.0) A[plo(r0 + i, c)] = vi;
+    }
+    if (lane == 0) { sm.e[c] = e; sm.tau[c] = tau; }
+}
+
+// Inverse iteration for one eigenvector of the tridiagonal T (d, e) at shift sigma, by ONE thread: the LU
+// factors of T - sigma I with row interchanges (dgttrf form: multiplier l_k, pivot flag, U row
+// 1/u_kk, u_k,k+1, u_k,k+2), four solves, re-orthogonalisation against the earlier vectors q0 .. t-1 of the
+// same cluster (dstein), normalisation.  The factor arrays and the iterate are interleaved by vector (stride
+// ld) so the threads of a warp access them coalesced.  Pivoting is branch-free (selects), so the lanes of a
+// warp never diverge; loads are issued in blocks of eight ahead of the dependent recurrence.
+__device__ void inverse_iteration(int N, int t, double sigma, double tiny, const double *__restrict__ d, const double *__restrict__ e,
+                                  double *__restrict__ u0, double *__restrict__ u1, double *__restrict__ u2, double *__restrict__ lm,
+                                  unsigned char *__restrict__ pv, double *__restrict__ y, int ld, const double *zq0, int nq, int ldz,
+                                  double *__restrict__ zout)
+{
+    double ak = d[0] - sigma, bk = e[0];
+    for (int k = 0; k < N - 1; k++) {
+        const double ck = e[k], an = d[k + 1] - sigma, bn = e[k + 1];
+        const bool sw = fabs(ak) < fabs(ck);
+        double piv = sw ? ck : ak;
+        if (fabs(piv) < tiny) piv = copysign(tiny, piv);
+        const double r = __drcp_rn(piv), l = (sw ? ak : ck) * r;
+        const double uu1 = sw ? an : bk, uu2 = sw ? bn : 0.0;
+        u0[(size_t)k * ld] = r; u1[(size_t)k * ld] = uu1; u2[(size_t)k * ld] = uu2; lm[(size_t)k * ld] = l; pv[(size_t)k * ld] = sw;
+        ak = fma(-l, uu1, sw ? bk : an);
+        bk = fma(-l, uu2, sw ? 0.0 : bn);
+    }
+    if (fabs(ak) < tiny) ak = copysign(tiny, ak);
+    u0[(size_t)(N - 1) * ld] = __drcp_rn(ak);
+    for (int i = 0; i < N; i++) y[(size_t)i * ld] = ((hash2(t * 2654435761u + 17u, i) >> 8) * (1.0 / 16777216.0)) * 2.0 - 1.0;
+    for (int it = 0; it < 4; it++) {
+        // forward: interchanges and L
+        double c = y[0];
+        int k = 0;
+        for (; k + 8 <= N - 1; k += 8) {
+            double xn[8], l[8]; bool sw[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) { xn[q] = y[(size_t)(k + 1 + q) * ld]; l[q] = lm[(size_t)(k + q) * ld]; sw[q] = pv[(size_t)(k + q) * ld]; }
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const double yk = sw[q] ? xn[q] : c, cn = sw[q] ? c : xn[q];
+                y[(size_t)(k + q) * ld] = yk;
+                c = fma(-l[q], yk, cn);
+            }
+        }
+        for (; k < N - 1; k++) {
+            const double xn = y[(size_t)(k + 1) * ld], l = lm[(size_t)k * ld];
+            const bool sw = pv[(size_t)k * ld];
+            const double yk = sw ? xn : c, cn = sw ? c : xn;
+            y[(size_t)k * ld] = yk;
+            c = fma(-l, yk, cn);
+        }
+        // back substitution with U
+        double x1 = c * u0[(size_t)(N - 1) * ld], x2 = 0.0;
+        y[(size_t)(N - 1) * ld] = x1;
+        k = N - 2;
+        for (; k - 7 >= 0; k -= 8) {
+            double yy[8], a0[8], a1[8], a2[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const size_t o = (size_t)(k - q) * ld;
+                yy[q] = y[o]; a0[q] = u0[o]; a1[q] = u1[o]; a2[q] = u2[o];
+            }
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const double x0 = fma(-a2[q], x2, fma(-a1[q], x1, yy[q])) * a0[q];
+                y[(size_t)(k - q) * ld] = x0;
+                x2 = x1; x1 = x0;
+            }
+        }
+        for (; k >= 0; k--) {
+            const size_t o = (size_t)k * ld;
+            const double x0 = fma(-u2[o], x2, fma(-u1[o], x1, y[o])) * u0[o];
+            y[o] = x0;
+            x2 = x1; x1 = x0;
+        }
+        // the iterate is never rescaled between solves: four solves grow it by at most (1/tiny)^4, far
+        // inside the double range, and the projections below do not depend on its scale
+        for (int q = 0; q < nq; q++) {
+            const double *zq = zq0 + (size_t)q * ldz;
+            double dt = 0.0;
+            for (int i = 0; i < N; i++) dt = fma(y[(size_t)i * ld], zq[i], dt);
+            for (int i = 0; i < N; i++) y[(size_t)i * ld] = fma(-dt, zq[i], y[(size_t)i * ld]);
+        }
+    }
+    double nr = 0.0;
+    for (int i = 0; i < N; i++) { const double v = y[(size_t)i * ld]; nr = fma(v, v, nr); }
+    const double sc = rsqrt(nr);
+    for (int i = 0; i < N; i++) zout[i] = y[(size_t)i * ld] * sc;
+}
+
 __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, double *P, Smem &sm, Timer &tm)
 {
     const DeviceSystem &s = a.s;
     const FramePlan &pl = a.plan;
     const int N = s.n_basis, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int kv = s.n_vec;
-    double *A = wsf + pl.A, *HV = wsf + pl.HV, *Z = wsf + pl.Z;
-    for (size_t k = tid; k < (size_t)N * N; k += PDG_BLOCK) A[k] = F[k];
+    const int kv = s.n_vec, ldz = sm.ldz;
+    double *A = sm.amat ? sm.amat : wsf + pl.A;   // packed lower triangle
+    double *Z = sm.zs ? sm.zs : wsf + pl.Z;       // wanted eigenvectors, kv rows of ldz
+    for (int i = w; i < N; i += PDG_WARPS)
+        for (int j = lane; j <= i; j += 32) A[plo(i, j)] = F[(size_t)i * N + j];
     __syncthreads();
-    // --- Householder tridiagonalisation A = Q T Q^T (lower, dsytd2-style; the full square is updated so
-    //     every access is a contiguous row).
+    // --- Householder tridiagonalisation A = Q T Q^T (dsytd2 'L'), (2/3) N^3 FMA.  Per step: the product
+    //     p = tau A22 v one thread per row (no reductions); K = tau (p.v)/2 and w = p - K v; the rank-2
+    //     update of the lower triangle over all warps by flat element index, while warp 0 updates the
+    //     first column of A22 and builds the next reflector from it (look-ahead).
+    double *vc = sm.v, *vn = sm.v2;
+    if (tid == 0) sm.d[0] = A[0];
+    if (N >= 3 && w == 0) make_reflector(A, N, 0, vc, sm);
+    __syncthreads();
     for (int k = 0; k + 2 < N; k++) {
-        int m = N - k - 1;
-        const double *row = A + (size_t)k * N + k + 1;
-        double part = 0.0;
-        for (int i = 1 + tid; i < m; i += PDG_BLOCK) part += row[i] * row[i];
-        double xn2 = block_sum(part, sm.red);
-        double alpha = row[0];
-        if (tid == 0) sm.d[k] = A[(size_t)k * N + k];
-        if (xn2 == 0.0) {
-            if (tid == 0) { sm.e[k] = alpha; sm.tau[k] = 0.0; }
-            __syncthreads();
-            continue;
-        }
-        double beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
-        double tau = (beta - alpha) / beta, scal = 1.0 / (alpha - beta);
-        for (int i = tid; i < m; i += PDG_BLOCK) {
-            double vi = (i == 0) ? 1.0 : row[i] * scal;
-            sm.v[i] = vi;
-            HV[(size_t)k * N + i] = vi;
-        }
-        if (tid == 0) { sm.e[k] = beta; sm.tau[k] = tau; }
-        __syncthreads();
-        // p = tau A22 v (warp per row)
-        for (int i = w; i < m; i += PDG_WARPS) {
-            const double *ar = A + (size_t)(k + 1 + i) * N + k + 1;
+        const int m = N - k - 1, c0 = k + 1, R = (m + 31) >> 5;
+        const double tau = sm.tau[k];
+        for (int rb = w; rb < R; rb += PDG_WARPS) {
+            const int i = rb * 32 + lane;
             double t = 0.0;
-            for (int j = lane; j < m; j += 32) t += ar[j] * sm.v[j];
-            t = warp_sum(t);
-            if (lane == 0) sm.p[i] = tau * t;
+            if (i < m) {
+                const int bi = plo(c0 + i, c0);
+                int tj = plo(c0, c0);
+                for (int j = 0; j < m; j++) {
+                    const int ad = (j <= i) ? bi + j : tj + i;
+                    t = fma(A[ad], vc[j], t);
+                    tj += c0 + j + 1;
+                }
+                t *= tau;
+                sm.p[i] = t;
+            }
+            const double pv = warp_sum(i < m ? t * vc[i] : 0.0);
+            if (lane == 0) sm.dot[rb] = pv;
         }
         __syncthreads();
-        double pv = 0.0;
-        for (int i = tid; i < m; i += PDG_BLOCK) pv += sm.p[i] * sm.v[i];
-        double K = 0.5 * tau * block_sum(pv, sm.red);
-        for (int i = tid; i < m; i += PDG_BLOCK) sm.p[i] -= K * sm.v[i];   // p <- w
-        __syncthreads();
-        for (int t = tid; t < m * m; t += PDG_BLOCK) {
-            int i = t / m, j = t % m;
-            A[(size_t)(k + 1 + i) * N + k + 1 + j] -= sm.v[i] * sm.p[j] + sm.p[i] * sm.v[j];
+        for (int rb = w; rb < R; rb += PDG_WARPS) {
+            double sdot = 0.0;
+            for (int q = lane; q < R; q += 32) sdot += sm.dot[q];
+            const double K = 0.5 * tau * warp_sum(sdot);
+            const int i = rb * 32 + lane;
+            if (i < m) sm.w[i] = fma(-K, vc[i], sm.p[i]);
         }
         __syncthreads();
+        if (w == 0) {
+            const double v0 = vc[0], w0 = sm.w[0];
+            for (int i = lane; i < m; i += 32) { const int ad = plo(c0 + i, c0); A[ad] -= fma(vc[i], w0, sm.w[i] * v0); }
+            __syncwarp();
+            if (lane == 0) sm.d[c0] = A[plo(c0, c0)];
+            if (m >= 3) make_reflector(A, N, c0, vn, sm);
+            else if (lane == 0) { sm.e[c0] = A[plo(c0 + 1, c0)]; sm.tau[c0] = 0.0; }
+        } else {
+            const int nt = (m - 1) * m / 2;   // elements (i, j) of A22 with 1 <= j <= i < m
+            for (int el = tid - 32; el < nt; el += PDG_BLOCK - 32) {
+                int ii = (int)((sqrtf(8.0f * (float)el + 1.0f) - 1.0f) * 0.5f);
+                while ((ii + 1) * (ii + 2) / 2 <= el) ii++;
+                while (ii * (ii + 1) / 2 > el) ii--;
+                const int i = ii + 1, j = el - ii * (ii + 1) / 2 + 1;
+                const int ad = plo(c0 + i, c0 + j);
+                A[ad] -= fma(vc[i], sm.w[j], sm.w[i] * vc[j]);
+            }
+        }
+        __syncthreads();
+        double *tmp = vc; vc = vn; vn = tmp;
     }
     if (tid == 0) {
-        if (N >= 2) { sm.d[N - 2] = A[(size_t)(N - 2) * N + N - 2]; sm.e[N - 2] = A[(size_t)(N - 2) * N + N - 1]; sm.tau[N - 2] = 0.0; }
-        sm.d[N - 1] = A[(size_t)(N - 1) * N + N - 1];
+        if (N == 2) { sm.e[0] = A[plo(1, 0)]; sm.tau[0] = 0.0; }
+        if (N >= 2) sm.d[N - 1] = A[plo(N - 1, N - 1)];
         sm.e[N - 1] = 0.0;
     }
     __syncthreads();
     tm.lap(PDG_T_TRIDIAGONAL);
-    // --- eigenvalues by bisection, one thread per wanted index (ascending)
-    double gl = 1e300, gu = -1e300, emax2 = 0.0;
+    // --- shifts: the wanted eigenvalues of T by FP32 Sturm multisection, eight threads per eigenvalue,
+    //     each round narrowing the bracket ninefold
+    float *d32 = (float *)sm.e2, *e232 = d32 + N;
+    double gl = 1e300, gu = -1e300, emax2 = 0.0, onen = 0.0;
     for (int i = tid; i < N; i += PDG_BLOCK) {
-        double r = (i > 0 ? fabs(sm.e[i - 1]) : 0.0) + (i < N - 1 ? fabs(sm.e[i]) : 0.0);
-        gl = fmin(gl, sm.d[i] - r); gu = fmax(gu, sm.d[i] + r);
-        if (i < N - 1) { sm.e2[i] = sm.e[i] * sm.e[i]; emax2 = fmax(emax2, sm.e2[i]); }
+        const double r = (i > 0 ? fabs(sm.e[i - 1]) : 0.0) + (i < N - 1 ? fabs(sm.e[i]) : 0.0);
+        gl = fmin(gl, sm.d[i] - r); gu = fmax(gu, sm.d[i] + r); onen = fmax(onen, fabs(sm.d[i]) + r);
+        d32[i] = (float)sm.d[i];
+        const double e2 = (i < N - 1) ? sm.e[i] * sm.e[i] : 0.0;
+        e232[i] = (float)e2; emax2 = fmax(emax2, e2);
     }
-    gl = -block_max(-gl, sm.red); gu = block_max(gu, sm.red); emax2 = block_max(emax2, sm.red);
-    double tnorm = fmax(fabs(gl), fabs(gu));
-    double pivmin = 1.0e-290 * fmax(1.0, emax2);
-    gl -= 2.2e-16 * tnorm * 4.0 * N + pivmin; gu += 2.2e-16 * tnorm * 4.0 * N + pivmin;
-    int first = s.vec_occupied ? 0 : N - kv;
-    for (int t = tid; t < kv; t += PDG_BLOCK) {
-        int m = first + t;
-        double lo = gl, hi = gu;
-        for (int it = 0; it < 200; it++) {
-            double mid = 0.5 * (lo + hi);
-            if (hi - lo <= 2.2e-16 * fmax(fabs(lo), fabs(hi)) + 4.0 * pivmin || mid == lo || mid == hi) break;
-            if (sturm_count(N, sm.d, sm.e2, mid, pivmin) <= m) lo = mid; else hi = mid;
+    gl = -block_max(-gl, sm.red); gu = block_max(gu, sm.red); emax2 = block_max(emax2, sm.red); onen = block_max(onen, sm.red);
+    const double tnorm = fmax(fabs(gl), fabs(gu));
+    const float pivmin = (float)(1.0e-30 * fmax(1.0, emax2));
+    const float glo = (float)(gl - 1.0e-6 * tnorm - 1.0e-30), ghi = (float)(gu + 1.0e-6 * tnorm + 1.0e-30);
+    const int first = s.vec_occupied ? 0 : N - kv;
+    for (int g0 = 0; g0 < kv; g0 += PDG_BLOCK / 8) {
+        const int t = g0 + tid / 8, sl = tid % 8;
+        const unsigned gmask = 0xFFu << (lane & ~7);
+        const bool live = t < kv;
+        const int mi = first + t;
+        float lo = glo, hi = ghi;
+        for (int round = 0; round < 16; round++) {
+            const float x = lo + (hi - lo) * (float)(sl + 1) * (1.0f / 9.0f);
+            const bool below = live && sturm_count32(N, d32, e232, x, pivmin) <= mi;   // x <= lambda_mi
+            const unsigned bal = (__ballot_sync(0xffffffffu, below) & gmask) >> (lane & ~7);
+            const int nb = __popc(bal);   // Sturm counts grow with x: the first nb points lie below
+            const float xl = __shfl_sync(0xffffffffu, x, (lane & ~7) + (nb > 0 ? nb - 1 : 0));
+            const float xh = __shfl_sync(0xffffffffu, x, (lane & ~7) + (nb < 8 ? nb : 7));
+            const float nlo = nb > 0 ? xl : lo, nhi = nb < 8 ? xh : hi;
+            const bool progress = live && (nlo > lo || nhi < hi);
+            lo = nlo; hi = nhi;
+            if (!__any_sync(0xffffffffu, progress)) break;   // every group of the warp is at FP32 resolution
         }
-        sm.eig[t] = 0.5 * (lo + hi);
+        if (live && sl == 0) sm.eig[t] = 0.5 * ((double)lo + (double)hi);
     }
     __syncthreads();
     tm.lap(PDG_T_EIGENVALUES);
-    // --- clusters (dstein-style): gaps below ortol share re-orthogonalisation; equal values are split
+    // --- clusters: neighbours closer than ortol are re-orthogonalised against each other (dstein-style);
+    //     shifts within the FP32 resolution are separated.  iv[64 + t] = first vector of t's cluster,
+    //     iv[0] = largest cluster.
     if (tid == 0) {
-        double onenrm = 0.0;
-        for (int i = 0; i < N; i++) onenrm = fmax(onenrm, fabs(sm.d[i]) + (i > 0 ? fabs(sm.e[i - 1]) : 0.0) + (i < N - 1 ? fabs(sm.e[i]) : 0.0));
-        double ortol = 1.0e-5 * fmax(onenrm, 1.0);
-        int nc = 0;
+        const double ortol = 1.0e-4 * fmax(onen, 1.0);
+        int start = 0, big = kv > 0 ? 1 : 0;
         sm.iv[64] = 0;
         for (int t = 1; t < kv; t++) {
-            double pert = 10.0 * fabs(2.2e-16 * sm.eig[t]) + 1e-300;
+            const double pert = 1.0e-7 * fmax(fabs(sm.eig[t]), 1.0);
             if (sm.eig[t] - sm.eig[t - 1] < pert) sm.eig[t] = sm.eig[t - 1] + pert;
-            if (sm.eig[t] - sm.eig[t - 1] > ortol) sm.iv[64 + (++nc)] = t;
+            if (sm.eig[t] - sm.eig[t - 1] > ortol) start = t;
+            sm.iv[64 + t] = start;
+            big = max(big, t - start + 1);
         }
-        sm.iv[64 + (++nc)] = kv;
-        sm.iv[0] = nc;
-        sm.small[0] = onenrm;
+        sm.iv[0] = big;
+        sm.small[0] = onen;
     }
     __syncthreads();
-    const int nclusters = sm.iv[0];
-    const double tiny = 2.2e-16 * fmax(sm.small[0], 1.0);
-    // --- inverse iteration: one warp per cluster, members in order, 3 iterations each
-    double *lu = wsf + pl.LU + (size_t)w * 8 * N;
-    double *u0 = lu, *u1 = lu + N, *u2 = lu + 2 * N, *lm = lu + 3 * N, *pv = lu + 4 * N, *x = lu + 5 * N;
-    for (int c = w; c < nclusters; c += PDG_WARPS) {
-        int c0 = sm.iv[64 + c], c1 = sm.iv[64 + c + 1];
-        for (int t = c0; t < c1; t++) {
-            double sigma = sm.eig[t];
-            if (lane == 0) {   // T - sigma I = P L U, partial pivoting (U has two super-diagonals)
-                double ak = sm.d[0] - sigma, bk = N > 1 ? sm.e[0] : 0.0;
-                for (int k = 0; k < N - 1; k++) {
-                    double ck = sm.e[k], an = sm.d[k + 1] - sigma, bn = (k + 1 < N - 1) ? sm.e[k + 1] : 0.0;
-                    if (fabs(ak) >= fabs(ck)) {
-                        if (ak == 0.0) ak = tiny;
-                        double l = ck / ak;
-                        u0[k] = ak; u1[k] = bk; u2[k] = 0.0; lm[k] = l; pv[k] = 0.0;
-                        ak = an - l * bk; bk = bn;
-                    } else {
-                        double l = ak / ck;
-                        u0[k] = ck; u1[k] = an; u2[k] = bn; lm[k] = l; pv[k] = 1.0;
-                        ak = bk - l * an; bk = -l * bn;
-                    }
-                }
-                u0[N - 1] = (ak == 0.0) ? tiny : ak;
-                for (int k = 0; k < N; k++) { if (fabs(u0[k]) < tiny) u0[k] = copysign(tiny, u0[k]); u0[k] = 1.0 / u0[k]; }
+    // --- eigenvectors: one thread per vector; cluster members in rounds so that each one is projected
+    //     against the finished earlier members
+    {
+        const int rounds = sm.iv[0], kvp = (kv + 31) & ~31;
+        const double tiny = 2.2e-16 * fmax(sm.small[0], 1.0);
+        double *U0 = wsf + pl.LU, *U1 = U0 + (size_t)N * kvp, *U2 = U1 + (size_t)N * kvp, *LM = U2 + (size_t)N * kvp;
+        double *Y = LM + (size_t)N * kvp;
+        unsigned char *PV = (unsigned char *)(Y + (size_t)N * kvp);
+        for (int r = 0; r < rounds; r++) {
+            for (int t = tid; t < kv; t += PDG_BLOCK) {
+                const int cs = sm.iv[64 + t];
+                if (t - cs != r) continue;
+                inverse_iteration(N, t, sm.eig[t], tiny, sm.d, sm.e, U0 + t, U1 + t, U2 + t, LM + t, PV + t, Y + t, kvp,
+                                  Z + (size_t)cs * ldz, t - cs, ldz, Z + (size_t)t * ldz);
             }
-            for (int i = lane; i < N; i += 32) x[i] = ((hash2(t * 2654435761u + 17u, i) >> 8) * (1.0 / 16777216.0)) * 2.0 - 1.0;
-            __syncwarp();
-            for (int it = 0; it < 3; it++) {
-                if (lane == 0) {
-                    for (int k = 0; k < N - 1; k++) {
-                        if (pv[k] != 0.0) { double tt = x[k]; x[k] = x[k + 1]; x[k + 1] = tt; }
-                        x[k + 1] -= lm[k] * x[k];
-                    }
-                    x[N - 1] *= u0[N - 1];
-                    if (N > 1) x[N - 2] = (x[N - 2] - u1[N - 2] * x[N - 1]) * u0[N - 2];
-                    for (int k = N - 3; k >= 0; k--) x[k] = (x[k] - u1[k] * x[k + 1] - u2[k] * x[k + 2]) * u0[k];
-                }
-                __syncwarp();
-                for (int q = c0; q < t; q++) {   // re-orthogonalise against earlier cluster members
-                    const double *zq = Z + (size_t)q * N;
-                    double dt = 0.0;
-                    for (int i = lane; i < N; i += 32) dt += x[i] * zq[i];
-                    dt = warp_sum(dt);
-                    for (int i = lane; i < N; i += 32) x[i] -= dt * zq[i];
-                    __syncwarp();
-                }
-                double nr = 0.0;
-                for (int i = lane; i < N; i += 32) nr += x[i] * x[i];
-                nr = warp_sum(nr);
-                double sc = 1.0 / sqrt(nr);
-                for (int i = lane; i < N; i += 32) x[i] *= sc;
-                __syncwarp();
-            }
-            double *zt = Z + (size_t)t * N;
-            for (int i = lane; i < N; i += 32) zt[i] = x[i];
-            __syncwarp();
+            __syncthreads();
         }
     }
-    __syncthreads();
     tm.lap(PDG_T_EIGENVECTORS);
-    // --- back-transformation z <- Q z (reflectors applied last to first), one warp per vector
+    // --- back-transformation z <- Q z with the reflectors stored in A (last to first), one warp per vector
     for (int t = w; t < kv; t += PDG_WARPS) {
-        double *zt = Z + (size_t)t * N;
+        double *zt = Z + (size_t)t * ldz;
         for (int k = N - 3; k >= 0; k--) {
-            double tau = sm.tau[k];
+            const double tau = sm.tau[k];
             if (tau == 0.0) continue;
-            int m = N - k - 1;
-            const double *hv = HV + (size_t)k * N;
+            const int m = N - k - 1;
             double dt = 0.0;
-            for (int i = lane; i < m; i += 32) dt += hv[i] * zt[k + 1 + i];
+            for (int i = lane; i < m; i += 32) dt = fma(i == 0 ? 1.0 : A[plo(k + 1 + i, k)], zt[k + 1 + i], dt);
             dt = warp_sum(dt) * tau;
-            for (int i = lane; i < m; i += 32) zt[k + 1 + i] -= dt * hv[i];
+            for (int i = lane; i < m; i += 32) zt[k + 1 + i] = fma(-dt, i == 0 ? 1.0 : A[plo(k + 1 + i, k)], zt[k + 1 + i]);
             __syncwarp();
         }
     }
@@ -426,15 +567,16 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
     // --- P = 2 Z^T Z (occupied) or 2 (1 - Z^T Z) (virtual); lower triangle then mirrored
     const bool occ = s.vec_occupied;
     double rms = 0.0;
-    block_gemm(N, N, kv, Z, 1, N, Z, N, 1, true, sm, [&](int i, int j, double v) {
+    tgemm<false, false>(N, N, kv, [&](int i, int k) { return Z[(size_t)k * ldz + i]; }, [&](int k, int j) { return Z[(size_t)k * ldz + j]; },
+                        true, sm, [&](int i, int j, double v) {
         if (j > i) return;
-        double pn = occ ? 2.0 * v : ((i == j ? 2.0 : 0.0) - 2.0 * v);
-        double dlt = pn - P[(size_t)i * N + j];
+        const double pn = occ ? 2.0 * v : ((i == j ? 2.0 : 0.0) - 2.0 * v);
+        const double dlt = pn - P[(size_t)i * N + j];
         rms += (i == j) ? dlt * dlt : 2.0 * dlt * dlt;
         P[(size_t)i * N + j] = pn;
         if (i != j) P[(size_t)j * N + i] = pn;
     });
-    double out = sqrt(block_sum(rms, sm.red)) / (double)N;
+    const double out = sqrt(block_sum(rms, sm.red)) / (double)N;
     tm.lap(PDG_T_DENSITY);
     return out;
 }
@@ -447,7 +589,7 @@ __global__ void __launch_bounds__(PDG_BLOCK, 1) k_scf(SCFArgs a)
     const FramePlan &pl = a.plan;
     const int f = blockIdx.x, tid = threadIdx.x, N = s.n_basis;
     const size_t NN = (size_t)N * N;
-    Smem sm = carve(shm, N);
+    Smem sm = carve(shm, N, s.n_vec);
     double *wsf = a.ws + (size_t)f * pl.stride;
     double *H = wsf + pl.H, *F = wsf + pl.F, *P = a.density + (size_t)f * NN;
     const double *tei = wsf + pl.tei;
@@ -490,6 +632,7 @@ __global__ void __launch_bounds__(PDG_BLOCK, 1) k_scf(SCFArgs a)
     double eold = 0.0, deltaeold = 0.0, rms = 0.0, eel = 0.0;
     __syncthreads();
     int ncyc = 0;
+    bool have_z = false;   // P is the density of the vectors in Z
     while (iteration < o.maximum_scf_cycles && !converged) {
         fock_build(a, f, H, P, F, tei, sm, &e1, &e2, &eq);
         tm.lap(PDG_T_FOCK);
@@ -512,16 +655,37 @@ __global__ void __launch_bounds__(PDG_BLOCK, 1) k_scf(SCFArgs a)
             double *hp = wsf + pl.hP + (size_t)newest * hl, *hf = wsf + pl.hF + (size_t)newest * hl, *he = wsf + pl.hE + (size_t)newest * hl;
             for (int i = tid / 32; i < N; i += PDG_WARPS)
                 for (int j = tid % 32; j <= i; j += 32) { hp[i * (i + 1) / 2 + j] = P[(size_t)i * N + j]; hf[i * (i + 1) / 2 + j] = F[(size_t)i * N + j]; }
-            double *FP = wsf + pl.A;
-            block_gemm(N, N, N, F, N, 1, P, N, 1, false, sm, [&](int i, int j, double v) { FP[(size_t)i * N + j] = v; });
             double emx = 0.0;
-            for (int i = tid / 32; i < N; i += PDG_WARPS)
-                for (int j = tid % 32; j < i; j += 32) {
-                    double ev = FP[(size_t)i * N + j] - FP[(size_t)j * N + i];
-                    he[i * (i - 1) / 2 + j] = ev;
-                    emx = fmax(emx, fabs(ev));
-                }
-            __syncthreads();
+            if (have_z) {
+                // P = 2 Z^T Z (occupied) or 2 (1 - Z^T Z) (virtual) with the vectors Z of the last density step,
+                // so with G = Z F:  F P - P F = sg (G^T Z - Z^T G), sg = +2 / -2.  2 N^2 kv FMA instead of N^3.
+                const double *Zc = sm.zs ? sm.zs : wsf + pl.Z;
+                const int ldz = sm.ldz, kv = s.n_vec;
+                const double sg = s.vec_occupied ? 2.0 : -2.0;
+                double *G = wsf + pl.G;
+                tgemm<true, false>(kv, N, N, [&](int t, int k) { return Zc[(size_t)t * ldz + k]; }, [&](int k, int i) { return F[(size_t)k * N + i]; },
+                                   false, sm, [&](int t, int i, double v) { G[(size_t)t * N + i] = v; });
+                tgemm<false, false>(N, N, 2 * kv,
+                    [&](int i, int k) { return k < kv ? G[(size_t)k * N + i] : Zc[(size_t)(k - kv) * ldz + i]; },
+                    [&](int k, int j) { return k < kv ? Zc[(size_t)k * ldz + j] : -G[(size_t)(k - kv) * N + j]; },
+                    true, sm, [&](int i, int j, double v) {
+                        if (j >= i) return;
+                        const double ev = sg * v;
+                        he[i * (i - 1) / 2 + j] = ev;
+                        emx = fmax(emx, fabs(ev));
+                    });
+            } else {
+                double *FP = wsf + pl.A;
+                tgemm<true, false>(N, N, N, [&](int i, int k) { return F[(size_t)i * N + k]; }, [&](int k, int j) { return P[(size_t)k * N + j]; },
+                                   false, sm, [&](int i, int j, double v) { FP[(size_t)i * N + j] = v; });
+                for (int i = tid / 32; i < N; i += PDG_WARPS)
+                    for (int j = tid % 32; j < i; j += 32) {
+                        const double ev = FP[(size_t)i * N + j] - FP[(size_t)j * N + i];
+                        he[i * (i - 1) / 2 + j] = ev;
+                        emx = fmax(emx, fabs(ev));
+                    }
+                __syncthreads();
+            }
             double maxerr = block_max(emx, sm.red);
             double dots[PDG_MAX_HISTORY];
             for (int m = 0; m < PDG_MAX_HISTORY; m++) dots[m] = 0.0;
@@ -619,6 +783,7 @@ __global__ void __launch_bounds__(PDG_BLOCK, 1) k_scf(SCFArgs a)
         tm.lap(PDG_T_ITERATE);
         rms = density_step(a, wsf, F, P, sm, tm);
         valid = true;
+        have_z = true;
     }
     if (converged) st = PDG_OK;
     if (tid == 0) {
@@ -631,7 +796,7 @@ __global__ void __launch_bounds__(PDG_BLOCK, 1) k_scf(SCFArgs a)
     }
 }
 
-size_t scf_smem_bytes(int N) { return sizeof(double) * (32 + 2 * TILE * KCH + 256 + 7 * (size_t)N) + sizeof(int) * (64 + (size_t)N + 2); }
+size_t scf_smem_bytes(int N, int kv) { return smem_plan(N, kv).bytes; }
 
 void launch_scf(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *phi, const pdg_scf_options &o,
                 double *density, int use_density, double *energies, double *charges, int *status, int *ncycles,
@@ -641,7 +806,7 @@ void launch_scf(const DeviceSystem &s, const FramePlan &p, int n_frames, const d
     a.s = s; a.plan = p; a.n_frames = n_frames; a.phi = phi; a.o = o; a.density = density; a.use_density = use_density;
     a.energies = energies; a.charges = charges; a.status = status; a.ncycles = ncycles; a.ws = ws;
     a.fock_only = fock_only; a.fock_out = fock_out;
-    size_t sm = scf_smem_bytes(s.n_basis);
+    size_t sm = scf_smem_bytes(s.n_basis, s.n_vec);
     static size_t configured = 0;
     if (sm > 48 * 1024 && sm > configured) {
         cudaFuncSetAttribute(k_scf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
