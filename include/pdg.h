@@ -132,6 +132,22 @@ int pdg_fock(pdg_system *sys, int n_frames, const double *d_xyz, const double *d
 int pdg_gradients(pdg_system *sys, int n_frames, const double *d_xyz, const double *d_density,
                   double *d_gradients, void *d_workspace, size_t workspace_bytes, void *stream);
 
+/* pdg_gradients without a workspace: the same gradients (Eh/Bohr) for given densities, with the
+ * scratch held in the library itself, so the call allocates no device memory.  For callers that may
+ * not allocate at call time: an MD or Monte Carlo inner step that must not synchronise the device
+ * (cudaMalloc and cudaFree can), or a host application whose own allocator already owns the device
+ * memory and gives the library none.  No counterpart in the reference (QCModelMNDO_Gradients,
+ * QCModelMNDO.c:732, needs no scratch on the CPU).
+ *   - Limit: n_frames * n_pairs * 3 <= 524288 doubles (4 MiB; e.g. 65 atoms = 2080 pairs: 84 frames);
+ *     larger requests return PDG_TOO_LARGE with the sizes in pdg_last_error().
+ *   - The scratch is one buffer per device: calls that overlap in time on the same device (two streams,
+ *     or two host threads) race on it and give wrong gradients; serialise them.
+ *   - The first call on each device looks the buffer's address up (cudaGetSymbolAddress, with that
+ *     device current); make that first call before any stream capture.
+ *   - Nothing in the scratch has to start at zero: every element read is written first in the call. */
+int pdg_gradients_static_scratch(pdg_system *sys, int n_frames, const double *d_xyz, const double *d_density,
+                                 double *d_gradients, void *stream);
+
 /* Per-phase SCF timings of the last pdg_energy_gradients call that used this workspace: for every frame
  * PDG_NTIMERS GPU clock-cycle counts (clock64 of the frame's CTA), the device counterpart of the phase
  * timings of pMolecule.QCModel.pyx:208-275 (EnergyWithTimings: QC Fock, QC Converger Iterate,

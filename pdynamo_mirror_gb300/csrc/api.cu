@@ -1,6 +1,7 @@
 // api.cu - the extern "C" boundary of libpdg.so (declared in include/pdg.h).
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -240,4 +241,50 @@ extern "C" int pdg_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, c
     if (model == 1 && (n_knots < 2 || !knots || cutoff <= 0.0)) return fail(PDG_BAD_ARGUMENT, "ABFS needs spline knots and a cutoff");
     launch_qcmm_gradients(model, n_frames, n_qc, n_mm, qc, mm, q, qcq, n_knots, knots, cutoff, gqc, gmm, (cudaStream_t)stream);
     return cuda_check(cudaGetLastError(), "qcmm gradients");
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Gradients with library-owned scratch: pdg_gradients without a caller workspace and without any device
+// allocation at call time, for callers that may not allocate (declared in include/pdg.h).  The scratch
+// is a file-scope device array; every device has its own instance, whose address is looked up once per
+// device and cached.  It holds the per-pair gradient terms, n_frames * n_pairs * 3 doubles; each element
+// the reduction reads is written earlier in the same call, so nothing needs to start at zero.
+#define PDG_STATIC_SCRATCH_DOUBLES (512 * 1024)
+#define PDG_STATIC_MAX_DEVICES 64
+static __device__ __align__(256) double g_static_scratch[PDG_STATIC_SCRATCH_DOUBLES];
+static std::mutex g_static_mutex;
+static double *g_static_ptr[PDG_STATIC_MAX_DEVICES] = {};
+
+extern "C" int pdg_gradients_static_scratch(pdg_system *s, int n_frames, const double *d_xyz, const double *d_density,
+                                            double *d_gradients, void *stream)
+{
+    if (!s) return fail(PDG_BAD_ARGUMENT, "null system");
+    if (n_frames <= 0) return fail(PDG_BAD_ARGUMENT, "n_frames must be positive");
+    if (!d_xyz || !d_density || !d_gradients) return fail(PDG_BAD_ARGUMENT, "null argument");
+    FramePlan p = {};
+    p.pair_g = 0;
+    p.stride = align32((size_t)s->d.n_pairs * 3);
+    const size_t need = p.stride * (size_t)n_frames;
+    if (need > PDG_STATIC_SCRATCH_DOUBLES)
+        return fail(PDG_TOO_LARGE, "pdg_gradients_static_scratch: " + std::to_string(n_frames) + " frames of " +
+                                       std::to_string(s->d.n_pairs) + " atom pairs need " + std::to_string(need) +
+                                       " doubles of scratch, more than the " + std::to_string(PDG_STATIC_SCRATCH_DOUBLES) +
+                                       " compiled in; use pdg_gradients with a workspace");
+    int dev = 0, rc;
+    if ((rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice"))) return rc;
+    if (dev < 0 || dev >= PDG_STATIC_MAX_DEVICES) return fail(PDG_TOO_LARGE, "device ordinal beyond 63");
+    double *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_static_mutex);
+        if (!g_static_ptr[dev]) {
+            void *ptr = nullptr;
+            if ((rc = cuda_check(cudaGetSymbolAddress(&ptr, g_static_scratch), "cudaGetSymbolAddress (static scratch)"))) return rc;
+            g_static_ptr[dev] = (double *)ptr;
+        }
+        scratch = g_static_ptr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    launch_pair_gradients(s->d, p, n_frames, d_xyz, d_density, scratch, st);
+    launch_reduce_gradients(s->d, p, n_frames, scratch, d_gradients, st);
+    return cuda_check(cudaGetLastError(), "gradient kernels (static scratch)");
 }

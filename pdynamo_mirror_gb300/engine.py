@@ -151,3 +151,14 @@ class QCEngine:
                                            _native.ptr(ws), ws.numel(), _native.stream_handle(torch.cuda.current_stream(self.device))),
                       "pdg_gradients")
         return g
+
+    def gradients_static_scratch(self, qc_xyz, density):
+        """Gradients for given densities through pdg_gradients_static_scratch (no workspace, no allocation
+        inside the library)."""
+        F = qc_xyz.shape[0]
+        g = torch.empty((F, self.n_atoms, 3), dtype=torch.float64, device=self.device)
+        xyz_bohr = (qc_xyz * ANGSTROMS_TO_BOHRS).contiguous()
+        _native.check(self.L.pdg_gradients_static_scratch(self.handle, F, _native.ptr(xyz_bohr), _native.ptr(density.contiguous()),
+                                                          _native.ptr(g), _native.stream_handle(torch.cuda.current_stream(self.device))),
+                      "pdg_gradients_static_scratch")
+        return g
