@@ -45,29 +45,82 @@ __device__ __forceinline__ bool pair_term(int model, const Spline &sp, double r2
     return true;
 }
 
-#define QB 256
+// GB300 runs FP64 at one warp instruction per ~64 cycles per sub-partition whatever the active lanes, so
+// the FP32 cutoff test runs on FP32 copies of the MM coordinates staged in shared memory, and the pairs that
+// pass are queued per warp and evaluated in FP64 thirty-two at a time: only ~6 % of the QC x MM pairs of a
+// 12 A cutoff in a 50 A box are inside, and no warp runs the spline for one lane.  The queue keeps the scan
+// order, so every sum is taken in a fixed order (deterministic).
+#define QW 8              // QC atoms per block, one warp each
+#define QB (QW * 32)
+#define MCH 1024          // MM atoms staged per chunk
+
+__device__ __forceinline__ float cutoff_r2(int model, const Spline &sp)
+{
+    return model == 1 ? (float)(sp.r2off * (1.0 + 1.0e-4)) + 1.0e-3f : __int_as_float(0x7f800000);
+}
+
+// Scan this frame's MM atoms for the warp's QC atom; call body(m) for every MM atom that passes the FP32
+// test, on all 32 lanes at once (lane k handles queue entry k), then on the final partial batch.
+template <typename Body>
+__device__ __forceinline__ void scan_mm(int n_mm, const double *__restrict__ xm, float fax, float fay, float faz, float r2cut,
+                                        bool live, float4 *sxm, int *queue, Body body)
+{
+    const int lane = threadIdx.x & 31;
+    int qn = 0;
+    for (int c0 = 0; c0 < n_mm; c0 += MCH) {
+        const int cn = min(MCH, n_mm - c0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cn; k += QB) {
+            const double *p = xm + 3 * (size_t)(c0 + k);
+            sxm[k] = make_float4((float)p[0], (float)p[1], (float)p[2], 0.0f);
+        }
+        __syncthreads();
+        if (!live) continue;
+        for (int k0 = 0; k0 < cn; k0 += 32) {
+            const int k = k0 + lane;
+            bool in = false;
+            if (k < cn) {
+                const float4 p = sxm[k];
+                const float dx = fax - p.x, dy = fay - p.y, dz = faz - p.z;
+                in = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= r2cut;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, in);
+            if (in) queue[qn + __popc(bal & ((1u << lane) - 1u))] = c0 + k;
+            qn += __popc(bal);
+            __syncwarp();
+            if (qn >= 32) {
+                body(queue[lane]);
+                const int rest = qn - 32;
+                const int carry = lane < rest ? queue[32 + lane] : 0;
+                __syncwarp();
+                if (lane < rest) queue[lane] = carry;
+                __syncwarp();
+                qn = rest;
+            }
+        }
+    }
+    if (live && lane < qn) body(queue[lane]);
+}
 
 __global__ void __launch_bounds__(QB) k_qcmm_potentials(int model, Spline sp, int n_qc, int n_mm, const double *__restrict__ qc,
                                                         const double *__restrict__ mm, const double *__restrict__ q, double *__restrict__ phi)
 {
-    __shared__ double red[QB / 32];
-    int f = blockIdx.x / n_qc, A = blockIdx.x % n_qc;
-    const double *xa = qc + ((size_t)f * n_qc + A) * 3;
+    __shared__ float4 sxm[MCH];
+    __shared__ int queue[QW][64];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, groups = (n_qc + QW - 1) / QW;
+    const int f = blockIdx.x / groups, A = (blockIdx.x % groups) * QW + w;
+    const bool live = A < n_qc;
     const double *xm = mm + (size_t)f * n_mm * 3;
-    double ax = xa[0], ay = xa[1], az = xa[2];
-    float r2cut = (float)(sp.r2off * (1.0 + 1.0e-4)) + 1.0e-3f;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    if (live) { const double *xa = qc + ((size_t)f * n_qc + A) * 3; ax = xa[0]; ay = xa[1]; az = xa[2]; }
     double pot = 0.0;
-    for (int m = threadIdx.x; m < n_mm; m += QB) {
-        double dx = ax - xm[3 * m], dy = ay - xm[3 * m + 1], dz = az - xm[3 * m + 2];
-        if (model == 1) {
-            float fx = (float)dx, fy = (float)dy, fz = (float)dz;
-            if (fx * fx + fy * fy + fz * fz > r2cut) continue;
-        }
+    scan_mm(n_mm, xm, (float)ax, (float)ay, (float)az, cutoff_r2(model, sp), live, sxm, queue[w], [&](int m) {
+        const double dx = ax - xm[3 * m], dy = ay - xm[3 * m + 1], dz = az - xm[3 * m + 2];
         double fv;
         if (pair_term(model, sp, dx * dx + dy * dy + dz * dz, &fv, nullptr)) pot += q[m] * fv;
-    }
-    double t = block_sum(pot, red);
-    if (threadIdx.x == 0) phi[(size_t)f * n_qc + A] = t;
+    });
+    pot = warp_sum(pot);
+    if (live && lane == 0) phi[(size_t)f * n_qc + A] = pot;
 }
 
 // dE/dx_A = sum_m 2 q_A q_m f'(r^2) (x_A - x_m), converted from per-A to per-Bohr.
@@ -75,60 +128,81 @@ __global__ void __launch_bounds__(QB) k_qcmm_grad_qc(int model, Spline sp, int n
                                                      const double *__restrict__ mm, const double *__restrict__ q,
                                                      const double *__restrict__ qcq, double *__restrict__ gqc)
 {
-    __shared__ double red[QB / 32];
-    int f = blockIdx.x / n_qc, A = blockIdx.x % n_qc;
-    const double *xa = qc + ((size_t)f * n_qc + A) * 3;
+    __shared__ float4 sxm[MCH];
+    __shared__ int queue[QW][64];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, groups = (n_qc + QW - 1) / QW;
+    const int f = blockIdx.x / groups, A = (blockIdx.x % groups) * QW + w;
+    const bool live = A < n_qc;
     const double *xm = mm + (size_t)f * n_mm * 3;
-    double ax = xa[0], ay = xa[1], az = xa[2], qa = qcq[(size_t)f * n_qc + A];
-    float r2cut = (float)(sp.r2off * (1.0 + 1.0e-4)) + 1.0e-3f;
-    double g[3] = { 0, 0, 0 };
-    for (int m = threadIdx.x; m < n_mm; m += QB) {
-        double dx = ax - xm[3 * m], dy = ay - xm[3 * m + 1], dz = az - xm[3 * m + 2];
-        if (model == 1) {
-            float fx = (float)dx, fy = (float)dy, fz = (float)dz;
-            if (fx * fx + fy * fy + fz * fz > r2cut) continue;
-        }
+    double ax = 0.0, ay = 0.0, az = 0.0, qa = 0.0;
+    if (live) { const double *xa = qc + ((size_t)f * n_qc + A) * 3; ax = xa[0]; ay = xa[1]; az = xa[2]; qa = qcq[(size_t)f * n_qc + A]; }
+    double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+    scan_mm(n_mm, xm, (float)ax, (float)ay, (float)az, cutoff_r2(model, sp), live, sxm, queue[w], [&](int m) {
+        const double dx = ax - xm[3 * m], dy = ay - xm[3 * m + 1], dz = az - xm[3 * m + 2];
         double fv, gv;
-        if (!pair_term(model, sp, dx * dx + dy * dy + dz * dz, &fv, &gv)) continue;
-        double s = 2.0 * qa * q[m] * gv / PDG_ANGSTROMS_TO_BOHRS;
-        g[0] += s * dx; g[1] += s * dy; g[2] += s * dz;
-    }
-    for (int k = 0; k < 3; k++) {
-        double t = block_sum(g[k], red);
-        if (threadIdx.x == 0) gqc[((size_t)f * n_qc + A) * 3 + k] = t;
-    }
+        if (!pair_term(model, sp, dx * dx + dy * dy + dz * dz, &fv, &gv)) return;
+        const double s = 2.0 * qa * q[m] * gv / PDG_ANGSTROMS_TO_BOHRS;
+        g0 += s * dx; g1 += s * dy; g2 += s * dz;
+    });
+    g0 = warp_sum(g0); g1 = warp_sum(g1); g2 = warp_sum(g2);
+    if (live && lane == 0) { double *o = gqc + ((size_t)f * n_qc + A) * 3; o[0] = g0; o[1] = g1; o[2] = g2; }
 }
 
-__global__ void __launch_bounds__(QB) k_qcmm_grad_mm(int model, Spline sp, int n_qc, int n_mm, const double *__restrict__ qc,
+// MM side: a block takes 256 MM atoms of one frame.  An FP32 pass marks the atoms within the cutoff of any
+// QC atom and packs them (block prefix in atom order); the packed atoms then run the FP64 loop over the QC
+// atoms one per thread, and the others get zero.
+#define MB 256
+__global__ void __launch_bounds__(MB) k_qcmm_grad_mm(int model, Spline sp, int n_qc, int n_mm, const double *__restrict__ qc,
                                                      const double *__restrict__ mm, const double *__restrict__ q,
                                                      const double *__restrict__ qcq, double *__restrict__ gmm)
 {
-    extern __shared__ double sq[];   // QC coordinates and charges of this frame
-    int blocks_per_frame = (n_mm + QB - 1) / QB;
-    int f = blockIdx.x / blocks_per_frame, m = (blockIdx.x % blocks_per_frame) * QB + threadIdx.x;
-    for (int k = threadIdx.x; k < n_qc; k += QB) {
-        sq[4 * k] = qc[((size_t)f * n_qc + k) * 3]; sq[4 * k + 1] = qc[((size_t)f * n_qc + k) * 3 + 1];
-        sq[4 * k + 2] = qc[((size_t)f * n_qc + k) * 3 + 2]; sq[4 * k + 3] = qcq[(size_t)f * n_qc + k];
+    extern __shared__ double sq[];   // QC atoms: x, y, z, charge (doubles), then x, y, z (floats)
+    __shared__ int wcount[MB / 32], near_list[MB];
+    float *sf = (float *)(sq + 4 * (size_t)n_qc);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int blocks_per_frame = (n_mm + MB - 1) / MB;
+    const int f = blockIdx.x / blocks_per_frame, m = (blockIdx.x % blocks_per_frame) * MB + threadIdx.x;
+    for (int k = threadIdx.x; k < n_qc; k += MB) {
+        const double *x = qc + ((size_t)f * n_qc + k) * 3;
+        sq[4 * k] = x[0]; sq[4 * k + 1] = x[1]; sq[4 * k + 2] = x[2]; sq[4 * k + 3] = qcq[(size_t)f * n_qc + k];
+        sf[3 * k] = (float)x[0]; sf[3 * k + 1] = (float)x[1]; sf[3 * k + 2] = (float)x[2];
     }
     __syncthreads();
-    if (m >= n_mm) return;
-    const double *xm = mm + ((size_t)f * n_mm + m) * 3;
-    double mx = xm[0], my = xm[1], mz = xm[2], qm = q[m];
-    float r2cut = (float)(sp.r2off * (1.0 + 1.0e-4)) + 1.0e-3f;
-    double g[3] = { 0, 0, 0 };
-    for (int A = 0; A < n_qc; A++) {
-        double dx = sq[4 * A] - mx, dy = sq[4 * A + 1] - my, dz = sq[4 * A + 2] - mz;
-        if (model == 1) {
-            float fx = (float)dx, fy = (float)dy, fz = (float)dz;
-            if (fx * fx + fy * fy + fz * fz > r2cut) continue;
+    const float r2cut = cutoff_r2(model, sp);
+    bool near = false;
+    if (m < n_mm) {
+        const double *xm = mm + ((size_t)f * n_mm + m) * 3;
+        const float fx = (float)xm[0], fy = (float)xm[1], fz = (float)xm[2];
+        for (int A = 0; A < n_qc && !near; A++) {
+            const float dx = sf[3 * A] - fx, dy = sf[3 * A + 1] - fy, dz = sf[3 * A + 2] - fz;
+            near = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= r2cut;
         }
+        if (!near) { double *o = gmm + ((size_t)f * n_mm + m) * 3; o[0] = 0.0; o[1] = 0.0; o[2] = 0.0; }
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, near);
+    if (lane == 0) wcount[w] = __popc(bal);
+    __syncthreads();
+    int off = 0, total = 0;
+    for (int k = 0; k < MB / 32; k++) { if (k < w) off += wcount[k]; total += wcount[k]; }
+    if (near) near_list[off + __popc(bal & ((1u << lane) - 1u))] = m;
+    __syncthreads();
+    if (threadIdx.x >= total) return;
+    const int mi = near_list[threadIdx.x];
+    const double *xm = mm + ((size_t)f * n_mm + mi) * 3;
+    const double mx = xm[0], my = xm[1], mz = xm[2], qm = q[mi];
+    const float fx = (float)mx, fy = (float)my, fz = (float)mz;
+    double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+    for (int A = 0; A < n_qc; A++) {
+        const float ex = sf[3 * A] - fx, ey = sf[3 * A + 1] - fy, ez = sf[3 * A + 2] - fz;
+        if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > r2cut) continue;
+        const double dx = sq[4 * A] - mx, dy = sq[4 * A + 1] - my, dz = sq[4 * A + 2] - mz;
         double fv, gv;
         if (!pair_term(model, sp, dx * dx + dy * dy + dz * dz, &fv, &gv)) continue;
-        double s = 2.0 * sq[4 * A + 3] * qm * gv / PDG_ANGSTROMS_TO_BOHRS;
-        g[0] -= s * dx; g[1] -= s * dy; g[2] -= s * dz;
+        const double s = 2.0 * sq[4 * A + 3] * qm * gv / PDG_ANGSTROMS_TO_BOHRS;
+        g0 -= s * dx; g1 -= s * dy; g2 -= s * dz;
     }
-    double *o = gmm + ((size_t)f * n_mm + m) * 3;
-    o[0] = g[0]; o[1] = g[1]; o[2] = g[2];
+    double *o = gmm + ((size_t)f * n_mm + mi) * 3;
+    o[0] = g0; o[1] = g1; o[2] = g2;
 }
 
 static Spline make_spline(int n, const double *knots, double cutoff)
@@ -144,7 +218,8 @@ int launch_qcmm_potentials(int model, int n_frames, int n_qc, int n_mm, const do
 {
     if (n_frames <= 0 || n_qc <= 0) return 0;
     Spline sp = make_spline(n_knots, knots, cutoff);
-    k_qcmm_potentials<<<n_frames * n_qc, QB, 0, st>>>(model, sp, n_qc, n_mm, qc, mm, q, phi);
+    const int groups = (n_qc + QW - 1) / QW;
+    k_qcmm_potentials<<<n_frames * groups, QB, 0, st>>>(model, sp, n_qc, n_mm, qc, mm, q, phi);
     return 0;
 }
 
@@ -154,12 +229,13 @@ int launch_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const dou
 {
     if (n_frames <= 0 || n_qc <= 0) return 0;
     Spline sp = make_spline(n_knots, knots, cutoff);
-    k_qcmm_grad_qc<<<n_frames * n_qc, QB, 0, st>>>(model, sp, n_qc, n_mm, qc, mm, q, qcq, gqc);
+    const int groups = (n_qc + QW - 1) / QW;
+    k_qcmm_grad_qc<<<n_frames * groups, QB, 0, st>>>(model, sp, n_qc, n_mm, qc, mm, q, qcq, gqc);
     if (n_mm > 0) {
-        int bpf = (n_mm + QB - 1) / QB;
-        size_t sm = sizeof(double) * 4 * (size_t)n_qc;
+        const int bpf = (n_mm + MB - 1) / MB;
+        const size_t sm = sizeof(double) * 4 * (size_t)n_qc + sizeof(float) * 3 * (size_t)n_qc;
         if (sm > 48 * 1024) cudaFuncSetAttribute(k_qcmm_grad_mm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k_qcmm_grad_mm<<<n_frames * bpf, QB, sm, st>>>(model, sp, n_qc, n_mm, qc, mm, q, qcq, gmm);
+        k_qcmm_grad_mm<<<n_frames * bpf, MB, sm, st>>>(model, sp, n_qc, n_mm, qc, mm, q, qcq, gmm);
     }
     return 0;
 }
