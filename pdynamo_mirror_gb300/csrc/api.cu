@@ -7,6 +7,7 @@
 
 #include "common.cuh"
 #include "multipole.cuh"
+#include "overlap.cuh"
 
 static thread_local std::string g_error;
 
@@ -27,7 +28,7 @@ struct pdg_system {
     std::vector<double> elements;
     int charge;
     // device allocations owned by the system (tables only; no per-frame data)
-    double *d_elements = nullptr, *d_terms = nullptr;
+    double *d_elements = nullptr, *d_terms = nullptr, *d_ovl = nullptr;
     int *d_ints = nullptr;
 };
 
@@ -70,6 +71,17 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
             double *o = &terms[(size_t)(a * n_elements + b) * 2 * MP_NTERMS];
             multipole_terms(h_elements + a * PDG_ELEMENT_STRIDE, h_elements + b * PDG_ELEMENT_STRIDE, o, o + MP_NTERMS);
         }
+    // overlap primitive records per ordered element pair
+    std::vector<double> ovl;
+    std::vector<int> ovl_off(n_elements * n_elements), ovl_n(n_elements * n_elements);
+    for (int a = 0; a < n_elements; a++)
+        for (int b = 0; b < n_elements; b++) {
+            const size_t before = ovl.size() / OV_REC;
+            overlap_records(h_elements + a * PDG_ELEMENT_STRIDE, h_elements + b * PDG_ELEMENT_STRIDE, ovl);
+            ovl_off[a * n_elements + b] = (int)before;
+            ovl_n[a * n_elements + b] = (int)(ovl.size() / OV_REC - before);
+        }
+    if (ovl.empty()) ovl.assign(OV_REC, 0.0);
     pdg_system *s = new pdg_system();
     s->elements.assign(h_elements, h_elements + (size_t)n_elements * PDG_ELEMENT_STRIDE);
     s->charge = charge;
@@ -80,10 +92,14 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     ints.insert(ints.end(), pi.begin(), pi.end());
     ints.insert(ints.end(), pj.begin(), pj.end());
     ints.insert(ints.end(), pt.begin(), pt.end());
+    ints.insert(ints.end(), ovl_off.begin(), ovl_off.end());
+    ints.insert(ints.end(), ovl_n.begin(), ovl_n.end());
     int rc = PDG_OK;
     if ((rc = cuda_check(cudaMalloc(&s->d_elements, sizeof(double) * s->elements.size()), "cudaMalloc elements")) ||
         (rc = cuda_check(cudaMalloc(&s->d_terms, sizeof(double) * terms.size()), "cudaMalloc terms")) ||
         (rc = cuda_check(cudaMalloc(&s->d_ints, sizeof(int) * ints.size()), "cudaMalloc tables")) ||
+        (rc = cuda_check(cudaMalloc(&s->d_ovl, sizeof(double) * ovl.size()), "cudaMalloc overlap records")) ||
+        (rc = cuda_check(cudaMemcpy(s->d_ovl, ovl.data(), sizeof(double) * ovl.size(), cudaMemcpyHostToDevice), "copy overlap records")) ||
         (rc = cuda_check(cudaMemcpy(s->d_elements, s->elements.data(), sizeof(double) * s->elements.size(), cudaMemcpyHostToDevice), "copy elements")) ||
         (rc = cuda_check(cudaMemcpy(s->d_terms, terms.data(), sizeof(double) * terms.size(), cudaMemcpyHostToDevice), "copy terms")) ||
         (rc = cuda_check(cudaMemcpy(s->d_ints, ints.data(), sizeof(int) * ints.size(), cudaMemcpyHostToDevice), "copy tables"))) {
@@ -99,6 +115,7 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     const int *b = s->d_ints;
     d.atom_elem = b; d.atom_start = b + n_atoms; d.atom_norb = b + 2 * n_atoms;
     d.pair_i = b + 3 * n_atoms; d.pair_j = d.pair_i + npairs; d.pair_tei = d.pair_j + npairs;
+    d.ovl = s->d_ovl; d.ovl_off = d.pair_tei + npairs; d.ovl_n = d.ovl_off + n_elements * n_elements;
     *out = s;
     return PDG_OK;
 }
@@ -106,7 +123,7 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
 extern "C" int pdg_system_destroy(pdg_system *s)
 {
     if (!s) return PDG_OK;
-    cudaFree(s->d_elements); cudaFree(s->d_terms); cudaFree(s->d_ints);
+    cudaFree(s->d_elements); cudaFree(s->d_terms); cudaFree(s->d_ints); cudaFree(s->d_ovl);
     delete s;
     return PDG_OK;
 }

@@ -25,6 +25,8 @@ struct DeviceSystem {
     const int *atom_elem, *atom_start, *atom_norb;
     const int *pair_i, *pair_j, *pair_tei;   // n_pairs
     const double *terms;           // multipole (o, a) tables per ordered element pair (multipole.cuh)
+    const double *ovl;             // overlap primitive records (overlap.cuh), all ordered element pairs
+    const int *ovl_off, *ovl_n;    // per ordered element pair: first record, record count
 };
 
 // Per-frame workspace plan (all offsets in doubles from the frame's base).

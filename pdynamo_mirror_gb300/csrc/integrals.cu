@@ -1,20 +1,21 @@
 // integrals.cu - per-atom-pair integral and gradient kernels (FP64).
 //
-// k_pair_integrals   one warp per (frame, atom pair i > j): local-frame multipole TEIs and electron-core
-//                    terms (multipole.cuh), rotation to the molecular frame, STO-6G overlap -> resonance
-//                    block of H, core-core energy.  Replaces the pair body of QCModelMNDO_Integrals
+// k_pair_integrals   one warp per batch of 32 atom pairs (i > j) of a frame: core-core energy and the
+//                    rotation's direction cosines one thread per pair, then per pair across the lanes:
+//                    local-frame multipole TEIs and electron-core terms (multipole.cuh), rotation to the
+//                    molecular frame, STO-6G overlap (overlap.cuh) -> resonance block of H.  Replaces the pair body of QCModelMNDO_Integrals
 //                    (QCModelMNDO.c:1062-1112) with MNDOIntegrals_MolecularFrame2CIntegrals (MNDOIntegrals.c:147).
 // k_assemble_h       one warp per (frame, atom): diagonal blocks of H = U + sum of electron-core terms.
-// k_pair_gradients   one warp per (frame, atom pair): dE/dR of the pair (QCModelMNDO_Gradients,
+// k_pair_gradients   one warp per batch of 32 atom pairs, laid out as k_pair_integrals: dE/dR of the pair (QCModelMNDO_Gradients,
 //                    QCModelMNDO.c:732-840 with MNDOIntegrals_MolecularFrame2CIntegralsD, MNDOIntegrals.c:274,
 //                    and QCModelMNDOState_GetGradientDensityTerms, QCModelMNDOState.c:178).
 // k_reduce_gradients one warp per (frame, atom): sums the pair terms in a fixed order (deterministic).
 #include "common.cuh"
 #include "multipole.cuh"
+#include "overlap.cuh"
 
 #define PI_D 3.14159265358979323846
 #define EXPONENT_TOLERANCE 25.0
-#define PRIMITIVE_OVERLAP_TOLERANCE (2.30258509299405 * 18.0)
 
 // Core-core repulsion and d/dr, non-diatomic branch (MNDOIntegralUtilities.c:35-150, :152-281).
 __device__ double core_core(const double *a, const double *b, double r, double *dedr)
@@ -73,66 +74,26 @@ __device__ double core_core(const double *a, const double *b, double r, double *
     return enuc + scale;
 }
 
-// STO-6G overlap of the shells of atoms i and j (orbital order s, pz, px, py) and, optionally, its
-// derivative with respect to atom i (GaussianBasis_2Overlap / _2OverlapD, GaussianBasisCore.c:469,570).
-// Each lane takes every 32nd primitive pair; results are warp-reduced into S[16] and SD[48].
-__device__ void pair_overlap(const double *Ei, const double *Ej, double abx, double aby, double abz,
-                             bool derivs, int lane, double *S, double *SD)
-{
-    const int ORB[3] = { 2, 3, 1 };
-    double s[16], sd[48];
-    for (int k = 0; k < 16; k++) s[k] = 0.0;
-    if (derivs) for (int k = 0; k < 48; k++) sd[k] = 0.0;
-    double AB[3] = { abx, aby, abz }, R2 = abx * abx + aby * aby + abz * abz;
-    int nsi = (int)Ei[PDG_E_NSHELL], nsj = (int)Ej[PDG_E_NSHELL];
-    int npi[2] = { (int)Ei[PDG_E_NPRIM_S], (int)Ei[PDG_E_NPRIM_P] }, npj[2] = { (int)Ej[PDG_E_NPRIM_S], (int)Ej[PDG_E_NPRIM_P] };
-    int base = 0;
-    for (int sa = 0; sa < nsi; sa++)
-        for (int sb = 0; sb < nsj; sb++) {
-            int n = npi[sa] * npj[sb];
-            for (int t = lane - base % 32 < 0 ? lane - base % 32 + 32 : lane - base % 32; t < n; t += 32) {
-                int p = t / npj[sb], q = t % npj[sb];
-                double a = Ei[(sa ? PDG_E_EXP_P : PDG_E_EXP_S) + p], b = Ej[(sb ? PDG_E_EXP_P : PDG_E_EXP_S) + q], g = a + b;
-                double fac = a * b * R2 / g;
-                if (fac > PRIMITIVE_OVERLAP_TOLERANCE) continue;
-                double tg = PI_D / g;
-                double s0 = Ei[(sa ? PDG_E_CCBF_P : PDG_E_CCBF_S) + p] * Ej[(sb ? PDG_E_CCBF_P : PDG_E_CCBF_S) + q] * tg * sqrt(tg) * exp(-fac);
-                double PA[3], PB[3], h = 0.5 / g;
-                for (int k = 0; k < 3; k++) { PA[k] = b / g * AB[k]; PB[k] = -a / g * AB[k]; }
-                if (sa == 0 && sb == 0) {
-                    s[0] += s0;
-                    if (derivs) for (int k = 0; k < 3; k++) sd[k * 16] += 2.0 * a * PA[k] * s0;
-                } else if (sa == 1 && sb == 0) {
-                    for (int i = 0; i < 3; i++) {
-                        s[ORB[i] * 4] += PA[i] * s0;
-                        if (derivs) for (int k = 0; k < 3; k++) sd[k * 16 + ORB[i] * 4] += (2.0 * a * (PA[i] * PA[k] + (i == k) * h) - (i == k)) * s0;
-                    }
-                } else if (sa == 0 && sb == 1) {
-                    for (int j = 0; j < 3; j++) {
-                        s[ORB[j]] += PB[j] * s0;
-                        if (derivs) for (int k = 0; k < 3; k++) sd[k * 16 + ORB[j]] += 2.0 * a * (PA[k] * PB[j] + (k == j) * h) * s0;
-                    }
-                } else {
-                    for (int i = 0; i < 3; i++)
-                        for (int j = 0; j < 3; j++) {
-                            s[ORB[i] * 4 + ORB[j]] += (PA[i] * PB[j] + (i == j) * h) * s0;
-                            if (derivs)
-                                for (int k = 0; k < 3; k++) {
-                                    double dpp = PA[i] * PA[k] * PB[j] + ((i == k) * PB[j] + (i == j) * PA[k] + (k == j) * PA[i]) * h;
-                                    sd[k * 16 + ORB[i] * 4 + ORB[j]] += (2.0 * a * dpp - (i == k) * PB[j]) * s0;
-                                }
-                        }
-                }
-            }
-            base += n;
-        }
-    for (int k = 0; k < 16; k++) S[k] = warp_sum(s[k]);
-    if (derivs) for (int k = 0; k < 48; k++) SD[k] = warp_sum(sd[k]);
-}
-
 // Warp-private shared scratch (doubles).
 #define PI_WARPS 8
 #define PI_SM 640
+
+// Pair batches: a warp takes pairs b0 .. b0 + nb - 1 (nb <= 32) of frame f.
+__device__ __forceinline__ bool pair_batch(const DeviceSystem &s, int n_frames, int warps_per_block, int &f, int &b0, int &nb)
+{
+    const int nbatch = (s.n_pairs + 31) / 32;
+    const long gw = (long)blockIdx.x * warps_per_block + (threadIdx.x >> 5);
+    if (gw >= (long)n_frames * nbatch) return false;
+    f = (int)(gw / nbatch);
+    b0 = (int)(gw % nbatch) * 32;
+    nb = min(32, s.n_pairs - b0);
+    return true;
+}
+
+__device__ __forceinline__ int overlap_used(int noi, int noj)
+{
+    return 1 | (noi > 1 ? 2 : 0) | (noj > 1 ? 4 : 0) | (noi > 1 && noj > 1 ? 8 : 0);
+}
 
 __global__ void __launch_bounds__(PI_WARPS * 32)
 k_pair_integrals(DeviceSystem s, FramePlan plan, int n_frames, const double *__restrict__ xyz,
@@ -140,74 +101,91 @@ k_pair_integrals(DeviceSystem s, FramePlan plan, int n_frames, const double *__r
 {
     __shared__ double smem[PI_WARPS][PI_SM];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    long gw = (long)blockIdx.x * PI_WARPS + w;
-    if (gw >= (long)n_frames * s.n_pairs) return;
-    int f = (int)(gw / s.n_pairs), p = (int)(gw % s.n_pairs);
+    int f, b0, nb;
+    if (!pair_batch(s, n_frames, PI_WARPS, f, b0, nb)) return;
     double *W = smem[w];
-    double *St = W, *L = W + 96, *ci = W + 196, *cj = W + 206, *X = W + 216, *C = W + 316, *Y = W + 416;
-    int i = s.pair_i[p], j = s.pair_j[p];
-    int eli = s.atom_elem[i], elj = s.atom_elem[j];
-    const double *Ei = elem(s, eli), *Ej = elem(s, elj);
-    int noi = s.atom_norb[i], noj = s.atom_norb[j];
-    int ni = noi * (noi + 1) / 2, nj = noj * (noj + 1) / 2;
-    bool spi = noi > 1, spj = noj > 1;
+    double *St = W, *L = W + 96, *ci = W + 196, *cj = W + 206, *X = W + 216, *C = W + 316;
     const double *R = xyz + (size_t)f * 3 * s.n_atoms;
-    double x = R[3 * j] - R[3 * i], y = R[3 * j + 1] - R[3 * i + 1], z = R[3 * j + 2] - R[3 * i + 2];
-    double r = sqrt(x * x + y * y + z * z);
     double *wsf = ws + (size_t)f * plan.stride;
-
-    const double *to = terms + (size_t)(eli * s.n_elements + elj) * 2 * MP_NTERMS, *ta = to + MP_NTERMS;
-    for (int k = lane; k < MP_TERMS_USED; k += 32) {
-        double a = ta[k];
-        St[k] = (a < 0.0) ? 0.0 : rsqrt((r + to[k]) * (r + to[k]) + a);
-    }
-    for (int k = lane; k < 120; k += 32) L[k] = 0.0;   // L, ci, cj
-    Rotation rot;
-    make_rotation(x, y, z, r, noi > noj ? noi : noj, false, rot);
-    for (int k = lane; k < 100; k += 32) C[k] = ctrans(rot.T, k / 10, k % 10);
-    __syncwarp();
-    if (lane == 0) multipole_combine(St, spi, spj, L, ci, cj);
-    __syncwarp();
-    // X = C_i L  (ni x nj),  Y = X C_j^T (ni x nj)
-    for (int k = lane; k < ni * nj; k += 32) {
-        int ab = k / nj, q = k % nj;
-        double v = 0.0;
-        for (int m = 0; m < ni; m++) v += C[ab * 10 + m] * L[m * 10 + q];
-        X[k] = v;
-    }
-    __syncwarp();
-    double *tei = wsf + plan.tei + s.pair_tei[p];
-    for (int k = lane; k < ni * nj; k += 32) {
-        int ab = k / nj, cd = k % nj;
-        double v = 0.0;
-        for (int q = 0; q < nj; q++) v += X[ab * nj + q] * C[cd * 10 + q];
-        tei[k] = (fabs(v) > PDG_TEI_UNDERFLOW) ? v : 0.0;   // BlockStorage underflow, QCModelMNDO.c:1029
-    }
-    // electron-core terms rotated to the molecular frame, scaled by -Z of the other core
-    double *pe = wsf + plan.pair_e + (size_t)p * PDG_PAIR_E_STRIDE;
-    if (lane < ni) {
-        double v = 0.0;
-        for (int m = 0; m < ni; m++) v += C[lane * 10 + m] * ci[m];
-        pe[lane] = -Ej[PDG_E_ZCORE] * v;
-    }
-    if (lane >= 16 && lane - 16 < nj) {
-        int cd = lane - 16;
-        double v = 0.0;
-        for (int m = 0; m < nj; m++) v += C[cd * 10 + m] * cj[m];
-        pe[10 + cd] = -Ei[PDG_E_ZCORE] * v;
-    }
-    // resonance integrals H_ab = S_ab (beta_a + beta_b) / 2 (QCModelMNDO.c:1075-1092)
-    double Sv[16];
-    pair_overlap(Ei, Ej, x, y, z, false, lane, Sv, nullptr);
-    int N = s.n_basis, is = s.atom_start[i], js = s.atom_start[j];
+    const int N = s.n_basis;
     double *H = wsf + plan.H;
-    if (lane < noi * noj) {
-        int a = lane / noj, b = lane % noj;
-        double v = Sv[a * 4 + b] * 0.5 * (Ei[PDG_E_BETA + a] + Ej[PDG_E_BETA + b]);
-        H[(size_t)(is + a) * N + js + b] = v;
-        H[(size_t)(js + b) * N + is + a] = v;
+    // one thread per pair: geometry, core-core energy, direction cosines
+    int mi = 0, mj = 0;
+    double mx = 0.0, my = 0.0, mz = 0.0, mr = 1.0;
+    RotScalars mq = {};
+    if (lane < nb) {
+        const int p = b0 + lane;
+        mi = s.pair_i[p]; mj = s.pair_j[p];
+        mx = R[3 * mj] - R[3 * mi]; my = R[3 * mj + 1] - R[3 * mi + 1]; mz = R[3 * mj + 2] - R[3 * mi + 2];
+        mr = sqrt(mx * mx + my * my + mz * mz);
+        wsf[plan.pair_e + (size_t)p * PDG_PAIR_E_STRIDE + 20] = core_core(elem(s, s.atom_elem[mi]), elem(s, s.atom_elem[mj]), mr, nullptr);
+        rot_scalars(mx, my, mz, mr, max(s.atom_norb[mi], s.atom_norb[mj]), false, mq);
     }
-    if (lane == 0) pe[20] = core_core(Ei, Ej, r, nullptr);
+    for (int t = 0; t < nb; t++) {
+        const int p = b0 + t;
+        const int i = __shfl_sync(0xffffffffu, mi, t), j = __shfl_sync(0xffffffffu, mj, t);
+        const double x = __shfl_sync(0xffffffffu, mx, t), y = __shfl_sync(0xffffffffu, my, t), z = __shfl_sync(0xffffffffu, mz, t);
+        const double r = __shfl_sync(0xffffffffu, mr, t);
+        const RotScalars q = rot_shfl(mq, t, false);
+        const int eli = s.atom_elem[i], elj = s.atom_elem[j];
+        const double *Ei = elem(s, eli), *Ej = elem(s, elj);
+        const int noi = s.atom_norb[i], noj = s.atom_norb[j];
+        const int ni = noi * (noi + 1) / 2, nj = noj * (noj + 1) / 2;
+        const bool spi = noi > 1, spj = noj > 1;
+        const double *to = terms + (size_t)(eli * s.n_elements + elj) * 2 * MP_NTERMS, *ta = to + MP_NTERMS;
+        for (int k = lane; k < MP_TERMS_USED; k += 32) {
+            const double a = ta[k];
+            St[k] = (a < 0.0) ? 0.0 : rsqrt((r + to[k]) * (r + to[k]) + a);
+        }
+        for (int k = lane; k < 120; k += 32) L[k] = 0.0;   // L, ci, cj
+        Rotation rot;
+        rot_assemble(q, false, rot);
+        for (int k = lane; k < 100; k += 32) C[k] = ctrans(rot.T, k / 10, k % 10);
+        __syncwarp();
+        if (lane == 0) multipole_combine(St, spi, spj, L, ci, cj);
+        __syncwarp();
+        // X = C_i L  (ni x nj),  TEI = X C_j^T (ni x nj)
+        for (int k = lane; k < ni * nj; k += 32) {
+            const int ab = k / nj, qq = k % nj;
+            double v = 0.0;
+            for (int m = 0; m < ni; m++) v += C[ab * 10 + m] * L[m * 10 + qq];
+            X[k] = v;
+        }
+        __syncwarp();
+        double *tei = wsf + plan.tei + s.pair_tei[p];
+        for (int k = lane; k < ni * nj; k += 32) {
+            const int ab = k / nj, cd = k % nj;
+            double v = 0.0;
+            for (int qq = 0; qq < nj; qq++) v += X[ab * nj + qq] * C[cd * 10 + qq];
+            tei[k] = (fabs(v) > PDG_TEI_UNDERFLOW) ? v : 0.0;   // BlockStorage underflow, QCModelMNDO.c:1029
+        }
+        // electron-core terms rotated to the molecular frame, scaled by -Z of the other core
+        double *pe = wsf + plan.pair_e + (size_t)p * PDG_PAIR_E_STRIDE;
+        if (lane < ni) {
+            double v = 0.0;
+            for (int m = 0; m < ni; m++) v += C[lane * 10 + m] * ci[m];
+            pe[lane] = -Ej[PDG_E_ZCORE] * v;
+        }
+        if (lane >= 16 && lane - 16 < nj) {
+            const int cd = lane - 16;
+            double v = 0.0;
+            for (int m = 0; m < nj; m++) v += C[cd * 10 + m] * cj[m];
+            pe[10 + cd] = -Ei[PDG_E_ZCORE] * v;
+        }
+        // resonance integrals H_ab = S_ab (beta_a + beta_b) / 2 (QCModelMNDO.c:1075-1092)
+        const int eo = eli * s.n_elements + elj;
+        double Fo[5], Do[5];
+        overlap_sums(s.ovl + (size_t)s.ovl_off[eo] * OV_REC, s.ovl_n[eo], x * x + y * y + z * z, false, overlap_used(noi, noj), Fo, Do);
+        const int is = s.atom_start[i], js = s.atom_start[j];
+        if (lane < noi * noj) {
+            const int a = lane / noj, b = lane % noj;
+            const double AB[3] = { x, y, z };
+            const double v = overlap_element(a, b, AB, Fo) * 0.5 * (Ei[PDG_E_BETA + a] + Ej[PDG_E_BETA + b]);
+            H[(size_t)(is + a) * N + js + b] = v;
+            H[(size_t)(js + b) * N + is + a] = v;
+        }
+        __syncwarp();
+    }
 }
 
 __global__ void __launch_bounds__(256) k_assemble_h(DeviceSystem s, FramePlan plan, int n_frames, double *__restrict__ ws)
@@ -239,7 +217,7 @@ __global__ void __launch_bounds__(256) k_assemble_h(DeviceSystem s, FramePlan pl
 
 void launch_pair_integrals(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *xyz, double *ws, cudaStream_t st)
 {
-    long warps = (long)n_frames * s.n_pairs;
+    long warps = (long)n_frames * ((s.n_pairs + 31) / 32);
     if (warps > 0) {
         int blocks = (int)((warps + PI_WARPS - 1) / PI_WARPS);
         k_pair_integrals<<<blocks, PI_WARPS * 32, 0, st>>>(s, p, n_frames, xyz, s.terms, ws);
@@ -263,123 +241,141 @@ k_pair_gradients(DeviceSystem s, FramePlan plan, int n_frames, const double *__r
 {
     __shared__ double smem[PG_WARPS][PG_SM];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    long gw = (long)blockIdx.x * PG_WARPS + w;
-    if (gw >= (long)n_frames * s.n_pairs) return;
-    int f = (int)(gw / s.n_pairs), p = (int)(gw % s.n_pairs);
+    int f, b0, nb;
+    if (!pair_batch(s, n_frames, PG_WARPS, f, b0, nb)) return;
     double *W = smem[w];
     double *St = W, *dSt = W + 96, *L = W + 192, *dL = W + 292, *ci = W + 392, *cj = W + 402, *dci = W + 412, *dcj = W + 422;
     double *C = W + 432, *CD = W + 532, *G = W + 832, *W1 = W + 932, *W2 = W + 1032, *W3 = W + 1132;
-    double *oneI = W + 1232, *oneJ = W + 1242;
-    int i = s.pair_i[p], j = s.pair_j[p];
-    int eli = s.atom_elem[i], elj = s.atom_elem[j];
-    const double *Ei = elem(s, eli), *Ej = elem(s, elj);
-    int noi = s.atom_norb[i], noj = s.atom_norb[j];
-    int ni = noi * (noi + 1) / 2, nj = noj * (noj + 1) / 2;
-    bool spi = noi > 1, spj = noj > 1;
-    int N = s.n_basis, is = s.atom_start[i], js = s.atom_start[j];
+    double *oneI = W + 1232, *oneJ = W + 1242, *Wres = W + 1252;
+    const int N = s.n_basis;
     const double *R = xyz + (size_t)f * 3 * s.n_atoms;
     const double *P = density + (size_t)f * N * N;
-    double v3[3] = { R[3 * j] - R[3 * i], R[3 * j + 1] - R[3 * i + 1], R[3 * j + 2] - R[3 * i + 2] };
-    double r = sqrt(v3[0] * v3[0] + v3[1] * v3[1] + v3[2] * v3[2]);
-    double eng[3] = { 0.0, 0.0, 0.0 };
-
-    // one-centre density vectors (off-diagonal elements doubled) and the two-centre density
-    // Gamma = 1/4 aa bb (P_mk P_nl + P_nk P_ml) - oneI (x) oneJ  (QCModelMNDOState.c:196-250)
-    if (lane < ni) { int a = MP_DA[lane], b = MP_DB[lane]; oneI[lane] = (a == b ? 1.0 : 2.0) * P[(size_t)(is + a) * N + is + b]; }
-    if (lane >= 16 && lane - 16 < nj) { int k = lane - 16, a = MP_DA[k], b = MP_DB[k]; oneJ[k] = (a == b ? 1.0 : 2.0) * P[(size_t)(js + a) * N + js + b]; }
-    __syncwarp();
-    for (int k = lane; k < ni * nj; k += 32) {
-        int kl = k / nj, mn = k % nj;
-        int l = MP_DA[kl], kk = MP_DB[kl], n = MP_DA[mn], m = MP_DB[mn];   // kl = (l >= kk), mn = (n >= m)
-        double aa = (kk == l) ? 1.0 : 2.0, bb = (m == n) ? 1.0 : 2.0;
-        int K = is + kk, Lx = is + l, M = js + m, Nn = js + n;
-        double fv = P[(size_t)M * N + K] * P[(size_t)Nn * N + Lx] + P[(size_t)Nn * N + K] * P[(size_t)M * N + Lx];
-        G[k] = 0.25 * aa * bb * fv - oneI[kl] * oneJ[mn];
+    // one thread per pair: geometry, core-core derivative, direction cosines and their derivatives
+    int mi = 0, mj = 0;
+    double mx = 0.0, my = 0.0, mz = 0.0, mr = 1.0, mdc = 0.0;
+    RotScalars mq = {};
+    if (lane < nb) {
+        const int p = b0 + lane;
+        mi = s.pair_i[p]; mj = s.pair_j[p];
+        mx = R[3 * mj] - R[3 * mi]; my = R[3 * mj + 1] - R[3 * mi + 1]; mz = R[3 * mj + 2] - R[3 * mi + 2];
+        mr = sqrt(mx * mx + my * my + mz * mz);
+        core_core(elem(s, s.atom_elem[mi]), elem(s, s.atom_elem[mj]), mr, &mdc);
+        rot_scalars(mx, my, mz, mr, max(s.atom_norb[mi], s.atom_norb[mj]), true, mq);
     }
-    if (r >= 5.0e-3) {
-        const double *to = terms + (size_t)(eli * s.n_elements + elj) * 2 * MP_NTERMS, *ta = to + MP_NTERMS;
-        for (int k = lane; k < MP_TERMS_USED; k += 32) {
-            double a = ta[k];
-            if (a < 0.0) { St[k] = 0.0; dSt[k] = 0.0; continue; }
-            double ro = r + to[k], sv = rsqrt(ro * ro + a);
-            St[k] = sv; dSt[k] = -ro * sv * sv * sv;
-        }
-        for (int k = lane; k < 240; k += 32) L[k] = 0.0;     // L, dL, ci, cj, dci, dcj (contiguous)
-        Rotation rot;
-        make_rotation(v3[0], v3[1], v3[2], r, noi > noj ? noi : noj, true, rot);
-        for (int k = lane; k < 100; k += 32) {
-            int ab = k / 10, mn = k % 10;
-            C[k] = ctrans(rot.T, ab, mn);
-            for (int x = 0; x < 3; x++) CD[x * 100 + k] = rot.active ? ctrans_d(rot.T, rot.D[x], ab, mn) : 0.0;
+    for (int t = 0; t < nb; t++) {
+        const int p = b0 + t;
+        const int i = __shfl_sync(0xffffffffu, mi, t), j = __shfl_sync(0xffffffffu, mj, t);
+        const double v3[3] = { __shfl_sync(0xffffffffu, mx, t), __shfl_sync(0xffffffffu, my, t), __shfl_sync(0xffffffffu, mz, t) };
+        const double r = __shfl_sync(0xffffffffu, mr, t), dcore = __shfl_sync(0xffffffffu, mdc, t);
+        const RotScalars q = rot_shfl(mq, t, true);
+        const int eli = s.atom_elem[i], elj = s.atom_elem[j];
+        const double *Ei = elem(s, eli), *Ej = elem(s, elj);
+        const int noi = s.atom_norb[i], noj = s.atom_norb[j];
+        const int ni = noi * (noi + 1) / 2, nj = noj * (noj + 1) / 2;
+        const bool spi = noi > 1, spj = noj > 1;
+        const int is = s.atom_start[i], js = s.atom_start[j];
+        double eng[3] = { 0.0, 0.0, 0.0 };
+        // one-centre density vectors (off-diagonal elements doubled) and the two-centre density
+        // Gamma = 1/4 aa bb (P_mk P_nl + P_nk P_ml) - oneI (x) oneJ  (QCModelMNDOState.c:196-250)
+        if (lane < ni) { const int a = MP_DA[lane], b = MP_DB[lane]; oneI[lane] = (a == b ? 1.0 : 2.0) * P[(size_t)(is + a) * N + is + b]; }
+        if (lane >= 16 && lane - 16 < nj) { const int k = lane - 16, a = MP_DA[k], b = MP_DB[k]; oneJ[k] = (a == b ? 1.0 : 2.0) * P[(size_t)(js + a) * N + js + b]; }
+        // resonance weights (beta_a + beta_b) P_ab (QCModelMNDO.c:800-823)
+        if (lane < 16) {
+            const int a = lane / 4, b = lane % 4;
+            Wres[lane] = (a < noi && b < noj) ? (Ei[PDG_E_BETA + a] + Ej[PDG_E_BETA + b]) * P[(size_t)(is + a) * N + js + b] : 0.0;
         }
         __syncwarp();
-        if (lane == 0) multipole_combine(St, spi, spj, L, ci, cj);
-        if (lane == 1) multipole_combine(dSt, spi, spj, dL, dci, dcj);
-        __syncwarp();
-        // W1 = L C_j^T, W2 = C_i L, W3 = dL C_j^T
         for (int k = lane; k < ni * nj; k += 32) {
-            int a = k / nj, b = k % nj;
-            double w1 = 0.0, w3 = 0.0, w2 = 0.0;
-            for (int q = 0; q < nj; q++) { w1 += L[a * 10 + q] * C[b * 10 + q]; w3 += dL[a * 10 + q] * C[b * 10 + q]; }
-            for (int m = 0; m < ni; m++) w2 += C[a * 10 + m] * L[m * 10 + b];
-            W1[k] = w1; W2[k] = w2; W3[k] = w3;
+            const int kl = k / nj, mn = k % nj;
+            const int l = MP_DA[kl], kk = MP_DB[kl], n = MP_DA[mn], m = MP_DB[mn];   // kl = (l >= kk), mn = (n >= m)
+            const double aa = (kk == l) ? 1.0 : 2.0, bb = (m == n) ? 1.0 : 2.0;
+            const int K = is + kk, Lx = is + l, M = js + m, Nn = js + n;
+            const double fv = P[(size_t)M * N + K] * P[(size_t)Nn * N + Lx] + P[(size_t)Nn * N + K] * P[(size_t)M * N + Lx];
+            G[k] = 0.25 * aa * bb * fv - oneI[kl] * oneJ[mn];
+        }
+        if (r >= 5.0e-3) {
+            const double *to = terms + (size_t)(eli * s.n_elements + elj) * 2 * MP_NTERMS, *ta = to + MP_NTERMS;
+            for (int k = lane; k < MP_TERMS_USED; k += 32) {
+                const double a = ta[k];
+                if (a < 0.0) { St[k] = 0.0; dSt[k] = 0.0; continue; }
+                const double ro = r + to[k], sv = rsqrt(ro * ro + a);
+                St[k] = sv; dSt[k] = -ro * sv * sv * sv;
+            }
+            for (int k = lane; k < 240; k += 32) L[k] = 0.0;     // L, dL, ci, cj, dci, dcj (contiguous)
+            Rotation rot;
+            rot_assemble(q, true, rot);
+            for (int k = lane; k < 100; k += 32) {
+                const int ab = k / 10, mn = k % 10;
+                C[k] = ctrans(rot.T, ab, mn);
+                for (int xx = 0; xx < 3; xx++) CD[xx * 100 + k] = rot.active ? ctrans_d(rot.T, rot.D[xx], ab, mn) : 0.0;
+            }
+            __syncwarp();
+            if (lane == 0) multipole_combine(St, spi, spj, L, ci, cj);
+            if (lane == 1) multipole_combine(dSt, spi, spj, dL, dci, dcj);
+            __syncwarp();
+            // W1 = L C_j^T, W2 = C_i L, W3 = dL C_j^T
+            for (int k = lane; k < ni * nj; k += 32) {
+                const int a = k / nj, b = k % nj;
+                double w1 = 0.0, w3 = 0.0, w2 = 0.0;
+                for (int qq = 0; qq < nj; qq++) { w1 += L[a * 10 + qq] * C[b * 10 + qq]; w3 += dL[a * 10 + qq] * C[b * 10 + qq]; }
+                for (int m = 0; m < ni; m++) w2 += C[a * 10 + m] * L[m * 10 + b];
+                W1[k] = w1; W2[k] = w2; W3[k] = w3;
+            }
+            __syncwarp();
+            double t0 = 0.0, ti[3] = { 0, 0, 0 }, tj[3] = { 0, 0, 0 };
+            for (int k = lane; k < ni * nj; k += 32) {
+                const int ab = k / nj, cd = k % nj;
+                const double g = G[k];
+                double u0 = 0.0, ui[3] = { 0, 0, 0 }, uj[3] = { 0, 0, 0 };
+                for (int m = 0; m < ni; m++) {
+                    const double w1 = W1[m * nj + cd];
+                    u0 += C[ab * 10 + m] * W3[m * nj + cd];
+                    if (spi) for (int xx = 0; xx < 3; xx++) ui[xx] += CD[xx * 100 + ab * 10 + m] * w1;
+                }
+                if (spj) for (int qq = 0; qq < nj; qq++) { const double w2 = W2[ab * nj + qq]; for (int xx = 0; xx < 3; xx++) uj[xx] += w2 * CD[xx * 100 + cd * 10 + qq]; }
+                t0 += g * u0;
+                for (int xx = 0; xx < 3; xx++) { ti[xx] += g * ui[xx]; tj[xx] += g * uj[xx]; }
+            }
+            // electron-core parts
+            double o0 = 0.0, oi[3] = { 0, 0, 0 };
+            if (lane < ni) {
+                double u = 0.0, ux[3] = { 0, 0, 0 };
+                for (int m = 0; m < ni; m++) {
+                    u += C[lane * 10 + m] * dci[m];
+                    if (spi) for (int xx = 0; xx < 3; xx++) ux[xx] += CD[xx * 100 + lane * 10 + m] * ci[m];
+                }
+                o0 += oneI[lane] * u * (-Ej[PDG_E_ZCORE]);
+                for (int xx = 0; xx < 3; xx++) oi[xx] += oneI[lane] * ux[xx] * (-Ej[PDG_E_ZCORE]);
+            }
+            if (lane >= 16 && lane - 16 < nj) {
+                const int cd = lane - 16;
+                double u = 0.0, ux[3] = { 0, 0, 0 };
+                for (int m = 0; m < nj; m++) {
+                    u += C[cd * 10 + m] * dcj[m];
+                    if (spj) for (int xx = 0; xx < 3; xx++) ux[xx] += CD[xx * 100 + cd * 10 + m] * cj[m];
+                }
+                o0 += oneJ[cd] * u * (-Ei[PDG_E_ZCORE]);
+                for (int xx = 0; xx < 3; xx++) oi[xx] += oneJ[cd] * ux[xx] * (-Ei[PDG_E_ZCORE]);
+            }
+            t0 = warp_sum(t0); o0 = warp_sum(o0);
+            for (int xx = 0; xx < 3; xx++) { ti[xx] = warp_sum(ti[xx]); tj[xx] = warp_sum(tj[xx]); oi[xx] = warp_sum(oi[xx]); }
+            // eng = -s (dcore + doei0f + dtei0f) + doei1 + dtei1   (MNDOIntegrals.c:392-418)
+            for (int xx = 0; xx < 3; xx++) {
+                const double sx = v3[xx] / r;
+                eng[xx] = -sx * dcore - sx * o0 + sx * t0 - oi[xx] + ti[xx] + tj[xx];
+            }
+        }
+        // resonance integral derivatives: sum (beta_a + beta_b) P_ab dS_ab / dR_i
+        const int eo = eli * s.n_elements + elj;
+        double Fo[5], Do[5], gr[3];
+        overlap_sums(s.ovl + (size_t)s.ovl_off[eo] * OV_REC, s.ovl_n[eo], v3[0] * v3[0] + v3[1] * v3[1] + v3[2] * v3[2], true,
+                     overlap_used(noi, noj), Fo, Do);
+        overlap_gradient(Wres, noi, noj, v3, Fo, Do, gr);
+        if (lane == 0) {
+            double *pg = ws + (size_t)f * plan.stride + plan.pair_g + (size_t)p * 3;
+            pg[0] = eng[0] + gr[0]; pg[1] = eng[1] + gr[1]; pg[2] = eng[2] + gr[2];
         }
         __syncwarp();
-        double t0 = 0.0, ti[3] = { 0, 0, 0 }, tj[3] = { 0, 0, 0 };
-        for (int k = lane; k < ni * nj; k += 32) {
-            int ab = k / nj, cd = k % nj;
-            double g = G[k], u0 = 0.0, ui[3] = { 0, 0, 0 }, uj[3] = { 0, 0, 0 };
-            for (int m = 0; m < ni; m++) {
-                double w1 = W1[m * nj + cd];
-                u0 += C[ab * 10 + m] * W3[m * nj + cd];
-                if (spi) for (int x = 0; x < 3; x++) ui[x] += CD[x * 100 + ab * 10 + m] * w1;
-            }
-            if (spj) for (int q = 0; q < nj; q++) { double w2 = W2[ab * nj + q]; for (int x = 0; x < 3; x++) uj[x] += w2 * CD[x * 100 + cd * 10 + q]; }
-            t0 += g * u0;
-            for (int x = 0; x < 3; x++) { ti[x] += g * ui[x]; tj[x] += g * uj[x]; }
-        }
-        // electron-core parts
-        double o0 = 0.0, oi[3] = { 0, 0, 0 };
-        if (lane < ni) {
-            double u = 0.0, ux[3] = { 0, 0, 0 };
-            for (int m = 0; m < ni; m++) {
-                u += C[lane * 10 + m] * dci[m];
-                if (spi) for (int x = 0; x < 3; x++) ux[x] += CD[x * 100 + lane * 10 + m] * ci[m];
-            }
-            o0 += oneI[lane] * u * (-Ej[PDG_E_ZCORE]);
-            for (int x = 0; x < 3; x++) oi[x] += oneI[lane] * ux[x] * (-Ej[PDG_E_ZCORE]);
-        }
-        if (lane >= 16 && lane - 16 < nj) {
-            int cd = lane - 16;
-            double u = 0.0, ux[3] = { 0, 0, 0 };
-            for (int m = 0; m < nj; m++) {
-                u += C[cd * 10 + m] * dcj[m];
-                if (spj) for (int x = 0; x < 3; x++) ux[x] += CD[x * 100 + cd * 10 + m] * cj[m];
-            }
-            o0 += oneJ[cd] * u * (-Ei[PDG_E_ZCORE]);
-            for (int x = 0; x < 3; x++) oi[x] += oneJ[cd] * ux[x] * (-Ei[PDG_E_ZCORE]);
-        }
-        t0 = warp_sum(t0); o0 = warp_sum(o0);
-        for (int x = 0; x < 3; x++) { ti[x] = warp_sum(ti[x]); tj[x] = warp_sum(tj[x]); oi[x] = warp_sum(oi[x]); }
-        double dcore = 0.0;
-        core_core(Ei, Ej, r, &dcore);
-        // eng = -s (dcore + doei0f + dtei0f) + doei1 + dtei1   (MNDOIntegrals.c:392-418)
-        for (int x = 0; x < 3; x++) {
-            double sx = v3[x] / r;
-            eng[x] = -sx * dcore - sx * o0 + sx * t0 - oi[x] + ti[x] + tj[x];
-        }
-    }
-    // resonance integral derivatives: sum (beta_a + beta_b) P_ab dS_ab (QCModelMNDO.c:800-823)
-    double Sv[16], SDv[48];
-    pair_overlap(Ei, Ej, v3[0], v3[1], v3[2], true, lane, Sv, SDv);
-    for (int a = 0; a < noi; a++)
-        for (int b = 0; b < noj; b++) {
-            double bp = (Ei[PDG_E_BETA + a] + Ej[PDG_E_BETA + b]) * P[(size_t)(is + a) * N + js + b];
-            for (int x = 0; x < 3; x++) eng[x] += bp * SDv[x * 16 + a * 4 + b];
-        }
-    if (lane == 0) {
-        double *pg = ws + (size_t)f * plan.stride + plan.pair_g + (size_t)p * 3;
-        pg[0] = eng[0]; pg[1] = eng[1]; pg[2] = eng[2];
     }
 }
 
@@ -406,7 +402,7 @@ __global__ void __launch_bounds__(256) k_reduce_gradients(DeviceSystem s, FrameP
 void launch_pair_gradients(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *xyz,
                            const double *density, double *ws, cudaStream_t st)
 {
-    long warps = (long)n_frames * s.n_pairs;
+    long warps = (long)n_frames * ((s.n_pairs + 31) / 32);
     if (warps > 0)
         k_pair_gradients<<<(int)((warps + PG_WARPS - 1) / PG_WARPS), PG_WARPS * 32, 0, st>>>(s, p, n_frames, xyz, s.terms, density, ws);
 }

@@ -150,40 +150,78 @@ __device__ inline void multipole_combine(const double *s, bool spi, bool spj, do
 // (s, sigma, pi+, pi-).  Returns false when no rotation applies (identity, zero derivatives).
 struct Rotation { double T[4][4]; double D[3][4][4]; bool active; };
 
-__device__ __forceinline__ void make_rotation(double x, double y, double z, double r, int norb_max, bool derivs, Rotation &R)
+// The geometry-dependent scalars of the rotation (square root, divisions): direction cosines and, for
+// gradients, their derivatives.  Computed once per pair (one thread per pair) and broadcast to the
+// lanes that assemble T and D from them.
+struct RotScalars { double ca, sa, cb, sb, caX, caY, saX, saY, cbX, cbY, cbZ, sbX, sbY, sbZ; int swapped, active; };
+
+__device__ __forceinline__ void rot_scalars(double x, double y, double z, double r, int norb_max, bool derivs, RotScalars &q)
+{
+    q.active = (norb_max > 1) && (r * r > 2.0e-5);
+    q.swapped = 0;
+    q.ca = q.sa = q.cb = q.sb = 0.0;
+    q.caX = q.caY = q.saX = q.saY = q.cbX = q.cbY = q.cbZ = q.sbX = q.sbY = q.sbZ = 0.0;
+    if (!q.active) return;
+    q.swapped = fabs(z / r) > 0.99999999;
+    if (q.swapped) { double t = x; x = z; z = t; }
+    const double b2 = x * x + y * y, b = sqrt(b2);
+    q.sb = b / r; q.ca = x / b; q.sa = y / b; q.cb = z / r;
+    if (!derivs) return;
+    const double r3 = r * r * r;
+    q.caX = y * y / (b2 * b); q.caY = -x * y / (b2 * b); q.saX = q.caY; q.saY = x * x / (b2 * b);
+    q.cbX = -x * z / r3; q.cbY = -y * z / r3; q.cbZ = b2 / r3;
+    q.sbX = x * z * z / (b * r3); q.sbY = y * z * z / (b * r3); q.sbZ = -b * z / r3;
+}
+
+__device__ __forceinline__ RotScalars rot_shfl(const RotScalars &q, int src, bool derivs)
+{
+    RotScalars o;
+    const unsigned m = 0xffffffffu;
+    o.active = __shfl_sync(m, q.active, src); o.swapped = __shfl_sync(m, q.swapped, src);
+    o.ca = __shfl_sync(m, q.ca, src); o.sa = __shfl_sync(m, q.sa, src); o.cb = __shfl_sync(m, q.cb, src); o.sb = __shfl_sync(m, q.sb, src);
+    if (derivs) {
+        o.caX = __shfl_sync(m, q.caX, src); o.caY = __shfl_sync(m, q.caY, src); o.saX = __shfl_sync(m, q.saX, src);
+        o.saY = __shfl_sync(m, q.saY, src); o.cbX = __shfl_sync(m, q.cbX, src); o.cbY = __shfl_sync(m, q.cbY, src);
+        o.cbZ = __shfl_sync(m, q.cbZ, src); o.sbX = __shfl_sync(m, q.sbX, src); o.sbY = __shfl_sync(m, q.sbY, src);
+        o.sbZ = __shfl_sync(m, q.sbZ, src);
+    } else {
+        o.caX = o.caY = o.saX = o.saY = o.cbX = o.cbY = o.cbZ = o.sbX = o.sbY = o.sbZ = 0.0;
+    }
+    return o;
+}
+
+// Local-to-molecular rotation of the p shell and its derivatives with respect to the coordinates of
+// atom j (MNDOIntegralUtilities_GetTransformationMatrices, MNDOIntegralUtilities.c:449-465 for s/p,
+// axes swapped when |z/r| > 0.99999999).  T[a][m]: molecular orbital a (s, pz, px, py), local m
+// (s, sigma, pi+, pi-).  Inactive: identity, zero derivatives.
+__device__ __forceinline__ void rot_assemble(const RotScalars &q, bool derivs, Rotation &R)
 {
     for (int a = 0; a < 4; a++) for (int m = 0; m < 4; m++) {
         R.T[a][m] = (a == m) ? 1.0 : 0.0;
         if (derivs) { R.D[0][a][m] = 0.0; R.D[1][a][m] = 0.0; R.D[2][a][m] = 0.0; }
     }
-    R.active = (norb_max > 1) && (r * r > 2.0e-5);
-    if (!R.active) return;
-    bool swapped = fabs(z / r) > 0.99999999;
-    if (swapped) { double t = x; x = z; z = t; }
-    double b2 = x * x + y * y, b = sqrt(b2), sb = b / r, ca = x / b, sa = y / b, cb = z / r;
+    R.active = q.active;
+    if (!q.active) return;
     const int PZ = 1, PX = 2, PY = 3;
+    const double ca = q.ca, sa = q.sa, cb = q.cb, sb = q.sb;
     double T[4][4] = {{1, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
     T[PX][1] = ca * sb; T[PX][2] = ca * cb; T[PX][3] = -sa;
     T[PY][1] = sa * sb; T[PY][2] = sa * cb; T[PY][3] = ca;
     T[PZ][1] = cb;      T[PZ][2] = -sb;
-    if (swapped) for (int c = 0; c < 4; c++) { double t = T[PX][c]; T[PX][c] = T[PZ][c]; T[PZ][c] = t; }
+    if (q.swapped) for (int c = 0; c < 4; c++) { double t = T[PX][c]; T[PX][c] = T[PZ][c]; T[PZ][c] = t; }
     for (int a = 0; a < 4; a++) for (int m = 0; m < 4; m++) R.T[a][m] = T[a][m];
     if (!derivs) return;
-    double r3 = r * r * r;
-    double caX = y * y / (b2 * b), caY = -x * y / (b2 * b), saX = caY, saY = x * x / (b2 * b);
-    double cbX = -x * z / r3, cbY = -y * z / r3, cbZ = b2 / r3;
-    double sbX = x * z * z / (b * r3), sbY = y * z * z / (b * r3), sbZ = -b * z / r3;
     double D[3][4][4] = {};
-    D[0][PX][1] = caX * sb + ca * sbX; D[0][PX][2] = caX * cb + ca * cbX; D[0][PX][3] = -saX;
-    D[0][PY][1] = saX * sb + sa * sbX; D[0][PY][2] = saX * cb + sa * cbX; D[0][PY][3] = caX;
-    D[0][PZ][1] = cbX; D[0][PZ][2] = -sbX;
-    D[1][PX][1] = caY * sb + ca * sbY; D[1][PX][2] = caY * cb + ca * cbY; D[1][PX][3] = -saY;
-    D[1][PY][1] = saY * sb + sa * sbY; D[1][PY][2] = saY * cb + sa * cbY; D[1][PY][3] = caY;
-    D[1][PZ][1] = cbY; D[1][PZ][2] = -sbY;
-    D[2][PX][1] = ca * sbZ; D[2][PX][2] = ca * cbZ;
-    D[2][PY][1] = sa * sbZ; D[2][PY][2] = sa * cbZ;
-    D[2][PZ][1] = cbZ; D[2][PZ][2] = -sbZ;
-    if (swapped) {
+    D[0][PX][1] = q.caX * sb + ca * q.sbX; D[0][PX][2] = q.caX * cb + ca * q.cbX; D[0][PX][3] = -q.saX;
+    D[0][PY][1] = q.saX * sb + sa * q.sbX; D[0][PY][2] = q.saX * cb + sa * q.cbX; D[0][PY][3] = q.caX;
+    D[0][PZ][1] = q.cbX; D[0][PZ][2] = -q.sbX;
+    D[1][PX][1] = q.caY * sb + ca * q.sbY; D[1][PX][2] = q.caY * cb + ca * q.cbY; D[1][PX][3] = -q.saY;
+    D[1][PY][1] = q.saY * sb + sa * q.sbY; D[1][PY][2] = q.saY * cb + sa * q.cbY; D[1][PY][3] = q.caY;
+    D[1][PZ][1] = q.cbY; D[1][PZ][2] = -q.sbY;
+    D[2][PX][1] = ca * q.sbZ; D[2][PX][2] = ca * q.cbZ;
+    D[2][PY][1] = sa * q.sbZ; D[2][PY][2] = sa * q.cbZ;
+    D[2][PZ][1] = q.cbZ; D[2][PZ][2] = -q.sbZ;
+    if (q.swapped) {
         for (int k = 0; k < 3; k++) for (int c = 0; c < 4; c++) { double t = D[k][PX][c]; D[k][PX][c] = D[k][PZ][c]; D[k][PZ][c] = t; }
         for (int a = 0; a < 4; a++) for (int c = 0; c < 4; c++) { double t = D[0][a][c]; D[0][a][c] = D[2][a][c]; D[2][a][c] = t; }
     }

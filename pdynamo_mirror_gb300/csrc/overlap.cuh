@@ -1,0 +1,112 @@
+// overlap.cuh - STO-6G overlap of two sp shells and its derivative in closed form.
+//
+// For primitives a (on atom i) and b (on atom j), g = a + b, AB = R_j - R_i, the s/p overlap blocks of
+// GaussianBasis_2Overlap (GaussianBasisCore.c:469, orbital order s, pz, px, py) are
+//     ss = s0,  p_k s = (b/g) AB_k s0,  s p_k = -(a/g) AB_k s0,  p_k p_l = (-(ab/g^2) AB_k AB_l + delta_kl / 2g) s0,
+// with s0 = c_a c_b (pi/g)^(3/2) exp(-(ab/g) |AB|^2).  So every element of a shell pair's block is AB
+// times a few radial sums over the primitive pairs (F), and the derivative with respect to R_i
+// (GaussianBasis_2OverlapD, :570) needs the same sums weighted by 2ab/g (D).  The primitive constants are
+// tabulated per ordered element pair on the host; on the device one exp per primitive pair remains.
+// Primitive pairs with (ab/g)|AB|^2 above 18 ln 10 are skipped, as the reference does (GaussianBasis.h:43).
+#pragma once
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+#define OV_REC 4   // per primitive pair: ab/g, pre * w1, pre * w2, type
+enum { OV_SS = 0, OV_PS = 1, OV_SP = 2, OV_PP = 3 };
+#define PRIMITIVE_OVERLAP_TOLERANCE (2.30258509299405 * 18.0)
+
+// Host: append the records of the ordered element pair (A holds atom i's basis, B atom j's).
+inline void overlap_records(const double *A, const double *B, std::vector<double> &out)
+{
+    const int nsa = (int)A[PDG_E_NSHELL], nsb = (int)B[PDG_E_NSHELL];
+    const int kinds[4][3] = { { OV_SS, 0, 0 }, { OV_PS, 1, 0 }, { OV_SP, 0, 1 }, { OV_PP, 1, 1 } };
+    for (const auto &k : kinds) {
+        const int ty = k[0], sa = k[1], sb = k[2];
+        if (sa >= nsa || sb >= nsb) continue;
+        const int npa = (int)A[sa ? PDG_E_NPRIM_P : PDG_E_NPRIM_S], npb = (int)B[sb ? PDG_E_NPRIM_P : PDG_E_NPRIM_S];
+        for (int p = 0; p < npa; p++)
+            for (int q = 0; q < npb; q++) {
+                const double a = A[(sa ? PDG_E_EXP_P : PDG_E_EXP_S) + p], b = B[(sb ? PDG_E_EXP_P : PDG_E_EXP_S) + q], g = a + b;
+                const double abg = a * b / g, tg = M_PI / g;
+                const double pre = A[(sa ? PDG_E_CCBF_P : PDG_E_CCBF_S) + p] * B[(sb ? PDG_E_CCBF_P : PDG_E_CCBF_S) + q] * tg * sqrt(tg);
+                const double w1 = ty == OV_SS ? 1.0 : ty == OV_PS ? b / g : ty == OV_SP ? a / g : abg / g;
+                const double w2 = ty == OV_PP ? 0.5 / g : 0.0;
+                out.push_back(abg); out.push_back(pre * w1); out.push_back(pre * w2); out.push_back((double)ty);
+            }
+    }
+}
+
+// Radial sums of one atom pair: F[0..4] = ss, ps, sp, pp(AB AB), pp(delta); D[0..4] their 2ab/g-weighted
+// companions (derivs only).  Primitive pairs are spread over the lanes; `used` (bit k = sum k) selects the
+// sums the pair's shells need, and only those are warp-reduced.
+__device__ __forceinline__ void overlap_sums(const double *__restrict__ rec, int nrec, double R2, bool derivs, int used,
+                                             double *F, double *D)
+{
+    const int lane = threadIdx.x & 31;
+    double f0 = 0.0, f1 = 0.0, f2 = 0.0, f3 = 0.0, f4 = 0.0, d0 = 0.0, d1 = 0.0, d2 = 0.0, d3 = 0.0, d4 = 0.0;
+    for (int t = lane; t < nrec; t += 32) {
+        const double *r = rec + OV_REC * t;
+        const double abg = r[0], fac = abg * R2;
+        const double e = fac > PRIMITIVE_OVERLAP_TOLERANCE ? 0.0 : exp(-fac);
+        const int ty = (int)r[3];
+        const double t1 = r[1] * e, t2 = r[2] * e;
+        f0 += ty == OV_SS ? t1 : 0.0; f1 += ty == OV_PS ? t1 : 0.0; f2 += ty == OV_SP ? t1 : 0.0; f3 += ty == OV_PP ? t1 : 0.0;
+        f4 += t2;
+        if (derivs) {
+            const double a2 = abg + abg, u1 = a2 * t1;
+            d0 += ty == OV_SS ? u1 : 0.0; d1 += ty == OV_PS ? u1 : 0.0; d2 += ty == OV_SP ? u1 : 0.0; d3 += ty == OV_PP ? u1 : 0.0;
+            d4 = fma(a2, t2, d4);
+        }
+    }
+    const double fl[5] = { f0, f1, f2, f3, f4 }, dl[5] = { d0, d1, d2, d3, d4 };
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const int bit = k < 4 ? k : 3;
+        F[k] = (used >> bit & 1) ? warp_sum(fl[k]) : 0.0;
+        D[k] = (derivs && (used >> bit & 1)) ? warp_sum(dl[k]) : 0.0;
+    }
+}
+
+// Cartesian axis of orbital o (1 pz, 2 px, 3 py).
+__device__ __forceinline__ int ov_axis(int o) { return o == 1 ? 2 : o - 2; }
+
+// Overlap element S_ab (a on i, b on j) from the radial sums.
+__device__ __forceinline__ double overlap_element(int a, int b, const double *AB, const double *F)
+{
+    if (a == 0 && b == 0) return F[0];
+    if (b == 0) return AB[ov_axis(a)] * F[1];
+    if (a == 0) return -AB[ov_axis(b)] * F[2];
+    return -AB[ov_axis(a)] * AB[ov_axis(b)] * F[3] + (a == b ? F[4] : 0.0);
+}
+
+// sum_ab W_ab dS_ab / dR_i,k for a weight matrix W (W[a*4+b], a < noi, b < noj), from the radial sums.
+__device__ __forceinline__ void overlap_gradient(const double *W, int noi, int noj, const double *AB, const double *F,
+                                                 const double *D, double *g)
+{
+    const int ox[3] = { 2, 3, 1 };   // orbital of axis k: x -> px, y -> py, z -> pz
+    double radial = W[0] * D[0];
+    double wps[3] = { 0, 0, 0 }, wsp[3] = { 0, 0, 0 }, u[3] = { 0, 0, 0 }, v[3] = { 0, 0, 0 };
+    if (noi > 1) {
+        double s = 0.0;
+        for (int k = 0; k < 3; k++) { wps[k] = W[ox[k] * 4]; s += wps[k] * AB[k]; }
+        radial += s * D[1];
+    }
+    if (noj > 1) {
+        double s = 0.0;
+        for (int k = 0; k < 3; k++) { wsp[k] = W[ox[k]]; s += wsp[k] * AB[k]; }
+        radial -= s * D[2];
+    }
+    if (noi > 1 && noj > 1) {
+        double q = 0.0, tr = 0.0;
+        for (int k = 0; k < 3; k++) {
+            for (int l = 0; l < 3; l++) { const double w = W[ox[k] * 4 + ox[l]]; u[k] += w * AB[l]; v[l] += w * AB[k]; }
+            tr += W[ox[k] * 4 + ox[k]];
+        }
+        for (int k = 0; k < 3; k++) q += AB[k] * u[k];
+        radial += -q * D[3] + tr * D[4];
+    }
+    for (int k = 0; k < 3; k++) g[k] = AB[k] * radial - wps[k] * F[1] + wsp[k] * F[2] + (u[k] + v[k]) * F[3];
+}
