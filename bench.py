@@ -6,7 +6,8 @@ for molecular-dynamics frames).  One step = one full energy + gradient of every 
 (QC/MM potentials, integrals, SCF to 1e-8 on the density, QC and QC/MM gradients).
 
 value  frames / device time per step, inputs resident on the device (CUDA events on the launching stream);
-e2e    the same through System.EnergyBatch with host numpy inputs and results (host<->device copies timed).
+e2e    the same through System.EnergyBatch with the frames in pinned host memory and energies + gradients
+       returned to the host (host<->device copies inside the timed region).
 The working set per step (~4 MB per frame, >1 GB per batch) is far larger than L2, so no flush is needed.
 
 --impl reference times the CPU restatement of pDynamo's path (oracle/liboracle.so, built from mndo_oracle.c)
@@ -19,6 +20,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
 import numpy as np
+
+# DRAM bytes (read + write) of one k_scf launch on this workload (304 frames), from the ncu capture summarised
+# in profiles/k_scf_dram_304frames.md; per launch, like `achieved`.
+K_SCF_DRAM_BYTES_304 = 4.85e9 + 4.10e9
 
 METRIC = "QC/MM E+grad evals/s (AM1 RHF, 65 QC atoms in 4000 TIP3P waters, ABFS 8/12 A)"
 UNIT = "evals/s"
@@ -70,6 +75,22 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for s in self.samples for k in range(4) if s[2 + k].lower().startswith("active")})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None, "reasons": reasons}
+
+
+def fp64_peak_tflops(dev, n=4096, reps=3):
+    """cuBLAS DGEMM throughput (torch.matmul, float64, n^3), best of reps: the FP64 roofline peak."""
+    import torch
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(); torch.matmul(a, b); e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
 def workload(n_frames, seed=1):
@@ -185,62 +206,60 @@ def main():
         r = step()
     e1.record(stream)
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     ms = e0.elapsed_time(e1) / args.steps
-    # per-kernel timing of the dominant kernel (the SCF), events on the same stream
-    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    from pdynamo_mirror_gb300.parameters import ANGSTROMS_TO_BOHRS
-    import ctypes
-    xyz_bohr = (qc * ANGSTROMS_TO_BOHRS).contiguous()
-    ws = eng.workspace(len(frames))
-    opts = conv.options()
-    dens = torch.empty_like(eng.density)
-    en = torch.empty_like(r["energies"]); stt = torch.empty_like(r["status"]); nc = torch.empty_like(r["ncycles"])
-    sh = _native.stream_handle(stream)
-    k0.record(stream)
-    _native.check(eng.L.pdg_energy_gradients(eng.handle, len(frames), _native.ptr(xyz_bohr), _native.ptr(r["phi"]), ctypes.byref(opts),
-                                             _native.ptr(dens), 0, _native.ptr(en), None, None, _native.ptr(stt), _native.ptr(nc),
-                                             _native.ptr(ws), ws.numel(), sh), "scf timing")
-    k1.record(stream)
-    torch.cuda.synchronize()
-    scf_ms = k0.elapsed_time(k1)
     clk = clocks.stop()
+    # the dominant kernel alone: k_scf through pdg_scf on the integrals the last step left in the workspace
+    # (same frames, cold guess), CUDA events on the launching stream
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    scf_times = []
+    for _ in range(3):
+        k0.record(stream)
+        _, stt, nc = eng.scf(conv, phi=r["phi"], use_density=False)
+        k1.record(stream)
+        torch.cuda.synchronize()
+        scf_times.append(k0.elapsed_time(k1))
+    scf_ms = float(np.median(scf_times))
     if world > 1:
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     n_total = len(frames) * world
     value = n_total / (ms * 1e-3)
-    # e2e through the public API with host inputs and results
+    # e2e through the public API: frames from pinned host memory in, energies and gradients out
+    frames_h = torch.from_numpy(np.ascontiguousarray(frames)).pin_memory()
     te = []
     for k in range(2 + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        E, G, terms = s.EnergyBatch(frames, doGradients=True, warmStart=False)
+        E, G, terms = s.EnergyBatch(frames_h, doGradients=True, warmStart=False)
         torch.cuda.synchronize()
         if k >= 2:
             te.append(time.perf_counter() - t0)
     e2e = n_total / (sum(te) / len(te))
-    # FP64 roofline of the SCF kernel: algorithmic FP64 flops per frame-cycle
-    N, nocc, kv = eng.n_basis, eng.n_occupied, min(eng.n_occupied, eng.n_basis - eng.n_occupied)
-    cyc = float(ncyc.mean()) + 1.0
-    flops_cycle = 2.0 * N ** 3 + (4.0 / 3.0) * N ** 3 + 4.0 * N * N * kv + 2.0 * N * N * kv
-    scf_flops = flops_cycle * cyc * len(frames)
+    # FP64 roofline of k_scf.  Algorithmic FP64 flops of this SCF per frame: every density
+    # step (4/3) N^3 tridiagonalisation + 2 N^2 kv back-transformation + N^2 kv density; every DIIS save
+    # 4 N^2 kv (the commutator through the orbital factor).  Density steps = SCF cycles + 1.
+    N, kv = eng.n_basis, min(eng.n_occupied, eng.n_basis - eng.n_occupied)
+    ncyc_f = float(ncyc.mean())
+    scf_flops = len(frames) * ((ncyc_f + 1.0) * ((4.0 / 3.0) * N ** 3 + 3.0 * N * N * kv) + ncyc_f * 4.0 * N * N * kv)
     achieved_tf = scf_flops / (scf_ms * 1e-3) / 1e12
-    pk = peaks()
-    fp64_peak = 1.25
+    fp64_peak = fp64_peak_tflops(dev)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded water box, perturbed frames)",
             "config": {"workload": "qcmm_water_box_am1_abfs", "qc_atoms": len(sel), "mm_atoms": len(Z) - len(sel),
                        "basis_functions": N, "frames_per_step": len(frames), "method": "plain FP64",
-                       "density_tolerance": conv.densityTolerance, "mean_scf_cycles": float(ncyc.mean()),
+                       "density_tolerance": conv.densityTolerance, "mean_scf_cycles": ncyc_f,
                        "l2": "working set > L2 (no flush needed)"},
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(frames.nbytes),
-                    "d2h_bytes_per_step": int(E.nbytes + G.nbytes)},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(frames_h.numel() * 8),
+                    "d2h_bytes_per_step": int(G.nbytes + len(frames) * (_native.NENERGY + 2) * 8)},
             "gpu_launches": 8 * args.steps,
             "roofline": {"bound": "fp64", "kernel": "k_scf", "achieved": achieved_tf, "peak": fp64_peak, "unit": "TFLOP/s",
-                         "frac": achieved_tf / fp64_peak, "traffic": None,
-                         "note": "GB300 FP64 nominal 1.25 TFLOP/s (no measured FP64 peak in MEASURED_PEAKS.json); k_scf %.2f ms of a %.2f ms step" % (scf_ms, ms)},
+                         "frac": achieved_tf / fp64_peak, "traffic": K_SCF_DRAM_BYTES_304 if len(frames) == 304 else None,
+                         "note": "peak = cuBLAS DGEMM 4096^3 measured in this run (of measured; MEASURED_PEAKS.json has no FP64 figure); "
+                                 "k_scf %.2f ms per %d-frame launch, step %.2f ms" % (scf_ms, len(frames), ms)},
             "clocks": clk}
     if rank == 0 and not args.no_cpu_baseline:
         n = min(len(frames), 96)

@@ -121,6 +121,14 @@ int pdg_energy_gradients(pdg_system *sys, int n_frames, const double *d_xyz, con
                          double *d_energies, double *d_gradients, double *d_charges, int *d_status,
                          int *d_ncycles, void *d_workspace, size_t workspace_bytes, void *stream);
 
+/* The SCF alone, on the integrals a previous pdg_energy_gradients / pdg_one_electron / pdg_fock call left
+ * in this workspace for the same frames and geometry (QCModel.Energy's loop, pMolecule.QCModel.pyx:160-170,
+ * without QCModelMNDO_Integrals): e.g. to converge again with other options or other QC/MM potentials.
+ * Arguments as pdg_energy_gradients; no gradients. */
+int pdg_scf(pdg_system *sys, int n_frames, const double *d_phi, const pdg_scf_options *options, double *d_density,
+            int use_density, double *d_energies, double *d_charges, int *d_status, int *d_ncycles,
+            void *d_workspace, size_t workspace_bytes, void *stream);
+
 /* Diagnostics for parity tests: the one-electron matrix H (n_frames * N * N) and the Fock matrix
  * F = H + G(P) - phi for given densities (QCModelMNDO_Fock + QCMMFockLowdin on one density), with
  * the energies of that density in d_energies. */

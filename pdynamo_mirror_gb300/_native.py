@@ -15,7 +15,7 @@ EN_TOTAL_ELECTRONIC, EN_ELECTRONIC, EN_NUCLEAR, EN_BASELINE, EN_QCMM, EN_ONE_ELE
 MAX_HISTORY = 16
 
 EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system_info", "pdg_workspace_bytes",
-           "pdg_energy_gradients", "pdg_one_electron", "pdg_fock", "pdg_gradients", "pdg_qcmm_potentials",
+           "pdg_energy_gradients", "pdg_scf", "pdg_one_electron", "pdg_fock", "pdg_gradients", "pdg_qcmm_potentials",
            "pdg_qcmm_gradients", "pdg_scf_timings", "pdg_gradients_static_scratch", "pdg_last_error")
 TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densities Tridiagonal", "QC Densities Eigenvalues",
           "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds")
@@ -52,6 +52,7 @@ def load(path=LIB_PATH):
     L.pdg_workspace_bytes.argtypes = [P, I]
     L.pdg_workspace_bytes.restype = S
     L.pdg_energy_gradients.argtypes = [P, I, P, P, ctypes.POINTER(SCFOptions), P, I, P, P, P, P, P, P, S, P]
+    L.pdg_scf.argtypes = [P, I, P, ctypes.POINTER(SCFOptions), P, I, P, P, P, P, P, S, P]
     L.pdg_one_electron.argtypes = [P, I, P, P, P, S, P]
     L.pdg_fock.argtypes = [P, I, P, P, P, P, P, P, S, P]
     L.pdg_gradients.argtypes = [P, I, P, P, P, P, S, P]

@@ -184,6 +184,21 @@ extern "C" int pdg_energy_gradients(pdg_system *s, int n_frames, const double *d
     return PDG_OK;
 }
 
+extern "C" int pdg_scf(pdg_system *s, int n_frames, const double *d_phi, const pdg_scf_options *o, double *d_density,
+                       int use_density, double *d_energies, double *d_charges, int *d_status, int *d_ncycles,
+                       void *ws, size_t bytes, void *stream)
+{
+    int rc = check_workspace(s, n_frames, ws, bytes);
+    if (rc) return rc;
+    if (!o || !d_density || !d_energies || !d_status) return fail(PDG_BAD_ARGUMENT, "null argument");
+    if (o->history < 1 || o->history > PDG_MAX_HISTORY) return fail(PDG_BAD_ARGUMENT, "history must be 1..16");
+    if (o->maximum_scf_cycles < 0) return fail(PDG_BAD_ARGUMENT, "maximum_scf_cycles must be >= 0");
+    FramePlan p = plan_for(s, PDG_MAX_HISTORY);
+    launch_scf(s->d, p, n_frames, d_phi, *o, d_density, use_density, d_energies, d_charges, d_status, d_ncycles, (double *)ws, 0,
+               nullptr, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "scf kernel");
+}
+
 extern "C" int pdg_one_electron(pdg_system *s, int n_frames, const double *d_xyz, double *d_h, void *ws, size_t bytes, void *stream)
 {
     int rc = check_workspace(s, n_frames, ws, bytes);

@@ -112,6 +112,20 @@ class QCEngine:
             out.update(qcmm_qc_gradients=gqc, qcmm_mm_gradients=gmm)
         return out
 
+    def scf(self, converger, phi=None, use_density=False):
+        """pdg_scf: the SCF alone on the integrals of the last run (same frames); returns (energies, status,
+        ncycles) device tensors and updates self.density."""
+        F = self.density.shape[0]
+        ws = self.workspace(F)
+        energies = torch.empty((F, _native.NENERGY), dtype=torch.float64, device=self.device)
+        status = torch.empty(F, dtype=torch.int32, device=self.device)
+        ncycles = torch.empty(F, dtype=torch.int32, device=self.device)
+        opts = converger.options()
+        _native.check(self.L.pdg_scf(self.handle, F, _native.ptr(phi), ctypes.byref(opts), _native.ptr(self.density), 1 if use_density else 0,
+                                     _native.ptr(energies), None, _native.ptr(status), _native.ptr(ncycles), _native.ptr(ws), ws.numel(),
+                                     _native.stream_handle(torch.cuda.current_stream(self.device))), "pdg_scf")
+        return energies, status, ncycles
+
     def timings(self, n_frames):
         """Per-frame SCF phase timings (GPU clock cycles) of the last run, as {name: array}."""
         out = torch.empty((n_frames, len(_native.TIMERS)), dtype=torch.float64, device=self.device)

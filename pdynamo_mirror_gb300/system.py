@@ -77,46 +77,83 @@ class System:
             self._engine = QCEngine(self.qcModel.mndoModel, qcZ, self.electronicState.charge)
         return self._engine
 
+    def _selections(self):
+        """Device index data of the QC and MM atoms, cached per model definition: a slice when the atoms are
+        one contiguous range (no gather), else an index tensor."""
+        key = (id(self._engine), tuple(self.qcSelection), self.nbModel is not None)
+        if getattr(self, "_sel_key", None) != key:
+            dev = self.engine().device
+
+            def sel(idx):
+                if not idx:
+                    return None
+                if idx == list(range(idx[0], idx[-1] + 1)):
+                    return slice(idx[0], idx[-1] + 1)
+                return torch.as_tensor(idx, dtype=torch.long, device=dev)
+
+            mm_idx = self.mm_indices() if self.nbModel is not None else []
+            q = torch.as_tensor(self.mmCharges[mm_idx], dtype=torch.float64, device=dev).contiguous() if mm_idx else None
+            self._sel = (sel(self.qcSelection), sel(mm_idx), q, mm_idx)
+            self._sel_key = key
+        return self._sel
+
+    @staticmethod
+    def _take(X, s):
+        return X[:, s].contiguous() if isinstance(s, slice) else X.index_select(1, s)
+
     def _device_inputs(self, frames):
+        """frames: [F, n, 3] host (numpy or torch, ideally pinned) or device tensor.  One copy to the device,
+        QC/MM split on the device."""
         dev = self.engine().device
-        qc = torch.as_tensor(frames[:, self.qcSelection, :], dtype=torch.float64).to(dev, non_blocking=True).contiguous()
-        mm_idx = self.mm_indices() if self.nbModel is not None else []
-        if mm_idx:
-            mm = torch.as_tensor(frames[:, mm_idx, :], dtype=torch.float64).to(dev, non_blocking=True).contiguous()
-            q = torch.as_tensor(self.mmCharges[mm_idx], dtype=torch.float64).to(dev).contiguous()
-        else:
-            mm = q = None
+        X = frames if isinstance(frames, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(frames, dtype=np.float64))
+        X = X.to(device=dev, dtype=torch.float64, non_blocking=True)
+        qs, ms, q, mm_idx = self._selections()
+        qc = self._take(X, qs)
+        mm = self._take(X, ms) if ms is not None else None
         return qc, mm, q, mm_idx
 
     def EnergyBatch(self, frames, doGradients=True, warmStart=True):
-        """frames [F, n_atoms, 3] (Angstrom).  Returns (energies kJ/mol [F], gradients kJ/mol/A [F, n, 3] or None,
-        terms dict of [F] arrays).  Raises SCFNotConverged if any frame fails to converge."""
+        """frames [F, n_atoms, 3] (Angstrom; numpy array or torch tensor, host or device).  Returns (energies
+        kJ/mol [F], gradients kJ/mol/A [F, n, 3] or None, terms dict of [F] arrays).  Raises SCFNotConverged
+        if any frame fails to converge."""
         if self.qcModel is None:
             raise ValueError("No QC model defined.")
-        frames = np.asarray(frames, dtype=np.float64)
+        if not isinstance(frames, torch.Tensor):
+            frames = np.asarray(frames, dtype=np.float64)
         if frames.ndim == 2:
             frames = frames[None]
         eng = self.engine()
         qc, mm, q, mm_idx = self._device_inputs(frames)
         r = eng.run(qc, self.qcModel.converger, mm, q, self.nbModel if mm is not None else None, gradients=doGradients,
                     warm_start=warmStart)
-        E = r["energies"].cpu().numpy()
-        st = r["status"].cpu().numpy()
+        F = qc.shape[0]
+        # one device -> host copy of the small per-frame results
+        small = torch.cat([r["energies"], r["status"].to(torch.float64)[:, None], r["ncycles"].to(torch.float64)[:, None]], 1)
+        G = None
+        if doGradients:
+            qs, ms, _, _ = self._selections()
+            Gd = torch.zeros((F, len(self.atomicNumbers), 3), dtype=torch.float64, device=eng.device)
+            gq = r["qc_gradients"]
+            if "qcmm_qc_gradients" in r:
+                gq = gq + r["qcmm_qc_gradients"]
+                Gd[:, ms] = r["qcmm_mm_gradients"]
+            Gd[:, qs] = gq
+            Gd *= GRADIENT_TO_KJ_PER_A
+            Gh = torch.empty(Gd.shape, dtype=torch.float64, pin_memory=True)
+            Gh.copy_(Gd, non_blocking=True)
+        small = small.cpu().numpy()
+        if doGradients:
+            torch.cuda.current_stream(eng.device).synchronize()
+            G = Gh.numpy()
+        E = small[:, :_native.NENERGY]
+        st = small[:, _native.NENERGY].astype(np.int32)
         pure = HARTREES_TO_KJ * (E[:, _native.EN_ELECTRONIC] + E[:, _native.EN_NUCLEAR] + E[:, _native.EN_BASELINE])
         qcmm = HARTREES_TO_KJ * E[:, _native.EN_QCMM]
-        terms = {"Pure QC": pure, "QC/MM Elect.": qcmm, "SCF Cycles": r["ncycles"].cpu().numpy(), "Status": st}
+        terms = {"Pure QC": pure, "QC/MM Elect.": qcmm, "SCF Cycles": small[:, _native.NENERGY + 1].astype(np.int32), "Status": st}
         if (st != _native.PDG_OK).any():
             self._engine.density = None
             raise SCFNotConverged("SCF procedure not converged.")
         total = pure + (qcmm if mm is not None else 0.0)
-        G = None
-        if doGradients:
-            G = np.zeros(frames.shape)
-            gq = r["qc_gradients"]
-            if "qcmm_qc_gradients" in r:
-                gq = gq + r["qcmm_qc_gradients"]
-                G[:, mm_idx, :] = (r["qcmm_mm_gradients"] * GRADIENT_TO_KJ_PER_A).cpu().numpy()
-            G[:, self.qcSelection, :] = (gq * GRADIENT_TO_KJ_PER_A).cpu().numpy()
         return total, G, terms
 
     def Energy(self, doGradients=False, log=None):

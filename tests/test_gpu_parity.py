@@ -214,3 +214,20 @@ def test_qcmm_water_box_energy_matches_oracle():
     g = s.configuration.gradients3 / (A2B * KJ)
     assert np.abs(g[:nq] - (r["gradients"] + gq)).max() < G_TOL
     assert np.abs(g[nq:] - gm).max() < G_TOL
+
+
+def test_scf_alone_reproduces_energy_gradients():
+    """pdg_scf on the integrals left by pdg_energy_gradients gives the same converged energies."""
+    import torch
+    from pdynamo_mirror_gb300 import DIISSCFConverger, workloads
+    from pdynamo_mirror_gb300.engine import QCEngine
+    Z, X = workloads.water_cluster(8, seed=21)
+    frames = workloads.perturbed_frames(X, 3, sigma=0.03, seed=22)
+    eng = QCEngine("am1", Z, 0)
+    conv = DIISSCFConverger()
+    out = eng.run(_dev(frames), conv, gradients=False, warm_start=False)
+    e1 = out["energies"].cpu().numpy()
+    e2, st, nc = eng.scf(conv)
+    assert (st.cpu().numpy() == 0).all()
+    np.testing.assert_allclose(e2.cpu().numpy()[:, :7], e1[:, :7], rtol=0, atol=1e-12)
+    assert (nc.cpu().numpy() == out["ncycles"].cpu().numpy()).all()
