@@ -94,6 +94,17 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     ints.insert(ints.end(), pt.begin(), pt.end());
     ints.insert(ints.end(), ovl_off.begin(), ovl_off.end());
     ints.insert(ints.end(), ovl_n.begin(), ovl_n.end());
+    // Fock output lists: diagonal-block elements per atom; off-diagonal-block elements sorted by pair class
+    std::vector<int> cel, xel;
+    for (int a = 0; a < n_atoms; a++)
+        for (int ab = 0; ab < norb[a] * (norb[a] + 1) / 2; ab++) cel.push_back(a << 4 | ab);
+    for (int cls = 16; cls >= 1; cls--)
+        for (int p = 0; p < npairs; p++)
+            if (norb[pi[p]] * norb[pj[p]] == cls)
+                for (int k = 0; k < cls; k++) xel.push_back(p << 4 | k);
+    const size_t cel_at = ints.size();
+    ints.insert(ints.end(), cel.begin(), cel.end());
+    ints.insert(ints.end(), xel.begin(), xel.end());
     int rc = PDG_OK;
     if ((rc = cuda_check(cudaMalloc(&s->d_elements, sizeof(double) * s->elements.size()), "cudaMalloc elements")) ||
         (rc = cuda_check(cudaMalloc(&s->d_terms, sizeof(double) * terms.size()), "cudaMalloc terms")) ||
@@ -116,6 +127,7 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     d.atom_elem = b; d.atom_start = b + n_atoms; d.atom_norb = b + 2 * n_atoms;
     d.pair_i = b + 3 * n_atoms; d.pair_j = d.pair_i + npairs; d.pair_tei = d.pair_j + npairs;
     d.ovl = s->d_ovl; d.ovl_off = d.pair_tei + npairs; d.ovl_n = d.ovl_off + n_elements * n_elements;
+    d.cel = b + cel_at; d.xel = d.cel + cel.size(); d.n_cel = (int)cel.size(); d.n_xel = (int)xel.size();
     *out = s;
     return PDG_OK;
 }

@@ -27,6 +27,8 @@ struct DeviceSystem {
     const double *terms;           // multipole (o, a) tables per ordered element pair (multipole.cuh)
     const double *ovl;             // overlap primitive records (overlap.cuh), all ordered element pairs
     const int *ovl_off, *ovl_n;    // per ordered element pair: first record, record count
+    const int *cel, *xel;          // Fock outputs: diagonal-block elements (atom << 4 | mn), off-diagonal (pair << 4 | ac)
+    int n_cel, n_xel;
 };
 
 // Per-frame workspace plan (all offsets in doubles from the frame's base).

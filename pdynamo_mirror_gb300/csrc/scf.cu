@@ -14,6 +14,7 @@
 // GB300's FP64 rate (~2 DFMA/clk/SM) makes this arithmetic-bound; the dense products run as register-tiled
 // shared-memory GEMMs and everything sequential is confined to O(N) or O(N^2) work.
 #include "common.cuh"
+#include "multipole.cuh"
 
 
 struct SCFArgs {
@@ -25,7 +26,7 @@ struct SCFArgs {
 };
 
 struct Smem {
-    double *red, *small, *d, *e, *e2, *tau, *eig, *v, *v2, *p, *w, *dot;
+    double *red, *small, *d, *e, *e2, *tau, *eig, *v, *v2, *p, *w, *part, *dot;
     double *ta, *tb;   // GEMM staging
     double *amat;      // packed lower triangle of the matrix being tridiagonalised (null: in the workspace)
     double *zs;        // the wanted eigenvectors, one row of ldz per vector (null: in the workspace)
@@ -40,14 +41,14 @@ struct Smem {
 #define GA_LD (GM + 1)
 #define GB_LD (GN + 1)
 
-// Shared memory plan: red | small | d e e2 tau eig v v2 p w (9N) | dot | ints | GEMM staging | amat | zs.
+// Shared memory plan: red | small | d e e2 tau eig v v2 p w (9N) | part (4N) | dot | ints | GEMM staging | amat | zs.
 // The packed matrix goes to shared memory when it fits, then the eigenvectors.
 struct SmemPlan { size_t head, work, amat, zs, bytes; int ldz; };
 
 __host__ __device__ inline SmemPlan smem_plan(int N, int kv)
 {
     SmemPlan p;
-    p.head = 32 + 256 + 9 * (size_t)N + 64 + ((64 + (size_t)N + 2) * sizeof(int) + 7) / 8;
+    p.head = 32 + 256 + 13 * (size_t)N + 64 + ((64 + (size_t)N + 2) * sizeof(int) + 7) / 8;
     p.work = (size_t)GK * GA_LD + (size_t)GK * GB_LD;
     p.ldz = N | 1;
     const size_t limit = 220 * 1024 / 8, packed = (size_t)N * (N + 1) / 2, zsz = (size_t)(kv > 0 ? kv : 1) * p.ldz;
@@ -63,7 +64,7 @@ __device__ __forceinline__ Smem carve(double *base, int N, int kv)
     SmemPlan sp = smem_plan(N, kv);
     m.red = base; m.small = base + 32;
     m.d = m.small + 256; m.e = m.d + N; m.e2 = m.e + N; m.tau = m.e2 + N; m.eig = m.tau + N;
-    m.v = m.eig + N; m.v2 = m.v + N; m.p = m.v2 + N; m.w = m.p + N; m.dot = m.w + N;
+    m.v = m.eig + N; m.v2 = m.v + N; m.p = m.v2 + N; m.w = m.p + N; m.part = m.w + N; m.dot = m.part + 4 * (size_t)N;
     m.iv = (int *)(m.dot + 64);
     double *work = base + sp.head;
     m.ta = work; m.tb = work + GK * GA_LD;
@@ -130,41 +131,31 @@ __device__ void fock_build(const SCFArgs &a, int f, const double *H, const doubl
 {
     const DeviceSystem &s = a.s;
     const int N = s.n_basis, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    // diagonal blocks: one-centre G plus Coulomb from every partner atom
-    for (int A = w; A < s.n_atoms; A += PDG_WARPS) {
-        int no = s.atom_norb[A], as = s.atom_start[A], na = no * (no + 1) / 2;
-        double acc[10];
-        for (int k = 0; k < 10; k++) acc[k] = 0.0;
-        for (int B = lane; B < s.n_atoms; B += 32) {
-            if (B == A) continue;
-            int hi = A > B ? A : B, lo = A > B ? B : A;
-            int p = hi * (hi - 1) / 2 + lo;
-            int nob = s.atom_norb[B], bs = s.atom_start[B], nb = nob * (nob + 1) / 2;
-            double pb[10];
-            for (int cd = 0; cd < nb; cd++) {
-                int c = cd == 0 ? 0 : (cd < 3 ? 1 : (cd < 6 ? 2 : 3)), dd = cd - c * (c + 1) / 2;
-                pb[cd] = (c == dd ? 1.0 : 2.0) * P[(size_t)(bs + c) * N + bs + dd];
-            }
-            const double *blk = tei + s.pair_tei[p];
-            if (A > B) {   // A holds the rows of the block
-                for (int ab = 0; ab < na; ab++) {
-                    double t = 0.0;
-                    for (int cd = 0; cd < nb; cd++) t += blk[ab * nb + cd] * pb[cd];
-                    acc[ab] += t;
-                }
-            } else {
-                for (int cd = 0; cd < na; cd++) {
-                    double t = 0.0;
-                    for (int ab = 0; ab < nb; ab++) t += blk[ab * na + cd] * pb[ab];
-                    acc[cd] += t;
+    // One flat pass, one thread per output element (lists built by pdg_system_create):
+    //  * diagonal-block element (A, m >= n): H + one-centre G + Coulomb sum_B sum_cd (mn|cd) P_B,cd over every
+    //    partner atom B (QCModelMNDO_Fock's one-centre terms and MakeFockG's Coulomb part);
+    //  * off-diagonal-block element (pair, a, c): F_ac = H_ac - 1/2 sum_bd (ab|cd) P_bd (exchange), the
+    //    elements sorted by pair class so that the lanes of a warp run the same loop lengths.
+    const int n_out = s.n_cel + s.n_xel;
+    for (int e = threadIdx.x; e < n_out; e += PDG_BLOCK) {
+        if (e < s.n_cel) {
+            const int A = s.cel[e] >> 4, ab = s.cel[e] & 15;
+            const int no = s.atom_norb[A], as = s.atom_start[A], na = no * (no + 1) / 2;
+            const int m = MP_DA[ab], n = MP_DB[ab];   // m >= n
+            double acc = 0.0;
+            for (int B = 0; B < s.n_atoms; B++) {
+                if (B == A) continue;
+                const int hi = A > B ? A : B, lo = A > B ? B : A, pp = hi * (hi - 1) / 2 + lo;
+                const int nob = s.atom_norb[B], bs = s.atom_start[B], nb = nob * (nob + 1) / 2;
+                const double *blk = tei + s.pair_tei[pp];
+                for (int cd = 0; cd < nb; cd++) {
+                    const int c = MP_DA[cd], d = MP_DB[cd];
+                    const double pb = (c == d ? 1.0 : 2.0) * P[(size_t)(bs + c) * N + bs + d];
+                    acc = fma(A > B ? blk[ab * nb + cd] : blk[cd * na + ab], pb, acc);
                 }
             }
-        }
-        for (int k = 0; k < na; k++) acc[k] = warp_sum(acc[k]);
-        if (lane < no * no) {
-            int m = lane / no, n = lane % no;
             const double *E = elem(s, s.atom_elem[A]);
-            double gss = E[PDG_E_GSS], gsp = E[PDG_E_GSP], gpp = E[PDG_E_GPP], gp2 = E[PDG_E_GP2], hsp = E[PDG_E_HSP], hpp = E[PDG_E_HPP];
+            const double gss = E[PDG_E_GSS], gsp = E[PDG_E_GSP], gpp = E[PDG_E_GPP], gp2 = E[PDG_E_GP2], hsp = E[PDG_E_HSP], hpp = E[PDG_E_HPP];
             const double *PA = P + (size_t)as * N + as;
             double g = 0.0;
             if (no == 1) g = 0.5 * PA[0] * gss;
@@ -172,29 +163,26 @@ __device__ void fock_build(const SCFArgs &a, int f, const double *H, const doubl
             else if (m == n) {
                 g = PA[0] * (gsp - 0.5 * hsp) + 0.5 * PA[m * N + m] * gpp;
                 for (int q = 1; q < 4; q++) if (q != m) g += PA[q * N + q] * (gp2 - 0.5 * hpp);
-            } else if (m == 0 || n == 0) g = PA[m * N + n] * (1.5 * hsp - 0.5 * gsp);
+            } else if (n == 0) g = PA[m * N + n] * (1.5 * hsp - 0.5 * gsp);
             else g = PA[m * N + n] * (1.5 * hpp - 0.5 * gp2);
-            int idx = (m >= n) ? m * (m + 1) / 2 + n : n * (n + 1) / 2 + m;
-            F[(size_t)(as + m) * N + as + n] = H[(size_t)(as + m) * N + as + n] + g + acc[idx];
-        }
-    }
-    // off-diagonal blocks: exchange, F_ac = H_ac - 1/2 sum_bd (ab|cd) P_bd
-    for (int p = w; p < s.n_pairs; p += PDG_WARPS) {
-        int i = s.pair_i[p], j = s.pair_j[p];
-        int noi = s.atom_norb[i], noj = s.atom_norb[j], is = s.atom_start[i], js = s.atom_start[j];
-        int nj = noj * (noj + 1) / 2;
-        const double *blk = tei + s.pair_tei[p];
-        if (lane < noi * noj) {
-            int aa = lane / noj, c = lane % noj;
+            const double v = H[(size_t)(as + m) * N + as + n] + g + acc;
+            F[(size_t)(as + m) * N + as + n] = v;
+            F[(size_t)(as + n) * N + as + m] = v;
+        } else {
+            const int x = s.xel[e - s.n_cel], pp = x >> 4, lid = x & 15;
+            const int i = s.pair_i[pp], j = s.pair_j[pp];
+            const int noi = s.atom_norb[i], noj = s.atom_norb[j], is = s.atom_start[i], js = s.atom_start[j];
+            const int nj = noj * (noj + 1) / 2, aa = lid / noj, c = lid % noj;
+            const double *blk = tei + s.pair_tei[pp];
             double t = 0.0;
             for (int b = 0; b < noi; b++) {
-                int ab = aa >= b ? aa * (aa + 1) / 2 + b : b * (b + 1) / 2 + aa;
+                const int ab = aa >= b ? aa * (aa + 1) / 2 + b : b * (b + 1) / 2 + aa;
                 for (int d = 0; d < noj; d++) {
-                    int cd = c >= d ? c * (c + 1) / 2 + d : d * (d + 1) / 2 + c;
-                    t += blk[ab * nj + cd] * P[(size_t)(is + b) * N + js + d];
+                    const int cd = c >= d ? c * (c + 1) / 2 + d : d * (d + 1) / 2 + c;
+                    t = fma(blk[ab * nj + cd], P[(size_t)(is + b) * N + js + d], t);
                 }
             }
-            double v = H[(size_t)(is + aa) * N + js + c] - 0.5 * t;
+            const double v = fma(-0.5, t, H[(size_t)(is + aa) * N + js + c]);
             F[(size_t)(is + aa) * N + js + c] = v;
             F[(size_t)(js + c) * N + is + aa] = v;
         }
@@ -222,32 +210,54 @@ __device__ void fock_build(const SCFArgs &a, int f, const double *H, const doubl
 }
 
 // ----------------------------------------------------------------------------------------------------
-// Small dense solve by thread 0 (partial pivoting); rejects a reciprocal 1-norm condition below 1e-15
-// (SymmetricMatrix_SolveLinearEquations' test, SymmetricMatrix.c:1412-1450).
-__device__ bool small_solve(int n, double *A, double *b)
+// Small dense solve A x = b (n <= 17) by one warp: Gauss-Jordan with partial pivoting on [A | I | b] in
+// shared memory M (n x (2n+1)), lanes over columns; rejects a reciprocal 1-norm condition below 1e-15
+// (SymmetricMatrix_SolveLinearEquations' test, SymmetricMatrix.c:1412-1450, computed exactly from the
+// inverse).  A(i, j) and b(i) are accessors; the solution is returned in x (lanes < n hold x[lane]).
+template <typename FA, typename FB>
+__device__ bool warp_small_solve(int n, FA A, FB b, double *M, double *x)
 {
-    double M[17][17], Inv[17][17], x[17], anorm = 0.0;
-    for (int j = 0; j < n; j++) { double t = 0.0; for (int i = 0; i < n; i++) t += fabs(A[i * n + j]); anorm = fmax(anorm, t); }
-    for (int i = 0; i < n; i++) { x[i] = b[i]; for (int j = 0; j < n; j++) { M[i][j] = A[i * n + j]; Inv[i][j] = (i == j); } }
-    for (int k = 0; k < n; k++) {
-        int pv = k;
-        for (int i = k + 1; i < n; i++) if (fabs(M[i][k]) > fabs(M[pv][k])) pv = i;
-        if (M[pv][k] == 0.0) return false;
-        if (pv != k) {
-            for (int j = 0; j < n; j++) { double t = M[k][j]; M[k][j] = M[pv][j]; M[pv][j] = t; t = Inv[k][j]; Inv[k][j] = Inv[pv][j]; Inv[pv][j] = t; }
-            double t = x[k]; x[k] = x[pv]; x[pv] = t;
-        }
-        for (int i = 0; i < n; i++) {
-            if (i == k) continue;
-            double fct = M[i][k] / M[k][k];
-            if (fct == 0.0) continue;
-            for (int j = 0; j < n; j++) { M[i][j] -= fct * M[k][j]; Inv[i][j] -= fct * Inv[k][j]; }
-            x[i] -= fct * x[k];
-        }
+    const int lane = threadIdx.x & 31, w2 = 2 * n + 1;
+    for (int e = lane; e < n * w2; e += 32) {
+        const int i = e / w2, j = e % w2;
+        M[e] = j < n ? A(i, j) : (j < 2 * n ? (j - n == i ? 1.0 : 0.0) : b(i));
     }
-    double inorm = 0.0;
-    for (int j = 0; j < n; j++) { double t = 0.0; for (int i = 0; i < n; i++) t += fabs(Inv[i][j] / M[i][i]); inorm = fmax(inorm, t); }
-    for (int i = 0; i < n; i++) b[i] = x[i] / M[i][i];
+    __syncwarp();
+    double cs = 0.0;
+    if (lane < n) for (int i = 0; i < n; i++) cs += fabs(M[i * w2 + lane]);
+    const double anorm = warp_max(cs);
+    bool ok = true;
+    for (int k = 0; k < n; k++) {
+        // pivot: the first row i >= k of largest |M[i][k]|
+        double v = (lane >= k && lane < n) ? fabs(M[lane * w2 + k]) : -1.0;
+        int iv = lane;
+        for (int o = 16; o > 0; o >>= 1) {
+            const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
+            const int i2 = __shfl_xor_sync(0xffffffffu, iv, o);
+            if (v2 > v || (v2 == v && i2 < iv)) { v = v2; iv = i2; }
+        }
+        if (v == 0.0) { ok = false; break; }
+        if (iv != k)
+            for (int j = lane; j < w2; j += 32) { const double t = M[k * w2 + j]; M[k * w2 + j] = M[iv * w2 + j]; M[iv * w2 + j] = t; }
+        __syncwarp();
+        const double r = 1.0 / M[k * w2 + k];
+        const double fi = lane < n ? M[lane * w2 + k] * r : 0.0;
+        const double pk0 = lane < w2 ? M[k * w2 + lane] : 0.0, pk1 = lane + 32 < w2 ? M[k * w2 + lane + 32] : 0.0;
+        __syncwarp();
+        for (int i = 0; i < n; i++) {
+            const double f = __shfl_sync(0xffffffffu, fi, i);
+            if (i == k) continue;
+            if (lane < w2) M[i * w2 + lane] = fma(-f, pk0, M[i * w2 + lane]);
+            if (lane + 32 < w2) M[i * w2 + lane + 32] = fma(-f, pk1, M[i * w2 + lane + 32]);
+        }
+        __syncwarp();
+    }
+    if (!ok) return false;
+    double ci = 0.0;
+    if (lane < n) for (int i = 0; i < n; i++) ci += fabs(M[i * w2 + n + lane] / M[i * w2 + i]);
+    const double inorm = warp_max(ci);
+    if (lane < n) x[lane] = M[lane * w2 + 2 * n] / M[lane * w2 + lane];
+    __syncwarp();
     return anorm * inorm < 1.0e15;
 }
 
@@ -318,8 +328,8 @@ __device__ void make_reflector(double *A, int N, int c, double *vout, Smem &sm)
 // warp never diverge; loads are issued in blocks of eight ahead of the dependent recurrence.
 __device__ void inverse_iteration(int N, int t, double sigma, double tiny, const double *__restrict__ d, const double *__restrict__ e,
                                   double *__restrict__ u0, double *__restrict__ u1, double *__restrict__ u2, double *__restrict__ lm,
-                                  unsigned char *__restrict__ pv, double *__restrict__ y, int ld, const double *zq0, int nq, int ldz,
-                                  double *__restrict__ zout)
+                                  unsigned char *__restrict__ pv, double *y, int ldy, int ld, const double *zq0, int nq, int ldz,
+                                  double *zout)
 {
     double ak = d[0] - sigma, bk = e[0];
     for (int k = 0; k < N - 1; k++) {
@@ -335,7 +345,7 @@ __device__ void inverse_iteration(int N, int t, double sigma, double tiny, const
     }
     if (fabs(ak) < tiny) ak = copysign(tiny, ak);
     u0[(size_t)(N - 1) * ld] = __drcp_rn(ak);
-    for (int i = 0; i < N; i++) y[(size_t)i * ld] = ((hash2(t * 2654435761u + 17u, i) >> 8) * (1.0 / 16777216.0)) * 2.0 - 1.0;
+    for (int i = 0; i < N; i++) y[(size_t)i * ldy] = ((hash2(t * 2654435761u + 17u, i) >> 8) * (1.0 / 16777216.0)) * 2.0 - 1.0;
     for (int it = 0; it < 4; it++) {
         // forward: interchanges and L
         double c = y[0];
@@ -343,43 +353,43 @@ __device__ void inverse_iteration(int N, int t, double sigma, double tiny, const
         for (; k + 8 <= N - 1; k += 8) {
             double xn[8], l[8]; bool sw[8];
 #pragma unroll
-            for (int q = 0; q < 8; q++) { xn[q] = y[(size_t)(k + 1 + q) * ld]; l[q] = lm[(size_t)(k + q) * ld]; sw[q] = pv[(size_t)(k + q) * ld]; }
+            for (int q = 0; q < 8; q++) { xn[q] = y[(size_t)(k + 1 + q) * ldy]; l[q] = lm[(size_t)(k + q) * ld]; sw[q] = pv[(size_t)(k + q) * ld]; }
 #pragma unroll
             for (int q = 0; q < 8; q++) {
                 const double yk = sw[q] ? xn[q] : c, cn = sw[q] ? c : xn[q];
-                y[(size_t)(k + q) * ld] = yk;
+                y[(size_t)(k + q) * ldy] = yk;
                 c = fma(-l[q], yk, cn);
             }
         }
         for (; k < N - 1; k++) {
-            const double xn = y[(size_t)(k + 1) * ld], l = lm[(size_t)k * ld];
+            const double xn = y[(size_t)(k + 1) * ldy], l = lm[(size_t)k * ld];
             const bool sw = pv[(size_t)k * ld];
             const double yk = sw ? xn : c, cn = sw ? c : xn;
-            y[(size_t)k * ld] = yk;
+            y[(size_t)k * ldy] = yk;
             c = fma(-l, yk, cn);
         }
         // back substitution with U
         double x1 = c * u0[(size_t)(N - 1) * ld], x2 = 0.0;
-        y[(size_t)(N - 1) * ld] = x1;
+        y[(size_t)(N - 1) * ldy] = x1;
         k = N - 2;
         for (; k - 7 >= 0; k -= 8) {
             double yy[8], a0[8], a1[8], a2[8];
 #pragma unroll
             for (int q = 0; q < 8; q++) {
                 const size_t o = (size_t)(k - q) * ld;
-                yy[q] = y[o]; a0[q] = u0[o]; a1[q] = u1[o]; a2[q] = u2[o];
+                yy[q] = y[(size_t)(k - q) * ldy]; a0[q] = u0[o]; a1[q] = u1[o]; a2[q] = u2[o];
             }
 #pragma unroll
             for (int q = 0; q < 8; q++) {
                 const double x0 = fma(-a2[q], x2, fma(-a1[q], x1, yy[q])) * a0[q];
-                y[(size_t)(k - q) * ld] = x0;
+                y[(size_t)(k - q) * ldy] = x0;
                 x2 = x1; x1 = x0;
             }
         }
         for (; k >= 0; k--) {
             const size_t o = (size_t)k * ld;
-            const double x0 = fma(-u2[o], x2, fma(-u1[o], x1, y[o])) * u0[o];
-            y[o] = x0;
+            const double x0 = fma(-u2[o], x2, fma(-u1[o], x1, y[(size_t)k * ldy])) * u0[o];
+            y[(size_t)k * ldy] = x0;
             x2 = x1; x1 = x0;
         }
         // the iterate is never rescaled between solves: four solves grow it by at most (1/tiny)^4, far
@@ -387,14 +397,14 @@ __device__ void inverse_iteration(int N, int t, double sigma, double tiny, const
         for (int q = 0; q < nq; q++) {
             const double *zq = zq0 + (size_t)q * ldz;
             double dt = 0.0;
-            for (int i = 0; i < N; i++) dt = fma(y[(size_t)i * ld], zq[i], dt);
-            for (int i = 0; i < N; i++) y[(size_t)i * ld] = fma(-dt, zq[i], y[(size_t)i * ld]);
+            for (int i = 0; i < N; i++) dt = fma(y[(size_t)i * ldy], zq[i], dt);
+            for (int i = 0; i < N; i++) y[(size_t)i * ldy] = fma(-dt, zq[i], y[(size_t)i * ldy]);
         }
     }
     double nr = 0.0;
-    for (int i = 0; i < N; i++) { const double v = y[(size_t)i * ld]; nr = fma(v, v, nr); }
+    for (int i = 0; i < N; i++) { const double v = y[(size_t)i * ldy]; nr = fma(v, v, nr); }
     const double sc = rsqrt(nr);
-    for (int i = 0; i < N; i++) zout[i] = y[(size_t)i * ld] * sc;
+    for (int i = 0; i < N; i++) zout[i] = y[(size_t)i * ldy] * sc;
 }
 
 __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, double *P, Smem &sm, Timer &tm)
@@ -419,35 +429,44 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
     for (int k = 0; k + 2 < N; k++) {
         const int m = N - k - 1, c0 = k + 1, R = (m + 31) >> 5;
         const double tau = sm.tau[k];
-        for (int rb = w; rb < R; rb += PDG_WARPS) {
-            const int i = rb * 32 + lane;
+        // items (row block rb, column segment q): Q segments per row so that short steps still spread over
+        // the four FP64 units; each item leaves its partial products and its partial p.v
+        const int Q = R >= 16 ? 1 : min(4, PDG_WARPS / R), seg = (m + Q - 1) / Q;
+        for (int item = w; item < R * Q; item += PDG_WARPS) {
+            const int rb = item % R, qs = item / R, i = rb * 32 + lane;
+            const int j0 = qs * seg, j1 = min(m, j0 + seg);
             double t = 0.0;
             if (i < m) {
                 const int bi = plo(c0 + i, c0);
-                int tj = plo(c0, c0);
-                for (int j = 0; j < m; j++) {
+                int tj = plo(c0 + j0, c0);
+                for (int j = j0; j < j1; j++) {
                     const int ad = (j <= i) ? bi + j : tj + i;
                     t = fma(A[ad], vc[j], t);
                     tj += c0 + j + 1;
                 }
-                t *= tau;
-                sm.p[i] = t;
+                sm.part[qs * N + i] = t;
             }
             const double pv = warp_sum(i < m ? t * vc[i] : 0.0);
-            if (lane == 0) sm.dot[rb] = pv;
+            if (lane == 0) sm.dot[item] = pv;
         }
         __syncthreads();
         for (int rb = w; rb < R; rb += PDG_WARPS) {
             double sdot = 0.0;
-            for (int q = lane; q < R; q += 32) sdot += sm.dot[q];
-            const double K = 0.5 * tau * warp_sum(sdot);
+            for (int q = lane; q < R * Q; q += 32) sdot += sm.dot[q];
+            const double K = 0.5 * tau * tau * warp_sum(sdot);   // K = tau (p.v) / 2 with p = tau A v
             const int i = rb * 32 + lane;
-            if (i < m) sm.w[i] = fma(-K, vc[i], sm.p[i]);
+            if (i < m) {
+                double t = 0.0;
+                for (int q = 0; q < Q; q++) t += sm.part[q * N + i];
+                const double p = tau * t;
+                sm.p[i] = p;
+                sm.w[i] = fma(-K, vc[i], p);
+            }
         }
         __syncthreads();
         if (w == 0) {
             const double v0 = vc[0], w0 = sm.w[0];
-            for (int i = lane; i < m; i += 32) { const int ad = plo(c0 + i, c0); A[ad] -= fma(vc[i], w0, sm.w[i] * v0); }
+            for (int i = lane; i < m; i += 32) { const int ad = plo(c0 + i, c0); A[ad] = fma(-vc[i], w0, fma(-sm.w[i], v0, A[ad])); }
             __syncwarp();
             if (lane == 0) sm.d[c0] = A[plo(c0, c0)];
             if (m >= 3) make_reflector(A, N, c0, vn, sm);
@@ -460,7 +479,7 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
                 while (ii * (ii + 1) / 2 > el) ii--;
                 const int i = ii + 1, j = el - ii * (ii + 1) / 2 + 1;
                 const int ad = plo(c0 + i, c0 + j);
-                A[ad] -= fma(vc[i], sm.w[j], sm.w[i] * vc[j]);
+                A[ad] = fma(-vc[i], sm.w[j], fma(-sm.w[i], vc[j], A[ad]));
             }
         }
         __syncthreads();
@@ -541,7 +560,8 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
             for (int t = tid; t < kv; t += PDG_BLOCK) {
                 const int cs = sm.iv[64 + t];
                 if (t - cs != r) continue;
-                inverse_iteration(N, t, sm.eig[t], tiny, sm.d, sm.e, U0 + t, U1 + t, U2 + t, LM + t, PV + t, Y + t, kvp,
+                double *y = sm.zs ? Z + (size_t)t * ldz : Y + t;   // in place in the output row when Z is in shared memory
+                inverse_iteration(N, t, sm.eig[t], tiny, sm.d, sm.e, U0 + t, U1 + t, U2 + t, LM + t, PV + t, y, sm.zs ? 1 : kvp, kvp,
                                   Z + (size_t)cs * ldz, t - cs, ldz, Z + (size_t)t * ldz);
             }
             __syncthreads();
@@ -587,7 +607,7 @@ __global__ void __launch_bounds__(PDG_BLOCK, 1) k_scf(SCFArgs a)
     extern __shared__ double shm[];
     const DeviceSystem &s = a.s;
     const FramePlan &pl = a.plan;
-    const int f = blockIdx.x, tid = threadIdx.x, N = s.n_basis;
+    const int f = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5, N = s.n_basis;
     const size_t NN = (size_t)N * N;
     Smem sm = carve(shm, N, s.n_vec);
     double *wsf = a.ws + (size_t)f * pl.stride;
@@ -706,40 +726,47 @@ __global__ void __launch_bounds__(PDG_BLOCK, 1) k_scf(SCFArgs a)
                     else if (iteration > 1 && qrca && maxerr < o.diis_onset) { qdiis = 1; qrca = 0; }
                 }
                 if (qdiis) {
-                    if (tid == 0) {   // DIIS_Iterate: bordered solve, drop the oldest until well conditioned
-                        int mn = ctl[1];
-                        ctl[21] = 0;
+                    if (w == 0) {   // DIIS_Iterate: bordered solve, drop the oldest until well conditioned (warp 0)
+                        int mn = ctl[1], good = 0;
                         while (mn > 1) {
-                            int n1 = mn + 1;
-                            double Am[17 * 17], bv[17];
-                            for (int i = 0; i < n1 * n1; i++) Am[i] = 0.0;
-                            for (int i = 0; i < mn; i++)
-                                for (int j = 0; j < mn; j++) Am[i * n1 + j] = Bm[ctl[2 + i] * PDG_MAX_HISTORY + ctl[2 + j]];
-                            for (int i = 0; i < mn; i++) { Am[mn * n1 + i] = -1.0; Am[i * n1 + mn] = -1.0; bv[i] = 0.0; }
-                            bv[mn] = -1.0;
-                            bool ok = small_solve(n1, Am, bv);
-                            bv[mn] = -1.0;
+                            const int n1 = mn + 1;
+                            double *x = sm.small + 64;
+                            const bool okk = warp_small_solve(n1,
+                                [&](int i, int j) { return (i < mn && j < mn) ? Bm[ctl[2 + i] * PDG_MAX_HISTORY + ctl[2 + j]] : ((i == mn && j == mn) ? 0.0 : -1.0); },
+                                [&](int i) { return i == mn ? -1.0 : 0.0; }, sm.ta, x);
                             double dev = 0.0;
-                            for (int i = 0; i < n1; i++) dev += bv[i];
-                            if (ok && fabs(dev) < 1.0e-6) { for (int i = 0; i < mn; i++) cf[i] = bv[i]; ctl[21] = 1; break; }
+                            for (int i = 0; i < mn; i++) dev += x[i];
+                            dev += -1.0;
+                            if (okk && fabs(dev) < 1.0e-6) {
+                                if (lane < mn) cf[lane] = x[lane];
+                                good = 1;
+                                break;
+                            }
                             mn--;
-                            for (int i = 0; i < mn; i++) ctl[2 + i] = ctl[3 + i];
-                            for (int i = mn; i < hist; i++) { ctl[2 + i] = ctl[2 + i - 1] + 1; if (ctl[2 + i] >= hist) ctl[2 + i] -= hist; }
+                            __syncwarp();
+                            if (lane == 0) {
+                                for (int i = 0; i < mn; i++) ctl[2 + i] = ctl[3 + i];
+                                for (int i = mn; i < hist; i++) { ctl[2 + i] = ctl[2 + i - 1] + 1; if (ctl[2 + i] >= hist) ctl[2 + i] -= hist; }
+                            }
+                            __syncwarp();
                         }
-                        ctl[1] = mn;
+                        if (lane == 0) { ctl[1] = mn; ctl[21] = good; }
                     }
                     __syncthreads();
                     if (ctl[21]) {
                         const int mn = ctl[1];
-                        for (size_t k = tid; k < NN; k += PDG_BLOCK) {
-                            int i = (int)(k / N), j = (int)(k % N);
-                            int pkk = (i >= j) ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i;
+                        for (int q = tid; q < hl; q += PDG_BLOCK) {   // packed lower triangle, then mirrored
+                            int i = (int)((sqrtf(8.0f * (float)q + 1.0f) - 1.0f) * 0.5f);
+                            while ((i + 1) * (i + 2) / 2 <= q) i++;
+                            while (i * (i + 1) / 2 > q) i--;
+                            const int j = q - i * (i + 1) / 2;
                             double pp = 0.0, ff = 0.0;
                             for (int m = 0; m < mn; m++) {
-                                size_t off = (size_t)ctl[2 + m] * hl + pkk;
-                                pp += cf[m] * wsf[pl.hP + off]; ff += cf[m] * wsf[pl.hF + off];
+                                const size_t off = (size_t)ctl[2 + m] * hl + q;
+                                pp = fma(cf[m], wsf[pl.hP + off], pp); ff = fma(cf[m], wsf[pl.hF + off], ff);
                             }
-                            P[k] = pp; F[k] = ff;
+                            P[(size_t)i * N + j] = pp; F[(size_t)i * N + j] = ff;
+                            P[(size_t)j * N + i] = pp; F[(size_t)j * N + i] = ff;
                         }
                         __syncthreads();
                     }
