@@ -18,7 +18,8 @@ EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system
            "pdg_energy_gradients", "pdg_scf", "pdg_one_electron", "pdg_fock", "pdg_gradients", "pdg_qcmm_potentials",
            "pdg_qcmm_gradients", "pdg_scf_timings", "pdg_gradients_static_scratch", "pdg_last_error")
 TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densities Tridiagonal", "QC Densities Eigenvalues",
-          "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds")
+          "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds",
+          "QC Densities Cluster Rounds", "QC Densities Steps")
 
 
 class SCFOptions(ctypes.Structure):

@@ -25,6 +25,12 @@ def _nvcc():
     return "nvcc"
 
 
+def _defines():
+    """Extra -D options from PDG_NVCC_DEFINES (space separated, e.g. "PDG_SCF_CTAS_PER_SM=2"), for trying
+    compile-time configurations; empty by default."""
+    return ["-D" + d for d in os.environ.get("PDG_NVCC_DEFINES", "").split()]
+
+
 def _stale():
     if not os.path.exists(LIB):
         return True
@@ -42,7 +48,7 @@ def build(force=False, verbose=False):
 
     def compile_one(args):
         src, obj = args
-        cmd = [nvcc] + ARCH + FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc] + ARCH + FLAGS + _defines() + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s%s" % (src, r.stdout, r.stderr))

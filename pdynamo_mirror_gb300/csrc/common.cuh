@@ -12,7 +12,11 @@
 #include <stdint.h>
 #include "../../include/pdg.h"
 
-#define PDG_BLOCK 512
+// SCF CTAs resident per SM (one frame each) and the threads of one SCF CTA.
+#ifndef PDG_SCF_CTAS_PER_SM
+#define PDG_SCF_CTAS_PER_SM 2
+#endif
+#define PDG_BLOCK (512 / PDG_SCF_CTAS_PER_SM)
 #define PDG_WARPS (PDG_BLOCK / 32)
 #define PDG_MAX_HISTORY 16
 #define PDG_PAIR_E_STRIDE 24   // e1b[10] | e2a[10] | enuc | spare

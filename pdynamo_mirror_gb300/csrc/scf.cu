@@ -34,8 +34,10 @@ struct Smem {
     int *iv;           // ints: [0..63] control, [64..64+N) per-vector cluster starts
 };
 
-// GEMM tile: GM x GN outputs per pass, GK-deep staged chunks (padded rows against bank conflicts).
-#define GM 32
+// GEMM tile: GM x GN outputs per pass (GWR x 4 warps of 8 x 16), GK-deep staged chunks (padded rows
+// against bank conflicts).
+#define GWR (PDG_WARPS / 4)
+#define GM (8 * GWR)
 #define GN 64
 #define GK 16
 #define GA_LD (GM + 1)
@@ -51,7 +53,7 @@ __host__ __device__ inline SmemPlan smem_plan(int N, int kv)
     p.head = 32 + 256 + 13 * (size_t)N + 64 + ((64 + (size_t)N + 2) * sizeof(int) + 7) / 8;
     p.work = (size_t)GK * GA_LD + (size_t)GK * GB_LD;
     p.ldz = N | 1;
-    const size_t limit = 220 * 1024 / 8, packed = (size_t)N * (N + 1) / 2, zsz = (size_t)(kv > 0 ? kv : 1) * p.ldz;
+    const size_t limit = (PDG_SCF_CTAS_PER_SM == 1 ? 220 * 1024 : 110 * 1024) / 8, packed = (size_t)N * (N + 1) / 2, zsz = (size_t)(kv > 0 ? kv : 1) * p.ldz;
     p.amat = (p.head + p.work + packed <= limit) ? packed : 0;
     p.zs = (p.amat && p.head + p.work + packed + zsz <= limit) ? zsz : 0;
     p.bytes = 8 * (p.head + p.work + p.amat + p.zs);
@@ -95,8 +97,8 @@ __device__ void tgemm(int M, int Nc, int K, FA fa, FB fb, bool lower_only, Smem 
             for (int k0 = 0; k0 < K; k0 += GK) {
                 const int kc = min(GK, K - k0);
                 __syncthreads();
-                {
-                    const int r = AK ? tid / GK : tid % GM, kk = AK ? tid % GK : tid / GM, gi = i0 + r;
+                for (int t = tid; t < GM * GK; t += PDG_BLOCK) {
+                    const int r = AK ? t / GK : t % GM, kk = AK ? t % GK : t / GM, gi = i0 + r;
                     ga[kk * GA_LD + r] = (kk < kc && gi < M) ? fa(gi, k0 + kk) : 0.0;
                 }
                 for (int t = tid; t < GK * GN; t += PDG_BLOCK) {
@@ -431,7 +433,7 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
         const double tau = sm.tau[k];
         // items (row block rb, column segment q): Q segments per row so that short steps still spread over
         // the four FP64 units; each item leaves its partial products and its partial p.v
-        const int Q = R >= 16 ? 1 : min(4, PDG_WARPS / R), seg = (m + Q - 1) / Q;
+        const int Q = max(1, min(4, PDG_WARPS / R)), seg = (m + Q - 1) / Q;
         for (int item = w; item < R * Q; item += PDG_WARPS) {
             const int rb = item % R, qs = item / R, i = rb * 32 + lane;
             const int j0 = qs * seg, j1 = min(m, j0 + seg);
@@ -473,7 +475,7 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
             else if (lane == 0) { sm.e[c0] = A[plo(c0 + 1, c0)]; sm.tau[c0] = 0.0; }
         } else {
             const int nt = (m - 1) * m / 2;   // elements (i, j) of A22 with 1 <= j <= i < m
-            for (int el = tid - 32; el < nt; el += PDG_BLOCK - 32) {
+            for (int el = tid - 32; el < nt; el += PDG_BLOCK - 32) {   // warps 1 .. PDG_WARPS-1
                 int ii = (int)((sqrtf(8.0f * (float)el + 1.0f) - 1.0f) * 0.5f);
                 while ((ii + 1) * (ii + 2) / 2 <= el) ii++;
                 while (ii * (ii + 1) / 2 > el) ii--;
@@ -552,6 +554,7 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
     //     against the finished earlier members
     {
         const int rounds = sm.iv[0], kvp = (kv + 31) & ~31;
+        if (tid == 0) { tm.slot[PDG_T_ROUNDS] += rounds; tm.slot[PDG_T_DENSITY_STEPS] += 1.0; }
         const double tiny = 2.2e-16 * fmax(sm.small[0], 1.0);
         double *U0 = wsf + pl.LU, *U1 = U0 + (size_t)N * kvp, *U2 = U1 + (size_t)N * kvp, *LM = U2 + (size_t)N * kvp;
         double *Y = LM + (size_t)N * kvp;
@@ -602,7 +605,7 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
 }
 
 // ----------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(PDG_BLOCK, 1) k_scf(SCFArgs a)
+__global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf(SCFArgs a)
 {
     extern __shared__ double shm[];
     const DeviceSystem &s = a.s;
