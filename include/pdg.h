@@ -187,6 +187,12 @@ int pdg_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const double
                        int n_knots, const double *d_knots, double outer_cutoff,
                        double *d_qc_grad, double *d_mm_grad, void *stream);
 
+/* Check of the tensor-core (tcgen05) split-BF16 product used by the purification density step:
+ * d_c = X X for a symmetric n x n FP32 matrix d_x (n <= 144), with kprod = 1, 3 or 6 BF16 partial
+ * products accumulated in FP32.  d_status (one int) is 0, or 1 when the tensor-core completion wait ran out.
+ * No counterpart in the reference (its density step is an FP64 eigensolve). */
+int pdg_tc_selftest(int n, int kprod, const float *d_x, float *d_c, int *d_status, void *stream);
+
 /* Text of the last error on this host thread (never NULL). */
 const char *pdg_last_error(void);
 

@@ -16,7 +16,7 @@ MAX_HISTORY = 16
 
 EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system_info", "pdg_workspace_bytes",
            "pdg_energy_gradients", "pdg_scf", "pdg_one_electron", "pdg_fock", "pdg_gradients", "pdg_qcmm_potentials",
-           "pdg_qcmm_gradients", "pdg_scf_timings", "pdg_gradients_static_scratch", "pdg_last_error")
+           "pdg_qcmm_gradients", "pdg_scf_timings", "pdg_gradients_static_scratch", "pdg_tc_selftest", "pdg_last_error")
 TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densities Tridiagonal", "QC Densities Eigenvalues",
           "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds",
           "QC Densities Cluster Rounds", "QC Densities Steps")
@@ -59,6 +59,7 @@ def load(path=LIB_PATH):
     L.pdg_gradients.argtypes = [P, I, P, P, P, P, S, P]
     L.pdg_scf_timings.argtypes = [P, I, P, S, P, P]
     L.pdg_gradients_static_scratch.argtypes = [P, I, P, P, P, P]
+    L.pdg_tc_selftest.argtypes = [I, I, P, P, P, P]
     L.pdg_qcmm_potentials.argtypes = [I, I, I, I, P, P, P, I, P, D, P, P]
     L.pdg_qcmm_gradients.argtypes = [I, I, I, I, P, P, P, P, I, P, D, P, P, P]
     for name in EXPORTS:

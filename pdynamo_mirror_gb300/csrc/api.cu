@@ -332,3 +332,12 @@ extern "C" int pdg_gradients_static_scratch(pdg_system *s, int n_frames, const d
     launch_reduce_gradients(s->d, p, n_frames, scratch, d_gradients, st);
     return cuda_check(cudaGetLastError(), "gradient kernels (static scratch)");
 }
+
+extern "C" int pdg_tc_selftest(int n, int kprod, const float *d_x, float *d_c, int *d_status, void *stream)
+{
+    if (n < 1 || n > 144) return fail(PDG_TOO_LARGE, "pdg_tc_selftest: n must be 1..144");
+    if (kprod != 1 && kprod != 3 && kprod != 6) return fail(PDG_BAD_ARGUMENT, "pdg_tc_selftest: kprod must be 1, 3 or 6");
+    if (!d_x || !d_c || !d_status) return fail(PDG_BAD_ARGUMENT, "null argument");
+    launch_tc_selftest(n, kprod, d_x, d_c, d_status, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "tensor-core self-test kernel");
+}

@@ -129,3 +129,4 @@ int launch_qcmm_potentials(int model, int n_frames, int n_qc, int n_mm, const do
 int launch_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,
                           const double *q, const double *qcq, int n_knots, const double *knots, double cutoff,
                           double *gqc, double *gmm, cudaStream_t st);
+int launch_tc_selftest(int n, int kprod, const float *x, float *c, int *status, cudaStream_t st);
