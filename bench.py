@@ -25,7 +25,7 @@ import numpy as np
 # in profiles/k_scf_dram_304frames.md; per launch, like `achieved`.
 K_SCF_DRAM_BYTES_304 = 4.85e9 + 4.10e9
 
-METRIC = "QC/MM E+grad evals/s (AM1 RHF, 65 QC atoms in 4000 TIP3P waters, ABFS 8/12 A)"
+METRIC = "QC/MM E+grad evals/s at |dE|<1e-6 Eh (AM1 RHF, 65 QC atoms in 4000 TIP3P waters, ABFS 8/12 A)"
 UNIT = "evals/s"
 KJ = 2625.5
 
@@ -93,6 +93,19 @@ def fp64_peak_tflops(dev, n=4096, reps=3):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
+def scf_cta_layout(eng, T):
+    """Threads and shared memory of one SCF CTA, and how many CTAs (frames) the SMs actually ran at once,
+    from the SM id and %globaltimer interval that every CTA records (pdg_scf_timings)."""
+    threads, smem, _ = eng.occupancy()
+    sm, st, en = T["SM"].astype(int), T["Start ns"], T["End ns"]
+    most = 0
+    for s_ in set(sm.tolist()):
+        iv = sorted(zip(st[sm == s_], en[sm == s_]))
+        for k, (a, b) in enumerate(iv):
+            most = max(most, sum(1 for (c, d) in iv if c < b and d > a))
+    return {"threads": threads, "shared_bytes": smem, "ctas_per_sm_observed": most, "sms_used": len(set(sm.tolist()))}
+
+
 def workload(n_frames, seed=1):
     from pdynamo_mirror_gb300 import workloads
     Z, X, Q, sel, charge = workloads.qcmm_water_box(seed=seed)
@@ -157,6 +170,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--reference-sample", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--method", default="mixed", choices=["mixed", "fp64"],
+                    help="density step of the early SCF cycles: split-BF16 purification (mixed) or FP64 throughout")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -175,92 +190,133 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     dev = torch.device("cuda")
     Z, X, Q, sel, charge, frames = workload(args.frames, seed=1 + rank)
-    s = System(Z, X, mmCharges=Q)
-    s.electronicState.charge = charge
-    s.DefineQCModel(QCModelMNDO("am1"), qcSelection=sel)
-    s.DefineNBModel(NBModelABFS(innerCutoff=8.0, outerCutoff=12.0))
-    eng = s.engine()
-    qc, mm, q, mm_idx = s._device_inputs(frames)
-    conv = s.qcModel.converger
-    nb = s.nbModel
+    from pdynamo_mirror_gb300 import DIISSCFConverger
+    METHODS = {"fp64": dict(densityStep="fp64"),
+               "mixed": dict(densityStep="purification", purificationProducts=6, purificationSwitch=1e-5)}
 
-    def step():
-        return eng.run(qc, conv, mm, q, nb, gradients=True, warm_start=False)
+    def measure(method, timed_clocks):
+        s = System(Z, X, mmCharges=Q)
+        s.electronicState.charge = charge
+        s.DefineQCModel(QCModelMNDO("am1", converger=DIISSCFConverger(**METHODS[method])), qcSelection=sel)
+        s.DefineNBModel(NBModelABFS(innerCutoff=8.0, outerCutoff=12.0))
+        eng = s.engine()
+        qc, mm, q, mm_idx = s._device_inputs(frames)
+        conv, nb = s.qcModel.converger, s.nbModel
 
-    for _ in range(args.warmup):
-        r = step()
-    torch.cuda.synchronize()
-    st = r["status"].cpu().numpy()
-    if (st != 0).any():
-        raise SystemExit("SCF did not converge for %d frames" % int((st != 0).sum()))
-    ncyc = r["ncycles"].cpu().numpy()
-    stream = torch.cuda.current_stream()
-    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        r = step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    ms = e0.elapsed_time(e1) / args.steps
-    clk = clocks.stop()
-    # the dominant kernel alone: k_scf through pdg_scf on the integrals the last step left in the workspace
-    # (same frames, cold guess), CUDA events on the launching stream
-    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    scf_times = []
-    for _ in range(3):
-        k0.record(stream)
-        _, stt, nc = eng.scf(conv, phi=r["phi"], use_density=False)
-        k1.record(stream)
+        def step():
+            return eng.run(qc, conv, mm, q, nb, gradients=True, warm_start=False)
+
+        for _ in range(args.warmup):
+            r = step()
         torch.cuda.synchronize()
-        scf_times.append(k0.elapsed_time(k1))
-    scf_ms = float(np.median(scf_times))
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        st = r["status"].cpu().numpy()
+        if (st != 0).any():
+            raise SystemExit("%s: SCF did not converge for %d frames" % (method, int((st != 0).sum())))
+        stream = torch.cuda.current_stream()
+        clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) if timed_clocks else None
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        if clocks:
+            clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            r = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        ms = e0.elapsed_time(e1) / args.steps
+        clk = clocks.stop() if clocks else None
+        timers = eng.timings(len(frames))
+        # the dominant kernel alone: k_scf through pdg_scf on the integrals the last step left in the
+        # workspace (same frames, cold guess), CUDA events on the launching stream
+        k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        scf_times = []
+        for _ in range(3):
+            k0.record(stream)
+            eng.scf(conv, phi=r["phi"], use_density=False)
+            k1.record(stream)
+            torch.cuda.synchronize()
+            scf_times.append(k0.elapsed_time(k1))
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        # e2e through the public API: frames from pinned host memory in, energies and gradients out
+        frames_h = torch.from_numpy(np.ascontiguousarray(frames)).pin_memory()
+        te = []
+        for k in range(2 + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            E, G, terms = s.EnergyBatch(frames_h, doGradients=True, warmStart=False)
+            torch.cuda.synchronize()
+            if k >= 2:
+                te.append(time.perf_counter() - t0)
+        return dict(ms=ms, clk=clk, scf_ms=float(np.median(scf_times)), e2e_s=sum(te) / len(te), E=E, G=G,
+                    ncyc=r["ncycles"].cpu().numpy(), timers=timers, eng=eng, conv=conv, frames_h=frames_h)
+
+    plain = measure("fp64", args.method == "fp64")
+    head = plain if args.method == "fp64" else measure(args.method, True)
+    eng, conv = head["eng"], head["conv"]
     n_total = len(frames) * world
-    value = n_total / (ms * 1e-3)
-    # e2e through the public API: frames from pinned host memory in, energies and gradients out
-    frames_h = torch.from_numpy(np.ascontiguousarray(frames)).pin_memory()
-    te = []
-    for k in range(2 + args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        E, G, terms = s.EnergyBatch(frames_h, doGradients=True, warmStart=False)
-        torch.cuda.synchronize()
-        if k >= 2:
-            te.append(time.perf_counter() - t0)
-    e2e = n_total / (sum(te) / len(te))
-    # FP64 roofline of k_scf.  Algorithmic FP64 flops of this SCF per frame: every density
-    # step (4/3) N^3 tridiagonalisation + 2 N^2 kv back-transformation + N^2 kv density; every DIIS save
-    # 4 N^2 kv (the commutator through the orbital factor).  Density steps = SCF cycles + 1.
+    value = n_total / (head["ms"] * 1e-3)
+    e2e = n_total / head["e2e_s"]
     N, kv = eng.n_basis, min(eng.n_occupied, eng.n_basis - eng.n_occupied)
-    ncyc_f = float(ncyc.mean())
-    scf_flops = len(frames) * ((ncyc_f + 1.0) * ((4.0 / 3.0) * N ** 3 + 3.0 * N * N * kv) + ncyc_f * 4.0 * N * N * kv)
-    achieved_tf = scf_flops / (scf_ms * 1e-3) / 1e12
+    T = head["timers"]
+    fp64_steps = float(T["QC Densities Steps"].mean())
+    pur_steps = float(T["QC Densities Purification Steps"].mean())
+    ncyc_f = float(head["ncyc"].mean())
+    # FP64 roofline of k_scf.  Algorithmic FP64 flops per frame: every FP64 density step
+    # (4/3) N^3 tridiagonalisation + 2 N^2 kv back-transformation + N^2 kv density; every DIIS save after an
+    # FP64 step 4 N^2 kv (the commutator through the orbital factor); every other DIIS save the full 2 N^3.
+    fp64_saves = max(fp64_steps - 1.0, 0.0)
+    other_saves = max(ncyc_f - fp64_saves, 0.0)
+    scf_flops = len(frames) * (fp64_steps * ((4.0 / 3.0) * N ** 3 + 3.0 * N * N * kv) + fp64_saves * 4.0 * N * N * kv
+                               + (other_saves * 2.0 * N ** 3 if args.method == "fp64" else 0.0))
+    achieved_tf = scf_flops / (head["scf_ms"] * 1e-3) / 1e12
     fp64_peak = fp64_peak_tflops(dev)
+    clk = head["clk"]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded water box, perturbed frames)",
             "config": {"workload": "qcmm_water_box_am1_abfs", "qc_atoms": len(sel), "mm_atoms": len(Z) - len(sel),
-                       "basis_functions": N, "frames_per_step": len(frames), "method": "plain FP64",
+                       "basis_functions": N, "frames_per_step": len(frames),
+                       "method": "plain FP64" if args.method == "fp64" else
+                                 "mixed: split-BF16 SP2 purification on tcgen05 (6 partial products, FP32 accumulation) until the RMS density change < 1e-5, then FP64",
                        "density_tolerance": conv.densityTolerance, "mean_scf_cycles": ncyc_f,
+                       "purification_steps_per_frame": pur_steps, "fp64_density_steps_per_frame": fp64_steps,
+                       "scf_cta": scf_cta_layout(eng, T),
                        "l2": "working set > L2 (no flush needed)"},
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(frames_h.numel() * 8),
-                    "d2h_bytes_per_step": int(G.nbytes + len(frames) * (_native.NENERGY + 2) * 8)},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(head["frames_h"].numel() * 8),
+                    "d2h_bytes_per_step": int(head["G"].nbytes + len(frames) * (_native.NENERGY + 2) * 8)},
             "gpu_launches": 8 * args.steps,
             "roofline": {"bound": "fp64", "kernel": "k_scf", "achieved": achieved_tf, "peak": fp64_peak, "unit": "TFLOP/s",
-                         "frac": achieved_tf / fp64_peak, "traffic": K_SCF_DRAM_BYTES_304 if len(frames) == 304 else None,
+                         "frac": achieved_tf / fp64_peak,
+                         "traffic": K_SCF_DRAM_BYTES_304 if (len(frames) == 304 and args.method == "fp64") else None,
                          "note": "peak = cuBLAS DGEMM 4096^3 measured in this run (of measured; MEASURED_PEAKS.json has no FP64 figure); "
-                                 "k_scf %.2f ms per %d-frame launch, step %.2f ms" % (scf_ms, len(frames), ms)},
+                                 "k_scf %.2f ms per %d-frame launch, step %.2f ms" % (head["scf_ms"], len(frames), head["ms"])},
             "clocks": clk}
+    if args.method != "fp64":
+        # tensor-core part: SP2 iterations x k partial products x 2 N^3 algorithmic flops, over the purification
+        # steps' device time (their clock64 cycles at the sampled SM clock)
+        sp2 = float(T["QC Densities SP2 Iterations"].mean())
+        pur_cycles = float(T["QC Densities Purification"].mean())
+        mhz = (clk or {}).get("sm_mhz") or 2070.0
+        t_pur = pur_cycles / (mhz * 1e6)
+        tc_tf = (sp2 * 6 * 2.0 * N ** 3) / t_pur / 1e12 if t_pur > 0 else 0.0
+        pk = peaks()
+        bf16 = pk.get("bf16_tflops", 1900.0) / 152.0 / 2   # per SM, two SCF CTAs per SM share it
+        line["roofline"]["tensor"] = {"achieved_per_cta": tc_tf, "unit": "TFLOP/s", "peak_per_cta": bf16,
+                                      "frac": tc_tf / bf16 if bf16 else None,
+                                      "note": "split-BF16 SP2 products of one frame's CTA (measured BF16 peak / 152 SMs / 2 CTAs per SM)"}
+        dE = float(np.abs(head["E"] - plain["E"]).max()) / KJ
+        dG = float(np.abs(head["G"] - plain["G"]).max()) / (KJ * 1.0e-10 / 5.291772083e-11)
+        line["plain_fp64"] = {"value": n_total / (plain["ms"] * 1e-3), "ms_per_step": plain["ms"], "e2e": n_total / plain["e2e_s"],
+                              "mean_scf_cycles": float(plain["ncyc"].mean())}
+        line["accuracy_vs_plain_fp64"] = {"max_abs_dE_hartree": dE, "max_abs_dF_hartree_per_bohr": dG,
+                                          "gate": "|dE| < 1e-6 Eh, |dF| < 1e-5 Eh/Bohr", "pass": bool(dE < 1e-6 and dG < 1e-5)}
     if rank == 0 and not args.no_cpu_baseline:
         n = min(len(frames), 96)
         t, k = cpu_reference_sample(list(Z), Q, sel, charge, frames, n, 1)

@@ -35,7 +35,8 @@ typedef enum {
     PDG_DIIS_SINGULAR  = 3,   /* reserved: DIIS never recovered a well-conditioned subspace */
     PDG_BAD_ARGUMENT   = 4,
     PDG_CUDA_ERROR     = 5,
-    PDG_TOO_LARGE      = 6    /* a size exceeds a compiled limit */
+    PDG_TOO_LARGE      = 6,   /* a size exceeds a compiled limit */
+    PDG_TENSOR_TIMEOUT = 7    /* a tensor-core completion wait ran out (the frame's SCF was stopped) */
 } pdg_status;
 
 /* Per-element parameter record: PDG_ELEMENT_STRIDE doubles, all in atomic units, filled by the host
@@ -65,7 +66,12 @@ typedef struct {
     int    maximum_scf_cycles;  /* 100  */
     int    history;             /* 10, at most 16 */
     int    use_rca;             /* 1: ODA/RCA before DIIS, as the reference default */
-    int    reserved;            /* must be 0 */
+    int    density_step;        /* 0: FP64 eigensolve every cycle (the reference's method);
+                                   3 or 6: split-BF16 SP2 purification on the tensor cores with that many BF16
+                                   partial products accumulated in FP32, for the cycles before the density RMS
+                                   change falls below mixed_switch, then the FP64 eigensolve to convergence
+                                   (N <= 144; larger systems use the FP64 step throughout). Not in the reference. */
+    double mixed_switch;        /* RMS density change that ends the purification cycles (e.g. 1e-4) */
 } pdg_scf_options;
 
 /* Energy terms returned per frame (PDG_NENERGY doubles). */
@@ -129,6 +135,12 @@ int pdg_scf(pdg_system *sys, int n_frames, const double *d_phi, const pdg_scf_op
             int use_density, double *d_energies, double *d_charges, int *d_status, int *d_ncycles,
             void *d_workspace, size_t workspace_bytes, void *stream);
 
+/* One density step for given Fock matrices d_fock (n_frames * N * N): d_density (in: the previous density,
+ * out: the density of the n_occ lowest eigenvectors) by the FP64 eigensolve (density_step 0) or by split-BF16
+ * purification (3 or 6 partial products; N <= 144).  d_energies[PDG_EN_RMS_DENSITY] gets the RMS change. */
+int pdg_density(pdg_system *sys, int n_frames, const double *d_fock, int density_step, double *d_density,
+                double *d_energies, int *d_status, void *d_workspace, size_t workspace_bytes, void *stream);
+
 /* Diagnostics for parity tests: the one-electron matrix H (n_frames * N * N) and the Fock matrix
  * F = H + G(P) - phi for given densities (QCModelMNDO_Fock + QCMMFockLowdin on one density), with
  * the energies of that density in d_energies. */
@@ -160,12 +172,21 @@ int pdg_gradients_static_scratch(pdg_system *sys, int n_frames, const double *d_
  * PDG_NTIMERS GPU clock-cycle counts (clock64 of the frame's CTA), the device counterpart of the phase
  * timings of pMolecule.QCModel.pyx:208-275 (EnergyWithTimings: QC Fock, QC Converger Iterate,
  * QC Converger Densities), with the density step split into its parts.  d_out: n_frames * PDG_NTIMERS. */
-#define PDG_NTIMERS 12
+#define PDG_RMS_HISTORY 40
+#define PDG_NTIMERS (18 + PDG_RMS_HISTORY)
 enum {
     PDG_T_FOCK = 0, PDG_T_DIIS_SAVE = 1, PDG_T_ITERATE = 2, PDG_T_TRIDIAGONAL = 3, PDG_T_EIGENVALUES = 4,
     PDG_T_EIGENVECTORS = 5, PDG_T_BACKTRANSFORM = 6, PDG_T_DENSITY = 7, PDG_T_TOTAL = 8, PDG_T_CYCLES = 9,
     PDG_T_ROUNDS = 10,         /* counts, not cycles: inverse-iteration rounds (largest eigenvalue cluster) summed over density steps */
-    PDG_T_DENSITY_STEPS = 11   /* density steps */
+    PDG_T_DENSITY_STEPS = 11,  /* FP64 density steps */
+    PDG_T_PURIFICATION = 12,   /* cycles of the split-BF16 purification density steps */
+    PDG_T_PURIFICATION_STEPS = 13, /* count: purification density steps */
+    PDG_T_SP2_ITERATIONS = 14, /* count: SP2 iterations summed over them */
+    PDG_T_SM_ID = 15,          /* the SM that ran the frame's CTA */
+    PDG_T_START_NS = 16,       /* %globaltimer at the CTA's start and end (ns) */
+    PDG_T_END_NS = 17,
+    PDG_T_RMS_HISTORY = 18     /* PDG_RMS_HISTORY entries: RMS density change of each density step, in SCF cycle
+                                  order, negative for purification steps, 0 beyond the last */
 };
 int pdg_scf_timings(const pdg_system *sys, int n_frames, const void *d_workspace, size_t workspace_bytes,
                     double *d_out, void *stream);
@@ -192,6 +213,11 @@ int pdg_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const double
  * products accumulated in FP32.  d_status (one int) is 0, or 1 when the tensor-core completion wait ran out.
  * No counterpart in the reference (its density step is an FP64 eigensolve). */
 int pdg_tc_selftest(int n, int kprod, const float *d_x, float *d_c, int *d_status, void *stream);
+
+/* Launch configuration of the SCF kernel for this system on the current device: threads per CTA (one CTA
+ * per frame), dynamic shared memory per CTA, and the CUDA runtime's occupancy estimate in CTAs per SM (the
+ * SM id and start/end times each CTA records in pdg_scf_timings show what the hardware actually ran). */
+int pdg_scf_occupancy(const pdg_system *sys, int *threads, int *smem_bytes, int *ctas_per_sm);
 
 /* Text of the last error on this host thread (never NULL). */
 const char *pdg_last_error(void);

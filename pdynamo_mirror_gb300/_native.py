@@ -9,23 +9,25 @@ import ctypes, os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libpdg.so")
 
-PDG_OK, PDG_NOT_CONVERGED, PDG_NAN, PDG_DIIS_SINGULAR, PDG_BAD_ARGUMENT, PDG_CUDA_ERROR, PDG_TOO_LARGE = range(7)
+PDG_OK, PDG_NOT_CONVERGED, PDG_NAN, PDG_DIIS_SINGULAR, PDG_BAD_ARGUMENT, PDG_CUDA_ERROR, PDG_TOO_LARGE, PDG_TENSOR_TIMEOUT = range(8)
 NENERGY = 8
 EN_TOTAL_ELECTRONIC, EN_ELECTRONIC, EN_NUCLEAR, EN_BASELINE, EN_QCMM, EN_ONE_ELECTRON, EN_TWO_ELECTRON, EN_RMS_DENSITY = range(8)
 MAX_HISTORY = 16
 
 EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system_info", "pdg_workspace_bytes",
-           "pdg_energy_gradients", "pdg_scf", "pdg_one_electron", "pdg_fock", "pdg_gradients", "pdg_qcmm_potentials",
-           "pdg_qcmm_gradients", "pdg_scf_timings", "pdg_gradients_static_scratch", "pdg_tc_selftest", "pdg_last_error")
+           "pdg_energy_gradients", "pdg_scf", "pdg_density", "pdg_one_electron", "pdg_fock", "pdg_gradients", "pdg_qcmm_potentials",
+           "pdg_qcmm_gradients", "pdg_scf_timings", "pdg_gradients_static_scratch", "pdg_tc_selftest", "pdg_scf_occupancy", "pdg_last_error")
 TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densities Tridiagonal", "QC Densities Eigenvalues",
           "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds",
-          "QC Densities Cluster Rounds", "QC Densities Steps")
+          "QC Densities Cluster Rounds", "QC Densities Steps", "QC Densities Purification",
+          "QC Densities Purification Steps", "QC Densities SP2 Iterations", "SM", "Start ns", "End ns") + tuple("RMS %d" % k for k in range(40))
 
 
 class SCFOptions(ctypes.Structure):
     _fields_ = [("density_tolerance", ctypes.c_double), ("energy_tolerance", ctypes.c_double),
                 ("diis_onset", ctypes.c_double), ("maximum_scf_cycles", ctypes.c_int),
-                ("history", ctypes.c_int), ("use_rca", ctypes.c_int), ("reserved", ctypes.c_int)]
+                ("history", ctypes.c_int), ("use_rca", ctypes.c_int), ("density_step", ctypes.c_int),
+                ("mixed_switch", ctypes.c_double)]
 
 
 class NativeError(RuntimeError):
@@ -54,12 +56,14 @@ def load(path=LIB_PATH):
     L.pdg_workspace_bytes.restype = S
     L.pdg_energy_gradients.argtypes = [P, I, P, P, ctypes.POINTER(SCFOptions), P, I, P, P, P, P, P, P, S, P]
     L.pdg_scf.argtypes = [P, I, P, ctypes.POINTER(SCFOptions), P, I, P, P, P, P, P, S, P]
+    L.pdg_density.argtypes = [P, I, P, I, P, P, P, P, S, P]
     L.pdg_one_electron.argtypes = [P, I, P, P, P, S, P]
     L.pdg_fock.argtypes = [P, I, P, P, P, P, P, P, S, P]
     L.pdg_gradients.argtypes = [P, I, P, P, P, P, S, P]
     L.pdg_scf_timings.argtypes = [P, I, P, S, P, P]
     L.pdg_gradients_static_scratch.argtypes = [P, I, P, P, P, P]
     L.pdg_tc_selftest.argtypes = [I, I, P, P, P, P]
+    L.pdg_scf_occupancy.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]
     L.pdg_qcmm_potentials.argtypes = [I, I, I, I, P, P, P, I, P, D, P, P]
     L.pdg_qcmm_gradients.argtypes = [I, I, I, I, P, P, P, P, I, P, D, P, P, P]
     for name in EXPORTS:

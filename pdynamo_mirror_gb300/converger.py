@@ -8,10 +8,18 @@ from . import _native
 
 
 class DIISSCFConverger:
-    """DIIS with ODA (RCA) start-up, as pDynamo's default converger."""
+    """DIIS with ODA (RCA) start-up, as pDynamo's default converger.
+
+    Two keywords beyond the reference's select the density step of the early cycles:
+    densityStep "fp64" (default: the FP64 eigensolve every cycle, as the reference) or "purification"
+    (split-BF16 SP2 purification on the tensor cores until the RMS density change falls below
+    purificationSwitch, then the FP64 eigensolve to convergence); purificationProducts 3 or 6 is the
+    number of BF16 partial products accumulated in FP32.  The converged result is that of the FP64 step.
+    """
 
     _DEFAULTS = {"densityTolerance": 1.0e-8, "diisOnset": 0.2, "energyTolerance": 2.0e-4, "history": 10,
-                 "maximumSCFCycles": 100, "useRCA": True}
+                 "maximumSCFCycles": 100, "useRCA": True, "densityStep": "fp64", "purificationSwitch": 1.0e-4,
+                 "purificationProducts": 3}
 
     def __init__(self, **options):
         for k, v in self._DEFAULTS.items():
@@ -26,10 +34,16 @@ class DIISSCFConverger:
             raise ValueError("Invalid options: " + ", ".join(sorted(options)) + ".")
         if not (1 <= int(self.history) <= _native.MAX_HISTORY):
             raise ValueError("history must be between 1 and %d." % _native.MAX_HISTORY)
+        if self.densityStep not in ("fp64", "purification"):
+            raise ValueError("densityStep must be 'fp64' or 'purification'.")
+        if int(self.purificationProducts) not in (3, 6):
+            raise ValueError("purificationProducts must be 3 or 6.")
 
     def options(self):
+        step = 0 if self.densityStep == "fp64" else int(self.purificationProducts)
         return _native.SCFOptions(float(self.densityTolerance), float(self.energyTolerance), float(self.diisOnset),
-                                  int(self.maximumSCFCycles), int(self.history), 1 if self.useRCA else 0, 0)
+                                  int(self.maximumSCFCycles), int(self.history), 1 if self.useRCA else 0, step,
+                                  float(self.purificationSwitch))
 
     def __getstate__(self):
         return {k: getattr(self, k) for k in self._DEFAULTS}

@@ -182,6 +182,7 @@ extern "C" int pdg_energy_gradients(pdg_system *s, int n_frames, const double *d
     if (!o || !d_xyz || !d_density || !d_energies || !d_status) return fail(PDG_BAD_ARGUMENT, "null argument");
     if (o->history < 1 || o->history > PDG_MAX_HISTORY) return fail(PDG_BAD_ARGUMENT, "history must be 1..16");
     if (o->maximum_scf_cycles < 0) return fail(PDG_BAD_ARGUMENT, "maximum_scf_cycles must be >= 0");
+    if (o->density_step != 0 && o->density_step != 3 && o->density_step != 6) return fail(PDG_BAD_ARGUMENT, "density_step must be 0, 3 or 6");
     cudaStream_t st = (cudaStream_t)stream;
     FramePlan p = plan_for(s, PDG_MAX_HISTORY);
     double *w = (double *)ws;
@@ -205,6 +206,7 @@ extern "C" int pdg_scf(pdg_system *s, int n_frames, const double *d_phi, const p
     if (!o || !d_density || !d_energies || !d_status) return fail(PDG_BAD_ARGUMENT, "null argument");
     if (o->history < 1 || o->history > PDG_MAX_HISTORY) return fail(PDG_BAD_ARGUMENT, "history must be 1..16");
     if (o->maximum_scf_cycles < 0) return fail(PDG_BAD_ARGUMENT, "maximum_scf_cycles must be >= 0");
+    if (o->density_step != 0 && o->density_step != 3 && o->density_step != 6) return fail(PDG_BAD_ARGUMENT, "density_step must be 0, 3 or 6");
     FramePlan p = plan_for(s, PDG_MAX_HISTORY);
     launch_scf(s->d, p, n_frames, d_phi, *o, d_density, use_density, d_energies, d_charges, d_status, d_ncycles, (double *)ws, 0,
                nullptr, (cudaStream_t)stream);
@@ -234,7 +236,7 @@ extern "C" int pdg_fock(pdg_system *s, int n_frames, const double *d_xyz, const 
     FramePlan p = plan_for(s, PDG_MAX_HISTORY);
     double *w = (double *)ws;
     if ((rc = integrals(s, p, n_frames, d_xyz, w, st))) return rc;
-    pdg_scf_options o = { 1e-8, 2e-4, 0.2, 0, 10, 1, 0 };
+    pdg_scf_options o = { 1e-8, 2e-4, 0.2, 0, 10, 1, 0, 1e-4 };
     launch_scf(s->d, p, n_frames, d_phi, o, const_cast<double *>(d_density), 1, d_energies, nullptr, nullptr, nullptr, w, 1, d_fock, st);
     return cuda_check(cudaGetLastError(), "fock kernel");
 }
@@ -340,4 +342,25 @@ extern "C" int pdg_tc_selftest(int n, int kprod, const float *d_x, float *d_c, i
     if (!d_x || !d_c || !d_status) return fail(PDG_BAD_ARGUMENT, "null argument");
     launch_tc_selftest(n, kprod, d_x, d_c, d_status, (cudaStream_t)stream);
     return cuda_check(cudaGetLastError(), "tensor-core self-test kernel");
+}
+
+extern "C" int pdg_density(pdg_system *s, int n_frames, const double *d_fock, int density_step, double *d_density,
+                           double *d_energies, int *d_status, void *ws, size_t bytes, void *stream)
+{
+    int rc = check_workspace(s, n_frames, ws, bytes);
+    if (rc) return rc;
+    if (!d_fock || !d_density || !d_energies || !d_status) return fail(PDG_BAD_ARGUMENT, "null argument");
+    if (density_step != 0 && density_step != 3 && density_step != 6) return fail(PDG_BAD_ARGUMENT, "density_step must be 0, 3 or 6");
+    FramePlan p = plan_for(s, PDG_MAX_HISTORY);
+    pdg_scf_options o = { 1e-8, 2e-4, 0.2, 0, 10, 1, density_step, 1e-4 };
+    launch_scf(s->d, p, n_frames, nullptr, o, d_density, 1, d_energies, nullptr, d_status, nullptr, (double *)ws, 2,
+               const_cast<double *>(d_fock), (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "density step kernel");
+}
+
+extern "C" int pdg_scf_occupancy(const pdg_system *s, int *threads, int *smem_bytes, int *ctas_per_sm)
+{
+    if (!s || !threads || !smem_bytes || !ctas_per_sm) return fail(PDG_BAD_ARGUMENT, "null argument");
+    if (scf_occupancy(s->d, threads, smem_bytes, ctas_per_sm)) return cuda_check(cudaGetLastError(), "occupancy query");
+    return PDG_OK;
 }

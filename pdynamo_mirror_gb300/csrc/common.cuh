@@ -53,8 +53,9 @@ __host__ inline FramePlan make_plan(const DeviceSystem &s, int history)
     p.pair_g = o; o += align32((size_t)s.n_pairs * 3);
     p.H = o;      o += align32(NN);
     p.F = o;      o += align32(NN);
-    p.P0 = o;     o += align32(NN);          // previous density (for the RMS change)
-    p.A = o;      o += align32(NN);          // work matrix: F P product, tridiagonalisation
+    p.P0 = o;     o += align32(NN);          // F in FP32 (N x round4(N)) for the commutator after a purification step
+    p.A = o;      o += align32(2 * NN + 4 * N);  // work matrix: F P product, packed tridiagonal matrix, or the FP32
+                                                 // purification iterates (two N x N) and P in FP32 (N x round4(N))
     const size_t kv = s.n_vec > 0 ? s.n_vec : 1, kvp = (kv + 31) & ~size_t(31);
     p.G = o;      o += align32(kv * N);      // DIIS: the vectors times F
     p.Z = o;      o += align32(kv * (N | 1)); // wanted eigenvectors when they do not fit in shared memory
@@ -130,3 +131,4 @@ int launch_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const dou
                           const double *q, const double *qcq, int n_knots, const double *knots, double cutoff,
                           double *gqc, double *gmm, cudaStream_t st);
 int launch_tc_selftest(int n, int kprod, const float *x, float *c, int *status, cudaStream_t st);
+int scf_occupancy(const DeviceSystem &s, int *threads, int *smem_bytes, int *ctas_per_sm);

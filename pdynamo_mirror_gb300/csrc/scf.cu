@@ -15,6 +15,7 @@
 // shared-memory GEMMs and everything sequential is confined to O(N) or O(N^2) work.
 #include "common.cuh"
 #include "multipole.cuh"
+#include "tc.cuh"
 
 
 struct SCFArgs {
@@ -47,15 +48,28 @@ struct Smem {
 // The packed matrix goes to shared memory when it fits, then the eigenvectors.
 struct SmemPlan { size_t head, work, amat, zs, bytes; int ldz; };
 
+// Doubles of the split-BF16 operand arrays (hi and mid or lo parts, R x Kp bf16 each) of the purification
+// density step; 0 when N is beyond its one-tile limit.
+__host__ __device__ inline size_t mix_doubles(int N)
+{
+    if (N > 144) return 0;
+    const size_t Kp = (N + 15) & ~15, R = Kp > 128 ? Kp : 128;
+    return 2 * R * Kp * 2 / 8;
+}
+
+__host__ __device__ inline size_t round16(size_t x) { return (x + 15) & ~size_t(15); }
+
 __host__ __device__ inline SmemPlan smem_plan(int N, int kv)
 {
     SmemPlan p;
-    p.head = 32 + 256 + 13 * (size_t)N + 64 + ((64 + (size_t)N + 2) * sizeof(int) + 7) / 8;
-    p.work = (size_t)GK * GA_LD + (size_t)GK * GB_LD;
+    p.head = round16(32 + 256 + 13 * (size_t)N + 64 + ((64 + (size_t)N + 2) * sizeof(int) + 7) / 8);
+    p.work = round16((size_t)GK * GA_LD + (size_t)GK * GB_LD);
     p.ldz = N | 1;
-    const size_t limit = (PDG_SCF_CTAS_PER_SM == 1 ? 220 * 1024 : 110 * 1024) / 8, packed = (size_t)N * (N + 1) / 2, zsz = (size_t)(kv > 0 ? kv : 1) * p.ldz;
-    p.amat = (p.head + p.work + packed <= limit) ? packed : 0;
-    p.zs = (p.amat && p.head + p.work + packed + zsz <= limit) ? zsz : 0;
+    const size_t limit = (PDG_SCF_CTAS_PER_SM == 1 ? 220 * 1024 : 112 * 1024) / 8, packed = (size_t)N * (N + 1) / 2;
+    const size_t zsz = (size_t)(kv > 0 ? kv : 1) * p.ldz, mix = mix_doubles(N);
+    const size_t slot = round16(packed > mix ? packed : mix);
+    p.amat = (p.head + p.work + slot <= limit) ? slot : 0;
+    p.zs = (p.amat && p.head + p.work + p.amat + zsz <= limit) ? zsz : 0;
     p.bytes = 8 * (p.head + p.work + p.amat + p.zs);
     return p;
 }
@@ -82,45 +96,45 @@ __device__ __forceinline__ Smem carve(double *base, int N, int kv)
 // outside the output, or above the diagonal when lower_only; warp (wr, wc) sits on FP64 unit (wr + wc) % 4,
 // so the partial warps of edge tiles stay spread over all four.  The epilogue receives every (i, j) < (M, Nc)
 // of an active sub-tile; lower_only callers filter j > i there.
-template <bool AK, bool BK, typename FA, typename FB, typename Epi>
-__device__ void tgemm(int M, int Nc, int K, FA fa, FB fb, bool lower_only, Smem &sm, Epi epi)
+template <bool AK, bool BK, typename FA, typename FB, typename Epi, typename T = double>
+__device__ void tgemm(int M, int Nc, int K, FA fa, FB fb, bool lower_only, Smem &sm, Epi epi, T = T())
 {
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int wr = w >> 2, wc = ((w & 3) - wr) & 3;
     const int r0 = wr * 8 + (lane >> 3) * 2, c0 = wc * 16 + (lane & 7) * 2;
-    double *ga = sm.ta, *gb = sm.tb;
+    T *ga = (T *)sm.ta, *gb = (T *)sm.tb;
     for (int i0 = 0; i0 < M; i0 += GM)
         for (int j0 = 0; j0 < Nc; j0 += GN) {
             if (lower_only && j0 > i0 + GM - 1) continue;
             const bool active = (i0 + wr * 8 < M) && (j0 + wc * 16 < Nc) && !(lower_only && j0 + wc * 16 > i0 + wr * 8 + 7);
-            double a00 = 0.0, a01 = 0.0, a10 = 0.0, a11 = 0.0;
+            T a00 = 0, a01 = 0, a10 = 0, a11 = 0;
             for (int k0 = 0; k0 < K; k0 += GK) {
                 const int kc = min(GK, K - k0);
                 __syncthreads();
                 for (int t = tid; t < GM * GK; t += PDG_BLOCK) {
                     const int r = AK ? t / GK : t % GM, kk = AK ? t % GK : t / GM, gi = i0 + r;
-                    ga[kk * GA_LD + r] = (kk < kc && gi < M) ? fa(gi, k0 + kk) : 0.0;
+                    ga[kk * GA_LD + r] = (kk < kc && gi < M) ? (T)fa(gi, k0 + kk) : (T)0;
                 }
                 for (int t = tid; t < GK * GN; t += PDG_BLOCK) {
                     const int c = BK ? t / GK : t % GN, kk = BK ? t % GK : t / GN, gj = j0 + c;
-                    gb[kk * GB_LD + c] = (kk < kc && gj < Nc) ? fb(k0 + kk, gj) : 0.0;
+                    gb[kk * GB_LD + c] = (kk < kc && gj < Nc) ? (T)fb(k0 + kk, gj) : (T)0;
                 }
                 __syncthreads();
                 if (active) {
 #pragma unroll 4
                     for (int kk = 0; kk < kc; kk++) {
-                        const double x0 = ga[kk * GA_LD + r0], x1 = ga[kk * GA_LD + r0 + 1];
-                        const double y0 = gb[kk * GB_LD + c0], y1 = gb[kk * GB_LD + c0 + 1];
+                        const T x0 = ga[kk * GA_LD + r0], x1 = ga[kk * GA_LD + r0 + 1];
+                        const T y0 = gb[kk * GB_LD + c0], y1 = gb[kk * GB_LD + c0 + 1];
                         a00 = fma(x0, y0, a00); a01 = fma(x0, y1, a01); a10 = fma(x1, y0, a10); a11 = fma(x1, y1, a11);
                     }
                 }
             }
             if (active) {
                 const int gi = i0 + r0, gj = j0 + c0;
-                if (gi < M && gj < Nc) epi(gi, gj, a00);
-                if (gi < M && gj + 1 < Nc) epi(gi, gj + 1, a01);
-                if (gi + 1 < M && gj < Nc) epi(gi + 1, gj, a10);
-                if (gi + 1 < M && gj + 1 < Nc) epi(gi + 1, gj + 1, a11);
+                if (gi < M && gj < Nc) epi(gi, gj, (double)a00);
+                if (gi < M && gj + 1 < Nc) epi(gi, gj + 1, (double)a01);
+                if (gi + 1 < M && gj < Nc) epi(gi + 1, gj, (double)a10);
+                if (gi + 1 < M && gj + 1 < Nc) epi(gi + 1, gj + 1, (double)a11);
             }
         }
     __syncthreads();
@@ -605,9 +619,182 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
 }
 
 // ----------------------------------------------------------------------------------------------------
+// Mixed density step: SP2 purification (Niklasson's second-order spectral projection) with every product
+// X X on the tensor cores as kprod split-BF16 partial products accumulated in FP32 (N <= 144: one M = 128
+// tcgen05 tile, rows >= 128 by symmetry, the trailing corner on FP32 cores).  X0 = (e_max - F) / (e_max -
+// e_min) from Gershgorin bounds maps the occupied spectrum to [~1, 1]; each step takes X^2 or 2X - X^2,
+// whichever trace is closer to n_occ, until the idempotency defect tr X - tr X^2 stops falling.  P = X + X^T
+// (closed shell, symmetrised).  The FP32 iterate lives in the workspace matrix A; the BF16 parts in the
+// shared-memory slot of the packed matrix.  Returns the RMS change of P, or -1 when a tensor-core wait ran
+// out (P is then left unchanged).
+struct TCState { uint32_t tmem, bar, phase; };
+
+__device__ double density_step_mixed(const SCFArgs &a, double *wsf, const double *F, double *P, Smem &sm, Timer &tm,
+                                     TCState &tc, int kprod)
+{
+    const DeviceSystem &s = a.s;
+    const int N = s.n_basis, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int Kp = (N + 15) & ~15, R = Kp > TC_M ? Kp : TC_M, m2 = Kp - TC_M;   // second tile: rows m2 .. m2+127
+    const size_t NN4 = ((size_t)N * N + 3) & ~size_t(3);
+    float *Xa = (float *)(wsf + a.plan.A), *Xb = Xa + NN4, *P32 = Xb + NN4;
+    unsigned char *ph = (unsigned char *)sm.amat, *pm = ph + (size_t)R * Kp * 2;
+    const double nocc = (double)s.n_occ;
+    // Gershgorin bounds and X0 = (e_max - F) / (e_max - e_min)
+    double lo = 1e300, hi = -1e300;
+    for (int i = w; i < N; i += PDG_WARPS) {
+        double off = 0.0;
+        for (int j = lane; j < N; j += 32) if (j != i) off += fabs(F[(size_t)i * N + j]);
+        off = warp_sum(off);
+        const double d = F[(size_t)i * N + i];
+        lo = fmin(lo, d - off); hi = fmax(hi, d + off);
+    }
+    lo = -block_max(-lo, sm.red); hi = block_max(hi, sm.red);
+    const float scale = (float)(1.0 / fmax(hi - lo, 1e-12)), fhi = (float)hi;
+    float trl = 0.0f, sql = 0.0f;
+    for (int e = tid; e < N * N; e += PDG_BLOCK) {
+        const int i = e / N, j = e % N;
+        const float x = ((i == j ? fhi : 0.0f) - (float)F[e]) * scale;
+        Xa[e] = x;
+        trl += (i == j) ? x : 0.0f; sql = fmaf(x, x, sql);
+    }
+    double tr = block_sum((double)trl, sm.red), sq = block_sum((double)sql, sm.red);
+    double defect_1 = 1e300, defect_2 = 1e300;   // defects of the last two iterations
+    const int rr = 32 * (w & 3) + lane, nch = Kp / 16, half = (nch + 1) / 2, c0 = w < 4 ? 0 : half, c1 = w < 4 ? half : nch;
+    float *X = Xa, *Xn = Xb;
+    for (int it = 0; it < 100; it++) {
+        const bool square = fabs(sq - nocc) < fabs(2.0 * tr - sq - nocc);   // X <- X^2, else 2X - X^2
+        for (int e = tid; e < R * Kp; e += PDG_BLOCK) {   // BF16 parts of X; rows beyond N and the padding zero
+            const int r = e / Kp, c = e % Kp;
+            const float x = (r < N && c < N) ? X[(size_t)r * N + c] : 0.0f;
+            __nv_bfloat16 h, m, l;
+            bf16_split3(x, h, m, l);
+            const uint32_t o = tc_offset(r, c, Kp);
+            *(__nv_bfloat16 *)(ph + o) = h;
+            *(__nv_bfloat16 *)(pm + o) = m;
+        }
+        tc_fence_proxy();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        // tile 1: rows 0..127 x all Kp columns (tensor-memory columns 0..Kp-1); tile 2, when N > 128: rows
+        // m2..m2+127 x columns 128..Kp-1 (tensor-memory columns Kp..Kp+m2-1), whose last m2 lanes are the corner
+        const uint32_t t2 = tc.tmem + (uint32_t)Kp;
+        if (tid == 0) {
+            const uint32_t H = tc_smem_addr(ph), M = tc_smem_addr(pm);
+            tc_product(tc.tmem, H, 0, H, Kp, Kp, false);
+            tc_product(tc.tmem, H, 0, M, Kp, Kp, true);
+            tc_product(tc.tmem, M, 0, H, Kp, Kp, true);
+            if (kprod == 6) tc_product(tc.tmem, M, 0, M, Kp, Kp, true);
+            if (m2 > 0) {
+                tc_product(t2, H, m2, H, m2, Kp, false, TC_M);
+                tc_product(t2, H, m2, M, m2, Kp, true, TC_M);
+                tc_product(t2, M, m2, H, m2, Kp, true, TC_M);
+                if (kprod == 6) tc_product(t2, M, m2, M, m2, Kp, true, TC_M);
+            }
+            tc_commit(tc.bar);
+        }
+        bool ok = mbar_wait(tc.bar, tc.phase, 1 << 22);
+        tc.phase ^= 1u;
+        if (kprod == 6 && ok) {
+            // second phase: lo parts in the mid array (hi.lo + lo.hi)
+            tc_fence_after();
+            __syncthreads();
+            for (int e = tid; e < R * Kp; e += PDG_BLOCK) {
+                const int r = e / Kp, c = e % Kp;
+                const float x = (r < N && c < N) ? X[(size_t)r * N + c] : 0.0f;
+                __nv_bfloat16 h, m, l;
+                bf16_split3(x, h, m, l);
+                *(__nv_bfloat16 *)(pm + tc_offset(r, c, Kp)) = l;
+            }
+            tc_fence_proxy();
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+            if (tid == 0) {
+                const uint32_t H = tc_smem_addr(ph), L = tc_smem_addr(pm);
+                tc_product(tc.tmem, H, 0, L, Kp, Kp, true);
+                tc_product(tc.tmem, L, 0, H, Kp, Kp, true);
+                if (m2 > 0) { tc_product(t2, H, m2, L, m2, Kp, true, TC_M); tc_product(t2, L, m2, H, m2, Kp, true, TC_M); }
+                tc_commit(tc.bar);
+            }
+            ok = mbar_wait(tc.bar, tc.phase, 1 << 22);
+            tc.phase ^= 1u;
+        }
+        if (__syncthreads_or(!ok)) return -1.0;
+        tc_fence_after();
+        // X <- X X or 2X - X X.  X is symmetric up to rounding, so the new matrix is stored transposed:
+        // thread (row r) writes Xn[c][r] and reads the old X[c][r], both coalesced across the warp; the
+        // columns >= 128 of tile 1 also give rows >= 128 (Xn[r][c]), and tile 2's last lanes the corner.
+        float trn = 0.0f, sqn = 0.0f;
+        for (int ch = c0; ch < c1; ch++) {
+            float v[16];
+            tc_ld16(tc.tmem + ((uint32_t)(32 * (w & 3)) << 16) + (uint32_t)(ch * 16), v);
+            if (rr < N) {
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int c = ch * 16 + j;
+                    if (c >= N) continue;
+                    const float xo = X[(size_t)c * N + rr], xn = square ? v[j] : 2.0f * xo - v[j];
+                    Xn[(size_t)c * N + rr] = xn;
+                    if (c >= TC_M) Xn[(size_t)rr * N + c] = xn;
+                    sqn = fmaf((c >= TC_M) ? 2.0f * xn : xn, xn, sqn);
+                    if (c == rr) trn += xn;
+                }
+            }
+        }
+        if (m2 > 0 && w == 3) {   // lanes 128-m2 .. 127 of tile 2 hold corner rows 128 .. Kp-1
+            float v[16];
+            tc_ld16(t2 + ((uint32_t)96 << 16), v);
+            const int r = m2 + 96 + lane;   // matrix row of this lane in tile 2
+            if (r >= TC_M && r < N) {
+                for (int j = 0; j < m2 && j < 16; j++) {
+                    const int c = TC_M + j;
+                    if (c >= N) continue;
+                    const float xo = X[(size_t)c * N + r], xn = square ? v[j] : 2.0f * xo - v[j];
+                    Xn[(size_t)c * N + r] = xn;
+                    sqn = fmaf(xn, xn, sqn);
+                    if (c == r) trn += xn;
+                }
+            }
+        }
+        tc_fence_before();
+        tr = block_sum((double)trn, sm.red); sq = block_sum((double)sqn, sm.red);
+        float *tmp = X; X = Xn; Xn = tmp;
+        const double defect = tr - sq;   // sum of lambda (1 - lambda) over the spectrum
+        if (tid == 0) tm.slot[PDG_T_SP2_ITERATIONS] += 1.0;
+        // converged (after Kruchinina, Rudberg and Rubensson's criterion for SP2): in the asymptotic regime the
+        // defect falls quadratically every two steps until rounding dominates; stop at the first step where it
+        // no longer falls below the value two steps back.  The regime is entered only once every eigenvalue is
+        // within the products' precision of 0 or 1 (defect below 1e-3 for 3 partial products, 1e-5 for 6):
+        // before that, a nearly degenerate HOMO/LUMO pair separating slowly around 1/2 also stalls the defect.
+        const double floor_defect = kprod == 6 ? 1e-5 : 1e-3;
+        if ((defect < floor_defect && defect >= defect_2) || defect < 1e-9 * nocc || it >= 80) break;
+        defect_2 = defect_1; defect_1 = defect;
+    }
+    double rms = 0.0;
+    const int N4 = (N + 3) & ~3;
+    for (int e = tid; e < N * N; e += PDG_BLOCK) {
+        const int i = e / N, j = e % N;
+        const float p32 = X[(size_t)i * N + j] + X[(size_t)j * N + i];
+        P32[(size_t)i * N4 + j] = p32;
+        if (j == 0) for (int q = N; q < N4; q++) P32[(size_t)i * N4 + q] = 0.0f;
+        if (j > i) continue;
+        const double pn = (double)X[(size_t)i * N + j] + (double)X[(size_t)j * N + i];
+        const double dlt = pn - P[e];
+        rms += (i == j) ? dlt * dlt : 2.0 * dlt * dlt;
+        P[e] = pn;
+        if (i != j) P[(size_t)j * N + i] = pn;
+    }
+    const double out = sqrt(block_sum(rms, sm.red)) / (double)N;
+    if (tid == 0) tm.slot[PDG_T_PURIFICATION_STEPS] += 1.0;
+    tm.lap(PDG_T_PURIFICATION);
+    return out;
+}
+
+// ----------------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf(SCFArgs a)
 {
-    extern __shared__ double shm[];
+    extern __shared__ __align__(128) double shm[];
     const DeviceSystem &s = a.s;
     const FramePlan &pl = a.plan;
     const int f = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5, N = s.n_basis;
@@ -621,6 +808,12 @@ __global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf(SCFArgs 
     tm.slot = wsf + pl.misc + PDG_MAX_HISTORY * PDG_MAX_HISTORY;
     long long t_begin = clock64();
     if (tid < PDG_NTIMERS) tm.slot[tid] = 0.0;
+    if (tid == 0) {
+        unsigned int smid; unsigned long long gt;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(gt));
+        tm.slot[PDG_T_SM_ID] = (double)smid; tm.slot[PDG_T_START_NS] = (double)gt;
+    }
     __syncthreads();
     tm.start();
     // nuclear energy: sum of the pair terms in pair order
@@ -630,6 +823,25 @@ __global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf(SCFArgs 
     double base = 0.0;
     for (int A = tid; A < s.n_atoms; A += PDG_BLOCK) { const double *E = elem(s, s.atom_elem[A]); base += E[PDG_E_EHEAT] - E[PDG_E_EISOL]; }
     base = block_sum(base, sm.red);
+    // tensor memory and the completion barrier of the purification density step
+    __shared__ uint32_t tc_taddr_s;
+    __shared__ __align__(8) uint64_t tc_bar_s;
+    const bool want_mixed = a.fock_only != 1 && a.o.density_step != 0 && N <= 144 && sm.amat != nullptr;
+    TCState tc = { 0u, 0u, 0u };
+    // A CTA of a kernel that contains tcgen05 code holds the tensor-memory allocation permit until it allocates
+    // and relinquishes it (or exits), and no other such CTA is placed on its SM meanwhile: CTAs that will not
+    // allocate give it up at once, so that two frames share each SM in every mode.
+    if (!want_mixed && w == 0) asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    if (want_mixed) {
+        if (w == 0) tc_alloc(tc_smem_addr(&tc_taddr_s), 256);
+        if (tid == 0) mbar_init(tc_smem_addr(&tc_bar_s), 1);
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        tc.tmem = tc_taddr_s; tc.bar = tc_smem_addr(&tc_bar_s);
+    }
+    bool mixed = want_mixed, last_mixed = false;
+    int n_mixed = 0;
     bool valid = a.use_density != 0;
     if (!valid) {   // uniform diagonal guess (QCOnePDM.c:326-331)
         double g = (double)s.n_electrons / (double)N;
@@ -637,6 +849,23 @@ __global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf(SCFArgs 
     }
     __syncthreads();
     double e1, e2, eq;
+    if (a.fock_only == 2) {   // one density step for the given Fock matrices (pdg_density)
+        for (size_t k = tid; k < NN; k += PDG_BLOCK) F[k] = a.fock_out[(size_t)f * NN + k];
+        __syncthreads();
+        const double r = want_mixed ? density_step_mixed(a, wsf, F, P, sm, tm, tc, a.o.density_step) : density_step(a, wsf, F, P, sm, tm);
+        if (want_mixed) {
+            tc_fence_before();
+            __syncthreads();
+            if (w == 0) tc_dealloc(tc.tmem, 256);
+        }
+        if (tid == 0) {
+            double *E = a.energies + (size_t)f * PDG_NENERGY;
+            for (int k = 0; k < PDG_NENERGY; k++) E[k] = 0.0;
+            E[PDG_EN_RMS_DENSITY] = r;
+            a.status[f] = r < 0.0 ? PDG_TENSOR_TIMEOUT : PDG_OK;
+        }
+        return;
+    }
     if (a.fock_only) {
         fock_build(a, f, H, P, F, tei, sm, &e1, &e2, &eq);
         for (size_t k = tid; k < NN; k += PDG_BLOCK) a.fock_out[(size_t)f * NN + k] = F[k];
@@ -662,7 +891,7 @@ __global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf(SCFArgs 
         ncyc++;
         eel = e1 + e2 + eq;
         if (!isfinite(eel)) { st = PDG_NAN; break; }
-        converged = (iteration > 0) && (rms <= o.density_tolerance) && (deltaeold <= o.energy_tolerance);
+        converged = (iteration > 0) && !last_mixed && (rms <= o.density_tolerance) && (deltaeold <= o.energy_tolerance);
         if (converged) break;
         double deltae = eel - eold, etemp = eel;
         if (valid) {
@@ -698,9 +927,42 @@ __global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf(SCFArgs 
                         emx = fmax(emx, fabs(ev));
                     });
             } else {
+                // full commutator: FP64, or FP32 after a purification step (whose density carries BF16-level
+                // errors anyway)
                 double *FP = wsf + pl.A;
-                tgemm<true, false>(N, N, N, [&](int i, int k) { return F[(size_t)i * N + k]; }, [&](int k, int j) { return P[(size_t)k * N + j]; },
-                                   false, sm, [&](int i, int j, double v) { FP[(size_t)i * N + j] = v; });
+                if (last_mixed) {
+                    // FP32 outer products over k: thread block (i0..i0+3, j0..j0+3) += F[k][i0..] (x) P[k][j0..]
+                    // (F symmetric), operands read as float4 rows with no shared-memory staging or barriers
+                    const int N4 = (N + 3) & ~3;
+                    float *F32 = (float *)(wsf + pl.P0);
+                    const float *P32 = (const float *)(wsf + pl.A) + 2 * (((size_t)N * N + 3) & ~size_t(3));
+                    for (int e = tid; e < N * N4; e += PDG_BLOCK) {
+                        const int i = e / N4, j = e % N4;
+                        F32[e] = j < N ? (float)F[(size_t)i * N + j] : 0.0f;
+                    }
+                    __syncthreads();
+                    const int nb4 = N4 / 4;
+                    for (int t = tid; t < nb4 * nb4; t += PDG_BLOCK) {
+                        const int i0 = (t / nb4) * 4, j0 = (t % nb4) * 4;
+                        float acc[4][4] = {};
+#pragma unroll 4
+                        for (int k = 0; k < N; k++) {
+                            const float4 fa = *(const float4 *)(F32 + (size_t)k * N4 + i0);
+                            const float4 pb = *(const float4 *)(P32 + (size_t)k * N4 + j0);
+                            const float av[4] = { fa.x, fa.y, fa.z, fa.w }, bv[4] = { pb.x, pb.y, pb.z, pb.w };
+#pragma unroll
+                            for (int x = 0; x < 4; x++)
+#pragma unroll
+                                for (int y = 0; y < 4; y++) acc[x][y] = fmaf(av[x], bv[y], acc[x][y]);
+                        }
+                        for (int x = 0; x < 4; x++)
+                            for (int y = 0; y < 4; y++)
+                                if (i0 + x < N && j0 + y < N) FP[(size_t)(i0 + x) * N + j0 + y] = (double)acc[x][y];
+                    }
+                    __syncthreads();
+                } else
+                    tgemm<true, false>(N, N, N, [&](int i, int k) { return F[(size_t)i * N + k]; }, [&](int k, int j) { return P[(size_t)k * N + j]; },
+                                       false, sm, [&](int i, int j, double v) { FP[(size_t)i * N + j] = v; });
                 for (int i = tid / 32; i < N; i += PDG_WARPS)
                     for (int j = tid % 32; j < i; j += 32) {
                         const double ev = FP[(size_t)i * N + j] - FP[(size_t)j * N + i];
@@ -811,9 +1073,26 @@ __global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf(SCFArgs 
         deltaeold = deltae; eold = etemp;
         __syncthreads();
         tm.lap(PDG_T_ITERATE);
-        rms = density_step(a, wsf, F, P, sm, tm);
+        if (mixed) {
+            rms = density_step_mixed(a, wsf, F, P, sm, tm, tc, o.density_step);
+            if (rms < 0.0) { st = PDG_TENSOR_TIMEOUT; break; }
+            last_mixed = true;
+            have_z = false;
+            // leave purification once the density has settled to its accuracy, or when it stalls
+            n_mixed++;
+            if (rms < o.mixed_switch || n_mixed >= 20) mixed = false;
+        } else {
+            rms = density_step(a, wsf, F, P, sm, tm);
+            last_mixed = false;
+            have_z = true;
+        }
+        if (tid == 0 && ncyc <= PDG_RMS_HISTORY) tm.slot[PDG_T_RMS_HISTORY + ncyc - 1] = last_mixed ? -rms : rms;
         valid = true;
-        have_z = true;
+    }
+    if (want_mixed) {
+        tc_fence_before();
+        __syncthreads();
+        if (w == 0) tc_dealloc(tc.tmem, 256);
     }
     if (converged) st = PDG_OK;
     if (tid == 0) {
@@ -822,11 +1101,27 @@ __global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf(SCFArgs 
         a.status[f] = st;
         if (a.ncycles) a.ncycles[f] = iteration;
         tm.slot[PDG_T_TOTAL] = (double)(clock64() - t_begin);
+        unsigned long long gt;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(gt));
+        tm.slot[PDG_T_END_NS] = (double)gt;
         tm.slot[PDG_T_CYCLES] = (double)ncyc;
     }
 }
 
 size_t scf_smem_bytes(int N, int kv) { return smem_plan(N, kv).bytes; }
+
+int scf_occupancy(const DeviceSystem &s, int *threads, int *smem_bytes, int *ctas_per_sm)
+{
+    const size_t sm = scf_smem_bytes(s.n_basis, s.n_vec);
+    if (sm > 48 * 1024) {
+        cudaFuncSetAttribute(k_scf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_scf, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    }
+    int n = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_scf, PDG_BLOCK, sm);
+    *threads = PDG_BLOCK; *smem_bytes = (int)sm; *ctas_per_sm = n;
+    return e == cudaSuccess ? 0 : 1;
+}
 
 void launch_scf(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *phi, const pdg_scf_options &o,
                 double *density, int use_density, double *energies, double *charges, int *status, int *ncycles,
@@ -840,6 +1135,8 @@ void launch_scf(const DeviceSystem &s, const FramePlan &p, int n_frames, const d
     static size_t configured = 0;
     if (sm > 48 * 1024 && sm > configured) {
         cudaFuncSetAttribute(k_scf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        // two SCF CTAs per SM need the largest shared-memory carveout
+        cudaFuncSetAttribute(k_scf, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
         configured = sm;
     }
     k_scf<<<n_frames, PDG_BLOCK, sm, st>>>(a);

@@ -96,14 +96,15 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float *v)
     for (int k = 0; k < 16; k++) v[k] = __uint_as_float(r[k]);
 }
 
-// Issue D[0:128, 0:Nn] (+)= A[m0 : m0+128, 0:Kp] * B[0:Nn, 0:Kp]^T, K-major operands in the canonical
+// Issue D[0:128, 0:Nn] (+)= A[m0 : m0+128, 0:Kp] * B[n0 : n0+Nn, 0:Kp]^T, K-major operands in the canonical
 // layout (A and B may be the same array), one instruction per 16-deep K chunk.  One thread only.
-__device__ __forceinline__ void tc_product(uint32_t d_tmem, uint32_t a_base, int m0, uint32_t b_base, int Nn, int Kp, bool accumulate)
+__device__ __forceinline__ void tc_product(uint32_t d_tmem, uint32_t a_base, int m0, uint32_t b_base, int Nn, int Kp, bool accumulate,
+                                           int n0 = 0)
 {
     const uint32_t idesc = tc_idesc_bf16(TC_M, Nn), sbo = (uint32_t)Kp * 16u;
     for (int k0 = 0; k0 < Kp; k0 += 16) {
         const uint64_t a = tc_desc(a_base + tc_offset(m0, k0, Kp), 128u, sbo);
-        const uint64_t b = tc_desc(b_base + tc_offset(0, k0, Kp), 128u, sbo);
+        const uint64_t b = tc_desc(b_base + tc_offset(n0, k0, Kp), 128u, sbo);
         tc_mma(d_tmem, a, b, idesc, (accumulate || k0 > 0) ? 1u : 0u);
     }
 }

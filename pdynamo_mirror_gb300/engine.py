@@ -126,6 +126,24 @@ class QCEngine:
                                      _native.stream_handle(torch.cuda.current_stream(self.device))), "pdg_scf")
         return energies, status, ncycles
 
+    def density_step(self, fock, density_step=0, previous=None):
+        """pdg_density: one density step for Fock matrices fock [F, N, N] (device float64)."""
+        F = fock.shape[0]
+        ws = self.workspace(F)
+        P = previous.clone() if previous is not None else torch.zeros_like(fock)
+        en = torch.empty((F, _native.NENERGY), dtype=torch.float64, device=self.device)
+        st = torch.empty(F, dtype=torch.int32, device=self.device)
+        _native.check(self.L.pdg_density(self.handle, F, _native.ptr(fock.contiguous()), int(density_step), _native.ptr(P), _native.ptr(en),
+                                         _native.ptr(st), _native.ptr(ws), ws.numel(), _native.stream_handle(torch.cuda.current_stream(self.device))),
+                      "pdg_density")
+        return P, en, st
+
+    def occupancy(self):
+        """(threads per SCF CTA, dynamic shared bytes, resident SCF CTAs per SM)."""
+        t, b, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _native.check(self.L.pdg_scf_occupancy(self.handle, ctypes.byref(t), ctypes.byref(b), ctypes.byref(n)), "pdg_scf_occupancy")
+        return t.value, b.value, n.value
+
     def timings(self, n_frames):
         """Per-frame SCF phase timings (GPU clock cycles) of the last run, as {name: array}."""
         out = torch.empty((n_frames, len(_native.TIMERS)), dtype=torch.float64, device=self.device)

@@ -231,3 +231,43 @@ def test_scf_alone_reproduces_energy_gradients():
     assert (st.cpu().numpy() == 0).all()
     np.testing.assert_allclose(e2.cpu().numpy()[:, :7], e1[:, :7], rtol=0, atol=1e-12)
     assert (nc.cpu().numpy() == out["ncycles"].cpu().numpy()).all()
+
+
+@pytest.mark.parametrize("products", [3, 6])
+def test_purification_density_step_converges_to_the_fp64_result(products):
+    """Split-BF16 purification cycles followed by FP64 cycles reach the plain FP64 path's converged
+    energies and gradients (the last cycles are FP64, so the difference is convergence-level)."""
+    from pdynamo_mirror_gb300 import DIISSCFConverger, QCModelMNDO, System, workloads
+    Z, X = workloads.water_cluster(16, seed=0)
+    frames = workloads.perturbed_frames(X, 4, sigma=0.03, seed=5)
+    out = {}
+    for step in ("fp64", "purification"):
+        s = System(Z, X)
+        s.DefineQCModel(QCModelMNDO("am1", converger=DIISSCFConverger(densityStep=step, purificationProducts=products)))
+        out[step] = s.EnergyBatch(frames, doGradients=True, warmStart=False)
+    (E0, G0, _), (E1, G1, t1) = out["fp64"], out["purification"]
+    assert np.abs(E1 - E0).max() / KJ < 1e-8
+    assert np.abs(G1 - G0).max() / (A2B * KJ) < 1e-6
+    assert (t1["Status"] == 0).all()
+
+
+def test_purification_qcmm_water_box_matches_oracle():
+    """The benchmark system with the purification density step: same gate against the oracle."""
+    from pdynamo_mirror_gb300 import DIISSCFConverger, NBModelABFS, QCModelMNDO, System, workloads
+    Z, X, Q, sel, charge = workloads.qcmm_water_box(seed=1)
+    s = System(Z, X, mmCharges=Q)
+    s.electronicState.charge = charge
+    s.DefineQCModel(QCModelMNDO("am1", converger=DIISSCFConverger(densityStep="purification")), qcSelection=sel)
+    s.DefineNBModel(NBModelABFS(innerCutoff=8.0, outerCutoff=12.0))
+    s.Energy(doGradients=True)
+    t = s.configuration.energyTerms
+    nq = len(sel)
+    knots = O.abfs_knots(8.0, 12.0)
+    phi, _, _ = O.qcmm("abfs", X[:nq], X[nq:], Q[nq:], knots=knots)
+    r = O.System(O.Hamiltonian("am1", Z[:nq]), list(Z[:nq]), charge=charge).energy(X[:nq], phi=phi)
+    _, gq, gm = O.qcmm("abfs", X[:nq], X[nq:], Q[nq:], qcq=r["charges"], knots=knots)
+    assert abs(t["Pure QC"] / KJ - (r["eelectronic"] + r["enuclear"] + r["baseline"])) < E_TOL
+    assert abs(t["QC/MM Elect."] / KJ - r["eqcmm"]) < E_TOL
+    g = s.configuration.gradients3 / (A2B * KJ)
+    assert np.abs(g[:nq] - (r["gradients"] + gq)).max() < G_TOL
+    assert np.abs(g[nq:] - gm).max() < G_TOL
