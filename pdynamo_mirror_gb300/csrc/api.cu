@@ -105,6 +105,12 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     const size_t cel_at = ints.size();
     ints.insert(ints.end(), cel.begin(), cel.end());
     ints.insert(ints.end(), xel.begin(), xel.end());
+    // s-s pairs (thread-per-pair kernels) and the others (warp-per-pair kernels)
+    std::vector<int> pss, pgen;
+    for (int p = 0; p < npairs; p++) (norb[pi[p]] == 1 && norb[pj[p]] == 1 ? pss : pgen).push_back(p);
+    const size_t pl_at = ints.size();
+    ints.insert(ints.end(), pss.begin(), pss.end());
+    ints.insert(ints.end(), pgen.begin(), pgen.end());
     int rc = PDG_OK;
     if ((rc = cuda_check(cudaMalloc(&s->d_elements, sizeof(double) * s->elements.size()), "cudaMalloc elements")) ||
         (rc = cuda_check(cudaMalloc(&s->d_terms, sizeof(double) * terms.size()), "cudaMalloc terms")) ||
@@ -128,6 +134,7 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     d.pair_i = b + 3 * n_atoms; d.pair_j = d.pair_i + npairs; d.pair_tei = d.pair_j + npairs;
     d.ovl = s->d_ovl; d.ovl_off = d.pair_tei + npairs; d.ovl_n = d.ovl_off + n_elements * n_elements;
     d.cel = b + cel_at; d.xel = d.cel + cel.size(); d.n_cel = (int)cel.size(); d.n_xel = (int)xel.size();
+    d.pairs_ss = b + pl_at; d.pairs_gen = d.pairs_ss + pss.size(); d.n_ss = (int)pss.size(); d.n_gen = (int)pgen.size();
     *out = s;
     return PDG_OK;
 }

@@ -33,6 +33,8 @@ struct DeviceSystem {
     const int *ovl_off, *ovl_n;    // per ordered element pair: first record, record count
     const int *cel, *xel;          // Fock outputs: diagonal-block elements (atom << 4 | mn), off-diagonal (pair << 4 | ac)
     int n_cel, n_xel;
+    const int *pairs_ss, *pairs_gen;   // pairs of two one-orbital (s) atoms, and all other pairs, in pair order
+    int n_ss, n_gen;
 };
 
 // Per-frame workspace plan (all offsets in doubles from the frame's base).

@@ -78,15 +78,15 @@ __device__ double core_core(const double *a, const double *b, double r, double *
 #define PI_WARPS 8
 #define PI_SM 640
 
-// Pair batches: a warp takes pairs b0 .. b0 + nb - 1 (nb <= 32) of frame f.
+// Pair batches: a warp takes entries b0 .. b0 + nb - 1 (nb <= 32) of frame f's list of pairs that are not s-s.
 __device__ __forceinline__ bool pair_batch(const DeviceSystem &s, int n_frames, int warps_per_block, int &f, int &b0, int &nb)
 {
-    const int nbatch = (s.n_pairs + 31) / 32;
+    const int nbatch = (s.n_gen + 31) / 32;
     const long gw = (long)blockIdx.x * warps_per_block + (threadIdx.x >> 5);
     if (gw >= (long)n_frames * nbatch) return false;
     f = (int)(gw / nbatch);
     b0 = (int)(gw % nbatch) * 32;
-    nb = min(32, s.n_pairs - b0);
+    nb = min(32, s.n_gen - b0);
     return true;
 }
 
@@ -114,7 +114,7 @@ k_pair_integrals(DeviceSystem s, FramePlan plan, int n_frames, const double *__r
     double mx = 0.0, my = 0.0, mz = 0.0, mr = 1.0;
     RotScalars mq = {};
     if (lane < nb) {
-        const int p = b0 + lane;
+        const int p = s.pairs_gen[b0 + lane];
         mi = s.pair_i[p]; mj = s.pair_j[p];
         mx = R[3 * mj] - R[3 * mi]; my = R[3 * mj + 1] - R[3 * mi + 1]; mz = R[3 * mj + 2] - R[3 * mi + 2];
         mr = sqrt(mx * mx + my * my + mz * mz);
@@ -122,7 +122,7 @@ k_pair_integrals(DeviceSystem s, FramePlan plan, int n_frames, const double *__r
         rot_scalars(mx, my, mz, mr, max(s.atom_norb[mi], s.atom_norb[mj]), false, mq);
     }
     for (int t = 0; t < nb; t++) {
-        const int p = b0 + t;
+        const int p = s.pairs_gen[b0 + t];
         const int i = __shfl_sync(0xffffffffu, mi, t), j = __shfl_sync(0xffffffffu, mj, t);
         const double x = __shfl_sync(0xffffffffu, mx, t), y = __shfl_sync(0xffffffffu, my, t), z = __shfl_sync(0xffffffffu, mz, t);
         const double r = __shfl_sync(0xffffffffu, mr, t);
@@ -188,6 +188,45 @@ k_pair_integrals(DeviceSystem s, FramePlan plan, int n_frames, const double *__r
     }
 }
 
+// s-s pairs (two one-orbital atoms), one thread per pair: the (ss|ss) integral and the two electron-core
+// terms (the single multipole terms 0, MP_CORE_I and MP_CORE_J; no rotation), the resonance integral from
+// the ss radial sum, and the core-core energy.  Same results as the general kernel, without its warp-wide
+// machinery for a pair that has one integral.
+__global__ void __launch_bounds__(256) k_pair_integrals_ss(DeviceSystem s, FramePlan plan, int n_frames, const double *__restrict__ xyz,
+                                                          const double *__restrict__ terms, double *__restrict__ ws)
+{
+    const long g = (long)blockIdx.x * 256 + threadIdx.x;
+    if (g >= (long)n_frames * s.n_ss) return;
+    const int f = (int)(g / s.n_ss), p = s.pairs_ss[g % s.n_ss];
+    const int i = s.pair_i[p], j = s.pair_j[p], eli = s.atom_elem[i], elj = s.atom_elem[j];
+    const double *Ei = elem(s, eli), *Ej = elem(s, elj);
+    const double *R = xyz + (size_t)f * 3 * s.n_atoms;
+    const double x = R[3 * j] - R[3 * i], y = R[3 * j + 1] - R[3 * i + 1], z = R[3 * j + 2] - R[3 * i + 2];
+    const double R2 = x * x + y * y + z * z, r = sqrt(R2);
+    double *wsf = ws + (size_t)f * plan.stride;
+    const double *to = terms + (size_t)(eli * s.n_elements + elj) * 2 * MP_NTERMS, *ta = to + MP_NTERMS;
+    const double s0 = rsqrt((r + to[0]) * (r + to[0]) + ta[0]);
+    const double ci = rsqrt((r + to[MP_CORE_I]) * (r + to[MP_CORE_I]) + ta[MP_CORE_I]);
+    const double cj = rsqrt((r + to[MP_CORE_J]) * (r + to[MP_CORE_J]) + ta[MP_CORE_J]);
+    wsf[plan.tei + s.pair_tei[p]] = (fabs(s0) > PDG_TEI_UNDERFLOW) ? s0 : 0.0;
+    double *pe = wsf + plan.pair_e + (size_t)p * PDG_PAIR_E_STRIDE;
+    pe[0] = -Ej[PDG_E_ZCORE] * ci;
+    pe[10] = -Ei[PDG_E_ZCORE] * cj;
+    pe[20] = core_core(Ei, Ej, r, nullptr);
+    const int eo = eli * s.n_elements + elj;
+    const double *rec = s.ovl + (size_t)s.ovl_off[eo] * OV_REC;
+    double S = 0.0;
+    for (int t = 0; t < s.ovl_n[eo]; t++) {
+        const double fac = rec[OV_REC * t] * R2;
+        if (fac <= PRIMITIVE_OVERLAP_TOLERANCE) S = fma(rec[OV_REC * t + 1], exp(-fac), S);
+    }
+    const int N = s.n_basis, is = s.atom_start[i], js = s.atom_start[j];
+    const double v = S * 0.5 * (Ei[PDG_E_BETA] + Ej[PDG_E_BETA]);
+    double *H = wsf + plan.H;
+    H[(size_t)is * N + js] = v;
+    H[(size_t)js * N + is] = v;
+}
+
 __global__ void __launch_bounds__(256) k_assemble_h(DeviceSystem s, FramePlan plan, int n_frames, double *__restrict__ ws)
 {
     const int lane = threadIdx.x & 31;
@@ -217,11 +256,13 @@ __global__ void __launch_bounds__(256) k_assemble_h(DeviceSystem s, FramePlan pl
 
 void launch_pair_integrals(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *xyz, double *ws, cudaStream_t st)
 {
-    long warps = (long)n_frames * ((s.n_pairs + 31) / 32);
+    long warps = (long)n_frames * ((s.n_gen + 31) / 32);
     if (warps > 0) {
         int blocks = (int)((warps + PI_WARPS - 1) / PI_WARPS);
         k_pair_integrals<<<blocks, PI_WARPS * 32, 0, st>>>(s, p, n_frames, xyz, s.terms, ws);
     }
+    const long nss = (long)n_frames * s.n_ss;
+    if (nss > 0) k_pair_integrals_ss<<<(int)((nss + 255) / 256), 256, 0, st>>>(s, p, n_frames, xyz, s.terms, ws);
 }
 
 void launch_assemble_h(const DeviceSystem &s, const FramePlan &p, int n_frames, double *ws, cudaStream_t st)
@@ -255,7 +296,7 @@ k_pair_gradients(DeviceSystem s, FramePlan plan, int n_frames, const double *__r
     double mx = 0.0, my = 0.0, mz = 0.0, mr = 1.0, mdc = 0.0;
     RotScalars mq = {};
     if (lane < nb) {
-        const int p = b0 + lane;
+        const int p = s.pairs_gen[b0 + lane];
         mi = s.pair_i[p]; mj = s.pair_j[p];
         mx = R[3 * mj] - R[3 * mi]; my = R[3 * mj + 1] - R[3 * mi + 1]; mz = R[3 * mj + 2] - R[3 * mi + 2];
         mr = sqrt(mx * mx + my * my + mz * mz);
@@ -263,7 +304,7 @@ k_pair_gradients(DeviceSystem s, FramePlan plan, int n_frames, const double *__r
         rot_scalars(mx, my, mz, mr, max(s.atom_norb[mi], s.atom_norb[mj]), true, mq);
     }
     for (int t = 0; t < nb; t++) {
-        const int p = b0 + t;
+        const int p = s.pairs_gen[b0 + t];
         const int i = __shfl_sync(0xffffffffu, mi, t), j = __shfl_sync(0xffffffffu, mj, t);
         const double v3[3] = { __shfl_sync(0xffffffffu, mx, t), __shfl_sync(0xffffffffu, my, t), __shfl_sync(0xffffffffu, mz, t) };
         const double r = __shfl_sync(0xffffffffu, mr, t), dcore = __shfl_sync(0xffffffffu, mdc, t);
@@ -379,6 +420,51 @@ k_pair_gradients(DeviceSystem s, FramePlan plan, int n_frames, const double *__r
     }
 }
 
+// s-s pairs, one thread per pair: the gradient terms of k_pair_gradients for a pair with one orbital on each
+// atom (no rotation, Gamma = P_ij^2 / 2 - P_ii P_jj), with the resonance term from the ss radial sums.
+__global__ void __launch_bounds__(256) k_pair_gradients_ss(DeviceSystem s, FramePlan plan, int n_frames, const double *__restrict__ xyz,
+                                                          const double *__restrict__ terms, const double *__restrict__ density,
+                                                          double *__restrict__ ws)
+{
+    const long g = (long)blockIdx.x * 256 + threadIdx.x;
+    if (g >= (long)n_frames * s.n_ss) return;
+    const int f = (int)(g / s.n_ss), p = s.pairs_ss[g % s.n_ss];
+    const int i = s.pair_i[p], j = s.pair_j[p], eli = s.atom_elem[i], elj = s.atom_elem[j];
+    const double *Ei = elem(s, eli), *Ej = elem(s, elj);
+    const double *R = xyz + (size_t)f * 3 * s.n_atoms;
+    const double v3[3] = { R[3 * j] - R[3 * i], R[3 * j + 1] - R[3 * i + 1], R[3 * j + 2] - R[3 * i + 2] };
+    const double R2 = v3[0] * v3[0] + v3[1] * v3[1] + v3[2] * v3[2], r = sqrt(R2);
+    const int N = s.n_basis, is = s.atom_start[i], js = s.atom_start[j];
+    const double *P = density + (size_t)f * N * N;
+    const double pii = P[(size_t)is * N + is], pjj = P[(size_t)js * N + js], pij = P[(size_t)is * N + js];
+    double eng[3] = { 0.0, 0.0, 0.0 };
+    if (r >= 5.0e-3) {
+        double dcore = 0.0;
+        core_core(Ei, Ej, r, &dcore);
+        const double *to = terms + (size_t)(eli * s.n_elements + elj) * 2 * MP_NTERMS, *ta = to + MP_NTERMS;
+        const double ro = r + to[0], sv = rsqrt(ro * ro + ta[0]), ds0 = -ro * sv * sv * sv;
+        const double roi = r + to[MP_CORE_I], svi = rsqrt(roi * roi + ta[MP_CORE_I]), dci = -roi * svi * svi * svi;
+        const double roj = r + to[MP_CORE_J], svj = rsqrt(roj * roj + ta[MP_CORE_J]), dcj = -roj * svj * svj * svj;
+        const double gam = 0.5 * pij * pij - pii * pjj;
+        const double t0 = gam * ds0;
+        const double o0 = pii * dci * (-Ej[PDG_E_ZCORE]) + pjj * dcj * (-Ei[PDG_E_ZCORE]);
+        for (int x = 0; x < 3; x++) {
+            const double sx = v3[x] / r;
+            eng[x] = -sx * dcore - sx * o0 + sx * t0;
+        }
+    }
+    const int eo = eli * s.n_elements + elj;
+    const double *rec = s.ovl + (size_t)s.ovl_off[eo] * OV_REC;
+    double D = 0.0;
+    for (int t = 0; t < s.ovl_n[eo]; t++) {
+        const double abg = rec[OV_REC * t], fac = abg * R2;
+        if (fac <= PRIMITIVE_OVERLAP_TOLERANCE) D = fma((abg + abg) * rec[OV_REC * t + 1], exp(-fac), D);
+    }
+    const double w = (Ei[PDG_E_BETA] + Ej[PDG_E_BETA]) * pij;
+    double *pg = ws + (size_t)f * plan.stride + plan.pair_g + (size_t)p * 3;
+    for (int x = 0; x < 3; x++) pg[x] = eng[x] + v3[x] * w * D;
+}
+
 __global__ void __launch_bounds__(256) k_reduce_gradients(DeviceSystem s, FramePlan plan, int n_frames,
                                                           const double *__restrict__ ws, double *__restrict__ grad)
 {
@@ -402,9 +488,11 @@ __global__ void __launch_bounds__(256) k_reduce_gradients(DeviceSystem s, FrameP
 void launch_pair_gradients(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *xyz,
                            const double *density, double *ws, cudaStream_t st)
 {
-    long warps = (long)n_frames * ((s.n_pairs + 31) / 32);
+    long warps = (long)n_frames * ((s.n_gen + 31) / 32);
     if (warps > 0)
         k_pair_gradients<<<(int)((warps + PG_WARPS - 1) / PG_WARPS), PG_WARPS * 32, 0, st>>>(s, p, n_frames, xyz, s.terms, density, ws);
+    const long nss = (long)n_frames * s.n_ss;
+    if (nss > 0) k_pair_gradients_ss<<<(int)((nss + 255) / 256), 256, 0, st>>>(s, p, n_frames, xyz, s.terms, density, ws);
 }
 
 void launch_reduce_gradients(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *ws, double *grad, cudaStream_t st)
