@@ -208,6 +208,37 @@ int pdg_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const double
                        int n_knots, const double *d_knots, double outer_cutoff,
                        double *d_qc_grad, double *d_mm_grad, void *stream);
 
+/* Learned start density (no counterpart in the reference, whose SCF starts from the diagonal guess,
+ * QCOnePDM.c:280, or from the previous density).  A per-atom-pair MLP (64 features -> 256 -> 256 -> 16, SiLU,
+ * BF16 weights, FP32 accumulation) predicts, for every pair closer than 3.5 A, its density block and
+ * one-centre contributions in the pair's local frame; pdg_guess_assemble rotates them into a start density.
+ * Rows (pairs) of all frames are stored consecutively; *d_rows-style arguments point at the device count
+ * (d_offsets[n_frames]), and max_rows = n_frames * n_pairs bounds every buffer.
+ *   pdg_guess_features  d_xyz (Angstrom, n_frames * n_atoms * 3), d_phi (QC/MM potentials or NULL) ->
+ *                       d_env (n_frames * n_atoms * 8), d_count (n_frames), d_offsets (n_frames + 1),
+ *                       d_x (max_rows * 64), d_row_frame, d_row_pair (max_rows)
+ *   pdg_mlp_forward     d_h = act(d_x W^T + b) (act 1: SiLU, 0: none), d_z = the pre-activation (or NULL);
+ *                       W n x k BF16, rows x k in, rows x n out
+ *   pdg_mlp_backward    d_dzin = (d_dz W) * SiLU'(d_zin) (if d_dzin), and per row segment the weight and bias
+ *                       gradients d_part[segments][n][k + 1] from d_dz and the layer input d_hin
+ *   pdg_mlp_adam        Adam step on the FP32 master weights d_wm (n x k) and biases d_bm (n) from the summed
+ *                       segment gradients times scale; refreshes the BF16 weights d_w
+ *   pdg_guess_assemble  start densities d_density (n_frames * N * N) from the outputs d_y (max_rows * 16)
+ *   pdg_guess_loss      squared error of the assembled blocks against d_target; d_dy (max_rows * 16) its
+ *                       gradient with respect to the outputs, d_loss (n_frames) */
+int pdg_guess_features(pdg_system *sys, int n_frames, const double *d_xyz, const double *d_phi, float *d_env, int *d_count,
+                       int *d_offsets, float *d_x, int *d_row_frame, int *d_row_pair, void *stream);
+int pdg_mlp_forward(int max_rows, const int *d_rows, int k, int n, const float *d_x, const void *d_w, const float *d_b,
+                    float *d_z, float *d_h, int act, void *stream);
+int pdg_mlp_backward(int max_rows, const int *d_rows, int n, int k, const float *d_dz, const void *d_w, const float *d_zin,
+                     const float *d_hin, float *d_dzin, int segments, float *d_part, void *stream);
+int pdg_mlp_adam(int n, int k, int segments, const float *d_part, float scale, float *d_wm, float *d_bm, float *d_m1, float *d_m2,
+                 void *d_w, float lr, float beta1, float beta2, int step, void *stream);
+int pdg_guess_assemble(pdg_system *sys, int n_frames, const double *d_xyz, const int *d_offsets, const int *d_row_pair,
+                       const float *d_y, double *d_density, void *stream);
+int pdg_guess_loss(pdg_system *sys, int n_frames, const double *d_xyz, const int *d_offsets, const int *d_row_pair,
+                   const double *d_density, const double *d_target, float *d_dy, double *d_loss, void *stream);
+
 /* Check of the tensor-core (tcgen05) split-BF16 product used by the purification density step:
  * d_c = X X for a symmetric n x n FP32 matrix d_x (n <= 144), with kprod = 1, 3 or 6 BF16 partial
  * products accumulated in FP32.  d_status (one int) is 0, or 1 when the tensor-core completion wait ran out.

@@ -2,12 +2,14 @@
 
 Public surface (mirroring pDynamo 1.9.0's names):
     QCModelMNDO, DIISSCFConverger, NBModelABFS, NBModelFull, System, ElectronicState
+and, beyond the reference, LearnedDensityGuess (System.DefineDensityGuess).
 The compute path is libpdg.so (CUDA, include/pdg.h); nothing here computes on the CPU.
 """
 
 from .converger import DIISSCFConverger
+from .guess import LearnedDensityGuess
 from .nbmodel import NBModelABFS, NBModelFull
 from .qcmodel import QCModelMNDO
 from .system import ElectronicState, SCFNotConverged, System
 
-__all__ = ["DIISSCFConverger", "ElectronicState", "NBModelABFS", "NBModelFull", "QCModelMNDO", "SCFNotConverged", "System"]
+__all__ = ["DIISSCFConverger", "ElectronicState", "LearnedDensityGuess", "NBModelABFS", "NBModelFull", "QCModelMNDO", "SCFNotConverged", "System"]

@@ -16,7 +16,8 @@ MAX_HISTORY = 16
 
 EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system_info", "pdg_workspace_bytes",
            "pdg_energy_gradients", "pdg_scf", "pdg_density", "pdg_one_electron", "pdg_fock", "pdg_gradients", "pdg_qcmm_potentials",
-           "pdg_qcmm_gradients", "pdg_scf_timings", "pdg_gradients_static_scratch", "pdg_tc_selftest", "pdg_scf_occupancy", "pdg_last_error")
+           "pdg_qcmm_gradients", "pdg_scf_timings", "pdg_gradients_static_scratch", "pdg_tc_selftest", "pdg_scf_occupancy", "pdg_guess_features", "pdg_mlp_forward",
+           "pdg_mlp_backward", "pdg_mlp_adam", "pdg_guess_assemble", "pdg_guess_loss", "pdg_last_error")
 TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densities Tridiagonal", "QC Densities Eigenvalues",
           "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds",
           "QC Densities Cluster Rounds", "QC Densities Steps", "QC Densities Purification",
@@ -64,6 +65,13 @@ def load(path=LIB_PATH):
     L.pdg_gradients_static_scratch.argtypes = [P, I, P, P, P, P]
     L.pdg_tc_selftest.argtypes = [I, I, P, P, P, P]
     L.pdg_scf_occupancy.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]
+    F = ctypes.c_float
+    L.pdg_guess_features.argtypes = [P, I, P, P, P, P, P, P, P, P, P]
+    L.pdg_mlp_forward.argtypes = [I, P, I, I, P, P, P, P, P, I, P]
+    L.pdg_mlp_backward.argtypes = [I, P, I, I, P, P, P, P, P, I, P, P]
+    L.pdg_mlp_adam.argtypes = [I, I, I, P, F, P, P, P, P, P, F, F, F, I, P]
+    L.pdg_guess_assemble.argtypes = [P, I, P, P, P, P, P, P]
+    L.pdg_guess_loss.argtypes = [P, I, P, P, P, P, P, P, P, P]
     L.pdg_qcmm_potentials.argtypes = [I, I, I, I, P, P, P, I, P, D, P, P]
     L.pdg_qcmm_gradients.argtypes = [I, I, I, I, P, P, P, P, I, P, D, P, P, P]
     for name in EXPORTS:

@@ -371,3 +371,57 @@ extern "C" int pdg_scf_occupancy(const pdg_system *s, int *threads, int *smem_by
     if (scf_occupancy(s->d, threads, smem_bytes, ctas_per_sm)) return cuda_check(cudaGetLastError(), "occupancy query");
     return PDG_OK;
 }
+
+// ---------------------------------------------------------------------------------------------------
+// Learned start density (guess.cu)
+extern "C" int pdg_guess_features(pdg_system *s, int n_frames, const double *d_xyz, const double *d_phi, float *d_env, int *d_count,
+                                  int *d_offsets, float *d_x, int *d_row_frame, int *d_row_pair, void *stream)
+{
+    if (!s || n_frames <= 0 || !d_xyz || !d_env || !d_count || !d_offsets || !d_x || !d_row_frame || !d_row_pair)
+        return fail(PDG_BAD_ARGUMENT, "pdg_guess_features: bad argument");
+    launch_guess_features(s->d, n_frames, d_xyz, d_phi, d_env, d_count, d_offsets, d_x, d_row_frame, d_row_pair, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "guess feature kernels");
+}
+
+extern "C" int pdg_mlp_forward(int max_rows, const int *d_rows, int k, int n, const float *d_x, const void *d_w, const float *d_b,
+                               float *d_z, float *d_h, int act, void *stream)
+{
+    if (max_rows <= 0 || !d_rows || k <= 0 || n <= 0 || !d_x || !d_w || !d_b || !d_h) return fail(PDG_BAD_ARGUMENT, "pdg_mlp_forward: bad argument");
+    launch_mlp_forward(max_rows, d_rows, k, n, d_x, d_w, d_b, d_z, d_h, act, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "mlp forward kernel");
+}
+
+extern "C" int pdg_mlp_backward(int max_rows, const int *d_rows, int n, int k, const float *d_dz, const void *d_w, const float *d_zin,
+                                const float *d_hin, float *d_dzin, int segments, float *d_part, void *stream)
+{
+    if (max_rows <= 0 || !d_rows || !d_dz || !d_w || !d_hin || !d_part || segments < 1 || (d_dzin && !d_zin))
+        return fail(PDG_BAD_ARGUMENT, "pdg_mlp_backward: bad argument");
+    launch_mlp_backward(max_rows, d_rows, n, k, d_dz, d_w, d_zin, d_hin, d_dzin, segments, d_part, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "mlp backward kernels");
+}
+
+extern "C" int pdg_mlp_adam(int n, int k, int segments, const float *d_part, float scale, float *d_wm, float *d_bm, float *d_m1, float *d_m2,
+                            void *d_w, float lr, float beta1, float beta2, int step, void *stream)
+{
+    if (!d_part || !d_wm || !d_bm || !d_m1 || !d_m2 || !d_w || step < 1) return fail(PDG_BAD_ARGUMENT, "pdg_mlp_adam: bad argument");
+    const float c1 = 1.0f / (1.0f - powf(beta1, (float)step)), c2 = 1.0f / (1.0f - powf(beta2, (float)step));
+    launch_mlp_adam(n, k, segments, d_part, scale, d_wm, d_bm, d_m1, d_m2, d_w, lr, beta1, beta2, c1, c2, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "mlp adam kernel");
+}
+
+extern "C" int pdg_guess_assemble(pdg_system *s, int n_frames, const double *d_xyz, const int *d_offsets, const int *d_row_pair,
+                                  const float *d_y, double *d_density, void *stream)
+{
+    if (!s || n_frames <= 0 || !d_xyz || !d_offsets || !d_row_pair || !d_y || !d_density) return fail(PDG_BAD_ARGUMENT, "pdg_guess_assemble: bad argument");
+    launch_guess_assemble(s->d, n_frames, d_xyz, d_offsets, d_row_pair, d_y, d_density, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "guess assembly kernel");
+}
+
+extern "C" int pdg_guess_loss(pdg_system *s, int n_frames, const double *d_xyz, const int *d_offsets, const int *d_row_pair,
+                              const double *d_density, const double *d_target, float *d_dy, double *d_loss, void *stream)
+{
+    if (!s || n_frames <= 0 || !d_xyz || !d_offsets || !d_row_pair || !d_density || !d_target || !d_dy || !d_loss)
+        return fail(PDG_BAD_ARGUMENT, "pdg_guess_loss: bad argument");
+    launch_guess_loss(s->d, n_frames, d_xyz, d_offsets, d_row_pair, d_density, d_target, d_dy, d_loss, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "guess loss kernel");
+}

@@ -134,3 +134,15 @@ int launch_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const dou
                           double *gqc, double *gmm, cudaStream_t st);
 int launch_tc_selftest(int n, int kprod, const float *x, float *c, int *status, cudaStream_t st);
 int scf_occupancy(const DeviceSystem &s, int *threads, int *smem_bytes, int *ctas_per_sm);
+void launch_guess_features(const DeviceSystem &s, int n_frames, const double *xyz, const double *phi, float *env, int *count,
+                           int *offsets, float *X, int *row_frame, int *row_pair, cudaStream_t st);
+void launch_mlp_forward(int max_rows, const int *rows, int K, int N, const float *X, const void *W, const float *b, float *Z, float *H,
+                        int act, cudaStream_t st);
+void launch_mlp_backward(int max_rows, const int *rows, int N, int K, const float *dZ, const void *W, const float *Zin, const float *Hin,
+                         float *dZin, int segments, float *part, cudaStream_t st);
+void launch_mlp_adam(int N, int K, int segments, const float *part, float scale, float *Wm, float *bm, float *m1, float *m2, void *W,
+                     float lr, float b1, float b2, float c1, float c2, cudaStream_t st);
+void launch_guess_assemble(const DeviceSystem &s, int n_frames, const double *xyz, const int *offsets, const int *row_pair,
+                           const float *Y, double *P, cudaStream_t st);
+void launch_guess_loss(const DeviceSystem &s, int n_frames, const double *xyz, const int *offsets, const int *row_pair, const double *P,
+                       const double *Ptarget, float *dY, double *loss, cudaStream_t st);

@@ -47,6 +47,7 @@ class System:
         self.qcSelection = None
         self.configuration = Configuration()
         self._engine = None
+        self.densityGuess = None
 
     # -- model definition (System.py:182-230)
     def DefineQCModel(self, qcModel, qcSelection=None):
@@ -66,6 +67,10 @@ class System:
         if mm and self.mmCharges is None:
             raise ValueError("MM atoms need point charges.")
         self.nbModel = nbModel
+
+    def DefineDensityGuess(self, guess):
+        """Start cold SCFs from a LearnedDensityGuess (None: the diagonal guess).  Not in the reference."""
+        self.densityGuess = guess
 
     def mm_indices(self):
         qc = set(self.qcSelection or [])
@@ -125,7 +130,7 @@ class System:
         eng = self.engine()
         qc, mm, q, mm_idx = self._device_inputs(frames)
         r = eng.run(qc, self.qcModel.converger, mm, q, self.nbModel if mm is not None else None, gradients=doGradients,
-                    warm_start=warmStart)
+                    warm_start=warmStart, guess=self.densityGuess)
         F = qc.shape[0]
         # one device -> host copy of the small per-frame results
         small = torch.cat([r["energies"], r["status"].to(torch.float64)[:, None], r["ncycles"].to(torch.float64)[:, None]], 1)
