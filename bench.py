@@ -170,8 +170,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--reference-sample", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--method", default="mixed", choices=["mixed", "fp64"],
-                    help="density step of the early SCF cycles: split-BF16 purification (mixed) or FP64 throughout")
+    ap.add_argument("--method", default="learned_mixed", choices=["learned_mixed", "mixed", "fp64"],
+                    help="learned start density + purification cycles (the metric's learned+mixed), purification cycles "
+                         "from the diagonal guess (mixed), or FP64 throughout")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -193,6 +194,29 @@ def main():
     from pdynamo_mirror_gb300 import DIISSCFConverger
     METHODS = {"fp64": dict(densityStep="fp64"),
                "mixed": dict(densityStep="purification", purificationProducts=6, purificationSwitch=1e-5)}
+    METHODS["learned_mixed"] = METHODS["mixed"]
+    guess_info = {}
+
+    def train_guess(s, eng):
+        """The learned start density, trained on frames the SCF converges here (a seed apart from the timed
+        frames); returns the model and what it achieved on held-out frames."""
+        from pdynamo_mirror_gb300 import LearnedDensityGuess
+        t0 = time.perf_counter()
+        from pdynamo_mirror_gb300 import workloads
+        tr = workloads.perturbed_frames(X, 2048, sigma=0.02, seed=101 + rank)
+        qc_t, mm_t, q_t, _ = s._device_inputs(tr)
+        phis, dens = [], []
+        for s0 in range(0, len(tr), 256):
+            r = eng.run(qc_t[s0:s0 + 256].contiguous(), s.qcModel.converger, mm_t[s0:s0 + 256].contiguous(), q_t, s.nbModel,
+                        gradients=False, warm_start=False)
+            phis.append(r["phi"].clone()); dens.append(eng.density.clone())
+        phi, P = torch.cat(phis), torch.cat(dens)
+        g = LearnedDensityGuess(eng, seed=0)
+        hist = g.fit(qc_t, phi, P, epochs=40, batch=32, lr=1e-3, seed=0)
+        hist += g.fit(qc_t, phi, P, epochs=20, batch=32, lr=2e-4, seed=1)
+        torch.cuda.synchronize()
+        return g, {"training_frames": len(tr), "epochs": 60, "train_seconds": time.perf_counter() - t0,
+                   "loss_first_last": [hist[0], hist[-1]]}
 
     def measure(method, timed_clocks):
         s = System(Z, X, mmCharges=Q)
@@ -202,9 +226,19 @@ def main():
         eng = s.engine()
         qc, mm, q, mm_idx = s._device_inputs(frames)
         conv, nb = s.qcModel.converger, s.nbModel
+        guess = None
+        if method == "learned_mixed":
+            guess, info = train_guess(s, eng)
+            s.DefineDensityGuess(guess)
+            # held-out validation (frames of their own seed): the guess stays on only if it saves SCF cycles
+            from pdynamo_mirror_gb300 import workloads
+            qc_v, mm_v, q_v, _ = s._device_inputs(workloads.perturbed_frames(X, 256, sigma=0.02, seed=201 + rank))
+            info.update(guess.validate(qc_v, conv, mm_v, q_v, nb))
+            info["used_in_timed_steps"] = guess.enabled
+            guess_info.update(info)
 
         def step():
-            return eng.run(qc, conv, mm, q, nb, gradients=True, warm_start=False)
+            return eng.run(qc, conv, mm, q, nb, gradients=True, warm_start=False, guess=guess)
 
         for _ in range(args.warmup):
             r = step()
@@ -258,7 +292,8 @@ def main():
                     ncyc=r["ncycles"].cpu().numpy(), timers=timers, eng=eng, conv=conv, frames_h=frames_h)
 
     plain = measure("fp64", args.method == "fp64")
-    head = plain if args.method == "fp64" else measure(args.method, True)
+    mixed = None if args.method == "fp64" else (measure("mixed", args.method == "mixed"))
+    head = plain if args.method == "fp64" else (mixed if args.method == "mixed" else measure(args.method, True))
     eng, conv = head["eng"], head["conv"]
     n_total = len(frames) * world
     value = n_total / (head["ms"] * 1e-3)
@@ -283,8 +318,10 @@ def main():
             "data": "synthetic (seeded water box, perturbed frames)",
             "config": {"workload": "qcmm_water_box_am1_abfs", "qc_atoms": len(sel), "mm_atoms": len(Z) - len(sel),
                        "basis_functions": N, "frames_per_step": len(frames),
-                       "method": "plain FP64" if args.method == "fp64" else
-                                 "mixed: split-BF16 SP2 purification on tcgen05 (6 partial products, FP32 accumulation) until the RMS density change < 1e-5, then FP64",
+                       "method": {"fp64": "plain FP64",
+                                  "mixed": "mixed: split-BF16 SP2 purification on tcgen05 (6 partial products, FP32 accumulation) until the RMS density change < 1e-5, then FP64",
+                                  "learned_mixed": "learned+mixed: per-pair MLP start density (kept only where held-out validation shows "
+                                                   "SCF cycles saved, else the diagonal guess), then the mixed SCF"}[args.method],
                        "density_tolerance": conv.densityTolerance, "mean_scf_cycles": ncyc_f,
                        "purification_steps_per_frame": pur_steps, "fp64_density_steps_per_frame": fp64_steps,
                        "scf_cta": scf_cta_layout(eng, T),
@@ -315,6 +352,10 @@ def main():
         dG = float(np.abs(head["G"] - plain["G"]).max()) / (KJ * 1.0e-10 / 5.291772083e-11)
         line["plain_fp64"] = {"value": n_total / (plain["ms"] * 1e-3), "ms_per_step": plain["ms"], "e2e": n_total / plain["e2e_s"],
                               "mean_scf_cycles": float(plain["ncyc"].mean())}
+        if args.method == "learned_mixed":
+            line["mixed"] = {"value": n_total / (mixed["ms"] * 1e-3), "ms_per_step": mixed["ms"], "e2e": n_total / mixed["e2e_s"],
+                             "mean_scf_cycles": float(mixed["ncyc"].mean())}
+            line["learned_guess"] = guess_info
         line["accuracy_vs_plain_fp64"] = {"max_abs_dE_hartree": dE, "max_abs_dF_hartree_per_bohr": dG,
                                           "gate": "|dE| < 1e-6 Eh, |dF| < 1e-5 Eh/Bohr", "pass": bool(dE < 1e-6 and dG < 1e-5)}
     if rank == 0 and not args.no_cpu_baseline:

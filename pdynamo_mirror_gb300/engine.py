@@ -71,7 +71,7 @@ class QCEngine:
     def run(self, qc_xyz, converger, mm_xyz=None, mm_charges=None, nbmodel=None, gradients=True, warm_start=True, guess=None):
         """qc_xyz [F, n, 3] and mm_xyz [F, m, 3] in Angstrom (device float64), mm_charges [m].  The SCF starts
         from the previous density (warm_start, same batch shape), else from guess.predict (a
-        LearnedDensityGuess), else from the diagonal guess.  Returns a dict of device tensors in Hartree /
+        LearnedDensityGuess, unless its validation disabled it), else from the diagonal guess.  Returns a dict of device tensors in Hartree /
         Hartree per Bohr."""
         F = qc_xyz.shape[0]
         n, N = self.n_atoms, self.n_basis
@@ -91,7 +91,7 @@ class QCEngine:
                                                      _native.ptr(phi), sh), "pdg_qcmm_potentials")
         xyz_bohr = (qc_xyz * ANGSTROMS_TO_BOHRS).contiguous()
         use = 1 if (warm_start and self.density is not None and self.density.shape[0] == F) else 0
-        if not use and guess is not None:
+        if not use and guess is not None and guess.enabled:
             self.density = guess.predict(qc_xyz, phi)
             use = 1
         if not use:

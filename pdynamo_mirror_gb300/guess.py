@@ -35,6 +35,8 @@ class LearnedDensityGuess:
                                 "m2": torch.zeros(n * (k + 1), dtype=torch.float32, device=dev)})
         self.step = 0
         self._buf = {}
+        self.enabled = True       # False after validate() found no cycles saved: the SCF falls back to the diagonal guess
+        self.validation = None
 
     # -- buffers
     def _buffers(self, F):
@@ -128,6 +130,31 @@ class LearnedDensityGuess:
                 tot += float(loss.sum())
             hist.append(tot / F)
         return hist
+
+    def validate(self, qc_xyz, converger, mm_xyz=None, mm_charges=None, nbmodel=None):
+        """Held-out check with the converged SCF as the judge: run the frames [F, n, 3] cold from the diagonal
+        guess and from this guess, compare the mean SCF cycles and the energies, and keep the guess enabled
+        only if it saved cycles (else the standard guess is the fallback).  Returns the figures as a dict."""
+        eng = self.eng
+        self.enabled = True
+        std = eng.run(qc_xyz, converger, mm_xyz, mm_charges, nbmodel, gradients=False, warm_start=False)
+        e_std, c_std = std["energies"].sum(1).clone(), float(std["ncycles"].double().mean())
+        P_std, phi = eng.density.clone(), std["phi"]
+        N = eng.n_basis
+        P_g = self.predict(qc_xyz, phi)
+        diag = torch.zeros_like(P_g)
+        diag.diagonal(dim1=1, dim2=2).fill_(2.0 * eng.n_occupied / N)
+        err = lambda A: float(((A - P_std) ** 2).sum(dim=(1, 2)).sqrt().mean()) / N
+        lrn = eng.run(qc_xyz, converger, mm_xyz, mm_charges, nbmodel, gradients=False, warm_start=False, guess=self)
+        c_lrn = float(lrn["ncycles"].double().mean())
+        ok = bool((std["status"] == 0).all()) and bool((lrn["status"] == 0).all())
+        self.enabled = ok and c_lrn < c_std
+        self.validation = {"frames": int(qc_xyz.shape[0]), "rms_error_learned": err(P_g), "rms_error_diagonal": err(diag),
+                           "mean_scf_cycles_diagonal_guess": c_std, "mean_scf_cycles_learned_guess": c_lrn,
+                           "iterations_saved": c_std - c_lrn,
+                           "max_abs_dE_hartree": float((lrn["energies"].sum(1) - e_std).abs().max()),
+                           "enabled": self.enabled}
+        return self.validation
 
     def state_dict(self):
         return {"w%d" % i: p["wm"].cpu().numpy() for i, p in enumerate(self.params)} | \

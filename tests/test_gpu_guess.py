@@ -80,3 +80,11 @@ def test_learned_guess_is_closer_than_the_diagonal_guess_and_keeps_the_energies(
     assert (learned["status"].cpu().numpy() == 0).all()
     e0, e1 = base["energies"][:, 0].cpu().numpy(), learned["energies"][:, 0].cpu().numpy()
     assert np.abs(e1 - e0).max() < 1e-8
+    # held-out validation: the guess stays on only where it saves cycles; when off, the diagonal guess runs
+    v = g.validate(qt, conv, mt, q, nb)
+    assert v["enabled"] == (v["mean_scf_cycles_learned_guess"] < v["mean_scf_cycles_diagonal_guess"])
+    assert v["max_abs_dE_hartree"] < 1e-8
+    g.enabled = False
+    off = eng.run(qt, conv, mt, q, nb, gradients=False, warm_start=False, guess=g)
+    assert (off["ncycles"] == base["ncycles"]).all()
+    assert np.abs(off["energies"][:, 0].cpu().numpy() - e0).max() < 1e-12
