@@ -250,6 +250,40 @@ int pdg_tc_selftest(int n, int kprod, const float *d_x, float *d_c, int *d_statu
  * SM id and start/end times each CTA records in pdg_scf_timings show what the hardware actually ran). */
 int pdg_scf_occupancy(const pdg_system *sys, int *threads, int *smem_bytes, int *ctas_per_sm);
 
+/* ---- Heterogeneous batches: independent molecules of different sizes, computed together ----
+ * A batch is a list of items, each a system with one geometry (the same system may appear for several
+ * items).  Per-item data are concatenated in item order: d_xyz, d_gradients (3 per atom, Bohr and
+ * Hartree/Bohr), d_phi and d_charges (1 per atom), d_density (N_k^2 per item), d_energies
+ * (PDG_NENERGY per item), d_status and d_ncycles (1 per item).  pdg_batch_energy_gradients queues one
+ * launch per kernel over the whole batch: integrals, a persistent SCF kernel whose CTAs take items from a
+ * queue (largest first), gradients.  The reference evaluates one molecule per QCModel.Energy call
+ * (pMolecule.QCModel.pyx:146-185); its batched counterpart is a Python loop over systems. */
+typedef struct pdg_batch pdg_batch;
+typedef struct pdg_graph pdg_graph;
+
+int pdg_batch_create(pdg_system *const *systems, int n_items, pdg_batch **out);
+int pdg_batch_destroy(pdg_batch *batch);
+/* n_items, total atoms, total density doubles, and the SCF launch the schedule gives: persistent CTAs, dynamic
+ * shared memory per CTA, items that can use the tensor-core purification step (N <= 144, matrix in shared memory). */
+int pdg_batch_info(const pdg_batch *batch, int *n_items, int *n_atoms, long long *density_doubles, int *grid, int *smem_bytes,
+                   int *tensor_items);
+size_t pdg_batch_workspace_bytes(const pdg_batch *batch);
+/* Schedule of the persistent SCF kernel (the autotuner's knobs): ctas_per_sm 1 (each CTA may keep matrices
+ * up to 220 KB in shared memory) or 2 (112 KB each); order 0 = largest item first, 1 = item order. */
+int pdg_batch_schedule(pdg_batch *batch, int ctas_per_sm, int order);
+int pdg_batch_energy_gradients(pdg_batch *batch, const double *d_xyz, const double *d_phi, const pdg_scf_options *options,
+                               double *d_density, int use_density, double *d_energies, double *d_gradients,
+                               double *d_charges, int *d_status, int *d_ncycles, void *d_workspace, size_t workspace_bytes,
+                               void *stream);
+/* The same work captured once into a CUDA graph on the given buffers (a queue reset and five kernel launches);
+ * pdg_graph_launch replays it on a stream.  The buffers must outlive the graph.  No reference counterpart. */
+int pdg_batch_graph_create(pdg_batch *batch, const double *d_xyz, const double *d_phi, const pdg_scf_options *options,
+                           double *d_density, int use_density, double *d_energies, double *d_gradients,
+                           double *d_charges, int *d_status, int *d_ncycles, void *d_workspace, size_t workspace_bytes,
+                           pdg_graph **out);
+int pdg_graph_launch(pdg_graph *graph, void *stream);
+int pdg_graph_destroy(pdg_graph *graph);
+
 /* Text of the last error on this host thread (never NULL). */
 const char *pdg_last_error(void);
 

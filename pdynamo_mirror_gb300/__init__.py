@@ -6,10 +6,11 @@ and, beyond the reference, LearnedDensityGuess (System.DefineDensityGuess).
 The compute path is libpdg.so (CUDA, include/pdg.h); nothing here computes on the CPU.
 """
 
+from .batch import MoleculeBatch
 from .converger import DIISSCFConverger
 from .guess import LearnedDensityGuess
 from .nbmodel import NBModelABFS, NBModelFull
 from .qcmodel import QCModelMNDO
 from .system import ElectronicState, SCFNotConverged, System
 
-__all__ = ["DIISSCFConverger", "ElectronicState", "LearnedDensityGuess", "NBModelABFS", "NBModelFull", "QCModelMNDO", "SCFNotConverged", "System"]
+__all__ = ["DIISSCFConverger", "MoleculeBatch", "ElectronicState", "LearnedDensityGuess", "NBModelABFS", "NBModelFull", "QCModelMNDO", "SCFNotConverged", "System"]

@@ -1,5 +1,7 @@
 // api.cu - the extern "C" boundary of libpdg.so (declared in include/pdg.h).
 #include <cstdio>
+#include <algorithm>
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -369,6 +371,206 @@ extern "C" int pdg_scf_occupancy(const pdg_system *s, int *threads, int *smem_by
 {
     if (!s || !threads || !smem_bytes || !ctas_per_sm) return fail(PDG_BAD_ARGUMENT, "null argument");
     if (scf_occupancy(s->d, threads, smem_bytes, ctas_per_sm)) return cuda_check(cudaGetLastError(), "occupancy query");
+    return PDG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Heterogeneous batches: independent molecules of different sizes in one launch per kernel.
+struct pdg_batch {
+    std::vector<BatchItem> items;   // host copy of the device table
+    BatchItem *d_items = nullptr;
+    int *d_order = nullptr, *d_queue = nullptr;
+    Batch b = {};
+    size_t ws_doubles = 0, dens_doubles = 0;
+    int n_atoms = 0, sms = 0;
+    // schedule (pdg_batch_schedule)
+    int ctas_per_sm = PDG_SCF_CTAS_PER_SM, order_mode = 0, grid = 0, smem_limit = 0, tensor_items = 0;
+    size_t smem_bytes = 0;
+};
+
+static int batch_schedule(pdg_batch *bt, int ctas_per_sm, int order_mode)
+{
+    const int n = bt->b.n;
+    bt->ctas_per_sm = ctas_per_sm;
+    bt->order_mode = order_mode;
+    bt->smem_limit = ctas_per_sm == 1 ? PDG_SMEM_LIMIT_1 : PDG_SMEM_LIMIT_2;
+    bt->grid = std::max(1, std::min(n, bt->sms * ctas_per_sm));
+    bt->smem_bytes = 0;
+    bt->tensor_items = 0;
+    for (const BatchItem &it : bt->items) {
+        const size_t by = scf_smem_bytes_limit(it.s.n_basis, it.s.n_vec, bt->smem_limit);
+        bt->smem_bytes = std::max(bt->smem_bytes, by);
+        // the purification step needs N <= 144 and the packed matrix in shared memory (the plan's amat)
+        const size_t small = scf_smem_bytes_limit(it.s.n_basis, it.s.n_vec, 0);
+        if (it.s.n_basis <= 144 && by > small) bt->tensor_items++;
+    }
+    std::vector<int> order(n);
+    for (int k = 0; k < n; k++) order[k] = k;
+    if (order_mode == 0)   // largest first (N^3 work), so that the last CTAs to finish hold the smallest items
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return bt->items[x].s.n_basis > bt->items[y].s.n_basis; });
+    int rc;
+    if ((rc = cuda_check(cudaMemcpy(bt->d_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice), "copy batch order"))) return rc;
+    if (configure_batch_scf(bt->smem_bytes)) return cuda_check(cudaGetLastError(), "batch SCF launch attributes");
+    return PDG_OK;
+}
+
+extern "C" int pdg_batch_create(pdg_system *const *systems, int n_items, pdg_batch **out)
+{
+    if (!out || !systems) return fail(PDG_BAD_ARGUMENT, "null argument");
+    *out = nullptr;
+    if (n_items <= 0) return fail(PDG_BAD_ARGUMENT, "n_items must be positive");
+    pdg_batch *bt = new pdg_batch();
+    long long ws = 0, dens = 0, atom = 0, work[3] = { 0, 0, 0 };
+    for (int k = 0; k < n_items; k++) {
+        if (!systems[k]) { delete bt; return fail(PDG_BAD_ARGUMENT, "null system in batch"); }
+        BatchItem it = {};
+        it.s = systems[k]->d;
+        it.plan = plan_for(systems[k], PDG_MAX_HISTORY);
+        it.ws = ws; it.dens = dens; it.atom = (int)atom;
+        for (int c = 0; c < 3; c++) it.work[c] = (int)work[c];
+        ws += (long long)it.plan.stride;
+        dens += (long long)it.s.n_basis * it.s.n_basis;
+        atom += it.s.n_atoms;
+        for (int c = 0; c < 3; c++) work[c] += work_units(it.s, c);
+        bt->items.push_back(it);
+    }
+    if (work[0] > INT32_MAX || work[1] > INT32_MAX || work[2] > INT32_MAX || atom > INT32_MAX) {
+        delete bt;
+        return fail(PDG_TOO_LARGE, "batch work exceeds 2^31 units");
+    }
+    bt->b.n = n_items;
+    for (int c = 0; c < 3; c++) bt->b.total[c] = (int)work[c];
+    bt->ws_doubles = (size_t)ws; bt->dens_doubles = (size_t)dens; bt->n_atoms = (int)atom;
+    int dev = 0, rc;
+    if ((rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice")) ||
+        (rc = cuda_check(cudaDeviceGetAttribute(&bt->sms, cudaDevAttrMultiProcessorCount, dev), "SM count")) ||
+        (rc = cuda_check(cudaMalloc(&bt->d_items, sizeof(BatchItem) * n_items), "cudaMalloc batch table")) ||
+        (rc = cuda_check(cudaMalloc(&bt->d_order, sizeof(int) * n_items), "cudaMalloc batch order")) ||
+        (rc = cuda_check(cudaMalloc(&bt->d_queue, sizeof(int)), "cudaMalloc batch queue")) ||
+        (rc = cuda_check(cudaMemcpy(bt->d_items, bt->items.data(), sizeof(BatchItem) * n_items, cudaMemcpyHostToDevice), "copy batch table"))) {
+        pdg_batch_destroy(bt);
+        return rc;
+    }
+    bt->b.items = bt->d_items;
+    if ((rc = batch_schedule(bt, PDG_SCF_CTAS_PER_SM, 0))) { pdg_batch_destroy(bt); return rc; }
+    *out = bt;
+    return PDG_OK;
+}
+
+extern "C" int pdg_batch_destroy(pdg_batch *bt)
+{
+    if (!bt) return PDG_OK;
+    cudaFree(bt->d_items); cudaFree(bt->d_order); cudaFree(bt->d_queue);
+    delete bt;
+    return PDG_OK;
+}
+
+extern "C" int pdg_batch_info(const pdg_batch *bt, int *n_items, int *n_atoms, long long *density_doubles, int *grid, int *smem_bytes,
+                              int *tensor_items)
+{
+    if (!bt) return fail(PDG_BAD_ARGUMENT, "null batch");
+    if (n_items) *n_items = bt->b.n;
+    if (n_atoms) *n_atoms = bt->n_atoms;
+    if (density_doubles) *density_doubles = (long long)bt->dens_doubles;
+    if (grid) *grid = bt->grid;
+    if (smem_bytes) *smem_bytes = (int)bt->smem_bytes;
+    if (tensor_items) *tensor_items = bt->tensor_items;
+    return PDG_OK;
+}
+
+extern "C" size_t pdg_batch_workspace_bytes(const pdg_batch *bt) { return bt ? sizeof(double) * bt->ws_doubles : 0; }
+
+extern "C" int pdg_batch_schedule(pdg_batch *bt, int ctas_per_sm, int order)
+{
+    if (!bt) return fail(PDG_BAD_ARGUMENT, "null batch");
+    if (ctas_per_sm != 1 && ctas_per_sm != 2) return fail(PDG_BAD_ARGUMENT, "ctas_per_sm must be 1 or 2");
+    if (order != 0 && order != 1) return fail(PDG_BAD_ARGUMENT, "order must be 0 (largest first) or 1 (item order)");
+    return batch_schedule(bt, ctas_per_sm, order);
+}
+
+static int batch_queue(pdg_batch *bt, const double *d_xyz, const double *d_phi, const pdg_scf_options *o, double *d_density,
+                       int use_density, double *d_energies, double *d_gradients, double *d_charges, int *d_status, int *d_ncycles,
+                       void *ws, cudaStream_t st)
+{
+    double *w = (double *)ws;
+    int rc;
+    launch_batch_integrals(bt->b, d_xyz, w, st);
+    if ((rc = cuda_check(cudaGetLastError(), "batch integral kernels"))) return rc;
+    if ((rc = cuda_check(cudaMemsetAsync(bt->d_queue, 0, sizeof(int), st), "reset batch queue"))) return rc;
+    launch_batch_scf(bt->b, bt->d_order, bt->d_queue, bt->grid, bt->smem_limit, bt->smem_bytes, bt->tensor_items, d_phi, *o, d_density,
+                     use_density, d_energies, d_charges, d_status, d_ncycles, w, st);
+    if ((rc = cuda_check(cudaGetLastError(), "batch scf kernel"))) return rc;
+    if (d_gradients) {
+        launch_batch_gradients(bt->b, d_xyz, d_density, w, d_gradients, st);
+        if ((rc = cuda_check(cudaGetLastError(), "batch gradient kernels"))) return rc;
+    }
+    return PDG_OK;
+}
+
+static int batch_check(const pdg_batch *bt, const double *d_xyz, const pdg_scf_options *o, const double *d_density,
+                       const double *d_energies, const int *d_status, const void *ws, size_t bytes)
+{
+    if (!bt) return fail(PDG_BAD_ARGUMENT, "null batch");
+    if (!o || !d_xyz || !d_density || !d_energies || !d_status) return fail(PDG_BAD_ARGUMENT, "null argument");
+    if (!ws || bytes < pdg_batch_workspace_bytes(bt)) return fail(PDG_BAD_ARGUMENT, "workspace missing or too small");
+    if (o->history < 1 || o->history > PDG_MAX_HISTORY) return fail(PDG_BAD_ARGUMENT, "history must be 1..16");
+    if (o->maximum_scf_cycles < 0) return fail(PDG_BAD_ARGUMENT, "maximum_scf_cycles must be >= 0");
+    if (o->density_step != 0 && o->density_step != 3 && o->density_step != 6) return fail(PDG_BAD_ARGUMENT, "density_step must be 0, 3 or 6");
+    return PDG_OK;
+}
+
+extern "C" int pdg_batch_energy_gradients(pdg_batch *bt, const double *d_xyz, const double *d_phi, const pdg_scf_options *o,
+                                          double *d_density, int use_density, double *d_energies, double *d_gradients,
+                                          double *d_charges, int *d_status, int *d_ncycles, void *ws, size_t bytes, void *stream)
+{
+    int rc = batch_check(bt, d_xyz, o, d_density, d_energies, d_status, ws, bytes);
+    if (rc) return rc;
+    return batch_queue(bt, d_xyz, d_phi, o, d_density, use_density, d_energies, d_gradients, d_charges, d_status, d_ncycles, ws,
+                       (cudaStream_t)stream);
+}
+
+struct pdg_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" int pdg_batch_graph_create(pdg_batch *bt, const double *d_xyz, const double *d_phi, const pdg_scf_options *o,
+                                      double *d_density, int use_density, double *d_energies, double *d_gradients,
+                                      double *d_charges, int *d_status, int *d_ncycles, void *ws, size_t bytes, pdg_graph **out)
+{
+    if (!out) return fail(PDG_BAD_ARGUMENT, "null argument");
+    *out = nullptr;
+    int rc = batch_check(bt, d_xyz, o, d_density, d_energies, d_status, ws, bytes);
+    if (rc) return rc;
+    cudaStream_t st = nullptr;
+    if ((rc = cuda_check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "capture stream"))) return rc;
+    pdg_graph *g = new pdg_graph();
+    rc = cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if (!rc) {
+        const int qr = batch_queue(bt, d_xyz, d_phi, o, d_density, use_density, d_energies, d_gradients, d_charges, d_status, d_ncycles,
+                                   ws, st);
+        const int er = cuda_check(cudaStreamEndCapture(st, &g->graph), "end capture");
+        rc = qr ? qr : er;
+    }
+    if (!rc) rc = cuda_check(cudaGraphInstantiate(&g->exec, g->graph, 0), "instantiate graph");
+    cudaStreamDestroy(st);
+    if (rc) { pdg_graph_destroy(g); return rc; }
+    *out = g;
+    return PDG_OK;
+}
+
+extern "C" int pdg_graph_launch(pdg_graph *g, void *stream)
+{
+    if (!g || !g->exec) return fail(PDG_BAD_ARGUMENT, "null graph");
+    return cuda_check(cudaGraphLaunch(g->exec, (cudaStream_t)stream), "graph launch");
+}
+
+extern "C" int pdg_graph_destroy(pdg_graph *g)
+{
+    if (!g) return PDG_OK;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
     return PDG_OK;
 }
 

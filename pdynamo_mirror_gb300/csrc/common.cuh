@@ -72,6 +72,70 @@ __host__ inline FramePlan make_plan(const DeviceSystem &s, int history)
     return p;
 }
 
+// Heterogeneous batches: independent molecules of different sizes (each its own system, one geometry each)
+// computed by the same launches.  Per-item data are concatenated in item order: coordinates, gradients,
+// charges and potentials by atom, densities by N_k^2, workspaces by the item's plan stride.
+enum { PDG_WORK_GEN = 0, PDG_WORK_SS = 1, PDG_WORK_ATOM = 2 };
+
+struct BatchItem {
+    DeviceSystem s;
+    FramePlan plan;
+    long long ws, dens;   // first workspace double, first density double
+    int atom;             // first atom
+    int work[3];          // first global work unit: pair batches of 32 general pairs, s-s pairs, atoms
+};
+
+struct Batch {
+    const BatchItem *items;   // device table (null: homogeneous frames of one system)
+    int n;
+    int total[3];             // work units of each kind over all items
+};
+
+// What a kernel thread (or warp) works on: the system, plan and data offsets of one frame or batch item
+// (s and plan are filled for batch items only; homogeneous frames use the kernel's own arguments).
+struct FrameView {
+    DeviceSystem s;
+    FramePlan plan;
+    size_t ws, dens, atom;
+    int f;   // frame (homogeneous) or item (batch): index of its energies, status and cycle count
+};
+
+__host__ __device__ inline int work_units(const DeviceSystem &s, int kind)
+{
+    return kind == PDG_WORK_GEN ? (s.n_gen + 31) / 32 : kind == PDG_WORK_SS ? s.n_ss : s.n_atoms;
+}
+
+// Global work unit g of the given kind -> its frame or item and the unit's index within it; false past the end.
+// Batch items are found by binary search on their first units (the last item starting at or before g owns it;
+// items with no units of this kind share their start with the next item and are skipped that way).
+template <bool BATCH, int KIND>
+__device__ __forceinline__ bool locate(const DeviceSystem &s0, const FramePlan &p0, int n_frames, const Batch &b, long g,
+                                       FrameView &v, int &local)
+{
+    if (!BATCH) {
+        const int per = work_units(s0, KIND);
+        if (per == 0 || g >= (long)n_frames * per) return false;
+        v.f = (int)(g / per);
+        local = (int)(g % per);
+        v.ws = (size_t)v.f * p0.stride;
+        v.dens = (size_t)v.f * s0.n_basis * s0.n_basis;
+        v.atom = (size_t)v.f * s0.n_atoms;
+        return true;
+    }
+    if (g >= b.total[KIND]) return false;
+    int lo = 0, hi = b.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (b.items[mid].work[KIND] <= g) lo = mid; else hi = mid - 1;
+    }
+    const BatchItem &it = b.items[lo];
+    v.f = lo;
+    local = (int)(g - it.work[KIND]);
+    v.s = it.s; v.plan = it.plan;
+    v.ws = (size_t)it.ws; v.dens = (size_t)it.dens; v.atom = (size_t)it.atom;
+    return true;
+}
+
 __device__ __forceinline__ const double *elem(const DeviceSystem &s, int e) { return s.elements + e * PDG_ELEMENT_STRIDE; }
 __device__ __forceinline__ int pk(int i, int j) { return i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i; }
 
@@ -127,6 +191,16 @@ void launch_pair_gradients(const DeviceSystem &s, const FramePlan &p, int n_fram
                            const double *density, double *ws, cudaStream_t st);
 void launch_reduce_gradients(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *ws,
                              double *gradients, cudaStream_t st);
+// Heterogeneous batches (the same kernels over a BatchItem table).
+void launch_batch_integrals(const Batch &b, const double *xyz, double *ws, cudaStream_t st);
+void launch_batch_gradients(const Batch &b, const double *xyz, const double *density, double *ws, double *gradients, cudaStream_t st);
+void launch_batch_scf(const Batch &b, const int *order, int *queue, int grid, int smem_limit, size_t smem_bytes, int tensor_items,
+                      const double *phi, const pdg_scf_options &o, double *density, int use_density, double *energies,
+                      double *charges, int *status, int *ncycles, double *ws, cudaStream_t st);
+size_t scf_smem_bytes_limit(int N, int kv, int limit_bytes);
+int configure_batch_scf(size_t smem_bytes);
+#define PDG_SMEM_LIMIT_1 (220 * 1024)   // shared-memory budget of one SCF CTA alone on its SM
+#define PDG_SMEM_LIMIT_2 (112 * 1024)   // ... of each of two
 int launch_qcmm_potentials(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,
                            const double *q, int n_knots, const double *knots, double cutoff, double *phi, cudaStream_t st);
 int launch_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,

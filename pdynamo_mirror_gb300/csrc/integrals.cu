@@ -78,35 +78,29 @@ __device__ double core_core(const double *a, const double *b, double r, double *
 #define PI_WARPS 8
 #define PI_SM 640
 
-// Pair batches: a warp takes entries b0 .. b0 + nb - 1 (nb <= 32) of frame f's list of pairs that are not s-s.
-__device__ __forceinline__ bool pair_batch(const DeviceSystem &s, int n_frames, int warps_per_block, int &f, int &b0, int &nb)
-{
-    const int nbatch = (s.n_gen + 31) / 32;
-    const long gw = (long)blockIdx.x * warps_per_block + (threadIdx.x >> 5);
-    if (gw >= (long)n_frames * nbatch) return false;
-    f = (int)(gw / nbatch);
-    b0 = (int)(gw % nbatch) * 32;
-    nb = min(32, s.n_gen - b0);
-    return true;
-}
-
 __device__ __forceinline__ int overlap_used(int noi, int noj)
 {
     return 1 | (noi > 1 ? 2 : 0) | (noj > 1 ? 4 : 0) | (noi > 1 && noj > 1 ? 8 : 0);
 }
 
+// A warp takes a batch of up to 32 entries of its frame's (or batch item's) list of pairs that are not s-s.
+template <bool BATCH>
 __global__ void __launch_bounds__(PI_WARPS * 32)
-k_pair_integrals(DeviceSystem s, FramePlan plan, int n_frames, const double *__restrict__ xyz,
-                 const double *__restrict__ terms, double *__restrict__ ws)
+k_pair_integrals(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, const double *__restrict__ xyz, double *__restrict__ ws)
 {
     __shared__ double smem[PI_WARPS][PI_SM];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int f, b0, nb;
-    if (!pair_batch(s, n_frames, PI_WARPS, f, b0, nb)) return;
+    FrameView fv;
+    int ub;
+    if (!locate<BATCH, PDG_WORK_GEN>(sys0, plan0, n_frames, bt, (long)blockIdx.x * PI_WARPS + w, fv, ub)) return;
+    const DeviceSystem &s = BATCH ? fv.s : sys0;
+    const FramePlan &plan = BATCH ? fv.plan : plan0;
+    const double *terms = s.terms;
+    const int b0 = ub * 32, nb = min(32, s.n_gen - b0);
     double *W = smem[w];
     double *St = W, *L = W + 96, *ci = W + 196, *cj = W + 206, *X = W + 216, *C = W + 316;
-    const double *R = xyz + (size_t)f * 3 * s.n_atoms;
-    double *wsf = ws + (size_t)f * plan.stride;
+    const double *R = xyz + 3 * fv.atom;
+    double *wsf = ws + fv.ws;
     const int N = s.n_basis;
     double *H = wsf + plan.H;
     // one thread per pair: geometry, core-core energy, direction cosines
@@ -192,18 +186,23 @@ k_pair_integrals(DeviceSystem s, FramePlan plan, int n_frames, const double *__r
 // terms (the single multipole terms 0, MP_CORE_I and MP_CORE_J; no rotation), the resonance integral from
 // the ss radial sum, and the core-core energy.  Same results as the general kernel, without its warp-wide
 // machinery for a pair that has one integral.
-__global__ void __launch_bounds__(256) k_pair_integrals_ss(DeviceSystem s, FramePlan plan, int n_frames, const double *__restrict__ xyz,
-                                                          const double *__restrict__ terms, double *__restrict__ ws)
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_pair_integrals_ss(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt,
+                                                          const double *__restrict__ xyz, double *__restrict__ ws)
 {
-    const long g = (long)blockIdx.x * 256 + threadIdx.x;
-    if (g >= (long)n_frames * s.n_ss) return;
-    const int f = (int)(g / s.n_ss), p = s.pairs_ss[g % s.n_ss];
+    FrameView fv;
+    int u;
+    if (!locate<BATCH, PDG_WORK_SS>(sys0, plan0, n_frames, bt, (long)blockIdx.x * 256 + threadIdx.x, fv, u)) return;
+    const DeviceSystem &s = BATCH ? fv.s : sys0;
+    const FramePlan &plan = BATCH ? fv.plan : plan0;
+    const double *terms = s.terms;
+    const int p = s.pairs_ss[u];
     const int i = s.pair_i[p], j = s.pair_j[p], eli = s.atom_elem[i], elj = s.atom_elem[j];
     const double *Ei = elem(s, eli), *Ej = elem(s, elj);
-    const double *R = xyz + (size_t)f * 3 * s.n_atoms;
+    const double *R = xyz + 3 * fv.atom;
     const double x = R[3 * j] - R[3 * i], y = R[3 * j + 1] - R[3 * i + 1], z = R[3 * j + 2] - R[3 * i + 2];
     const double R2 = x * x + y * y + z * z, r = sqrt(R2);
-    double *wsf = ws + (size_t)f * plan.stride;
+    double *wsf = ws + fv.ws;
     const double *to = terms + (size_t)(eli * s.n_elements + elj) * 2 * MP_NTERMS, *ta = to + MP_NTERMS;
     const double s0 = rsqrt((r + to[0]) * (r + to[0]) + ta[0]);
     const double ci = rsqrt((r + to[MP_CORE_I]) * (r + to[MP_CORE_I]) + ta[MP_CORE_I]);
@@ -227,13 +226,16 @@ __global__ void __launch_bounds__(256) k_pair_integrals_ss(DeviceSystem s, Frame
     H[(size_t)js * N + is] = v;
 }
 
-__global__ void __launch_bounds__(256) k_assemble_h(DeviceSystem s, FramePlan plan, int n_frames, double *__restrict__ ws)
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_assemble_h(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, double *__restrict__ ws)
 {
     const int lane = threadIdx.x & 31;
-    long gw = (long)blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (gw >= (long)n_frames * s.n_atoms) return;
-    int f = (int)(gw / s.n_atoms), A = (int)(gw % s.n_atoms);
-    double *wsf = ws + (size_t)f * plan.stride;
+    FrameView fv;
+    int A;
+    if (!locate<BATCH, PDG_WORK_ATOM>(sys0, plan0, n_frames, bt, (long)blockIdx.x * 8 + (threadIdx.x >> 5), fv, A)) return;
+    const DeviceSystem &s = BATCH ? fv.s : sys0;
+    const FramePlan &plan = BATCH ? fv.plan : plan0;
+    double *wsf = ws + fv.ws;
     double acc[10];
     for (int k = 0; k < 10; k++) acc[k] = 0.0;
     for (int B = lane; B < s.n_atoms; B += 32) {
@@ -256,19 +258,32 @@ __global__ void __launch_bounds__(256) k_assemble_h(DeviceSystem s, FramePlan pl
 
 void launch_pair_integrals(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *xyz, double *ws, cudaStream_t st)
 {
+    const Batch none = {};
     long warps = (long)n_frames * ((s.n_gen + 31) / 32);
     if (warps > 0) {
         int blocks = (int)((warps + PI_WARPS - 1) / PI_WARPS);
-        k_pair_integrals<<<blocks, PI_WARPS * 32, 0, st>>>(s, p, n_frames, xyz, s.terms, ws);
+        k_pair_integrals<false><<<blocks, PI_WARPS * 32, 0, st>>>(s, p, n_frames, none, xyz, ws);
     }
     const long nss = (long)n_frames * s.n_ss;
-    if (nss > 0) k_pair_integrals_ss<<<(int)((nss + 255) / 256), 256, 0, st>>>(s, p, n_frames, xyz, s.terms, ws);
+    if (nss > 0) k_pair_integrals_ss<false><<<(int)((nss + 255) / 256), 256, 0, st>>>(s, p, n_frames, none, xyz, ws);
 }
 
 void launch_assemble_h(const DeviceSystem &s, const FramePlan &p, int n_frames, double *ws, cudaStream_t st)
 {
+    const Batch none = {};
     long warps = (long)n_frames * s.n_atoms;
-    k_assemble_h<<<(int)((warps + 7) / 8), 256, 0, st>>>(s, p, n_frames, ws);
+    k_assemble_h<false><<<(int)((warps + 7) / 8), 256, 0, st>>>(s, p, n_frames, none, ws);
+}
+
+void launch_batch_integrals(const Batch &b, const double *xyz, double *ws, cudaStream_t st)
+{
+    const DeviceSystem s0 = {};
+    const FramePlan p0 = {};
+    if (b.total[PDG_WORK_GEN] > 0)
+        k_pair_integrals<true><<<(b.total[PDG_WORK_GEN] + PI_WARPS - 1) / PI_WARPS, PI_WARPS * 32, 0, st>>>(s0, p0, 0, b, xyz, ws);
+    if (b.total[PDG_WORK_SS] > 0)
+        k_pair_integrals_ss<true><<<(b.total[PDG_WORK_SS] + 255) / 256, 256, 0, st>>>(s0, p0, 0, b, xyz, ws);
+    k_assemble_h<true><<<(b.total[PDG_WORK_ATOM] + 7) / 8, 256, 0, st>>>(s0, p0, 0, b, ws);
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -276,21 +291,27 @@ void launch_assemble_h(const DeviceSystem &s, const FramePlan &p, int n_frames, 
 #define PG_WARPS 4
 #define PG_SM 1408
 
+template <bool BATCH>
 __global__ void __launch_bounds__(PG_WARPS * 32)
-k_pair_gradients(DeviceSystem s, FramePlan plan, int n_frames, const double *__restrict__ xyz,
-                 const double *__restrict__ terms, const double *__restrict__ density, double *__restrict__ ws)
+k_pair_gradients(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, const double *__restrict__ xyz,
+                 const double *__restrict__ density, double *__restrict__ ws)
 {
     __shared__ double smem[PG_WARPS][PG_SM];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int f, b0, nb;
-    if (!pair_batch(s, n_frames, PG_WARPS, f, b0, nb)) return;
+    FrameView fv;
+    int ub;
+    if (!locate<BATCH, PDG_WORK_GEN>(sys0, plan0, n_frames, bt, (long)blockIdx.x * PG_WARPS + w, fv, ub)) return;
+    const DeviceSystem &s = BATCH ? fv.s : sys0;
+    const FramePlan &plan = BATCH ? fv.plan : plan0;
+    const double *terms = s.terms;
+    const int b0 = ub * 32, nb = min(32, s.n_gen - b0);
     double *W = smem[w];
     double *St = W, *dSt = W + 96, *L = W + 192, *dL = W + 292, *ci = W + 392, *cj = W + 402, *dci = W + 412, *dcj = W + 422;
     double *C = W + 432, *CD = W + 532, *G = W + 832, *W1 = W + 932, *W2 = W + 1032, *W3 = W + 1132;
     double *oneI = W + 1232, *oneJ = W + 1242, *Wres = W + 1252;
     const int N = s.n_basis;
-    const double *R = xyz + (size_t)f * 3 * s.n_atoms;
-    const double *P = density + (size_t)f * N * N;
+    const double *R = xyz + 3 * fv.atom;
+    const double *P = density + fv.dens;
     // one thread per pair: geometry, core-core derivative, direction cosines and their derivatives
     int mi = 0, mj = 0;
     double mx = 0.0, my = 0.0, mz = 0.0, mr = 1.0, mdc = 0.0;
@@ -413,7 +434,7 @@ k_pair_gradients(DeviceSystem s, FramePlan plan, int n_frames, const double *__r
                      overlap_used(noi, noj), Fo, Do);
         overlap_gradient(Wres, noi, noj, v3, Fo, Do, gr);
         if (lane == 0) {
-            double *pg = ws + (size_t)f * plan.stride + plan.pair_g + (size_t)p * 3;
+            double *pg = ws + fv.ws + plan.pair_g + (size_t)p * 3;
             pg[0] = eng[0] + gr[0]; pg[1] = eng[1] + gr[1]; pg[2] = eng[2] + gr[2];
         }
         __syncwarp();
@@ -422,20 +443,25 @@ k_pair_gradients(DeviceSystem s, FramePlan plan, int n_frames, const double *__r
 
 // s-s pairs, one thread per pair: the gradient terms of k_pair_gradients for a pair with one orbital on each
 // atom (no rotation, Gamma = P_ij^2 / 2 - P_ii P_jj), with the resonance term from the ss radial sums.
-__global__ void __launch_bounds__(256) k_pair_gradients_ss(DeviceSystem s, FramePlan plan, int n_frames, const double *__restrict__ xyz,
-                                                          const double *__restrict__ terms, const double *__restrict__ density,
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_pair_gradients_ss(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt,
+                                                          const double *__restrict__ xyz, const double *__restrict__ density,
                                                           double *__restrict__ ws)
 {
-    const long g = (long)blockIdx.x * 256 + threadIdx.x;
-    if (g >= (long)n_frames * s.n_ss) return;
-    const int f = (int)(g / s.n_ss), p = s.pairs_ss[g % s.n_ss];
+    FrameView fv;
+    int u;
+    if (!locate<BATCH, PDG_WORK_SS>(sys0, plan0, n_frames, bt, (long)blockIdx.x * 256 + threadIdx.x, fv, u)) return;
+    const DeviceSystem &s = BATCH ? fv.s : sys0;
+    const FramePlan &plan = BATCH ? fv.plan : plan0;
+    const double *terms = s.terms;
+    const int p = s.pairs_ss[u];
     const int i = s.pair_i[p], j = s.pair_j[p], eli = s.atom_elem[i], elj = s.atom_elem[j];
     const double *Ei = elem(s, eli), *Ej = elem(s, elj);
-    const double *R = xyz + (size_t)f * 3 * s.n_atoms;
+    const double *R = xyz + 3 * fv.atom;
     const double v3[3] = { R[3 * j] - R[3 * i], R[3 * j + 1] - R[3 * i + 1], R[3 * j + 2] - R[3 * i + 2] };
     const double R2 = v3[0] * v3[0] + v3[1] * v3[1] + v3[2] * v3[2], r = sqrt(R2);
     const int N = s.n_basis, is = s.atom_start[i], js = s.atom_start[j];
-    const double *P = density + (size_t)f * N * N;
+    const double *P = density + fv.dens;
     const double pii = P[(size_t)is * N + is], pjj = P[(size_t)js * N + js], pij = P[(size_t)is * N + js];
     double eng[3] = { 0.0, 0.0, 0.0 };
     if (r >= 5.0e-3) {
@@ -461,18 +487,20 @@ __global__ void __launch_bounds__(256) k_pair_gradients_ss(DeviceSystem s, Frame
         if (fac <= PRIMITIVE_OVERLAP_TOLERANCE) D = fma((abg + abg) * rec[OV_REC * t + 1], exp(-fac), D);
     }
     const double w = (Ei[PDG_E_BETA] + Ej[PDG_E_BETA]) * pij;
-    double *pg = ws + (size_t)f * plan.stride + plan.pair_g + (size_t)p * 3;
+    double *pg = ws + fv.ws + plan.pair_g + (size_t)p * 3;
     for (int x = 0; x < 3; x++) pg[x] = eng[x] + v3[x] * w * D;
 }
 
-__global__ void __launch_bounds__(256) k_reduce_gradients(DeviceSystem s, FramePlan plan, int n_frames,
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_reduce_gradients(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt,
                                                           const double *__restrict__ ws, double *__restrict__ grad)
 {
     const int lane = threadIdx.x & 31;
-    long gw = (long)blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (gw >= (long)n_frames * s.n_atoms) return;
-    int f = (int)(gw / s.n_atoms), A = (int)(gw % s.n_atoms);
-    const double *pg = ws + (size_t)f * plan.stride + plan.pair_g;
+    FrameView fv;
+    int A;
+    if (!locate<BATCH, PDG_WORK_ATOM>(sys0, plan0, n_frames, bt, (long)blockIdx.x * 8 + (threadIdx.x >> 5), fv, A)) return;
+    const DeviceSystem &s = BATCH ? fv.s : sys0;
+    const double *pg = ws + fv.ws + (BATCH ? fv.plan.pair_g : plan0.pair_g);
     double g[3] = { 0, 0, 0 };
     for (int B = lane; B < s.n_atoms; B += 32) {
         if (B == A) continue;
@@ -482,21 +510,34 @@ __global__ void __launch_bounds__(256) k_reduce_gradients(DeviceSystem s, FrameP
         for (int x = 0; x < 3; x++) g[x] += sg * pg[(size_t)p * 3 + x];
     }
     for (int x = 0; x < 3; x++) g[x] = warp_sum(g[x]);
-    if (lane < 3) grad[((size_t)f * s.n_atoms + A) * 3 + lane] = g[lane];
+    if (lane < 3) grad[(fv.atom + A) * 3 + lane] = g[lane];
 }
 
 void launch_pair_gradients(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *xyz,
                            const double *density, double *ws, cudaStream_t st)
 {
+    const Batch none = {};
     long warps = (long)n_frames * ((s.n_gen + 31) / 32);
     if (warps > 0)
-        k_pair_gradients<<<(int)((warps + PG_WARPS - 1) / PG_WARPS), PG_WARPS * 32, 0, st>>>(s, p, n_frames, xyz, s.terms, density, ws);
+        k_pair_gradients<false><<<(int)((warps + PG_WARPS - 1) / PG_WARPS), PG_WARPS * 32, 0, st>>>(s, p, n_frames, none, xyz, density, ws);
     const long nss = (long)n_frames * s.n_ss;
-    if (nss > 0) k_pair_gradients_ss<<<(int)((nss + 255) / 256), 256, 0, st>>>(s, p, n_frames, xyz, s.terms, density, ws);
+    if (nss > 0) k_pair_gradients_ss<false><<<(int)((nss + 255) / 256), 256, 0, st>>>(s, p, n_frames, none, xyz, density, ws);
 }
 
 void launch_reduce_gradients(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *ws, double *grad, cudaStream_t st)
 {
+    const Batch none = {};
     long warps = (long)n_frames * s.n_atoms;
-    k_reduce_gradients<<<(int)((warps + 7) / 8), 256, 0, st>>>(s, p, n_frames, ws, grad);
+    k_reduce_gradients<false><<<(int)((warps + 7) / 8), 256, 0, st>>>(s, p, n_frames, none, ws, grad);
+}
+
+void launch_batch_gradients(const Batch &b, const double *xyz, const double *density, double *ws, double *grad, cudaStream_t st)
+{
+    const DeviceSystem s0 = {};
+    const FramePlan p0 = {};
+    if (b.total[PDG_WORK_GEN] > 0)
+        k_pair_gradients<true><<<(b.total[PDG_WORK_GEN] + PG_WARPS - 1) / PG_WARPS, PG_WARPS * 32, 0, st>>>(s0, p0, 0, b, xyz, density, ws);
+    if (b.total[PDG_WORK_SS] > 0)
+        k_pair_gradients_ss<true><<<(b.total[PDG_WORK_SS] + 255) / 256, 256, 0, st>>>(s0, p0, 0, b, xyz, density, ws);
+    k_reduce_gradients<true><<<(b.total[PDG_WORK_ATOM] + 7) / 8, 256, 0, st>>>(s0, p0, 0, b, ws, grad);
 }

@@ -24,6 +24,7 @@ struct SCFArgs {
     double *density; int use_density;
     double *energies, *charges; int *status, *ncycles;
     double *ws; int fock_only; double *fock_out;
+    int smem_limit;   // bytes of shared memory one CTA may plan for (the launch provides the plan's bytes)
 };
 
 struct Smem {
@@ -59,13 +60,16 @@ __host__ __device__ inline size_t mix_doubles(int N)
 
 __host__ __device__ inline size_t round16(size_t x) { return (x + 15) & ~size_t(15); }
 
-__host__ __device__ inline SmemPlan smem_plan(int N, int kv)
+// Default shared-memory budget of one SCF CTA: all of an SM's shared memory, or half of it for two CTAs.
+#define PDG_SMEM_LIMIT (PDG_SCF_CTAS_PER_SM == 1 ? PDG_SMEM_LIMIT_1 : PDG_SMEM_LIMIT_2)
+
+__host__ __device__ inline SmemPlan smem_plan(int N, int kv, int limit_bytes)
 {
     SmemPlan p;
     p.head = round16(32 + 256 + 13 * (size_t)N + 64 + ((64 + (size_t)N + 2) * sizeof(int) + 7) / 8);
     p.work = round16((size_t)GK * GA_LD + (size_t)GK * GB_LD);
     p.ldz = N | 1;
-    const size_t limit = (PDG_SCF_CTAS_PER_SM == 1 ? 220 * 1024 : 112 * 1024) / 8, packed = (size_t)N * (N + 1) / 2;
+    const size_t limit = (size_t)limit_bytes / 8, packed = (size_t)N * (N + 1) / 2;
     const size_t zsz = (size_t)(kv > 0 ? kv : 1) * p.ldz, mix = mix_doubles(N);
     const size_t slot = round16(packed > mix ? packed : mix);
     p.amat = (p.head + p.work + slot <= limit) ? slot : 0;
@@ -74,10 +78,10 @@ __host__ __device__ inline SmemPlan smem_plan(int N, int kv)
     return p;
 }
 
-__device__ __forceinline__ Smem carve(double *base, int N, int kv)
+__device__ __forceinline__ Smem carve(double *base, int N, int kv, int limit_bytes)
 {
     Smem m;
-    SmemPlan sp = smem_plan(N, kv);
+    SmemPlan sp = smem_plan(N, kv, limit_bytes);
     m.red = base; m.small = base + 32;
     m.d = m.small + 256; m.e = m.d + N; m.e2 = m.e + N; m.tau = m.e2 + N; m.eig = m.tau + N;
     m.v = m.eig + N; m.v2 = m.v + N; m.p = m.v2 + N; m.w = m.p + N; m.part = m.w + N; m.dot = m.part + 4 * (size_t)N;
@@ -792,14 +796,15 @@ __device__ double density_step_mixed(const SCFArgs &a, double *wsf, const double
 }
 
 // ----------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf(SCFArgs a)
+// The SCF of frame f of a (the whole of a batch item's SCF with f = 0), on shm; tc is the CTA's tensor memory
+// and completion barrier when tc_ok (allocated by the kernel).
+__device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double *shm, TCState &tc, const bool tc_ok)
 {
-    extern __shared__ __align__(128) double shm[];
     const DeviceSystem &s = a.s;
     const FramePlan &pl = a.plan;
-    const int f = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5, N = s.n_basis;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, N = s.n_basis;
     const size_t NN = (size_t)N * N;
-    Smem sm = carve(shm, N, s.n_vec);
+    Smem sm = carve(shm, N, s.n_vec, a.smem_limit);
     double *wsf = a.ws + (size_t)f * pl.stride;
     double *H = wsf + pl.H, *F = wsf + pl.F, *P = a.density + (size_t)f * NN;
     const double *tei = wsf + pl.tei;
@@ -823,23 +828,7 @@ __global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf(SCFArgs 
     double base = 0.0;
     for (int A = tid; A < s.n_atoms; A += PDG_BLOCK) { const double *E = elem(s, s.atom_elem[A]); base += E[PDG_E_EHEAT] - E[PDG_E_EISOL]; }
     base = block_sum(base, sm.red);
-    // tensor memory and the completion barrier of the purification density step
-    __shared__ uint32_t tc_taddr_s;
-    __shared__ __align__(8) uint64_t tc_bar_s;
-    const bool want_mixed = a.fock_only != 1 && a.o.density_step != 0 && N <= 144 && sm.amat != nullptr;
-    TCState tc = { 0u, 0u, 0u };
-    // A CTA of a kernel that contains tcgen05 code holds the tensor-memory allocation permit until it allocates
-    // and relinquishes it (or exits), and no other such CTA is placed on its SM meanwhile: CTAs that will not
-    // allocate give it up at once, so that two frames share each SM in every mode.
-    if (!want_mixed && w == 0) asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    if (want_mixed) {
-        if (w == 0) tc_alloc(tc_smem_addr(&tc_taddr_s), 256);
-        if (tid == 0) mbar_init(tc_smem_addr(&tc_bar_s), 1);
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
-        tc.tmem = tc_taddr_s; tc.bar = tc_smem_addr(&tc_bar_s);
-    }
+    const bool want_mixed = tc_ok && a.fock_only != 1 && a.o.density_step != 0 && N <= 144 && sm.amat != nullptr;
     bool mixed = want_mixed, last_mixed = false;
     int n_mixed = 0;
     bool valid = a.use_density != 0;
@@ -853,11 +842,6 @@ __global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf(SCFArgs 
         for (size_t k = tid; k < NN; k += PDG_BLOCK) F[k] = a.fock_out[(size_t)f * NN + k];
         __syncthreads();
         const double r = want_mixed ? density_step_mixed(a, wsf, F, P, sm, tm, tc, a.o.density_step) : density_step(a, wsf, F, P, sm, tm);
-        if (want_mixed) {
-            tc_fence_before();
-            __syncthreads();
-            if (w == 0) tc_dealloc(tc.tmem, 256);
-        }
         if (tid == 0) {
             double *E = a.energies + (size_t)f * PDG_NENERGY;
             for (int k = 0; k < PDG_NENERGY; k++) E[k] = 0.0;
@@ -1089,11 +1073,6 @@ __global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf(SCFArgs 
         if (tid == 0 && ncyc <= PDG_RMS_HISTORY) tm.slot[PDG_T_RMS_HISTORY + ncyc - 1] = last_mixed ? -rms : rms;
         valid = true;
     }
-    if (want_mixed) {
-        tc_fence_before();
-        __syncthreads();
-        if (w == 0) tc_dealloc(tc.tmem, 256);
-    }
     if (converged) st = PDG_OK;
     if (tid == 0) {
         double *E = a.energies + (size_t)f * PDG_NENERGY;
@@ -1108,7 +1087,90 @@ __global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf(SCFArgs 
     }
 }
 
-size_t scf_smem_bytes(int N, int kv) { return smem_plan(N, kv).bytes; }
+// Tensor memory (256 columns) and the completion mbarrier of the purification density step, for CTAs that may
+// run it.  A CTA of a kernel that contains tcgen05 code holds the tensor-memory allocation permit until it
+// allocates and relinquishes it (or exits), and no other such CTA is placed on its SM meanwhile: CTAs that
+// will not allocate give it up at once, so that two CTAs share each SM in every mode.
+__device__ __forceinline__ void tc_setup(bool ok, TCState &tc, uint32_t *taddr_s, uint64_t *bar_s)
+{
+    const int w = threadIdx.x >> 5;
+    tc.tmem = 0u; tc.bar = 0u; tc.phase = 0u;
+    if (!ok) {
+        if (w == 0) asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        return;
+    }
+    if (w == 0) tc_alloc(tc_smem_addr(taddr_s), 256);
+    if (threadIdx.x == 0) mbar_init(tc_smem_addr(bar_s), 1);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    tc.tmem = *taddr_s; tc.bar = tc_smem_addr(bar_s);
+}
+
+__device__ __forceinline__ void tc_teardown(bool ok, const TCState &tc)
+{
+    if (!ok) return;
+    tc_fence_before();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) tc_dealloc(tc.tmem, 256);
+}
+
+// One CTA per frame of one system.
+__global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf(SCFArgs a)
+{
+    extern __shared__ __align__(128) double shm[];
+    __shared__ uint32_t tc_taddr_s;
+    __shared__ __align__(8) uint64_t tc_bar_s;
+    const int N = a.s.n_basis;
+    const bool tc_ok = a.fock_only != 1 && a.o.density_step != 0 && N <= 144 && smem_plan(N, a.s.n_vec, a.smem_limit).amat != 0;
+    TCState tc;
+    tc_setup(tc_ok, tc, &tc_taddr_s, &tc_bar_s);
+    scf_frame(a, blockIdx.x, shm, tc, tc_ok);
+    tc_teardown(tc_ok, tc);
+}
+
+// Persistent SCF over a heterogeneous batch: each CTA takes the next item of `order` (largest first) from the
+// queue counter until the batch is exhausted; the tensor memory is allocated once per CTA when any item may
+// use the purification step.  Items are independent; the only shared state is the counter (zero at launch).
+__global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM)
+k_scf_batch(SCFArgs a, Batch b, const int *__restrict__ order, int *__restrict__ queue, int tensor_items)
+{
+    extern __shared__ __align__(128) double shm[];
+    __shared__ uint32_t tc_taddr_s;
+    __shared__ __align__(8) uint64_t tc_bar_s;
+    __shared__ SCFArgs ia;
+    __shared__ int next;
+    const bool tc_any = tensor_items != 0 && a.o.density_step != 0;
+    TCState tc;
+    tc_setup(tc_any, tc, &tc_taddr_s, &tc_bar_s);
+    for (int round = 0; round < b.n; round++) {
+        if (threadIdx.x == 0) next = atomicAdd(queue, 1);
+        __syncthreads();
+        const int q = next;
+        if (q >= b.n) break;
+        if (threadIdx.x == 0) {
+            const int k = order[q];
+            const BatchItem &it = b.items[k];
+            ia = a;
+            ia.s = it.s; ia.plan = it.plan; ia.n_frames = 1;
+            ia.ws = a.ws + it.ws; ia.density = a.density + it.dens;
+            ia.phi = a.phi ? a.phi + it.atom : nullptr;
+            ia.charges = a.charges ? a.charges + it.atom : nullptr;
+            ia.energies = a.energies + (size_t)k * PDG_NENERGY;
+            ia.status = a.status + k;
+            ia.ncycles = a.ncycles ? a.ncycles + k : nullptr;
+        }
+        __syncthreads();
+        const int N = ia.s.n_basis;
+        const bool ok = tc_any && N <= 144 && smem_plan(N, ia.s.n_vec, a.smem_limit).amat != 0;
+        scf_frame(ia, 0, shm, tc, ok);
+        __syncthreads();
+    }
+    tc_teardown(tc_any, tc);
+}
+
+size_t scf_smem_bytes(int N, int kv) { return smem_plan(N, kv, PDG_SMEM_LIMIT).bytes; }
+size_t scf_smem_bytes_limit(int N, int kv, int limit_bytes) { return smem_plan(N, kv, limit_bytes).bytes; }
 
 int scf_occupancy(const DeviceSystem &s, int *threads, int *smem_bytes, int *ctas_per_sm)
 {
@@ -1131,6 +1193,7 @@ void launch_scf(const DeviceSystem &s, const FramePlan &p, int n_frames, const d
     a.s = s; a.plan = p; a.n_frames = n_frames; a.phi = phi; a.o = o; a.density = density; a.use_density = use_density;
     a.energies = energies; a.charges = charges; a.status = status; a.ncycles = ncycles; a.ws = ws;
     a.fock_only = fock_only; a.fock_out = fock_out;
+    a.smem_limit = PDG_SMEM_LIMIT;
     size_t sm = scf_smem_bytes(s.n_basis, s.n_vec);
     static size_t configured = 0;
     if (sm > 48 * 1024 && sm > configured) {
@@ -1140,4 +1203,24 @@ void launch_scf(const DeviceSystem &s, const FramePlan &p, int n_frames, const d
         configured = sm;
     }
     k_scf<<<n_frames, PDG_BLOCK, sm, st>>>(a);
+}
+
+void launch_batch_scf(const Batch &b, const int *order, int *queue, int grid, int smem_limit, size_t smem_bytes, int tensor_items,
+                      const double *phi, const pdg_scf_options &o, double *density, int use_density, double *energies,
+                      double *charges, int *status, int *ncycles, double *ws, cudaStream_t st)
+{
+    SCFArgs a = {};
+    a.n_frames = b.n; a.phi = phi; a.o = o; a.density = density; a.use_density = use_density;
+    a.energies = energies; a.charges = charges; a.status = status; a.ncycles = ncycles; a.ws = ws;
+    a.fock_only = 0; a.fock_out = nullptr; a.smem_limit = smem_limit;
+    k_scf_batch<<<grid, PDG_BLOCK, smem_bytes, st>>>(a, b, order, queue, tensor_items);
+}
+
+// Launch attributes of the batch SCF kernel for a dynamic shared-memory size (outside any stream capture).
+int configure_batch_scf(size_t smem_bytes)
+{
+    if (cudaFuncSetAttribute(k_scf_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes) != cudaSuccess) return 1;
+    if (cudaFuncSetAttribute(k_scf_batch, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+        return 1;
+    return 0;
 }

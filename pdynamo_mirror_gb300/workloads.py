@@ -118,3 +118,12 @@ def perturbed_frames(xyz, n, sigma=0.02, seed=7):
     rng = np.random.default_rng(seed)
     xyz = np.asarray(xyz, float)
     return xyz[None] + rng.normal(scale=sigma, size=(n,) + xyz.shape)
+
+
+def water_clusters(n_clusters=512, smallest=4, largest=64, seed=2):
+    """n_clusters independent water clusters of seeded uniform size (smallest..largest molecules), each placed
+    as water_cluster (O positions uniform in a cube of edge 8 (w/16)^(1/3) A, O-O >= 2.6 A, random
+    orientations).  Returns a list of (atomic numbers, coordinates)."""
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(smallest, largest + 1, size=n_clusters)
+    return [water_cluster(int(w), seed=seed * 1000003 + k) for k, w in enumerate(sizes)]
