@@ -275,6 +275,8 @@ int pdg_batch_energy_gradients(pdg_batch *batch, const double *d_xyz, const doub
                                double *d_density, int use_density, double *d_energies, double *d_gradients,
                                double *d_charges, int *d_status, int *d_ncycles, void *d_workspace, size_t workspace_bytes,
                                void *stream);
+/* Per-item SCF phase timings of the last batch call, PDG_NTIMERS doubles per item (as pdg_scf_timings). */
+int pdg_batch_timings(const pdg_batch *batch, const void *d_workspace, size_t workspace_bytes, double *d_out, void *stream);
 /* The same work captured once into a CUDA graph on the given buffers (a queue reset and five kernel launches);
  * pdg_graph_launch replays it on a stream.  The buffers must outlive the graph.  No reference counterpart. */
 int pdg_batch_graph_create(pdg_batch *batch, const double *d_xyz, const double *d_phi, const pdg_scf_options *options,

@@ -18,7 +18,7 @@ EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system
            "pdg_energy_gradients", "pdg_scf", "pdg_density", "pdg_one_electron", "pdg_fock", "pdg_gradients", "pdg_qcmm_potentials",
            "pdg_qcmm_gradients", "pdg_scf_timings", "pdg_gradients_static_scratch", "pdg_tc_selftest", "pdg_scf_occupancy", "pdg_guess_features", "pdg_mlp_forward",
            "pdg_mlp_backward", "pdg_mlp_adam", "pdg_guess_assemble", "pdg_guess_loss", "pdg_batch_create", "pdg_batch_destroy",
-           "pdg_batch_info", "pdg_batch_workspace_bytes", "pdg_batch_schedule", "pdg_batch_energy_gradients",
+           "pdg_batch_info", "pdg_batch_workspace_bytes", "pdg_batch_schedule", "pdg_batch_energy_gradients", "pdg_batch_timings",
            "pdg_batch_graph_create", "pdg_graph_launch", "pdg_graph_destroy", "pdg_last_error")
 TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densities Tridiagonal", "QC Densities Eigenvalues",
           "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds",
@@ -86,6 +86,7 @@ def load(path=LIB_PATH):
     L.pdg_batch_schedule.argtypes = [P, I, I]
     L.pdg_batch_energy_gradients.argtypes = [P, P, P, ctypes.POINTER(SCFOptions), P, I, P, P, P, P, P, P, S, P]
     L.pdg_batch_graph_create.argtypes = [P, P, P, ctypes.POINTER(SCFOptions), P, I, P, P, P, P, P, P, S, PP]
+    L.pdg_batch_timings.argtypes = [P, P, S, P, P]
     L.pdg_graph_launch.argtypes = [P, P]
     L.pdg_graph_destroy.argtypes = [P]
     for name in EXPORTS:

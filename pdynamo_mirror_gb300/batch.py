@@ -157,6 +157,14 @@ class MoleculeBatch:
                        "best": {"ctas_per_sm": best[0], "order": "largest first" if best[1] == 0 else "item order"}}
         return times
 
+    def timings(self):
+        """Per-molecule SCF phase timings of the last call, as {name: array [n]} (names as QCEngine.timings)."""
+        out = torch.empty((self.n, len(_native.TIMERS)), dtype=torch.float64, device=self.device)
+        _native.check(self.L.pdg_batch_timings(self.handle, _native.ptr(self.ws), self.ws.numel(), _native.ptr(out),
+                                               _native.stream_handle(torch.cuda.current_stream(self.device))), "pdg_batch_timings")
+        t = out.cpu().numpy()
+        return {name: t[:, k] for k, name in enumerate(_native.TIMERS)}
+
     # -- results
     def results(self, b):
         """Host results: Pure QC energies (kJ/mol) [n], gradients (kJ/mol/A) per molecule, status, cycles."""

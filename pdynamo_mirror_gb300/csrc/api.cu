@@ -529,6 +529,21 @@ extern "C" int pdg_batch_energy_gradients(pdg_batch *bt, const double *d_xyz, co
                        (cudaStream_t)stream);
 }
 
+extern "C" int pdg_batch_timings(const pdg_batch *bt, const void *ws, size_t bytes, double *d_out, void *stream)
+{
+    if (!bt || !d_out) return fail(PDG_BAD_ARGUMENT, "null argument");
+    if (!ws || bytes < pdg_batch_workspace_bytes(bt)) return fail(PDG_BAD_ARGUMENT, "workspace missing or too small");
+    const double *w = (const double *)ws;
+    int rc;
+    for (int k = 0; k < bt->b.n; k++) {
+        const BatchItem &it = bt->items[k];
+        if ((rc = cuda_check(cudaMemcpyAsync(d_out + (size_t)k * PDG_NTIMERS, w + it.ws + it.plan.misc + PDG_MAX_HISTORY * PDG_MAX_HISTORY,
+                                             sizeof(double) * PDG_NTIMERS, cudaMemcpyDeviceToDevice, (cudaStream_t)stream), "copy timings")))
+            return rc;
+    }
+    return PDG_OK;
+}
+
 struct pdg_graph {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
