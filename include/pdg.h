@@ -263,14 +263,16 @@ typedef struct pdg_graph pdg_graph;
 
 int pdg_batch_create(pdg_system *const *systems, int n_items, pdg_batch **out);
 int pdg_batch_destroy(pdg_batch *batch);
-/* n_items, total atoms, total density doubles, and the SCF launch the schedule gives: persistent CTAs, dynamic
- * shared memory per CTA, items that can use the tensor-core purification step (N <= 144, matrix in shared memory). */
-int pdg_batch_info(const pdg_batch *batch, int *n_items, int *n_atoms, long long *density_doubles, int *grid, int *smem_bytes,
-                   int *tensor_items);
+/* n_items, total atoms, total density doubles, and the SCF launch the schedule gives: persistent CTAs, threads
+ * per CTA, dynamic shared memory per CTA, items that can use the tensor-core purification step (256-thread
+ * variant, N <= 144, matrix in shared memory). */
+int pdg_batch_info(const pdg_batch *batch, int *n_items, int *n_atoms, long long *density_doubles, int *grid, int *threads,
+                   int *smem_bytes, int *tensor_items);
 size_t pdg_batch_workspace_bytes(const pdg_batch *batch);
-/* Schedule of the persistent SCF kernel (the autotuner's knobs): ctas_per_sm 1 (each CTA may keep matrices
- * up to 220 KB in shared memory) or 2 (112 KB each); order 0 = largest item first, 1 = item order. */
-int pdg_batch_schedule(pdg_batch *batch, int ctas_per_sm, int order);
+/* Schedule of the persistent SCF kernel (the autotuner's knobs): threads 256 with ctas_per_sm 2 (112 KB of
+ * shared memory each) or 1 (220 KB), or threads 512 with ctas_per_sm 1 (FP64 steps only; all of an SM's warps
+ * on one molecule); order 0 = largest item first, 1 = item order. */
+int pdg_batch_schedule(pdg_batch *batch, int threads, int ctas_per_sm, int order);
 int pdg_batch_energy_gradients(pdg_batch *batch, const double *d_xyz, const double *d_phi, const pdg_scf_options *options,
                                double *d_density, int use_density, double *d_energies, double *d_gradients,
                                double *d_charges, int *d_status, int *d_ncycles, void *d_workspace, size_t workspace_bytes,

@@ -80,10 +80,10 @@ def load(path=LIB_PATH):
     L.pdg_batch_create.argtypes = [P, I, PP]
     L.pdg_batch_destroy.argtypes = [P]
     L.pdg_batch_info.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(LL), ctypes.POINTER(I), ctypes.POINTER(I),
-                                 ctypes.POINTER(I)]
+                                 ctypes.POINTER(I), ctypes.POINTER(I)]
     L.pdg_batch_workspace_bytes.argtypes = [P]
     L.pdg_batch_workspace_bytes.restype = S
-    L.pdg_batch_schedule.argtypes = [P, I, I]
+    L.pdg_batch_schedule.argtypes = [P, I, I, I]
     L.pdg_batch_energy_gradients.argtypes = [P, P, P, ctypes.POINTER(SCFOptions), P, I, P, P, P, P, P, P, S, P]
     L.pdg_batch_graph_create.argtypes = [P, P, P, ctypes.POINTER(SCFOptions), P, I, P, P, P, P, P, P, S, PP]
     L.pdg_batch_timings.argtypes = [P, P, S, P, P]

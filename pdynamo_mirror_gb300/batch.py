@@ -3,8 +3,8 @@
 One launch per kernel covers the whole batch: pair integrals and H, a persistent SCF kernel whose CTAs take
 molecules from a queue largest first (so the longest SCFs start first and the smallest fill the tail), and
 the gradients.  ``capture`` records that sequence once as a CUDA graph on fixed buffers; ``autotune`` times
-the SCF schedules (CTAs per SM and so the shared memory each CTA may plan for, and the queue order) on the
-batch itself and keeps the fastest.  The reference evaluates one molecule per ``QCModel.Energy`` call
+the SCF schedules (the 256- or 512-thread SCF variant, CTAs per SM and so the shared memory each CTA may plan
+for, and the queue order) on the batch itself and keeps the fastest.  The reference evaluates one molecule per ``QCModel.Energy`` call
 (pMolecule.QCModel.pyx:146-185); the per-molecule results here are the same quantities.
 """
 
@@ -17,7 +17,8 @@ from . import _native
 from .engine import GRADIENT_TO_KJ_PER_A, HARTREES_TO_KJ, QCEngine, require_cuda
 from .parameters import ANGSTROMS_TO_BOHRS
 
-SCHEDULES = ((2, 0), (1, 0), (2, 1))   # (SCF CTAs per SM, queue order: 0 largest first, 1 item order)
+# (threads per SCF CTA, SCF CTAs per SM, queue order: 0 largest first, 1 item order)
+SCHEDULES = ((256, 2, 0), (256, 1, 0), (512, 1, 0), (256, 2, 1))
 
 
 class BatchGraph:
@@ -81,15 +82,15 @@ class MoleculeBatch:
 
     # -- schedule
     def info(self):
-        n, na, gr, sm, ti = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        n, na, gr, th, sm, ti = (ctypes.c_int() for _ in range(6))
         nd = ctypes.c_longlong()
         _native.check(self.L.pdg_batch_info(self.handle, ctypes.byref(n), ctypes.byref(na), ctypes.byref(nd), ctypes.byref(gr),
-                                            ctypes.byref(sm), ctypes.byref(ti)), "pdg_batch_info")
-        return {"items": n.value, "atoms": na.value, "density_doubles": nd.value, "scf_ctas": gr.value, "scf_shared_bytes": sm.value,
-                "tensor_items": ti.value}
+                                            ctypes.byref(th), ctypes.byref(sm), ctypes.byref(ti)), "pdg_batch_info")
+        return {"items": n.value, "atoms": na.value, "density_doubles": nd.value, "scf_ctas": gr.value, "scf_threads": th.value,
+                "scf_shared_bytes": sm.value, "tensor_items": ti.value}
 
-    def schedule(self, ctas_per_sm=2, order=0):
-        _native.check(self.L.pdg_batch_schedule(self.handle, int(ctas_per_sm), int(order)), "pdg_batch_schedule")
+    def schedule(self, threads=256, ctas_per_sm=2, order=0):
+        _native.check(self.L.pdg_batch_schedule(self.handle, int(threads), int(ctas_per_sm), int(order)), "pdg_batch_schedule")
 
     # -- buffers and calls
     def coordinates(self, frames):
@@ -153,8 +154,8 @@ class MoleculeBatch:
             times[sch] = t0.elapsed_time(t1) / repeats
         best = min(times, key=times.get)
         self.schedule(*best)
-        self.tuning = {"schedules_ms": {"%d_ctas_per_sm_order_%d" % k: v for k, v in times.items()},
-                       "best": {"ctas_per_sm": best[0], "order": "largest first" if best[1] == 0 else "item order"}}
+        self.tuning = {"schedules_ms": {"%d_threads_%d_ctas_per_sm_order_%d" % k: v for k, v in times.items()},
+                       "best": {"threads": best[0], "ctas_per_sm": best[1], "order": "largest first" if best[2] == 0 else "item order"}}
         return times
 
     def timings(self):

@@ -383,14 +383,16 @@ struct pdg_batch {
     Batch b = {};
     size_t ws_doubles = 0, dens_doubles = 0;
     int n_atoms = 0, sms = 0;
-    // schedule (pdg_batch_schedule)
-    int ctas_per_sm = PDG_SCF_CTAS_PER_SM, order_mode = 0, grid = 0, smem_limit = 0, tensor_items = 0;
+    // schedule (pdg_batch_schedule): SCF variant (256 or 512 threads per CTA), CTAs per SM, queue order
+    int threads = 256, ctas_per_sm = 2, order_mode = 0, grid = 0, smem_limit = 0, tensor_items = 0;
     size_t smem_bytes = 0;
 };
 
-static int batch_schedule(pdg_batch *bt, int ctas_per_sm, int order_mode)
+static int batch_schedule(pdg_batch *bt, int threads, int ctas_per_sm, int order_mode)
 {
     const int n = bt->b.n;
+    const bool wide = threads == 512;
+    bt->threads = threads;
     bt->ctas_per_sm = ctas_per_sm;
     bt->order_mode = order_mode;
     bt->smem_limit = ctas_per_sm == 1 ? PDG_SMEM_LIMIT_1 : PDG_SMEM_LIMIT_2;
@@ -398,11 +400,13 @@ static int batch_schedule(pdg_batch *bt, int ctas_per_sm, int order_mode)
     bt->smem_bytes = 0;
     bt->tensor_items = 0;
     for (const BatchItem &it : bt->items) {
-        const size_t by = scf_smem_bytes_limit(it.s.n_basis, it.s.n_vec, bt->smem_limit);
+        const size_t by = wide ? scf_w::scf_smem_bytes_limit(it.s.n_basis, it.s.n_vec, bt->smem_limit)
+                               : scf_n::scf_smem_bytes_limit(it.s.n_basis, it.s.n_vec, bt->smem_limit);
         bt->smem_bytes = std::max(bt->smem_bytes, by);
-        // the purification step needs N <= 144 and the packed matrix in shared memory (the plan's amat)
-        const size_t small = scf_smem_bytes_limit(it.s.n_basis, it.s.n_vec, 0);
-        if (it.s.n_basis <= 144 && by > small) bt->tensor_items++;
+        // the purification step (256-thread variant only) needs N <= 144 and the packed matrix in shared
+        // memory (the plan's amat)
+        const size_t small = scf_n::scf_smem_bytes_limit(it.s.n_basis, it.s.n_vec, 0);
+        if (!wide && it.s.n_basis <= 144 && by > small) bt->tensor_items++;
     }
     std::vector<int> order(n);
     for (int k = 0; k < n; k++) order[k] = k;
@@ -410,7 +414,8 @@ static int batch_schedule(pdg_batch *bt, int ctas_per_sm, int order_mode)
         std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return bt->items[x].s.n_basis > bt->items[y].s.n_basis; });
     int rc;
     if ((rc = cuda_check(cudaMemcpy(bt->d_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice), "copy batch order"))) return rc;
-    if (configure_batch_scf(bt->smem_bytes)) return cuda_check(cudaGetLastError(), "batch SCF launch attributes");
+    if (wide ? scf_w::configure_batch_scf(bt->smem_bytes) : scf_n::configure_batch_scf(bt->smem_bytes))
+        return cuda_check(cudaGetLastError(), "batch SCF launch attributes");
     return PDG_OK;
 }
 
@@ -452,7 +457,7 @@ extern "C" int pdg_batch_create(pdg_system *const *systems, int n_items, pdg_bat
         return rc;
     }
     bt->b.items = bt->d_items;
-    if ((rc = batch_schedule(bt, PDG_SCF_CTAS_PER_SM, 0))) { pdg_batch_destroy(bt); return rc; }
+    if ((rc = batch_schedule(bt, 256, 2, 0))) { pdg_batch_destroy(bt); return rc; }
     *out = bt;
     return PDG_OK;
 }
@@ -465,10 +470,11 @@ extern "C" int pdg_batch_destroy(pdg_batch *bt)
     return PDG_OK;
 }
 
-extern "C" int pdg_batch_info(const pdg_batch *bt, int *n_items, int *n_atoms, long long *density_doubles, int *grid, int *smem_bytes,
-                              int *tensor_items)
+extern "C" int pdg_batch_info(const pdg_batch *bt, int *n_items, int *n_atoms, long long *density_doubles, int *grid, int *threads,
+                              int *smem_bytes, int *tensor_items)
 {
     if (!bt) return fail(PDG_BAD_ARGUMENT, "null batch");
+    if (threads) *threads = bt->threads;
     if (n_items) *n_items = bt->b.n;
     if (n_atoms) *n_atoms = bt->n_atoms;
     if (density_doubles) *density_doubles = (long long)bt->dens_doubles;
@@ -480,12 +486,13 @@ extern "C" int pdg_batch_info(const pdg_batch *bt, int *n_items, int *n_atoms, l
 
 extern "C" size_t pdg_batch_workspace_bytes(const pdg_batch *bt) { return bt ? sizeof(double) * bt->ws_doubles : 0; }
 
-extern "C" int pdg_batch_schedule(pdg_batch *bt, int ctas_per_sm, int order)
+extern "C" int pdg_batch_schedule(pdg_batch *bt, int threads, int ctas_per_sm, int order)
 {
     if (!bt) return fail(PDG_BAD_ARGUMENT, "null batch");
-    if (ctas_per_sm != 1 && ctas_per_sm != 2) return fail(PDG_BAD_ARGUMENT, "ctas_per_sm must be 1 or 2");
+    if (!((threads == 256 && (ctas_per_sm == 1 || ctas_per_sm == 2)) || (threads == 512 && ctas_per_sm == 1)))
+        return fail(PDG_BAD_ARGUMENT, "schedule must be 256 threads with 1 or 2 CTAs per SM, or 512 threads with 1");
     if (order != 0 && order != 1) return fail(PDG_BAD_ARGUMENT, "order must be 0 (largest first) or 1 (item order)");
-    return batch_schedule(bt, ctas_per_sm, order);
+    return batch_schedule(bt, threads, ctas_per_sm, order);
 }
 
 static int batch_queue(pdg_batch *bt, const double *d_xyz, const double *d_phi, const pdg_scf_options *o, double *d_density,
@@ -497,8 +504,12 @@ static int batch_queue(pdg_batch *bt, const double *d_xyz, const double *d_phi, 
     launch_batch_integrals(bt->b, d_xyz, w, st);
     if ((rc = cuda_check(cudaGetLastError(), "batch integral kernels"))) return rc;
     if ((rc = cuda_check(cudaMemsetAsync(bt->d_queue, 0, sizeof(int), st), "reset batch queue"))) return rc;
-    launch_batch_scf(bt->b, bt->d_order, bt->d_queue, bt->grid, bt->smem_limit, bt->smem_bytes, bt->tensor_items, d_phi, *o, d_density,
-                     use_density, d_energies, d_charges, d_status, d_ncycles, w, st);
+    if (bt->threads == 512)
+        scf_w::launch_batch_scf(bt->b, bt->d_order, bt->d_queue, bt->grid, bt->smem_limit, bt->smem_bytes, 0, d_phi, *o, d_density,
+                                use_density, d_energies, d_charges, d_status, d_ncycles, w, st);
+    else
+        scf_n::launch_batch_scf(bt->b, bt->d_order, bt->d_queue, bt->grid, bt->smem_limit, bt->smem_bytes, bt->tensor_items, d_phi, *o,
+                                d_density, use_density, d_energies, d_charges, d_status, d_ncycles, w, st);
     if ((rc = cuda_check(cudaGetLastError(), "batch scf kernel"))) return rc;
     if (d_gradients) {
         launch_batch_gradients(bt->b, d_xyz, d_density, w, d_gradients, st);

@@ -184,9 +184,6 @@ __device__ __forceinline__ double block_max(double v, double *red)
 // Kernel launchers (defined in the .cu files, called by api.cu).
 void launch_pair_integrals(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *xyz, double *ws, cudaStream_t st);
 void launch_assemble_h(const DeviceSystem &s, const FramePlan &p, int n_frames, double *ws, cudaStream_t st);
-void launch_scf(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *phi, const pdg_scf_options &o,
-                double *density, int use_density, double *energies, double *charges, int *status, int *ncycles,
-                double *ws, int fock_only, double *fock_out, cudaStream_t st);
 void launch_pair_gradients(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *xyz,
                            const double *density, double *ws, cudaStream_t st);
 void launch_reduce_gradients(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *ws,
@@ -194,11 +191,6 @@ void launch_reduce_gradients(const DeviceSystem &s, const FramePlan &p, int n_fr
 // Heterogeneous batches (the same kernels over a BatchItem table).
 void launch_batch_integrals(const Batch &b, const double *xyz, double *ws, cudaStream_t st);
 void launch_batch_gradients(const Batch &b, const double *xyz, const double *density, double *ws, double *gradients, cudaStream_t st);
-void launch_batch_scf(const Batch &b, const int *order, int *queue, int grid, int smem_limit, size_t smem_bytes, int tensor_items,
-                      const double *phi, const pdg_scf_options &o, double *density, int use_density, double *energies,
-                      double *charges, int *status, int *ncycles, double *ws, cudaStream_t st);
-size_t scf_smem_bytes_limit(int N, int kv, int limit_bytes);
-int configure_batch_scf(size_t smem_bytes);
 #define PDG_SMEM_LIMIT_1 (220 * 1024)   // shared-memory budget of one SCF CTA alone on its SM
 #define PDG_SMEM_LIMIT_2 (112 * 1024)   // ... of each of two
 int launch_qcmm_potentials(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,
@@ -207,7 +199,23 @@ int launch_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const dou
                           const double *q, const double *qcq, int n_knots, const double *knots, double cutoff,
                           double *gqc, double *gmm, cudaStream_t st);
 int launch_tc_selftest(int n, int kprod, const float *x, float *c, int *status, cudaStream_t st);
-int scf_occupancy(const DeviceSystem &s, int *threads, int *smem_bytes, int *ctas_per_sm);
+
+// SCF kernels (scf.cu), in two compiled variants: scf_n (256 threads per CTA, tensor-core step) and scf_w
+// (scf_wide.cu: 512 threads per CTA, FP64 only).  The single-system entry points use scf_n.
+#define PDG_SCF_LAUNCHERS                                                                                                   \
+    void launch_scf(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *phi, const pdg_scf_options &o, \
+                    double *density, int use_density, double *energies, double *charges, int *status, int *ncycles,      \
+                    double *ws, int fock_only, double *fock_out, cudaStream_t st);                                        \
+    int scf_occupancy(const DeviceSystem &s, int *threads, int *smem_bytes, int *ctas_per_sm);                           \
+    void launch_batch_scf(const Batch &b, const int *order, int *queue, int grid, int smem_limit, size_t smem_bytes,     \
+                          int tensor_items, const double *phi, const pdg_scf_options &o, double *density, int use_density, \
+                          double *energies, double *charges, int *status, int *ncycles, double *ws, cudaStream_t st);    \
+    size_t scf_smem_bytes_limit(int N, int kv, int limit_bytes);                                                         \
+    int configure_batch_scf(size_t smem_bytes);
+namespace scf_n { PDG_SCF_LAUNCHERS }
+namespace scf_w { PDG_SCF_LAUNCHERS }
+using scf_n::launch_scf;
+using scf_n::scf_occupancy;
 void launch_guess_features(const DeviceSystem &s, int n_frames, const double *xyz, const double *phi, float *env, int *count,
                            int *offsets, float *X, int *row_frame, int *row_pair, cudaStream_t st);
 void launch_mlp_forward(int max_rows, const int *rows, int K, int N, const float *X, const void *W, const float *b, float *Z, float *H,

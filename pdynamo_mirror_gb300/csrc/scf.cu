@@ -17,6 +17,13 @@
 #include "multipole.cuh"
 #include "tc.cuh"
 
+// The SCF kernels are compiled twice: as scf_n (this file: 256 threads per CTA, two CTAs per SM, with the
+// tensor-core purification step) and as scf_w (scf_wide.cu: 512 threads, one CTA per SM, FP64 steps only).
+#ifndef PDG_SCF_NS
+#define PDG_SCF_NS scf_n
+#endif
+namespace PDG_SCF_NS {
+
 
 struct SCFArgs {
     DeviceSystem s; FramePlan plan; int n_frames;
@@ -589,21 +596,66 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
         }
     }
     tm.lap(PDG_T_EIGENVECTORS);
-    // --- back-transformation z <- Q z with the reflectors stored in A (last to first), one warp per vector
-    for (int t = w; t < kv; t += PDG_WARPS) {
-        double *zt = Z + (size_t)t * ldz;
-        for (int k = N - 3; k >= 0; k--) {
-            const double tau = sm.tau[k];
-            if (tau == 0.0) continue;
-            const int m = N - k - 1;
-            double dt = 0.0;
-            for (int i = lane; i < m; i += 32) dt = fma(i == 0 ? 1.0 : A[plo(k + 1 + i, k)], zt[k + 1 + i], dt);
-            dt = warp_sum(dt) * tau;
-            for (int i = lane; i < m; i += 32) zt[k + 1 + i] = fma(-dt, i == 0 ? 1.0 : A[plo(k + 1 + i, k)], zt[k + 1 + i]);
-            __syncwarp();
+    // --- back-transformation Z <- Q Z, Q = H_0 H_1 ... H_{N-3} with the reflectors stored in A
+    if (N >= 32) {
+        // blocked (compact WY, as LAPACK's dlarft / dlarfb): blocks of up to 16 consecutive reflectors, last
+        // block first; block b is I - V T V^T with V the reflectors' unit lower-trapezoidal columns over rows
+        // k0 + 1 .. N - 1 (row i of V is contiguous in the packed A) and T upper triangular.  Per block one GEMM
+        // gives S = V^T V and W = V^T Z together, one warp builds T from S, W2 = T W, and a second GEMM applies
+        // Z^T -= W2^T V^T (stores along Z's rows).  Same 2 N^2 kv flops as reflector-by-reflector, but Z and the
+        // reflectors pass through the GEMM staging once per block instead of once per reflector and vector.
+        const int nref = N - 2;
+        double *Wm = wsf + pl.LU, *W2 = Wm + (size_t)16 * kv, *Sg = W2 + (size_t)16 * kv, *Tt = Sg + 256;
+        for (int k0 = ((nref - 1) / 16) * 16; k0 >= 0; k0 -= 16) {
+            const int nbk = min(16, nref - k0), m0 = N - k0 - 1;
+            auto V = [&](int i, int c) -> double { return i < c ? 0.0 : (i == c ? 1.0 : A[plo(k0 + 1 + i, k0 + c)]); };
+            tgemm<false, true>(nbk, 16 + kv, m0, [&](int c, int i) { return V(i, c); },
+                               [&](int i, int j) { return j < 16 ? (j < nbk ? V(i, j) : 0.0) : Z[(size_t)(j - 16) * ldz + k0 + 1 + i]; },
+                               false, sm, [&](int c, int j, double v) {
+                                   if (j < 16) Sg[c * 16 + j] = v;
+                                   else Wm[(size_t)c * kv + (j - 16)] = v;
+                               });
+            if (w == 0) {   // T(c, c) = tau_c;  T(0:c, c) = -tau_c T(0:c, 0:c) S(0:c, c)
+                for (int c = 0; c < nbk; c++) {
+                    const double tau = sm.tau[k0 + c];
+                    double t = 0.0;
+                    if (lane < c) {
+                        for (int j = lane; j < c; j++) t = fma(Tt[lane * 16 + j], Sg[j * 16 + c], t);
+                        t *= -tau;
+                    }
+                    __syncwarp();
+                    if (lane < 16) Tt[lane * 16 + c] = lane < c ? t : (lane == c ? tau : 0.0);
+                    __syncwarp();
+                }
+            }
+            __syncthreads();
+            for (int e = tid; e < nbk * kv; e += PDG_BLOCK) {
+                const int c = e / kv, t = e % kv;
+                double acc = 0.0;
+                for (int j = c; j < nbk; j++) acc = fma(Tt[c * 16 + j], Wm[(size_t)j * kv + t], acc);
+                W2[(size_t)c * kv + t] = acc;
+            }
+            __syncthreads();
+            tgemm<false, true>(kv, m0, nbk, [&](int t, int c) { return W2[(size_t)c * kv + t]; }, [&](int c, int i) { return V(i, c); },
+                               false, sm, [&](int t, int i, double v) { Z[(size_t)t * ldz + k0 + 1 + i] -= v; });
         }
+    } else {
+        // reflector by reflector, one warp per vector
+        for (int t = w; t < kv; t += PDG_WARPS) {
+            double *zt = Z + (size_t)t * ldz;
+            for (int k = N - 3; k >= 0; k--) {
+                const double tau = sm.tau[k];
+                if (tau == 0.0) continue;
+                const int m = N - k - 1;
+                double dt = 0.0;
+                for (int i = lane; i < m; i += 32) dt = fma(i == 0 ? 1.0 : A[plo(k + 1 + i, k)], zt[k + 1 + i], dt);
+                dt = warp_sum(dt) * tau;
+                for (int i = lane; i < m; i += 32) zt[k + 1 + i] = fma(-dt, i == 0 ? 1.0 : A[plo(k + 1 + i, k)], zt[k + 1 + i]);
+                __syncwarp();
+            }
+        }
+        __syncthreads();
     }
-    __syncthreads();
     tm.lap(PDG_T_BACKTRANSFORM);
     // --- P = 2 Z^T Z (occupied) or 2 (1 - Z^T Z) (virtual); lower triangle then mirrored
     const bool occ = s.vec_occupied;
@@ -828,7 +880,11 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
     double base = 0.0;
     for (int A = tid; A < s.n_atoms; A += PDG_BLOCK) { const double *E = elem(s, s.atom_elem[A]); base += E[PDG_E_EHEAT] - E[PDG_E_EISOL]; }
     base = block_sum(base, sm.red);
+#ifdef PDG_SCF_NO_TENSOR
+    const bool want_mixed = false;
+#else
     const bool want_mixed = tc_ok && a.fock_only != 1 && a.o.density_step != 0 && N <= 144 && sm.amat != nullptr;
+#endif
     bool mixed = want_mixed, last_mixed = false;
     int n_mixed = 0;
     bool valid = a.use_density != 0;
@@ -1095,6 +1151,9 @@ __device__ __forceinline__ void tc_setup(bool ok, TCState &tc, uint32_t *taddr_s
 {
     const int w = threadIdx.x >> 5;
     tc.tmem = 0u; tc.bar = 0u; tc.phase = 0u;
+#ifdef PDG_SCF_NO_TENSOR
+    return;   // no tcgen05 code in this variant: nothing to allocate or relinquish
+#endif
     if (!ok) {
         if (w == 0) asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
         return;
@@ -1109,6 +1168,9 @@ __device__ __forceinline__ void tc_setup(bool ok, TCState &tc, uint32_t *taddr_s
 
 __device__ __forceinline__ void tc_teardown(bool ok, const TCState &tc)
 {
+#ifdef PDG_SCF_NO_TENSOR
+    return;
+#endif
     if (!ok) return;
     tc_fence_before();
     __syncthreads();
@@ -1224,3 +1286,5 @@ int configure_batch_scf(size_t smem_bytes)
         return 1;
     return 0;
 }
+
+}   // namespace PDG_SCF_NS
