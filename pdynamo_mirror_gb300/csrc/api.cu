@@ -107,12 +107,16 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     const size_t cel_at = ints.size();
     ints.insert(ints.end(), cel.begin(), cel.end());
     ints.insert(ints.end(), xel.begin(), xel.end());
-    // s-s pairs (thread-per-pair kernels) and the others (warp-per-pair kernels)
-    std::vector<int> pss, pgen;
-    for (int p = 0; p < npairs; p++) (norb[pi[p]] == 1 && norb[pj[p]] == 1 ? pss : pgen).push_back(p);
+    // s-s and sp-s pairs (thread-per-pair kernels) and sp-sp pairs (warp-per-pair kernels)
+    std::vector<int> pss, pgen, psps;
+    for (int p = 0; p < npairs; p++) {
+        const int ns = (norb[pi[p]] == 1) + (norb[pj[p]] == 1);
+        (ns == 2 ? pss : ns == 1 ? psps : pgen).push_back(p);
+    }
     const size_t pl_at = ints.size();
     ints.insert(ints.end(), pss.begin(), pss.end());
     ints.insert(ints.end(), pgen.begin(), pgen.end());
+    ints.insert(ints.end(), psps.begin(), psps.end());
     int rc = PDG_OK;
     if ((rc = cuda_check(cudaMalloc(&s->d_elements, sizeof(double) * s->elements.size()), "cudaMalloc elements")) ||
         (rc = cuda_check(cudaMalloc(&s->d_terms, sizeof(double) * terms.size()), "cudaMalloc terms")) ||
@@ -137,6 +141,7 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     d.ovl = s->d_ovl; d.ovl_off = d.pair_tei + npairs; d.ovl_n = d.ovl_off + n_elements * n_elements;
     d.cel = b + cel_at; d.xel = d.cel + cel.size(); d.n_cel = (int)cel.size(); d.n_xel = (int)xel.size();
     d.pairs_ss = b + pl_at; d.pairs_gen = d.pairs_ss + pss.size(); d.n_ss = (int)pss.size(); d.n_gen = (int)pgen.size();
+    d.pairs_sps = d.pairs_gen + pgen.size(); d.n_sps = (int)psps.size();
     *out = s;
     return PDG_OK;
 }
@@ -425,26 +430,26 @@ extern "C" int pdg_batch_create(pdg_system *const *systems, int n_items, pdg_bat
     *out = nullptr;
     if (n_items <= 0) return fail(PDG_BAD_ARGUMENT, "n_items must be positive");
     pdg_batch *bt = new pdg_batch();
-    long long ws = 0, dens = 0, atom = 0, work[3] = { 0, 0, 0 };
+    long long ws = 0, dens = 0, atom = 0, work[PDG_WORK_KINDS] = {};
     for (int k = 0; k < n_items; k++) {
         if (!systems[k]) { delete bt; return fail(PDG_BAD_ARGUMENT, "null system in batch"); }
         BatchItem it = {};
         it.s = systems[k]->d;
         it.plan = plan_for(systems[k], PDG_MAX_HISTORY);
         it.ws = ws; it.dens = dens; it.atom = (int)atom;
-        for (int c = 0; c < 3; c++) it.work[c] = (int)work[c];
+        for (int c = 0; c < PDG_WORK_KINDS; c++) it.work[c] = (int)work[c];
         ws += (long long)it.plan.stride;
         dens += (long long)it.s.n_basis * it.s.n_basis;
         atom += it.s.n_atoms;
-        for (int c = 0; c < 3; c++) work[c] += work_units(it.s, c);
+        for (int c = 0; c < PDG_WORK_KINDS; c++) work[c] += work_units(it.s, c);
         bt->items.push_back(it);
     }
-    if (work[0] > INT32_MAX || work[1] > INT32_MAX || work[2] > INT32_MAX || atom > INT32_MAX) {
+    if (work[0] > INT32_MAX || work[1] > INT32_MAX || work[2] > INT32_MAX || work[3] > INT32_MAX || atom > INT32_MAX) {
         delete bt;
         return fail(PDG_TOO_LARGE, "batch work exceeds 2^31 units");
     }
     bt->b.n = n_items;
-    for (int c = 0; c < 3; c++) bt->b.total[c] = (int)work[c];
+    for (int c = 0; c < PDG_WORK_KINDS; c++) bt->b.total[c] = (int)work[c];
     bt->ws_doubles = (size_t)ws; bt->dens_doubles = (size_t)dens; bt->n_atoms = (int)atom;
     int dev = 0, rc;
     if ((rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice")) ||

@@ -33,8 +33,10 @@ struct DeviceSystem {
     const int *ovl_off, *ovl_n;    // per ordered element pair: first record, record count
     const int *cel, *xel;          // Fock outputs: diagonal-block elements (atom << 4 | mn), off-diagonal (pair << 4 | ac)
     int n_cel, n_xel;
-    const int *pairs_ss, *pairs_gen;   // pairs of two one-orbital (s) atoms, and all other pairs, in pair order
+    const int *pairs_ss, *pairs_gen;   // pairs of two one-orbital (s) atoms, and pairs of two sp atoms, in pair order
     int n_ss, n_gen;
+    const int *pairs_sps;              // pairs of one sp and one s atom, in pair order
+    int n_sps;
 };
 
 // Per-frame workspace plan (all offsets in doubles from the frame's base).
@@ -75,20 +77,20 @@ __host__ inline FramePlan make_plan(const DeviceSystem &s, int history)
 // Heterogeneous batches: independent molecules of different sizes (each its own system, one geometry each)
 // computed by the same launches.  Per-item data are concatenated in item order: coordinates, gradients,
 // charges and potentials by atom, densities by N_k^2, workspaces by the item's plan stride.
-enum { PDG_WORK_GEN = 0, PDG_WORK_SS = 1, PDG_WORK_ATOM = 2 };
+enum { PDG_WORK_GEN = 0, PDG_WORK_SS = 1, PDG_WORK_ATOM = 2, PDG_WORK_SPS = 3, PDG_WORK_KINDS = 4 };
 
 struct BatchItem {
     DeviceSystem s;
     FramePlan plan;
     long long ws, dens;   // first workspace double, first density double
     int atom;             // first atom
-    int work[3];          // first global work unit: pair batches of 32 general pairs, s-s pairs, atoms
+    int work[PDG_WORK_KINDS];   // first global work unit: batches of 32 sp-sp pairs, s-s pairs, atoms, sp-s pairs
 };
 
 struct Batch {
     const BatchItem *items;   // device table (null: homogeneous frames of one system)
     int n;
-    int total[3];             // work units of each kind over all items
+    int total[PDG_WORK_KINDS];   // work units of each kind over all items
 };
 
 // What a kernel thread (or warp) works on: the system, plan and data offsets of one frame or batch item
@@ -102,7 +104,7 @@ struct FrameView {
 
 __host__ __device__ inline int work_units(const DeviceSystem &s, int kind)
 {
-    return kind == PDG_WORK_GEN ? (s.n_gen + 31) / 32 : kind == PDG_WORK_SS ? s.n_ss : s.n_atoms;
+    return kind == PDG_WORK_GEN ? (s.n_gen + 31) / 32 : kind == PDG_WORK_SS ? s.n_ss : kind == PDG_WORK_SPS ? s.n_sps : s.n_atoms;
 }
 
 // Global work unit g of the given kind -> its frame or item and the unit's index within it; false past the end.
