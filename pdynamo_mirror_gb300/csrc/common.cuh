@@ -41,7 +41,7 @@ struct DeviceSystem {
 
 // Per-frame workspace plan (all offsets in doubles from the frame's base).
 struct FramePlan {
-    size_t tei, pair_e, pair_g, H, F, P0, A, G, Z, LU, hP, hF, hE, rP, rF, misc, stride;
+    size_t tei, pair_e, pair_g, H, F, P0, A, G, Z, LU, LO, hP, hF, hE, rP, rF, misc, stride;
     int hist_len;   // packed history vector length N(N+1)/2 (errors use N(N-1)/2 within the same slot)
 };
 
@@ -64,6 +64,9 @@ __host__ inline FramePlan make_plan(const DeviceSystem &s, int history)
     p.G = o;      o += align32(kv * N);      // DIIS: the vectors times F
     p.Z = o;      o += align32(kv * (N | 1)); // wanted eigenvectors when they do not fit in shared memory
     p.LU = o;     o += align32(5 * N * kvp + (N * kvp + 7) / 8);   // inverse iteration factors + iterates
+    // BF16 lo parts of the purification iterate (canonical tensor-core layout, R x Kp, R = max(Kp, 128)), N <= 144
+    const size_t Kp = (N + 15) & ~size_t(15), Rr = Kp > 128 ? Kp : 128;
+    p.LO = o;     o += align32(N <= 144 ? (Rr * Kp * 2 + 7) / 8 : 0);
     p.hP = o;     o += align32((size_t)history * p.hist_len);
     p.hF = o;     o += align32((size_t)history * p.hist_len);
     p.hE = o;     o += align32((size_t)history * p.hist_len);

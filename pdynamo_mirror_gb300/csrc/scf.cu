@@ -716,18 +716,21 @@ __device__ double density_step_mixed(const SCFArgs &a, double *wsf, const double
     double tr = block_sum((double)trl, sm.red), sq = block_sum((double)sql, sm.red);
     double defect_1 = 1e300, defect_2 = 1e300;   // defects of the last two iterations
     const int rr = 32 * (w & 3) + lane, nch = Kp / 16, half = (nch + 1) / 2, c0 = w < 4 ? 0 : half, c1 = w < 4 ? half : nch;
+    unsigned char *plo_g = (unsigned char *)(wsf + a.plan.LO);   // BF16 lo parts (global), copied in for phase 2
+    // BF16 parts of X0 (rows beyond N and the padding zero); later iterates get theirs from the readout
+    for (int e = tid; e < R * Kp; e += PDG_BLOCK) {
+        const int r = e / Kp, c = e % Kp;
+        const float x = (r < N && c < N) ? Xa[(size_t)r * N + c] : 0.0f;
+        __nv_bfloat16 h, m, l;
+        bf16_split3(x, h, m, l);
+        const uint32_t o = tc_offset(r, c, Kp);
+        *(__nv_bfloat16 *)(ph + o) = h;
+        *(__nv_bfloat16 *)(pm + o) = m;
+        *(__nv_bfloat16 *)(plo_g + o) = l;
+    }
     float *X = Xa, *Xn = Xb;
     for (int it = 0; it < 100; it++) {
         const bool square = fabs(sq - nocc) < fabs(2.0 * tr - sq - nocc);   // X <- X^2, else 2X - X^2
-        for (int e = tid; e < R * Kp; e += PDG_BLOCK) {   // BF16 parts of X; rows beyond N and the padding zero
-            const int r = e / Kp, c = e % Kp;
-            const float x = (r < N && c < N) ? X[(size_t)r * N + c] : 0.0f;
-            __nv_bfloat16 h, m, l;
-            bf16_split3(x, h, m, l);
-            const uint32_t o = tc_offset(r, c, Kp);
-            *(__nv_bfloat16 *)(ph + o) = h;
-            *(__nv_bfloat16 *)(pm + o) = m;
-        }
         tc_fence_proxy();
         tc_fence_before();
         __syncthreads();
@@ -751,17 +754,12 @@ __device__ double density_step_mixed(const SCFArgs &a, double *wsf, const double
         }
         bool ok = mbar_wait(tc.bar, tc.phase, 1 << 22);
         tc.phase ^= 1u;
-        if (kprod == 6 && ok) {
-            // second phase: lo parts in the mid array (hi.lo + lo.hi)
+        if (kprod == 6 && __syncthreads_and(ok)) {
+            // second phase: the lo parts into the mid array (hi.lo + lo.hi)
             tc_fence_after();
-            __syncthreads();
-            for (int e = tid; e < R * Kp; e += PDG_BLOCK) {
-                const int r = e / Kp, c = e % Kp;
-                const float x = (r < N && c < N) ? X[(size_t)r * N + c] : 0.0f;
-                __nv_bfloat16 h, m, l;
-                bf16_split3(x, h, m, l);
-                *(__nv_bfloat16 *)(pm + tc_offset(r, c, Kp)) = l;
-            }
+            const uint4 *src = (const uint4 *)plo_g;
+            uint4 *dst = (uint4 *)pm;
+            for (int e = tid; e < R * Kp / 8; e += PDG_BLOCK) dst[e] = src[e];
             tc_fence_proxy();
             tc_fence_before();
             __syncthreads();
@@ -781,20 +779,47 @@ __device__ double density_step_mixed(const SCFArgs &a, double *wsf, const double
         // X <- X X or 2X - X X.  X is symmetric up to rounding, so the new matrix is stored transposed:
         // thread (row r) writes Xn[c][r] and reads the old X[c][r], both coalesced across the warp; the
         // columns >= 128 of tile 1 also give rows >= 128 (Xn[r][c]), and tile 2's last lanes the corner.
+        // The same thread writes the BF16 parts of the next iterate: row r, eight columns per 16-byte store
+        // (the products are complete, so the operand arrays are free); rows >= 128 from the mirror and the
+        // corner, one element at a time; padding columns as zeros.
         float trn = 0.0f, sqn = 0.0f;
         for (int ch = c0; ch < c1; ch++) {
             float v[16];
             tc_ld16(tc.tmem + ((uint32_t)(32 * (w & 3)) << 16) + (uint32_t)(ch * 16), v);
             if (rr < N) {
+                float xv[16];
 #pragma unroll
                 for (int j = 0; j < 16; j++) {
                     const int c = ch * 16 + j;
+                    xv[j] = 0.0f;
                     if (c >= N) continue;
                     const float xo = X[(size_t)c * N + rr], xn = square ? v[j] : 2.0f * xo - v[j];
+                    xv[j] = xn;
                     Xn[(size_t)c * N + rr] = xn;
                     if (c >= TC_M) Xn[(size_t)rr * N + c] = xn;
                     sqn = fmaf((c >= TC_M) ? 2.0f * xn : xn, xn, sqn);
                     if (c == rr) trn += xn;
+                }
+#pragma unroll
+                for (int g = 0; g < 2; g++) {
+                    __align__(16) __nv_bfloat16 hv[8], mv[8], lv[8];
+#pragma unroll
+                    for (int j = 0; j < 8; j++) bf16_split3(xv[8 * g + j], hv[j], mv[j], lv[j]);
+                    const uint32_t o = tc_offset(rr, ch * 16 + 8 * g, Kp);
+                    *(uint4 *)(ph + o) = *(const uint4 *)hv;
+                    *(uint4 *)(pm + o) = *(const uint4 *)mv;
+                    if (kprod == 6) *(uint4 *)(plo_g + o) = *(const uint4 *)lv;
+                }
+#pragma unroll
+                for (int j = 0; j < 16; j++) {   // rows >= 128 of the operands: the mirror (c, r)
+                    const int c = ch * 16 + j;
+                    if (c < TC_M || c >= N) continue;
+                    __nv_bfloat16 h, m, l;
+                    bf16_split3(xv[j], h, m, l);
+                    const uint32_t o = tc_offset(c, rr, Kp);
+                    *(__nv_bfloat16 *)(ph + o) = h;
+                    *(__nv_bfloat16 *)(pm + o) = m;
+                    if (kprod == 6) *(__nv_bfloat16 *)(plo_g + o) = l;
                 }
             }
         }
@@ -810,6 +835,12 @@ __device__ double density_step_mixed(const SCFArgs &a, double *wsf, const double
                     Xn[(size_t)c * N + r] = xn;
                     sqn = fmaf(xn, xn, sqn);
                     if (c == r) trn += xn;
+                    __nv_bfloat16 h, m, l;
+                    bf16_split3(xn, h, m, l);
+                    const uint32_t o = tc_offset(r, c, Kp);
+                    *(__nv_bfloat16 *)(ph + o) = h;
+                    *(__nv_bfloat16 *)(pm + o) = m;
+                    if (kprod == 6) *(__nv_bfloat16 *)(plo_g + o) = l;
                 }
             }
         }
