@@ -148,20 +148,22 @@ __global__ void __launch_bounds__(QB) k_qcmm_grad_qc(int model, Spline sp, int n
     if (live && lane == 0) { double *o = gqc + ((size_t)f * n_qc + A) * 3; o[0] = g0; o[1] = g1; o[2] = g2; }
 }
 
-// MM side: a block takes 256 MM atoms of one frame.  An FP32 pass marks the atoms within the cutoff of any
-// QC atom and packs them (block prefix in atom order); the packed atoms then run the FP64 loop over the QC
-// atoms one per thread, and the others get zero.
+// MM side: a block takes 256 MM atoms of one frame.  An FP32 pass (one thread per atom) marks the atoms within
+// the cutoff of any QC atom, packs them (block prefix in atom order) and writes zero for the others; the warps
+// then take the packed atoms one at a time (w, w + 8, ...): for its atom a warp tests the QC atoms 32 at a time
+// in FP32, queues the ones inside the cutoff and evaluates the queue in FP64 thirty-two pairs at a time (as the
+// QC side does), so that no FP64 pass runs for a few lanes; lane partial sums are reduced in a fixed order.
 #define MB 256
 __global__ void __launch_bounds__(MB) k_qcmm_grad_mm(int model, Spline sp, int n_qc, int n_mm, const double *__restrict__ qc,
                                                      const double *__restrict__ mm, const double *__restrict__ q,
                                                      const double *__restrict__ qcq, double *__restrict__ gmm)
 {
     extern __shared__ double sq[];   // QC atoms: x, y, z, charge (doubles), then x, y, z (floats)
-    __shared__ int wcount[MB / 32], near_list[MB];
+    __shared__ int queue[MB / 32][64], wcount[MB / 32], near_list[MB];
     float *sf = (float *)(sq + 4 * (size_t)n_qc);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int blocks_per_frame = (n_mm + MB - 1) / MB;
-    const int f = blockIdx.x / blocks_per_frame, m = (blockIdx.x % blocks_per_frame) * MB + threadIdx.x;
+    const int f = blockIdx.x / blocks_per_frame, base = (blockIdx.x % blocks_per_frame) * MB;
     for (int k = threadIdx.x; k < n_qc; k += MB) {
         const double *x = qc + ((size_t)f * n_qc + k) * 3;
         sq[4 * k] = x[0]; sq[4 * k + 1] = x[1]; sq[4 * k + 2] = x[2]; sq[4 * k + 3] = qcq[(size_t)f * n_qc + k];
@@ -170,7 +172,8 @@ __global__ void __launch_bounds__(MB) k_qcmm_grad_mm(int model, Spline sp, int n
     __syncthreads();
     const float r2cut = cutoff_r2(model, sp);
     bool near = false;
-    if (m < n_mm) {
+    if (base + (int)threadIdx.x < n_mm) {
+        const int m = base + threadIdx.x;
         const double *xm = mm + ((size_t)f * n_mm + m) * 3;
         const float fx = (float)xm[0], fy = (float)xm[1], fz = (float)xm[2];
         for (int A = 0; A < n_qc && !near; A++) {
@@ -179,30 +182,54 @@ __global__ void __launch_bounds__(MB) k_qcmm_grad_mm(int model, Spline sp, int n
         }
         if (!near) { double *o = gmm + ((size_t)f * n_mm + m) * 3; o[0] = 0.0; o[1] = 0.0; o[2] = 0.0; }
     }
-    const unsigned bal = __ballot_sync(0xffffffffu, near);
-    if (lane == 0) wcount[w] = __popc(bal);
+    const unsigned nbal = __ballot_sync(0xffffffffu, near);
+    if (lane == 0) wcount[w] = __popc(nbal);
     __syncthreads();
     int off = 0, total = 0;
     for (int k = 0; k < MB / 32; k++) { if (k < w) off += wcount[k]; total += wcount[k]; }
-    if (near) near_list[off + __popc(bal & ((1u << lane) - 1u))] = m;
+    if (near) near_list[off + __popc(nbal & ((1u << lane) - 1u))] = base + threadIdx.x;
     __syncthreads();
-    if (threadIdx.x >= total) return;
-    const int mi = near_list[threadIdx.x];
-    const double *xm = mm + ((size_t)f * n_mm + mi) * 3;
-    const double mx = xm[0], my = xm[1], mz = xm[2], qm = q[mi];
-    const float fx = (float)mx, fy = (float)my, fz = (float)mz;
-    double g0 = 0.0, g1 = 0.0, g2 = 0.0;
-    for (int A = 0; A < n_qc; A++) {
-        const float ex = sf[3 * A] - fx, ey = sf[3 * A + 1] - fy, ez = sf[3 * A + 2] - fz;
-        if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > r2cut) continue;
-        const double dx = sq[4 * A] - mx, dy = sq[4 * A + 1] - my, dz = sq[4 * A + 2] - mz;
-        double fv, gv;
-        if (!pair_term(model, sp, dx * dx + dy * dy + dz * dz, &fv, &gv)) continue;
-        const double s = 2.0 * sq[4 * A + 3] * qm * gv / PDG_ANGSTROMS_TO_BOHRS;
-        g0 -= s * dx; g1 -= s * dy; g2 -= s * dz;
+    int *qw = queue[w];
+    for (int k = w; k < total; k += MB / 32) {
+        const int m = near_list[k];
+        const double *xm = mm + ((size_t)f * n_mm + m) * 3;
+        const double mx = xm[0], my = xm[1], mz = xm[2], qm = q[m];
+        const float fx = (float)mx, fy = (float)my, fz = (float)mz;
+        double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+        auto body = [&](int A) {
+            const double dx = sq[4 * A] - mx, dy = sq[4 * A + 1] - my, dz = sq[4 * A + 2] - mz;
+            double fv, gv;
+            if (!pair_term(model, sp, dx * dx + dy * dy + dz * dz, &fv, &gv)) return;
+            const double s = 2.0 * sq[4 * A + 3] * qm * gv / PDG_ANGSTROMS_TO_BOHRS;
+            g0 -= s * dx; g1 -= s * dy; g2 -= s * dz;
+        };
+        int qn = 0;
+        for (int A0 = 0; A0 < n_qc; A0 += 32) {
+            const int A = A0 + lane;
+            bool in = false;
+            if (A < n_qc) {
+                const float ex = sf[3 * A] - fx, ey = sf[3 * A + 1] - fy, ez = sf[3 * A + 2] - fz;
+                in = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= r2cut;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, in);
+            if (in) qw[qn + __popc(bal & ((1u << lane) - 1u))] = A;
+            qn += __popc(bal);
+            __syncwarp();
+            if (qn >= 32) {
+                body(qw[lane]);
+                const int rest = qn - 32;
+                const int carry = lane < rest ? qw[32 + lane] : 0;
+                __syncwarp();
+                if (lane < rest) qw[lane] = carry;
+                __syncwarp();
+                qn = rest;
+            }
+        }
+        if (lane < qn) body(qw[lane]);
+        __syncwarp();
+        g0 = warp_sum(g0); g1 = warp_sum(g1); g2 = warp_sum(g2);
+        if (lane == 0) { double *o = gmm + ((size_t)f * n_mm + m) * 3; o[0] = g0; o[1] = g1; o[2] = g2; }
     }
-    double *o = gmm + ((size_t)f * n_mm + mi) * 3;
-    o[0] = g0; o[1] = g1; o[2] = g2;
 }
 
 static Spline make_spline(int n, const double *knots, double cutoff)
