@@ -32,6 +32,7 @@ struct pdg_system {
     // device allocations owned by the system (tables only; no per-frame data)
     double *d_elements = nullptr, *d_terms = nullptr, *d_ovl = nullptr;
     int *d_ints = nullptr;
+    void *d_mp = nullptr;
 };
 
 extern "C" int pdg_version(void) { return 100; }
@@ -117,8 +118,12 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     ints.insert(ints.end(), pss.begin(), pss.end());
     ints.insert(ints.end(), pgen.begin(), pgen.end());
     ints.insert(ints.end(), psps.begin(), psps.end());
+    MultipoleMap mp;
+    if (!multipole_map_spsp(mp)) { pdg_system_destroy(s); return fail(PDG_BAD_ARGUMENT, "multipole map exceeds its term limit"); }
     int rc = PDG_OK;
-    if ((rc = cuda_check(cudaMalloc(&s->d_elements, sizeof(double) * s->elements.size()), "cudaMalloc elements")) ||
+    if ((rc = cuda_check(cudaMalloc(&s->d_mp, sizeof(MultipoleMap)), "cudaMalloc multipole map")) ||
+        (rc = cuda_check(cudaMemcpy(s->d_mp, &mp, sizeof(MultipoleMap), cudaMemcpyHostToDevice), "copy multipole map")) ||
+        (rc = cuda_check(cudaMalloc(&s->d_elements, sizeof(double) * s->elements.size()), "cudaMalloc elements")) ||
         (rc = cuda_check(cudaMalloc(&s->d_terms, sizeof(double) * terms.size()), "cudaMalloc terms")) ||
         (rc = cuda_check(cudaMalloc(&s->d_ints, sizeof(int) * ints.size()), "cudaMalloc tables")) ||
         (rc = cuda_check(cudaMalloc(&s->d_ovl, sizeof(double) * ovl.size()), "cudaMalloc overlap records")) ||
@@ -142,6 +147,7 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     d.cel = b + cel_at; d.xel = d.cel + cel.size(); d.n_cel = (int)cel.size(); d.n_xel = (int)xel.size();
     d.pairs_ss = b + pl_at; d.pairs_gen = d.pairs_ss + pss.size(); d.n_ss = (int)pss.size(); d.n_gen = (int)pgen.size();
     d.pairs_sps = d.pairs_gen + pgen.size(); d.n_sps = (int)psps.size();
+    d.mp_map = s->d_mp;
     *out = s;
     return PDG_OK;
 }
@@ -149,7 +155,7 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
 extern "C" int pdg_system_destroy(pdg_system *s)
 {
     if (!s) return PDG_OK;
-    cudaFree(s->d_elements); cudaFree(s->d_terms); cudaFree(s->d_ints); cudaFree(s->d_ovl);
+    cudaFree(s->d_elements); cudaFree(s->d_terms); cudaFree(s->d_ints); cudaFree(s->d_ovl); cudaFree(s->d_mp);
     delete s;
     return PDG_OK;
 }

@@ -37,6 +37,7 @@ struct DeviceSystem {
     int n_ss, n_gen;
     const int *pairs_sps;              // pairs of one sp and one s atom, in pair order
     int n_sps;
+    const void *mp_map;                // MultipoleMap of sp-sp pairs (multipole.cuh)
 };
 
 // Per-frame workspace plan (all offsets in doubles from the frame's base).

@@ -136,7 +136,16 @@ k_pair_integrals(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, con
         rot_assemble(q, false, rot);
         for (int k = lane; k < 100; k += 32) C[k] = ctrans(rot.T, k / 10, k % 10);
         __syncwarp();
-        if (lane == 0) multipole_combine(St, spi, spj, L, ci, cj);
+        {   // the local values as the sparse linear map of the terms, a few outputs per lane (L, ci, cj contiguous)
+            const MultipoleMap &mpm = *(const MultipoleMap *)s.mp_map;
+            for (int o = lane; o < mpm.n; o += 32) {
+                const int *tk = mpm.term + o * MP_MAP_NNZ;
+                const double *wk = mpm.w + o * MP_MAP_NNZ;
+                double v = 0.0;
+                for (int k = 0; k < mpm.nnz[o]; k++) v = fma(wk[k], St[tk[k]], v);
+                L[mpm.out[o]] = v;
+            }
+        }
         __syncwarp();
         // X = C_i L  (ni x nj),  TEI = X C_j^T (ni x nj)
         for (int k = lane; k < ni * nj; k += 32) {
@@ -490,8 +499,19 @@ k_pair_gradients(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, con
                 for (int xx = 0; xx < 3; xx++) CD[xx * 100 + k] = rot.active ? ctrans_d(rot.T, rot.D[xx], ab, mn) : 0.0;
             }
             __syncwarp();
-            if (lane == 0) multipole_combine(St, spi, spj, L, ci, cj);
-            if (lane == 1) multipole_combine(dSt, spi, spj, dL, dci, dcj);
+            {   // L, ci, cj and their r-derivatives as the sparse linear map of the terms, a few outputs per lane
+                const MultipoleMap &mpm = *(const MultipoleMap *)s.mp_map;
+                for (int o = lane; o < mpm.n; o += 32) {
+                    const int *tk = mpm.term + o * MP_MAP_NNZ;
+                    const double *wk = mpm.w + o * MP_MAP_NNZ;
+                    double v = 0.0, dv = 0.0;
+                    for (int k = 0; k < mpm.nnz[o]; k++) { v = fma(wk[k], St[tk[k]], v); dv = fma(wk[k], dSt[tk[k]], dv); }
+                    const int out = mpm.out[o];
+                    if (out < 100) { L[out] = v; dL[out] = dv; }
+                    else if (out < 110) { ci[out - 100] = v; dci[out - 100] = dv; }
+                    else { cj[out - 110] = v; dcj[out - 110] = dv; }
+                }
+            }
             __syncwarp();
             // W1 = L C_j^T, W2 = C_i L, W3 = dL C_j^T
             for (int k = lane; k < ni * nj; k += 32) {

@@ -82,7 +82,7 @@ inline void multipole_terms(const double *ei, const double *ej, double *o, doubl
 // Device: combine term values s (or their r-derivatives) into the local-frame TEI matrix L (10 x 10,
 // row = distribution on i, column = distribution on j) and the two electron-core vectors (before the
 // -Z scaling).  L, ci and cj must be zero on entry.  Formulas: MNDOIntegralUtilities.c:1130-1170,1198-1351.
-__device__ inline void multipole_combine(const double *s, bool spi, bool spj, double *L, double *ci, double *cj)
+__host__ __device__ inline void multipole_combine(const double *s, bool spi, bool spj, double *L, double *ci, double *cj)
 {
     const double E1 = 0.5, E2 = 0.25, E3 = 0.125, E4 = 0.0625;
     double ri0 = s[0];
@@ -142,6 +142,37 @@ __device__ inline void multipole_combine(const double *s, bool spi, bool spj, do
         double d1 = -E1 * (c[1] - c[2]), qz = E2 * (c[3] + c[4]) - E1 * c[5], qx = E1 * (c[6] - c[5]);
         cj[L_PZS] = d1; cj[L_PZPZ] = c[7] + qz; cj[L_PXPX] = c[7] + qx; cj[L_PYPY] = c[7] + qx;
     }
+}
+
+// multipole_combine of an sp-sp pair is linear in the term values: as a sparse map, output o (0-99 L,
+// 100-109 ci, 110-119 cj) = sum over at most MP_MAP_NNZ terms of weight * s[term].  Built once on the host
+// (by applying multipole_combine to unit vectors) so that the lanes of a warp each evaluate a few outputs.
+#define MP_MAP_NNZ 16
+#define MP_MAP_MAX 120
+struct MultipoleMap { int n; int out[MP_MAP_MAX], nnz[MP_MAP_MAX], term[MP_MAP_MAX * MP_MAP_NNZ]; double w[MP_MAP_MAX * MP_MAP_NNZ]; };
+
+inline bool multipole_map_spsp(MultipoleMap &m)
+{
+    double M[MP_MAP_MAX][MP_TERMS_USED] = {};
+    for (int k = 0; k < MP_TERMS_USED; k++) {
+        double sv[MP_NTERMS] = {}, L[100] = {}, ci[10] = {}, cj[10] = {};
+        sv[k] = 1.0;
+        multipole_combine(sv, true, true, L, ci, cj);
+        for (int o = 0; o < 100; o++) M[o][k] = L[o];
+        for (int o = 0; o < 10; o++) { M[100 + o][k] = ci[o]; M[110 + o][k] = cj[o]; }
+    }
+    m.n = 0;
+    for (int o = 0; o < MP_MAP_MAX; o++) {
+        int nz = 0;
+        for (int k = 0; k < MP_TERMS_USED; k++)
+            if (M[o][k] != 0.0) {
+                if (nz == MP_MAP_NNZ) return false;
+                m.term[m.n * MP_MAP_NNZ + nz] = k; m.w[m.n * MP_MAP_NNZ + nz] = M[o][k]; nz++;
+            }
+        if (nz == 0) continue;
+        m.out[m.n] = o; m.nnz[m.n] = nz; m.n++;
+    }
+    return true;
 }
 
 // Local-to-molecular rotation of the p shell and its derivatives with respect to the coordinates of
