@@ -288,6 +288,39 @@ int pdg_batch_graph_create(pdg_batch *batch, const double *d_xyz, const double *
 int pdg_graph_launch(pdg_graph *graph, void *stream);
 int pdg_graph_destroy(pdg_graph *graph);
 
+/* ---- Langevin dynamics of independent replicas (pCore-1.9.0/pCore/LangevinVelocityVerletIntegrator.py) ----
+ * The replicas are copies of one QC region in a fixed MM environment (System.DefineFixedAtoms on the MM atoms;
+ * this library has no MM force field).  Coordinates d_xyz: n_replicas x n_atoms x 3 (Angstrom, the QC atoms in
+ * the order the energy kernels take them); free atom f is atom d_free_atoms[f]; velocities and accelerations
+ * n_replicas x n_free x 3 in A/ps and A/ps^2.  factors = {facR1, facR2, facV1, facV2, sdR, sdV1, sdV2}, the
+ * integration constants of CalculateIntegrationConstants (:63-112; sdR, sdV1, sdV2 times
+ * sqrt(T / _AMUA2PS2_TO_K)), in the reference's mass-weighted units.
+ *   pdg_langevin_positions   the first half of Iteration (:126-137 and RandomForces :147-157): positions, half
+ *                            velocities, random forces from Philox4x32-10 normal deviates for (seed, element,
+ *                            step); d_deviates (NULL or n_replicas x n_free x 3 x 2) receives (w1, w2) per element.
+ *                            random = 0 applies no random forces.
+ *   pdg_langevin_velocities  the second half (:139-144): accelerations a = -100 grad_scale (g_a + g_b) / m from the
+ *                            gradients at the new point (rows d_grad_rows[f] of n_replicas x n_rows x 3 arrays;
+ *                            d_grad_b may be NULL; grad_scale converts them to kJ/mol/A), v += facV3 a, and per
+ *                            replica d_mv2 = sum m v^2 (amu A^2 ps^-2; NULL to skip), from which the host forms
+ *                            the kinetic energy and temperature (SystemGeometryObjectiveFunction.py:255-260). */
+int pdg_langevin_positions(int n_replicas, int n_atoms, int n_free, const int *d_free_atoms, const double *d_inv_sqrt_mass,
+                           double *d_xyz, double *d_velocities, const double *d_accelerations, const double *h_factors, int random,
+                           unsigned long long seed, unsigned int step, double *d_deviates, void *stream);
+int pdg_langevin_velocities(int n_replicas, int n_free, int n_rows, const int *d_grad_rows, const double *d_mass,
+                            const double *d_grad_a, const double *d_grad_b, double grad_scale, double facV3,
+                            double *d_velocities, double *d_accelerations, double *d_mv2, void *stream);
+/* n_pairs pairs of standard normal deviates for counters (pair index, step, stream_id) under key seed, the
+ * generator pdg_langevin_positions uses (stream_id 0); for tests and for velocity assignment. */
+int pdg_normal_deviates(long long n_pairs, unsigned long long seed, unsigned int step, unsigned int stream_id, double *d_out,
+                        void *stream);
+/* Start density of an SCF as a linear combination d_out = sum_k h_coefficients[k] d_terms[k] of up to 8 device
+ * arrays of n doubles (16-byte aligned): the previous step's density (the reference's warm start,
+ * pMolecule.QCModel.pyx:153), extrapolations over earlier steps, learned corrections.  No counterpart in the
+ * reference beyond the warm start. */
+int pdg_density_combine(long long n, int count, const double *const *h_terms, const double *h_coefficients, double *d_out,
+                        void *stream);
+
 /* Text of the last error on this host thread (never NULL). */
 const char *pdg_last_error(void);
 

@@ -2,15 +2,17 @@
 
 Public surface (mirroring pDynamo 1.9.0's names):
     QCModelMNDO, DIISSCFConverger, NBModelABFS, NBModelFull, System, ElectronicState
-and, beyond the reference, LearnedDensityGuess (System.DefineDensityGuess).
+LangevinDynamics_SystemGeometry (Langevin dynamics of the QC atoms with the MM atoms fixed), and, beyond the
+reference, LearnedDensityGuess (System.DefineDensityGuess) and LangevinDynamics (many replicas at once).
 The compute path is libpdg.so (CUDA, include/pdg.h); nothing here computes on the CPU.
 """
 
 from .batch import MoleculeBatch
 from .converger import DIISSCFConverger
+from .dynamics import LangevinDynamics, LangevinDynamics_SystemGeometry, LangevinVelocityVerletIntegrator
 from .guess import LearnedDensityGuess
 from .nbmodel import NBModelABFS, NBModelFull
 from .qcmodel import QCModelMNDO
 from .system import ElectronicState, SCFNotConverged, System
 
-__all__ = ["DIISSCFConverger", "MoleculeBatch", "ElectronicState", "LearnedDensityGuess", "NBModelABFS", "NBModelFull", "QCModelMNDO", "SCFNotConverged", "System"]
+__all__ = ["DIISSCFConverger", "LangevinDynamics", "LangevinDynamics_SystemGeometry", "LangevinVelocityVerletIntegrator", "MoleculeBatch", "ElectronicState", "LearnedDensityGuess", "NBModelABFS", "NBModelFull", "QCModelMNDO", "SCFNotConverged", "System"]

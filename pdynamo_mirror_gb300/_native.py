@@ -19,7 +19,8 @@ EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system
            "pdg_qcmm_gradients", "pdg_scf_timings", "pdg_gradients_static_scratch", "pdg_tc_selftest", "pdg_scf_occupancy", "pdg_guess_features", "pdg_mlp_forward",
            "pdg_mlp_backward", "pdg_mlp_adam", "pdg_guess_assemble", "pdg_guess_loss", "pdg_batch_create", "pdg_batch_destroy",
            "pdg_batch_info", "pdg_batch_workspace_bytes", "pdg_batch_schedule", "pdg_batch_energy_gradients", "pdg_batch_timings",
-           "pdg_batch_graph_create", "pdg_graph_launch", "pdg_graph_destroy", "pdg_last_error")
+           "pdg_batch_graph_create", "pdg_graph_launch", "pdg_graph_destroy", "pdg_langevin_positions", "pdg_langevin_velocities",
+           "pdg_normal_deviates", "pdg_density_combine", "pdg_last_error")
 TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densities Tridiagonal", "QC Densities Eigenvalues",
           "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds",
           "QC Densities Cluster Rounds", "QC Densities Steps", "QC Densities Purification",
@@ -89,6 +90,11 @@ def load(path=LIB_PATH):
     L.pdg_batch_timings.argtypes = [P, P, S, P, P]
     L.pdg_graph_launch.argtypes = [P, P]
     L.pdg_graph_destroy.argtypes = [P]
+    U32, U64 = ctypes.c_uint, ctypes.c_ulonglong
+    L.pdg_langevin_positions.argtypes = [I, I, I, P, P, P, P, P, P, I, U64, U32, P, P]
+    L.pdg_langevin_velocities.argtypes = [I, I, I, P, P, P, P, D, D, P, P, P, P]
+    L.pdg_normal_deviates.argtypes = [LL, U64, U32, U32, P, P]
+    L.pdg_density_combine.argtypes = [LL, I, P, P, P, P]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype or I
     _lib = L

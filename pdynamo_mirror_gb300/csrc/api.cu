@@ -664,3 +664,57 @@ extern "C" int pdg_guess_loss(pdg_system *s, int n_frames, const double *d_xyz, 
     launch_guess_loss(s->d, n_frames, d_xyz, d_offsets, d_row_pair, d_density, d_target, d_dy, d_loss, (cudaStream_t)stream);
     return cuda_check(cudaGetLastError(), "guess loss kernel");
 }
+
+// ---- Langevin dynamics and density combinations (dynamics.cu)
+extern "C" int pdg_langevin_positions(int n_replicas, int n_atoms, int n_free, const int *d_free_atoms, const double *d_inv_sqrt_mass,
+                                      double *d_xyz, double *d_velocities, const double *d_accelerations, const double *h_factors,
+                                      int random, unsigned long long seed, unsigned int step, double *d_deviates, void *stream)
+{
+    if (n_replicas <= 0 || n_atoms <= 0 || n_free <= 0 || n_free > n_atoms || !d_free_atoms || !d_inv_sqrt_mass || !d_xyz ||
+        !d_velocities || !d_accelerations || !h_factors)
+        return fail(PDG_BAD_ARGUMENT, "pdg_langevin_positions: bad argument");
+    LangevinFactors f;
+    f.facR1 = h_factors[0]; f.facR2 = h_factors[1]; f.facV1 = h_factors[2]; f.facV2 = h_factors[3];
+    f.sdR = h_factors[4]; f.sdV1 = h_factors[5]; f.sdV2 = h_factors[6];
+    f.random = random ? 1 : 0;
+    launch_langevin_positions(n_replicas, n_atoms, n_free, d_free_atoms, d_inv_sqrt_mass, d_xyz, d_velocities, d_accelerations, f,
+                              (uint64_t)seed, (uint32_t)step, d_deviates, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "langevin positions kernel");
+}
+
+extern "C" int pdg_langevin_velocities(int n_replicas, int n_free, int n_rows, const int *d_grad_rows, const double *d_mass,
+                                       const double *d_grad_a, const double *d_grad_b, double grad_scale, double facV3,
+                                       double *d_velocities, double *d_accelerations, double *d_mv2, void *stream)
+{
+    if (n_replicas <= 0 || n_free <= 0 || n_rows <= 0 || !d_grad_rows || !d_mass || !d_grad_a || !d_velocities || !d_accelerations)
+        return fail(PDG_BAD_ARGUMENT, "pdg_langevin_velocities: bad argument");
+    launch_langevin_velocities(n_replicas, n_free, n_rows, d_grad_rows, d_mass, d_grad_a, d_grad_b, grad_scale, facV3, d_velocities,
+                               d_accelerations, d_mv2, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "langevin velocities kernel");
+}
+
+extern "C" int pdg_normal_deviates(long long n_pairs, unsigned long long seed, unsigned int step, unsigned int stream_id, double *d_out,
+                                   void *stream)
+{
+    if (n_pairs <= 0 || !d_out) return fail(PDG_BAD_ARGUMENT, "pdg_normal_deviates: bad argument");
+    launch_normal_deviates(n_pairs, (uint64_t)seed, (uint32_t)step, (uint32_t)stream_id, d_out, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "normal deviates kernel");
+}
+
+extern "C" int pdg_density_combine(long long n, int count, const double *const *h_terms, const double *h_coefficients, double *d_out,
+                                   void *stream)
+{
+    if (n <= 0 || count < 1 || count > PDG_MAX_DENSITY_TERMS || !h_terms || !h_coefficients || !d_out)
+        return fail(PDG_BAD_ARGUMENT, "pdg_density_combine: bad argument");
+    DensityTerms t;
+    t.count = count;
+    if (reinterpret_cast<uintptr_t>(d_out) % 16) return fail(PDG_BAD_ARGUMENT, "pdg_density_combine: output not 16-byte aligned");
+    for (int k = 0; k < count; k++) {
+        if (!h_terms[k] || reinterpret_cast<uintptr_t>(h_terms[k]) % 16)
+            return fail(PDG_BAD_ARGUMENT, "pdg_density_combine: term missing or not 16-byte aligned");
+        t.d[k] = h_terms[k];
+        t.c[k] = h_coefficients[k];
+    }
+    launch_density_combine(n, t, d_out, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "density combination kernel");
+}

@@ -234,3 +234,25 @@ void launch_guess_assemble(const DeviceSystem &s, int n_frames, const double *xy
                            const float *Y, double *P, cudaStream_t st);
 void launch_guess_loss(const DeviceSystem &s, int n_frames, const double *xyz, const int *offsets, const int *row_pair, const double *P,
                        const double *Ptarget, float *dY, double *loss, cudaStream_t st);
+
+// Langevin dynamics (dynamics.cu).  Integration factors of LangevinVelocityVerletIntegrator
+// (pCore-1.9.0/pCore/LangevinVelocityVerletIntegrator.py:63-112), computed on the host; sdR, sdV1, sdV2 already
+// carry the temperature factor.
+struct LangevinFactors {
+    double facR1, facR2, facV1, facV2, sdR, sdV1, sdV2;
+    int random;   // 0: no random forces (plain velocity Verlet with friction), for tests
+};
+#define PDG_MAX_DENSITY_TERMS 8
+struct DensityTerms {
+    const double *d[PDG_MAX_DENSITY_TERMS];
+    double c[PDG_MAX_DENSITY_TERMS];
+    int count;
+};
+void launch_langevin_positions(int n_replicas, int n_atoms, int n_free, const int *free_atom, const double *inv_sqrt_mass, double *xyz,
+                               double *vel, const double *acc, const LangevinFactors &f, uint64_t seed, uint32_t step,
+                               double *deviates, cudaStream_t st);
+void launch_langevin_velocities(int n_replicas, int n_free, int n_rows, const int *grad_row, const double *mass, const double *grad_a,
+                                const double *grad_b, double grad_scale, double facV3, double *vel, double *acc, double *mv2,
+                                cudaStream_t st);
+void launch_density_combine(long long n, const DensityTerms &t, double *out, cudaStream_t st);
+void launch_normal_deviates(long long n_pairs, uint64_t seed, uint32_t step, uint32_t stream, double *out, cudaStream_t st);

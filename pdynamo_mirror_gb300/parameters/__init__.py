@@ -48,6 +48,14 @@ def table():
     return _TABLE
 
 
+def atomic_mass(atomic_number):
+    """Mass (amu) of an element, from pDynamo's element files (parameters/elements/<El>.yaml, "Mass")."""
+    m = table().get("masses", {}).get(str(int(atomic_number)))
+    if m is None or m <= 0.0:
+        raise ValueError("No mass for atomic number %d." % int(atomic_number))
+    return float(m)
+
+
 def available_elements(hamiltonian):
     return sorted(int(z) for z in table()["hamiltonians"][hamiltonian.lower()])
 

@@ -67,6 +67,22 @@ def read_basis(path):
     return shells
 
 
+def read_masses(folder):
+    """Atomic masses (amu) by atomic number from the element files (``Atomic Number`` and ``Mass`` lines):
+    the masses pDynamo's dynamics weights the coordinates with (SystemGeometryObjectiveFunction.py:106-120)."""
+    masses = {}
+    for fname in sorted(os.listdir(folder)):
+        if not fname.endswith(".yaml"): continue
+        z = m = None
+        for line in open(os.path.join(folder, fname)):
+            key, _, value = line.partition(":")
+            if key.strip() == "Atomic Number": z = int(value)
+            elif key.strip() == "Mass": m = float(value)
+        if z is not None and m is not None:
+            masses[str(z)] = m
+    return masses
+
+
 def main(root, output):
     base = os.path.join(root, "parameters", "mndoParameters")
     data = {"source": "pDynamo-1.9.0 parameters/mndoParameters", "hamiltonians": {}, "bases": {}}
@@ -88,6 +104,7 @@ def main(root, output):
         path = os.path.join(base, "mndostong", lab + ".yaml")
         if os.path.exists(path):  # pDynamo ships no 6s6p shells, so those elements cannot be set up there either
             data["bases"][lab] = read_basis(path)
+    data["masses"] = read_masses(os.path.join(root, "parameters", "elements"))
     with open(output, "w") as f:
         json.dump(data, f, indent=0, sort_keys=True)
 

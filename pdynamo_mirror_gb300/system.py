@@ -48,6 +48,7 @@ class System:
         self.configuration = Configuration()
         self._engine = None
         self.densityGuess = None
+        self.fixedAtoms = None
 
     # -- model definition (System.py:182-230)
     def DefineQCModel(self, qcModel, qcSelection=None):
@@ -67,6 +68,16 @@ class System:
         if mm and self.mmCharges is None:
             raise ValueError("MM atoms need point charges.")
         self.nbModel = nbModel
+
+    def DefineFixedAtoms(self, selection):
+        """Atoms that dynamics leaves in place (System.py:142-160; None clears them)."""
+        if selection is None:
+            self.fixedAtoms = None
+            return
+        sel = sorted(set(int(i) for i in selection))
+        if sel and (sel[0] < 0 or sel[-1] >= len(self.atomicNumbers)):
+            raise ValueError("Invalid fixed-atom selection.")
+        self.fixedAtoms = sel
 
     def DefineDensityGuess(self, guess):
         """Start cold SCFs from a LearnedDensityGuess (None: the diagonal guess).  Not in the reference."""
