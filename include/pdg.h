@@ -173,7 +173,7 @@ int pdg_gradients_static_scratch(pdg_system *sys, int n_frames, const double *d_
  * timings of pMolecule.QCModel.pyx:208-275 (EnergyWithTimings: QC Fock, QC Converger Iterate,
  * QC Converger Densities), with the density step split into its parts.  d_out: n_frames * PDG_NTIMERS. */
 #define PDG_RMS_HISTORY 40
-#define PDG_NTIMERS (18 + PDG_RMS_HISTORY)
+#define PDG_NTIMERS (23 + PDG_RMS_HISTORY)
 enum {
     PDG_T_FOCK = 0, PDG_T_DIIS_SAVE = 1, PDG_T_ITERATE = 2, PDG_T_TRIDIAGONAL = 3, PDG_T_EIGENVALUES = 4,
     PDG_T_EIGENVECTORS = 5, PDG_T_BACKTRANSFORM = 6, PDG_T_DENSITY = 7, PDG_T_TOTAL = 8, PDG_T_CYCLES = 9,
@@ -185,7 +185,12 @@ enum {
     PDG_T_SM_ID = 15,          /* the SM that ran the frame's CTA */
     PDG_T_START_NS = 16,       /* %globaltimer at the CTA's start and end (ns) */
     PDG_T_END_NS = 17,
-    PDG_T_RMS_HISTORY = 18     /* PDG_RMS_HISTORY entries: RMS density change of each density step, in SCF cycle
+    PDG_T_PUR_PRODUCTS = 18,   /* parts of PDG_T_PURIFICATION: tensor-core products from issue to completion, */
+    PDG_T_PUR_READOUT = 19,    /* the readout that forms the next iterate and its BF16 parts, */
+    PDG_T_PUR_CONTROL = 20,    /* traces and the SP2 step choice, */
+    PDG_T_PUR_SETUP = 21,      /* spectral bounds and the parts of the first iterate, */
+    PDG_T_PUR_FINISH = 22,     /* and the density from the last iterate */
+    PDG_T_RMS_HISTORY = 23     /* PDG_RMS_HISTORY entries: RMS density change of each density step, in SCF cycle
                                   order, negative for purification steps, 0 beyond the last */
 };
 int pdg_scf_timings(const pdg_system *sys, int n_frames, const void *d_workspace, size_t workspace_bytes,

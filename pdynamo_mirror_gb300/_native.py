@@ -24,7 +24,9 @@ EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system
 TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densities Tridiagonal", "QC Densities Eigenvalues",
           "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds",
           "QC Densities Cluster Rounds", "QC Densities Steps", "QC Densities Purification",
-          "QC Densities Purification Steps", "QC Densities SP2 Iterations", "SM", "Start ns", "End ns") + tuple("RMS %d" % k for k in range(40))
+          "QC Densities Purification Steps", "QC Densities SP2 Iterations", "SM", "Start ns", "End ns", "QC Densities Purification Products",
+          "QC Densities Purification Readout", "QC Densities Purification Control", "QC Densities Purification Setup",
+          "QC Densities Purification Finish") + tuple("RMS %d" % k for k in range(40))
 
 
 class SCFOptions(ctypes.Structure):

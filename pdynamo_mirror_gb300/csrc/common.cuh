@@ -170,6 +170,19 @@ __device__ __forceinline__ double block_sum(double v, double *red)
     __syncthreads();
     return t;
 }
+// Two block-wide sums at once (the same per-value summation order as block_sum); red must hold 32 doubles.
+__device__ __forceinline__ double2 block_sum2(double a, double b, double *red)
+{
+    a = warp_sum(a); b = warp_sum(b);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (l == 0) { red[w] = a; red[16 + w] = b; }
+    __syncthreads();
+    double s = 0.0, t = 0.0;
+    for (int i = 0; i < nw; i++) { s += red[i]; t += red[16 + i]; }
+    __syncthreads();
+    return make_double2(s, t);
+}
 __device__ __forceinline__ double block_max(double v, double *red)
 {
     v = warp_max(v);

@@ -316,10 +316,14 @@ __device__ int sturm_count32(int N, const float *d, const float *e2, float x, fl
 
 // Phase timers: thread 0 accumulates clock64() deltas between block-wide barriers into the frame's
 // timer slots (workspace misc area, after the DIIS B matrix).
+static_assert(PDG_NTIMERS <= 64, "timer slots live in the 64 doubles after the DIIS B matrix");
 struct Timer {
     double *slot; long long t;
     __device__ void start() { if (threadIdx.x == 0) t = clock64(); }
     __device__ void lap(int k) { if (threadIdx.x == 0) { long long n = clock64(); slot[k] += (double)(n - t); t = n; } }
+    // a sub-phase inside a lapped phase: adds the cycles since t0 to slot k without moving the lap origin
+    __device__ long long now() const { return clock64(); }
+    __device__ void add(int k, long long t0) { if (threadIdx.x == 0) slot[k] += (double)(clock64() - t0); }
 };
 
 // Packed lower-triangle element (i >= j) of the matrix being tridiagonalised.
@@ -685,6 +689,14 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
 // out (P is then left unchanged).
 struct TCState { uint32_t tmem, bar, phase; };
 
+// Sum of the BF16 parts of eight consecutive iterate elements (16 bytes of each part array).
+__device__ __forceinline__ void bf16_sum8(const uint4 &a, const uint4 &b, const uint4 &c, float *x)
+{
+    const __nv_bfloat16 *pa = (const __nv_bfloat16 *)&a, *pb = (const __nv_bfloat16 *)&b, *pc = (const __nv_bfloat16 *)&c;
+#pragma unroll
+    for (int j = 0; j < 8; j++) x[j] = __bfloat162float(pa[j]) + __bfloat162float(pb[j]) + __bfloat162float(pc[j]);
+}
+
 __device__ double density_step_mixed(const SCFArgs &a, double *wsf, const double *F, double *P, Smem &sm, Timer &tm,
                                      TCState &tc, int kprod)
 {
@@ -692,9 +704,17 @@ __device__ double density_step_mixed(const SCFArgs &a, double *wsf, const double
     const int N = s.n_basis, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int Kp = (N + 15) & ~15, R = Kp > TC_M ? Kp : TC_M, m2 = Kp - TC_M;   // second tile: rows m2 .. m2+127
     const size_t NN4 = ((size_t)N * N + 3) & ~size_t(3);
-    float *Xa = (float *)(wsf + a.plan.A), *Xb = Xa + NN4, *P32 = Xb + NN4;
+    // The iterate X lives only as its BF16 parts hi + mid + lo (24 significant bits, the FP32 value): hi and mid in
+    // shared memory as the tensor-core operands, lo in the workspace region LO.  With 6 partial products the second
+    // product phase copies lo over mid in shared memory, so mid is also kept in the workspace (region A).
+    float *P32 = (float *)(wsf + a.plan.A) + 2 * NN4;
     unsigned char *ph = (unsigned char *)sm.amat, *pm = ph + (size_t)R * Kp * 2;
+    unsigned char *plo_g = (unsigned char *)(wsf + a.plan.LO), *pmid_g = (unsigned char *)(wsf + a.plan.A);
+    // the part of the current iterate outside shared memory at readout time (shared memory then holds hi and
+    // either mid (3 products) or lo (6 products))
+    const unsigned char *third = kprod == 6 ? pmid_g : plo_g;
     const double nocc = (double)s.n_occ;
+    const long long t_setup = tm.now();
     // Gershgorin bounds and X0 = (e_max - F) / (e_max - e_min)
     double lo = 1e300, hi = -1e300;
     for (int i = w; i < N; i += PDG_WARPS) {
@@ -706,31 +726,29 @@ __device__ double density_step_mixed(const SCFArgs &a, double *wsf, const double
     }
     lo = -block_max(-lo, sm.red); hi = block_max(hi, sm.red);
     const float scale = (float)(1.0 / fmax(hi - lo, 1e-12)), fhi = (float)hi;
+    // BF16 parts of X0 (rows beyond N and the padding zero), its trace and squared norm; later iterates get their
+    // parts from the readout
     float trl = 0.0f, sql = 0.0f;
-    for (int e = tid; e < N * N; e += PDG_BLOCK) {
-        const int i = e / N, j = e % N;
-        const float x = ((i == j ? fhi : 0.0f) - (float)F[e]) * scale;
-        Xa[e] = x;
-        trl += (i == j) ? x : 0.0f; sql = fmaf(x, x, sql);
-    }
-    double tr = block_sum((double)trl, sm.red), sq = block_sum((double)sql, sm.red);
-    double defect_1 = 1e300, defect_2 = 1e300;   // defects of the last two iterations
-    const int rr = 32 * (w & 3) + lane, nch = Kp / 16, half = (nch + 1) / 2, c0 = w < 4 ? 0 : half, c1 = w < 4 ? half : nch;
-    unsigned char *plo_g = (unsigned char *)(wsf + a.plan.LO);   // BF16 lo parts (global), copied in for phase 2
-    // BF16 parts of X0 (rows beyond N and the padding zero); later iterates get theirs from the readout
     for (int e = tid; e < R * Kp; e += PDG_BLOCK) {
         const int r = e / Kp, c = e % Kp;
-        const float x = (r < N && c < N) ? Xa[(size_t)r * N + c] : 0.0f;
+        const float x = (r < N && c < N) ? ((r == c ? fhi : 0.0f) - (float)F[(size_t)r * N + c]) * scale : 0.0f;
+        trl += (r == c) ? x : 0.0f; sql = fmaf(x, x, sql);
         __nv_bfloat16 h, m, l;
         bf16_split3(x, h, m, l);
         const uint32_t o = tc_offset(r, c, Kp);
         *(__nv_bfloat16 *)(ph + o) = h;
         *(__nv_bfloat16 *)(pm + o) = m;
         *(__nv_bfloat16 *)(plo_g + o) = l;
+        if (kprod == 6) *(__nv_bfloat16 *)(pmid_g + o) = m;
     }
-    float *X = Xa, *Xn = Xb;
+    const double2 ts = block_sum2((double)trl, (double)sql, sm.red);
+    double tr = ts.x, sq = ts.y;
+    tm.add(PDG_T_PUR_SETUP, t_setup);
+    double defect_1 = 1e300, defect_2 = 1e300;   // defects of the last two iterations
+    const int rr = 32 * (w & 3) + lane, nch = Kp / 16, half = (nch + 1) / 2, c0 = w < 4 ? 0 : half, c1 = w < 4 ? half : nch;
     for (int it = 0; it < 100; it++) {
         const bool square = fabs(sq - nocc) < fabs(2.0 * tr - sq - nocc);   // X <- X^2, else 2X - X^2
+        const long long t_products = tm.now();
         tc_fence_proxy();
         tc_fence_before();
         __syncthreads();
@@ -776,27 +794,32 @@ __device__ double density_step_mixed(const SCFArgs &a, double *wsf, const double
         }
         if (__syncthreads_or(!ok)) return -1.0;
         tc_fence_after();
-        // X <- X X or 2X - X X.  X is symmetric up to rounding, so the new matrix is stored transposed:
-        // thread (row r) writes Xn[c][r] and reads the old X[c][r], both coalesced across the warp; the
-        // columns >= 128 of tile 1 also give rows >= 128 (Xn[r][c]), and tile 2's last lanes the corner.
-        // The same thread writes the BF16 parts of the next iterate: row r, eight columns per 16-byte store
-        // (the products are complete, so the operand arrays are free); rows >= 128 from the mirror and the
-        // corner, one element at a time; padding columns as zeros.
+        tm.add(PDG_T_PUR_PRODUCTS, t_products);
+        const long long t_readout = tm.now();
+        // X <- X X or 2X - X X.  Thread (row r) reads its 16 product columns from tensor memory and, for 2X - X X,
+        // the old X of the same elements as the sum of its parts (16-byte loads per 8 columns); then writes the
+        // new parts in place (the products are complete, so the operand arrays are free; each element is read
+        // and written by the same thread).  X X is symmetric: tile 1's columns >= 128 also give rows >= 128 (the
+        // mirror, one element at a time) and tile 2's last lanes the corner; padding columns stay zero.
         float trn = 0.0f, sqn = 0.0f;
         for (int ch = c0; ch < c1; ch++) {
             float v[16];
             tc_ld16(tc.tmem + ((uint32_t)(32 * (w & 3)) << 16) + (uint32_t)(ch * 16), v);
             if (rr < N) {
                 float xv[16];
+                if (!square) {
+#pragma unroll
+                    for (int g = 0; g < 2; g++) {
+                        const uint32_t o = tc_offset(rr, ch * 16 + 8 * g, Kp);
+                        const uint4 pc = *(const uint4 *)(third + o), pa = *(const uint4 *)(ph + o), pb = *(const uint4 *)(pm + o);
+                        bf16_sum8(pa, pb, pc, xv + 8 * g);
+                    }
+                }
 #pragma unroll
                 for (int j = 0; j < 16; j++) {
                     const int c = ch * 16 + j;
-                    xv[j] = 0.0f;
-                    if (c >= N) continue;
-                    const float xo = X[(size_t)c * N + rr], xn = square ? v[j] : 2.0f * xo - v[j];
+                    const float xn = c >= N ? 0.0f : (square ? v[j] : 2.0f * xv[j] - v[j]);
                     xv[j] = xn;
-                    Xn[(size_t)c * N + rr] = xn;
-                    if (c >= TC_M) Xn[(size_t)rr * N + c] = xn;
                     sqn = fmaf((c >= TC_M) ? 2.0f * xn : xn, xn, sqn);
                     if (c == rr) trn += xn;
                 }
@@ -808,7 +831,8 @@ __device__ double density_step_mixed(const SCFArgs &a, double *wsf, const double
                     const uint32_t o = tc_offset(rr, ch * 16 + 8 * g, Kp);
                     *(uint4 *)(ph + o) = *(const uint4 *)hv;
                     *(uint4 *)(pm + o) = *(const uint4 *)mv;
-                    if (kprod == 6) *(uint4 *)(plo_g + o) = *(const uint4 *)lv;
+                    *(uint4 *)(plo_g + o) = *(const uint4 *)lv;
+                    if (kprod == 6) *(uint4 *)(pmid_g + o) = *(const uint4 *)mv;
                 }
 #pragma unroll
                 for (int j = 0; j < 16; j++) {   // rows >= 128 of the operands: the mirror (c, r)
@@ -819,7 +843,8 @@ __device__ double density_step_mixed(const SCFArgs &a, double *wsf, const double
                     const uint32_t o = tc_offset(c, rr, Kp);
                     *(__nv_bfloat16 *)(ph + o) = h;
                     *(__nv_bfloat16 *)(pm + o) = m;
-                    if (kprod == 6) *(__nv_bfloat16 *)(plo_g + o) = l;
+                    *(__nv_bfloat16 *)(plo_g + o) = l;
+                    if (kprod == 6) *(__nv_bfloat16 *)(pmid_g + o) = m;
                 }
             }
         }
@@ -831,22 +856,29 @@ __device__ double density_step_mixed(const SCFArgs &a, double *wsf, const double
                 for (int j = 0; j < m2 && j < 16; j++) {
                     const int c = TC_M + j;
                     if (c >= N) continue;
-                    const float xo = X[(size_t)c * N + r], xn = square ? v[j] : 2.0f * xo - v[j];
-                    Xn[(size_t)c * N + r] = xn;
+                    const uint32_t o = tc_offset(r, c, Kp);
+                    float xn = v[j];
+                    if (!square) {
+                        const float xo = __bfloat162float(*(const __nv_bfloat16 *)(ph + o)) + __bfloat162float(*(const __nv_bfloat16 *)(pm + o))
+                                       + __bfloat162float(*(const __nv_bfloat16 *)(third + o));
+                        xn = 2.0f * xo - v[j];
+                    }
                     sqn = fmaf(xn, xn, sqn);
                     if (c == r) trn += xn;
                     __nv_bfloat16 h, m, l;
                     bf16_split3(xn, h, m, l);
-                    const uint32_t o = tc_offset(r, c, Kp);
                     *(__nv_bfloat16 *)(ph + o) = h;
                     *(__nv_bfloat16 *)(pm + o) = m;
-                    if (kprod == 6) *(__nv_bfloat16 *)(plo_g + o) = l;
+                    *(__nv_bfloat16 *)(plo_g + o) = l;
+                    if (kprod == 6) *(__nv_bfloat16 *)(pmid_g + o) = m;
                 }
             }
         }
         tc_fence_before();
-        tr = block_sum((double)trn, sm.red); sq = block_sum((double)sqn, sm.red);
-        float *tmp = X; X = Xn; Xn = tmp;
+        tm.add(PDG_T_PUR_READOUT, t_readout);
+        const long long t_control = tm.now();
+        const double2 tsn = block_sum2((double)trn, (double)sqn, sm.red);
+        tr = tsn.x; sq = tsn.y;
         const double defect = tr - sq;   // sum of lambda (1 - lambda) over the spectrum
         if (tid == 0) tm.slot[PDG_T_SP2_ITERATIONS] += 1.0;
         // converged (after Kruchinina, Rudberg and Rubensson's criterion for SP2): in the asymptotic regime the
@@ -855,24 +887,50 @@ __device__ double density_step_mixed(const SCFArgs &a, double *wsf, const double
         // within the products' precision of 0 or 1 (defect below 1e-3 for 3 partial products, 1e-5 for 6):
         // before that, a nearly degenerate HOMO/LUMO pair separating slowly around 1/2 also stalls the defect.
         const double floor_defect = kprod == 6 ? 1e-5 : 1e-3;
+        tm.add(PDG_T_PUR_CONTROL, t_control);
         if ((defect < floor_defect && defect >= defect_2) || defect < 1e-9 * nocc || it >= 80) break;
         defect_2 = defect_1; defect_1 = defect;
     }
+    // P = X + X^T from the parts of the last iterate (hi and mid in shared memory, lo in the workspace), in FP64
+    // for the SCF and in FP32 (N x round4(N)) for the commutator of the next DIIS save
+    const long long t_finish = tm.now();
     double rms = 0.0;
     const int N4 = (N + 3) & ~3;
-    for (int e = tid; e < N * N; e += PDG_BLOCK) {
-        const int i = e / N, j = e % N;
-        const float p32 = X[(size_t)i * N + j] + X[(size_t)j * N + i];
-        P32[(size_t)i * N4 + j] = p32;
-        if (j == 0) for (int q = N; q < N4; q++) P32[(size_t)i * N4 + q] = 0.0f;
-        if (j > i) continue;
-        const double pn = (double)X[(size_t)i * N + j] + (double)X[(size_t)j * N + i];
-        const double dlt = pn - P[e];
-        rms += (i == j) ? dlt * dlt : 2.0 * dlt * dlt;
-        P[e] = pn;
-        if (i != j) P[(size_t)j * N + i] = pn;
+    auto xval = [&](int i, int j) {
+        const uint32_t o = tc_offset(i, j, Kp);
+        return __bfloat162float(*(const __nv_bfloat16 *)(ph + o)) + __bfloat162float(*(const __nv_bfloat16 *)(pm + o))
+             + __bfloat162float(*(const __nv_bfloat16 *)(plo_g + o));
+    };
+    const int npk = N * (N + 1) / 2;
+    for (int q0 = tid; q0 < npk; q0 += 2 * PDG_BLOCK) {
+        int ii[2], jj[2];
+        float xij[2], xji[2];
+        double po[2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {   // element (i >= j) of packed index q; its loads issued before any store
+            const int q = q0 + u * PDG_BLOCK;
+            int i = (int)((sqrtf(8.0f * (float)q + 1.0f) - 1.0f) * 0.5f);
+            while ((i + 1) * (i + 2) / 2 <= q) i++;
+            while (i * (i + 1) / 2 > q) i--;
+            ii[u] = i; jj[u] = q - i * (i + 1) / 2;
+            if (q < npk) { xij[u] = xval(i, jj[u]); xji[u] = xval(jj[u], i); po[u] = P[(size_t)i * N + jj[u]]; }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            if (q0 + u * PDG_BLOCK >= npk) continue;
+            const int i = ii[u], j = jj[u];
+            const float p32 = xij[u] + xji[u];
+            const double pn = (double)xij[u] + (double)xji[u], dlt = pn - po[u];
+            rms += (i == j) ? dlt * dlt : 2.0 * dlt * dlt;
+            P[(size_t)i * N + j] = pn;
+            P[(size_t)j * N + i] = pn;
+            P32[(size_t)i * N4 + j] = p32;
+            P32[(size_t)j * N4 + i] = p32;
+        }
     }
+    for (int e = tid; e < N * (N4 - N); e += PDG_BLOCK) P32[(size_t)(e / (N4 - N)) * N4 + N + e % (N4 - N)] = 0.0f;
     const double out = sqrt(block_sum(rms, sm.red)) / (double)N;
+    tm.add(PDG_T_PUR_FINISH, t_finish);
     if (tid == 0) tm.slot[PDG_T_PURIFICATION_STEPS] += 1.0;
     tm.lap(PDG_T_PURIFICATION);
     return out;
@@ -956,7 +1014,15 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
     __syncthreads();
     int ncyc = 0;
     bool have_z = false;   // P is the density of the vectors in Z
+    // Mixed method: the Fock matrix of the last FP64 density step (the extrapolated one, still in F when the loop
+    // comes round), kept so that the next DIIS save can form its commutator from the small difference F - F~
+    double *Ft = wsf + pl.A;
+    const bool delta_commutator = o.density_step != 0;
     while (iteration < o.maximum_scf_cycles && !converged) {
+        if (delta_commutator && have_z) {
+            for (size_t k = tid; k < NN; k += PDG_BLOCK) Ft[k] = F[k];
+            __syncthreads();
+        }
         fock_build(a, f, H, P, F, tei, sm, &e1, &e2, &eq);
         tm.lap(PDG_T_FOCK);
         ncyc++;
@@ -985,18 +1051,32 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
                 const double *Zc = sm.zs ? sm.zs : wsf + pl.Z;
                 const int ldz = sm.ldz, kv = s.n_vec;
                 const double sg = s.vec_occupied ? 2.0 : -2.0;
-                double *G = wsf + pl.G;
-                tgemm<true, false>(kv, N, N, [&](int t, int k) { return Zc[(size_t)t * ldz + k]; }, [&](int k, int i) { return F[(size_t)k * N + i]; },
-                                   false, sm, [&](int t, int i, double v) { G[(size_t)t * N + i] = v; });
-                tgemm<false, false>(N, N, 2 * kv,
-                    [&](int i, int k) { return k < kv ? G[(size_t)k * N + i] : Zc[(size_t)(k - kv) * ldz + i]; },
-                    [&](int k, int j) { return k < kv ? Zc[(size_t)k * ldz + j] : -G[(size_t)(k - kv) * N + j]; },
-                    true, sm, [&](int i, int j, double v) {
-                        if (j >= i) return;
-                        const double ev = sg * v;
-                        he[i * (i - 1) / 2 + j] = ev;
-                        emx = fmax(emx, fabs(ev));
-                    });
+                auto store = [&](int i, int j, double v) {
+                    if (j >= i) return;
+                    const double ev = sg * v;
+                    he[i * (i - 1) / 2 + j] = ev;
+                    emx = fmax(emx, fabs(ev));
+                };
+                if (delta_commutator) {
+                    // mixed method: P commutes with F~ (the matrix it was made from), so F P - P F = dF P - P dF with
+                    // dF = F - F~, small once the SCF settles; its products in FP32 carry errors ~1e-7 |dF|.
+                    float *G32 = (float *)(wsf + pl.G);
+                    tgemm<true, false>(kv, N, N, [&](int t, int k) { return (float)Zc[(size_t)t * ldz + k]; },
+                                       [&](int k, int i) { return (float)(F[(size_t)k * N + i] - Ft[(size_t)k * N + i]); },
+                                       false, sm, [&](int t, int i, double v) { G32[(size_t)t * N + i] = (float)v; }, 0.0f);
+                    tgemm<false, false>(N, N, 2 * kv,
+                        [&](int i, int k) { return k < kv ? G32[(size_t)k * N + i] : (float)Zc[(size_t)(k - kv) * ldz + i]; },
+                        [&](int k, int j) { return k < kv ? (float)Zc[(size_t)k * ldz + j] : -G32[(size_t)(k - kv) * N + j]; },
+                        true, sm, store, 0.0f);
+                } else {
+                    double *G = wsf + pl.G;
+                    tgemm<true, false>(kv, N, N, [&](int t, int k) { return Zc[(size_t)t * ldz + k]; }, [&](int k, int i) { return F[(size_t)k * N + i]; },
+                                       false, sm, [&](int t, int i, double v) { G[(size_t)t * N + i] = v; });
+                    tgemm<false, false>(N, N, 2 * kv,
+                        [&](int i, int k) { return k < kv ? G[(size_t)k * N + i] : Zc[(size_t)(k - kv) * ldz + i]; },
+                        [&](int k, int j) { return k < kv ? Zc[(size_t)k * ldz + j] : -G[(size_t)(k - kv) * N + j]; },
+                        true, sm, store);
+                }
             } else {
                 // full commutator: FP64, or FP32 after a purification step (whose density carries BF16-level
                 // errors anyway)
