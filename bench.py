@@ -263,6 +263,143 @@ def bench_clusters(args):
     print(json.dumps(line))
 
 
+MD_METRIC = "QC/MM E+grad evals/s in 300 K Langevin dynamics (AM1, 65 QC atoms in 4000 fixed TIP3P waters, ABFS 8/12 A, 0.5 fs)"
+
+
+def bench_md(args):
+    """Config 3 of the metric's workload family: Langevin dynamics (300 K, 0.5 fs, 25 ps^-1) of `frames` replicas
+    of the QC/MM water box with the MM waters fixed, every step one energy + gradient per replica.  The learned
+    start density is trained on densities converged along training trajectories (seed apart), then judged on
+    held-out trajectories: (a) cold, against the diagonal guess, on held-out frames; (b) in dynamics, as a
+    correction of the extrapolated start (2 P(t-1) - P(t-2) + M(t) - 2 M(t-1) + M(t-2)), against the previous-step
+    start (the reference's behaviour) and the plain extrapolation.  The timed comparison: the learned+mixed method
+    (its start density kept only where held-out steps show it saves cycles, else the extrapolation) against plain
+    FP64 with the previous-step start, each over `steps` dynamics steps after `warmup`, from the same state."""
+    import torch
+    from pdynamo_mirror_gb300 import (DIISSCFConverger, LangevinDynamics, LearnedDensityGuess, NBModelABFS, QCModelMNDO, System,
+                                      workloads)
+    rank = int(os.environ.get("RANK", "0"))
+    Z, X, Q, sel, charge = workloads.qcmm_water_box(seed=1)
+    R = args.frames
+    MIXED = dict(densityStep="purification", purificationProducts=6, purificationSwitch=1e-5)
+
+    def make(method):
+        s = System(Z, X, mmCharges=Q)
+        s.electronicState.charge = charge
+        s.DefineQCModel(QCModelMNDO("am1", converger=DIISSCFConverger(**(MIXED if method == "mixed" else {}))), qcSelection=sel)
+        s.DefineNBModel(NBModelABFS(innerCutoff=8.0, outerCutoff=12.0))
+        s.DefineFixedAtoms(range(len(sel), len(Z)))
+        return s
+
+    def equilibrate(m):
+        """The seeded start geometry is not relaxed: a strongly damped bath (250 ps^-1) carries off the released
+        energy, then the production bath (25 ps^-1) for a third of the steps."""
+        m.set_bath(collisionFrequency=250.0)
+        m.run(args.md_equilibration)
+        m.set_bath(collisionFrequency=25.0)
+        m.run(args.md_equilibration // 3)
+
+    info = {}
+    t0 = time.perf_counter()
+    s_tr = make("fp64")
+    md = LangevinDynamics(s_tr, replicas=R, timeStep=0.0005, seed=101 + rank, densityGuess="extrapolate")
+    equilibrate(md)
+    frames, phis, dens = [], [], []
+
+    def keep(m, r):
+        frames.append(m.xyz.clone()); phis.append(r["phi"].clone()); dens.append(m.history[-1].clone())
+    md.run(args.md_training_steps, keep)
+    Ft, PHt, Pt = torch.cat(frames), torch.cat(phis), torch.cat(dens)
+    del frames, phis, dens
+    g = LearnedDensityGuess(s_tr.engine(), seed=0)
+    hist = g.fit(Ft, PHt, Pt, epochs=args.md_epochs, batch=64, lr=1e-3, seed=0)
+    hist += g.fit(Ft, PHt, Pt, epochs=max(1, args.md_epochs // 2), batch=64, lr=2e-4, seed=1)
+    torch.cuda.synchronize()
+    info.update(training_densities=int(Ft.shape[0]), training_trajectories=R, training_seconds=time.perf_counter() - t0,
+                loss_first_last=[hist[0], hist[-1]])
+    del Ft, PHt, Pt
+    # held-out trajectories: equilibrate, then snapshot the state every method starts from
+    s_ho = make("fp64")
+    ho = LangevinDynamics(s_ho, replicas=R, timeStep=0.0005, seed=202 + rank, densityGuess="extrapolate")
+    equilibrate(ho)
+    snap = dict(xyz=ho.xyz.clone(), vel=ho.vel.clone(), acc=ho.acc.clone(), hist=[h.clone() for h in ho.history], n=ho.n_step)
+    # (a) cold start on held-out frames: learned guess against the diagonal guess
+    cold = LearnedDensityGuess(s_ho.engine(), seed=0)
+    cold.load_state_dict(g.state_dict())
+    info["cold_start"] = cold.validate(ho.xyz.contiguous(), s_ho.qcModel.converger, ho.mm_xyz, ho.mm_q, s_ho.nbModel)
+
+    def run_mode(method, mode, steps, warm, clocks=None):
+        s = make(method)
+        guess = mode
+        if mode == "learned":
+            guess = LearnedDensityGuess(s.engine(), seed=0)
+            guess.load_state_dict(g.state_dict())
+        m = LangevinDynamics(s, replicas=R, timeStep=0.0005, seed=202 + rank, densityGuess=guess)
+        m.xyz.copy_(snap["xyz"]); m.vel.copy_(snap["vel"]); m.acc.copy_(snap["acc"]); m.n_step = snap["n"]
+        m.history = [h.clone() for h in snap["hist"]]
+        m.last = {}
+        m.run(warm)
+        torch.cuda.synchronize()
+        st = torch.cuda.current_stream()
+        if clocks:
+            clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        cyc = m.run(steps)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        clk = clocks.stop() if clocks else None
+        E = m.last["energies"][:, 0].cpu().numpy()
+        G = (m.last["qc_gradients"] + m.last["qcmm_qc_gradients"]).cpu().numpy()
+        T = m.temperatures()[1]
+        return dict(ms=ms, evals=R / (ms * 1e-3), cycles=float(np.mean([c.double().mean().item() for c in cyc])), E=E, G=G,
+                    T=float(T.mean()), clk=clk, xyz=m.xyz.clone(), md=m)
+
+    modes = {}
+    for method, mode in (("fp64", "previous"), ("fp64", "extrapolate"), ("fp64", "learned"), ("mixed", "previous"),
+                         ("mixed", "extrapolate"), ("mixed", "learned")):
+        modes[(method, mode)] = run_mode(method, mode, args.md_compare_steps, 3)
+    # the learned correction is kept only if it makes the held-out steps faster (cycles saved net of its inference)
+    use_learned = modes[("mixed", "learned")]["evals"] > modes[("mixed", "extrapolate")]["evals"]
+    best = "learned" if use_learned else "extrapolate"
+    # timed: learned+mixed (as validated) against plain FP64 with the reference's previous-step start
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    head = run_mode("mixed", best, args.steps, args.warmup, clocks)
+    plain = run_mode("fp64", "previous", args.steps, args.warmup)
+    # accuracy: plain FP64 (cold, diagonal guess) on the last geometry of the timed learned+mixed trajectories
+    hm = head["md"]
+    ref = make("fp64")
+    r = ref.engine().run(head["xyz"], ref.qcModel.converger, hm.mm_xyz, hm.mm_q, ref.nbModel, gradients=True, warm_start=False,
+                         mm_gradients=False)
+    dE = float(np.abs(head["E"] - r["energies"][:, 0].cpu().numpy()).max())
+    dG = float(np.abs(head["G"] - (r["qc_gradients"] + r["qcmm_qc_gradients"]).cpu().numpy()).max())
+    del head["md"], plain["md"]
+    line = {"metric": MD_METRIC, "value": head["evals"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded water box; Langevin trajectories of its QC atoms)",
+            "config": {"workload": "qcmm_water_box_langevin", "replicas": R, "time_step_fs": 0.5, "temperature_k": 300.0,
+                       "collision_frequency_per_ps": 25.0,
+                       "equilibration": "%d steps at 250 ps^-1, %d at 25 ps^-1" % (args.md_equilibration, args.md_equilibration // 3),
+                       "method": "learned+mixed: mixed density steps, start density %s" % (
+                           "extrapolation + learned correction" if use_learned else "extrapolation (the learned correction did not make held-out steps faster)"),
+                       "mean_scf_cycles": head["cycles"], "mean_temperature_k": head["T"],
+                       "l2": "working set > L2 (no flush needed)"},
+            # per step: positions, QC/MM potentials, 4 integral kernels, SCF, 4 gradient kernels, 2 QC/MM gradient
+            # kernels, velocities, and the start-density combination; the learned correction adds its features (4),
+            # three MLP layers, the assembly and a potentials launch
+            "gpu_launches": (16 + (9 if use_learned else 0)) * args.steps,
+            "clocks": head["clk"],
+            "plain_fp64_previous_start": {"value": plain["evals"], "ms_per_step": plain["ms"], "mean_scf_cycles": plain["cycles"]},
+            "start_density_comparison": {"%s/%s" % k: {"evals_per_s": v["evals"], "mean_scf_cycles": v["cycles"]} for k, v in modes.items()},
+            "learned_guess": info,
+            "accuracy_vs_plain_fp64": {"where": "last geometry of every timed learned+mixed trajectory, plain FP64 from the diagonal guess",
+                                       "max_abs_dE_hartree": dE,
+                                       "max_abs_dF_hartree_per_bohr": dG, "gate": "|dE| < 1e-6 Eh, |dF| < 1e-5 Eh/Bohr",
+                                       "pass": bool(dE < 1e-6 and dG < 1e-5)}}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -275,13 +412,20 @@ def main():
     ap.add_argument("--method", default="learned_mixed", choices=["learned_mixed", "mixed", "fp64"],
                     help="learned start density + purification cycles (the metric's learned+mixed), purification cycles "
                          "from the diagonal guess (mixed), or FP64 throughout")
-    ap.add_argument("--workload", default="qcmm_water_box", choices=["qcmm_water_box", "water_clusters"],
-                    help="the QC/MM water box (the headline metric) or 512 independent PM3 water clusters in one launch")
+    ap.add_argument("--workload", default="qcmm_water_box", choices=["qcmm_water_box", "water_clusters", "qcmm_md"],
+                    help="the QC/MM water box (the headline metric), 512 independent PM3 water clusters in one launch, or "
+                         "Langevin dynamics of water-box replicas with the learned start density trained on trajectories")
+    ap.add_argument("--md-equilibration", type=int, default=150)
+    ap.add_argument("--md-training-steps", type=int, default=66, help="training densities = replicas x this")
+    ap.add_argument("--md-epochs", type=int, default=6)
+    ap.add_argument("--md-compare-steps", type=int, default=12)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.workload == "water_clusters" and args.impl == "gb300":
         return bench_clusters(args)
+    if args.workload == "qcmm_md" and args.impl == "gb300":
+        return bench_md(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

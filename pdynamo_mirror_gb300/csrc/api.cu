@@ -118,6 +118,8 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     ints.insert(ints.end(), pss.begin(), pss.end());
     ints.insert(ints.end(), pgen.begin(), pgen.end());
     ints.insert(ints.end(), psps.begin(), psps.end());
+    const size_t pk_at = ints.size();
+    for (int a = 0, k = 0; a <= n_atoms; a++) { ints.push_back(k); if (a < n_atoms) k += norb[a] * (norb[a] + 1) / 2; }
     MultipoleMap mp;
     if (!multipole_map_spsp(mp)) { pdg_system_destroy(s); return fail(PDG_BAD_ARGUMENT, "multipole map exceeds its term limit"); }
     int rc = PDG_OK;
@@ -148,6 +150,7 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     d.pairs_ss = b + pl_at; d.pairs_gen = d.pairs_ss + pss.size(); d.n_ss = (int)pss.size(); d.n_gen = (int)pgen.size();
     d.pairs_sps = d.pairs_gen + pgen.size(); d.n_sps = (int)psps.size();
     d.mp_map = s->d_mp;
+    d.atom_pk = b + pk_at;
     *out = s;
     return PDG_OK;
 }
@@ -303,7 +306,7 @@ extern "C" int pdg_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, c
                                   double *gqc, double *gmm, void *stream)
 {
     if (model != 0 && model != 1) return fail(PDG_BAD_ARGUMENT, "model must be 0 (full) or 1 (ABFS)");
-    if (n_frames <= 0 || n_qc <= 0 || n_mm < 0 || !qc || !qcq || !gqc || (n_mm > 0 && (!mm || !q || !gmm))) return fail(PDG_BAD_ARGUMENT, "bad sizes or null pointers");
+    if (n_frames <= 0 || n_qc <= 0 || n_mm < 0 || !qc || !qcq || !gqc || (n_mm > 0 && (!mm || !q))) return fail(PDG_BAD_ARGUMENT, "bad sizes or null pointers");
     if (model == 1 && (n_knots < 2 || !knots || cutoff <= 0.0)) return fail(PDG_BAD_ARGUMENT, "ABFS needs spline knots and a cutoff");
     launch_qcmm_gradients(model, n_frames, n_qc, n_mm, qc, mm, q, qcq, n_knots, knots, cutoff, gqc, gmm, (cudaStream_t)stream);
     return cuda_check(cudaGetLastError(), "qcmm gradients");

@@ -38,6 +38,7 @@ struct DeviceSystem {
     const int *pairs_sps;              // pairs of one sp and one s atom, in pair order
     int n_sps;
     const void *mp_map;                // MultipoleMap of sp-sp pairs (multipole.cuh)
+    const int *atom_pk;                // n_atoms + 1: first entry of each atom's one-centre block in the cel order
 };
 
 // Per-frame workspace plan (all offsets in doubles from the frame's base).

@@ -258,7 +258,7 @@ int launch_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const dou
     Spline sp = make_spline(n_knots, knots, cutoff);
     const int groups = (n_qc + QW - 1) / QW;
     k_qcmm_grad_qc<<<n_frames * groups, QB, 0, st>>>(model, sp, n_qc, n_mm, qc, mm, q, qcq, gqc);
-    if (n_mm > 0) {
+    if (n_mm > 0 && gmm) {
         const int bpf = (n_mm + MB - 1) / MB;
         const size_t sm = sizeof(double) * 4 * (size_t)n_qc + sizeof(float) * 3 * (size_t)n_qc;
         if (sm > 48 * 1024) cudaFuncSetAttribute(k_qcmm_grad_mm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);

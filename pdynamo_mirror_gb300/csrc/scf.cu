@@ -154,10 +154,20 @@ __device__ void tgemm(int M, int Nc, int K, FA fa, FB fb, bool lower_only, Smem 
 // ----------------------------------------------------------------------------------------------------
 // F = H + G(P) and the energies tr(PH), tr(PG)/2; then the QC/MM Lowdin term.  Returns eqcmm.
 __device__ void fock_build(const SCFArgs &a, int f, const double *H, const double *P, double *F, const double *tei,
-                           Smem &sm, double *e1, double *e2, double *eqcmm)
+                           Smem &sm, double *e1, double *e2, double *eqcmm, double *scratch)
 {
     const DeviceSystem &s = a.s;
     const int N = s.n_basis, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    // One-centre densities of every atom with the off-diagonal factor 2 (the Coulomb contractions' right-hand
+    // sides), in the order of the diagonal-block element list: in the GEMM staging area when they fit, else in
+    // the workspace scratch.
+    double *pk = s.n_cel <= GK * (GA_LD + GB_LD) ? sm.ta : scratch;
+    for (int e = threadIdx.x; e < s.n_cel; e += PDG_BLOCK) {
+        const int A = s.cel[e] >> 4, ab = s.cel[e] & 15, as = s.atom_start[A];
+        const int m = MP_DA[ab], n = MP_DB[ab];
+        pk[e] = (m == n ? 1.0 : 2.0) * P[(size_t)(as + m) * N + as + n];
+    }
+    __syncthreads();
     // One flat pass, one thread per output element (lists built by pdg_system_create):
     //  * diagonal-block element (A, m >= n): H + one-centre G + Coulomb sum_B sum_cd (mn|cd) P_B,cd over every
     //    partner atom B (QCModelMNDO_Fock's one-centre terms and MakeFockG's Coulomb part);
@@ -173,13 +183,10 @@ __device__ void fock_build(const SCFArgs &a, int f, const double *H, const doubl
             for (int B = 0; B < s.n_atoms; B++) {
                 if (B == A) continue;
                 const int hi = A > B ? A : B, lo = A > B ? B : A, pp = hi * (hi - 1) / 2 + lo;
-                const int nob = s.atom_norb[B], bs = s.atom_start[B], nb = nob * (nob + 1) / 2;
-                const double *blk = tei + s.pair_tei[pp];
-                for (int cd = 0; cd < nb; cd++) {
-                    const int c = MP_DA[cd], d = MP_DB[cd];
-                    const double pb = (c == d ? 1.0 : 2.0) * P[(size_t)(bs + c) * N + bs + d];
-                    acc = fma(A > B ? blk[ab * nb + cd] : blk[cd * na + ab], pb, acc);
-                }
+                const int k0 = s.atom_pk[B], nb = s.atom_pk[B + 1] - k0;
+                const double *blk = tei + s.pair_tei[pp], *pb = pk + k0;
+                if (A > B) for (int cd = 0; cd < nb; cd++) acc = fma(blk[ab * nb + cd], pb[cd], acc);
+                else       for (int cd = 0; cd < nb; cd++) acc = fma(blk[cd * na + ab], pb[cd], acc);
             }
             const double *E = elem(s, s.atom_elem[A]);
             const double gss = E[PDG_E_GSS], gsp = E[PDG_E_GSP], gpp = E[PDG_E_GPP], gp2 = E[PDG_E_GP2], hsp = E[PDG_E_HSP], hpp = E[PDG_E_HPP];
@@ -215,10 +222,18 @@ __device__ void fock_build(const SCFArgs &a, int f, const double *H, const doubl
         }
     }
     __syncthreads();
-    double t1 = 0.0, t2 = 0.0;
-    for (size_t k = threadIdx.x; k < (size_t)N * N; k += PDG_BLOCK) { double pv = P[k], hv = H[k]; t1 += pv * hv; t2 += pv * (F[k] - hv); }
-    *e1 = block_sum(t1, sm.red);
-    *e2 = 0.5 * block_sum(t2, sm.red);
+    // tr(P H) and tr(P G) = tr(P F) - tr(P H) over the lower triangle (all three matrices are symmetric), warp per row
+    double th = 0.0, tf = 0.0, dh = 0.0, df = 0.0;
+    for (int i = w; i < N; i += PDG_WARPS)
+        for (int j = lane; j <= i; j += 32) {
+            const size_t k = (size_t)i * N + j;
+            const double pv = P[k];
+            if (j < i) { th = fma(pv, H[k], th); tf = fma(pv, F[k], tf); }
+            else { dh = fma(pv, H[k], dh); df = fma(pv, F[k], df); }
+        }
+    const double2 tr_h = block_sum2(th, dh, sm.red), tr_f = block_sum2(tf, df, sm.red);
+    *e1 = 2.0 * tr_h.x + tr_h.y;
+    *e2 = 0.5 * ((2.0 * tr_f.x + tr_f.y) - *e1);
     // QC/MM: q_A = Z_A - sum P_mm, E += q . phi, F_mm -= phi_A (QCModelMNDO.c:1459-1520, 1808-1860)
     double tq = 0.0;
     const double *phi = a.phi ? a.phi + (size_t)f * s.n_atoms : nullptr;
@@ -996,7 +1011,7 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
         return;
     }
     if (a.fock_only) {
-        fock_build(a, f, H, P, F, tei, sm, &e1, &e2, &eq);
+        fock_build(a, f, H, P, F, tei, sm, &e1, &e2, &eq, wsf + pl.P0);
         for (size_t k = tid; k < NN; k += PDG_BLOCK) a.fock_out[(size_t)f * NN + k] = F[k];
         if (tid == 0) {
             double *E = a.energies + (size_t)f * PDG_NENERGY;
@@ -1023,7 +1038,7 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
             for (size_t k = tid; k < NN; k += PDG_BLOCK) Ft[k] = F[k];
             __syncthreads();
         }
-        fock_build(a, f, H, P, F, tei, sm, &e1, &e2, &eq);
+        fock_build(a, f, H, P, F, tei, sm, &e1, &e2, &eq, wsf + pl.P0);
         tm.lap(PDG_T_FOCK);
         ncyc++;
         eel = e1 + e2 + eq;

@@ -186,7 +186,7 @@ class LangevinDynamics:
             # the SCF overwrites its start density with the converged one: never hand it a history entry
             eng.density = P0.clone() if any(P0 is h for h in self.history) else P0
             warm = True
-        r = eng.run(self.xyz, conv, self.mm_xyz, self.mm_q, self.nb, gradients=True, warm_start=warm)
+        r = eng.run(self.xyz, conv, self.mm_xyz, self.mm_q, self.nb, gradients=True, warm_start=warm, mm_gradients=False)
         if (r["status"] != _native.PDG_OK).any():
             raise _native.NativeError("SCF procedure not converged in dynamics step %d." % self.n_step)
         if self.mode != "diagonal":
@@ -223,6 +223,13 @@ class LangevinDynamics:
         r = self._evaluate()
         self._accelerations(r, self.integrator.constants["facV3"])
         return r
+
+    def set_bath(self, collisionFrequency=None, temperature=None):
+        """Change the bath (collision frequency ps^-1, temperature K) for the following steps, e.g. a strongly
+        damped equilibration before production."""
+        it = self.integrator
+        self.integrator = LangevinVelocityVerletIntegrator(it.collisionFrequency if collisionFrequency is None else collisionFrequency,
+                                                           it.temperature if temperature is None else temperature, it.timeStep)
 
     def temperatures(self):
         """Kinetic energy (kJ/mol) and temperature (K) per replica, host arrays (Temperature, :255-260)."""

@@ -68,11 +68,12 @@ class QCEngine:
             self._knots[k] = torch.as_tensor(nbmodel.knots(), dtype=torch.float64, device=self.device)
         return self._knots[k]
 
-    def run(self, qc_xyz, converger, mm_xyz=None, mm_charges=None, nbmodel=None, gradients=True, warm_start=True, guess=None):
+    def run(self, qc_xyz, converger, mm_xyz=None, mm_charges=None, nbmodel=None, gradients=True, warm_start=True, guess=None,
+            mm_gradients=True):
         """qc_xyz [F, n, 3] and mm_xyz [F, m, 3] in Angstrom (device float64), mm_charges [m].  The SCF starts
         from the previous density (warm_start, same batch shape), else from guess.predict (a
-        LearnedDensityGuess, unless its validation disabled it), else from the diagonal guess.  Returns a dict of device tensors in Hartree /
-        Hartree per Bohr."""
+        LearnedDensityGuess, unless its validation disabled it), else from the diagonal guess.  mm_gradients=False skips the
+        MM-side QC/MM gradients (fixed MM atoms).  Returns a dict of device tensors in Hartree / Hartree per Bohr."""
         F = qc_xyz.shape[0]
         n, N = self.n_atoms, self.n_basis
         dev = self.device
@@ -109,7 +110,7 @@ class QCEngine:
         out.update(energies=energies, qc_gradients=grad, charges=charges, status=status, ncycles=ncycles, phi=phi)
         if qcmm and gradients:
             gqc = torch.empty((F, n, 3), dtype=torch.float64, device=dev)
-            gmm = torch.empty((F, mm_xyz.shape[1], 3), dtype=torch.float64, device=dev)
+            gmm = torch.empty((F, mm_xyz.shape[1], 3), dtype=torch.float64, device=dev) if mm_gradients else None
             _native.check(self.L.pdg_qcmm_gradients(nbmodel.model_id, F, n, mm_xyz.shape[1], _native.ptr(qc_xyz), _native.ptr(mm_xyz),
                                                     _native.ptr(mm_charges), _native.ptr(charges), nk, _native.ptr(knots),
                                                     float(nbmodel.outerCutoff), _native.ptr(gqc), _native.ptr(gmm), sh),
