@@ -26,7 +26,8 @@ TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densi
           "QC Densities Cluster Rounds", "QC Densities Steps", "QC Densities Purification",
           "QC Densities Purification Steps", "QC Densities SP2 Iterations", "SM", "Start ns", "End ns", "QC Densities Purification Products",
           "QC Densities Purification Readout", "QC Densities Purification Control", "QC Densities Purification Setup",
-          "QC Densities Purification Finish") + tuple("RMS %d" % k for k in range(40))
+          "QC Densities Purification Finish", "QC Densities Perturbative", "QC Densities Perturbative Steps",
+          "QC Densities Perturbative Base", "QC Densities Perturbative Fallbacks") + tuple("RMS %d" % k for k in range(40))
 
 
 class SCFOptions(ctypes.Structure):

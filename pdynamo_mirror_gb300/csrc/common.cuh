@@ -44,10 +44,27 @@ struct DeviceSystem {
 // Per-frame workspace plan (all offsets in doubles from the frame's base).
 struct FramePlan {
     size_t tei, pair_e, pair_g, H, F, P0, A, G, Z, LU, LO, hP, hF, hE, rP, rF, misc, stride;
+    size_t BF, BP, BZ, BV, BL, BW;   // perturbative density steps: base F, P, wanted and complement vectors, eigenvalues, FP32 work
     int hist_len;   // packed history vector length N(N+1)/2 (errors use N(N-1)/2 within the same slot)
 };
 
 __host__ __device__ inline size_t align32(size_t x) { return (x + 31) & ~size_t(31); }
+
+// FP32 work of a perturbative density step (floats): dF (N x N), dF Z^T (N x kv), E (nc x kv), Lambda' (kv x kv),
+// dF V^T (N x nc), M' (nc x nc), K and its next iterate (nc x kv each), E^T K and U (kv x kv each), Y and W
+// (kv x N each), dQ (N x N).
+__host__ __device__ inline size_t pert_work_floats(int N, int kv)
+{
+    const size_t n = N, k = kv, c = N - kv;
+    return 2 * n * n + n * k + n * c + 3 * c * k + 3 * k * k + c * c + 2 * k * n + 64;
+}
+
+// Offset (floats) of dQ in that work.
+__host__ __device__ inline size_t pert_dq_offset(int N, int kv)
+{
+    const size_t n = N, k = kv, c = N - kv;
+    return n * n + n * k + c * k + k * k + n * c + c * c + 2 * c * k + 2 * k * k + 2 * k * n;
+}
 
 __host__ inline FramePlan make_plan(const DeviceSystem &s, int history)
 {
@@ -62,7 +79,8 @@ __host__ inline FramePlan make_plan(const DeviceSystem &s, int history)
     p.P0 = o;     o += align32(NN);          // F in FP32 (N x round4(N)) for the commutator after a purification step
     p.A = o;      o += align32(2 * NN + 4 * N);  // work matrix: F P product, packed tridiagonal matrix, or the FP32
                                                  // purification iterates (two N x N) and P in FP32 (N x round4(N))
-    const size_t kv = s.n_vec > 0 ? s.n_vec : 1, kvp = (kv + 31) & ~size_t(31);
+    const size_t kv = s.n_vec > 0 ? s.n_vec : 1, nc = N > kv ? N - kv : 1;
+    const size_t kvp = (nc + 31) & ~size_t(31);   // inverse iteration of the wanted vectors or of their complement
     p.G = o;      o += align32(kv * N);      // DIIS: the vectors times F
     p.Z = o;      o += align32(kv * (N | 1)); // wanted eigenvectors when they do not fit in shared memory
     p.LU = o;     o += align32(5 * N * kvp + (N * kvp + 7) / 8);   // inverse iteration factors + iterates
@@ -74,7 +92,15 @@ __host__ inline FramePlan make_plan(const DeviceSystem &s, int history)
     p.hE = o;     o += align32((size_t)history * p.hist_len);
     p.rP = o;     o += align32(NN);
     p.rF = o;     o += align32(NN);
-    p.misc = o;   o += align32(PDG_MAX_HISTORY * PDG_MAX_HISTORY + 64);   // DIIS B matrix, then PDG_NTIMERS phase timers
+    p.misc = o;   o += align32(PDG_MAX_HISTORY * PDG_MAX_HISTORY + 96);   // DIIS B matrix, then PDG_NTIMERS phase timers
+    // base of the perturbative density steps (mixed method): the Fock matrix and density of the last FP64
+    // step, its wanted vectors and their complement (FP64, rows of N | 1), their eigenvalues, and FP32 work
+    p.BF = o;     o += align32(NN);
+    p.BP = o;     o += align32(NN);
+    p.BZ = o;     o += align32(kv * (N | 1));
+    p.BV = o;     o += align32(nc * (N | 1));
+    p.BL = o;     o += align32(N);
+    p.BW = o;     o += align32((pert_work_floats(N, (int)kv) + 1) / 2);
     p.stride = align32(o);
     return p;
 }

@@ -151,6 +151,83 @@ __device__ void tgemm(int M, int Nc, int K, FA fa, FB fb, bool lower_only, Smem 
     __syncthreads();
 }
 
+// FP32 C = A B for the perturbative density step and the mixed method's commutators.  Output tiles of
+// (4 TY) x 64 (TY = threads / 16) with 4 x 4 outputs per thread, so every 16-deep staged chunk gives each thread
+// 16 FMAs per pair of float4 shared-memory reads; the next chunk's operands are loaded into registers while the
+// current one is multiplied, so the L2 latency of the staging loads overlaps the FMAs.  The staging fits in the
+// FP64 GEMM's staging area.  The epilogue receives every (i, j) < (M, Nc) of a computed tile; lower_only skips
+// tiles wholly above the diagonal (callers filter j > i).
+template <bool AK, bool BK, typename FA, typename FB, typename Epi>
+__device__ void tgemm32(int M, int Nc, int K, FA fa, FB fb, bool lower_only, Smem &sm, Epi epi)
+{
+    constexpr int TX = 16, TY = PDG_BLOCK / TX, TM = 4 * TY, TN = 64, KC = 16, LDA = TM + 4, LDB = TN;
+    constexpr int NA = TM * KC / PDG_BLOCK, NB = KC * TN / PDG_BLOCK;
+    static_assert(KC * (LDA + LDB) * sizeof(float) <= GK * (GA_LD + GB_LD) * sizeof(double), "staging area");
+    const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
+    float *ga = (float *)sm.ta, *gb = ga + KC * LDA;
+    for (int i0 = 0; i0 < M; i0 += TM)
+        for (int j0 = 0; j0 < Nc; j0 += TN) {
+            if (lower_only && j0 > i0 + TM - 1) continue;
+            float acc[4][4];
+#pragma unroll
+            for (int x = 0; x < 4; x++)
+#pragma unroll
+                for (int y = 0; y < 4; y++) acc[x][y] = 0.f;
+            float ra[NA], rb[NB];
+            auto fetch = [&](int k0) {
+                const int kc = min(KC, K - k0);
+#pragma unroll
+                for (int u = 0; u < NA; u++) {
+                    const int t = tid + u * PDG_BLOCK;
+                    const int r = AK ? t / KC : t % TM, kk = AK ? t % KC : t / TM, gi = i0 + r;
+                    ra[u] = (kk < kc && gi < M) ? (float)fa(gi, k0 + kk) : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < NB; u++) {
+                    const int t = tid + u * PDG_BLOCK;
+                    const int c = BK ? t / KC : t % TN, kk = BK ? t % KC : t / TN, gj = j0 + c;
+                    rb[u] = (kk < kc && gj < Nc) ? (float)fb(k0 + kk, gj) : 0.f;
+                }
+            };
+            fetch(0);
+            for (int k0 = 0; k0 < K; k0 += KC) {
+                const int kc = min(KC, K - k0);
+                __syncthreads();
+#pragma unroll
+                for (int u = 0; u < NA; u++) {
+                    const int t = tid + u * PDG_BLOCK;
+                    const int r = AK ? t / KC : t % TM, kk = AK ? t % KC : t / TM;
+                    ga[kk * LDA + r] = ra[u];
+                }
+#pragma unroll
+                for (int u = 0; u < NB; u++) {
+                    const int t = tid + u * PDG_BLOCK;
+                    const int c = BK ? t / KC : t % TN, kk = BK ? t % KC : t / TN;
+                    gb[kk * LDB + c] = rb[u];
+                }
+                __syncthreads();
+                if (k0 + KC < K) fetch(k0 + KC);
+#pragma unroll 4
+                for (int kk = 0; kk < kc; kk++) {
+                    const float4 av = *(const float4 *)(ga + kk * LDA + 4 * ty), bv = *(const float4 *)(gb + kk * LDB + 4 * tx);
+                    const float x4[4] = { av.x, av.y, av.z, av.w }, y4[4] = { bv.x, bv.y, bv.z, bv.w };
+#pragma unroll
+                    for (int x = 0; x < 4; x++)
+#pragma unroll
+                        for (int y = 0; y < 4; y++) acc[x][y] = fmaf(x4[x], y4[y], acc[x][y]);
+                }
+            }
+#pragma unroll
+            for (int x = 0; x < 4; x++)
+#pragma unroll
+                for (int y = 0; y < 4; y++) {
+                    const int gi = i0 + 4 * ty + x, gj = j0 + 4 * tx + y;
+                    if (gi < M && gj < Nc) epi(gi, gj, (double)acc[x][y]);
+                }
+        }
+    __syncthreads();
+}
+
 // ----------------------------------------------------------------------------------------------------
 // F = H + G(P) and the energies tr(PH), tr(PG)/2; then the QC/MM Lowdin term.  Returns eqcmm.
 __device__ void fock_build(const SCFArgs &a, int f, const double *H, const double *P, double *F, const double *tei,
@@ -331,7 +408,7 @@ __device__ int sturm_count32(int N, const float *d, const float *e2, float x, fl
 
 // Phase timers: thread 0 accumulates clock64() deltas between block-wide barriers into the frame's
 // timer slots (workspace misc area, after the DIIS B matrix).
-static_assert(PDG_NTIMERS <= 64, "timer slots live in the 64 doubles after the DIIS B matrix");
+static_assert(PDG_NTIMERS <= 96, "timer slots live in the 96 doubles after the DIIS B matrix");
 struct Timer {
     double *slot; long long t;
     __device__ void start() { if (threadIdx.x == 0) t = clock64(); }
@@ -453,7 +530,155 @@ __device__ void inverse_iteration(int N, int t, double sigma, double tiny, const
     for (int i = 0; i < N; i++) zout[i] = y[(size_t)i * ldy] * sc;
 }
 
-__device__ double density_step(const SCFArgs &a, double *wsf, const double *F, double *P, Smem &sm, Timer &tm)
+// Eigenvalues first .. first + kv - 1 of the tridiagonal T (sm.d, sm.e) left by the Householder reduction of the
+// matrix whose reflectors are in A, their eigenvectors by inverse iteration, back-transformed to the rows of Z
+// (kv rows of ldz; z_in_smem when Z is the shared-memory slot).  The eigenvalues are left in sm.eig[0 .. kv).
+__device__ void tridiag_vectors(const SCFArgs &a, double *wsf, const double *A, Smem &sm, Timer &tm, int first, int kv, double *Z,
+                                bool z_in_smem, bool count_step = true)
+{
+    const DeviceSystem &s = a.s;
+    const FramePlan &pl = a.plan;
+    const int N = s.n_basis, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int ldz = sm.ldz;
+    // --- shifts: eigenvalues first .. first + kv - 1 of T by FP32 Sturm multisection, eight threads per eigenvalue,
+    //     each round narrowing the bracket ninefold
+    float *d32 = (float *)sm.e2, *e232 = d32 + N;
+    double gl = 1e300, gu = -1e300, emax2 = 0.0, onen = 0.0;
+    for (int i = tid; i < N; i += PDG_BLOCK) {
+        const double r = (i > 0 ? fabs(sm.e[i - 1]) : 0.0) + (i < N - 1 ? fabs(sm.e[i]) : 0.0);
+        gl = fmin(gl, sm.d[i] - r); gu = fmax(gu, sm.d[i] + r); onen = fmax(onen, fabs(sm.d[i]) + r);
+        d32[i] = (float)sm.d[i];
+        const double e2 = (i < N - 1) ? sm.e[i] * sm.e[i] : 0.0;
+        e232[i] = (float)e2; emax2 = fmax(emax2, e2);
+    }
+    gl = -block_max(-gl, sm.red); gu = block_max(gu, sm.red); emax2 = block_max(emax2, sm.red); onen = block_max(onen, sm.red);
+    const double tnorm = fmax(fabs(gl), fabs(gu));
+    const float pivmin = (float)(1.0e-30 * fmax(1.0, emax2));
+    const float glo = (float)(gl - 1.0e-6 * tnorm - 1.0e-30), ghi = (float)(gu + 1.0e-6 * tnorm + 1.0e-30);
+    for (int g0 = 0; g0 < kv; g0 += PDG_BLOCK / 8) {
+        const int t = g0 + tid / 8, sl = tid % 8;
+        const unsigned gmask = 0xFFu << (lane & ~7);
+        const bool live = t < kv;
+        const int mi = first + t;
+        float lo = glo, hi = ghi;
+        for (int round = 0; round < 16; round++) {
+            const float x = lo + (hi - lo) * (float)(sl + 1) * (1.0f / 9.0f);
+            const bool below = live && sturm_count32(N, d32, e232, x, pivmin) <= mi;   // x <= lambda_mi
+            const unsigned bal = (__ballot_sync(0xffffffffu, below) & gmask) >> (lane & ~7);
+            const int nb = __popc(bal);   // Sturm counts grow with x: the first nb points lie below
+            const float xl = __shfl_sync(0xffffffffu, x, (lane & ~7) + (nb > 0 ? nb - 1 : 0));
+            const float xh = __shfl_sync(0xffffffffu, x, (lane & ~7) + (nb < 8 ? nb : 7));
+            const float nlo = nb > 0 ? xl : lo, nhi = nb < 8 ? xh : hi;
+            const bool progress = live && (nlo > lo || nhi < hi);
+            lo = nlo; hi = nhi;
+            if (!__any_sync(0xffffffffu, progress)) break;   // every group of the warp is at FP32 resolution
+        }
+        if (live && sl == 0) sm.eig[t] = 0.5 * ((double)lo + (double)hi);
+    }
+    __syncthreads();
+    tm.lap(PDG_T_EIGENVALUES);
+    // --- clusters: neighbours closer than ortol are re-orthogonalised against each other (dstein-style);
+    //     shifts within the FP32 resolution are separated.  iv[64 + t] = first vector of t's cluster,
+    //     iv[0] = largest cluster.
+    if (tid == 0) {
+        const double ortol = 1.0e-4 * fmax(onen, 1.0);
+        int start = 0, big = kv > 0 ? 1 : 0;
+        sm.iv[64] = 0;
+        for (int t = 1; t < kv; t++) {
+            const double pert = 1.0e-7 * fmax(fabs(sm.eig[t]), 1.0);
+            if (sm.eig[t] - sm.eig[t - 1] < pert) sm.eig[t] = sm.eig[t - 1] + pert;
+            if (sm.eig[t] - sm.eig[t - 1] > ortol) start = t;
+            sm.iv[64 + t] = start;
+            big = max(big, t - start + 1);
+        }
+        sm.iv[0] = big;
+        sm.small[0] = onen;
+    }
+    __syncthreads();
+    // --- eigenvectors: one thread per vector; cluster members in rounds so that each one is projected
+    //     against the finished earlier members
+    {
+        const int rounds = sm.iv[0], kvp = (kv + 31) & ~31;
+        if (tid == 0 && count_step) { tm.slot[PDG_T_ROUNDS] += rounds; tm.slot[PDG_T_DENSITY_STEPS] += 1.0; }
+        const double tiny = 2.2e-16 * fmax(sm.small[0], 1.0);
+        double *U0 = wsf + pl.LU, *U1 = U0 + (size_t)N * kvp, *U2 = U1 + (size_t)N * kvp, *LM = U2 + (size_t)N * kvp;
+        double *Y = LM + (size_t)N * kvp;
+        unsigned char *PV = (unsigned char *)(Y + (size_t)N * kvp);
+        for (int r = 0; r < rounds; r++) {
+            for (int t = tid; t < kv; t += PDG_BLOCK) {
+                const int cs = sm.iv[64 + t];
+                if (t - cs != r) continue;
+                double *y = z_in_smem ? Z + (size_t)t * ldz : Y + t;   // in place in the output row when Z is in shared memory
+                inverse_iteration(N, t, sm.eig[t], tiny, sm.d, sm.e, U0 + t, U1 + t, U2 + t, LM + t, PV + t, y, z_in_smem ? 1 : kvp, kvp,
+                                  Z + (size_t)cs * ldz, t - cs, ldz, Z + (size_t)t * ldz);
+            }
+            __syncthreads();
+        }
+    }
+    tm.lap(PDG_T_EIGENVECTORS);
+    // --- back-transformation Z <- Q Z, Q = H_0 H_1 ... H_{N-3} with the reflectors stored in A
+    if (N >= 32) {
+        // blocked (compact WY, as LAPACK's dlarft / dlarfb): blocks of up to 16 consecutive reflectors, last
+        // block first; block b is I - V T V^T with V the reflectors' unit lower-trapezoidal columns over rows
+        // k0 + 1 .. N - 1 (row i of V is contiguous in the packed A) and T upper triangular.  Per block one GEMM
+        // gives S = V^T V and W = V^T Z together, one warp builds T from S, W2 = T W, and a second GEMM applies
+        // Z^T -= W2^T V^T (stores along Z's rows).  Same 2 N^2 kv flops as reflector-by-reflector, but Z and the
+        // reflectors pass through the GEMM staging once per block instead of once per reflector and vector.
+        const int nref = N - 2;
+        double *Wm = wsf + pl.LU, *W2 = Wm + (size_t)16 * kv, *Sg = W2 + (size_t)16 * kv, *Tt = Sg + 256;
+        for (int k0 = ((nref - 1) / 16) * 16; k0 >= 0; k0 -= 16) {
+            const int nbk = min(16, nref - k0), m0 = N - k0 - 1;
+            auto V = [&](int i, int c) -> double { return i < c ? 0.0 : (i == c ? 1.0 : A[plo(k0 + 1 + i, k0 + c)]); };
+            tgemm<false, true>(nbk, 16 + kv, m0, [&](int c, int i) { return V(i, c); },
+                               [&](int i, int j) { return j < 16 ? (j < nbk ? V(i, j) : 0.0) : Z[(size_t)(j - 16) * ldz + k0 + 1 + i]; },
+                               false, sm, [&](int c, int j, double v) {
+                                   if (j < 16) Sg[c * 16 + j] = v;
+                                   else Wm[(size_t)c * kv + (j - 16)] = v;
+                               });
+            if (w == 0) {   // T(c, c) = tau_c;  T(0:c, c) = -tau_c T(0:c, 0:c) S(0:c, c)
+                for (int c = 0; c < nbk; c++) {
+                    const double tau = sm.tau[k0 + c];
+                    double t = 0.0;
+                    if (lane < c) {
+                        for (int j = lane; j < c; j++) t = fma(Tt[lane * 16 + j], Sg[j * 16 + c], t);
+                        t *= -tau;
+                    }
+                    __syncwarp();
+                    if (lane < 16) Tt[lane * 16 + c] = lane < c ? t : (lane == c ? tau : 0.0);
+                    __syncwarp();
+                }
+            }
+            __syncthreads();
+            for (int e = tid; e < nbk * kv; e += PDG_BLOCK) {
+                const int c = e / kv, t = e % kv;
+                double acc = 0.0;
+                for (int j = c; j < nbk; j++) acc = fma(Tt[c * 16 + j], Wm[(size_t)j * kv + t], acc);
+                W2[(size_t)c * kv + t] = acc;
+            }
+            __syncthreads();
+            tgemm<false, true>(kv, m0, nbk, [&](int t, int c) { return W2[(size_t)c * kv + t]; }, [&](int c, int i) { return V(i, c); },
+                               false, sm, [&](int t, int i, double v) { Z[(size_t)t * ldz + k0 + 1 + i] -= v; });
+        }
+    } else {
+        // reflector by reflector, one warp per vector
+        for (int t = w; t < kv; t += PDG_WARPS) {
+            double *zt = Z + (size_t)t * ldz;
+            for (int k = N - 3; k >= 0; k--) {
+                const double tau = sm.tau[k];
+                if (tau == 0.0) continue;
+                const int m = N - k - 1;
+                double dt = 0.0;
+                for (int i = lane; i < m; i += 32) dt = fma(i == 0 ? 1.0 : A[plo(k + 1 + i, k)], zt[k + 1 + i], dt);
+                dt = warp_sum(dt) * tau;
+                for (int i = lane; i < m; i += 32) zt[k + 1 + i] = fma(-dt, i == 0 ? 1.0 : A[plo(k + 1 + i, k)], zt[k + 1 + i]);
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__device__ double density_step(const SCFArgs &a, double *wsf, const double *F, double *P, Smem &sm, Timer &tm, bool make_base = false)
 {
     const DeviceSystem &s = a.s;
     const FramePlan &pl = a.plan;
@@ -538,143 +763,7 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
     }
     __syncthreads();
     tm.lap(PDG_T_TRIDIAGONAL);
-    // --- shifts: the wanted eigenvalues of T by FP32 Sturm multisection, eight threads per eigenvalue,
-    //     each round narrowing the bracket ninefold
-    float *d32 = (float *)sm.e2, *e232 = d32 + N;
-    double gl = 1e300, gu = -1e300, emax2 = 0.0, onen = 0.0;
-    for (int i = tid; i < N; i += PDG_BLOCK) {
-        const double r = (i > 0 ? fabs(sm.e[i - 1]) : 0.0) + (i < N - 1 ? fabs(sm.e[i]) : 0.0);
-        gl = fmin(gl, sm.d[i] - r); gu = fmax(gu, sm.d[i] + r); onen = fmax(onen, fabs(sm.d[i]) + r);
-        d32[i] = (float)sm.d[i];
-        const double e2 = (i < N - 1) ? sm.e[i] * sm.e[i] : 0.0;
-        e232[i] = (float)e2; emax2 = fmax(emax2, e2);
-    }
-    gl = -block_max(-gl, sm.red); gu = block_max(gu, sm.red); emax2 = block_max(emax2, sm.red); onen = block_max(onen, sm.red);
-    const double tnorm = fmax(fabs(gl), fabs(gu));
-    const float pivmin = (float)(1.0e-30 * fmax(1.0, emax2));
-    const float glo = (float)(gl - 1.0e-6 * tnorm - 1.0e-30), ghi = (float)(gu + 1.0e-6 * tnorm + 1.0e-30);
-    const int first = s.vec_occupied ? 0 : N - kv;
-    for (int g0 = 0; g0 < kv; g0 += PDG_BLOCK / 8) {
-        const int t = g0 + tid / 8, sl = tid % 8;
-        const unsigned gmask = 0xFFu << (lane & ~7);
-        const bool live = t < kv;
-        const int mi = first + t;
-        float lo = glo, hi = ghi;
-        for (int round = 0; round < 16; round++) {
-            const float x = lo + (hi - lo) * (float)(sl + 1) * (1.0f / 9.0f);
-            const bool below = live && sturm_count32(N, d32, e232, x, pivmin) <= mi;   // x <= lambda_mi
-            const unsigned bal = (__ballot_sync(0xffffffffu, below) & gmask) >> (lane & ~7);
-            const int nb = __popc(bal);   // Sturm counts grow with x: the first nb points lie below
-            const float xl = __shfl_sync(0xffffffffu, x, (lane & ~7) + (nb > 0 ? nb - 1 : 0));
-            const float xh = __shfl_sync(0xffffffffu, x, (lane & ~7) + (nb < 8 ? nb : 7));
-            const float nlo = nb > 0 ? xl : lo, nhi = nb < 8 ? xh : hi;
-            const bool progress = live && (nlo > lo || nhi < hi);
-            lo = nlo; hi = nhi;
-            if (!__any_sync(0xffffffffu, progress)) break;   // every group of the warp is at FP32 resolution
-        }
-        if (live && sl == 0) sm.eig[t] = 0.5 * ((double)lo + (double)hi);
-    }
-    __syncthreads();
-    tm.lap(PDG_T_EIGENVALUES);
-    // --- clusters: neighbours closer than ortol are re-orthogonalised against each other (dstein-style);
-    //     shifts within the FP32 resolution are separated.  iv[64 + t] = first vector of t's cluster,
-    //     iv[0] = largest cluster.
-    if (tid == 0) {
-        const double ortol = 1.0e-4 * fmax(onen, 1.0);
-        int start = 0, big = kv > 0 ? 1 : 0;
-        sm.iv[64] = 0;
-        for (int t = 1; t < kv; t++) {
-            const double pert = 1.0e-7 * fmax(fabs(sm.eig[t]), 1.0);
-            if (sm.eig[t] - sm.eig[t - 1] < pert) sm.eig[t] = sm.eig[t - 1] + pert;
-            if (sm.eig[t] - sm.eig[t - 1] > ortol) start = t;
-            sm.iv[64 + t] = start;
-            big = max(big, t - start + 1);
-        }
-        sm.iv[0] = big;
-        sm.small[0] = onen;
-    }
-    __syncthreads();
-    // --- eigenvectors: one thread per vector; cluster members in rounds so that each one is projected
-    //     against the finished earlier members
-    {
-        const int rounds = sm.iv[0], kvp = (kv + 31) & ~31;
-        if (tid == 0) { tm.slot[PDG_T_ROUNDS] += rounds; tm.slot[PDG_T_DENSITY_STEPS] += 1.0; }
-        const double tiny = 2.2e-16 * fmax(sm.small[0], 1.0);
-        double *U0 = wsf + pl.LU, *U1 = U0 + (size_t)N * kvp, *U2 = U1 + (size_t)N * kvp, *LM = U2 + (size_t)N * kvp;
-        double *Y = LM + (size_t)N * kvp;
-        unsigned char *PV = (unsigned char *)(Y + (size_t)N * kvp);
-        for (int r = 0; r < rounds; r++) {
-            for (int t = tid; t < kv; t += PDG_BLOCK) {
-                const int cs = sm.iv[64 + t];
-                if (t - cs != r) continue;
-                double *y = sm.zs ? Z + (size_t)t * ldz : Y + t;   // in place in the output row when Z is in shared memory
-                inverse_iteration(N, t, sm.eig[t], tiny, sm.d, sm.e, U0 + t, U1 + t, U2 + t, LM + t, PV + t, y, sm.zs ? 1 : kvp, kvp,
-                                  Z + (size_t)cs * ldz, t - cs, ldz, Z + (size_t)t * ldz);
-            }
-            __syncthreads();
-        }
-    }
-    tm.lap(PDG_T_EIGENVECTORS);
-    // --- back-transformation Z <- Q Z, Q = H_0 H_1 ... H_{N-3} with the reflectors stored in A
-    if (N >= 32) {
-        // blocked (compact WY, as LAPACK's dlarft / dlarfb): blocks of up to 16 consecutive reflectors, last
-        // block first; block b is I - V T V^T with V the reflectors' unit lower-trapezoidal columns over rows
-        // k0 + 1 .. N - 1 (row i of V is contiguous in the packed A) and T upper triangular.  Per block one GEMM
-        // gives S = V^T V and W = V^T Z together, one warp builds T from S, W2 = T W, and a second GEMM applies
-        // Z^T -= W2^T V^T (stores along Z's rows).  Same 2 N^2 kv flops as reflector-by-reflector, but Z and the
-        // reflectors pass through the GEMM staging once per block instead of once per reflector and vector.
-        const int nref = N - 2;
-        double *Wm = wsf + pl.LU, *W2 = Wm + (size_t)16 * kv, *Sg = W2 + (size_t)16 * kv, *Tt = Sg + 256;
-        for (int k0 = ((nref - 1) / 16) * 16; k0 >= 0; k0 -= 16) {
-            const int nbk = min(16, nref - k0), m0 = N - k0 - 1;
-            auto V = [&](int i, int c) -> double { return i < c ? 0.0 : (i == c ? 1.0 : A[plo(k0 + 1 + i, k0 + c)]); };
-            tgemm<false, true>(nbk, 16 + kv, m0, [&](int c, int i) { return V(i, c); },
-                               [&](int i, int j) { return j < 16 ? (j < nbk ? V(i, j) : 0.0) : Z[(size_t)(j - 16) * ldz + k0 + 1 + i]; },
-                               false, sm, [&](int c, int j, double v) {
-                                   if (j < 16) Sg[c * 16 + j] = v;
-                                   else Wm[(size_t)c * kv + (j - 16)] = v;
-                               });
-            if (w == 0) {   // T(c, c) = tau_c;  T(0:c, c) = -tau_c T(0:c, 0:c) S(0:c, c)
-                for (int c = 0; c < nbk; c++) {
-                    const double tau = sm.tau[k0 + c];
-                    double t = 0.0;
-                    if (lane < c) {
-                        for (int j = lane; j < c; j++) t = fma(Tt[lane * 16 + j], Sg[j * 16 + c], t);
-                        t *= -tau;
-                    }
-                    __syncwarp();
-                    if (lane < 16) Tt[lane * 16 + c] = lane < c ? t : (lane == c ? tau : 0.0);
-                    __syncwarp();
-                }
-            }
-            __syncthreads();
-            for (int e = tid; e < nbk * kv; e += PDG_BLOCK) {
-                const int c = e / kv, t = e % kv;
-                double acc = 0.0;
-                for (int j = c; j < nbk; j++) acc = fma(Tt[c * 16 + j], Wm[(size_t)j * kv + t], acc);
-                W2[(size_t)c * kv + t] = acc;
-            }
-            __syncthreads();
-            tgemm<false, true>(kv, m0, nbk, [&](int t, int c) { return W2[(size_t)c * kv + t]; }, [&](int c, int i) { return V(i, c); },
-                               false, sm, [&](int t, int i, double v) { Z[(size_t)t * ldz + k0 + 1 + i] -= v; });
-        }
-    } else {
-        // reflector by reflector, one warp per vector
-        for (int t = w; t < kv; t += PDG_WARPS) {
-            double *zt = Z + (size_t)t * ldz;
-            for (int k = N - 3; k >= 0; k--) {
-                const double tau = sm.tau[k];
-                if (tau == 0.0) continue;
-                const int m = N - k - 1;
-                double dt = 0.0;
-                for (int i = lane; i < m; i += 32) dt = fma(i == 0 ? 1.0 : A[plo(k + 1 + i, k)], zt[k + 1 + i], dt);
-                dt = warp_sum(dt) * tau;
-                for (int i = lane; i < m; i += 32) zt[k + 1 + i] = fma(-dt, i == 0 ? 1.0 : A[plo(k + 1 + i, k)], zt[k + 1 + i]);
-                __syncwarp();
-            }
-        }
-        __syncthreads();
-    }
+    tridiag_vectors(a, wsf, A, sm, tm, s.vec_occupied ? 0 : N - kv, kv, Z, sm.zs != nullptr);
     tm.lap(PDG_T_BACKTRANSFORM);
     // --- P = 2 Z^T Z (occupied) or 2 (1 - Z^T Z) (virtual); lower triangle then mirrored
     const bool occ = s.vec_occupied;
@@ -690,6 +779,131 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
     });
     const double out = sqrt(block_sum(rms, sm.red)) / (double)N;
     tm.lap(PDG_T_DENSITY);
+    if (make_base) {
+        // base of the following perturbative steps: this step's matrix, density, wanted vectors and, from a second
+        // pass over the same tridiagonal form, the complementary eigenvectors; all eigenvalues (wanted first)
+        const int nc = N - kv;
+        double *BF = wsf + pl.BF, *BP = wsf + pl.BP, *BZ = wsf + pl.BZ, *BV = wsf + pl.BV, *BL = wsf + pl.BL;
+        for (size_t k = tid; k < (size_t)N * N; k += PDG_BLOCK) { BF[k] = F[k]; BP[k] = P[k]; }
+        for (int e = tid; e < kv * N; e += PDG_BLOCK) BZ[(size_t)(e / N) * ldz + e % N] = Z[(size_t)(e / N) * ldz + e % N];
+        for (int t = tid; t < kv; t += PDG_BLOCK) BL[t] = sm.eig[t];
+        __syncthreads();
+        if (nc > 0) {
+            tridiag_vectors(a, wsf, A, sm, tm, s.vec_occupied ? kv : 0, nc, BV, false, false);
+            for (int t = tid; t < nc; t += PDG_BLOCK) BL[kv + t] = sm.eig[t];
+        }
+        __syncthreads();
+        tm.lap(PDG_T_PERT_BASE);
+    }
+    return out;
+}
+
+// ----------------------------------------------------------------------------------------------------
+// Perturbative density step (mixed method; no counterpart in the reference).  The last FP64 step left a base:
+// its matrix F0, density P0, wanted eigenvectors Z0 (kv rows) with eigenvalues lambda, and the complementary
+// eigenvectors V (nc = N - kv rows) with eigenvalues mu, all exact to FP64 round-off.  For the new matrix
+// F = F0 + dF, the wanted invariant subspace is spanned by the rows of Z0 + K^T V, where K (nc x kv) solves the
+// Riccati equation of block diagonalisation in the basis [Z0; V]:
+//     E + M' K - K L' - K (E^T K) = (lambda_a - mu_i) K_ia,   E = V dF Z0^T,  M' = V dF V^T,  L' = Z0 dF Z0^T,
+// solved by fixed-point iteration from K = E / (lambda_a - mu_i) (first-order perturbation theory).  The new
+// projector differs from Z0^T Z0 by dQ = Z0^T W + Y^T (Z0 + W), with Y = K^T V, U = -K^T K ((1 + K^T K)^-1 to
+// second order) and W = Y + U (Z0 + Y); P = P0 + 2 dQ (occupied vectors) or P0 - 2 dQ (virtual).  Every FP32
+// product here has a small factor (dF, K, Y, W), so its rounding error is ~1e-7 of a small quantity; only P0
+// (FP64) carries the full magnitude.  Returns the RMS change of P, or -1 without touching P when the base no
+// longer carries the step (the iteration does not settle, or K is not small): the caller then runs an FP64 step,
+// which makes a new base.
+__device__ double density_step_pert(const SCFArgs &a, double *wsf, const double *F, double *P, Smem &sm, Timer &tm)
+{
+    const DeviceSystem &s = a.s;
+    const FramePlan &pl = a.plan;
+    const int N = s.n_basis, kv = s.n_vec, nc = N - kv, ldz = sm.ldz, tid = threadIdx.x;
+    const double *BF = wsf + pl.BF, *BP = wsf + pl.BP, *BZ = wsf + pl.BZ, *BV = wsf + pl.BV, *BL = wsf + pl.BL;
+    float *D = (float *)(wsf + pl.BW), *T1 = D + (size_t)N * N, *E = T1 + (size_t)N * kv, *Lp = E + (size_t)nc * kv;
+    float *T2 = Lp + (size_t)kv * kv, *Mp = T2 + (size_t)N * nc, *K = Mp + (size_t)nc * nc, *K2 = K + (size_t)nc * kv;
+    float *EK = K2 + (size_t)nc * kv, *U = EK + (size_t)kv * kv, *Y = U + (size_t)kv * kv, *Wz = Y + (size_t)kv * N;
+    float *DQ = Wz + (size_t)kv * N;
+    if (nc <= 0) return -1.0;
+    for (size_t k = tid; k < (size_t)N * N; k += PDG_BLOCK) D[k] = (float)(F[k] - BF[k]);
+    __syncthreads();
+    auto Zf = [&](int t, int i) { return (float)BZ[(size_t)t * ldz + i]; };
+    auto Vf = [&](int j, int i) { return (float)BV[(size_t)j * ldz + i]; };
+    // T1 = dF Z0^T (N x kv);  E = V T1 (nc x kv);  L' = Z0 T1 (kv x kv)
+    tgemm32<true, true>(N, kv, N, [&](int i, int k) { return D[(size_t)i * N + k]; }, [&](int k, int t) { return Zf(t, k); }, false, sm,
+                      [&](int i, int t, double v) { T1[(size_t)i * kv + t] = (float)v; });
+    tgemm32<true, false>(nc, kv, N, [&](int j, int k) { return Vf(j, k); }, [&](int k, int t) { return T1[(size_t)k * kv + t]; }, false, sm,
+                       [&](int j, int t, double v) { E[(size_t)j * kv + t] = (float)v; });
+    tgemm32<true, false>(kv, kv, N, [&](int b, int k) { return Zf(b, k); }, [&](int k, int t) { return T1[(size_t)k * kv + t]; }, false, sm,
+                       [&](int b, int t, double v) { Lp[(size_t)b * kv + t] = (float)v; });
+    // T2 = dF V^T (N x nc);  M' = V T2 (nc x nc)
+    tgemm32<true, true>(N, nc, N, [&](int i, int k) { return D[(size_t)i * N + k]; }, [&](int k, int j) { return Vf(j, k); }, false, sm,
+                      [&](int i, int j, double v) { T2[(size_t)i * nc + j] = (float)v; });
+    tgemm32<true, false>(nc, nc, N, [&](int j, int k) { return Vf(j, k); }, [&](int k, int l) { return T2[(size_t)k * nc + l]; }, false, sm,
+                       [&](int j, int l, double v) { Mp[(size_t)j * nc + l] = (float)v; });
+    // K from first-order theory, then the fixed-point iteration (each sweep one GEMM over [M' | -K] [K ; L' + E^T K])
+    for (int e = tid; e < nc * kv; e += PDG_BLOCK) {
+        const int j = e / kv, t = e % kv;
+        K[e] = (float)((double)E[e] / (BL[t] - BL[kv + j]));
+    }
+    __syncthreads();
+    bool settled = false;
+    double kmax = 0.0;
+    for (int it = 0; it < 12 && !settled; it++) {
+        tgemm32<false, false>(kv, kv, nc, [&](int b, int j) { return E[(size_t)j * kv + b]; }, [&](int j, int t) { return K[(size_t)j * kv + t]; },
+                            false, sm, [&](int b, int t, double v) { EK[(size_t)b * kv + t] = (float)v; });
+        double dmax = 0.0, km = 0.0;
+        tgemm32<true, false>(nc, kv, nc + kv,
+            [&](int j, int k) { return k < nc ? Mp[(size_t)j * nc + k] : -K[(size_t)j * kv + (k - nc)]; },
+            [&](int k, int t) { return k < nc ? K[(size_t)k * kv + t] : Lp[(size_t)(k - nc) * kv + t] + EK[(size_t)(k - nc) * kv + t]; },
+            false, sm, [&](int j, int t, double v) {
+                const size_t e = (size_t)j * kv + t;
+                const float kn = (float)(((double)E[e] + v) / (BL[t] - BL[kv + j]));
+                K2[e] = kn;
+                dmax = fmax(dmax, fabs((double)kn - (double)K[e]));
+                km = fmax(km, fabs((double)kn));
+            });
+        dmax = block_max(dmax, sm.red); km = block_max(km, sm.red);
+        float *tmp = K; K = K2; K2 = tmp;
+        kmax = km;
+        settled = dmax <= 1.0e-5 * km + 1.0e-30;   // remaining error ~ (contraction) x this change
+    }
+    // |K| bounds the FP32 rounding carried into P (~1e-7 |K| per product): 2e-3 keeps it far below the SCF's
+    // 1e-8 density tolerance
+    if (!settled || !(kmax < 2.0e-3)) {
+        if (tid == 0) tm.slot[PDG_T_PERT_FALLBACKS] += 1.0;
+        tm.lap(PDG_T_PERT);
+        return -1.0;
+    }
+    // Y = K^T V (kv x N);  U = -K^T K (kv x kv)
+    tgemm32<false, false>(kv, N, nc, [&](int t, int j) { return K[(size_t)j * kv + t]; }, [&](int j, int i) { return Vf(j, i); }, false, sm,
+                        [&](int t, int i, double v) { Y[(size_t)t * N + i] = (float)v; });
+    // U = (1 + K^T K)^-1 - 1 = -A + A^2 + O(|K|^6), A = K^T K (kv x kv; EK holds A)
+    tgemm32<false, false>(kv, kv, nc, [&](int t, int j) { return K[(size_t)j * kv + t]; }, [&](int j, int b) { return K[(size_t)j * kv + b]; },
+                        false, sm, [&](int t, int b, double v) { EK[(size_t)t * kv + b] = (float)v; });
+    tgemm32<true, false>(kv, kv, kv, [&](int t, int j) { return EK[(size_t)t * kv + j]; }, [&](int j, int b) { return EK[(size_t)j * kv + b]; },
+                         false, sm, [&](int t, int b, double v) { U[(size_t)t * kv + b] = (float)(v - (double)EK[(size_t)t * kv + b]); });
+    // W = Y + U (Z0 + Y)
+    tgemm32<true, false>(kv, N, 2 * kv, [&](int t, int k) { return U[(size_t)t * kv + (k < kv ? k : k - kv)]; },
+                       [&](int k, int i) { return k < kv ? Zf(k, i) : Y[(size_t)(k - kv) * N + i]; }, false, sm,
+                       [&](int t, int i, double v) { Wz[(size_t)t * N + i] = (float)((double)Y[(size_t)t * N + i] + v); });
+    // dQ = Z0^T W + Y^T (Z0 + W) (symmetric; lower triangle) and P = P0 +- 2 dQ
+    const double c = s.vec_occupied ? 2.0 : -2.0;
+    double rms = 0.0;
+    tgemm32<false, false>(N, N, 2 * kv,
+        [&](int i, int k) { return k < kv ? Zf(k, i) : Y[(size_t)(k - kv) * N + i]; },
+        [&](int k, int j) { return k < kv ? Wz[(size_t)k * N + j] : Zf(k - kv, j) + Wz[(size_t)(k - kv) * N + j]; },
+        true, sm, [&](int i, int j, double v) {
+            if (j > i) return;
+            const double pn = BP[(size_t)i * N + j] + c * v;
+            const double dlt = pn - P[(size_t)i * N + j];
+            rms += (i == j) ? dlt * dlt : 2.0 * dlt * dlt;
+            P[(size_t)i * N + j] = pn;
+            P[(size_t)j * N + i] = pn;
+            DQ[(size_t)i * N + j] = (float)v;
+            DQ[(size_t)j * N + i] = (float)v;
+        });
+    const double out = sqrt(block_sum(rms, sm.red)) / (double)N;
+    if (tid == 0) tm.slot[PDG_T_PERT_STEPS] += 1.0;
+    tm.lap(PDG_T_PERT);
     return out;
 }
 
@@ -1029,12 +1243,13 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
     __syncthreads();
     int ncyc = 0;
     bool have_z = false;   // P is the density of the vectors in Z
+    bool have_pert = false, base_ok = false;   // P is a perturbative step's density; the base of those steps is valid
     // Mixed method: the Fock matrix of the last FP64 density step (the extrapolated one, still in F when the loop
     // comes round), kept so that the next DIIS save can form its commutator from the small difference F - F~
     double *Ft = wsf + pl.A;
     const bool delta_commutator = o.density_step != 0;
     while (iteration < o.maximum_scf_cycles && !converged) {
-        if (delta_commutator && have_z) {
+        if (delta_commutator && (have_z || have_pert)) {
             for (size_t k = tid; k < NN; k += PDG_BLOCK) Ft[k] = F[k];
             __syncthreads();
         }
@@ -1060,10 +1275,12 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
             for (int i = tid / 32; i < N; i += PDG_WARPS)
                 for (int j = tid % 32; j <= i; j += 32) { hp[i * (i + 1) / 2 + j] = P[(size_t)i * N + j]; hf[i * (i + 1) / 2 + j] = F[(size_t)i * N + j]; }
             double emx = 0.0;
-            if (have_z) {
+            if (have_z || have_pert) {
                 // P = 2 Z^T Z (occupied) or 2 (1 - Z^T Z) (virtual) with the vectors Z of the last density step,
                 // so with G = Z F:  F P - P F = sg (G^T Z - Z^T G), sg = +2 / -2.  2 N^2 kv FMA instead of N^3.
-                const double *Zc = sm.zs ? sm.zs : wsf + pl.Z;
+                // After a perturbative step P = P0 + c dQ with P0 the base's projector (Z = the base vectors):
+                // F P - P F = [dF, P0] + c [dF, dQ], dF = F - F~, the second term from one more FP32 product.
+                const double *Zc = have_pert ? wsf + pl.BZ : (sm.zs ? sm.zs : wsf + pl.Z);
                 const int ldz = sm.ldz, kv = s.n_vec;
                 const double sg = s.vec_occupied ? 2.0 : -2.0;
                 auto store = [&](int i, int j, double v) {
@@ -1076,13 +1293,29 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
                     // mixed method: P commutes with F~ (the matrix it was made from), so F P - P F = dF P - P dF with
                     // dF = F - F~, small once the SCF settles; its products in FP32 carry errors ~1e-7 |dF|.
                     float *G32 = (float *)(wsf + pl.G);
-                    tgemm<true, false>(kv, N, N, [&](int t, int k) { return (float)Zc[(size_t)t * ldz + k]; },
+                    tgemm32<true, false>(kv, N, N, [&](int t, int k) { return (float)Zc[(size_t)t * ldz + k]; },
                                        [&](int k, int i) { return (float)(F[(size_t)k * N + i] - Ft[(size_t)k * N + i]); },
-                                       false, sm, [&](int t, int i, double v) { G32[(size_t)t * N + i] = (float)v; }, 0.0f);
-                    tgemm<false, false>(N, N, 2 * kv,
-                        [&](int i, int k) { return k < kv ? G32[(size_t)k * N + i] : (float)Zc[(size_t)(k - kv) * ldz + i]; },
-                        [&](int k, int j) { return k < kv ? (float)Zc[(size_t)k * ldz + j] : -G32[(size_t)(k - kv) * N + j]; },
-                        true, sm, store, 0.0f);
+                                       false, sm, [&](int t, int i, double v) { G32[(size_t)t * N + i] = (float)v; });
+                    if (have_pert) {
+                        // X = dF dQ (FP32, N x N, into the perturbative work's dF slot), then the commutator adds
+                        // c (X - X^T) to the base part
+                        float *DQ = (float *)(wsf + pl.BW) + pert_dq_offset(N, kv), *X = (float *)(wsf + pl.BW);
+                        tgemm32<true, false>(N, N, N, [&](int i, int k) { return (float)(F[(size_t)i * N + k] - Ft[(size_t)i * N + k]); },
+                                           [&](int k, int j) { return DQ[(size_t)k * N + j]; }, false, sm,
+                                           [&](int i, int j, double v) { X[(size_t)i * N + j] = (float)v; });
+                        const double cq = s.vec_occupied ? 2.0 : -2.0;
+                        tgemm32<false, false>(N, N, 2 * kv,
+                            [&](int i, int k) { return k < kv ? G32[(size_t)k * N + i] : (float)Zc[(size_t)(k - kv) * ldz + i]; },
+                            [&](int k, int j) { return k < kv ? (float)Zc[(size_t)k * ldz + j] : -G32[(size_t)(k - kv) * N + j]; },
+                            true, sm, [&](int i, int j, double v) {
+                                if (j >= i) return;
+                                store(i, j, v + cq * ((double)X[(size_t)i * N + j] - (double)X[(size_t)j * N + i]) / sg);
+                            });
+                    } else
+                        tgemm32<false, false>(N, N, 2 * kv,
+                            [&](int i, int k) { return k < kv ? G32[(size_t)k * N + i] : (float)Zc[(size_t)(k - kv) * ldz + i]; },
+                            [&](int k, int j) { return k < kv ? (float)Zc[(size_t)k * ldz + j] : -G32[(size_t)(k - kv) * N + j]; },
+                            true, sm, store);
                 } else {
                     double *G = wsf + pl.G;
                     tgemm<true, false>(kv, N, N, [&](int t, int k) { return Zc[(size_t)t * ldz + k]; }, [&](int k, int i) { return F[(size_t)k * N + i]; },
@@ -1243,14 +1476,23 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
             rms = density_step_mixed(a, wsf, F, P, sm, tm, tc, o.density_step);
             if (rms < 0.0) { st = PDG_TENSOR_TIMEOUT; break; }
             last_mixed = true;
-            have_z = false;
+            have_z = false; have_pert = false;
             // leave purification once the density has settled to its accuracy, or when it stalls
             n_mixed++;
             if (rms < o.mixed_switch || n_mixed >= 20) mixed = false;
         } else {
-            rms = density_step(a, wsf, F, P, sm, tm);
+            double r = -1.0;
+            if (base_ok) r = density_step_pert(a, wsf, F, P, sm, tm);
+            if (r >= 0.0) {
+                rms = r;
+                have_z = false; have_pert = true;
+            } else {
+                // FP64 step; in the mixed method it also keeps the base of the following perturbative steps
+                rms = density_step(a, wsf, F, P, sm, tm, delta_commutator);
+                have_z = true; have_pert = false;
+                base_ok = delta_commutator;
+            }
             last_mixed = false;
-            have_z = true;
         }
         if (tid == 0 && ncyc <= PDG_RMS_HISTORY) tm.slot[PDG_T_RMS_HISTORY + ncyc - 1] = last_mixed ? -rms : rms;
         valid = true;
