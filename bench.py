@@ -93,6 +93,54 @@ def fp64_peak_tflops(dev, n=4096, reps=3):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
+def fp32_peak_tflops(dev, n=4096, reps=3):
+    """cuBLAS SGEMM throughput on the CUDA cores (TF32 off), best of reps: the FP32 peak of the mixed method's
+    FP32 products."""
+    import torch
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        a = torch.randn(n, n, dtype=torch.float32, device=dev)
+        b = torch.randn(n, n, dtype=torch.float32, device=dev)
+        torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(); torch.matmul(a, b); e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = old
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def scf_work(T, N, kv, frames, mixed):
+    """Algorithmic work of one k_scf launch (all frames) by unit, from the per-frame phase counts:
+    FP64 density steps (4/3) N^3 + 3 N^2 kv flops each, plus, when the step keeps a perturbative base, the
+    back-transformation of the nc = N - kv complementary vectors (2 N^2 nc); the plain method's DIIS saves after
+    FP64 steps 4 N^2 kv, its other saves 2 N^3.  Mixed method: FP32 flops of the perturbative steps (the coupling
+    blocks, the fixed-point sweeps, the new density), of its FP32 commutators (after FP64 and perturbative steps
+    the Z-form 4 N^2 kv plus 2 N^3 for dF dQ after a perturbative step; after purification steps 2 N^3), and the
+    split-BF16 SP2 products on the tensor cores (6 x 2 N^3 per SP2 iteration).  Returns flops (fp64, fp32, tensor)."""
+    nc = N - kv
+    fs = T["QC Densities Steps"].mean()
+    cyc = T["QC SCF Fock Builds"].mean()
+    if not mixed:
+        saves_z = max(fs - 1.0, 0.0)
+        f64 = fs * ((4.0 / 3.0) * N ** 3 + 3.0 * N * N * kv) + saves_z * 4.0 * N * N * kv + max(cyc - saves_z, 0.0) * 2.0 * N ** 3
+        return frames * f64, 0.0, 0.0
+    ps, sw = T["QC Densities Perturbative Steps"].mean(), T["QC Densities Perturbative Sweeps"].mean()
+    pur, sp2 = T["QC Densities Purification Steps"].mean(), T["QC Densities SP2 Iterations"].mean()
+    f64 = fs * ((4.0 / 3.0) * N ** 3 + 3.0 * N * N * kv + 2.0 * N * N * nc)
+    pert_fma = (N * N * kv + nc * N * kv + kv * N * kv + N * N * nc + nc * N * nc + kv * nc * N + kv * nc * kv + kv ** 3
+                + 2 * kv * kv * N + N * N * kv)
+    sweep_fma = kv * nc * kv + nc * (nc + kv) * kv
+    f32 = ps * 2.0 * pert_fma + sw * 2.0 * sweep_fma + (fs + ps) * 4.0 * N * N * kv + ps * 2.0 * N ** 3 + pur * 2.0 * N ** 3
+    tc = sp2 * 6 * 2.0 * N ** 3
+    return frames * f64, frames * f32, frames * tc
+
+
 def scf_cta_layout(eng, T):
     """Threads and shared memory of one SCF CTA, and how many CTAs (frames) the SMs actually ran at once,
     from the SM id and %globaltimer interval that every CTA records (pdg_scf_timings)."""
@@ -553,15 +601,29 @@ def main():
     fp64_steps = float(T["QC Densities Steps"].mean())
     pur_steps = float(T["QC Densities Purification Steps"].mean())
     ncyc_f = float(head["ncyc"].mean())
-    # FP64 roofline of k_scf.  Algorithmic FP64 flops per frame: every FP64 density step
-    # (4/3) N^3 tridiagonalisation + 2 N^2 kv back-transformation + N^2 kv density; every DIIS save after an
-    # FP64 step 4 N^2 kv (the commutator through the orbital factor); every other DIIS save the full 2 N^3.
-    fp64_saves = max(fp64_steps - 1.0, 0.0)
-    other_saves = max(ncyc_f - fp64_saves, 0.0)
-    scf_flops = len(frames) * (fp64_steps * ((4.0 / 3.0) * N ** 3 + 3.0 * N * N * kv) + fp64_saves * 4.0 * N * N * kv
-                               + (other_saves * 2.0 * N ** 3 if args.method == "fp64" else 0.0))
-    achieved_tf = scf_flops / (head["scf_ms"] * 1e-3) / 1e12
     fp64_peak = fp64_peak_tflops(dev)
+    fp32_peak = fp32_peak_tflops(dev)
+    bf16_peak = peaks().get("bf16_tflops", 1925.7)
+
+    def roofline(h, mixed):
+        """FP64 roofline of the method's k_scf (its FP64 algorithmic flops over the event-timed launch, against
+        cuBLAS DGEMM measured here) and, for the mixed method, the composite: the time its FP64, FP32 and tensor work
+        would take at the three measured peaks over the measured time."""
+        f64, f32, tc = scf_work(h["timers"], N, kv, len(frames), mixed)
+        t = h["scf_ms"] * 1e-3
+        r = {"bound": "fp64", "kernel": "k_scf", "achieved": f64 / t / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
+             "frac": f64 / t / 1e12 / fp64_peak, "traffic": None,
+             "note": "FP64 algorithmic flops of the density steps over the k_scf launch (%.2f ms, %d frames); peak = cuBLAS DGEMM "
+                     "4096^3 measured in this run (of measured; MEASURED_PEAKS.json has no FP64 figure)" % (h["scf_ms"], len(frames))}
+        if mixed:
+            t_ideal = f64 / (fp64_peak * 1e12) + f32 / (fp32_peak * 1e12) + tc / (bf16_peak * 1e12)
+            r["composite"] = {"t_ideal_ms": t_ideal * 1e3, "t_measured_ms": h["scf_ms"], "frac": t_ideal / t,
+                              "fp64_tflop": f64 / 1e12, "fp32_tflop": f32 / 1e12, "tensor_tflop": tc / 1e12,
+                              "fp32_peak_tflops": fp32_peak, "bf16_peak_tflops": bf16_peak,
+                              "note": "the mixed SCF spreads its work over the FP64 pipe (FP64 base steps), the FP32 pipe (perturbative "
+                                      "steps, commutators) and the tensor cores (SP2): time at the three measured peaks (FP32: cuBLAS "
+                                      "SGEMM 4096^3 without TF32, measured here; BF16: MEASURED_PEAKS.json) over the measured launch"}
+        return r
     clk = head["clk"]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -579,11 +641,7 @@ def main():
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(head["frames_h"].numel() * 8),
                     "d2h_bytes_per_step": int(head["G"].nbytes + len(frames) * (_native.NENERGY + 2) * 8)},
             "gpu_launches": 8 * args.steps,
-            "roofline": {"bound": "fp64", "kernel": "k_scf", "achieved": achieved_tf, "peak": fp64_peak, "unit": "TFLOP/s",
-                         "frac": achieved_tf / fp64_peak,
-                         "traffic": K_SCF_DRAM_BYTES_304 if (len(frames) == 304 and args.method == "fp64") else None,
-                         "note": "peak = cuBLAS DGEMM 4096^3 measured in this run (of measured; MEASURED_PEAKS.json has no FP64 figure); "
-                                 "k_scf %.2f ms per %d-frame launch, step %.2f ms" % (head["scf_ms"], len(frames), head["ms"])},
+            "roofline": roofline(head, args.method != "fp64"),
             "clocks": clk}
     if args.method != "fp64":
         # tensor-core part: SP2 iterations x k partial products x 2 N^3 algorithmic flops, over the purification
@@ -601,7 +659,7 @@ def main():
         dE = float(np.abs(head["E"] - plain["E"]).max()) / KJ
         dG = float(np.abs(head["G"] - plain["G"]).max()) / (KJ * 1.0e-10 / 5.291772083e-11)
         line["plain_fp64"] = {"value": n_total / (plain["ms"] * 1e-3), "ms_per_step": plain["ms"], "e2e": n_total / plain["e2e_s"],
-                              "mean_scf_cycles": float(plain["ncyc"].mean())}
+                              "mean_scf_cycles": float(plain["ncyc"].mean()), "roofline": roofline(plain, False)}
         if args.method == "learned_mixed":
             line["mixed"] = {"value": n_total / (mixed["ms"] * 1e-3), "ms_per_step": mixed["ms"], "e2e": n_total / mixed["e2e_s"],
                              "mean_scf_cycles": float(mixed["ncyc"].mean())}

@@ -173,7 +173,7 @@ int pdg_gradients_static_scratch(pdg_system *sys, int n_frames, const double *d_
  * timings of pMolecule.QCModel.pyx:208-275 (EnergyWithTimings: QC Fock, QC Converger Iterate,
  * QC Converger Densities), with the density step split into its parts.  d_out: n_frames * PDG_NTIMERS. */
 #define PDG_RMS_HISTORY 40
-#define PDG_NTIMERS (27 + PDG_RMS_HISTORY)
+#define PDG_NTIMERS (31 + PDG_RMS_HISTORY)
 enum {
     PDG_T_FOCK = 0, PDG_T_DIIS_SAVE = 1, PDG_T_ITERATE = 2, PDG_T_TRIDIAGONAL = 3, PDG_T_EIGENVALUES = 4,
     PDG_T_EIGENVECTORS = 5, PDG_T_BACKTRANSFORM = 6, PDG_T_DENSITY = 7, PDG_T_TOTAL = 8, PDG_T_CYCLES = 9,
@@ -193,8 +193,12 @@ enum {
     PDG_T_PERT = 23,           /* cycles of the perturbative density steps (mixed method), */
     PDG_T_PERT_STEPS = 24,     /* their count, */
     PDG_T_PERT_BASE = 25,      /* the cycles the FP64 steps spent keeping their base (the complement vectors), */
-    PDG_T_PERT_FALLBACKS = 26, /* and the count of perturbative steps that handed over to an FP64 step */
-    PDG_T_RMS_HISTORY = 27     /* PDG_RMS_HISTORY entries: RMS density change of each density step, in SCF cycle
+    PDG_T_PERT_FALLBACKS = 26, /* the count of perturbative steps that handed over to an FP64 step, */
+    PDG_T_PERT_SWEEPS = 27,    /* the count of their fixed-point sweeps, and their cycles in: */
+    PDG_T_PERT_COUPLING = 28,  /* the coupling blocks E, L', M' from dF, */
+    PDG_T_PERT_SOLVE = 29,     /* the fixed-point sweeps, */
+    PDG_T_PERT_DENSITY = 30,   /* the new density */
+    PDG_T_RMS_HISTORY = 31     /* PDG_RMS_HISTORY entries: RMS density change of each density step, in SCF cycle
                                   order, negative for purification steps, 0 beyond the last */
 };
 int pdg_scf_timings(const pdg_system *sys, int n_frames, const void *d_workspace, size_t workspace_bytes,

@@ -27,7 +27,8 @@ TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densi
           "QC Densities Purification Steps", "QC Densities SP2 Iterations", "SM", "Start ns", "End ns", "QC Densities Purification Products",
           "QC Densities Purification Readout", "QC Densities Purification Control", "QC Densities Purification Setup",
           "QC Densities Purification Finish", "QC Densities Perturbative", "QC Densities Perturbative Steps",
-          "QC Densities Perturbative Base", "QC Densities Perturbative Fallbacks") + tuple("RMS %d" % k for k in range(40))
+          "QC Densities Perturbative Base", "QC Densities Perturbative Fallbacks", "QC Densities Perturbative Sweeps",
+          "QC Densities Perturbative Coupling", "QC Densities Perturbative Solve", "QC Densities Perturbative Density") + tuple("RMS %d" % k for k in range(40))
 
 
 class SCFOptions(ctypes.Structure):

@@ -52,11 +52,15 @@ __host__ __device__ inline size_t align32(size_t x) { return (x + 31) & ~size_t(
 
 // FP32 work of a perturbative density step (floats): dF (N x N), dF Z^T (N x kv), E (nc x kv), Lambda' (kv x kv),
 // dF V^T (N x nc), M' (nc x nc), K and its next iterate (nc x kv each), E^T K and U (kv x kv each), Y and W
-// (kv x N each), dQ (N x N).
+// (kv x N each), dQ (N x N), then (from pert_dq_offset + N^2) the DIIS save's F - F~ (N x N) and the base's
+// wanted and complement vectors rounded to FP32 (kv rows of N, then nc rows of N), and the reciprocal eigenvalue
+// gaps 1 / (lambda_a - mu_i) (nc x kv).
 __host__ __device__ inline size_t pert_work_floats(int N, int kv)
 {
     const size_t n = N, k = kv, c = N - kv;
-    return 2 * n * n + n * k + n * c + 3 * c * k + 3 * k * k + c * c + 2 * k * n + 64;
+    return 2 * n * n + n * k + n * c + 3 * c * k + 3 * k * k + c * c + 2 * k * n + 64
+         + n * n + (k + c) * n    // + dF of the DIIS save (N x N), the base vectors in FP32 (kv + nc rows of N)
+         + c * k;                 // + 1 / (lambda_a - mu_i) (nc x kv)
 }
 
 // Offset (floats) of dQ in that work.

@@ -793,6 +793,13 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
             for (int t = tid; t < nc; t += PDG_BLOCK) BL[kv + t] = sm.eig[t];
         }
         __syncthreads();
+        // the same vectors rounded to FP32, the operands of the products with small factors
+        float *Zf = (float *)(wsf + pl.BW) + pert_dq_offset(N, kv) + 2 * (size_t)N * N, *Vf = Zf + (size_t)kv * N;
+        for (int e = tid; e < kv * N; e += PDG_BLOCK) Zf[e] = (float)BZ[(size_t)(e / N) * ldz + e % N];
+        for (int e = tid; e < nc * N; e += PDG_BLOCK) Vf[e] = (float)BV[(size_t)(e / N) * ldz + e % N];
+        float *Gi = Vf + (size_t)nc * N;   // reciprocal gaps, the fixed-point sweeps' divisors
+        for (int e = tid; e < nc * kv; e += PDG_BLOCK) Gi[e] = (float)(1.0 / (BL[e % kv] - BL[kv + e / kv]));
+        __syncthreads();
         tm.lap(PDG_T_PERT_BASE);
     }
     return out;
@@ -823,10 +830,12 @@ __device__ double density_step_pert(const SCFArgs &a, double *wsf, const double 
     float *EK = K2 + (size_t)nc * kv, *U = EK + (size_t)kv * kv, *Y = U + (size_t)kv * kv, *Wz = Y + (size_t)kv * N;
     float *DQ = Wz + (size_t)kv * N;
     if (nc <= 0) return -1.0;
+    const long long t_coupling = tm.now();
     for (size_t k = tid; k < (size_t)N * N; k += PDG_BLOCK) D[k] = (float)(F[k] - BF[k]);
     __syncthreads();
-    auto Zf = [&](int t, int i) { return (float)BZ[(size_t)t * ldz + i]; };
-    auto Vf = [&](int j, int i) { return (float)BV[(size_t)j * ldz + i]; };
+    const float *Z32 = DQ + 2 * (size_t)N * N, *V32 = Z32 + (size_t)kv * N, *Gi = V32 + (size_t)nc * N;
+    auto Zf = [&](int t, int i) { return Z32[(size_t)t * N + i]; };
+    auto Vf = [&](int j, int i) { return V32[(size_t)j * N + i]; };
     // T1 = dF Z0^T (N x kv);  E = V T1 (nc x kv);  L' = Z0 T1 (kv x kv)
     tgemm32<true, true>(N, kv, N, [&](int i, int k) { return D[(size_t)i * N + k]; }, [&](int k, int t) { return Zf(t, k); }, false, sm,
                       [&](int i, int t, double v) { T1[(size_t)i * kv + t] = (float)v; });
@@ -839,36 +848,38 @@ __device__ double density_step_pert(const SCFArgs &a, double *wsf, const double 
                       [&](int i, int j, double v) { T2[(size_t)i * nc + j] = (float)v; });
     tgemm32<true, false>(nc, nc, N, [&](int j, int k) { return Vf(j, k); }, [&](int k, int l) { return T2[(size_t)k * nc + l]; }, false, sm,
                        [&](int j, int l, double v) { Mp[(size_t)j * nc + l] = (float)v; });
+    tm.add(PDG_T_PERT_COUPLING, t_coupling);
+    const long long t_solve = tm.now();
     // K from first-order theory, then the fixed-point iteration (each sweep one GEMM over [M' | -K] [K ; L' + E^T K])
-    for (int e = tid; e < nc * kv; e += PDG_BLOCK) {
-        const int j = e / kv, t = e % kv;
-        K[e] = (float)((double)E[e] / (BL[t] - BL[kv + j]));
-    }
+    for (int e = tid; e < nc * kv; e += PDG_BLOCK) K[e] = E[e] * Gi[e];
     __syncthreads();
     bool settled = false;
-    double kmax = 0.0;
+    float kmax = 0.f;
     for (int it = 0; it < 12 && !settled; it++) {
         tgemm32<false, false>(kv, kv, nc, [&](int b, int j) { return E[(size_t)j * kv + b]; }, [&](int j, int t) { return K[(size_t)j * kv + t]; },
                             false, sm, [&](int b, int t, double v) { EK[(size_t)b * kv + t] = (float)v; });
-        double dmax = 0.0, km = 0.0;
+        float dmax = 0.f, km = 0.f;
         tgemm32<true, false>(nc, kv, nc + kv,
             [&](int j, int k) { return k < nc ? Mp[(size_t)j * nc + k] : -K[(size_t)j * kv + (k - nc)]; },
             [&](int k, int t) { return k < nc ? K[(size_t)k * kv + t] : Lp[(size_t)(k - nc) * kv + t] + EK[(size_t)(k - nc) * kv + t]; },
             false, sm, [&](int j, int t, double v) {
                 const size_t e = (size_t)j * kv + t;
-                const float kn = (float)(((double)E[e] + v) / (BL[t] - BL[kv + j]));
+                const float kn = (E[e] + (float)v) * Gi[e];
                 K2[e] = kn;
-                dmax = fmax(dmax, fabs((double)kn - (double)K[e]));
-                km = fmax(km, fabs((double)kn));
+                dmax = fmaxf(dmax, fabsf(kn - K[e]));
+                km = fmaxf(km, fabsf(kn));
             });
-        dmax = block_max(dmax, sm.red); km = block_max(km, sm.red);
+        dmax = (float)block_max((double)dmax, sm.red); km = (float)block_max((double)km, sm.red);
         float *tmp = K; K = K2; K2 = tmp;
         kmax = km;
-        settled = dmax <= 1.0e-5 * km + 1.0e-30;   // remaining error ~ (contraction) x this change
+        settled = dmax <= 1.0e-5f * km + 1.0e-30f;   // remaining error ~ (contraction) x this change
+        if (tid == 0) tm.slot[PDG_T_PERT_SWEEPS] += 1.0;
     }
+    tm.add(PDG_T_PERT_SOLVE, t_solve);
+    const long long t_density = tm.now();
     // |K| bounds the FP32 rounding carried into P (~1e-7 |K| per product): 2e-3 keeps it far below the SCF's
     // 1e-8 density tolerance
-    if (!settled || !(kmax < 2.0e-3)) {
+    if (!settled || !(kmax < 2.0e-3f)) {
         if (tid == 0) tm.slot[PDG_T_PERT_FALLBACKS] += 1.0;
         tm.lap(PDG_T_PERT);
         return -1.0;
@@ -902,6 +913,7 @@ __device__ double density_step_pert(const SCFArgs &a, double *wsf, const double 
             DQ[(size_t)j * N + i] = (float)v;
         });
     const double out = sqrt(block_sum(rms, sm.red)) / (double)N;
+    tm.add(PDG_T_PERT_DENSITY, t_density);
     if (tid == 0) tm.slot[PDG_T_PERT_STEPS] += 1.0;
     tm.lap(PDG_T_PERT);
     return out;
@@ -1291,30 +1303,35 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
                 };
                 if (delta_commutator) {
                     // mixed method: P commutes with F~ (the matrix it was made from), so F P - P F = dF P - P dF with
-                    // dF = F - F~, small once the SCF settles; its products in FP32 carry errors ~1e-7 |dF|.
+                    // dF = F - F~, small once the SCF settles; its products in FP32 carry errors ~1e-7 |dF|.  Every
+                    // FP64 step of the mixed method keeps a base, so Z is the base's vectors, also held in FP32.
                     float *G32 = (float *)(wsf + pl.G);
-                    tgemm32<true, false>(kv, N, N, [&](int t, int k) { return (float)Zc[(size_t)t * ldz + k]; },
-                                       [&](int k, int i) { return (float)(F[(size_t)k * N + i] - Ft[(size_t)k * N + i]); },
+                    float *DF = (float *)(wsf + pl.BW) + pert_dq_offset(N, kv) + (size_t)N * N;
+                    const float *Z32 = DF + (size_t)N * N;
+                    for (size_t k = tid; k < NN; k += PDG_BLOCK) DF[k] = (float)(F[k] - Ft[k]);
+                    __syncthreads();
+                    tgemm32<true, false>(kv, N, N, [&](int t, int k) { return Z32[(size_t)t * N + k]; },
+                                       [&](int k, int i) { return DF[(size_t)k * N + i]; },
                                        false, sm, [&](int t, int i, double v) { G32[(size_t)t * N + i] = (float)v; });
                     if (have_pert) {
                         // X = dF dQ (FP32, N x N, into the perturbative work's dF slot), then the commutator adds
                         // c (X - X^T) to the base part
                         float *DQ = (float *)(wsf + pl.BW) + pert_dq_offset(N, kv), *X = (float *)(wsf + pl.BW);
-                        tgemm32<true, false>(N, N, N, [&](int i, int k) { return (float)(F[(size_t)i * N + k] - Ft[(size_t)i * N + k]); },
+                        tgemm32<true, false>(N, N, N, [&](int i, int k) { return DF[(size_t)i * N + k]; },
                                            [&](int k, int j) { return DQ[(size_t)k * N + j]; }, false, sm,
                                            [&](int i, int j, double v) { X[(size_t)i * N + j] = (float)v; });
                         const double cq = s.vec_occupied ? 2.0 : -2.0;
                         tgemm32<false, false>(N, N, 2 * kv,
-                            [&](int i, int k) { return k < kv ? G32[(size_t)k * N + i] : (float)Zc[(size_t)(k - kv) * ldz + i]; },
-                            [&](int k, int j) { return k < kv ? (float)Zc[(size_t)k * ldz + j] : -G32[(size_t)(k - kv) * N + j]; },
+                            [&](int i, int k) { return k < kv ? G32[(size_t)k * N + i] : Z32[(size_t)(k - kv) * N + i]; },
+                            [&](int k, int j) { return k < kv ? Z32[(size_t)k * N + j] : -G32[(size_t)(k - kv) * N + j]; },
                             true, sm, [&](int i, int j, double v) {
                                 if (j >= i) return;
                                 store(i, j, v + cq * ((double)X[(size_t)i * N + j] - (double)X[(size_t)j * N + i]) / sg);
                             });
                     } else
                         tgemm32<false, false>(N, N, 2 * kv,
-                            [&](int i, int k) { return k < kv ? G32[(size_t)k * N + i] : (float)Zc[(size_t)(k - kv) * ldz + i]; },
-                            [&](int k, int j) { return k < kv ? (float)Zc[(size_t)k * ldz + j] : -G32[(size_t)(k - kv) * N + j]; },
+                            [&](int i, int k) { return k < kv ? G32[(size_t)k * N + i] : Z32[(size_t)(k - kv) * N + i]; },
+                            [&](int k, int j) { return k < kv ? Z32[(size_t)k * N + j] : -G32[(size_t)(k - kv) * N + j]; },
                             true, sm, store);
                 } else {
                     double *G = wsf + pl.G;
