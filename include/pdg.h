@@ -216,7 +216,10 @@ int pdg_qcmm_potentials(int model, int n_frames, int n_qc, int n_mm, const doubl
                         double outer_cutoff, double *d_phi, void *stream);
 /* Gradients (Eh/Bohr) of q_A phi_A with respect to QC and MM coordinates for given QC charges.
  * d_qc_grad (n_frames*n_qc*3) and d_mm_grad (n_frames*n_mm*3) are overwritten; d_mm_grad may be NULL, and the
- * MM-side gradients are then not computed (dynamics with the MM atoms fixed never uses them). */
+ * MM-side gradients are then not computed (dynamics with the MM atoms fixed never uses them).
+ * model | PDG_QCMM_FP32_PAIRS evaluates the pair terms in FP32 (per-atom sums in FP64; errors ~1e-7 Hartree/Bohr,
+ * used by the mixed method; the reference's arithmetic is FP64, which is the default here). */
+#define PDG_QCMM_FP32_PAIRS 0x100
 int pdg_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const double *d_qc_xyz,
                        const double *d_mm_xyz, const double *d_mm_charges, const double *d_qc_charges,
                        int n_knots, const double *d_knots, double outer_cutoff,

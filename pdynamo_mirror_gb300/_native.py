@@ -13,6 +13,7 @@ PDG_OK, PDG_NOT_CONVERGED, PDG_NAN, PDG_DIIS_SINGULAR, PDG_BAD_ARGUMENT, PDG_CUD
 NENERGY = 8
 EN_TOTAL_ELECTRONIC, EN_ELECTRONIC, EN_NUCLEAR, EN_BASELINE, EN_QCMM, EN_ONE_ELECTRON, EN_TWO_ELECTRON, EN_RMS_DENSITY = range(8)
 MAX_HISTORY = 16
+QCMM_FP32_PAIRS = 0x100   # pdg_qcmm_gradients model flag: FP32 pair terms (the mixed method)
 
 EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system_info", "pdg_workspace_bytes",
            "pdg_energy_gradients", "pdg_scf", "pdg_density", "pdg_one_electron", "pdg_fock", "pdg_gradients", "pdg_qcmm_potentials",

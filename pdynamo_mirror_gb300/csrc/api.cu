@@ -305,9 +305,11 @@ extern "C" int pdg_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, c
                                   const double *q, const double *qcq, int n_knots, const double *knots, double cutoff,
                                   double *gqc, double *gmm, void *stream)
 {
-    if (model != 0 && model != 1) return fail(PDG_BAD_ARGUMENT, "model must be 0 (full) or 1 (ABFS)");
+    const int base_model = model & ~PDG_QCMM_FP32_PAIRS;
+    if ((base_model != 0 && base_model != 1) || (model & ~(PDG_QCMM_FP32_PAIRS | 1))) return fail(PDG_BAD_ARGUMENT, "model must be 0 (full) or 1 (ABFS), optionally | PDG_QCMM_FP32_PAIRS");
+    if (model & PDG_QCMM_FP32_PAIRS && base_model == 1 && n_knots > 1024) return fail(PDG_TOO_LARGE, "FP32 pair terms take at most 1024 spline knots");
     if (n_frames <= 0 || n_qc <= 0 || n_mm < 0 || !qc || !qcq || !gqc || (n_mm > 0 && (!mm || !q))) return fail(PDG_BAD_ARGUMENT, "bad sizes or null pointers");
-    if (model == 1 && (n_knots < 2 || !knots || cutoff <= 0.0)) return fail(PDG_BAD_ARGUMENT, "ABFS needs spline knots and a cutoff");
+    if (base_model == 1 && (n_knots < 2 || !knots || cutoff <= 0.0)) return fail(PDG_BAD_ARGUMENT, "ABFS needs spline knots and a cutoff");
     launch_qcmm_gradients(model, n_frames, n_qc, n_mm, qc, mm, q, qcq, n_knots, knots, cutoff, gqc, gmm, (cudaStream_t)stream);
     return cuda_check(cudaGetLastError(), "qcmm gradients");
 }

@@ -232,6 +232,191 @@ __global__ void __launch_bounds__(MB) k_qcmm_grad_mm(int model, Spline sp, int n
     }
 }
 
+// ---------------------------------------------------------------------------------------------------
+// FP32 pair terms for the gradients (the mixed method; model | PDG_QCMM_FP32_PAIRS).  A gradient pair term is
+// up to ~0.1 Eh/Bohr at the closest contacts; in FP32 (coordinates, r^2 and the spline, with the knot value
+// differences formed in FP64) each carries ~1e-7 relative, and the per-atom sums stay near 1e-7 Eh/Bohr, two
+// orders inside the 1e-5 gate.  Lane partial sums are FP32, the sums over lanes FP64.
+// Coordinates, charges and knots are staged in FP32 shared memory and the queues carry FP32 coordinates, so no
+// FP64 instruction runs per pair.
+#define KMAX32 1024
+// knots x, second derivatives h, and the value differences y_{l+1} - y_l taken in FP64 before rounding (the
+// differences of neighbouring FP32 values would lose ~1e-5 relative where 1/r is large)
+struct Knots32 { float x[KMAX32], dy[KMAX32], h[KMAX32]; };
+
+__device__ __forceinline__ void stage_knots32(const Spline &sp, Knots32 &k)
+{
+    for (int i = threadIdx.x; i < sp.n; i += blockDim.x) {
+        k.x[i] = (float)sp.x[i]; k.h[i] = (float)sp.h[i];
+        k.dy[i] = i + 1 < sp.n ? (float)(sp.y[i + 1] - sp.y[i]) : 0.0f;
+    }
+}
+
+// df/d(r^2) in FP32 (per A^2, a.u. per unit charges); false beyond the cutoff
+__device__ __forceinline__ bool pair_grad32(int model, const Spline &sp, const Knots32 &k, float r2, float &g)
+{
+    if (model == 1) {
+        if (r2 > (float)sp.r2off) return false;
+        const int n = sp.n;
+        int l = (int)(sqrtf(r2) / (float)sp.inc);
+        l = max(0, min(l, n - 2));
+        while (l > 0 && k.x[l] > r2) l--;
+        while (l < n - 2 && k.x[l + 1] <= r2) l++;
+        const int u = l + 1;
+        const float d = k.x[u] - k.x[l], id = 1.0f / d;
+        const float s = (r2 - k.x[l]) * id, t = (k.x[u] - r2) * id;
+        const float hl = k.h[l] * d * (1.0f / 6.0f), hu = k.h[u] * d * (1.0f / 6.0f);
+        g = k.dy[l] * id + (-(3.0f * t * t - 1.0f) * hl + (3.0f * s * s - 1.0f) * hu);
+        return true;
+    }
+    const float ir = rsqrtf(r2);
+    g = -0.5f * ir * ir * ir * (float)(1.0 / PDG_ANGSTROMS_TO_BOHRS);
+    return true;
+}
+
+__global__ void __launch_bounds__(QB) k_qcmm_grad_qc32(int model, Spline sp, int n_qc, int n_mm, const double *__restrict__ qc,
+                                                       const double *__restrict__ mm, const double *__restrict__ q,
+                                                       const double *__restrict__ qcq, double *__restrict__ gqc)
+{
+    __shared__ float4 sxm[MCH];       // MM atoms of the chunk: x, y, z, charge
+    __shared__ float4 queue[QW][64];
+    __shared__ Knots32 kn;
+    if (model == 1) stage_knots32(sp, kn);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, groups = (n_qc + QW - 1) / QW;
+    const int f = blockIdx.x / groups, A = (blockIdx.x % groups) * QW + w;
+    const bool live = A < n_qc;
+    const double *xm = mm + (size_t)f * n_mm * 3;
+    float ax = 0.f, ay = 0.f, az = 0.f, qa = 0.f;
+    if (live) { const double *xa = qc + ((size_t)f * n_qc + A) * 3; ax = (float)xa[0]; ay = (float)xa[1]; az = (float)xa[2]; qa = (float)qcq[(size_t)f * n_qc + A]; }
+    const float r2cut = cutoff_r2(model, sp), sc = (float)(2.0 / PDG_ANGSTROMS_TO_BOHRS);
+    float g0 = 0.f, g1 = 0.f, g2 = 0.f;
+    float4 *qw = queue[w];
+    auto body = [&](const float4 p) {
+        const float dx = ax - p.x, dy = ay - p.y, dz = az - p.z;
+        float gv;
+        if (!pair_grad32(model, sp, kn, fmaf(dx, dx, fmaf(dy, dy, dz * dz)), gv)) return;
+        const float s = sc * qa * p.w * gv;
+        g0 = fmaf(s, dx, g0); g1 = fmaf(s, dy, g1); g2 = fmaf(s, dz, g2);
+    };
+    int qn = 0;
+    for (int c0 = 0; c0 < n_mm; c0 += MCH) {
+        const int cn = min(MCH, n_mm - c0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cn; k += QB) {
+            const double *p = xm + 3 * (size_t)(c0 + k);
+            sxm[k] = make_float4((float)p[0], (float)p[1], (float)p[2], (float)q[c0 + k]);
+        }
+        __syncthreads();
+        if (!live) continue;
+        for (int k0 = 0; k0 < cn; k0 += 32) {
+            const int k = k0 + lane;
+            bool in = false;
+            float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (k < cn) {
+                p = sxm[k];
+                const float dx = ax - p.x, dy = ay - p.y, dz = az - p.z;
+                in = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= r2cut;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, in);
+            if (in) qw[qn + __popc(bal & ((1u << lane) - 1u))] = p;
+            qn += __popc(bal);
+            __syncwarp();
+            if (qn >= 32) {
+                body(qw[lane]);
+                const int rest = qn - 32;
+                const float4 carry = lane < rest ? qw[32 + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+                __syncwarp();
+                if (lane < rest) qw[lane] = carry;
+                __syncwarp();
+                qn = rest;
+            }
+        }
+    }
+    if (live && lane < qn) body(qw[lane]);
+    const double d0 = warp_sum((double)g0), d1 = warp_sum((double)g1), d2 = warp_sum((double)g2);
+    if (live && lane == 0) { double *o = gqc + ((size_t)f * n_qc + A) * 3; o[0] = d0; o[1] = d1; o[2] = d2; }
+}
+
+__global__ void __launch_bounds__(MB) k_qcmm_grad_mm32(int model, Spline sp, int n_qc, int n_mm, const double *__restrict__ qc,
+                                                       const double *__restrict__ mm, const double *__restrict__ q,
+                                                       const double *__restrict__ qcq, double *__restrict__ gmm)
+{
+    extern __shared__ float4 sa[];    // QC atoms: x, y, z, charge
+    __shared__ int queue[MB / 32][64], wcount[MB / 32], near_list[MB];
+    __shared__ Knots32 kn;
+    if (model == 1) stage_knots32(sp, kn);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int blocks_per_frame = (n_mm + MB - 1) / MB;
+    const int f = blockIdx.x / blocks_per_frame, base = (blockIdx.x % blocks_per_frame) * MB;
+    for (int k = threadIdx.x; k < n_qc; k += MB) {
+        const double *x = qc + ((size_t)f * n_qc + k) * 3;
+        sa[k] = make_float4((float)x[0], (float)x[1], (float)x[2], (float)qcq[(size_t)f * n_qc + k]);
+    }
+    __syncthreads();
+    const float r2cut = cutoff_r2(model, sp), sc = (float)(2.0 / PDG_ANGSTROMS_TO_BOHRS);
+    bool near = false;
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    if (base + (int)threadIdx.x < n_mm) {
+        const int m = base + threadIdx.x;
+        const double *xm = mm + ((size_t)f * n_mm + m) * 3;
+        fx = (float)xm[0]; fy = (float)xm[1]; fz = (float)xm[2];
+        for (int A = 0; A < n_qc && !near; A++) {
+            const float dx = sa[A].x - fx, dy = sa[A].y - fy, dz = sa[A].z - fz;
+            near = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= r2cut;
+        }
+        if (!near) { double *o = gmm + ((size_t)f * n_mm + m) * 3; o[0] = 0.0; o[1] = 0.0; o[2] = 0.0; }
+    }
+    const unsigned nbal = __ballot_sync(0xffffffffu, near);
+    if (lane == 0) wcount[w] = __popc(nbal);
+    __syncthreads();
+    int off = 0, total = 0;
+    for (int k = 0; k < MB / 32; k++) { if (k < w) off += wcount[k]; total += wcount[k]; }
+    if (near) near_list[off + __popc(nbal & ((1u << lane) - 1u))] = base + threadIdx.x;
+    __syncthreads();
+    int *qw = queue[w];
+    for (int k = w; k < total; k += MB / 32) {
+        const int m = near_list[k];
+        const double *xm = mm + ((size_t)f * n_mm + m) * 3;
+        const float mx = (float)xm[0], my = (float)xm[1], mz = (float)xm[2], qm = (float)q[m];
+        float g0 = 0.f, g1 = 0.f, g2 = 0.f;
+        auto body = [&](int A) {
+            const float4 a = sa[A];
+            const float dx = a.x - mx, dy = a.y - my, dz = a.z - mz;
+            float gv;
+            if (!pair_grad32(model, sp, kn, fmaf(dx, dx, fmaf(dy, dy, dz * dz)), gv)) return;
+            const float s = sc * a.w * qm * gv;
+            g0 = fmaf(-s, dx, g0); g1 = fmaf(-s, dy, g1); g2 = fmaf(-s, dz, g2);
+        };
+        int qn = 0;
+        for (int A0 = 0; A0 < n_qc; A0 += 32) {
+            const int A = A0 + lane;
+            bool in = false;
+            if (A < n_qc) {
+                const float4 a = sa[A];
+                const float ex = a.x - mx, ey = a.y - my, ez = a.z - mz;
+                in = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= r2cut;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, in);
+            if (in) qw[qn + __popc(bal & ((1u << lane) - 1u))] = A;
+            qn += __popc(bal);
+            __syncwarp();
+            if (qn >= 32) {
+                body(qw[lane]);
+                const int rest = qn - 32;
+                const int carry = lane < rest ? qw[32 + lane] : 0;
+                __syncwarp();
+                if (lane < rest) qw[lane] = carry;
+                __syncwarp();
+                qn = rest;
+            }
+        }
+        if (lane < qn) body(qw[lane]);
+        __syncwarp();
+        const double d0 = warp_sum((double)g0), d1 = warp_sum((double)g1), d2 = warp_sum((double)g2);
+        if (lane == 0) { double *o = gmm + ((size_t)f * n_mm + m) * 3; o[0] = d0; o[1] = d1; o[2] = d2; }
+    }
+}
+
 static Spline make_spline(int n, const double *knots, double cutoff)
 {
     Spline s;
@@ -255,7 +440,20 @@ int launch_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const dou
                           double *gqc, double *gmm, cudaStream_t st)
 {
     if (n_frames <= 0 || n_qc <= 0) return 0;
+    const bool f32 = (model & PDG_QCMM_FP32_PAIRS) != 0 && n_knots <= KMAX32;
+    model &= ~PDG_QCMM_FP32_PAIRS;
     Spline sp = make_spline(n_knots, knots, cutoff);
+    if (f32) {
+        const int groups = (n_qc + QW - 1) / QW;
+        k_qcmm_grad_qc32<<<n_frames * groups, QB, 0, st>>>(model, sp, n_qc, n_mm, qc, mm, q, qcq, gqc);
+        if (n_mm > 0 && gmm) {
+            const int bpf = (n_mm + MB - 1) / MB;
+            const size_t sm = sizeof(float4) * (size_t)n_qc;
+            if (sm > 8 * 1024) cudaFuncSetAttribute(k_qcmm_grad_mm32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            k_qcmm_grad_mm32<<<n_frames * bpf, MB, sm, st>>>(model, sp, n_qc, n_mm, qc, mm, q, qcq, gmm);
+        }
+        return 0;
+    }
     const int groups = (n_qc + QW - 1) / QW;
     k_qcmm_grad_qc<<<n_frames * groups, QB, 0, st>>>(model, sp, n_qc, n_mm, qc, mm, q, qcq, gqc);
     if (n_mm > 0 && gmm) {

@@ -111,7 +111,9 @@ class QCEngine:
         if qcmm and gradients:
             gqc = torch.empty((F, n, 3), dtype=torch.float64, device=dev)
             gmm = torch.empty((F, mm_xyz.shape[1], 3), dtype=torch.float64, device=dev) if mm_gradients else None
-            _native.check(self.L.pdg_qcmm_gradients(nbmodel.model_id, F, n, mm_xyz.shape[1], _native.ptr(qc_xyz), _native.ptr(mm_xyz),
+            # the mixed method takes the QC/MM gradient pair terms in FP32 (per-atom sums in FP64); plain FP64 keeps FP64
+            gmodel = nbmodel.model_id | (_native.QCMM_FP32_PAIRS if opts.density_step != 0 else 0)
+            _native.check(self.L.pdg_qcmm_gradients(gmodel, F, n, mm_xyz.shape[1], _native.ptr(qc_xyz), _native.ptr(mm_xyz),
                                                     _native.ptr(mm_charges), _native.ptr(charges), nk, _native.ptr(knots),
                                                     float(nbmodel.outerCutoff), _native.ptr(gqc), _native.ptr(gmm), sh),
                           "pdg_qcmm_gradients")
