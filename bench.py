@@ -21,9 +21,9 @@ sys.path.insert(0, HERE)
 
 import numpy as np
 
-# DRAM bytes (read + write) of one k_scf launch on this workload (304 frames), from the ncu capture summarised
-# in profiles/k_scf_dram_304frames.md; per launch, like `achieved`.
-K_SCF_DRAM_BYTES_304 = 4.85e9 + 4.10e9
+# DRAM bytes (read + write) of one k_scf launch on this workload (304 frames), from the ncu captures summarised
+# in profiles/k_scf_dram_304frames.md; per launch, like `achieved` (mixed: this build; plain: an earlier build).
+K_SCF_DRAM_BYTES_304 = {"mixed": 8.59e9 + 5.12e9, "fp64": 4.85e9 + 4.10e9}
 
 METRIC = "QC/MM E+grad evals/s at |dE|<1e-6 Eh (AM1 RHF, 65 QC atoms in 4000 TIP3P waters, ABFS 8/12 A)"
 UNIT = "evals/s"
@@ -612,7 +612,8 @@ def main():
         f64, f32, tc = scf_work(h["timers"], N, kv, len(frames), mixed)
         t = h["scf_ms"] * 1e-3
         r = {"bound": "fp64", "kernel": "k_scf", "achieved": f64 / t / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
-             "frac": f64 / t / 1e12 / fp64_peak, "traffic": None,
+             "frac": f64 / t / 1e12 / fp64_peak,
+             "traffic": K_SCF_DRAM_BYTES_304["mixed" if mixed else "fp64"] if len(frames) == 304 else None,
              "note": "FP64 algorithmic flops of the density steps over the k_scf launch (%.2f ms, %d frames); peak = cuBLAS DGEMM "
                      "4096^3 measured in this run (of measured; MEASURED_PEAKS.json has no FP64 figure)" % (h["scf_ms"], len(frames))}
         if mixed:
