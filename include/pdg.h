@@ -70,7 +70,10 @@ typedef struct {
                                    3 or 6: split-BF16 SP2 purification on the tensor cores with that many BF16
                                    partial products accumulated in FP32, for the cycles before the density RMS
                                    change falls below mixed_switch, then the FP64 eigensolve to convergence
-                                   (N <= 144; larger systems use the FP64 step throughout). Not in the reference. */
+                                   (N <= 144; larger systems use the FP64 step throughout). Not in the reference.
+                                   3 and 6 (the mixed method) also turn on: perturbative density steps after the
+                                   first FP64 step, FP32 DIIS commutators, and FP32 sp-sp pair gradient terms
+                                   (assembled and summed in FP64) in pdg_energy_gradients / pdg_batch_*. */
     double mixed_switch;        /* RMS density change that ends the purification cycles (e.g. 1e-4) */
 } pdg_scf_options;
 

@@ -31,6 +31,7 @@ struct pdg_system {
     int charge;
     // device allocations owned by the system (tables only; no per-frame data)
     double *d_elements = nullptr, *d_terms = nullptr, *d_ovl = nullptr;
+    float *d_ovl32 = nullptr, *d_mpw32 = nullptr;
     int *d_ints = nullptr;
     void *d_mp = nullptr;
 };
@@ -122,6 +123,7 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     for (int a = 0, k = 0; a <= n_atoms; a++) { ints.push_back(k); if (a < n_atoms) k += norb[a] * (norb[a] + 1) / 2; }
     MultipoleMap mp;
     if (!multipole_map_spsp(mp)) { pdg_system_destroy(s); return fail(PDG_BAD_ARGUMENT, "multipole map exceeds its term limit"); }
+    std::vector<float> ovl32(ovl.begin(), ovl.end()), mpw32(mp.w, mp.w + MP_MAP_MAX * MP_MAP_NNZ);
     int rc = PDG_OK;
     if ((rc = cuda_check(cudaMalloc(&s->d_mp, sizeof(MultipoleMap)), "cudaMalloc multipole map")) ||
         (rc = cuda_check(cudaMemcpy(s->d_mp, &mp, sizeof(MultipoleMap), cudaMemcpyHostToDevice), "copy multipole map")) ||
@@ -130,6 +132,10 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
         (rc = cuda_check(cudaMalloc(&s->d_ints, sizeof(int) * ints.size()), "cudaMalloc tables")) ||
         (rc = cuda_check(cudaMalloc(&s->d_ovl, sizeof(double) * ovl.size()), "cudaMalloc overlap records")) ||
         (rc = cuda_check(cudaMemcpy(s->d_ovl, ovl.data(), sizeof(double) * ovl.size(), cudaMemcpyHostToDevice), "copy overlap records")) ||
+        (rc = cuda_check(cudaMalloc(&s->d_ovl32, sizeof(float) * ovl.size()), "cudaMalloc FP32 overlap records")) ||
+        (rc = cuda_check(cudaMemcpy(s->d_ovl32, ovl32.data(), sizeof(float) * ovl32.size(), cudaMemcpyHostToDevice), "copy FP32 overlap records")) ||
+        (rc = cuda_check(cudaMalloc(&s->d_mpw32, sizeof(float) * MP_MAP_MAX * MP_MAP_NNZ), "cudaMalloc FP32 multipole weights")) ||
+        (rc = cuda_check(cudaMemcpy(s->d_mpw32, mpw32.data(), sizeof(float) * mpw32.size(), cudaMemcpyHostToDevice), "copy FP32 multipole weights")) ||
         (rc = cuda_check(cudaMemcpy(s->d_elements, s->elements.data(), sizeof(double) * s->elements.size(), cudaMemcpyHostToDevice), "copy elements")) ||
         (rc = cuda_check(cudaMemcpy(s->d_terms, terms.data(), sizeof(double) * terms.size(), cudaMemcpyHostToDevice), "copy terms")) ||
         (rc = cuda_check(cudaMemcpy(s->d_ints, ints.data(), sizeof(int) * ints.size(), cudaMemcpyHostToDevice), "copy tables"))) {
@@ -151,6 +157,7 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     d.pairs_sps = d.pairs_gen + pgen.size(); d.n_sps = (int)psps.size();
     d.mp_map = s->d_mp;
     d.atom_pk = b + pk_at;
+    d.ovl32 = s->d_ovl32; d.mp_w32 = s->d_mpw32;
     *out = s;
     return PDG_OK;
 }
@@ -159,6 +166,7 @@ extern "C" int pdg_system_destroy(pdg_system *s)
 {
     if (!s) return PDG_OK;
     cudaFree(s->d_elements); cudaFree(s->d_terms); cudaFree(s->d_ints); cudaFree(s->d_ovl); cudaFree(s->d_mp);
+    cudaFree(s->d_ovl32); cudaFree(s->d_mpw32);
     delete s;
     return PDG_OK;
 }
@@ -213,7 +221,8 @@ extern "C" int pdg_energy_gradients(pdg_system *s, int n_frames, const double *d
     launch_scf(s->d, p, n_frames, d_phi, *o, d_density, use_density, d_energies, d_charges, d_status, d_ncycles, w, 0, nullptr, st);
     if ((rc = cuda_check(cudaGetLastError(), "scf kernel"))) return rc;
     if (d_gradients) {
-        launch_pair_gradients(s->d, p, n_frames, d_xyz, d_density, w, st);
+        // the mixed method takes the sp-sp pair gradient terms in FP32 (assembled and summed in FP64)
+        launch_pair_gradients(s->d, p, n_frames, d_xyz, d_density, w, st, o->density_step != 0);
         launch_reduce_gradients(s->d, p, n_frames, w, d_gradients, st);
         if ((rc = cuda_check(cudaGetLastError(), "gradient kernels"))) return rc;
     }
@@ -528,7 +537,7 @@ static int batch_queue(pdg_batch *bt, const double *d_xyz, const double *d_phi, 
                                 d_density, use_density, d_energies, d_charges, d_status, d_ncycles, w, st);
     if ((rc = cuda_check(cudaGetLastError(), "batch scf kernel"))) return rc;
     if (d_gradients) {
-        launch_batch_gradients(bt->b, d_xyz, d_density, w, d_gradients, st);
+        launch_batch_gradients(bt->b, d_xyz, d_density, w, d_gradients, st, o->density_step != 0);
         if ((rc = cuda_check(cudaGetLastError(), "batch gradient kernels"))) return rc;
     }
     return PDG_OK;

@@ -39,6 +39,8 @@ struct DeviceSystem {
     int n_sps;
     const void *mp_map;                // MultipoleMap of sp-sp pairs (multipole.cuh)
     const int *atom_pk;                // n_atoms + 1: first entry of each atom's one-centre block in the cel order
+    const float *ovl32;                // the overlap primitive records rounded to FP32 (the mixed method's gradients)
+    const float *mp_w32;               // the multipole map's weights rounded to FP32 (same layout as MultipoleMap::w)
 };
 
 // Per-frame workspace plan (all offsets in doubles from the frame's base).
@@ -235,12 +237,13 @@ __device__ __forceinline__ double block_max(double v, double *red)
 void launch_pair_integrals(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *xyz, double *ws, cudaStream_t st);
 void launch_assemble_h(const DeviceSystem &s, const FramePlan &p, int n_frames, double *ws, cudaStream_t st);
 void launch_pair_gradients(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *xyz,
-                           const double *density, double *ws, cudaStream_t st);
+                           const double *density, double *ws, cudaStream_t st, bool fp32_terms = false);
 void launch_reduce_gradients(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *ws,
                              double *gradients, cudaStream_t st);
 // Heterogeneous batches (the same kernels over a BatchItem table).
 void launch_batch_integrals(const Batch &b, const double *xyz, double *ws, cudaStream_t st);
-void launch_batch_gradients(const Batch &b, const double *xyz, const double *density, double *ws, double *gradients, cudaStream_t st);
+void launch_batch_gradients(const Batch &b, const double *xyz, const double *density, double *ws, double *gradients, cudaStream_t st,
+                            bool fp32_terms = false);
 #define PDG_SMEM_LIMIT_1 (220 * 1024)   // shared-memory budget of one SCF CTA alone on its SM
 #define PDG_SMEM_LIMIT_2 (112 * 1024)   // ... of each of two
 int launch_qcmm_potentials(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,

@@ -418,7 +418,13 @@ void launch_batch_integrals(const Batch &b, const double *xyz, double *ws, cudaS
 #define PG_WARPS 4
 #define PG_SM 1408
 
-template <bool BATCH>
+__device__ __forceinline__ double rsq(double x) { return rsqrt(x); }
+__device__ __forceinline__ float rsq(float x) { return rsqrtf(x); }
+
+// Real = double: the reference's FP64 arithmetic.  Real = float (the mixed method): the pair's multipole terms,
+// rotation, density terms, contractions and overlap sums in FP32, the core-core term and the assembly of the
+// pair gradient in FP64 (per-pair errors ~1e-7 Hartree/Bohr, summed per atom in FP64).
+template <bool BATCH, typename Real>
 __global__ void __launch_bounds__(PG_WARPS * 32)
 k_pair_gradients(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, const double *__restrict__ xyz,
                  const double *__restrict__ density, double *__restrict__ ws)
@@ -432,10 +438,10 @@ k_pair_gradients(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, con
     const FramePlan &plan = BATCH ? fv.plan : plan0;
     const double *terms = s.terms;
     const int b0 = ub * 32, nb = min(32, s.n_gen - b0);
-    double *W = smem[w];
-    double *St = W, *dSt = W + 96, *L = W + 192, *dL = W + 292, *ci = W + 392, *cj = W + 402, *dci = W + 412, *dcj = W + 422;
-    double *C = W + 432, *CD = W + 532, *G = W + 832, *W1 = W + 932, *W2 = W + 1032, *W3 = W + 1132;
-    double *oneI = W + 1232, *oneJ = W + 1242, *Wres = W + 1252;
+    Real *W = (Real *)smem[w];
+    Real *St = W, *dSt = W + 96, *L = W + 192, *dL = W + 292, *ci = W + 392, *cj = W + 402, *dci = W + 412, *dcj = W + 422;
+    Real *C = W + 432, *CD = W + 532, *G = W + 832, *W1 = W + 932, *W2 = W + 1032, *W3 = W + 1132;
+    Real *oneI = W + 1232, *oneJ = W + 1242, *Wres = W + 1252;
     const int N = s.n_basis;
     const double *R = xyz + 3 * fv.atom;
     const double *P = density + fv.dens;
@@ -466,12 +472,12 @@ k_pair_gradients(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, con
         double eng[3] = { 0.0, 0.0, 0.0 };
         // one-centre density vectors (off-diagonal elements doubled) and the two-centre density
         // Gamma = 1/4 aa bb (P_mk P_nl + P_nk P_ml) - oneI (x) oneJ  (QCModelMNDOState.c:196-250)
-        if (lane < ni) { const int a = MP_DA[lane], b = MP_DB[lane]; oneI[lane] = (a == b ? 1.0 : 2.0) * P[(size_t)(is + a) * N + is + b]; }
-        if (lane >= 16 && lane - 16 < nj) { const int k = lane - 16, a = MP_DA[k], b = MP_DB[k]; oneJ[k] = (a == b ? 1.0 : 2.0) * P[(size_t)(js + a) * N + js + b]; }
+        if (lane < ni) { const int a = MP_DA[lane], b = MP_DB[lane]; oneI[lane] = (Real)((a == b ? 1.0 : 2.0) * P[(size_t)(is + a) * N + is + b]); }
+        if (lane >= 16 && lane - 16 < nj) { const int k = lane - 16, a = MP_DA[k], b = MP_DB[k]; oneJ[k] = (Real)((a == b ? 1.0 : 2.0) * P[(size_t)(js + a) * N + js + b]); }
         // resonance weights (beta_a + beta_b) P_ab (QCModelMNDO.c:800-823)
         if (lane < 16) {
             const int a = lane / 4, b = lane % 4;
-            Wres[lane] = (a < noi && b < noj) ? (Ei[PDG_E_BETA + a] + Ej[PDG_E_BETA + b]) * P[(size_t)(is + a) * N + js + b] : 0.0;
+            Wres[lane] = (a < noi && b < noj) ? (Real)((Ei[PDG_E_BETA + a] + Ej[PDG_E_BETA + b]) * P[(size_t)(is + a) * N + js + b]) : Real(0);
         }
         __syncwarp();
         for (int k = lane; k < ni * nj; k += 32) {
@@ -480,31 +486,31 @@ k_pair_gradients(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, con
             const double aa = (kk == l) ? 1.0 : 2.0, bb = (m == n) ? 1.0 : 2.0;
             const int K = is + kk, Lx = is + l, M = js + m, Nn = js + n;
             const double fv = P[(size_t)M * N + K] * P[(size_t)Nn * N + Lx] + P[(size_t)Nn * N + K] * P[(size_t)M * N + Lx];
-            G[k] = 0.25 * aa * bb * fv - oneI[kl] * oneJ[mn];
+            G[k] = (Real)(0.25 * aa * bb * fv) - oneI[kl] * oneJ[mn];
         }
         if (r >= 5.0e-3) {
             const double *to = terms + (size_t)(eli * s.n_elements + elj) * 2 * MP_NTERMS, *ta = to + MP_NTERMS;
             for (int k = lane; k < MP_TERMS_USED; k += 32) {
                 const double a = ta[k];
-                if (a < 0.0) { St[k] = 0.0; dSt[k] = 0.0; continue; }
-                const double ro = r + to[k], sv = rsqrt(ro * ro + a);
+                if (a < 0.0) { St[k] = Real(0); dSt[k] = Real(0); continue; }
+                const Real ro = (Real)(r + to[k]), sv = rsq(ro * ro + (Real)a);
                 St[k] = sv; dSt[k] = -ro * sv * sv * sv;
             }
-            for (int k = lane; k < 240; k += 32) L[k] = 0.0;     // L, dL, ci, cj, dci, dcj (contiguous)
-            Rotation rot;
+            for (int k = lane; k < 240; k += 32) L[k] = Real(0);     // L, dL, ci, cj, dci, dcj (contiguous)
+            RotationT<Real> rot;
             rot_assemble(q, true, rot);
             for (int k = lane; k < 100; k += 32) {
                 const int ab = k / 10, mn = k % 10;
                 C[k] = ctrans(rot.T, ab, mn);
-                for (int xx = 0; xx < 3; xx++) CD[xx * 100 + k] = rot.active ? ctrans_d(rot.T, rot.D[xx], ab, mn) : 0.0;
+                for (int xx = 0; xx < 3; xx++) CD[xx * 100 + k] = rot.active ? ctrans_d(rot.T, rot.D[xx], ab, mn) : Real(0);
             }
             __syncwarp();
             {   // L, ci, cj and their r-derivatives as the sparse linear map of the terms, a few outputs per lane
                 const MultipoleMap &mpm = *(const MultipoleMap *)s.mp_map;
                 for (int o = lane; o < mpm.n; o += 32) {
                     const int *tk = mpm.term + o * MP_MAP_NNZ;
-                    const double *wk = mpm.w + o * MP_MAP_NNZ;
-                    double v = 0.0, dv = 0.0;
+                    const Real *wk = sizeof(Real) == sizeof(double) ? (const Real *)(mpm.w + o * MP_MAP_NNZ) : (const Real *)(s.mp_w32 + o * MP_MAP_NNZ);
+                    Real v = 0, dv = 0;
                     for (int k = 0; k < mpm.nnz[o]; k++) { v = fma(wk[k], St[tk[k]], v); dv = fma(wk[k], dSt[tk[k]], dv); }
                     const int out = mpm.out[o];
                     if (out < 100) { L[out] = v; dL[out] = dv; }
@@ -516,64 +522,69 @@ k_pair_gradients(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, con
             // W1 = L C_j^T, W2 = C_i L, W3 = dL C_j^T
             for (int k = lane; k < ni * nj; k += 32) {
                 const int a = k / nj, b = k % nj;
-                double w1 = 0.0, w3 = 0.0, w2 = 0.0;
+                Real w1 = 0, w3 = 0, w2 = 0;
                 for (int qq = 0; qq < nj; qq++) { w1 += L[a * 10 + qq] * C[b * 10 + qq]; w3 += dL[a * 10 + qq] * C[b * 10 + qq]; }
                 for (int m = 0; m < ni; m++) w2 += C[a * 10 + m] * L[m * 10 + b];
                 W1[k] = w1; W2[k] = w2; W3[k] = w3;
             }
             __syncwarp();
-            double t0 = 0.0, ti[3] = { 0, 0, 0 }, tj[3] = { 0, 0, 0 };
+            Real t0 = 0, ti[3] = { 0, 0, 0 }, tj[3] = { 0, 0, 0 };
             for (int k = lane; k < ni * nj; k += 32) {
                 const int ab = k / nj, cd = k % nj;
-                const double g = G[k];
-                double u0 = 0.0, ui[3] = { 0, 0, 0 }, uj[3] = { 0, 0, 0 };
+                const Real g = G[k];
+                Real u0 = 0, ui[3] = { 0, 0, 0 }, uj[3] = { 0, 0, 0 };
                 for (int m = 0; m < ni; m++) {
-                    const double w1 = W1[m * nj + cd];
+                    const Real w1 = W1[m * nj + cd];
                     u0 += C[ab * 10 + m] * W3[m * nj + cd];
                     if (spi) for (int xx = 0; xx < 3; xx++) ui[xx] += CD[xx * 100 + ab * 10 + m] * w1;
                 }
-                if (spj) for (int qq = 0; qq < nj; qq++) { const double w2 = W2[ab * nj + qq]; for (int xx = 0; xx < 3; xx++) uj[xx] += w2 * CD[xx * 100 + cd * 10 + qq]; }
+                if (spj) for (int qq = 0; qq < nj; qq++) { const Real w2 = W2[ab * nj + qq]; for (int xx = 0; xx < 3; xx++) uj[xx] += w2 * CD[xx * 100 + cd * 10 + qq]; }
                 t0 += g * u0;
                 for (int xx = 0; xx < 3; xx++) { ti[xx] += g * ui[xx]; tj[xx] += g * uj[xx]; }
             }
             // electron-core parts
-            double o0 = 0.0, oi[3] = { 0, 0, 0 };
+            Real o0 = 0, oi[3] = { 0, 0, 0 };
+            const Real zj = (Real)Ej[PDG_E_ZCORE], zi = (Real)Ei[PDG_E_ZCORE];
             if (lane < ni) {
-                double u = 0.0, ux[3] = { 0, 0, 0 };
+                Real u = 0, ux[3] = { 0, 0, 0 };
                 for (int m = 0; m < ni; m++) {
                     u += C[lane * 10 + m] * dci[m];
                     if (spi) for (int xx = 0; xx < 3; xx++) ux[xx] += CD[xx * 100 + lane * 10 + m] * ci[m];
                 }
-                o0 += oneI[lane] * u * (-Ej[PDG_E_ZCORE]);
-                for (int xx = 0; xx < 3; xx++) oi[xx] += oneI[lane] * ux[xx] * (-Ej[PDG_E_ZCORE]);
+                o0 += oneI[lane] * u * (-zj);
+                for (int xx = 0; xx < 3; xx++) oi[xx] += oneI[lane] * ux[xx] * (-zj);
             }
             if (lane >= 16 && lane - 16 < nj) {
                 const int cd = lane - 16;
-                double u = 0.0, ux[3] = { 0, 0, 0 };
+                Real u = 0, ux[3] = { 0, 0, 0 };
                 for (int m = 0; m < nj; m++) {
                     u += C[cd * 10 + m] * dcj[m];
                     if (spj) for (int xx = 0; xx < 3; xx++) ux[xx] += CD[xx * 100 + cd * 10 + m] * cj[m];
                 }
-                o0 += oneJ[cd] * u * (-Ei[PDG_E_ZCORE]);
-                for (int xx = 0; xx < 3; xx++) oi[xx] += oneJ[cd] * ux[xx] * (-Ei[PDG_E_ZCORE]);
+                o0 += oneJ[cd] * u * (-zi);
+                for (int xx = 0; xx < 3; xx++) oi[xx] += oneJ[cd] * ux[xx] * (-zi);
             }
-            t0 = warp_sum(t0); o0 = warp_sum(o0);
-            for (int xx = 0; xx < 3; xx++) { ti[xx] = warp_sum(ti[xx]); tj[xx] = warp_sum(tj[xx]); oi[xx] = warp_sum(oi[xx]); }
+            // lane sums in FP64 whatever Real is
+            const double T0 = warp_sum((double)t0), O0 = warp_sum((double)o0);
+            double TI[3], TJ[3], OI[3];
+            for (int xx = 0; xx < 3; xx++) { TI[xx] = warp_sum((double)ti[xx]); TJ[xx] = warp_sum((double)tj[xx]); OI[xx] = warp_sum((double)oi[xx]); }
             // eng = -s (dcore + doei0f + dtei0f) + doei1 + dtei1   (MNDOIntegrals.c:392-418)
             for (int xx = 0; xx < 3; xx++) {
                 const double sx = v3[xx] / r;
-                eng[xx] = -sx * dcore - sx * o0 + sx * t0 - oi[xx] + ti[xx] + tj[xx];
+                eng[xx] = -sx * dcore - sx * O0 + sx * T0 - OI[xx] + TI[xx] + TJ[xx];
             }
         }
         // resonance integral derivatives: sum (beta_a + beta_b) P_ab dS_ab / dR_i
         const int eo = eli * s.n_elements + elj;
-        double Fo[5], Do[5], gr[3];
-        overlap_sums(s.ovl + (size_t)s.ovl_off[eo] * OV_REC, s.ovl_n[eo], v3[0] * v3[0] + v3[1] * v3[1] + v3[2] * v3[2], true,
+        Real Fo[5], Do[5], gr[3];
+        const Real *orec = sizeof(Real) == sizeof(double) ? (const Real *)s.ovl : (const Real *)s.ovl32;
+        const Real ab3[3] = { (Real)v3[0], (Real)v3[1], (Real)v3[2] };
+        overlap_sums(orec + (size_t)s.ovl_off[eo] * OV_REC, s.ovl_n[eo], (Real)(v3[0] * v3[0] + v3[1] * v3[1] + v3[2] * v3[2]), true,
                      overlap_used(noi, noj), Fo, Do);
-        overlap_gradient(Wres, noi, noj, v3, Fo, Do, gr);
+        overlap_gradient(Wres, noi, noj, ab3, Fo, Do, gr);
         if (lane == 0) {
             double *pg = ws + fv.ws + plan.pair_g + (size_t)p * 3;
-            pg[0] = eng[0] + gr[0]; pg[1] = eng[1] + gr[1]; pg[2] = eng[2] + gr[2];
+            pg[0] = eng[0] + (double)gr[0]; pg[1] = eng[1] + (double)gr[1]; pg[2] = eng[2] + (double)gr[2];
         }
         __syncwarp();
     }
@@ -743,12 +754,16 @@ __global__ void __launch_bounds__(256) k_reduce_gradients(DeviceSystem sys0, Fra
 }
 
 void launch_pair_gradients(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *xyz,
-                           const double *density, double *ws, cudaStream_t st)
+                           const double *density, double *ws, cudaStream_t st, bool fp32_terms)
 {
     const Batch none = {};
     long warps = (long)n_frames * ((s.n_gen + 31) / 32);
-    if (warps > 0)
-        k_pair_gradients<false><<<(int)((warps + PG_WARPS - 1) / PG_WARPS), PG_WARPS * 32, 0, st>>>(s, p, n_frames, none, xyz, density, ws);
+    if (warps > 0) {
+        if (fp32_terms)
+            k_pair_gradients<false, float><<<(int)((warps + PG_WARPS - 1) / PG_WARPS), PG_WARPS * 32, 0, st>>>(s, p, n_frames, none, xyz, density, ws);
+        else
+            k_pair_gradients<false, double><<<(int)((warps + PG_WARPS - 1) / PG_WARPS), PG_WARPS * 32, 0, st>>>(s, p, n_frames, none, xyz, density, ws);
+    }
     const long nss = (long)n_frames * s.n_ss;
     if (nss > 0) k_pair_gradients_ss<false><<<(int)((nss + 255) / 256), 256, 0, st>>>(s, p, n_frames, none, xyz, density, ws);
     const long nsps = (long)n_frames * s.n_sps;
@@ -762,12 +777,17 @@ void launch_reduce_gradients(const DeviceSystem &s, const FramePlan &p, int n_fr
     k_reduce_gradients<false><<<(int)((warps + 7) / 8), 256, 0, st>>>(s, p, n_frames, none, ws, grad);
 }
 
-void launch_batch_gradients(const Batch &b, const double *xyz, const double *density, double *ws, double *grad, cudaStream_t st)
+void launch_batch_gradients(const Batch &b, const double *xyz, const double *density, double *ws, double *grad, cudaStream_t st,
+                            bool fp32_terms)
 {
     const DeviceSystem s0 = {};
     const FramePlan p0 = {};
-    if (b.total[PDG_WORK_GEN] > 0)
-        k_pair_gradients<true><<<(b.total[PDG_WORK_GEN] + PG_WARPS - 1) / PG_WARPS, PG_WARPS * 32, 0, st>>>(s0, p0, 0, b, xyz, density, ws);
+    if (b.total[PDG_WORK_GEN] > 0) {
+        if (fp32_terms)
+            k_pair_gradients<true, float><<<(b.total[PDG_WORK_GEN] + PG_WARPS - 1) / PG_WARPS, PG_WARPS * 32, 0, st>>>(s0, p0, 0, b, xyz, density, ws);
+        else
+            k_pair_gradients<true, double><<<(b.total[PDG_WORK_GEN] + PG_WARPS - 1) / PG_WARPS, PG_WARPS * 32, 0, st>>>(s0, p0, 0, b, xyz, density, ws);
+    }
     if (b.total[PDG_WORK_SS] > 0)
         k_pair_gradients_ss<true><<<(b.total[PDG_WORK_SS] + 255) / 256, 256, 0, st>>>(s0, p0, 0, b, xyz, density, ws);
     if (b.total[PDG_WORK_SPS] > 0)

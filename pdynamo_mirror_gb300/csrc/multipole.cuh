@@ -179,7 +179,8 @@ inline bool multipole_map_spsp(MultipoleMap &m)
 // atom j (MNDOIntegralUtilities_GetTransformationMatrices, MNDOIntegralUtilities.c:449-465 for s/p,
 // axes swapped when |z/r| > 0.99999999).  T[a][m]: molecular orbital a (s, pz, px, py), local m
 // (s, sigma, pi+, pi-).  Returns false when no rotation applies (identity, zero derivatives).
-struct Rotation { double T[4][4]; double D[3][4][4]; bool active; };
+template <typename R> struct RotationT { R T[4][4]; R D[3][4][4]; bool active; };
+using Rotation = RotationT<double>;
 
 // The geometry-dependent scalars of the rotation (square root, divisions): direction cosines and, for
 // gradients, their derivatives.  Computed once per pair (one thread per pair) and broadcast to the
@@ -225,36 +226,40 @@ __device__ __forceinline__ RotScalars rot_shfl(const RotScalars &q, int src, boo
 // atom j (MNDOIntegralUtilities_GetTransformationMatrices, MNDOIntegralUtilities.c:449-465 for s/p,
 // axes swapped when |z/r| > 0.99999999).  T[a][m]: molecular orbital a (s, pz, px, py), local m
 // (s, sigma, pi+, pi-).  Inactive: identity, zero derivatives.
-__device__ __forceinline__ void rot_assemble(const RotScalars &q, bool derivs, Rotation &R)
+// (R = float: the same assembly from the scalars rounded to FP32, for the mixed method's gradient terms.)
+template <typename Real>
+__device__ __forceinline__ void rot_assemble(const RotScalars &q, bool derivs, RotationT<Real> &R)
 {
     for (int a = 0; a < 4; a++) for (int m = 0; m < 4; m++) {
-        R.T[a][m] = (a == m) ? 1.0 : 0.0;
-        if (derivs) { R.D[0][a][m] = 0.0; R.D[1][a][m] = 0.0; R.D[2][a][m] = 0.0; }
+        R.T[a][m] = (a == m) ? Real(1) : Real(0);
+        if (derivs) { R.D[0][a][m] = Real(0); R.D[1][a][m] = Real(0); R.D[2][a][m] = Real(0); }
     }
     R.active = q.active;
     if (!q.active) return;
     const int PZ = 1, PX = 2, PY = 3;
-    const double ca = q.ca, sa = q.sa, cb = q.cb, sb = q.sb;
-    double T[4][4] = {{1, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
+    const Real ca = (Real)q.ca, sa = (Real)q.sa, cb = (Real)q.cb, sb = (Real)q.sb;
+    Real T[4][4] = {{1, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
     T[PX][1] = ca * sb; T[PX][2] = ca * cb; T[PX][3] = -sa;
     T[PY][1] = sa * sb; T[PY][2] = sa * cb; T[PY][3] = ca;
     T[PZ][1] = cb;      T[PZ][2] = -sb;
-    if (q.swapped) for (int c = 0; c < 4; c++) { double t = T[PX][c]; T[PX][c] = T[PZ][c]; T[PZ][c] = t; }
+    if (q.swapped) for (int c = 0; c < 4; c++) { Real t = T[PX][c]; T[PX][c] = T[PZ][c]; T[PZ][c] = t; }
     for (int a = 0; a < 4; a++) for (int m = 0; m < 4; m++) R.T[a][m] = T[a][m];
     if (!derivs) return;
-    double D[3][4][4] = {};
-    D[0][PX][1] = q.caX * sb + ca * q.sbX; D[0][PX][2] = q.caX * cb + ca * q.cbX; D[0][PX][3] = -q.saX;
-    D[0][PY][1] = q.saX * sb + sa * q.sbX; D[0][PY][2] = q.saX * cb + sa * q.cbX; D[0][PY][3] = q.caX;
-    D[0][PZ][1] = q.cbX; D[0][PZ][2] = -q.sbX;
-    D[1][PX][1] = q.caY * sb + ca * q.sbY; D[1][PX][2] = q.caY * cb + ca * q.cbY; D[1][PX][3] = -q.saY;
-    D[1][PY][1] = q.saY * sb + sa * q.sbY; D[1][PY][2] = q.saY * cb + sa * q.cbY; D[1][PY][3] = q.caY;
-    D[1][PZ][1] = q.cbY; D[1][PZ][2] = -q.sbY;
-    D[2][PX][1] = ca * q.sbZ; D[2][PX][2] = ca * q.cbZ;
-    D[2][PY][1] = sa * q.sbZ; D[2][PY][2] = sa * q.cbZ;
-    D[2][PZ][1] = q.cbZ; D[2][PZ][2] = -q.sbZ;
+    const Real caX = (Real)q.caX, caY = (Real)q.caY, saX = (Real)q.saX, saY = (Real)q.saY, cbX = (Real)q.cbX, cbY = (Real)q.cbY;
+    const Real cbZ = (Real)q.cbZ, sbX = (Real)q.sbX, sbY = (Real)q.sbY, sbZ = (Real)q.sbZ;
+    Real D[3][4][4] = {};
+    D[0][PX][1] = caX * sb + ca * sbX; D[0][PX][2] = caX * cb + ca * cbX; D[0][PX][3] = -saX;
+    D[0][PY][1] = saX * sb + sa * sbX; D[0][PY][2] = saX * cb + sa * cbX; D[0][PY][3] = caX;
+    D[0][PZ][1] = cbX; D[0][PZ][2] = -sbX;
+    D[1][PX][1] = caY * sb + ca * sbY; D[1][PX][2] = caY * cb + ca * cbY; D[1][PX][3] = -saY;
+    D[1][PY][1] = saY * sb + sa * sbY; D[1][PY][2] = saY * cb + sa * cbY; D[1][PY][3] = caY;
+    D[1][PZ][1] = cbY; D[1][PZ][2] = -sbY;
+    D[2][PX][1] = ca * sbZ; D[2][PX][2] = ca * cbZ;
+    D[2][PY][1] = sa * sbZ; D[2][PY][2] = sa * cbZ;
+    D[2][PZ][1] = cbZ; D[2][PZ][2] = -sbZ;
     if (q.swapped) {
-        for (int k = 0; k < 3; k++) for (int c = 0; c < 4; c++) { double t = D[k][PX][c]; D[k][PX][c] = D[k][PZ][c]; D[k][PZ][c] = t; }
-        for (int a = 0; a < 4; a++) for (int c = 0; c < 4; c++) { double t = D[0][a][c]; D[0][a][c] = D[2][a][c]; D[2][a][c] = t; }
+        for (int k = 0; k < 3; k++) for (int c = 0; c < 4; c++) { Real t = D[k][PX][c]; D[k][PX][c] = D[k][PZ][c]; D[k][PZ][c] = t; }
+        for (int a = 0; a < 4; a++) for (int c = 0; c < 4; c++) { Real t = D[0][a][c]; D[0][a][c] = D[2][a][c]; D[2][a][c] = t; }
     }
     for (int k = 0; k < 3; k++) for (int a = 0; a < 4; a++) for (int m = 0; m < 4; m++) R.D[k][a][m] = D[k][a][m];
 }
@@ -264,13 +269,15 @@ __device__ __forceinline__ void rot_assemble(const RotScalars &q, bool derivs, R
 __constant__ const int8_t MP_DA[10] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3};
 __constant__ const int8_t MP_DB[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
 
-__device__ __forceinline__ double ctrans(const double (*T)[4], int ab, int mn)
+template <typename Real>
+__device__ __forceinline__ Real ctrans(const Real (*T)[4], int ab, int mn)
 {
     int a = MP_DA[ab], b = MP_DB[ab], m = MP_DA[mn], n = MP_DB[mn];
     if (m == n) return T[a][m] * T[b][m];
     return T[a][m] * T[b][n] + T[a][n] * T[b][m];
 }
-__device__ __forceinline__ double ctrans_d(const double (*T)[4], const double (*D)[4], int ab, int mn)
+template <typename Real>
+__device__ __forceinline__ Real ctrans_d(const Real (*T)[4], const Real (*D)[4], int ab, int mn)
 {
     int a = MP_DA[ab], b = MP_DB[ab], m = MP_DA[mn], n = MP_DB[mn];
     if (m == n) return D[a][m] * T[b][m] + T[a][m] * D[b][m];

@@ -42,31 +42,42 @@ inline void overlap_records(const double *A, const double *B, std::vector<double
 // Radial sums of one atom pair: F[0..4] = ss, ps, sp, pp(AB AB), pp(delta); D[0..4] their 2ab/g-weighted
 // companions (derivs only).  Primitive pairs are spread over the lanes; `used` (bit k = sum k) selects the
 // sums the pair's shells need, and only those are warp-reduced.
-__device__ __forceinline__ void overlap_sums(const double *__restrict__ rec, int nrec, double R2, bool derivs, int used,
-                                             double *F, double *D)
+__device__ __forceinline__ double ov_exp(double x) { return exp(x); }
+__device__ __forceinline__ float ov_exp(float x) { return __expf(x); }
+__device__ __forceinline__ float warp_sum_r(float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_sum_r(double v) { return warp_sum(v); }
+
+// (Real = float: the records rounded to FP32 and the FP32 exponential, for the mixed method's gradients.)
+template <typename Real>
+__device__ __forceinline__ void overlap_sums(const Real *__restrict__ rec, int nrec, Real R2, bool derivs, int used,
+                                             Real *F, Real *D)
 {
     const int lane = threadIdx.x & 31;
-    double f0 = 0.0, f1 = 0.0, f2 = 0.0, f3 = 0.0, f4 = 0.0, d0 = 0.0, d1 = 0.0, d2 = 0.0, d3 = 0.0, d4 = 0.0;
+    Real f0 = 0, f1 = 0, f2 = 0, f3 = 0, f4 = 0, d0 = 0, d1 = 0, d2 = 0, d3 = 0, d4 = 0;
     for (int t = lane; t < nrec; t += 32) {
-        const double *r = rec + OV_REC * t;
-        const double abg = r[0], fac = abg * R2;
-        const double e = fac > PRIMITIVE_OVERLAP_TOLERANCE ? 0.0 : exp(-fac);
+        const Real *r = rec + OV_REC * t;
+        const Real abg = r[0], fac = abg * R2;
+        const Real e = fac > (Real)PRIMITIVE_OVERLAP_TOLERANCE ? Real(0) : ov_exp(-fac);
         const int ty = (int)r[3];
-        const double t1 = r[1] * e, t2 = r[2] * e;
-        f0 += ty == OV_SS ? t1 : 0.0; f1 += ty == OV_PS ? t1 : 0.0; f2 += ty == OV_SP ? t1 : 0.0; f3 += ty == OV_PP ? t1 : 0.0;
+        const Real t1 = r[1] * e, t2 = r[2] * e;
+        f0 += ty == OV_SS ? t1 : Real(0); f1 += ty == OV_PS ? t1 : Real(0); f2 += ty == OV_SP ? t1 : Real(0); f3 += ty == OV_PP ? t1 : Real(0);
         f4 += t2;
         if (derivs) {
-            const double a2 = abg + abg, u1 = a2 * t1;
-            d0 += ty == OV_SS ? u1 : 0.0; d1 += ty == OV_PS ? u1 : 0.0; d2 += ty == OV_SP ? u1 : 0.0; d3 += ty == OV_PP ? u1 : 0.0;
+            const Real a2 = abg + abg, u1 = a2 * t1;
+            d0 += ty == OV_SS ? u1 : Real(0); d1 += ty == OV_PS ? u1 : Real(0); d2 += ty == OV_SP ? u1 : Real(0); d3 += ty == OV_PP ? u1 : Real(0);
             d4 = fma(a2, t2, d4);
         }
     }
-    const double fl[5] = { f0, f1, f2, f3, f4 }, dl[5] = { d0, d1, d2, d3, d4 };
+    const Real fl[5] = { f0, f1, f2, f3, f4 }, dl[5] = { d0, d1, d2, d3, d4 };
 #pragma unroll
     for (int k = 0; k < 5; k++) {
         const int bit = k < 4 ? k : 3;
-        F[k] = (used >> bit & 1) ? warp_sum(fl[k]) : 0.0;
-        D[k] = (derivs && (used >> bit & 1)) ? warp_sum(dl[k]) : 0.0;
+        F[k] = (used >> bit & 1) ? warp_sum_r(fl[k]) : Real(0);
+        D[k] = (derivs && (used >> bit & 1)) ? warp_sum_r(dl[k]) : Real(0);
     }
 }
 
@@ -83,26 +94,27 @@ __device__ __forceinline__ double overlap_element(int a, int b, const double *AB
 }
 
 // sum_ab W_ab dS_ab / dR_i,k for a weight matrix W (W[a*4+b], a < noi, b < noj), from the radial sums.
-__device__ __forceinline__ void overlap_gradient(const double *W, int noi, int noj, const double *AB, const double *F,
-                                                 const double *D, double *g)
+template <typename Real>
+__device__ __forceinline__ void overlap_gradient(const Real *W, int noi, int noj, const Real *AB, const Real *F,
+                                                 const Real *D, Real *g)
 {
     const int ox[3] = { 2, 3, 1 };   // orbital of axis k: x -> px, y -> py, z -> pz
-    double radial = W[0] * D[0];
-    double wps[3] = { 0, 0, 0 }, wsp[3] = { 0, 0, 0 }, u[3] = { 0, 0, 0 }, v[3] = { 0, 0, 0 };
+    Real radial = W[0] * D[0];
+    Real wps[3] = { 0, 0, 0 }, wsp[3] = { 0, 0, 0 }, u[3] = { 0, 0, 0 }, v[3] = { 0, 0, 0 };
     if (noi > 1) {
-        double s = 0.0;
+        Real s = 0;
         for (int k = 0; k < 3; k++) { wps[k] = W[ox[k] * 4]; s += wps[k] * AB[k]; }
         radial += s * D[1];
     }
     if (noj > 1) {
-        double s = 0.0;
+        Real s = 0;
         for (int k = 0; k < 3; k++) { wsp[k] = W[ox[k]]; s += wsp[k] * AB[k]; }
         radial -= s * D[2];
     }
     if (noi > 1 && noj > 1) {
-        double q = 0.0, tr = 0.0;
+        Real q = 0, tr = 0;
         for (int k = 0; k < 3; k++) {
-            for (int l = 0; l < 3; l++) { const double w = W[ox[k] * 4 + ox[l]]; u[k] += w * AB[l]; v[l] += w * AB[k]; }
+            for (int l = 0; l < 3; l++) { const Real w = W[ox[k] * 4 + ox[l]]; u[k] += w * AB[l]; v[l] += w * AB[k]; }
             tr += W[ox[k] * 4 + ox[k]];
         }
         for (int k = 0; k < 3; k++) q += AB[k] * u[k];
