@@ -248,43 +248,48 @@ __constant__ const int8_t SPS_MN[5] = { L_SS, L_PZS, L_PZPZ, L_PXPX, L_PYPY };
 // The five local values on the sp side and the electron-core vector of the sp atom's electrons (from the
 // multipole terms s_k, or their r-derivatives), and the s atom's electron-core term.
 // sp_i: the sp atom is i (terms 1-6, core terms MP_CORE_I..), else j (terms 7-12, MP_CORE_J..).
-__device__ __forceinline__ void sps_local(const double *to, const double *ta, double r, bool sp_i, bool deriv, double *Lv,
-                                          double *cv, double &c_s)
+__device__ __forceinline__ double rsq(double x) { return rsqrt(x); }
+__device__ __forceinline__ float rsq(float x) { return rsqrtf(x); }
+
+template <typename Real>
+__device__ __forceinline__ void sps_local(const double *to, const double *ta, double r, bool sp_i, bool deriv, Real *Lv,
+                                          Real *cv, Real &c_s)
 {
-    auto term = [&](int k) -> double {
+    auto term = [&](int k) -> Real {
         const double a = ta[k];
-        if (a < 0.0) return 0.0;
-        const double ro = r + to[k], sv = rsqrt(ro * ro + a);
+        if (a < 0.0) return Real(0);
+        const Real ro = (Real)(r + to[k]), sv = rsq(ro * ro + (Real)a);
         return deriv ? -ro * sv * sv * sv : sv;
     };
     const int b = sp_i ? 1 : 7;
-    const double r0 = term(0), s1 = term(b), s2 = term(b + 1), s3 = term(b + 2), s4 = term(b + 3), s5 = term(b + 4), s6 = term(b + 5);
-    const double dz = -0.5 * (s1 - s2), qzz = 0.25 * (s3 + s4) - 0.5 * s5, qxx = 0.5 * (s6 - s5);
+    const Real r0 = term(0), s1 = term(b), s2 = term(b + 1), s3 = term(b + 2), s4 = term(b + 3), s5 = term(b + 4), s6 = term(b + 5);
+    const Real dz = Real(-0.5) * (s1 - s2), qzz = Real(0.25) * (s3 + s4) - Real(0.5) * s5, qxx = Real(0.5) * (s6 - s5);
     Lv[0] = r0; Lv[1] = dz; Lv[2] = r0 + qzz; Lv[3] = r0 + qxx; Lv[4] = r0 + qxx;
     const int c0 = sp_i ? MP_CORE_I : MP_CORE_J;
-    const double c1 = term(c0 + 1), c2 = term(c0 + 2), c3 = term(c0 + 3), c4 = term(c0 + 4), c5 = term(c0 + 5), c6 = term(c0 + 6);
-    const double c7 = term(c0 + 7);
-    const double cq = 0.25 * (c3 + c4) - 0.5 * c5, cx = 0.5 * (c6 - c5);
-    cv[0] = term(c0); cv[1] = -0.5 * (c1 - c2); cv[2] = c7 + cq; cv[3] = c7 + cx; cv[4] = c7 + cx;
+    const Real c1 = term(c0 + 1), c2 = term(c0 + 2), c3 = term(c0 + 3), c4 = term(c0 + 4), c5 = term(c0 + 5), c6 = term(c0 + 6);
+    const Real c7 = term(c0 + 7);
+    const Real cq = Real(0.25) * (c3 + c4) - Real(0.5) * c5, cx = Real(0.5) * (c6 - c5);
+    cv[0] = term(c0); cv[1] = Real(-0.5) * (c1 - c2); cv[2] = c7 + cq; cv[3] = c7 + cx; cv[4] = c7 + cx;
     c_s = term(sp_i ? MP_CORE_J : MP_CORE_I);
 }
 
 // Overlap radial sums of one pair by one thread (overlap_sums without the warp).
-__device__ __forceinline__ void overlap_sums_thread(const double *__restrict__ rec, int nrec, double R2, bool derivs, double *F, double *D)
+template <typename Real>
+__device__ __forceinline__ void overlap_sums_thread(const Real *__restrict__ rec, int nrec, Real R2, bool derivs, Real *F, Real *D)
 {
-    double f0 = 0.0, f1 = 0.0, f2 = 0.0, f3 = 0.0, f4 = 0.0, d0 = 0.0, d1 = 0.0, d2 = 0.0, d3 = 0.0, d4 = 0.0;
+    Real f0 = 0, f1 = 0, f2 = 0, f3 = 0, f4 = 0, d0 = 0, d1 = 0, d2 = 0, d3 = 0, d4 = 0;
     for (int t = 0; t < nrec; t++) {
-        const double *q = rec + OV_REC * t;
-        const double abg = q[0], fac = abg * R2;
-        if (fac > PRIMITIVE_OVERLAP_TOLERANCE) continue;
-        const double e = exp(-fac);
+        const Real *q = rec + OV_REC * t;
+        const Real abg = q[0], fac = abg * R2;
+        if (fac > (Real)PRIMITIVE_OVERLAP_TOLERANCE) continue;
+        const Real e = ov_exp(-fac);
         const int ty = (int)q[3];
-        const double t1 = q[1] * e, t2 = q[2] * e;
-        f0 += ty == OV_SS ? t1 : 0.0; f1 += ty == OV_PS ? t1 : 0.0; f2 += ty == OV_SP ? t1 : 0.0; f3 += ty == OV_PP ? t1 : 0.0;
+        const Real t1 = q[1] * e, t2 = q[2] * e;
+        f0 += ty == OV_SS ? t1 : Real(0); f1 += ty == OV_PS ? t1 : Real(0); f2 += ty == OV_SP ? t1 : Real(0); f3 += ty == OV_PP ? t1 : Real(0);
         f4 += t2;
         if (derivs) {
-            const double a2 = abg + abg, u1 = a2 * t1;
-            d0 += ty == OV_SS ? u1 : 0.0; d1 += ty == OV_PS ? u1 : 0.0; d2 += ty == OV_SP ? u1 : 0.0; d3 += ty == OV_PP ? u1 : 0.0;
+            const Real a2 = abg + abg, u1 = a2 * t1;
+            d0 += ty == OV_SS ? u1 : Real(0); d1 += ty == OV_PS ? u1 : Real(0); d2 += ty == OV_SP ? u1 : Real(0); d3 += ty == OV_PP ? u1 : Real(0);
             d4 = fma(a2, t2, d4);
         }
     }
@@ -417,9 +422,6 @@ void launch_batch_integrals(const Batch &b, const double *xyz, double *ws, cudaS
 // Gradients.
 #define PG_WARPS 4
 #define PG_SM 1408
-
-__device__ __forceinline__ double rsq(double x) { return rsqrt(x); }
-__device__ __forceinline__ float rsq(float x) { return rsqrtf(x); }
 
 // Real = double: the reference's FP64 arithmetic.  Real = float (the mixed method): the pair's multipole terms,
 // rotation, density terms, contractions and overlap sums in FP32, the core-core term and the assembly of the
@@ -643,7 +645,9 @@ __global__ void __launch_bounds__(256) k_pair_gradients_ss(DeviceSystem sys0, Fr
 
 // sp-s pairs, one thread per pair: the gradient terms of k_pair_gradients for a pair with one sp and one s
 // atom (Gamma over the sp atom's ten distributions, the five local values, dC/dx of the sp side only).
-template <bool BATCH>
+// Real = float (the mixed method): local values, rotation, contraction and overlap sums in FP32; the core-core
+// term and the assembly of the pair gradient in FP64.
+template <bool BATCH, typename Real>
 __global__ void __launch_bounds__(128) k_pair_gradients_sps(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt,
                                                            const double *__restrict__ xyz, const double *__restrict__ density,
                                                            double *__restrict__ ws)
@@ -666,39 +670,39 @@ __global__ void __launch_bounds__(128) k_pair_gradients_sps(DeviceSystem sys0, F
     // one-centre densities (off-diagonal elements doubled) and Gamma over the sp atom's distributions:
     // Gamma_ab = 1/4 aa (P_{s,a} P_{s,b} + P_{s,b} P_{s,a}) - one_sp[ab] one_s  (QCModelMNDOState.c:196-250)
     const double one_s = P[(size_t)bs * N + bs];
-    double one_sp[10], gam[10];
+    Real one_sp[10], gam[10];
 #pragma unroll
     for (int ab = 0; ab < 10; ab++) {
         const int a = MP_DA[ab], b = MP_DB[ab];
-        const double f = (a == b) ? 1.0 : 2.0;
-        one_sp[ab] = f * P[(size_t)(as + a) * N + as + b];
-        gam[ab] = 0.5 * f * P[(size_t)bs * N + as + a] * P[(size_t)bs * N + as + b] - one_sp[ab] * one_s;
+        const double f = (a == b) ? 1.0 : 2.0, o = f * P[(size_t)(as + a) * N + as + b];
+        one_sp[ab] = (Real)o;
+        gam[ab] = (Real)(0.5 * f * P[(size_t)bs * N + as + a] * P[(size_t)bs * N + as + b] - o * one_s);
     }
     double eng[3] = { 0.0, 0.0, 0.0 };
     if (r >= 5.0e-3) {
         double dcore = 0.0;
         core_core(Ei, Ej, r, &dcore);
         const double *to = s.terms + (size_t)(eli * s.n_elements + elj) * 2 * MP_NTERMS, *ta = to + MP_NTERMS;
-        double Lv[5], cv[5], dLv[5], dcv[5], c_s, dc_s;
+        Real Lv[5], cv[5], dLv[5], dcv[5], c_s, dc_s;
         sps_local(to, ta, r, sp_i, false, Lv, cv, c_s);
         sps_local(to, ta, r, sp_i, true, dLv, dcv, dc_s);
         RotScalars q;
         rot_scalars(v3[0], v3[1], v3[2], r, 4, true, q);
-        Rotation rot;
+        RotationT<Real> rot;
         rot_assemble(q, true, rot);
-        const double zs = sp_i ? Ej[PDG_E_ZCORE] : Ei[PDG_E_ZCORE], zp = sp_i ? Ei[PDG_E_ZCORE] : Ej[PDG_E_ZCORE];
-        double t0 = 0.0, o0 = 0.0, tr[3] = { 0.0, 0.0, 0.0 }, orr[3] = { 0.0, 0.0, 0.0 };
+        const Real zs = (Real)(sp_i ? Ej[PDG_E_ZCORE] : Ei[PDG_E_ZCORE]), zp = (Real)(sp_i ? Ei[PDG_E_ZCORE] : Ej[PDG_E_ZCORE]);
+        Real t0 = 0, o0 = 0, tr[3] = { 0, 0, 0 }, orr[3] = { 0, 0, 0 };
 #pragma unroll
         for (int ab = 0; ab < 10; ab++) {
-            double u0 = 0.0, w0 = 0.0, ur[3] = { 0.0, 0.0, 0.0 }, wr[3] = { 0.0, 0.0, 0.0 };
+            Real u0 = 0, w0 = 0, ur[3] = { 0, 0, 0 }, wr[3] = { 0, 0, 0 };
 #pragma unroll
             for (int k = 0; k < 5; k++) {
-                const double c = ctrans(rot.T, ab, SPS_MN[k]);
+                const Real c = ctrans(rot.T, ab, SPS_MN[k]);
                 u0 = fma(c, dLv[k], u0);
                 w0 = fma(c, dcv[k], w0);
 #pragma unroll
                 for (int xx = 0; xx < 3; xx++) {
-                    const double cd = ctrans_d(rot.T, rot.D[xx], ab, SPS_MN[k]);
+                    const Real cd = ctrans_d(rot.T, rot.D[xx], ab, SPS_MN[k]);
                     ur[xx] = fma(cd, Lv[k], ur[xx]);
                     wr[xx] = fma(cd, cv[k], wr[xx]);
                 }
@@ -708,27 +712,29 @@ __global__ void __launch_bounds__(128) k_pair_gradients_sps(DeviceSystem sys0, F
 #pragma unroll
             for (int xx = 0; xx < 3; xx++) { tr[xx] = fma(gam[ab], ur[xx], tr[xx]); orr[xx] = fma(one_sp[ab] * wr[xx], -zs, orr[xx]); }
         }
-        o0 = fma(one_s * dc_s, -zp, o0);
+        o0 = fma((Real)one_s * dc_s, -zp, o0);
         // eng = -s (dcore + doei0f + dtei0f) + doei1 + dtei1   (MNDOIntegrals.c:392-418)
         for (int xx = 0; xx < 3; xx++) {
             const double sx = v3[xx] / r;
-            eng[xx] = -sx * dcore - sx * o0 + sx * t0 - orr[xx] + tr[xx];
+            eng[xx] = -sx * dcore - sx * (double)o0 + sx * (double)t0 - (double)orr[xx] + (double)tr[xx];
         }
     }
     // resonance integral derivatives: sum (beta_a + beta_b) P_ab dS_ab / dR_i
     const int noi = s.atom_norb[i], noj = s.atom_norb[j];
-    double Wres[16];
+    Real Wres[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) {
         const int a = k / 4, b = k % 4;
-        Wres[k] = (a < noi && b < noj) ? (Ei[PDG_E_BETA + a] + Ej[PDG_E_BETA + b]) * P[(size_t)(is + a) * N + js + b] : 0.0;
+        Wres[k] = (a < noi && b < noj) ? (Real)((Ei[PDG_E_BETA + a] + Ej[PDG_E_BETA + b]) * P[(size_t)(is + a) * N + js + b]) : Real(0);
     }
     const int eo = eli * s.n_elements + elj;
-    double Fo[5], Do[5], gr[3];
-    overlap_sums_thread(s.ovl + (size_t)s.ovl_off[eo] * OV_REC, s.ovl_n[eo], R2, true, Fo, Do);
-    overlap_gradient(Wres, noi, noj, v3, Fo, Do, gr);
+    Real Fo[5], Do[5], gr[3];
+    const Real *orec = sizeof(Real) == sizeof(double) ? (const Real *)s.ovl : (const Real *)s.ovl32;
+    const Real ab3[3] = { (Real)v3[0], (Real)v3[1], (Real)v3[2] };
+    overlap_sums_thread(orec + (size_t)s.ovl_off[eo] * OV_REC, s.ovl_n[eo], (Real)R2, true, Fo, Do);
+    overlap_gradient(Wres, noi, noj, ab3, Fo, Do, gr);
     double *pg = ws + fv.ws + plan.pair_g + (size_t)p * 3;
-    for (int x = 0; x < 3; x++) pg[x] = eng[x] + gr[x];
+    for (int x = 0; x < 3; x++) pg[x] = eng[x] + (double)gr[x];
 }
 
 template <bool BATCH>
@@ -767,7 +773,10 @@ void launch_pair_gradients(const DeviceSystem &s, const FramePlan &p, int n_fram
     const long nss = (long)n_frames * s.n_ss;
     if (nss > 0) k_pair_gradients_ss<false><<<(int)((nss + 255) / 256), 256, 0, st>>>(s, p, n_frames, none, xyz, density, ws);
     const long nsps = (long)n_frames * s.n_sps;
-    if (nsps > 0) k_pair_gradients_sps<false><<<(int)((nsps + 127) / 128), 128, 0, st>>>(s, p, n_frames, none, xyz, density, ws);
+    if (nsps > 0) {
+        if (fp32_terms) k_pair_gradients_sps<false, float><<<(int)((nsps + 127) / 128), 128, 0, st>>>(s, p, n_frames, none, xyz, density, ws);
+        else k_pair_gradients_sps<false, double><<<(int)((nsps + 127) / 128), 128, 0, st>>>(s, p, n_frames, none, xyz, density, ws);
+    }
 }
 
 void launch_reduce_gradients(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *ws, double *grad, cudaStream_t st)
@@ -791,6 +800,9 @@ void launch_batch_gradients(const Batch &b, const double *xyz, const double *den
     if (b.total[PDG_WORK_SS] > 0)
         k_pair_gradients_ss<true><<<(b.total[PDG_WORK_SS] + 255) / 256, 256, 0, st>>>(s0, p0, 0, b, xyz, density, ws);
     if (b.total[PDG_WORK_SPS] > 0)
-        k_pair_gradients_sps<true><<<(b.total[PDG_WORK_SPS] + 127) / 128, 128, 0, st>>>(s0, p0, 0, b, xyz, density, ws);
+    {
+        if (fp32_terms) k_pair_gradients_sps<true, float><<<(b.total[PDG_WORK_SPS] + 127) / 128, 128, 0, st>>>(s0, p0, 0, b, xyz, density, ws);
+        else k_pair_gradients_sps<true, double><<<(b.total[PDG_WORK_SPS] + 127) / 128, 128, 0, st>>>(s0, p0, 0, b, xyz, density, ws);
+    }
     k_reduce_gradients<true><<<(b.total[PDG_WORK_ATOM] + 7) / 8, 256, 0, st>>>(s0, p0, 0, b, ws, grad);
 }
