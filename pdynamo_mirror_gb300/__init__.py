@@ -14,5 +14,6 @@ from .guess import LearnedDensityGuess
 from .nbmodel import NBModelABFS, NBModelFull
 from .qcmodel import QCModelMNDO
 from .system import ElectronicState, SCFNotConverged, System
+from .trajectory import DCDTrajectoryFileReader, DCDTrajectoryFileWriter
 
-__all__ = ["DIISSCFConverger", "LangevinDynamics", "LangevinDynamics_SystemGeometry", "LangevinVelocityVerletIntegrator", "MoleculeBatch", "ElectronicState", "LearnedDensityGuess", "NBModelABFS", "NBModelFull", "QCModelMNDO", "SCFNotConverged", "System"]
+__all__ = ["DCDTrajectoryFileReader", "DCDTrajectoryFileWriter", "DIISSCFConverger", "LangevinDynamics", "LangevinDynamics_SystemGeometry", "LangevinVelocityVerletIntegrator", "MoleculeBatch", "ElectronicState", "LearnedDensityGuess", "NBModelABFS", "NBModelFull", "QCModelMNDO", "SCFNotConverged", "System"]

@@ -236,25 +236,48 @@ class LangevinDynamics:
         mv2 = self.mv2.cpu().numpy()
         return 0.5 * AMUA2PS2_TO_KJMOL * mv2, AMUA2PS2_TO_K * mv2 / self.dof
 
-    def run(self, steps, callback=None):
-        """steps Iterations; callback(self, r) after each.  Returns the SCF cycles per step (device tensors)."""
+    def replica_coordinates(self, replica=0):
+        """All atoms of one replica (host, Angstrom): the system's coordinates with that replica's QC atoms."""
+        X = np.array(self.system.coordinates3, dtype=np.float64)
+        X[self.system.qcSelection] = self.xyz[replica].cpu().numpy()
+        if self.mm_xyz is not None:   # the replica's fixed atoms, as it was given them
+            X[self.system.mm_indices()] = self.mm_xyz[replica].cpu().numpy()
+        return X
+
+    def run(self, steps, callback=None, trajectories=None, replica=0):
+        """steps Iterations; callback(self, r) after each.  trajectories: [(writer, saveFrequency)], e.g. a
+        DCDTrajectoryFileWriter, written with the coordinates of `replica` at iteration 0 and at every multiple of
+        saveFrequency, as the reference's objective function logs them (pCore-1.9.0/pCore/ObjectiveFunction.py:274-295).
+        Returns the SCF cycles per step (device tensors)."""
+        trajectories = [(t, int(f)) for (t, f) in (trajectories or []) if t is not None and int(f) > 0]
+        if trajectories and self.last is None:
+            self.initialize()
+        for t, f in trajectories:
+            if len(t) == 0:
+                t.WriteHeader()
+            if self.n_step % f == 0:
+                t.WriteFrame(self.replica_coordinates(replica))
         cycles = []
         for _ in range(int(steps)):
             r = self.step()
             cycles.append(r["ncycles"])
+            for t, f in trajectories:
+                if self.n_step % f == 0:
+                    t.WriteFrame(self.replica_coordinates(replica))
             if callback is not None:
                 callback(self, r)
         return cycles
 
 
 def LangevinDynamics_SystemGeometry(system, steps=1000, timeStep=0.001, temperature=300.0, collisionFrequency=25.0, seed=0,
-                                    densityGuess="previous", replicas=1, callback=None):
+                                    densityGuess="previous", replicas=1, callback=None, trajectories=None):
     """Langevin dynamics of the system's free atoms (MolecularDynamics.py:42-48 keywords: steps, timeStep in ps,
-    temperature, collisionFrequency).  Leaves the last coordinates of replica 0 on system.coordinates3 and its
-    velocities on system.configuration.velocities; returns the LangevinDynamics object."""
+    temperature, collisionFrequency, trajectories = [(trajectory, saveFrequency)] of replica 0).  Leaves the last
+    coordinates of replica 0 on system.coordinates3 and its velocities on system.configuration.velocities; returns
+    the LangevinDynamics object."""
     md = LangevinDynamics(system, replicas=replicas, timeStep=timeStep, temperature=temperature,
                           collisionFrequency=collisionFrequency, seed=seed, densityGuess=densityGuess)
-    md.run(steps, callback)
+    md.run(steps, callback, trajectories=trajectories)
     X = md.xyz[0].cpu().numpy()
     for k, i in enumerate(system.qcSelection):
         system.coordinates3[i] = X[k]

@@ -192,3 +192,21 @@ def test_trajectories_do_not_depend_on_the_start_density():
         np.testing.assert_allclose(xs[mode], xs["diagonal"], rtol=0, atol=1e-7)
     assert cycles["extrapolate"] < cycles["diagonal"]
     assert cycles["previous"] < cycles["diagonal"]
+
+
+def test_dynamics_writes_a_dcd_trajectory(tmp_path):
+    """Frames at iteration 0 and every saveFrequency-th step of the chosen replica, fixed MM atoms once."""
+    from pdynamo_mirror_gb300 import DCDTrajectoryFileReader, DCDTrajectoryFileWriter, LangevinDynamics
+    s, Zq, mmX, q = _trimer()
+    md = LangevinDynamics(s, replicas=2, timeStep=0.0005, seed=3)
+    X0 = md.replica_coordinates(1)
+    w = DCDTrajectoryFileWriter(tmp_path / "md.dcd", s, timeStep=0.0005, saveFrequency=2)
+    snaps = []
+    md.run(6, callback=lambda m, r: snaps.append(m.replica_coordinates(1)), trajectories=[(w, 2)], replica=1)
+    w.Close()
+    r = DCDTrajectoryFileReader(tmp_path / "md.dcd")
+    assert len(r) == 4 and r.numberOfFixedAtoms == 3
+    np.testing.assert_array_equal(r.ReadFrame(0), X0.astype(np.float32))
+    for k in range(1, 4):
+        np.testing.assert_array_equal(r.ReadFrame(k), snaps[2 * k - 1].astype(np.float32))
+    assert not np.allclose(r.ReadFrame(3)[:len(Zq)], r.ReadFrame(0)[:len(Zq)])
