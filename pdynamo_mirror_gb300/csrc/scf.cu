@@ -1284,6 +1284,10 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
             __syncthreads();
             const int newest = ctl[20], matnum = ctl[1];
             double *hp = wsf + pl.hP + (size_t)newest * hl, *hf = wsf + pl.hF + (size_t)newest * hl, *he = wsf + pl.hE + (size_t)newest * hl;
+            // the mixed method keeps its DIIS error vectors in FP32 (in the same slots) and forms the B matrix from
+            // FP32 products: the error vectors only steer the extrapolation
+            float *hef = (float *)he;
+            auto put_error = [&](int idx, double ev) { if (delta_commutator) hef[idx] = (float)ev; else he[idx] = ev; };
             for (int i = tid / 32; i < N; i += PDG_WARPS)
                 for (int j = tid % 32; j <= i; j += 32) { hp[i * (i + 1) / 2 + j] = P[(size_t)i * N + j]; hf[i * (i + 1) / 2 + j] = F[(size_t)i * N + j]; }
             double emx = 0.0;
@@ -1298,7 +1302,7 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
                 auto store = [&](int i, int j, double v) {
                     if (j >= i) return;
                     const double ev = sg * v;
-                    he[i * (i - 1) / 2 + j] = ev;
+                    put_error(i * (i - 1) / 2 + j, ev);
                     emx = fmax(emx, fabs(ev));
                 };
                 if (delta_commutator) {
@@ -1382,7 +1386,7 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
                 for (int i = tid / 32; i < N; i += PDG_WARPS)
                     for (int j = tid % 32; j < i; j += 32) {
                         const double ev = FP[(size_t)i * N + j] - FP[(size_t)j * N + i];
-                        he[i * (i - 1) / 2 + j] = ev;
+                        put_error(i * (i - 1) / 2 + j, ev);
                         emx = fmax(emx, fabs(ev));
                     }
                 __syncthreads();
@@ -1391,13 +1395,34 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
             double dots[PDG_MAX_HISTORY];
             for (int m = 0; m < PDG_MAX_HISTORY; m++) dots[m] = 0.0;
             const int ne = N * (N - 1) / 2;
-            for (int k = tid; k < ne; k += PDG_BLOCK) {
-                double en_ = he[k];
-                for (int m = 0; m < matnum; m++) dots[m] += wsf[pl.hE + (size_t)ctl[2 + m] * hl + k] * en_;
+            if (delta_commutator) {
+                float d32[PDG_MAX_HISTORY];
+                for (int m = 0; m < PDG_MAX_HISTORY; m++) d32[m] = 0.f;
+                for (int k = tid; k < ne; k += PDG_BLOCK) {
+                    const float en_ = hef[k];
+                    for (int m = 0; m < matnum; m++) d32[m] = fmaf(((const float *)(wsf + pl.hE + (size_t)ctl[2 + m] * hl))[k], en_, d32[m]);
+                }
+                for (int m = 0; m < matnum; m++) dots[m] = (double)d32[m];
+            } else {
+                for (int k = tid; k < ne; k += PDG_BLOCK) {
+                    double en_ = he[k];
+                    for (int m = 0; m < matnum; m++) dots[m] += wsf[pl.hE + (size_t)ctl[2 + m] * hl + k] * en_;
+                }
             }
-            for (int m = 0; m < matnum; m++) {
-                double b = 2.0 * block_sum(dots[m], sm.red);
-                if (tid == 0) { int n = ctl[2 + m]; Bm[n * PDG_MAX_HISTORY + newest] = b; Bm[newest * PDG_MAX_HISTORY + n] = b; }
+            {   // all B-matrix entries in one block reduction (per entry the order of block_sum: lanes, then warps)
+                double *rs = sm.ta;
+                for (int m = 0; m < matnum; m++) {
+                    const double v = warp_sum(dots[m]);
+                    if (lane == 0) rs[w * PDG_MAX_HISTORY + m] = v;
+                }
+                __syncthreads();
+                if (tid < matnum) {
+                    double t = 0.0;
+                    for (int q = 0; q < PDG_WARPS; q++) t += rs[q * PDG_MAX_HISTORY + tid];
+                    const double b = 2.0 * t;
+                    const int n = ctl[2 + tid];
+                    Bm[n * PDG_MAX_HISTORY + newest] = b; Bm[newest * PDG_MAX_HISTORY + n] = b;
+                }
             }
             __syncthreads();
             tm.lap(PDG_T_DIIS_SAVE);
