@@ -534,7 +534,7 @@ __device__ void inverse_iteration(int N, int t, double sigma, double tiny, const
 // matrix whose reflectors are in A, their eigenvectors by inverse iteration, back-transformed to the rows of Z
 // (kv rows of ldz; z_in_smem when Z is the shared-memory slot).  The eigenvalues are left in sm.eig[0 .. kv).
 __device__ void tridiag_vectors(const SCFArgs &a, double *wsf, const double *A, Smem &sm, Timer &tm, int first, int kv, double *Z,
-                                bool z_in_smem, bool count_step = true)
+                                bool z_in_smem, bool count_step = true, bool back = true)
 {
     const DeviceSystem &s = a.s;
     const FramePlan &pl = a.plan;
@@ -617,6 +617,7 @@ __device__ void tridiag_vectors(const SCFArgs &a, double *wsf, const double *A, 
     }
     tm.lap(PDG_T_EIGENVECTORS);
     // --- back-transformation Z <- Q Z, Q = H_0 H_1 ... H_{N-3} with the reflectors stored in A
+    if (!back) return;
     if (N >= 32) {
         // blocked (compact WY, as LAPACK's dlarft / dlarfb): blocks of up to 16 consecutive reflectors, last
         // block first; block b is I - V T V^T with V the reflectors' unit lower-trapezoidal columns over rows
@@ -675,6 +676,51 @@ __device__ void tridiag_vectors(const SCFArgs &a, double *wsf, const double *A, 
             }
         }
         __syncthreads();
+    }
+}
+
+// Back-transformation of nv vectors of T in FP32 (rows of Zt, N floats each): the blocked compact-WY scheme of
+// tridiag_vectors with V^T V, T and both products in FP32.  For the complementary vectors of the perturbative base:
+// they enter the perturbative steps only in products with a small factor (dF, K), so their FP32 errors (~1e-7,
+// their orthogonality to the FP64 wanted vectors included) stay ~1e-7 of a small quantity, while the wanted vectors,
+// whose projector is the base density, keep the FP64 transformation.  work: 32 nv + 512 floats.  N >= 32.
+__device__ void back_transform32(int N, float *work, const double *A, Smem &sm, int nv, float *Zt)
+{
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int nref = N - 2;
+    float *Wm = work, *W2 = Wm + (size_t)16 * nv, *Sg = W2 + (size_t)16 * nv, *Tt = Sg + 256;
+    for (int k0 = ((nref - 1) / 16) * 16; k0 >= 0; k0 -= 16) {
+        const int nbk = min(16, nref - k0), m0 = N - k0 - 1;
+        auto V = [&](int i, int c) -> float { return i < c ? 0.f : (i == c ? 1.f : (float)A[plo(k0 + 1 + i, k0 + c)]); };
+        tgemm32<false, true>(nbk, 16 + nv, m0, [&](int c, int i) { return V(i, c); },
+                             [&](int i, int j) { return j < 16 ? (j < nbk ? V(i, j) : 0.f) : Zt[(size_t)(j - 16) * N + k0 + 1 + i]; },
+                             false, sm, [&](int c, int j, double v) {
+                                 if (j < 16) Sg[c * 16 + j] = (float)v;
+                                 else Wm[(size_t)c * nv + (j - 16)] = (float)v;
+                             });
+        if (w == 0) {   // T(c, c) = tau_c;  T(0:c, c) = -tau_c T(0:c, 0:c) S(0:c, c)
+            for (int c = 0; c < nbk; c++) {
+                const float tau = (float)sm.tau[k0 + c];
+                float t = 0.f;
+                if (lane < c) {
+                    for (int j = lane; j < c; j++) t = fmaf(Tt[lane * 16 + j], Sg[j * 16 + c], t);
+                    t *= -tau;
+                }
+                __syncwarp();
+                if (lane < 16) Tt[lane * 16 + c] = lane < c ? t : (lane == c ? tau : 0.f);
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        for (int e = tid; e < nbk * nv; e += PDG_BLOCK) {
+            const int c = e / nv, t = e % nv;
+            float acc = 0.f;
+            for (int j = c; j < nbk; j++) acc = fmaf(Tt[c * 16 + j], Wm[(size_t)j * nv + t], acc);
+            W2[(size_t)c * nv + t] = acc;
+        }
+        __syncthreads();
+        tgemm32<false, true>(nv, m0, nbk, [&](int t, int c) { return W2[(size_t)c * nv + t]; }, [&](int c, int i) { return V(i, c); },
+                             false, sm, [&](int t, int i, double v) { Zt[(size_t)t * N + k0 + 1 + i] -= (float)v; });
     }
 }
 
@@ -788,15 +834,18 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
         for (int e = tid; e < kv * N; e += PDG_BLOCK) BZ[(size_t)(e / N) * ldz + e % N] = Z[(size_t)(e / N) * ldz + e % N];
         for (int t = tid; t < kv; t += PDG_BLOCK) BL[t] = sm.eig[t];
         __syncthreads();
+        // (the complementary vectors are back-transformed in FP32 below, straight into their FP32 copy)
         if (nc > 0) {
-            tridiag_vectors(a, wsf, A, sm, tm, s.vec_occupied ? kv : 0, nc, BV, false, false);
+            tridiag_vectors(a, wsf, A, sm, tm, s.vec_occupied ? kv : 0, nc, BV, false, false, N < 32);
             for (int t = tid; t < nc; t += PDG_BLOCK) BL[kv + t] = sm.eig[t];
         }
         __syncthreads();
-        // the same vectors rounded to FP32, the operands of the products with small factors
+        // the vectors in FP32, the operands of the products with small factors
         float *Zf = (float *)(wsf + pl.BW) + pert_dq_offset(N, kv) + 2 * (size_t)N * N, *Vf = Zf + (size_t)kv * N;
         for (int e = tid; e < kv * N; e += PDG_BLOCK) Zf[e] = (float)BZ[(size_t)(e / N) * ldz + e % N];
         for (int e = tid; e < nc * N; e += PDG_BLOCK) Vf[e] = (float)BV[(size_t)(e / N) * ldz + e % N];
+        __syncthreads();
+        if (N >= 32 && nc > 0) back_transform32(N, (float *)(wsf + pl.LU), A, sm, nc, Vf);
         float *Gi = Vf + (size_t)nc * N;   // reciprocal gaps, the fixed-point sweeps' divisors
         for (int e = tid; e < nc * kv; e += PDG_BLOCK) Gi[e] = (float)(1.0 / (BL[e % kv] - BL[kv + e / kv]));
         __syncthreads();
