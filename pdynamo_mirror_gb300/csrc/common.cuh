@@ -46,7 +46,7 @@ struct DeviceSystem {
 // Per-frame workspace plan (all offsets in doubles from the frame's base).
 struct FramePlan {
     size_t tei, pair_e, pair_g, H, F, P0, A, G, Z, LU, LO, hP, hF, hE, rP, rF, misc, stride;
-    size_t BF, BP, BZ, BV, BL, BW;   // perturbative density steps: base F, P, wanted and complement vectors, eigenvalues, FP32 work
+    size_t BF, BP, BZ, BL, BW;   // perturbative density steps: base F, P, wanted vectors, eigenvalues, FP32 work (incl. the complement)
     int hist_len;   // packed history vector length N(N+1)/2 (errors use N(N-1)/2 within the same slot)
 };
 
@@ -100,11 +100,11 @@ __host__ inline FramePlan make_plan(const DeviceSystem &s, int history)
     p.rF = o;     o += align32(NN);
     p.misc = o;   o += align32(PDG_MAX_HISTORY * PDG_MAX_HISTORY + 96);   // DIIS B matrix, then PDG_NTIMERS phase timers
     // base of the perturbative density steps (mixed method): the Fock matrix and density of the last FP64
-    // step, its wanted vectors and their complement (FP64, rows of N | 1), their eigenvalues, and FP32 work
+    // step, its wanted vectors (FP64, rows of N | 1), all eigenvalues, and FP32 work (which holds the complementary
+    // vectors, computed in FP32)
     p.BF = o;     o += align32(NN);
     p.BP = o;     o += align32(NN);
     p.BZ = o;     o += align32(kv * (N | 1));
-    p.BV = o;     o += align32(nc * (N | 1));
     p.BL = o;     o += align32(N);
     p.BW = o;     o += align32((pert_work_floats(N, (int)kv) + 1) / 2);
     p.stride = align32(o);

@@ -443,60 +443,71 @@ __device__ void make_reflector(double *A, int N, int c, double *vout, Smem &sm)
     if (lane == 0) { sm.e[c] = e; sm.tau[c] = tau; }
 }
 
+__device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
+__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
+
 // Inverse iteration for one eigenvector of the tridiagonal T (d, e) at shift sigma, by ONE thread: the LU
 // factors of T - sigma I with row interchanges (dgttrf form: multiplier l_k, pivot flag, U row
 // 1/u_kk, u_k,k+1, u_k,k+2), four solves, re-orthogonalisation against the earlier vectors q0 .. t-1 of the
 // same cluster (dstein), normalisation.  The factor arrays and the iterate are interleaved by vector (stride
 // ld) so the threads of a warp access them coalesced.  Pivoting is branch-free (selects), so the lanes of a
-// warp never diverge; loads are issued in blocks of eight ahead of the dependent recurrence.
+// warp never diverge; loads are issued in blocks of eight ahead of the dependent recurrence.  R = float (the
+// perturbative base's complementary vectors): T - sigma I is formed in FP64 and rounded, everything after it is
+// FP32, and the iterate is rescaled by its largest element between solves (folded into the next forward pass).
+template <typename R>
 __device__ void inverse_iteration(int N, int t, double sigma, double tiny, const double *__restrict__ d, const double *__restrict__ e,
-                                  double *__restrict__ u0, double *__restrict__ u1, double *__restrict__ u2, double *__restrict__ lm,
-                                  unsigned char *__restrict__ pv, double *y, int ldy, int ld, const double *zq0, int nq, int ldz,
-                                  double *zout)
+                                  R *__restrict__ u0, R *__restrict__ u1, R *__restrict__ u2, R *__restrict__ lm,
+                                  unsigned char *__restrict__ pv, R *y, int ldy, int ld, const R *zq0, int nq, int ldz, R *zout)
 {
-    double ak = d[0] - sigma, bk = e[0];
+    constexpr bool F32 = sizeof(R) == 4;
+    const R rtiny = (R)tiny;
+    R ak = (R)(d[0] - sigma), bk = (R)e[0];
     for (int k = 0; k < N - 1; k++) {
-        const double ck = e[k], an = d[k + 1] - sigma, bn = e[k + 1];
+        const R ck = (R)e[k], an = (R)(d[k + 1] - sigma), bn = (R)e[k + 1];
         const bool sw = fabs(ak) < fabs(ck);
-        double piv = sw ? ck : ak;
-        if (fabs(piv) < tiny) piv = copysign(tiny, piv);
-        const double r = __drcp_rn(piv), l = (sw ? ak : ck) * r;
-        const double uu1 = sw ? an : bk, uu2 = sw ? bn : 0.0;
+        R piv = sw ? ck : ak;
+        if (fabs(piv) < rtiny) piv = copysign(rtiny, piv);
+        const R r = rcp_rn(piv), l = (sw ? ak : ck) * r;
+        const R uu1 = sw ? an : bk, uu2 = sw ? bn : (R)0;
         u0[(size_t)k * ld] = r; u1[(size_t)k * ld] = uu1; u2[(size_t)k * ld] = uu2; lm[(size_t)k * ld] = l; pv[(size_t)k * ld] = sw;
         ak = fma(-l, uu1, sw ? bk : an);
-        bk = fma(-l, uu2, sw ? 0.0 : bn);
+        bk = fma(-l, uu2, sw ? (R)0 : bn);
     }
-    if (fabs(ak) < tiny) ak = copysign(tiny, ak);
-    u0[(size_t)(N - 1) * ld] = __drcp_rn(ak);
-    for (int i = 0; i < N; i++) y[(size_t)i * ldy] = ((hash2(t * 2654435761u + 17u, i) >> 8) * (1.0 / 16777216.0)) * 2.0 - 1.0;
+    if (fabs(ak) < rtiny) ak = copysign(rtiny, ak);
+    u0[(size_t)(N - 1) * ld] = rcp_rn(ak);
+    for (int i = 0; i < N; i++) y[(size_t)i * ldy] = (R)(((hash2(t * 2654435761u + 17u, i) >> 8) * (1.0 / 16777216.0)) * 2.0 - 1.0);
+    R sc = (R)1;   // FP32: scale of the stored iterate (1 / its largest element after the last solve)
     for (int it = 0; it < 4; it++) {
         // forward: interchanges and L
-        double c = y[0];
+        R c = F32 ? y[0] * sc : y[0];
         int k = 0;
         for (; k + 8 <= N - 1; k += 8) {
-            double xn[8], l[8]; bool sw[8];
-#pragma unroll
-            for (int q = 0; q < 8; q++) { xn[q] = y[(size_t)(k + 1 + q) * ldy]; l[q] = lm[(size_t)(k + q) * ld]; sw[q] = pv[(size_t)(k + q) * ld]; }
+            R xn[8], l[8]; bool sw[8];
 #pragma unroll
             for (int q = 0; q < 8; q++) {
-                const double yk = sw[q] ? xn[q] : c, cn = sw[q] ? c : xn[q];
+                xn[q] = y[(size_t)(k + 1 + q) * ldy]; l[q] = lm[(size_t)(k + q) * ld]; sw[q] = pv[(size_t)(k + q) * ld];
+                if (F32) xn[q] *= sc;
+            }
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const R yk = sw[q] ? xn[q] : c, cn = sw[q] ? c : xn[q];
                 y[(size_t)(k + q) * ldy] = yk;
                 c = fma(-l[q], yk, cn);
             }
         }
         for (; k < N - 1; k++) {
-            const double xn = y[(size_t)(k + 1) * ldy], l = lm[(size_t)k * ld];
+            const R xn = F32 ? y[(size_t)(k + 1) * ldy] * sc : y[(size_t)(k + 1) * ldy], l = lm[(size_t)k * ld];
             const bool sw = pv[(size_t)k * ld];
-            const double yk = sw ? xn : c, cn = sw ? c : xn;
+            const R yk = sw ? xn : c, cn = sw ? c : xn;
             y[(size_t)k * ldy] = yk;
             c = fma(-l, yk, cn);
         }
         // back substitution with U
-        double x1 = c * u0[(size_t)(N - 1) * ld], x2 = 0.0;
+        R x1 = c * u0[(size_t)(N - 1) * ld], x2 = (R)0, mx = fabs(x1);
         y[(size_t)(N - 1) * ldy] = x1;
         k = N - 2;
         for (; k - 7 >= 0; k -= 8) {
-            double yy[8], a0[8], a1[8], a2[8];
+            R yy[8], a0[8], a1[8], a2[8];
 #pragma unroll
             for (int q = 0; q < 8; q++) {
                 const size_t o = (size_t)(k - q) * ld;
@@ -504,42 +515,92 @@ __device__ void inverse_iteration(int N, int t, double sigma, double tiny, const
             }
 #pragma unroll
             for (int q = 0; q < 8; q++) {
-                const double x0 = fma(-a2[q], x2, fma(-a1[q], x1, yy[q])) * a0[q];
+                const R x0 = fma(-a2[q], x2, fma(-a1[q], x1, yy[q])) * a0[q];
                 y[(size_t)(k - q) * ldy] = x0;
                 x2 = x1; x1 = x0;
+                if (F32) mx = fmax(mx, fabs(x0));
             }
         }
         for (; k >= 0; k--) {
             const size_t o = (size_t)k * ld;
-            const double x0 = fma(-u2[o], x2, fma(-u1[o], x1, y[(size_t)k * ldy])) * u0[o];
+            const R x0 = fma(-u2[o], x2, fma(-u1[o], x1, y[(size_t)k * ldy])) * u0[o];
             y[(size_t)k * ldy] = x0;
             x2 = x1; x1 = x0;
+            if (F32) mx = fmax(mx, fabs(x0));
         }
-        // the iterate is never rescaled between solves: four solves grow it by at most (1/tiny)^4, far
-        // inside the double range, and the projections below do not depend on its scale
+        // FP64: the iterate is never rescaled between solves: four solves grow it by at most (1/tiny)^4, far
+        // inside the double range, and the projections below do not depend on its scale.  FP32: one solve grows
+        // it by at most 1/tiny (~1e7), and the next pass reads it times 1/max.
+        if (F32) sc = mx > (R)0 ? (R)1 / mx : (R)1;
         for (int q = 0; q < nq; q++) {
-            const double *zq = zq0 + (size_t)q * ldz;
-            double dt = 0.0;
+            const R *zq = zq0 + (size_t)q * ldz;
+            R dt = (R)0;
             for (int i = 0; i < N; i++) dt = fma(y[(size_t)i * ldy], zq[i], dt);
             for (int i = 0; i < N; i++) y[(size_t)i * ldy] = fma(-dt, zq[i], y[(size_t)i * ldy]);
         }
     }
-    double nr = 0.0;
-    for (int i = 0; i < N; i++) { const double v = y[(size_t)i * ldy]; nr = fma(v, v, nr); }
-    const double sc = rsqrt(nr);
-    for (int i = 0; i < N; i++) zout[i] = y[(size_t)i * ldy] * sc;
+    R nr = (R)0;
+    for (int i = 0; i < N; i++) { const R v = F32 ? y[(size_t)i * ldy] * sc : y[(size_t)i * ldy]; nr = fma(v, v, nr); }
+    const R nsc = F32 ? sc * rsqrt(nr) : rsqrt(nr);
+    for (int i = 0; i < N; i++) zout[i] = y[(size_t)i * ldy] * nsc;
+}
+
+// Back-transformation of nv vectors of T in FP32 (rows of Zt, N floats each): the blocked compact-WY scheme of
+// tridiag_vectors with V^T V, T and both products in FP32.  For the complementary vectors of the perturbative base:
+// they enter the perturbative steps only in products with a small factor (dF, K), so their FP32 errors (~1e-7,
+// their orthogonality to the FP64 wanted vectors included) stay ~1e-7 of a small quantity, while the wanted vectors,
+// whose projector is the base density, keep the FP64 transformation.  work: 32 nv + 512 floats.  N >= 32.
+__device__ void back_transform32(int N, float *work, const double *A, Smem &sm, int nv, float *Zt)
+{
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int nref = N - 2;
+    float *Wm = work, *W2 = Wm + (size_t)16 * nv, *Sg = W2 + (size_t)16 * nv, *Tt = Sg + 256;
+    for (int k0 = ((nref - 1) / 16) * 16; k0 >= 0; k0 -= 16) {
+        const int nbk = min(16, nref - k0), m0 = N - k0 - 1;
+        auto V = [&](int i, int c) -> float { return i < c ? 0.f : (i == c ? 1.f : (float)A[plo(k0 + 1 + i, k0 + c)]); };
+        tgemm32<false, true>(nbk, 16 + nv, m0, [&](int c, int i) { return V(i, c); },
+                             [&](int i, int j) { return j < 16 ? (j < nbk ? V(i, j) : 0.f) : Zt[(size_t)(j - 16) * N + k0 + 1 + i]; },
+                             false, sm, [&](int c, int j, double v) {
+                                 if (j < 16) Sg[c * 16 + j] = (float)v;
+                                 else Wm[(size_t)c * nv + (j - 16)] = (float)v;
+                             });
+        if (w == 0) {   // T(c, c) = tau_c;  T(0:c, c) = -tau_c T(0:c, 0:c) S(0:c, c)
+            for (int c = 0; c < nbk; c++) {
+                const float tau = (float)sm.tau[k0 + c];
+                float t = 0.f;
+                if (lane < c) {
+                    for (int j = lane; j < c; j++) t = fmaf(Tt[lane * 16 + j], Sg[j * 16 + c], t);
+                    t *= -tau;
+                }
+                __syncwarp();
+                if (lane < 16) Tt[lane * 16 + c] = lane < c ? t : (lane == c ? tau : 0.f);
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        for (int e = tid; e < nbk * nv; e += PDG_BLOCK) {
+            const int c = e / nv, t = e % nv;
+            float acc = 0.f;
+            for (int j = c; j < nbk; j++) acc = fmaf(Tt[c * 16 + j], Wm[(size_t)j * nv + t], acc);
+            W2[(size_t)c * nv + t] = acc;
+        }
+        __syncthreads();
+        tgemm32<false, true>(nv, m0, nbk, [&](int t, int c) { return W2[(size_t)c * nv + t]; }, [&](int c, int i) { return V(i, c); },
+                             false, sm, [&](int t, int i, double v) { Zt[(size_t)t * N + k0 + 1 + i] -= (float)v; });
+    }
 }
 
 // Eigenvalues first .. first + kv - 1 of the tridiagonal T (sm.d, sm.e) left by the Householder reduction of the
 // matrix whose reflectors are in A, their eigenvectors by inverse iteration, back-transformed to the rows of Z
 // (kv rows of ldz; z_in_smem when Z is the shared-memory slot).  The eigenvalues are left in sm.eig[0 .. kv).
-__device__ void tridiag_vectors(const SCFArgs &a, double *wsf, const double *A, Smem &sm, Timer &tm, int first, int kv, double *Z,
-                                bool z_in_smem, bool count_step = true, bool back = true)
+template <typename R>
+__device__ void tridiag_vectors(const SCFArgs &a, double *wsf, const double *A, Smem &sm, Timer &tm, int first, int kv, R *Z, int ldz,
+                                bool z_in_smem, bool count_step = true)
 {
+    constexpr bool F32 = sizeof(R) == 4;
     const DeviceSystem &s = a.s;
     const FramePlan &pl = a.plan;
     const int N = s.n_basis, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int ldz = sm.ldz;
     // --- shifts: eigenvalues first .. first + kv - 1 of T by FP32 Sturm multisection, eight threads per eigenvalue,
     //     each round narrowing the bracket ninefold
     float *d32 = (float *)sm.e2, *e232 = d32 + N;
@@ -600,16 +661,16 @@ __device__ void tridiag_vectors(const SCFArgs &a, double *wsf, const double *A, 
     {
         const int rounds = sm.iv[0], kvp = (kv + 31) & ~31;
         if (tid == 0 && count_step) { tm.slot[PDG_T_ROUNDS] += rounds; tm.slot[PDG_T_DENSITY_STEPS] += 1.0; }
-        const double tiny = 2.2e-16 * fmax(sm.small[0], 1.0);
-        double *U0 = wsf + pl.LU, *U1 = U0 + (size_t)N * kvp, *U2 = U1 + (size_t)N * kvp, *LM = U2 + (size_t)N * kvp;
-        double *Y = LM + (size_t)N * kvp;
+        const double tiny = (F32 ? 1.2e-7 : 2.2e-16) * fmax(sm.small[0], 1.0);
+        R *U0 = (R *)(wsf + pl.LU), *U1 = U0 + (size_t)N * kvp, *U2 = U1 + (size_t)N * kvp, *LM = U2 + (size_t)N * kvp;
+        R *Y = LM + (size_t)N * kvp;
         unsigned char *PV = (unsigned char *)(Y + (size_t)N * kvp);
         for (int r = 0; r < rounds; r++) {
             for (int t = tid; t < kv; t += PDG_BLOCK) {
                 const int cs = sm.iv[64 + t];
                 if (t - cs != r) continue;
-                double *y = z_in_smem ? Z + (size_t)t * ldz : Y + t;   // in place in the output row when Z is in shared memory
-                inverse_iteration(N, t, sm.eig[t], tiny, sm.d, sm.e, U0 + t, U1 + t, U2 + t, LM + t, PV + t, y, z_in_smem ? 1 : kvp, kvp,
+                R *y = z_in_smem ? Z + (size_t)t * ldz : Y + t;   // in place in the output row when Z is in shared memory
+                inverse_iteration<R>(N, t, sm.eig[t], tiny, sm.d, sm.e, U0 + t, U1 + t, U2 + t, LM + t, PV + t, y, z_in_smem ? 1 : kvp, kvp,
                                   Z + (size_t)cs * ldz, t - cs, ldz, Z + (size_t)t * ldz);
             }
             __syncthreads();
@@ -617,8 +678,10 @@ __device__ void tridiag_vectors(const SCFArgs &a, double *wsf, const double *A, 
     }
     tm.lap(PDG_T_EIGENVECTORS);
     // --- back-transformation Z <- Q Z, Q = H_0 H_1 ... H_{N-3} with the reflectors stored in A
-    if (!back) return;
-    if (N >= 32) {
+    if constexpr (F32) {
+        if (N >= 32) { back_transform32(N, (float *)(wsf + pl.LU), A, sm, kv, Z); return; }   // rows of N floats
+    }
+    if (!F32 && N >= 32) {
         // blocked (compact WY, as LAPACK's dlarft / dlarfb): blocks of up to 16 consecutive reflectors, last
         // block first; block b is I - V T V^T with V the reflectors' unit lower-trapezoidal columns over rows
         // k0 + 1 .. N - 1 (row i of V is contiguous in the packed A) and T upper triangular.  Per block one GEMM
@@ -631,7 +694,7 @@ __device__ void tridiag_vectors(const SCFArgs &a, double *wsf, const double *A, 
             const int nbk = min(16, nref - k0), m0 = N - k0 - 1;
             auto V = [&](int i, int c) -> double { return i < c ? 0.0 : (i == c ? 1.0 : A[plo(k0 + 1 + i, k0 + c)]); };
             tgemm<false, true>(nbk, 16 + kv, m0, [&](int c, int i) { return V(i, c); },
-                               [&](int i, int j) { return j < 16 ? (j < nbk ? V(i, j) : 0.0) : Z[(size_t)(j - 16) * ldz + k0 + 1 + i]; },
+                               [&](int i, int j) { return j < 16 ? (j < nbk ? V(i, j) : 0.0) : (double)Z[(size_t)(j - 16) * ldz + k0 + 1 + i]; },
                                false, sm, [&](int c, int j, double v) {
                                    if (j < 16) Sg[c * 16 + j] = v;
                                    else Wm[(size_t)c * kv + (j - 16)] = v;
@@ -663,64 +726,19 @@ __device__ void tridiag_vectors(const SCFArgs &a, double *wsf, const double *A, 
     } else {
         // reflector by reflector, one warp per vector
         for (int t = w; t < kv; t += PDG_WARPS) {
-            double *zt = Z + (size_t)t * ldz;
+            R *zt = Z + (size_t)t * ldz;
             for (int k = N - 3; k >= 0; k--) {
                 const double tau = sm.tau[k];
                 if (tau == 0.0) continue;
                 const int m = N - k - 1;
                 double dt = 0.0;
-                for (int i = lane; i < m; i += 32) dt = fma(i == 0 ? 1.0 : A[plo(k + 1 + i, k)], zt[k + 1 + i], dt);
+                for (int i = lane; i < m; i += 32) dt = fma(i == 0 ? 1.0 : A[plo(k + 1 + i, k)], (double)zt[k + 1 + i], dt);
                 dt = warp_sum(dt) * tau;
-                for (int i = lane; i < m; i += 32) zt[k + 1 + i] = fma(-dt, i == 0 ? 1.0 : A[plo(k + 1 + i, k)], zt[k + 1 + i]);
+                for (int i = lane; i < m; i += 32) zt[k + 1 + i] = (R)fma(-dt, i == 0 ? 1.0 : A[plo(k + 1 + i, k)], (double)zt[k + 1 + i]);
                 __syncwarp();
             }
         }
         __syncthreads();
-    }
-}
-
-// Back-transformation of nv vectors of T in FP32 (rows of Zt, N floats each): the blocked compact-WY scheme of
-// tridiag_vectors with V^T V, T and both products in FP32.  For the complementary vectors of the perturbative base:
-// they enter the perturbative steps only in products with a small factor (dF, K), so their FP32 errors (~1e-7,
-// their orthogonality to the FP64 wanted vectors included) stay ~1e-7 of a small quantity, while the wanted vectors,
-// whose projector is the base density, keep the FP64 transformation.  work: 32 nv + 512 floats.  N >= 32.
-__device__ void back_transform32(int N, float *work, const double *A, Smem &sm, int nv, float *Zt)
-{
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int nref = N - 2;
-    float *Wm = work, *W2 = Wm + (size_t)16 * nv, *Sg = W2 + (size_t)16 * nv, *Tt = Sg + 256;
-    for (int k0 = ((nref - 1) / 16) * 16; k0 >= 0; k0 -= 16) {
-        const int nbk = min(16, nref - k0), m0 = N - k0 - 1;
-        auto V = [&](int i, int c) -> float { return i < c ? 0.f : (i == c ? 1.f : (float)A[plo(k0 + 1 + i, k0 + c)]); };
-        tgemm32<false, true>(nbk, 16 + nv, m0, [&](int c, int i) { return V(i, c); },
-                             [&](int i, int j) { return j < 16 ? (j < nbk ? V(i, j) : 0.f) : Zt[(size_t)(j - 16) * N + k0 + 1 + i]; },
-                             false, sm, [&](int c, int j, double v) {
-                                 if (j < 16) Sg[c * 16 + j] = (float)v;
-                                 else Wm[(size_t)c * nv + (j - 16)] = (float)v;
-                             });
-        if (w == 0) {   // T(c, c) = tau_c;  T(0:c, c) = -tau_c T(0:c, 0:c) S(0:c, c)
-            for (int c = 0; c < nbk; c++) {
-                const float tau = (float)sm.tau[k0 + c];
-                float t = 0.f;
-                if (lane < c) {
-                    for (int j = lane; j < c; j++) t = fmaf(Tt[lane * 16 + j], Sg[j * 16 + c], t);
-                    t *= -tau;
-                }
-                __syncwarp();
-                if (lane < 16) Tt[lane * 16 + c] = lane < c ? t : (lane == c ? tau : 0.f);
-                __syncwarp();
-            }
-        }
-        __syncthreads();
-        for (int e = tid; e < nbk * nv; e += PDG_BLOCK) {
-            const int c = e / nv, t = e % nv;
-            float acc = 0.f;
-            for (int j = c; j < nbk; j++) acc = fmaf(Tt[c * 16 + j], Wm[(size_t)j * nv + t], acc);
-            W2[(size_t)c * nv + t] = acc;
-        }
-        __syncthreads();
-        tgemm32<false, true>(nv, m0, nbk, [&](int t, int c) { return W2[(size_t)c * nv + t]; }, [&](int c, int i) { return V(i, c); },
-                             false, sm, [&](int t, int i, double v) { Zt[(size_t)t * N + k0 + 1 + i] -= (float)v; });
     }
 }
 
@@ -809,7 +827,7 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
     }
     __syncthreads();
     tm.lap(PDG_T_TRIDIAGONAL);
-    tridiag_vectors(a, wsf, A, sm, tm, s.vec_occupied ? 0 : N - kv, kv, Z, sm.zs != nullptr);
+    tridiag_vectors<double>(a, wsf, A, sm, tm, s.vec_occupied ? 0 : N - kv, kv, Z, ldz, sm.zs != nullptr);
     tm.lap(PDG_T_BACKTRANSFORM);
     // --- P = 2 Z^T Z (occupied) or 2 (1 - Z^T Z) (virtual); lower triangle then mirrored
     const bool occ = s.vec_occupied;
@@ -827,25 +845,24 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
     tm.lap(PDG_T_DENSITY);
     if (make_base) {
         // base of the following perturbative steps: this step's matrix, density, wanted vectors and, from a second
-        // pass over the same tridiagonal form, the complementary eigenvectors; all eigenvalues (wanted first)
+        // pass over the same tridiagonal form in FP32, the complementary eigenvectors; all eigenvalues (wanted first)
         const int nc = N - kv;
-        double *BF = wsf + pl.BF, *BP = wsf + pl.BP, *BZ = wsf + pl.BZ, *BV = wsf + pl.BV, *BL = wsf + pl.BL;
+        double *BF = wsf + pl.BF, *BP = wsf + pl.BP, *BZ = wsf + pl.BZ, *BL = wsf + pl.BL;
         for (size_t k = tid; k < (size_t)N * N; k += PDG_BLOCK) { BF[k] = F[k]; BP[k] = P[k]; }
         for (int e = tid; e < kv * N; e += PDG_BLOCK) BZ[(size_t)(e / N) * ldz + e % N] = Z[(size_t)(e / N) * ldz + e % N];
         for (int t = tid; t < kv; t += PDG_BLOCK) BL[t] = sm.eig[t];
         __syncthreads();
-        // (the complementary vectors are back-transformed in FP32 below, straight into their FP32 copy)
+        // The vectors in FP32 are the operands of the products with small factors: the wanted ones rounded, the
+        // complementary ones computed in FP32 (inverse iteration and back-transformation), since they enter the
+        // perturbative steps only in products with dF or K.
+        float *Zf = (float *)(wsf + pl.BW) + pert_dq_offset(N, kv) + 2 * (size_t)N * N, *Vf = Zf + (size_t)kv * N;
+        for (int e = tid; e < kv * N; e += PDG_BLOCK) Zf[e] = (float)BZ[(size_t)(e / N) * ldz + e % N];
+        __syncthreads();
         if (nc > 0) {
-            tridiag_vectors(a, wsf, A, sm, tm, s.vec_occupied ? kv : 0, nc, BV, false, false, N < 32);
+            tridiag_vectors<float>(a, wsf, A, sm, tm, s.vec_occupied ? kv : 0, nc, Vf, N, false, false);
             for (int t = tid; t < nc; t += PDG_BLOCK) BL[kv + t] = sm.eig[t];
         }
         __syncthreads();
-        // the vectors in FP32, the operands of the products with small factors
-        float *Zf = (float *)(wsf + pl.BW) + pert_dq_offset(N, kv) + 2 * (size_t)N * N, *Vf = Zf + (size_t)kv * N;
-        for (int e = tid; e < kv * N; e += PDG_BLOCK) Zf[e] = (float)BZ[(size_t)(e / N) * ldz + e % N];
-        for (int e = tid; e < nc * N; e += PDG_BLOCK) Vf[e] = (float)BV[(size_t)(e / N) * ldz + e % N];
-        __syncthreads();
-        if (N >= 32 && nc > 0) back_transform32(N, (float *)(wsf + pl.LU), A, sm, nc, Vf);
         float *Gi = Vf + (size_t)nc * N;   // reciprocal gaps, the fixed-point sweeps' divisors
         for (int e = tid; e < nc * kv; e += PDG_BLOCK) Gi[e] = (float)(1.0 / (BL[e % kv] - BL[kv + e / kv]));
         __syncthreads();
@@ -873,7 +890,7 @@ __device__ double density_step_pert(const SCFArgs &a, double *wsf, const double 
     const DeviceSystem &s = a.s;
     const FramePlan &pl = a.plan;
     const int N = s.n_basis, kv = s.n_vec, nc = N - kv, ldz = sm.ldz, tid = threadIdx.x;
-    const double *BF = wsf + pl.BF, *BP = wsf + pl.BP, *BZ = wsf + pl.BZ, *BV = wsf + pl.BV, *BL = wsf + pl.BL;
+    const double *BF = wsf + pl.BF, *BP = wsf + pl.BP, *BZ = wsf + pl.BZ, *BL = wsf + pl.BL;
     float *D = (float *)(wsf + pl.BW), *T1 = D + (size_t)N * N, *E = T1 + (size_t)N * kv, *Lp = E + (size_t)nc * kv;
     float *T2 = Lp + (size_t)kv * kv, *Mp = T2 + (size_t)N * nc, *K = Mp + (size_t)nc * nc, *K2 = K + (size_t)nc * kv;
     float *EK = K2 + (size_t)nc * kv, *U = EK + (size_t)kv * kv, *Y = U + (size_t)kv * kv, *Wz = Y + (size_t)kv * N;
