@@ -176,7 +176,7 @@ int pdg_gradients_static_scratch(pdg_system *sys, int n_frames, const double *d_
  * timings of pMolecule.QCModel.pyx:208-275 (EnergyWithTimings: QC Fock, QC Converger Iterate,
  * QC Converger Densities), with the density step split into its parts.  d_out: n_frames * PDG_NTIMERS. */
 #define PDG_RMS_HISTORY 40
-#define PDG_NTIMERS (31 + PDG_RMS_HISTORY)
+#define PDG_NTIMERS (37 + PDG_RMS_HISTORY)
 enum {
     PDG_T_FOCK = 0, PDG_T_DIIS_SAVE = 1, PDG_T_ITERATE = 2, PDG_T_TRIDIAGONAL = 3, PDG_T_EIGENVALUES = 4,
     PDG_T_EIGENVECTORS = 5, PDG_T_BACKTRANSFORM = 6, PDG_T_DENSITY = 7, PDG_T_TOTAL = 8, PDG_T_CYCLES = 9,
@@ -201,7 +201,14 @@ enum {
     PDG_T_PERT_COUPLING = 28,  /* the coupling blocks E, L', M' from dF, */
     PDG_T_PERT_SOLVE = 29,     /* the fixed-point sweeps, */
     PDG_T_PERT_DENSITY = 30,   /* the new density */
-    PDG_T_RMS_HISTORY = 31     /* PDG_RMS_HISTORY entries: RMS density change of each density step, in SCF cycle
+    PDG_T_DIIS_PACK = 31,      /* parts of PDG_T_DIIS_SAVE: P and F into the history, */
+    PDG_T_DIIS_COMMUTATOR = 32,/* the error vector F P - P F, */
+    PDG_T_DIIS_DOTS = 33,      /* its products with the stored error vectors (the B-matrix row); */
+    PDG_T_ITER_EXTRAPOLATE = 34, /* parts of PDG_T_ITERATE: the DIIS solve and extrapolation of P and F, */
+    PDG_T_ITER_RCA = 35,       /* the ODA (RCA) step and the copies of P and F it keeps */
+    PDG_T_DIIS_COMMUTATOR_FULL = 36, /* the part of PDG_T_DIIS_COMMUTATOR spent on full products F P (after a
+                                  purification step, or from a caller's start density) */
+    PDG_T_RMS_HISTORY = 37     /* PDG_RMS_HISTORY entries: RMS density change of each density step, in SCF cycle
                                   order, negative for purification steps, 0 beyond the last */
 };
 int pdg_scf_timings(const pdg_system *sys, int n_frames, const void *d_workspace, size_t workspace_bytes,

@@ -29,7 +29,9 @@ TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densi
           "QC Densities Purification Readout", "QC Densities Purification Control", "QC Densities Purification Setup",
           "QC Densities Purification Finish", "QC Densities Perturbative", "QC Densities Perturbative Steps",
           "QC Densities Perturbative Base", "QC Densities Perturbative Fallbacks", "QC Densities Perturbative Sweeps",
-          "QC Densities Perturbative Coupling", "QC Densities Perturbative Solve", "QC Densities Perturbative Density") + tuple("RMS %d" % k for k in range(40))
+          "QC Densities Perturbative Coupling", "QC Densities Perturbative Solve", "QC Densities Perturbative Density",
+          "QC Converger DIIS Pack", "QC Converger DIIS Commutator", "QC Converger DIIS Dots", "QC Converger Extrapolate",
+          "QC Converger RCA", "QC Converger DIIS Commutator Full") + tuple("RMS %d" % k for k in range(40))
 
 
 class SCFOptions(ctypes.Structure):

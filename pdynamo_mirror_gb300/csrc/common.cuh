@@ -72,6 +72,9 @@ __host__ __device__ inline size_t pert_dq_offset(int N, int kv)
     return n * n + n * k + c * k + k * k + n * c + c * c + 2 * c * k + 2 * k * k + 2 * k * n;
 }
 
+// Offset (floats) of Y (then W) in that work.
+__host__ __device__ inline size_t pert_y_offset(int N, int kv) { return pert_dq_offset(N, kv) - 2 * (size_t)kv * N; }
+
 __host__ inline FramePlan make_plan(const DeviceSystem &s, int history)
 {
     FramePlan p;

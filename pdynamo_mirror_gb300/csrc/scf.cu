@@ -894,7 +894,7 @@ __device__ double density_step_pert(const SCFArgs &a, double *wsf, const double 
     float *D = (float *)(wsf + pl.BW), *T1 = D + (size_t)N * N, *E = T1 + (size_t)N * kv, *Lp = E + (size_t)nc * kv;
     float *T2 = Lp + (size_t)kv * kv, *Mp = T2 + (size_t)N * nc, *K = Mp + (size_t)nc * nc, *K2 = K + (size_t)nc * kv;
     float *EK = K2 + (size_t)nc * kv, *U = EK + (size_t)kv * kv, *Y = U + (size_t)kv * kv, *Wz = Y + (size_t)kv * N;
-    float *DQ = Wz + (size_t)kv * N;
+    float *DQ = Wz + (size_t)kv * N;   // Y, W (and dQ) stay for the DIIS save's commutator: pert_y_offset, pert_dq_offset
     if (nc <= 0) return -1.0;
     const long long t_coupling = tm.now();
     for (size_t k = tid; k < (size_t)N * N; k += PDG_BLOCK) D[k] = (float)(F[k] - BF[k]);
@@ -1354,14 +1354,19 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
             // FP32 products: the error vectors only steer the extrapolation
             float *hef = (float *)he;
             auto put_error = [&](int idx, double ev) { if (delta_commutator) hef[idx] = (float)ev; else he[idx] = ev; };
+            long long t_sub = tm.now();
             for (int i = tid / 32; i < N; i += PDG_WARPS)
                 for (int j = tid % 32; j <= i; j += 32) { hp[i * (i + 1) / 2 + j] = P[(size_t)i * N + j]; hf[i * (i + 1) / 2 + j] = F[(size_t)i * N + j]; }
+            __syncthreads();
+            tm.add(PDG_T_DIIS_PACK, t_sub);
+            t_sub = tm.now();
             double emx = 0.0;
             if (have_z || have_pert) {
                 // P = 2 Z^T Z (occupied) or 2 (1 - Z^T Z) (virtual) with the vectors Z of the last density step,
                 // so with G = Z F:  F P - P F = sg (G^T Z - Z^T G), sg = +2 / -2.  2 N^2 kv FMA instead of N^3.
-                // After a perturbative step P = P0 + c dQ with P0 the base's projector (Z = the base vectors):
-                // F P - P F = [dF, P0] + c [dF, dQ], dF = F - F~, the second term from one more FP32 product.
+                // After a perturbative step the new projector is Q = S^T (1 + U) S with S = Z0 + Y (the step's K^T V
+                // and U = (1 + K^T K)^-1 - 1), and (1 + U) S = Z0 + W, so with G = S dF and T = Z0 + W:
+                // F P - P F = sg (G^T T - T^T G), dF = F - F~: the same two products as after an FP64 step.
                 const double *Zc = have_pert ? wsf + pl.BZ : (sm.zs ? sm.zs : wsf + pl.Z);
                 const int ldz = sm.ldz, kv = s.n_vec;
                 const double sg = s.vec_occupied ? 2.0 : -2.0;
@@ -1380,29 +1385,16 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
                     const float *Z32 = DF + (size_t)N * N;
                     for (size_t k = tid; k < NN; k += PDG_BLOCK) DF[k] = (float)(F[k] - Ft[k]);
                     __syncthreads();
-                    tgemm32<true, false>(kv, N, N, [&](int t, int k) { return Z32[(size_t)t * N + k]; },
-                                       [&](int k, int i) { return DF[(size_t)k * N + i]; },
+                    // S = Z0 (+ Y after a perturbative step), T = Z0 (+ W); both kv x N in FP32
+                    const float *Yp = (const float *)(wsf + pl.BW) + pert_y_offset(N, kv), *Wp = Yp + (size_t)kv * N;
+                    auto Sv = [&](int t, int k) { return have_pert ? Z32[(size_t)t * N + k] + Yp[(size_t)t * N + k] : Z32[(size_t)t * N + k]; };
+                    auto Tv = [&](int t, int k) { return have_pert ? Z32[(size_t)t * N + k] + Wp[(size_t)t * N + k] : Z32[(size_t)t * N + k]; };
+                    tgemm32<true, false>(kv, N, N, Sv, [&](int k, int i) { return DF[(size_t)k * N + i]; },
                                        false, sm, [&](int t, int i, double v) { G32[(size_t)t * N + i] = (float)v; });
-                    if (have_pert) {
-                        // X = dF dQ (FP32, N x N, into the perturbative work's dF slot), then the commutator adds
-                        // c (X - X^T) to the base part
-                        float *DQ = (float *)(wsf + pl.BW) + pert_dq_offset(N, kv), *X = (float *)(wsf + pl.BW);
-                        tgemm32<true, false>(N, N, N, [&](int i, int k) { return DF[(size_t)i * N + k]; },
-                                           [&](int k, int j) { return DQ[(size_t)k * N + j]; }, false, sm,
-                                           [&](int i, int j, double v) { X[(size_t)i * N + j] = (float)v; });
-                        const double cq = s.vec_occupied ? 2.0 : -2.0;
-                        tgemm32<false, false>(N, N, 2 * kv,
-                            [&](int i, int k) { return k < kv ? G32[(size_t)k * N + i] : Z32[(size_t)(k - kv) * N + i]; },
-                            [&](int k, int j) { return k < kv ? Z32[(size_t)k * N + j] : -G32[(size_t)(k - kv) * N + j]; },
-                            true, sm, [&](int i, int j, double v) {
-                                if (j >= i) return;
-                                store(i, j, v + cq * ((double)X[(size_t)i * N + j] - (double)X[(size_t)j * N + i]) / sg);
-                            });
-                    } else
-                        tgemm32<false, false>(N, N, 2 * kv,
-                            [&](int i, int k) { return k < kv ? G32[(size_t)k * N + i] : Z32[(size_t)(k - kv) * N + i]; },
-                            [&](int k, int j) { return k < kv ? Z32[(size_t)k * N + j] : -G32[(size_t)(k - kv) * N + j]; },
-                            true, sm, store);
+                    tgemm32<false, false>(N, N, 2 * kv,
+                        [&](int i, int k) { return k < kv ? G32[(size_t)k * N + i] : Tv(k - kv, i); },
+                        [&](int k, int j) { return k < kv ? Tv(k, j) : -G32[(size_t)(k - kv) * N + j]; },
+                        true, sm, store);
                 } else {
                     double *G = wsf + pl.G;
                     tgemm<true, false>(kv, N, N, [&](int t, int k) { return Zc[(size_t)t * ldz + k]; }, [&](int k, int i) { return F[(size_t)k * N + i]; },
@@ -1416,6 +1408,7 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
                 // full commutator: FP64, or FP32 after a purification step (whose density carries BF16-level
                 // errors anyway)
                 double *FP = wsf + pl.A;
+                const long long t_pur = tm.now();
                 if (last_mixed) {
                     // FP32 outer products over k: thread block (i0..i0+3, j0..j0+3) += F[k][i0..] (x) P[k][j0..]
                     // (F symmetric), operands read as float4 rows with no shared-memory staging or barriers
@@ -1456,8 +1449,11 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
                         emx = fmax(emx, fabs(ev));
                     }
                 __syncthreads();
+                tm.add(PDG_T_DIIS_COMMUTATOR_FULL, t_pur);
             }
             double maxerr = block_max(emx, sm.red);
+            tm.add(PDG_T_DIIS_COMMUTATOR, t_sub);
+            t_sub = tm.now();
             double dots[PDG_MAX_HISTORY];
             for (int m = 0; m < PDG_MAX_HISTORY; m++) dots[m] = 0.0;
             const int ne = N * (N - 1) / 2;
@@ -1491,7 +1487,9 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
                 }
             }
             __syncthreads();
+            tm.add(PDG_T_DIIS_DOTS, t_sub);
             tm.lap(PDG_T_DIIS_SAVE);
+            t_sub = tm.now();
             if (iteration > 0) {
                 if (o.use_rca) {
                     if (qdiis && maxerr > 0.8) { qdiis = 0; qrca = 1; }
@@ -1542,6 +1540,8 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
                         }
                         __syncthreads();
                     }
+                    tm.add(PDG_T_ITER_EXTRAPOLATE, t_sub);
+                    t_sub = tm.now();
                 } else if (o.use_rca && qrca) {
                     // RCA_Iterate: cubic in mu from four traces (DIISSCFConverger.c:661-760)
                     const double *rP = wsf + pl.rP, *rF = wsf + pl.rF;
@@ -1574,7 +1574,9 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
             if (o.use_rca) {
                 double *rP = wsf + pl.rP, *rF = wsf + pl.rF;
                 for (size_t k = tid; k < NN; k += PDG_BLOCK) { rP[k] = P[k]; rF[k] = F[k]; }
+                __syncthreads();
             }
+            tm.add(PDG_T_ITER_RCA, t_sub);
             iteration++;
         }
         deltaeold = deltae; eold = etemp;
