@@ -117,12 +117,12 @@ def fp32_peak_tflops(dev, n=4096, reps=3):
 
 def scf_work(T, N, kv, frames, mixed):
     """Algorithmic work of one k_scf launch (all frames) by unit, from the per-frame phase counts:
-    FP64 density steps (4/3) N^3 + 3 N^2 kv flops each, plus, when the step keeps a perturbative base, the
-    back-transformation of the nc = N - kv complementary vectors (2 N^2 nc); the plain method's DIIS saves after
-    FP64 steps 4 N^2 kv, its other saves 2 N^3.  Mixed method: FP32 flops of the perturbative steps (the coupling
-    blocks, the fixed-point sweeps, the new density), of its FP32 commutators (after FP64 and perturbative steps
-    the Z-form 4 N^2 kv plus 2 N^3 for dF dQ after a perturbative step; after purification steps 2 N^3), and the
-    split-BF16 SP2 products on the tensor cores (6 x 2 N^3 per SP2 iteration).  Returns flops (fp64, fp32, tensor)."""
+    FP64 density steps (4/3) N^3 + 3 N^2 kv flops each; the plain method's DIIS saves after FP64 steps 4 N^2 kv,
+    its other saves 2 N^3.  Mixed method: FP32 flops of the perturbative base (the back-transformation of the
+    nc = N - kv complementary vectors, 2 N^2 nc per FP64 step), of the perturbative steps (the coupling blocks, the
+    fixed-point sweeps, the new density), of its FP32 commutators (after FP64 and perturbative steps the factored
+    form 4 N^2 kv; after purification steps 2 N^3), and the split-BF16 SP2 products on the tensor cores (6 x 2 N^3
+    per SP2 iteration).  Returns flops (fp64, fp32, tensor)."""
     nc = N - kv
     fs = T["QC Densities Steps"].mean()
     cyc = T["QC SCF Fock Builds"].mean()
@@ -132,11 +132,12 @@ def scf_work(T, N, kv, frames, mixed):
         return frames * f64, 0.0, 0.0
     ps, sw = T["QC Densities Perturbative Steps"].mean(), T["QC Densities Perturbative Sweeps"].mean()
     pur, sp2 = T["QC Densities Purification Steps"].mean(), T["QC Densities SP2 Iterations"].mean()
-    f64 = fs * ((4.0 / 3.0) * N ** 3 + 3.0 * N * N * kv + 2.0 * N * N * nc)
+    f64 = fs * ((4.0 / 3.0) * N ** 3 + 3.0 * N * N * kv)
     pert_fma = (N * N * kv + nc * N * kv + kv * N * kv + N * N * nc + nc * N * nc + kv * nc * N + kv * nc * kv + kv ** 3
                 + 2 * kv * kv * N + N * N * kv)
     sweep_fma = kv * nc * kv + nc * (nc + kv) * kv
-    f32 = ps * 2.0 * pert_fma + sw * 2.0 * sweep_fma + (fs + ps) * 4.0 * N * N * kv + ps * 2.0 * N ** 3 + pur * 2.0 * N ** 3
+    f32 = (ps * 2.0 * pert_fma + sw * 2.0 * sweep_fma + (fs + ps) * 4.0 * N * N * kv + fs * 2.0 * N * N * nc
+           + pur * 2.0 * N ** 3)
     tc = sp2 * 6 * 2.0 * N ** 3
     return frames * f64, frames * f32, frames * tc
 
