@@ -348,6 +348,32 @@ int pdg_normal_deviates(long long n_pairs, unsigned long long seed, unsigned int
 int pdg_density_combine(long long n, int count, const double *const *h_terms, const double *h_coefficients, double *d_out,
                         void *stream);
 
+/* ---- MM/MM and QC/MM Lennard-Jones energies of NBModelABFS ----
+ * Replace NBModelABFS_MMMMEnergy and NBModelABFS_QCMMEnergyLJ (pMolecule-1.9.0/extensions/csource/NBModelABFS.c:228,
+ * :306) with PairwiseInteractionABFS_MMMMEnergy in its default analytic form (PairwiseInteraction.c:292) over the
+ * pair lists of GenerateLists / GenerateLists14 (NBModelABFS.c:1050-1160), which the reference's cell-grid
+ * generator makes (pCore-1.9.0/extensions/csource/PairListGenerator.c:414-530); here a cell grid is rebuilt on the
+ * device for every call.  No symmetry images.
+ *   pdg_mm_create  the MM side of a system (host arrays, copied): per atom the charge (e), LJ type and flags
+ *                  (1 an active MM atom, 2 a QC atom with LJ interactions, 4 fixed: pairs of two fixed atoms are
+ *                  left out, as the reference's free-atom selection does); LJ tables A and B (n_lj_types^2, full,
+ *                  symmetric; kJ/mol A^12 and kJ/mol A^6: E = A / r^12 - B / r^6) and the 1-4 tables; exclusion
+ *                  pairs and 1-4 pairs (i, j); the ABFS cutoffs (A), the dielectric and electrostaticScale14.
+ *   pdg_mm_energy_gradients  for n_frames frames of d_xyz (n_frames x n_atoms x 3, A): d_energies n_frames x 6 in
+ *                  kJ/mol (MM/MM Elect., MM/MM LJ, MM/MM 1-4 Elect., MM/MM 1-4 LJ, QC/MM LJ, QC/MM 1-4 LJ, the
+ *                  labels of NBModelABFSState.GetEnergies, pMolecule.NBModelABFSState.pyx:41-52) and, unless NULL,
+ *                  d_gradients n_frames x n_atoms x 3 in kJ/mol/A (overwritten; zero on atoms without terms). */
+typedef struct pdg_mm_system pdg_mm_system;
+int pdg_mm_create(int n_atoms, const double *h_charges, const int *h_lj_types, const unsigned char *h_flags, int n_lj_types,
+                  const double *h_table_a, const double *h_table_b, const double *h_table_a14, const double *h_table_b14,
+                  int n_exclusions, const int *h_exclusions, int n_pairs14, const int *h_pairs14, double inner_cutoff,
+                  double outer_cutoff, double damping_cutoff, double dielectric, double electrostatic_scale14,
+                  pdg_mm_system **out);
+int pdg_mm_destroy(pdg_mm_system *m);
+size_t pdg_mm_workspace_bytes(const pdg_mm_system *m, int n_frames);
+int pdg_mm_energy_gradients(const pdg_mm_system *m, int n_frames, const double *d_xyz, double *d_energies, double *d_gradients,
+                            void *d_workspace, size_t workspace_bytes, void *stream);
+
 /* Text of the last error on this host thread (never NULL). */
 const char *pdg_last_error(void);
 

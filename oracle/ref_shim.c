@@ -16,6 +16,9 @@
  *   SCF loop                           pMolecule.QCModel.pyx:146-185, pMolecule.DIISSCFConverger.pyx:93-125
  *   energies                           pMolecule.QCModelMNDOState.pyx:168-185
  *   QC/MM electrostatics               pMolecule.NBModelABFS.pyx:124-138 over PairwiseInteraction.c:542,612
+ *   MM/MM and QC/MM LJ energies        pMolecule.NBModelABFS.pyx:59-82,108-122 (generator and pairwise-interaction
+ *                                      defaults, Energy), NBModelABFS.c:228-330 (MMMMEnergy, QCMMEnergyLJ) and
+ *                                      :1050-1140 (GenerateLists, GenerateLists14), NBModelABFSState.c:207-226 (grids)
  */
 # include <math.h>
 # include <stdlib.h>
@@ -24,6 +27,12 @@
 # include "BlockStorage.h"
 # include "Coordinates3.h"
 # include "CubicSpline.h"
+# include "LJParameterContainer.h"
+# include "MMAtomContainer.h"
+# include "PairListGenerator.h"
+# include "RegularGrid.h"
+# include "RegularGridOccupancy.h"
+# include "Selection.h"
 # include "DIISSCFConverger.h"
 # include "DIISSCFConvergerState.h"
 # include "GaussianBasis.h"
@@ -510,5 +519,99 @@ int ref_abfs_qcmm ( void *vp, void *vs, const double *qcxyz, const int nMM, cons
     Coordinates3_Deallocate ( &crd1 ) ; Coordinates3_Deallocate ( &crd2 ) ;
     Coordinates3_Deallocate ( &grd1 ) ; Coordinates3_Deallocate ( &grd2 ) ;
     Real1DArray_Deallocate ( &q ) ; Real1DArray_Deallocate ( &phi ) ; Real1DArray_Deallocate ( &qc ) ;
+    return 0 ;
+}
+
+/*----------------------------------------------------------------------------------------------------------------------------------
+! . MM/MM electrostatic and LJ energies and QC/MM LJ energies of NBModelABFS (no symmetry), through the reference's
+! . pair-list generator and PairwiseInteractionABFS_MMMMEnergy (PairwiseInteraction.c:292), analytic form.
+! . flags per atom: bit 0 active MM atom (mmSelection), bit 1 QC atom with LJ interactions (qcpSelection),
+! . bit 2 fixed.  Exclusions and 1-4 interactions as (i, j) pairs.  LJ types with epsilon (kJ/mol) and sigma (A)
+! . turned into tables by the OPLS (opls != 0) or AMBER rule; 1-4 LJ from their own epsilon and sigma.
+! . energies (kJ/mol): MM/MM Elect., MM/MM LJ, MM/MM 1-4 Elect., MM/MM 1-4 LJ, QC/MM LJ, QC/MM 1-4 LJ.
+! . gradients (kJ/mol/A, nAtoms x 3) are overwritten.
+!---------------------------------------------------------------------------------------------------------------------------------*/
+static Selection *SelectFlag ( const int n, const int *flags, const int bit, const int want )
+{
+    Integer *ix = ( Integer * ) malloc ( sizeof ( Integer ) * ( size_t ) ( n > 0 ? n : 1 ) ) ;
+    int i, k = 0 ;
+    Selection *sel ;
+    for ( i = 0 ; i < n ; i++ ) if ( ( ( flags[i] >> bit ) & 1 ) == want ) ix[k++] = i ;
+    sel = Selection_FromIntegerArray ( k, ix ) ;
+    free ( ix ) ;
+    return sel ;
+}
+
+static LJParameterContainer *MakeLJ ( const int nTypes, const double *epsilon, const double *sigma, const int opls )
+{
+    LJParameterContainer *lj = LJParameterContainer_Allocate ( nTypes ) ;
+    int t ;
+    for ( t = 0 ; t < nTypes ; t++ ) { lj->epsilon[t] = epsilon[t] ; lj->sigma[t] = sigma[t] ; }
+    if ( opls ) LJParameterContainer_MakeTableOPLS ( lj ) ;
+    else        LJParameterContainer_MakeTableAMBER ( lj ) ;
+    return lj ;
+}
+
+int ref_mmmm_energy ( const int nAtoms, const double *xyz, const double *charges, const int *ljTypes, const int *flags,
+                      const int nTypes, const double *epsilon, const double *sigma, const double *epsilon14, const double *sigma14,
+                      const int opls, const int nExclusions, const int *exclusions, const int n14, const int *pairs14,
+                      const double innerCutoff, const double outerCutoff, const double dampingCutoff, const double listCutoff,
+                      const double dielectric, const double scale14, double *energies, double *gradients )
+{
+    Coordinates3 *crd = Coordinates3_Allocate ( nAtoms ), *grd = Coordinates3_Allocate ( nAtoms ) ;
+    MMAtomContainer *mm = MMAtomContainer_Allocate ( nAtoms ) ;
+    LJParameterContainer *lj = MakeLJ ( nTypes, epsilon, sigma, opls ), *lj14 = MakeLJ ( nTypes, epsilon14, sigma14, opls ) ;
+    PairwiseInteractionABFS *p = PairwiseInteractionABFS_Allocate ( ) ;
+    PairListGenerator *g = PairListGenerator_Allocate ( ) ;
+    Selection *mmSel = SelectFlag ( nAtoms, flags, 0, 1 ), *qcpSel = SelectFlag ( nAtoms, flags, 1, 1 ), *freeSel = NULL ;
+    PairList *excl = NULL, *i14 = NULL, *nbmmmm = NULL, *nbqcmmlj = NULL, *nbmmmm14 = NULL, *nbqcmmlj14 = NULL ;
+    RegularGrid *grid = NULL ;
+    RegularGridOccupancy *occupancy = NULL ;
+    Real eScale = 1.0 / dielectric ;
+    int i, nFixed = 0 ;
+    for ( i = 0 ; i < 6 ; i++ ) energies[i] = 0.0 ;
+    for ( i = 0 ; i < nAtoms ; i++ )
+    {
+        Coordinates3_SetRow ( crd, i, xyz[3*i], xyz[3*i+1], xyz[3*i+2] ) ;
+        mm->data[i].QACTIVE  = ( flags[i] & 1 ) ? True : False ;
+        mm->data[i].atomtype = 0 ;
+        mm->data[i].ljtype   = ljTypes[i] ;
+        mm->data[i].charge   = charges[i] ;
+        if ( ( flags[i] >> 2 ) & 1 ) nFixed++ ;
+    }
+    Coordinates3_Set ( grd, 0.0 ) ;
+    /* . pMolecule.NBModelABFS.pyx:79-82: the MM/MM interaction takes the model's cutoffs (analytic form). */
+    p->innerCutoff = innerCutoff ; p->outerCutoff = outerCutoff ; p->dampingCutoff = dampingCutoff ; p->useAnalyticForm = True ;
+    /* . pMolecule.NBModelABFS.pyx:62-69 and pCore.PairListGenerator.pyx:104. */
+    g->cutoff = listCutoff ; g->cutoffCellSizeFactor = 0.5 ; g->minimumCellExtent = 2 ; g->minimumCellSize = 3.0 ;
+    g->minimumExtentFactor = 1.5 ; g->minimumPoints = 500 ; g->sortIndices = False ; g->useGridByCell = True ;
+    g->cellSize = g->cutoffCellSizeFactor * g->cutoff ;
+    if ( nFixed > 0 ) freeSel = SelectFlag ( nAtoms, flags, 2, 0 ) ;
+    excl = PairList_FromIntegerPairArray ( True, nExclusions, ( Integer * ) exclusions ) ;
+    if ( n14 > 0 ) i14 = PairList_FromIntegerPairArray ( True, n14, ( Integer * ) pairs14 ) ;
+    /* . NBModelABFSState.c:207-226: a grid when the generator chooses a grid search. */
+    if ( PairListGenerator_DetermineMethod ( g, crd, NULL ) ) Coordinates3_MakeGridAndOccupancy ( crd, NULL, g->cellSize, &grid, &occupancy, NULL ) ;
+    /* . NBModelABFS.c:1050-1100 (GenerateLists). */
+    nbmmmm   = PairListGenerator_SelfPairListFromCoordinates3 ( g, crd, NULL, mmSel, freeSel, excl, grid, occupancy, NULL ) ;
+    nbqcmmlj = PairListGenerator_CrossPairListFromSingleCoordinates3 ( g, crd, NULL, qcpSel, mmSel, freeSel, excl, False, grid, occupancy, NULL ) ;
+    /* . GenerateLists14. */
+    if ( i14 != NULL )
+    {
+        nbmmmm14   = SelfPairList_FromSelfPairList ( i14, mmSel, freeSel, False ) ;
+        nbqcmmlj14 = SelfPairList_ToCrossPairList  ( i14, qcpSel, mmSel, freeSel, False, False, False, False ) ;
+    }
+    /* . NBModelABFS.c:228-330 (MMMMEnergy, QCMMEnergyLJ; their 1-4 and QC/MM LJ lists). */
+    if ( nbmmmm     != NULL ) PairwiseInteractionABFS_MMMMEnergy ( p, mm, lj,   nbmmmm,     eScale,           1.0, crd, crd, &energies[0], &energies[1], grd, grd ) ;
+    if ( nbmmmm14   != NULL ) PairwiseInteractionABFS_MMMMEnergy ( p, mm, lj14, nbmmmm14,   eScale * scale14, 1.0, crd, crd, &energies[2], &energies[3], grd, grd ) ;
+    if ( nbqcmmlj   != NULL ) PairwiseInteractionABFS_MMMMEnergy ( p, mm, lj,   nbqcmmlj,   0.0,              1.0, crd, crd, NULL,         &energies[4], grd, grd ) ;
+    if ( nbqcmmlj14 != NULL ) PairwiseInteractionABFS_MMMMEnergy ( p, mm, lj14, nbqcmmlj14, 0.0,              1.0, crd, crd, NULL,         &energies[5], grd, grd ) ;
+    for ( i = 0 ; i < nAtoms ; i++ ) Coordinates3_GetRow ( grd, i, gradients[3*i], gradients[3*i+1], gradients[3*i+2] ) ;
+    PairList_Deallocate ( &nbmmmm ) ; PairList_Deallocate ( &nbqcmmlj ) ; PairList_Deallocate ( &nbmmmm14 ) ; PairList_Deallocate ( &nbqcmmlj14 ) ;
+    PairList_Deallocate ( &excl ) ; PairList_Deallocate ( &i14 ) ;
+    RegularGrid_Deallocate ( &grid ) ; RegularGridOccupancy_Deallocate ( &occupancy ) ;
+    Selection_Deallocate ( &mmSel ) ; Selection_Deallocate ( &qcpSel ) ; Selection_Deallocate ( &freeSel ) ;
+    PairListGenerator_Deallocate ( &g ) ; PairwiseInteractionABFS_Deallocate ( &p ) ;
+    LJParameterContainer_Deallocate ( &lj ) ; LJParameterContainer_Deallocate ( &lj14 ) ; MMAtomContainer_Deallocate ( &mm ) ;
+    Coordinates3_Deallocate ( &crd ) ; Coordinates3_Deallocate ( &grd ) ;
     return 0 ;
 }

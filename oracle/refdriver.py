@@ -49,6 +49,7 @@ def lib():
         L.ref_abfs_create.argtypes = [D, D, I, pd, pd]
         L.ref_abfs_spline.argtypes = [P, I, pd, pd, pd]
         L.ref_abfs_qcmm.argtypes = [P, P, pd, I, pd, pd, pd, pd, pd, pd]
+        L.ref_mmmm_energy.argtypes = [I, pd, pd, pi, pi, I, pd, pd, pd, pd, I, I, pi, I, pi, D, D, D, D, D, D, pd, pd]
         _lib = L
     return _lib
 
@@ -158,3 +159,26 @@ class RefABFS:
                             np.ascontiguousarray(mmxyz, dtype=np.float64).ravel(), np.ascontiguousarray(mmq, dtype=np.float64),
                             np.ascontiguousarray(qcq, dtype=np.float64), phi, gq, gm)
         return phi, gq.reshape(n, 3), gm.reshape(m, 3)
+
+
+def mmmm_energy(xyz, charges, lj_types, flags, epsilon, sigma, epsilon14, sigma14, opls, exclusions, pairs14,
+                inner=8.0, outer=12.0, damp=0.5, listCutoff=13.5, dielectric=1.0, scale14=1.0):
+    """NBModelABFS MM/MM and QC/MM LJ energies (kJ/mol, the order of oracle.mmmm.TERMS) and gradients (kJ/mol/A)
+    from the reference's pair-list generator and pair routine (ref_mmmm_energy in ref_shim.c)."""
+    X = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = len(X)
+    i32 = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.int32).ravel())
+    f64 = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.float64).ravel())
+    ex, p14 = i32(np.asarray(exclusions).reshape(-1, 2)), i32(np.asarray(pairs14).reshape(-1, 2))
+    if len(ex) == 0:
+        ex = np.zeros(2, np.int32)
+    n_ex = len(np.asarray(exclusions).reshape(-1, 2))
+    n14 = len(np.asarray(pairs14).reshape(-1, 2))
+    if len(p14) == 0:
+        p14 = np.zeros(2, np.int32)
+    E = np.zeros(6)
+    G = np.zeros(3 * n)
+    lib().ref_mmmm_energy(n, X.ravel(), f64(charges), i32(lj_types), i32(flags), len(epsilon), f64(epsilon), f64(sigma),
+                          f64(epsilon14), f64(sigma14), 1 if opls else 0, n_ex, ex, n14, p14, inner, outer, damp, listCutoff,
+                          dielectric, scale14, E, G)
+    return E, G.reshape(n, 3)

@@ -11,9 +11,10 @@ from .batch import MoleculeBatch
 from .converger import DIISSCFConverger
 from .dynamics import LangevinDynamics, LangevinDynamics_SystemGeometry, LangevinVelocityVerletIntegrator
 from .guess import LearnedDensityGuess
+from .mmmodel import LJParameterContainer, MMModel
 from .nbmodel import NBModelABFS, NBModelFull
 from .qcmodel import QCModelMNDO
 from .system import ElectronicState, SCFNotConverged, System
 from .trajectory import DCDTrajectoryFileReader, DCDTrajectoryFileWriter
 
-__all__ = ["DCDTrajectoryFileReader", "DCDTrajectoryFileWriter", "DIISSCFConverger", "LangevinDynamics", "LangevinDynamics_SystemGeometry", "LangevinVelocityVerletIntegrator", "MoleculeBatch", "ElectronicState", "LearnedDensityGuess", "NBModelABFS", "NBModelFull", "QCModelMNDO", "SCFNotConverged", "System"]
+__all__ = ["DCDTrajectoryFileReader", "DCDTrajectoryFileWriter", "DIISSCFConverger", "LangevinDynamics", "LangevinDynamics_SystemGeometry", "LangevinVelocityVerletIntegrator", "LJParameterContainer", "MMModel", "MoleculeBatch", "ElectronicState", "LearnedDensityGuess", "NBModelABFS", "NBModelFull", "QCModelMNDO", "SCFNotConverged", "System"]

@@ -14,6 +14,8 @@ NENERGY = 8
 EN_TOTAL_ELECTRONIC, EN_ELECTRONIC, EN_NUCLEAR, EN_BASELINE, EN_QCMM, EN_ONE_ELECTRON, EN_TWO_ELECTRON, EN_RMS_DENSITY = range(8)
 MAX_HISTORY = 16
 QCMM_FP32_PAIRS = 0x100   # pdg_qcmm_gradients model flag: FP32 pair terms (the mixed method)
+MM_FLAG_MM, MM_FLAG_QC_LJ, MM_FLAG_FIXED = 1, 2, 4   # pdg_mm_create atom flags
+MM_TERMS = ("MM/MM Elect.", "MM/MM LJ", "MM/MM 1-4 Elect.", "MM/MM 1-4 LJ", "QC/MM LJ", "QC/MM 1-4 LJ")
 
 EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system_info", "pdg_workspace_bytes",
            "pdg_energy_gradients", "pdg_scf", "pdg_density", "pdg_one_electron", "pdg_fock", "pdg_gradients", "pdg_qcmm_potentials",
@@ -21,7 +23,8 @@ EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system
            "pdg_mlp_backward", "pdg_mlp_adam", "pdg_guess_assemble", "pdg_guess_loss", "pdg_batch_create", "pdg_batch_destroy",
            "pdg_batch_info", "pdg_batch_workspace_bytes", "pdg_batch_schedule", "pdg_batch_energy_gradients", "pdg_batch_timings",
            "pdg_batch_graph_create", "pdg_graph_launch", "pdg_graph_destroy", "pdg_langevin_positions", "pdg_langevin_velocities",
-           "pdg_normal_deviates", "pdg_density_combine", "pdg_last_error")
+           "pdg_normal_deviates", "pdg_density_combine", "pdg_mm_create", "pdg_mm_destroy", "pdg_mm_workspace_bytes",
+           "pdg_mm_energy_gradients", "pdg_last_error")
 TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densities Tridiagonal", "QC Densities Eigenvalues",
           "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds",
           "QC Densities Cluster Rounds", "QC Densities Steps", "QC Densities Purification",
@@ -102,6 +105,11 @@ def load(path=LIB_PATH):
     L.pdg_langevin_velocities.argtypes = [I, I, I, P, P, P, P, D, D, P, P, P, P]
     L.pdg_normal_deviates.argtypes = [LL, U64, U32, U32, P, P]
     L.pdg_density_combine.argtypes = [LL, I, P, P, P, P]
+    L.pdg_mm_create.argtypes = [I, P, P, P, I, P, P, P, P, I, P, I, P, D, D, D, D, D, PP]
+    L.pdg_mm_destroy.argtypes = [P]
+    L.pdg_mm_workspace_bytes.argtypes = [P, I]
+    L.pdg_mm_workspace_bytes.restype = S
+    L.pdg_mm_energy_gradients.argtypes = [P, I, P, P, P, P, S, P]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype or I
     _lib = L

@@ -732,3 +732,152 @@ extern "C" int pdg_density_combine(long long n, int count, const double *const *
     launch_density_combine(n, t, d_out, (cudaStream_t)stream);
     return cuda_check(cudaGetLastError(), "density combination kernel");
 }
+
+// ---- MM/MM and QC/MM Lennard-Jones energies ----
+struct pdg_mm_system {
+    MMDevice d;
+    double *d_real = nullptr;   // charges, then the four LJ tables
+    int *d_int = nullptr;       // LJ types, exclusion offsets and partners, 1-4 offsets and partners
+    unsigned char *d_flags = nullptr;
+};
+
+// PairwiseInteractionABFS_MakeFactors (PairwiseInteraction.c:89-140) for the MM/MM interaction.
+static MMFactors mm_factors(double inner, double outer, double damp)
+{
+    MMFactors f;
+    f.r2Damp = damp * damp; f.r2Off = outer * outer; f.r2On = inner * inner;
+    const double gamma = std::pow(f.r2Off - f.r2On, 3);
+    f.a = f.r2Off * f.r2Off * (f.r2Off - 3.0 * f.r2On) / gamma;
+    f.b = 6.0 * f.r2Off * f.r2On / gamma;
+    f.c = -(f.r2Off + f.r2On) / gamma;
+    f.d = 0.4 / gamma;
+    f.qShift1 = 8.0 * (f.r2Off * f.r2On * (outer - inner) - 0.2 * (outer * f.r2Off * f.r2Off - inner * f.r2On * f.r2On)) / gamma;
+    f.qShift2 = -(f.a / outer) + f.b * outer + f.c * outer * f.r2Off + f.d * outer * f.r2Off * f.r2Off;
+    f.qF0 = f.qAlpha = f.aF0 = f.aAlpha = f.bF0 = f.bAlpha = 0.0;
+    if (damp > 0.0) {
+        const double g = -1.0 / f.r2Damp, fq = 1.0 / damp + f.qShift1;
+        f.qF0 = fq - 0.5 * damp * g; f.qAlpha = -0.5 * g / damp;
+    }
+    f.aF6 = 1.0 / (f.r2Off * f.r2Off * f.r2Off);
+    f.aK12 = std::pow(f.r2Off, 3) / (std::pow(f.r2Off, 3) - std::pow(f.r2On, 3));
+    f.aShift12 = 1.0 / std::pow(inner * outer, 6);
+    f.bF3 = 1.0 / (outer * f.r2Off);
+    f.bK6 = (outer * f.r2Off) / (outer * f.r2Off - inner * f.r2On);
+    f.bShift6 = 1.0 / std::pow(inner * outer, 3);
+    if (damp > 0.0) {
+        const double s12 = 1.0 / std::pow(damp, 12), fa = s12 - f.aShift12, ga = -12.0 * s12 / damp;
+        f.aF0 = fa - 0.5 * damp * ga; f.aAlpha = -0.5 * ga / damp;
+        const double s6 = 1.0 / std::pow(damp, 6), fb = -s6 + f.bShift6, gb = 6.0 * s6 / damp;
+        f.bF0 = fb - 0.5 * damp * gb; f.bAlpha = -0.5 * gb / damp;
+    }
+    return f;
+}
+
+// pair list (i, j) -> offsets (n + 1) and partners, both directions, partners in list order
+static void mm_csr(int n, int np, const int *pairs, std::vector<int> &start, std::vector<int> &idx)
+{
+    start.assign((size_t)n + 1, 0);
+    for (int k = 0; k < np; k++) { start[pairs[2 * k] + 1]++; start[pairs[2 * k + 1] + 1]++; }
+    for (int i = 0; i < n; i++) start[i + 1] += start[i];
+    idx.assign((size_t)start[n], 0);
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int k = 0; k < np; k++) {
+        const int i = pairs[2 * k], j = pairs[2 * k + 1];
+        idx[fill[i]++] = j; idx[fill[j]++] = i;
+    }
+}
+
+extern "C" int pdg_mm_create(int n_atoms, const double *h_charges, const int *h_lj_types, const unsigned char *h_flags, int n_lj_types,
+                             const double *h_table_a, const double *h_table_b, const double *h_table_a14, const double *h_table_b14,
+                             int n_exclusions, const int *h_exclusions, int n_pairs14, const int *h_pairs14, double inner_cutoff,
+                             double outer_cutoff, double damping_cutoff, double dielectric, double electrostatic_scale14,
+                             pdg_mm_system **out)
+{
+    if (!out || n_atoms <= 0 || !h_charges || !h_lj_types || !h_flags || n_lj_types <= 0 || !h_table_a || !h_table_b ||
+        !h_table_a14 || !h_table_b14 || n_exclusions < 0 || n_pairs14 < 0 || (n_exclusions > 0 && !h_exclusions) ||
+        (n_pairs14 > 0 && !h_pairs14))
+        return fail(PDG_BAD_ARGUMENT, "pdg_mm_create: bad argument");
+    if (!(damping_cutoff >= 0.0 && damping_cutoff < inner_cutoff && inner_cutoff < outer_cutoff && dielectric > 0.0))
+        return fail(PDG_BAD_ARGUMENT, "pdg_mm_create: cutoffs must satisfy 0 <= damping < inner < outer, dielectric > 0");
+    for (int i = 0; i < n_atoms; i++) {
+        if (h_lj_types[i] < 0 || h_lj_types[i] >= n_lj_types) return fail(PDG_BAD_ARGUMENT, "pdg_mm_create: LJ type out of range");
+        if (h_flags[i] & ~7) return fail(PDG_BAD_ARGUMENT, "pdg_mm_create: unknown atom flag");
+        if ((h_flags[i] & MM_FLAG_MM) && (h_flags[i] & MM_FLAG_QC_LJ))
+            return fail(PDG_BAD_ARGUMENT, "pdg_mm_create: an atom is either an MM atom or a QC atom");
+    }
+    for (int k = 0; k < n_exclusions + n_pairs14; k++) {
+        const int *p = k < n_exclusions ? h_exclusions + 2 * k : h_pairs14 + 2 * (k - n_exclusions);
+        if (p[0] < 0 || p[0] >= n_atoms || p[1] < 0 || p[1] >= n_atoms || p[0] == p[1])
+            return fail(PDG_BAD_ARGUMENT, "pdg_mm_create: pair index out of range or self pair");
+    }
+    std::vector<int> es, ei, ps, pi;
+    mm_csr(n_atoms, n_exclusions, h_exclusions, es, ei);
+    mm_csr(n_atoms, n_pairs14, h_pairs14, ps, pi);
+    const size_t nt2 = (size_t)n_lj_types * n_lj_types;
+    std::vector<double> real((size_t)n_atoms + 4 * nt2);
+    std::copy(h_charges, h_charges + n_atoms, real.begin());
+    std::copy(h_table_a, h_table_a + nt2, real.begin() + n_atoms);
+    std::copy(h_table_b, h_table_b + nt2, real.begin() + n_atoms + nt2);
+    std::copy(h_table_a14, h_table_a14 + nt2, real.begin() + n_atoms + 2 * nt2);
+    std::copy(h_table_b14, h_table_b14 + nt2, real.begin() + n_atoms + 3 * nt2);
+    std::vector<int> ints;
+    ints.insert(ints.end(), h_lj_types, h_lj_types + n_atoms);
+    const size_t o_es = ints.size(); ints.insert(ints.end(), es.begin(), es.end());
+    const size_t o_ei = ints.size(); ints.insert(ints.end(), ei.begin(), ei.end());
+    const size_t o_ps = ints.size(); ints.insert(ints.end(), ps.begin(), ps.end());
+    const size_t o_pi = ints.size(); ints.insert(ints.end(), pi.begin(), pi.end());
+    ints.push_back(0);   // never an empty allocation
+    pdg_mm_system *m = new pdg_mm_system();
+    int rc;
+    if ((rc = cuda_check(cudaMalloc(&m->d_real, sizeof(double) * real.size()), "allocate MM tables")) ||
+        (rc = cuda_check(cudaMalloc(&m->d_int, sizeof(int) * ints.size()), "allocate MM lists")) ||
+        (rc = cuda_check(cudaMalloc(&m->d_flags, (size_t)n_atoms), "allocate MM flags")) ||
+        (rc = cuda_check(cudaMemcpy(m->d_real, real.data(), sizeof(double) * real.size(), cudaMemcpyHostToDevice), "copy MM tables")) ||
+        (rc = cuda_check(cudaMemcpy(m->d_int, ints.data(), sizeof(int) * ints.size(), cudaMemcpyHostToDevice), "copy MM lists")) ||
+        (rc = cuda_check(cudaMemcpy(m->d_flags, h_flags, (size_t)n_atoms, cudaMemcpyHostToDevice), "copy MM flags"))) {
+        pdg_mm_destroy(m);
+        return rc;
+    }
+    MMDevice &d = m->d;
+    d.n_atoms = n_atoms; d.n_types = n_lj_types;
+    d.charge = m->d_real;
+    d.A = m->d_real + n_atoms; d.B = d.A + nt2; d.A14 = d.B + nt2; d.B14 = d.A14 + nt2;
+    d.lj_type = m->d_int;
+    d.excl_start = m->d_int + o_es; d.excl = m->d_int + o_ei; d.p14_start = m->d_int + o_ps; d.p14 = m->d_int + o_pi;
+    d.flags = m->d_flags;
+    d.fac = mm_factors(inner_cutoff, outer_cutoff, damping_cutoff);
+    // UNITS_ENERGY_E2ANGSTROMS_TO_KILOJOULES_PER_MOLE (pCore-1.9.0/extensions/cinclude/Units.h:18-49)
+    const double e2a_kj = (1.0e7 * 6.0221415e23 * 1.60217653e-19 * 1.60217653e-19) / (4.0 * M_PI * 8.854187817e-12);
+    d.escale = e2a_kj / dielectric;
+    d.escale14 = d.escale * electrostatic_scale14;
+    d.outer = outer_cutoff;
+    *out = m;
+    return PDG_OK;
+}
+
+extern "C" int pdg_mm_destroy(pdg_mm_system *m)
+{
+    if (!m) return PDG_OK;
+    if (m->d_real) cudaFree(m->d_real);
+    if (m->d_int) cudaFree(m->d_int);
+    if (m->d_flags) cudaFree(m->d_flags);
+    delete m;
+    return PDG_OK;
+}
+
+extern "C" size_t pdg_mm_workspace_bytes(const pdg_mm_system *m, int n_frames)
+{
+    if (!m || n_frames <= 0) return 0;
+    return mm_layout(m->d.n_atoms).stride * (size_t)n_frames;
+}
+
+extern "C" int pdg_mm_energy_gradients(const pdg_mm_system *m, int n_frames, const double *d_xyz, double *d_energies, double *d_gradients,
+                                       void *d_workspace, size_t workspace_bytes, void *stream)
+{
+    if (!m || n_frames <= 0 || n_frames > 65535 || !d_xyz || !d_energies || !d_workspace)
+        return fail(PDG_BAD_ARGUMENT, "pdg_mm_energy_gradients: bad argument");
+    if (workspace_bytes < pdg_mm_workspace_bytes(m, n_frames)) return fail(PDG_BAD_ARGUMENT, "pdg_mm_energy_gradients: workspace too small");
+    if (reinterpret_cast<uintptr_t>(d_workspace) % 256) return fail(PDG_BAD_ARGUMENT, "pdg_mm_energy_gradients: workspace not 256-byte aligned");
+    launch_mm_energy(m->d, n_frames, d_xyz, d_energies, d_gradients, (char *)d_workspace, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "MM/MM energy kernels");
+}

@@ -306,3 +306,33 @@ void launch_langevin_velocities(int n_replicas, int n_free, int n_rows, const in
                                 cudaStream_t st);
 void launch_density_combine(long long n, const DensityTerms &t, double *out, cudaStream_t st);
 void launch_normal_deviates(long long n_pairs, uint64_t seed, uint32_t step, uint32_t stream, double *out, cudaStream_t st);
+
+// ---- MM/MM and QC/MM Lennard-Jones energies (mmmm.cu) ----
+// Per-atom flags: an active MM atom, a QC atom with LJ interactions (the reference's qcpSelection), a fixed atom.
+constexpr int MM_FLAG_MM = 1, MM_FLAG_QC_LJ = 2, MM_FLAG_FIXED = 4;
+constexpr int MM_NCH = 6;             // energies: MM/MM Elect., MM/MM LJ, MM/MM 1-4 Elect., MM/MM 1-4 LJ, QC/MM LJ, QC/MM 1-4 LJ
+constexpr int MM_MAX_CELLS_1D = 32;   // cell-grid cells per dimension at most
+// PairwiseInteractionABFSFactors (cinclude/PairwiseInteraction.h:39-66), made by the host (PairwiseInteraction.c:89-140)
+struct MMFactors {
+    double r2Damp, r2Off, r2On, a, b, c, d, qShift1, qShift2, qF0, qAlpha;
+    double aF6, aK12, aShift12, aF0, aAlpha, bF3, bK6, bShift6, bF0, bAlpha;
+};
+struct MMDevice {
+    int n_atoms, n_types;
+    const double *charge;                 // n_atoms (e)
+    const int *lj_type;                   // n_atoms
+    const unsigned char *flags;           // n_atoms: MM_FLAG_*
+    const double *A, *B, *A14, *B14;      // LJ tables, n_types x n_types (kJ/mol A^12, kJ/mol A^6)
+    const int *excl_start, *excl;         // exclusions, both directions (n_atoms + 1 offsets)
+    const int *p14_start, *p14;           // 1-4 partners, both directions
+    MMFactors fac;
+    double escale, escale14;              // e^2/A -> kJ/mol over the dielectric; times electrostaticScale14
+    double outer;                         // outer cutoff (A)
+};
+// Per-frame workspace (byte offsets from the frame's base; stride bytes per frame)
+struct MMLayout {
+    size_t grid, count, start, cell_of, order, sxyzq, part, stride;
+    int n_blocks;
+};
+MMLayout mm_layout(int n_atoms);
+void launch_mm_energy(const MMDevice &m, int n_frames, const double *xyz, double *energies, double *grad, char *ws, cudaStream_t st);

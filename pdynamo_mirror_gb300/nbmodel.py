@@ -147,14 +147,19 @@ class NBModelABFS:
 
     model_id = 1
 
-    def __init__(self, innerCutoff=8.0, outerCutoff=12.0, listCutoff=13.5, dielectric=1.0, **options):
+    def __init__(self, innerCutoff=8.0, outerCutoff=12.0, listCutoff=13.5, dielectric=1.0, dampingCutoff=0.5,
+                 electrostaticScale14=1.0, **options):
+        # defaults as NBModelABFS.c:29-36; dampingCutoff and electrostaticScale14 act on the MM/MM terms (mmmodel.py)
         if options:
             raise ValueError("Invalid options: " + ", ".join(sorted(options)) + ".")
         if dielectric != 1.0:
             raise ValueError("Only dielectric 1 is supported.")
         if not (0.0 < innerCutoff < outerCutoff <= listCutoff):
             raise ValueError("Cutoffs must satisfy 0 < inner < outer <= list.")
+        if not (0.0 <= dampingCutoff < innerCutoff):
+            raise ValueError("The damping cutoff must satisfy 0 <= damping < inner.")
         self.innerCutoff, self.outerCutoff, self.listCutoff = float(innerCutoff), float(outerCutoff), float(listCutoff)
+        self.dielectric, self.dampingCutoff, self.electrostaticScale14 = float(dielectric), float(dampingCutoff), float(electrostaticScale14)
         self._knots = None
 
     def knots(self):

@@ -49,6 +49,8 @@ class System:
         self._engine = None
         self.densityGuess = None
         self.fixedAtoms = None
+        self.mmModel = None
+        self._mm = None
 
     # -- model definition (System.py:182-230)
     def DefineQCModel(self, qcModel, qcSelection=None):
@@ -78,6 +80,30 @@ class System:
         if sel and (sel[0] < 0 or sel[-1] >= len(self.atomicNumbers)):
             raise ValueError("Invalid fixed-atom selection.")
         self.fixedAtoms = sel
+
+    def DefineMMModel(self, mmModel):
+        """The MM side of the system (mmmodel.MMModel: charges, LJ types and parameters, exclusions, 1-4 pairs):
+        with an NBModelABFS, the energy then includes the MM/MM electrostatic and LJ terms and the QC/MM LJ terms
+        (NBModelABFS.pyx:108-122).  The model's charges become the MM point charges.  None removes it."""
+        if mmModel is not None:
+            if mmModel.natoms != len(self.atomicNumbers):
+                raise ValueError("The MM model must cover every atom of the system.")
+            self.mmCharges = np.array(mmModel.charges, dtype=np.float64)
+            if self.qcSelection is not None:
+                self.mmCharges[self.qcSelection] = 0.0
+        self.mmModel = mmModel
+        self._mm = None
+        self._sel_key = None
+
+    def _mm_interactions(self):
+        from .mmmodel import MMInteractions
+        from .nbmodel import NBModelABFS
+        if not isinstance(self.nbModel, NBModelABFS):
+            raise ValueError("MM/MM energies need an NBModelABFS.")
+        key = (id(self.mmModel), id(self.nbModel), tuple(self.qcSelection or []), tuple(self.fixedAtoms or []))
+        if self._mm is None or self._mm[0] != key:
+            self._mm = (key, MMInteractions(self.mmModel, self.nbModel, self.qcSelection, self.fixedAtoms, self.engine().device))
+        return self._mm[1]
 
     def DefineDensityGuess(self, guess):
         """Start cold SCFs from a LearnedDensityGuess (None: the diagonal guess).  Not in the reference."""
@@ -117,12 +143,16 @@ class System:
     def _take(X, s):
         return X[:, s].contiguous() if isinstance(s, slice) else X.index_select(1, s)
 
-    def _device_inputs(self, frames):
-        """frames: [F, n, 3] host (numpy or torch, ideally pinned) or device tensor.  One copy to the device,
-        QC/MM split on the device."""
+    def _device_frames(self, frames):
+        """frames: [F, n, 3] host (numpy or torch, ideally pinned) or device tensor -> one copy on the device."""
         dev = self.engine().device
         X = frames if isinstance(frames, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(frames, dtype=np.float64))
-        X = X.to(device=dev, dtype=torch.float64, non_blocking=True)
+        return X.to(device=dev, dtype=torch.float64, non_blocking=True)
+
+    def _device_inputs(self, frames, X=None):
+        """QC and MM coordinates of the frames, split on the device (X: the frames already on the device)."""
+        if X is None:
+            X = self._device_frames(frames)
         qs, ms, q, mm_idx = self._selections()
         qc = self._take(X, qs)
         mm = self._take(X, ms) if ms is not None else None
@@ -139,12 +169,17 @@ class System:
         if frames.ndim == 2:
             frames = frames[None]
         eng = self.engine()
-        qc, mm, q, mm_idx = self._device_inputs(frames)
+        X = self._device_frames(frames)
+        qc, mm, q, mm_idx = self._device_inputs(None, X)
+        mmi = self._mm_interactions() if self.mmModel is not None else None
         r = eng.run(qc, self.qcModel.converger, mm, q, self.nbModel if mm is not None else None, gradients=doGradients,
                     warm_start=warmStart, guess=self.densityGuess)
         F = qc.shape[0]
         # one device -> host copy of the small per-frame results
         small = torch.cat([r["energies"], r["status"].to(torch.float64)[:, None], r["ncycles"].to(torch.float64)[:, None]], 1)
+        if mmi is not None:
+            Emm, Gmm = mmi.run(X, gradients=doGradients)
+            small = torch.cat([small, Emm], 1)
         G = None
         if doGradients:
             qs, ms, _, _ = self._selections()
@@ -155,6 +190,8 @@ class System:
                 Gd[:, ms] = r["qcmm_mm_gradients"]
             Gd[:, qs] = gq
             Gd *= GRADIENT_TO_KJ_PER_A
+            if mmi is not None:
+                Gd += Gmm
             Gh = torch.empty(Gd.shape, dtype=torch.float64, pin_memory=True)
             Gh.copy_(Gd, non_blocking=True)
         small = small.cpu().numpy()
@@ -170,6 +207,12 @@ class System:
             self._engine.density = None
             raise SCFNotConverged("SCF procedure not converged.")
         total = pure + (qcmm if mm is not None else 0.0)
+        if mmi is not None:
+            Emm = small[:, _native.NENERGY + 2:]
+            for k, name in enumerate(_native.MM_TERMS):
+                if name in mmi.term_names():
+                    terms[name] = Emm[:, k]
+            total = total + Emm.sum(1)
         return total, G, terms
 
     def Energy(self, doGradients=False, log=None):
