@@ -15,6 +15,6 @@ from .mmmodel import LJParameterContainer, MMModel
 from .nbmodel import NBModelABFS, NBModelFull
 from .qcmodel import QCModelMNDO
 from .system import ElectronicState, SCFNotConverged, System
-from .trajectory import DCDTrajectoryFileReader, DCDTrajectoryFileWriter
+from .trajectory import DCDTrajectoryFileReader, DCDTrajectoryFileWriter, SystemGeometryTrajectory
 
-__all__ = ["DCDTrajectoryFileReader", "DCDTrajectoryFileWriter", "DIISSCFConverger", "LangevinDynamics", "LangevinDynamics_SystemGeometry", "LangevinVelocityVerletIntegrator", "LJParameterContainer", "MMModel", "MoleculeBatch", "ElectronicState", "LearnedDensityGuess", "NBModelABFS", "NBModelFull", "QCModelMNDO", "SCFNotConverged", "System"]
+__all__ = ["DCDTrajectoryFileReader", "DCDTrajectoryFileWriter", "DIISSCFConverger", "LangevinDynamics", "LangevinDynamics_SystemGeometry", "LangevinVelocityVerletIntegrator", "LJParameterContainer", "MMModel", "MoleculeBatch", "SystemGeometryTrajectory", "ElectronicState", "LearnedDensityGuess", "NBModelABFS", "NBModelFull", "QCModelMNDO", "SCFNotConverged", "System"]

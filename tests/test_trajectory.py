@@ -80,3 +80,108 @@ def test_round_trip_and_errors(tmp_path):
     (tmp_path / "bad.dcd").write_bytes(b"\0" * 300)
     with pytest.raises(ValueError):
         DCDTrajectoryFileReader(tmp_path / "bad.dcd")
+
+
+# ---- directory trajectories (SystemGeometryTrajectory) ----
+class _Owner:
+    def __init__(self, X, fixed=None):
+        self.coordinates3 = np.array(X, dtype=np.float64)
+        self.fixedAtoms = fixed
+
+
+def _rotation(angle, axis):
+    a = np.asarray(axis, float) / np.linalg.norm(axis)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    return np.eye(3) + np.sin(angle) * K + (1 - np.cos(angle)) * K @ K
+
+
+def test_directory_trajectory_modes_and_frames(tmp_path):
+    from pdynamo_mirror_gb300 import SystemGeometryTrajectory
+    rng = np.random.default_rng(1)
+    X = rng.normal(size=(7, 3))
+    owner = _Owner(X)
+    path = tmp_path / "traj"
+    with pytest.raises(IOError):
+        SystemGeometryTrajectory(path, owner, mode="r")
+    t = SystemGeometryTrajectory(path, owner)           # new: "w"
+    assert t.mode == "w" and t.isWritable and t.isReadable
+    for k in range(3):
+        owner.coordinates3 = X + k
+        t.WriteOwnerData()
+    assert len(t) == 3
+    r = SystemGeometryTrajectory(path, owner)           # existing: "r"
+    assert r.mode == "r" and len(r) == 3 and not r.isWritable
+    with pytest.raises(IOError):
+        r.WriteFrame(X)
+    np.testing.assert_array_equal(r[2], X + 2)
+    with pytest.raises(IndexError):
+        r[3]
+    seen = []
+    while r.RestoreOwnerData():
+        seen.append(owner.coordinates3.copy())
+    assert len(seen) == 3 and np.array_equal(seen[1], X + 1)
+    assert r.RestoreOwnerData(index=0) and np.array_equal(owner.coordinates3, X)
+    a = SystemGeometryTrajectory(path, owner, mode="a")
+    assert len(a) == 3
+    a.WriteFrame(X - 1)
+    assert len(SystemGeometryTrajectory(path, owner, mode="r")) == 4
+    w = SystemGeometryTrajectory(path, owner, mode="w")  # write modes clear the frames
+    assert len(w) == 0 and len(SystemGeometryTrajectory(path, owner, mode="r")) == 0
+    f = tmp_path / "file"
+    f.write_text("x")
+    with pytest.raises(IOError):
+        SystemGeometryTrajectory(f, owner)
+    with pytest.raises(IOError):
+        SystemGeometryTrajectory(tmp_path / "other", owner, mode="q")
+
+
+def test_superposition_recovers_a_rigid_motion():
+    from pdynamo_mirror_gb300.trajectory import rms_deviation, superimpose
+    rng = np.random.default_rng(2)
+    X = rng.normal(size=(12, 3)) * 3.0
+    Y = X @ _rotation(1.1, [1, 2, -0.5]).T + np.array([4.0, -2.0, 9.0])
+    assert rms_deviation(Y, X) > 1.0
+    np.testing.assert_allclose(superimpose(Y, X), X, atol=1e-12)
+    w = rng.uniform(0.5, 2.0, size=12)
+    np.testing.assert_allclose(superimpose(Y, X, w), X, atol=1e-12)
+    assert rms_deviation(superimpose(Y + rng.normal(scale=0.1, size=Y.shape), X), X) < 0.2
+
+
+def test_linear_interpolation_and_expansion(tmp_path):
+    from pdynamo_mirror_gb300 import SystemGeometryTrajectory
+    rng = np.random.default_rng(3)
+    X0 = rng.normal(size=(6, 3)) * 2.0
+    Xn = X0 + rng.normal(scale=0.3, size=X0.shape)
+    # fixed atoms: plain linear interpolation, no superposition
+    owner = _Owner(X0, fixed=[0])
+    t = SystemGeometryTrajectory.LinearlyInterpolate(tmp_path / "i", owner, 5, X0, Xn)
+    assert len(t) == 5
+    for k in range(5):
+        np.testing.assert_allclose(t[k], X0 + (Xn - X0) * k / 4.0, atol=1e-12)
+    # expansion: ninsert frames between each pair, the old frames kept at their new places
+    t.LinearlyExpand(2)
+    assert len(t) == 13
+    for k in range(13):
+        np.testing.assert_allclose(t[k], X0 + (Xn - X0) * k / 12.0, atol=1e-12)
+    # without fixed atoms the end point is superimposed on the start first: a rigidly moved copy interpolates
+    # to the start structure everywhere
+    owner = _Owner(X0)
+    Y = X0 @ _rotation(0.7, [0, 1, 1]).T + 3.0
+    t = SystemGeometryTrajectory.LinearlyInterpolate(tmp_path / "j", owner, 3, X0, Y)
+    for k in range(3):
+        np.testing.assert_allclose(t[k], X0, atol=1e-12)
+
+
+def test_trajectory_superimpose(tmp_path):
+    from pdynamo_mirror_gb300 import SystemGeometryTrajectory
+    rng = np.random.default_rng(4)
+    X = rng.normal(size=(9, 3)) * 2.0
+    owner = _Owner(X)
+    t = SystemGeometryTrajectory(tmp_path / "s", owner, mode="w")
+    for k in range(4):
+        t.WriteFrame(X @ _rotation(0.3 * k, [1, 0, 1]).T + k)
+    res = t.Superimpose()
+    assert len(res) == 4 and all(after <= before + 1e-12 for before, after in res) and res[3][0] > 1.0
+    for k in range(4):
+        np.testing.assert_allclose(t[k], X, atol=1e-12)
+    np.testing.assert_array_equal(owner.coordinates3, X)
