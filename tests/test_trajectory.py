@@ -1,7 +1,9 @@
 """DCD trajectories (pdynamo_mirror_gb300/trajectory.py) against the record layout of pBabel's DCDWrite.c
 (pBabel-1.9.0/extensions/csource/DCDWrite.c:62-269): header words, title records, the atom count and free-atom
 index records, float32 coordinate records (all atoms first, free atoms afterwards when atoms are fixed), the
-NFILE / NSTEP words rewritten after every frame, and the round trip through the reader.  No GPU."""
+NFILE / NSTEP words rewritten after every frame, and the round trip through the reader; and the directory
+trajectories (SystemGeometryTrajectory, pBabel-1.9.0/pBabel/SystemGeometryTrajectory.py): modes, frame order,
+interpolation, expansion and superposition.  No GPU."""
 import struct
 
 import numpy as np
