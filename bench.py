@@ -318,7 +318,7 @@ MD_METRIC = "QC/MM E+grad evals/s in 300 K Langevin dynamics (AM1, 65 QC atoms i
 def bench_md(args):
     """Config 3 of the metric's workload family: Langevin dynamics (300 K, 0.5 fs, 25 ps^-1) of `frames` replicas
     of the QC/MM water box with the MM waters fixed, every step one energy + gradient per replica.  The learned
-    start density is trained on densities converged along training trajectories (seed apart), then judged on
+    start density is trained on densities converged along training trajectories (seed apart), then evaluated on
     held-out trajectories: (a) cold, against the diagonal guess, on held-out frames; (b) in dynamics, as a
     correction of the extrapolated start (2 P(t-1) - P(t-2) + M(t) - 2 M(t-1) + M(t-2)), against the previous-step
     start (the reference's behaviour) and the plain extrapolation.  The timed comparison: the learned+mixed method

@@ -132,7 +132,7 @@ class LearnedDensityGuess:
         return hist
 
     def validate(self, qc_xyz, converger, mm_xyz=None, mm_charges=None, nbmodel=None):
-        """Held-out check with the converged SCF as the judge: run the frames [F, n, 3] cold from the diagonal
+        """Held-out check, the converged SCF deciding: run the frames [F, n, 3] cold from the diagonal
         guess and from this guess, compare the mean SCF cycles and the energies, and keep the guess enabled
         only if it saved cycles (else the standard guess is the fallback).  Returns the figures as a dict."""
         eng = self.eng

@@ -2,7 +2,7 @@
 the counter-based normal deviates against the oracle's restatement, the two half-step kernels against the
 oracle's restatement of LangevinVelocityVerletIntegrator.Iteration for given deviates, a QC/MM trajectory against
 the oracle's energies and gradients step by step, the thermostat's temperature and position variance in a
-harmonic well, and the invariance of trajectories under the SCF start density (the converged SCF is the judge)."""
+harmonic well, and the invariance of trajectories under the SCF start density (the converged SCF decides)."""
 import ctypes, math
 
 import numpy as np
