@@ -272,12 +272,16 @@ int ref_element_basis ( void *vh, const int e, double *exponents, double *ccbf )
     return 0 ;
 }
 
-/* . System set-up: QC atom container (QCAtomContainer.pyx:218-278), model and state (QCModelMNDO.pyx:623-672). */
-void *ref_system_create ( void *vh, const int nAtoms, const int *elementIndex, const int charge, const int withQCMM,
-                          const double densityTolerance, const int maximumSCFCycles, const int history,
-                          const double diisOnset, const double energyTolerance, const int useRCA )
+/* . System set-up: QC atom container (QCAtomContainer.pyx:218-278), model and state (QCModelMNDO.pyx:623-672).
+!  . alphaCharge / betaCharge as QCModel.CrossCheckModelAndState forms them (pMolecule.QCModel.pyx:99-118); the
+!  . state as QCModelMNDOState_Setup (QCModelMNDOState.c) with the model's occupancy options; nFractional: the
+!  . numbers of fractionally occupied HOOs / LUOs (restricted), then alpha HOOs / LUOs and beta HOOs / LUOs. */
+static RefSystem *MakeSystem ( RefHamiltonian *h, const int nAtoms, const int *elementIndex, const int withQCMM,
+                               const double densityTolerance, const int maximumSCFCycles, const int history,
+                               const double diisOnset, const double energyTolerance, const int useRCA,
+                               const int openShell, const double alphaCharge, const double betaCharge, const int isSpinRestricted,
+                               const int occupancyType, const int *nFractional, const double fermiBroadening, const int charge )
 {
-    RefHamiltonian *h = ( RefHamiltonian * ) vh ;
     RefSystem *s ;
     QCAtomContainer *a ;
     int i, nElectrons ;
@@ -306,8 +310,18 @@ void *ref_system_create ( void *vh, const int nAtoms, const int *elementIndex, c
     s->qcAtoms = a ;
     nElectrons = a->nuclearCharge - charge ;
     s->model = QCModelMNDO_Allocate ( ) ;
-    s->state = QCModelMNDOState_Setup ( a, h->parameters, 0.5 * nElectrons, 0.5 * nElectrons, s->model->occupancyType, True,
-                                        0, 0, 0, 0, 0, 0, s->model->fermiBroadening ) ;
+    if ( openShell )
+    {
+        s->model->isSpinRestricted = isSpinRestricted ? True : False ;
+        s->model->occupancyType    = ( QCOnePDMOccupancyType ) occupancyType ;
+        s->model->fermiBroadening  = fermiBroadening ;
+        s->state = QCModelMNDOState_Setup ( a, h->parameters, alphaCharge, betaCharge, s->model->occupancyType, s->model->isSpinRestricted,
+                                            nFractional[0], nFractional[1], nFractional[2], nFractional[3], nFractional[4], nFractional[5],
+                                            s->model->fermiBroadening ) ;
+    }
+    else
+        s->state = QCModelMNDOState_Setup ( a, h->parameters, 0.5 * nElectrons, 0.5 * nElectrons, s->model->occupancyType, True,
+                                            0, 0, 0, 0, 0, 0, s->model->fermiBroadening ) ;
     s->converger = DIISSCFConverger_Allocate ( ) ;
     s->converger->densityTolerance = densityTolerance ;
     s->converger->maximumSCFCycles = maximumSCFCycles ;
@@ -319,6 +333,38 @@ void *ref_system_create ( void *vh, const int nAtoms, const int *elementIndex, c
     s->gradients3   = Coordinates3_Allocate ( nAtoms ) ;
     if ( withQCMM ) s->qcmm = QCMMInteractionState_Allocate ( nAtoms, False, NULL ) ;
     return s ;
+}
+
+void *ref_system_create ( void *vh, const int nAtoms, const int *elementIndex, const int charge, const int withQCMM,
+                          const double densityTolerance, const int maximumSCFCycles, const int history,
+                          const double diisOnset, const double energyTolerance, const int useRCA )
+{
+    return MakeSystem ( ( RefHamiltonian * ) vh, nAtoms, elementIndex, withQCMM, densityTolerance, maximumSCFCycles, history,
+                        diisOnset, energyTolerance, useRCA, 0, 0.0, 0.0, 1, 0, NULL, 0.0, charge ) ;
+}
+
+/* . Open-shell and fractional-occupancy states (QCModelMNDO keywords isSpinRestricted, occupancyType (0 cardinal,
+!  . 1 fixed fractional, 2 variable fractional), numberFractional*, fermiBroadening). */
+void *ref_system_create_open ( void *vh, const int nAtoms, const int *elementIndex, const double alphaCharge, const double betaCharge,
+                               const int isSpinRestricted, const int occupancyType, const int *nFractional, const double fermiBroadening,
+                               const double densityTolerance, const int maximumSCFCycles, const int history,
+                               const double diisOnset, const double energyTolerance, const int useRCA )
+{
+    return MakeSystem ( ( RefHamiltonian * ) vh, nAtoms, elementIndex, 0, densityTolerance, maximumSCFCycles, history,
+                        diisOnset, energyTolerance, useRCA, 1, alphaCharge, betaCharge, isSpinRestricted, occupancyType,
+                        nFractional, fermiBroadening, 0 ) ;
+}
+
+/* . The state's densities (packed lower triangles): restricted, the total density in p (q untouched); unrestricted,
+!  . alpha in p and beta in q.  Returns 1 for unrestricted states. */
+int ref_system_get_densities ( void *vs, double *p, double *q )
+{
+    RefSystem *s = ( RefSystem * ) vs ;
+    if ( s == NULL ) return -1 ;
+    memcpy ( p, s->state->densityp->density->data, sizeof ( double ) * s->state->densityp->density->size ) ;
+    if ( s->state->densityq == NULL ) return 0 ;
+    if ( q != NULL ) memcpy ( q, s->state->densityq->density->data, sizeof ( double ) * s->state->densityq->density->size ) ;
+    return 1 ;
 }
 
 int ref_system_nbasis ( void *vs ) { RefSystem *s = ( RefSystem * ) vs ; return ( s == NULL ) ? -1 : s->qcAtoms->nobasis ; }

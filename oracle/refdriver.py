@@ -49,6 +49,9 @@ def lib():
         L.ref_abfs_create.argtypes = [D, D, I, pd, pd]
         L.ref_abfs_spline.argtypes = [P, I, pd, pd, pd]
         L.ref_abfs_qcmm.argtypes = [P, P, pd, I, pd, pd, pd, pd, pd, pd]
+        L.ref_system_create_open.restype = P
+        L.ref_system_create_open.argtypes = [P, I, pi, D, D, I, I, pi, D, D, I, I, D, D, I]
+        L.ref_system_get_densities.argtypes = [P, pd, P]
         L.ref_mmmm_energy.argtypes = [I, pd, pd, pi, pi, I, pd, pd, pd, pd, I, I, pi, I, pi, D, D, D, D, D, D, pd, pd]
         _lib = L
     return _lib
@@ -79,6 +82,10 @@ class RefHamiltonian:
             names[key] = out[o:o + n].copy() if n > 1 else float(out[o]); o += n
         return names
 
+    def nuclear_charge(self, z):
+        """The element's core charge (zcore), as the QC atom container sums it."""
+        return int(round(self.derived(z)["zcore"]))
+
     def basis(self, z):
         e = np.zeros(2 * MAXPRIM); c = np.zeros(2 * MAXPRIM)
         lib().ref_element_basis(self.handle, self.elements.index(z), e, c)
@@ -91,14 +98,39 @@ class RefSystem:
     KJ_PER_HARTREE = 2625.5
     ANGSTROMS_TO_BOHRS = 1.0e-10 / 5.291772083e-11
 
+    OCCUPANCY_TYPES = {"Cardinal": 0, "Fixed Fractional": 1, "Variable Fractional": 2}
+
     def __init__(self, ham, atomic_numbers, charge=0, qcmm=False, densityTolerance=1.0e-8, maximumSCFCycles=100,
-                 history=10, diisOnset=0.2, energyTolerance=2.0e-4, useRCA=True):
+                 history=10, diisOnset=0.2, energyTolerance=2.0e-4, useRCA=True, multiplicity=None, isSpinRestricted=True,
+                 occupancyType="Cardinal", numberFractional=(1, 0, 1, 0, 1, 0), fermiBroadening=1.0e3):
+        """multiplicity None: the closed-shell set-up.  Otherwise the open-shell and fractional-occupancy state of
+        QCModelMNDO's keywords, with the alpha and beta electron counts of QCModel.CrossCheckModelAndState
+        (pMolecule.QCModel.pyx:91-140); numberFractional = (HOOs, LUOs, alpha HOOs, alpha LUOs, beta HOOs, beta LUOs)."""
         self.ham = ham
         self.atomic_numbers = [int(z) for z in atomic_numbers]
         idx = np.array([ham.elements.index(z) for z in self.atomic_numbers], dtype=np.int32)
         self.n = len(idx)
-        self.handle = lib().ref_system_create(ham.handle, self.n, idx, int(charge), int(qcmm), densityTolerance,
-                                              maximumSCFCycles, history, diisOnset, energyTolerance, int(useRCA))
+        self.restricted = True
+        if multiplicity is None:
+            self.handle = lib().ref_system_create(ham.handle, self.n, idx, int(charge), int(qcmm), densityTolerance,
+                                                  maximumSCFCycles, history, diisOnset, energyTolerance, int(useRCA))
+        else:
+            if qcmm:
+                raise ValueError("open-shell reference systems are QC only here")
+            ne = float(sum(ham.nuclear_charge(z) for z in self.atomic_numbers)) - float(charge)
+            a, b = (ne + (multiplicity - 1.0)) / 2.0, (ne - (multiplicity - 1.0)) / 2.0
+            if occupancyType == "Cardinal":
+                if abs(round(ne) - ne) > 1e-6:
+                    raise ValueError("Cardinal occupancy requires integral charge.")
+                if isSpinRestricted and multiplicity > 1:
+                    raise ValueError("A spin-unrestricted calculation is required for non-singlet states with cardinal occupancy.")
+            elif isSpinRestricted and multiplicity > 1:
+                raise ValueError("A spin-unrestricted calculation is required for non-singlet states with fractional occupancy.")
+            nf = np.ascontiguousarray(numberFractional, dtype=np.int32)
+            self.handle = lib().ref_system_create_open(ham.handle, self.n, idx, a, b, int(bool(isSpinRestricted)),
+                                                       self.OCCUPANCY_TYPES[occupancyType], nf, fermiBroadening, densityTolerance,
+                                                       maximumSCFCycles, history, diisOnset, energyTolerance, int(useRCA))
+            self.restricted = bool(isSpinRestricted)
         self.nbasis = lib().ref_system_nbasis(self.handle)
 
     def __del__(self):
@@ -115,13 +147,17 @@ class RefSystem:
         ph = None if phi is None else np.ascontiguousarray(phi, dtype=np.float64)
         rc = lib().ref_system_energy(self.handle, xyz, _ptr(ph), int(gradients), en, g, _ptr(q), _ptr(h), ctypes.byref(nc))
         P = np.zeros_like(h)
-        lib().ref_system_get_density(self.handle, P)
+        Q = np.zeros_like(h)
+        lib().ref_system_get_densities(self.handle, P, Q.ctypes.data_as(ctypes.c_void_p))
         conv = 1.0 / (self.ANGSTROMS_TO_BOHRS * self.KJ_PER_HARTREE)
-        return {"total_electronic": en[0], "eelectronic": en[1], "enuclear": en[2], "baseline": en[3], "eqcmm": en[4],
-                "eocc": en[5], "eoei": en[6], "etei": en[7],
-                "pure_qc_kj": self.KJ_PER_HARTREE * (en[1] + en[2] + en[3]),
-                "gradients": (g * conv).reshape(self.n, 3), "density": P, "H": h, "charges": q,
-                "ncycles": nc.value, "converged": rc == 0}
+        out = {"total_electronic": en[0], "eelectronic": en[1], "enuclear": en[2], "baseline": en[3], "eqcmm": en[4],
+               "eocc": en[5], "eoei": en[6], "etei": en[7],
+               "pure_qc_kj": self.KJ_PER_HARTREE * (en[1] + en[2] + en[3]),
+               "gradients": (g * conv).reshape(self.n, 3), "density": P, "H": h, "charges": q,
+               "ncycles": nc.value, "converged": rc == 0}
+        if not self.restricted:
+            out["density"], out["density_alpha"], out["density_beta"] = P + Q, P, Q
+        return out
 
     def set_density(self, P):
         lib().ref_system_set_density(self.handle, np.ascontiguousarray(P, dtype=np.float64))

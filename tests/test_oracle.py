@@ -73,3 +73,25 @@ def test_oracle_abfs_matches_reference_fixture():
     assert abs(2625.5 * r["eqcmm"] - c["qcmm_kj"]) < 1.0e-7
     assert np.abs(r["gradients"] + gq - np.array(c["qc_gradients"])).max() < 1.0e-8
     assert np.abs(gm - np.array(c["mm_gradients"])).max() < 1.0e-10
+
+
+def test_open_shell_fixture_regenerates_from_the_reference_core():
+    """tests/golden/open_shell_reference.json (UHF / fractional occupancy, the reference's radical set) is what the
+    reference core gives: one case recomputed where the core is built."""
+    import json, os
+    R = pytest.importorskip("oracle.refdriver")
+    try:
+        R.lib()
+    except R.RefUnavailable:
+        pytest.skip("reference core not built")
+    d = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "open_shell_reference.json")))
+    c = [c for c in d["cases"] if c["label"] == "Allyl Radical" and c["occupancyType"] == "Cardinal"][0]
+    ham = R.RefHamiltonian("am1", c["atomic_numbers"])
+    s = R.RefSystem(ham, c["atomic_numbers"], charge=c["charge"], multiplicity=c["multiplicity"],
+                    isSpinRestricted=c["isSpinRestricted"], occupancyType=c["occupancyType"], densityTolerance=1.0e-8,
+                    maximumSCFCycles=500)
+    r = s.energy(np.array(c["xyz"]))
+    assert r["converged"] and r["ncycles"] == c["ncycles"]
+    assert abs(r["pure_qc_kj"] - c["pure_qc_kj"]) < 1e-9
+    np.testing.assert_allclose(r["gradients"], c["gradients_hartree_per_bohr"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(r["density_alpha"], c["density_alpha"], rtol=0, atol=1e-12)
