@@ -882,7 +882,7 @@ static double build_fock(const Config *c, const double *P, double *F, const doub
 /* ================================================================================================ */
 /* Gradients: csource/QCModelMNDO.c:732-855 with csource/QCModelMNDOState.c:178-260 (density terms) and
  * csource/MNDOIntegrals.c:274-450 (MolecularFrame2CIntegralsD).  Output in Eh/Bohr.               */
-static void gradients(const Config *c, const double *P, double *g)
+static void gradients(const Config *c, const double *P, const double *S, double *g)
 {
     int N = c->nBasis;
     memset(g, 0, sizeof(double) * 3 * c->nAtoms);
@@ -907,6 +907,9 @@ static void gradients(const Config *c, const double *P, double *g)
                             double bb = (m == n) ? 1.0 : 2.0;
                             int K = is + k, Lx = is + l, M = js + m, Nn = js + n;
                             double f = P[M * N + K] * P[Nn * N + Lx] + P[Nn * N + K] * P[M * N + Lx];
+                            /* open shell: the spin density's products join the exchange part
+                               (csource/QCModelMNDOState.c:178-260, dspin) */
+                            if (S) f += S[M * N + K] * S[Nn * N + Lx] + S[Nn * N + K] * S[M * N + Lx];
                             gam[kl][mn] = 0.25 * aa * bb * f - oneI[kl] * oneJ[mn];
                         }
                 }
@@ -1122,10 +1125,368 @@ int oracle_energy(const OracleHamiltonian *h, int nAtoms, const int *elementInde
     energies[0] = eqc + eqcmm; energies[1] = eqc; energies[2] = c.enuc;
     double base = 0.0; for (int i = 0; i < nAtoms; i++) base += c.el[i]->eheat - c.el[i]->eisol;
     energies[3] = base; energies[4] = eqcmm; energies[5] = 0.0; energies[6] = eoei; energies[7] = etei;
-    if (grad && converged) gradients(&c, P, grad);
+    if (grad && converged) gradients(&c, P, NULL, grad);
     if (density) for (int i = 0; i < N; i++) for (int j = 0; j <= i; j++) density[PK(i, j)] = P[i * N + j];
     for (int i = 0; i < d.ndiis; i++) { free(d.xP[i]); free(d.xF[i]); free(d.err[i]); }
     free(d.rP); free(d.rF); free(P); free(F); free(work);
+    config_free(&c);
+    return converged ? 0 : 1;
+}
+
+/* ================================================================================================ */
+/* Open-shell and fractional-occupancy states (QCModelMNDO keywords isSpinRestricted, occupancyType):
+ * restricted densities hold the total density (occupancy factor 2), unrestricted ones alpha and beta
+ * (factor 1) (csource/QCModelMNDOState.c QCModelMNDOState_Setup).                                   */
+
+/* Two-electron part G = J(Pt) - K(Ps) of one spin's Fock matrix: Coulomb from the total density, exchange
+ * from the density of that spin (csource/MNDOIntegrals.c:51-143 MakeFockG with its second density;
+ * the one-centre terms split as (ss|ss) = gss, (ss|pp) = gsp, (sp|sp) = hsp, (pp|pp) = gpp,
+ * (pp|qq) = gp2, (pq|pq) = hpp).  fock_g is the case Ps = Pt / 2.                                  */
+static void fock_g_spin(const Config *c, const double *Pt, const double *Ps, double *G)
+{
+    int N = c->nBasis;
+    memset(G, 0, sizeof(double) * N * N);
+    for (int i = 0; i < c->nAtoms; i++) {
+        const Element *e = c->el[i];
+        int s = c->start[i];
+        if (fabs(e->gss) > TEI_UNDERFLOW) G[s * N + s] += (Pt[s * N + s] - Ps[s * N + s]) * e->gss;
+        if (e->norb == 4) {
+            for (int p = 1; p < 4; p++) {
+                int pp = s + p;
+                G[s * N + s] += Pt[pp * N + pp] * e->gsp - Ps[pp * N + pp] * e->hsp;
+                G[pp * N + pp] += Pt[s * N + s] * e->gsp - Ps[s * N + s] * e->hsp + (Pt[pp * N + pp] - Ps[pp * N + pp]) * e->gpp;
+                double v = 2.0 * Pt[s * N + pp] * e->hsp - Ps[s * N + pp] * (e->hsp + e->gsp);
+                G[s * N + pp] += v; G[pp * N + s] += v;
+                for (int q = 1; q < 4; q++) {
+                    if (q == p) continue;
+                    int qq = s + q;
+                    G[pp * N + pp] += Pt[qq * N + qq] * e->gp2 - Ps[qq * N + qq] * e->hpp;
+                    G[pp * N + qq] += 2.0 * Pt[pp * N + qq] * e->hpp - Ps[pp * N + qq] * (e->hpp + e->gp2);
+                }
+            }
+        }
+        for (int j = 0; j < i; j++) {
+            const double *blk = c->tei + (size_t)pair_index(i, j) * 100;
+            int is = c->start[i], js = c->start[j], ni = c->norb[i], nj = c->norb[j];
+            int ab = 0;
+            for (int a = 0; a < ni; a++)
+                for (int b = 0; b <= a; b++, ab++) {
+                    int cd = 0;
+                    for (int cc = 0; cc < nj; cc++)
+                        for (int d = 0; d <= cc; d++, cd++) {
+                            double v = blk[ab * 10 + cd];
+                            if (fabs(v) <= TEI_UNDERFLOW) continue;
+                            int A[2] = { is + a, is + b }, B[2] = { js + cc, js + d };
+                            int na = (a == b) ? 1 : 2, nb = (cc == d) ? 1 : 2;
+                            for (int u = 0; u < na; u++)
+                                for (int w = 0; w < nb; w++) {
+                                    int m = A[u], n = A[1 - u], l = B[w], sg = B[1 - w];
+                                    if (na == 1) n = m;
+                                    if (nb == 1) sg = l;
+                                    G[m * N + n] += v * Pt[l * N + sg];
+                                    G[l * N + sg] += v * Pt[m * N + n];
+                                    G[m * N + l] -= v * Ps[n * N + sg];
+                                    G[l * N + m] -= v * Ps[n * N + sg];
+                                }
+                        }
+                }
+        }
+    }
+}
+
+/* Orbital occupancies of one density (csource/QCOnePDM.c:256-275 FermiOccupancies, :280-345
+ * FromDiagonalGuess, :505-570 Occupancies, :572-599 OccupancyEnergy).                               */
+typedef struct {
+    int type, nOccupied, nOrbitals;
+    double factor, charge, broadening, eocc, *occ;
+} Occupancy;
+
+static int occupancy_init(Occupancy *o, int type, double factor, double charge, int nHOO, int nLUO, int N, double broadening)
+{
+    memset(o, 0, sizeof(*o));
+    o->type = type; o->factor = factor; o->charge = charge; o->broadening = broadening; o->nOrbitals = N;
+    o->occ = (double *)calloc((size_t)N, sizeof(double));
+    int nOcc = (int)lround(ceil(charge / factor)), nCard = 0, nFrac = 0;
+    double frac = 0.0;
+    int ok = 1;
+    if (type == 0) { ok = fabs((double)nOcc * factor - charge) < 1.0e-10; nCard = nOcc; }
+    else if (type == 1) {
+        nCard = nOcc - nHOO; nFrac = nHOO + nLUO; nOcc = nCard + nFrac;
+        frac = (charge / factor - (double)nCard) / (double)(nFrac > 1 ? nFrac : 1);
+        ok = nHOO > 0 && nLUO >= 0 && nCard >= 0 && nCard + nFrac <= N && frac >= 0.0 && frac <= 1.0;
+    }
+    if (!ok || charge < 0.0) return 0;
+    if (type != 2) {
+        o->nOccupied = nOcc;
+        for (int i = 0; i < nCard; i++) o->occ[i] = factor;
+        for (int i = 0; i < nFrac; i++) o->occ[nCard + i] = frac * factor;
+    }
+    return 1;
+}
+
+static double fermi_occupancies(Occupancy *o, const double *w, double ef)
+{
+    double q = 0.0;
+    for (int i = 0; i < o->nOrbitals; i++) {
+        double e = -o->broadening * (ef - w[i]);
+        o->occ[i] = (e > 500.0) ? 0.0 : (e < -500.0 ? 1.0 : 1.0 / (1.0 + exp(e)));
+        q += o->occ[i];
+    }
+    return q;
+}
+
+static void occupancy_update(Occupancy *o, const double *w)
+{
+    o->eocc = 0.0;
+    if (o->type != 2) return;
+    double target = o->charge / o->factor;
+    o->nOccupied = 0;
+    for (int i = 0; i < o->nOrbitals; i++) o->occ[i] = 0.0;
+    if (!(target > 0.0)) return;
+    double lo = -1000.0, hi = 1000.0, fm = 0.0;
+    fermi_occupancies(o, w, lo);
+    fermi_occupancies(o, w, hi);
+    double dx = hi - lo;
+    for (int it = 0; it < 500; it++) {   /* bisection as the reference's (the upper bound is never moved) */
+        dx *= 0.5;
+        double ef = lo + dx;
+        fm = fermi_occupancies(o, w, ef) - target;
+        if (fm <= 0.0) lo = ef;
+        if (fabs(fm) <= 1.0e-12) break;
+    }
+    double e = 0.0;
+    for (int i = 0; i < o->nOrbitals; i++) {
+        double p = o->occ[i], q = 1.0 - p;
+        if (p > 1.0e-10) {
+            o->nOccupied++;
+            e += p * log(p);
+            if (q > 1.0e-10) e += q * log(q);
+        }
+    }
+    o->eocc = e / o->broadening;
+    if (o->factor != 1.0) { o->eocc *= o->factor; for (int i = 0; i < o->nOrbitals; i++) o->occ[i] *= o->factor; }
+}
+
+/* Density from a Fock matrix with the occupancies (QCOnePDM_MakeFromFock, QCOnePDM.c:403-460 and
+ * QCOnePDM_Make :369-400): P = sum over the first nOccupied orbitals of occ_i c_i c_i^T; returns the
+ * RMS change as density_from_fock does.                                                             */
+static double density_from_fock_occ(int N, Occupancy *o, const double *F, double *P, double *work)
+{
+    memcpy(work, F, sizeof(double) * N * N);
+    double *w = (double *)malloc(sizeof(double) * N);
+    eigen(N, work, w);
+    occupancy_update(o, w);
+    double rms = 0.0;
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j <= i; j++) {
+            double v = 0.0;
+            for (int k = 0; k < o->nOccupied; k++) v += o->occ[k] * work[i * N + k] * work[j * N + k];
+            double d = v - P[i * N + j];
+            rms += (i == j) ? d * d : 2.0 * d * d;
+            P[i * N + j] = P[j * N + i] = v;
+        }
+    free(w);
+    return sqrt(rms) / (double)N;
+}
+
+/* DIIS / ODA over one or two density sets (DIISSCFConverger.c:385-528 with densityq, :530-650,
+ * :661-760): B entries summed over the sets, the largest error doubled for two sets, every set
+ * extrapolated or mixed with the same coefficients.                                                  */
+typedef struct {
+    int n, ndiis, matnum, matind[16], nsets;
+    double *xP[2][16], *xF[2][16], *err[2][16], b[16][16];
+    double *rP[2], *rF[2];
+} DIIS2;
+
+static double diis2_save(DIIS2 *d, int N, double *const *P, double *const *F, double *work)
+{
+    int newest;
+    if (d->matnum < d->ndiis) { d->matnum++; newest = d->matind[d->matnum - 1]; }
+    else {
+        d->matnum = d->ndiis; newest = d->matind[0];
+        for (int i = 0; i < d->ndiis - 1; i++) d->matind[i] = d->matind[i + 1];
+        d->matind[d->ndiis - 1] = newest;
+    }
+    double emax = 0.0;
+    int ne = N * (N - 1) / 2;
+    for (int s = 0; s < d->nsets; s++) {
+        memcpy(d->xP[s][newest], P[s], sizeof(double) * N * N);
+        memcpy(d->xF[s][newest], F[s], sizeof(double) * N * N);
+        for (int i = 0; i < N; i++)
+            for (int j = 0; j < N; j++) { double t = 0; for (int k = 0; k < N; k++) t += F[s][i * N + k] * P[s][k * N + j]; work[i * N + j] = t; }
+        double *e = d->err[s][newest];
+        int t = 0;
+        for (int i = 0; i < N; i++)
+            for (int j = 0; j < i; j++, t++) { e[t] = work[i * N + j] - work[j * N + i]; if (fabs(e[t]) > emax) emax = fabs(e[t]); }
+        for (int m = 0; m < d->matnum; m++) {
+            int n = d->matind[m];
+            double x = 0.0;
+            for (int k = 0; k < ne; k++) x += d->err[s][n][k] * e[k];
+            double f = 2.0 * x;
+            if (s == 0) { d->b[n][newest] = f; if (n != newest) d->b[newest][n] = f; }
+            else { d->b[n][newest] += f; if (n != newest) d->b[newest][n] += f; }
+        }
+    }
+    return d->nsets == 2 ? 2.0 * emax : emax;
+}
+
+static void diis2_iterate(DIIS2 *d, int N, double **P, double **F)
+{
+    if (d->matnum <= 1) return;
+    double A[144], b[12];
+    while (1) {
+        int m = d->matnum, n = m + 1;
+        for (int i = 0; i < n * n; i++) A[i] = 0.0;
+        for (int i = 0; i < m; i++)
+            for (int j = 0; j < m; j++) A[i * n + j] = d->b[d->matind[i]][d->matind[j]];
+        for (int i = 0; i < m; i++) { A[m * n + i] = -1.0; A[i * n + m] = -1.0; }
+        for (int i = 0; i < n; i++) b[i] = 0.0;
+        b[m] = -1.0;
+        int bad = solve_small(n, A, b);
+        b[m] = -1.0;
+        double dev = 0.0; for (int i = 0; i < n; i++) dev += b[i];
+        if (!bad && fabs(dev) < 1.0e-6) break;
+        d->matnum--;
+        for (int i = 0; i < d->matnum; i++) d->matind[i] = d->matind[i + 1];
+        for (int i = d->matnum; i < d->ndiis; i++) {
+            d->matind[i] = d->matind[i - 1] + 1;
+            if (d->matind[i] >= d->ndiis) d->matind[i] -= d->ndiis;
+        }
+        if (d->matnum <= 1) return;
+    }
+    for (int s = 0; s < d->nsets; s++) {
+        memset(P[s], 0, sizeof(double) * N * N); memset(F[s], 0, sizeof(double) * N * N);
+        for (int m = 0; m < d->matnum; m++) {
+            int n = d->matind[m];
+            for (int k = 0; k < N * N; k++) { P[s][k] += b[m] * d->xP[s][n][k]; F[s][k] += b[m] * d->xF[s][n][k]; }
+        }
+    }
+}
+
+static void rca2_iterate(DIIS2 *d, int N, double **P, double **F, double eold, double *energy)
+{
+    double a = 0.0, c = 0.0;
+    for (int s = 0; s < d->nsets; s++) {
+        a += trace2(N, F[s], P[s]) - trace2(N, F[s], d->rP[s]);
+        c += trace2(N, d->rF[s], P[s]) - trace2(N, d->rF[s], d->rP[s]);
+    }
+    double dd = eold;
+    a += c + 2.0 * (dd - *energy);
+    double b = *energy - a - c - dd;
+    double fmin = *energy, mubmin = 1.0, mu;
+    if (eold < *energy) { fmin = eold; mubmin = 0.0; }
+    if (a == 0.0) {
+        if (b == 0.0) mu = mubmin;
+        else { double mut = -c / (2.0 * b); mu = (b > 0.0 && mut > 0.0 && mut < 1.0) ? mut : mubmin; }
+    } else {
+        double fac = b * b - 3.0 * a * c;
+        if (fac >= 0.0) {
+            double m1 = (-b + sqrt(fac)) / (3.0 * a), m2 = (-b - sqrt(fac)) / (3.0 * a);
+            if (m1 > 0.0 && m1 < 1.0) { double f = ((a * m1 + b) * m1 + c) * m1 + dd; if (f < fmin) { fmin = f; mubmin = m1; } }
+            if (m2 > 0.0 && m2 < 1.0) { double f = ((a * m2 + b) * m2 + c) * m2 + dd; if (f < fmin) { fmin = f; mubmin = m2; } }
+        }
+        mu = mubmin;
+    }
+    if (mu < 0.01) mu = 0.01;
+    double nu = 1.0 - mu;
+    for (int s = 0; s < d->nsets; s++)
+        for (int k = 0; k < N * N; k++) { P[s][k] = mu * P[s][k] + nu * d->rP[s][k]; F[s][k] = mu * F[s][k] + nu * d->rF[s][k]; }
+    *energy = ((a * mu + b) * mu + c) * mu + dd;
+}
+
+/* The QC energy and gradients of an open-shell or fractional-occupancy state (QC only), as the reference
+ * computes it (QCModelMNDO_Fock, QCModelMNDO.c: eelectronic = eocc + eoei + etei summed over the density
+ * sets).  alphaCharge / betaCharge: QCModel.CrossCheckModelAndState (pMolecule.QCModel.pyx:99-118);
+ * nFractional: (HOOs, LUOs, alpha HOOs, alpha LUOs, beta HOOs, beta LUOs).  energies as oracle_energy
+ * (eocc in [5]); densityA / densityB (packed): total density when restricted (densityB untouched),
+ * else alpha and beta.                                                                               */
+int oracle_energy_open(const OracleHamiltonian *h, int nAtoms, const int *elementIndex, const double *xyz,
+                       double alphaCharge, double betaCharge, int restricted, int occupancyType, const int *nFractional,
+                       double fermiBroadening, const OracleSCFOptions *o, double *energies, double *grad,
+                       double *densityA, double *densityB, int *ncycles)
+{
+    if (!h || nAtoms <= 0 || !o || !nFractional || occupancyType < 0 || occupancyType > 2) return 4;
+    Config c;
+    config_init(&c, h, nAtoms, elementIndex, xyz);
+    integrals(&c);
+    int N = c.nBasis, ns = restricted ? 1 : 2;
+    Occupancy occ[2];
+    memset(occ, 0, sizeof(occ));
+    int ok = restricted ? occupancy_init(&occ[0], occupancyType, 2.0, alphaCharge + betaCharge, nFractional[0], nFractional[1], N, fermiBroadening)
+                        : occupancy_init(&occ[0], occupancyType, 1.0, alphaCharge, nFractional[2], nFractional[3], N, fermiBroadening) &&
+                          occupancy_init(&occ[1], occupancyType, 1.0, betaCharge, nFractional[4], nFractional[5], N, fermiBroadening);
+    if (!ok) { for (int s = 0; s < ns; s++) free(occ[s].occ); config_free(&c); return 4; }
+    double *P[2] = {NULL, NULL}, *F[2] = {NULL, NULL}, *G = (double *)calloc((size_t)N * N, sizeof(double));
+    double *Pt = (double *)calloc((size_t)N * N, sizeof(double)), *Ps = (double *)calloc((size_t)N * N, sizeof(double));
+    double *work = (double *)calloc((size_t)N * N, sizeof(double));
+    for (int s = 0; s < ns; s++) {
+        P[s] = (double *)calloc((size_t)N * N, sizeof(double)); F[s] = (double *)calloc((size_t)N * N, sizeof(double));
+        for (int i = 0; i < N; i++) P[s][i * N + i] = occ[s].charge / (double)N;   /* diagonal guess (QCOnePDM.c:330) */
+    }
+    DIIS2 d; memset(&d, 0, sizeof(d));
+    d.ndiis = o->history; d.nsets = ns;
+    for (int i = 0; i < d.ndiis; i++) {
+        d.matind[i] = i;
+        for (int s = 0; s < ns; s++) {
+            d.xP[s][i] = (double *)calloc((size_t)N * N, sizeof(double));
+            d.xF[s][i] = (double *)calloc((size_t)N * N, sizeof(double));
+            d.err[s][i] = (double *)calloc((size_t)N * (N - 1) / 2 + 1, sizeof(double));
+        }
+    }
+    for (int s = 0; s < ns; s++) { d.rP[s] = (double *)calloc((size_t)N * N, sizeof(double)); d.rF[s] = (double *)calloc((size_t)N * N, sizeof(double)); }
+    int iteration = 0, converged = 0, qdiis = 0, qrca = o->useRCA ? 1 : 0, valid = 0;
+    double eold = 0.0, deltaeold = 0.0, rms = 0.0, eqc = 0.0, eoei = 0.0, etei = 0.0, eocc = 0.0;
+    while (iteration < o->maximumSCFCycles && !converged) {
+        /* Fock matrices and energies (QCModelMNDO_Fock) */
+        for (int k = 0; k < N * N; k++) Pt[k] = restricted ? P[0][k] : P[0][k] + P[1][k];
+        eoei = etei = 0.0;
+        eocc = occ[0].eocc + (ns == 2 ? occ[1].eocc : 0.0);
+        for (int s = 0; s < ns; s++) {
+            if (restricted) for (int k = 0; k < N * N; k++) Ps[k] = 0.5 * P[0][k];
+            fock_g_spin(&c, Pt, restricted ? Ps : P[s], G);
+            eoei += trace2(N, P[s], c.H);
+            etei += 0.5 * trace2(N, P[s], G);
+            for (int k = 0; k < N * N; k++) F[s][k] = G[k] + c.H[k];
+        }
+        eqc = eocc + eoei + etei;
+        double eel = eqc;
+        converged = (iteration > 0) && (rms <= o->densityTolerance) && (deltaeold <= o->energyTolerance);
+        if (converged) break;
+        double deltae = eel - eold, etemp = eel;
+        if (valid) {
+            double maxerr = (N > 1) ? diis2_save(&d, N, P, F, work) : 0.0;
+            if (iteration > 0) {
+                if (o->useRCA) {
+                    if (qdiis && maxerr > 0.8) { qdiis = 0; qrca = 1; }
+                    else if (iteration > 1 && qrca && maxerr < o->diisOnset) { qdiis = 1; qrca = 0; }
+                }
+                if (qdiis && N > 1) diis2_iterate(&d, N, P, F);
+                else if (o->useRCA && qrca) rca2_iterate(&d, N, P, F, eold, &etemp);
+            }
+            if (o->useRCA)
+                for (int s = 0; s < ns; s++) { memcpy(d.rP[s], P[s], sizeof(double) * N * N); memcpy(d.rF[s], F[s], sizeof(double) * N * N); }
+            iteration++;
+        }
+        deltaeold = deltae; eold = etemp;
+        rms = 0.0;
+        for (int s = 0; s < ns; s++) { double r = density_from_fock_occ(N, &occ[s], F[s], P[s], work); if (r > rms) rms = r; }
+        valid = 1;
+    }
+    if (ncycles) *ncycles = iteration;
+    energies[0] = eqc; energies[1] = eqc; energies[2] = c.enuc;
+    double base = 0.0; for (int i = 0; i < nAtoms; i++) base += c.el[i]->eheat - c.el[i]->eisol;
+    energies[3] = base; energies[4] = 0.0; energies[5] = eocc; energies[6] = eoei; energies[7] = etei;
+    if (grad && converged) {
+        for (int k = 0; k < N * N; k++) { Pt[k] = restricted ? P[0][k] : P[0][k] + P[1][k]; Ps[k] = restricted ? 0.0 : P[0][k] - P[1][k]; }
+        gradients(&c, Pt, restricted ? NULL : Ps, grad);
+    }
+    for (int s = 0; s < ns; s++) {
+        double *out = s == 0 ? densityA : densityB;
+        if (out) for (int i = 0; i < N; i++) for (int j = 0; j <= i; j++) out[PK(i, j)] = P[s][i * N + j];
+    }
+    for (int i = 0; i < d.ndiis; i++) for (int s = 0; s < ns; s++) { free(d.xP[s][i]); free(d.xF[s][i]); free(d.err[s][i]); }
+    for (int s = 0; s < ns; s++) { free(d.rP[s]); free(d.rF[s]); free(P[s]); free(F[s]); free(occ[s].occ); }
+    free(G); free(Pt); free(Ps); free(work);
     config_free(&c);
     return converged ? 0 : 1;
 }
@@ -1154,7 +1515,7 @@ int oracle_gradients(const OracleHamiltonian *h, int nAtoms, const int *elementI
     int N = c.nBasis;
     double *P = (double *)malloc(sizeof(double) * N * N);
     for (int i = 0; i < N; i++) for (int j = 0; j <= i; j++) P[i * N + j] = P[j * N + i] = density[PK(i, j)];
-    gradients(&c, P, g);
+    gradients(&c, P, NULL, g);
     free(P); config_free(&c);
     return 0;
 }

@@ -41,6 +41,8 @@ def lib():
         L.oracle_element_derived.argtypes = [P, I, pd]
         L.oracle_energy.argtypes = [P, I, pi, pd, I, P, ctypes.POINTER(_Options), pd, I, pd, P, P,
                                     ctypes.POINTER(I), P]
+        L.oracle_energy_open.argtypes = [P, I, pi, pd, D, D, I, I, pi, D, ctypes.POINTER(_Options), pd, P, pd, P,
+                                         ctypes.POINTER(I)]
         L.oracle_fock.argtypes = [P, I, pi, pd, P, pd, pd, pd]
         L.oracle_gradients.argtypes = [P, I, pi, pd, pd, pd]
         L.oracle_abfs_knots.argtypes = [D, D, D, I, I, pd, pd]
@@ -149,3 +151,42 @@ def qcmm(model, qcxyz, mmxyz, mmq, qcq=None, knots=None, inner=8.0, outer=12.0):
     lib().oracle_qcmm(1 if model == "abfs" else 0, inner, outer, 0 if x is None else len(x), _ptr(x), _ptr(y),
                       n, qcxyz, m, mmxyz, mmq, _ptr(qq), phi, _ptr(gq), _ptr(gm))
     return phi, (None if gq is None else gq.reshape(n, 3)), (None if gm is None else gm.reshape(m, 3))
+
+
+OCCUPANCY_TYPES = {"Cardinal": 0, "Fixed Fractional": 1, "Variable Fractional": 2}
+
+
+def energy_open(ham, atomic_numbers, xyz_angstrom, charge=0, multiplicity=1, isSpinRestricted=True, occupancyType="Cardinal",
+                numberFractional=(1, 0, 1, 0, 1, 0), fermiBroadening=1.0e3, densityTolerance=1.0e-8, maximumSCFCycles=500,
+                history=10, diisOnset=0.2, energyTolerance=2.0e-4, useRCA=True, gradients=True):
+    """Open-shell / fractional-occupancy QC energy (pMolecule.QCModelMNDO keywords isSpinRestricted, occupancyType),
+    alpha and beta charges as QCModel.CrossCheckModelAndState (pMolecule.QCModel.pyx:91-140) forms them."""
+    Z = [int(z) for z in atomic_numbers]
+    idx = np.array([ham.elements.index(z) for z in Z], dtype=np.int32)
+    n = len(Z)
+    norb = {z: int(o) for z, o in zip(ham.elements, ham._keep[1])}
+    nb = sum(norb[z] for z in Z)
+    ne = float(sum(int(round(ham.derived(z)["zcore"])) for z in Z)) - float(charge)
+    a, b = (ne + (multiplicity - 1.0)) / 2.0, (ne - (multiplicity - 1.0)) / 2.0
+    if occupancyType == "Cardinal" and isSpinRestricted and multiplicity > 1:
+        raise ValueError("A spin-unrestricted calculation is required for non-singlet states with cardinal occupancy.")
+    if occupancyType != "Cardinal" and isSpinRestricted and multiplicity > 1:
+        raise ValueError("A spin-unrestricted calculation is required for non-singlet states with fractional occupancy.")
+    opts = _Options(densityTolerance, diisOnset, energyTolerance, maximumSCFCycles, history, int(useRCA))
+    en = np.zeros(8); g = np.zeros(3 * n) if gradients else None
+    PA, PB = np.zeros(nb * (nb + 1) // 2), np.zeros(nb * (nb + 1) // 2)
+    nc = ctypes.c_int(0)
+    rc = lib().oracle_energy_open(ham.handle, n, idx, np.ascontiguousarray(xyz_angstrom, dtype=np.float64).ravel(), a, b,
+                                  int(bool(isSpinRestricted)), OCCUPANCY_TYPES[occupancyType],
+                                  np.ascontiguousarray(numberFractional, dtype=np.int32), fermiBroadening, ctypes.byref(opts), en,
+                                  _ptr(g), PA, _ptr(PB), ctypes.byref(nc))
+    if rc == 4:
+        raise ValueError("invalid occupancy settings")
+    out = {"eelectronic": en[1], "enuclear": en[2], "baseline": en[3], "eocc": en[5], "eoei": en[6], "etei": en[7],
+           "pure_qc_kj": 2625.5 * (en[1] + en[2] + en[3]), "gradients": None if g is None else g.reshape(n, 3),
+           "ncycles": nc.value, "converged": rc == 0}
+    if isSpinRestricted:
+        out["density"] = PA
+    else:
+        out["density_alpha"], out["density_beta"], out["density"] = PA, PB, PA + PB
+    return out
