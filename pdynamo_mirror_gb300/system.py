@@ -114,9 +114,16 @@ class System:
         return [i for i in range(len(self.atomicNumbers)) if i not in qc]
 
     def engine(self):
-        if self._engine is None:
+        """The device engine of the QC region, rebuilt when the electronic state's charge changes."""
+        if self.electronicState.multiplicity != 1:
+            raise ValueError("Only singlet (closed-shell) states are on this path.")
+        charge = int(self.electronicState.charge)
+        if self._engine is None or getattr(self, "_engine_charge", None) != charge:
             qcZ = [self.atomicNumbers[i] for i in self.qcSelection]
-            self._engine = QCEngine(self.qcModel.mndoModel, qcZ, self.electronicState.charge)
+            self._engine = QCEngine(self.qcModel.mndoModel, qcZ, charge)
+            self._engine_charge = charge
+            self._sel_key = None
+            self._mm = None
         return self._engine
 
     def _selections(self):

@@ -74,3 +74,27 @@ def test_library_exports_every_declared_symbol():
     for name in declared:
         assert hasattr(lib, name), name
     assert lib.pdg_version() == 100
+
+
+def test_system_engine_follows_the_electronic_state(monkeypatch):
+    """The device engine is rebuilt when the charge changes and non-singlet states are refused (host logic; the
+    engine itself is replaced by a stand-in, as it needs a GPU)."""
+    import pdynamo_mirror_gb300.system as S
+    made = []
+
+    class Stand:
+        def __init__(self, hamiltonian, atomic_numbers, charge):
+            made.append(charge)
+            self.device = "cpu"
+
+    monkeypatch.setattr(S, "QCEngine", Stand)
+    s = S.System([8, 1, 1], [[0.0, 0.0, 0.0], [0.96, 0.0, 0.0], [-0.24, 0.93, 0.0]])
+    s.DefineQCModel(QCModelMNDO("am1"))
+    e1 = s.engine()
+    assert s.engine() is e1
+    s.electronicState.charge = 2
+    e2 = s.engine()
+    assert e2 is not e1 and made == [0, 2]
+    s.electronicState.multiplicity = 3
+    with pytest.raises(ValueError):
+        s.engine()
