@@ -91,6 +91,9 @@ class LangevinDynamics:
         mm = system.mm_indices()
         if any(i not in fixed for i in mm):
             raise ValueError("MM atoms must be fixed (System.DefineFixedAtoms): there is no MM force field on this path.")
+        if getattr(system, "mmModel", None) is not None:
+            raise ValueError("The dynamics driver does not include the MM model's LJ terms yet: remove the MM model "
+                             "(System.DefineMMModel(None)) to run QC/MM electrostatics only.")
         self.system = system
         self.eng = eng = system.engine()
         self.dev = eng.device

@@ -83,6 +83,12 @@ def test_dynamics_requires_fixed_mm_atoms():
         LangevinDynamics(s)
     with pytest.raises(ValueError):
         s.DefineFixedAtoms([len(allZ)])
+    # an MM model's LJ terms are not in the dynamics driver: refused rather than left out
+    from pdynamo_mirror_gb300 import MMModel
+    s.DefineFixedAtoms(range(len(Z), len(allZ)))
+    s.DefineMMModel(MMModel.TIP3PWater(allZ, allX))
+    with pytest.raises(ValueError, match="LJ"):
+        LangevinDynamics(s)
 
 
 def test_oracle_velocity_assignment_hits_the_temperature():
