@@ -1402,8 +1402,8 @@ static void rca2_iterate(DIIS2 *d, int N, double **P, double **F, double eold, d
  * else alpha and beta.                                                                               */
 int oracle_energy_open(const OracleHamiltonian *h, int nAtoms, const int *elementIndex, const double *xyz,
                        double alphaCharge, double betaCharge, int restricted, int occupancyType, const int *nFractional,
-                       double fermiBroadening, const OracleSCFOptions *o, double *energies, double *grad,
-                       double *densityA, double *densityB, int *ncycles)
+                       double fermiBroadening, const double *phi, const OracleSCFOptions *o, double *energies, double *grad,
+                       double *charges, double *densityA, double *densityB, int *ncycles)
 {
     if (!h || nAtoms <= 0 || !o || !nFractional || occupancyType < 0 || occupancyType > 2) return 4;
     Config c;
@@ -1435,7 +1435,7 @@ int oracle_energy_open(const OracleHamiltonian *h, int nAtoms, const int *elemen
     }
     for (int s = 0; s < ns; s++) { d.rP[s] = (double *)calloc((size_t)N * N, sizeof(double)); d.rF[s] = (double *)calloc((size_t)N * N, sizeof(double)); }
     int iteration = 0, converged = 0, qdiis = 0, qrca = o->useRCA ? 1 : 0, valid = 0;
-    double eold = 0.0, deltaeold = 0.0, rms = 0.0, eqc = 0.0, eoei = 0.0, etei = 0.0, eocc = 0.0;
+    double eold = 0.0, deltaeold = 0.0, rms = 0.0, eqc = 0.0, eoei = 0.0, etei = 0.0, eocc = 0.0, eqcmm = 0.0;
     while (iteration < o->maximumSCFCycles && !converged) {
         /* Fock matrices and energies (QCModelMNDO_Fock) */
         for (int k = 0; k < N * N; k++) Pt[k] = restricted ? P[0][k] : P[0][k] + P[1][k];
@@ -1449,7 +1449,14 @@ int oracle_energy_open(const OracleHamiltonian *h, int nAtoms, const int *elemen
             for (int k = 0; k < N * N; k++) F[s][k] = G[k] + c.H[k];
         }
         eqc = eocc + eoei + etei;
-        double eel = eqc;
+        /* QC/MM: Lowdin charges of the total density, -phi on the diagonal of every spin's Fock matrix
+           (QCModelMNDO_QCMMFockLowdin, QCModelMNDO.c) */
+        eqcmm = 0.0;
+        if (phi) {
+            eqcmm = qcmm_fock(&c, phi, Pt, F[0], charges);
+            if (ns == 2) qcmm_fock(&c, phi, Pt, F[1], NULL);
+        }
+        double eel = eqc + eqcmm;
         converged = (iteration > 0) && (rms <= o->densityTolerance) && (deltaeold <= o->energyTolerance);
         if (converged) break;
         double deltae = eel - eold, etemp = eel;
@@ -1473,9 +1480,9 @@ int oracle_energy_open(const OracleHamiltonian *h, int nAtoms, const int *elemen
         valid = 1;
     }
     if (ncycles) *ncycles = iteration;
-    energies[0] = eqc; energies[1] = eqc; energies[2] = c.enuc;
+    energies[0] = eqc + eqcmm; energies[1] = eqc; energies[2] = c.enuc;
     double base = 0.0; for (int i = 0; i < nAtoms; i++) base += c.el[i]->eheat - c.el[i]->eisol;
-    energies[3] = base; energies[4] = 0.0; energies[5] = eocc; energies[6] = eoei; energies[7] = etei;
+    energies[3] = base; energies[4] = eqcmm; energies[5] = eocc; energies[6] = eoei; energies[7] = etei;
     if (grad && converged) {
         for (int k = 0; k < N * N; k++) { Pt[k] = restricted ? P[0][k] : P[0][k] + P[1][k]; Ps[k] = restricted ? 0.0 : P[0][k] - P[1][k]; }
         gradients(&c, Pt, restricted ? NULL : Ps, grad);

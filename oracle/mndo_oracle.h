@@ -54,11 +54,12 @@ int oracle_energy(const OracleHamiltonian *h, int nAtoms, const int *elementInde
 /* Fock matrix (packed) and energies [total electronic, electronic, nuclear] for a given density, no SCF. */
 /* Open-shell and fractional-occupancy states (QC only): restricted (total density) or unrestricted (alpha, beta)
  * densities, occupancyType 0 cardinal, 1 fixed fractional, 2 variable fractional (Fermi), nFractional = (HOOs,
- * LUOs, alpha HOOs, alpha LUOs, beta HOOs, beta LUOs).  energies[5] = occupancy energy. */
+ * LUOs, alpha HOOs, alpha LUOs, beta HOOs, beta LUOs).  energies[5] = occupancy energy.  phi (nullable): QC/MM
+ * potentials at the QC atoms (a.u.), charges (nullable): the Lowdin charges of the last Fock build. */
 int oracle_energy_open(const OracleHamiltonian *h, int nAtoms, const int *elementIndex, const double *xyz,
                        double alphaCharge, double betaCharge, int restricted, int occupancyType, const int *nFractional,
-                       double fermiBroadening, const OracleSCFOptions *o, double *energies, double *grad,
-                       double *densityA, double *densityB, int *ncycles);
+                       double fermiBroadening, const double *phi, const OracleSCFOptions *o, double *energies, double *grad,
+                       double *charges, double *densityA, double *densityB, int *ncycles);
 int oracle_fock(const OracleHamiltonian *h, int nAtoms, const int *elementIndex, const double *xyz,
                 const double *phi, const double *density, double *fock, double *energies);
 

@@ -41,7 +41,7 @@ def lib():
         L.oracle_element_derived.argtypes = [P, I, pd]
         L.oracle_energy.argtypes = [P, I, pi, pd, I, P, ctypes.POINTER(_Options), pd, I, pd, P, P,
                                     ctypes.POINTER(I), P]
-        L.oracle_energy_open.argtypes = [P, I, pi, pd, D, D, I, I, pi, D, ctypes.POINTER(_Options), pd, P, pd, P,
+        L.oracle_energy_open.argtypes = [P, I, pi, pd, D, D, I, I, pi, D, P, ctypes.POINTER(_Options), pd, P, P, pd, P,
                                          ctypes.POINTER(I)]
         L.oracle_fock.argtypes = [P, I, pi, pd, P, pd, pd, pd]
         L.oracle_gradients.argtypes = [P, I, pi, pd, pd, pd]
@@ -158,7 +158,7 @@ OCCUPANCY_TYPES = {"Cardinal": 0, "Fixed Fractional": 1, "Variable Fractional": 
 
 def energy_open(ham, atomic_numbers, xyz_angstrom, charge=0, multiplicity=1, isSpinRestricted=True, occupancyType="Cardinal",
                 numberFractional=(1, 0, 1, 0, 1, 0), fermiBroadening=1.0e3, densityTolerance=1.0e-8, maximumSCFCycles=500,
-                history=10, diisOnset=0.2, energyTolerance=2.0e-4, useRCA=True, gradients=True):
+                history=10, diisOnset=0.2, energyTolerance=2.0e-4, useRCA=True, gradients=True, phi=None):
     """Open-shell / fractional-occupancy QC energy (pMolecule.QCModelMNDO keywords isSpinRestricted, occupancyType),
     alpha and beta charges as QCModel.CrossCheckModelAndState (pMolecule.QCModel.pyx:91-140) forms them."""
     Z = [int(z) for z in atomic_numbers]
@@ -176,13 +176,16 @@ def energy_open(ham, atomic_numbers, xyz_angstrom, charge=0, multiplicity=1, isS
     en = np.zeros(8); g = np.zeros(3 * n) if gradients else None
     PA, PB = np.zeros(nb * (nb + 1) // 2), np.zeros(nb * (nb + 1) // 2)
     nc = ctypes.c_int(0)
+    ph = None if phi is None else np.ascontiguousarray(phi, dtype=np.float64)
+    q = np.zeros(n)
     rc = lib().oracle_energy_open(ham.handle, n, idx, np.ascontiguousarray(xyz_angstrom, dtype=np.float64).ravel(), a, b,
                                   int(bool(isSpinRestricted)), OCCUPANCY_TYPES[occupancyType],
-                                  np.ascontiguousarray(numberFractional, dtype=np.int32), fermiBroadening, ctypes.byref(opts), en,
-                                  _ptr(g), PA, _ptr(PB), ctypes.byref(nc))
+                                  np.ascontiguousarray(numberFractional, dtype=np.int32), fermiBroadening, _ptr(ph),
+                                  ctypes.byref(opts), en, _ptr(g), _ptr(q), PA, _ptr(PB), ctypes.byref(nc))
     if rc == 4:
         raise ValueError("invalid occupancy settings")
-    out = {"eelectronic": en[1], "enuclear": en[2], "baseline": en[3], "eocc": en[5], "eoei": en[6], "etei": en[7],
+    out = {"total_electronic": en[0], "eelectronic": en[1], "enuclear": en[2], "baseline": en[3], "eqcmm": en[4],
+           "eocc": en[5], "eoei": en[6], "etei": en[7], "charges": q,
            "pure_qc_kj": 2625.5 * (en[1] + en[2] + en[3]), "gradients": None if g is None else g.reshape(n, 3),
            "ncycles": nc.value, "converged": rc == 0}
     if isSpinRestricted:

@@ -347,10 +347,10 @@ void *ref_system_create ( void *vh, const int nAtoms, const int *elementIndex, c
 !  . 1 fixed fractional, 2 variable fractional), numberFractional*, fermiBroadening). */
 void *ref_system_create_open ( void *vh, const int nAtoms, const int *elementIndex, const double alphaCharge, const double betaCharge,
                                const int isSpinRestricted, const int occupancyType, const int *nFractional, const double fermiBroadening,
-                               const double densityTolerance, const int maximumSCFCycles, const int history,
+                               const int withQCMM, const double densityTolerance, const int maximumSCFCycles, const int history,
                                const double diisOnset, const double energyTolerance, const int useRCA )
 {
-    return MakeSystem ( ( RefHamiltonian * ) vh, nAtoms, elementIndex, 0, densityTolerance, maximumSCFCycles, history,
+    return MakeSystem ( ( RefHamiltonian * ) vh, nAtoms, elementIndex, withQCMM, densityTolerance, maximumSCFCycles, history,
                         diisOnset, energyTolerance, useRCA, 1, alphaCharge, betaCharge, isSpinRestricted, occupancyType,
                         nFractional, fermiBroadening, 0 ) ;
 }

@@ -50,7 +50,7 @@ def lib():
         L.ref_abfs_spline.argtypes = [P, I, pd, pd, pd]
         L.ref_abfs_qcmm.argtypes = [P, P, pd, I, pd, pd, pd, pd, pd, pd]
         L.ref_system_create_open.restype = P
-        L.ref_system_create_open.argtypes = [P, I, pi, D, D, I, I, pi, D, D, I, I, D, D, I]
+        L.ref_system_create_open.argtypes = [P, I, pi, D, D, I, I, pi, D, I, D, I, I, D, D, I]
         L.ref_system_get_densities.argtypes = [P, pd, P]
         L.ref_mmmm_energy.argtypes = [I, pd, pd, pi, pi, I, pd, pd, pd, pd, I, I, pi, I, pi, D, D, D, D, D, D, pd, pd]
         _lib = L
@@ -115,8 +115,6 @@ class RefSystem:
             self.handle = lib().ref_system_create(ham.handle, self.n, idx, int(charge), int(qcmm), densityTolerance,
                                                   maximumSCFCycles, history, diisOnset, energyTolerance, int(useRCA))
         else:
-            if qcmm:
-                raise ValueError("open-shell reference systems are QC only here")
             ne = float(sum(ham.nuclear_charge(z) for z in self.atomic_numbers)) - float(charge)
             a, b = (ne + (multiplicity - 1.0)) / 2.0, (ne - (multiplicity - 1.0)) / 2.0
             if occupancyType == "Cardinal":
@@ -128,7 +126,7 @@ class RefSystem:
                 raise ValueError("A spin-unrestricted calculation is required for non-singlet states with fractional occupancy.")
             nf = np.ascontiguousarray(numberFractional, dtype=np.int32)
             self.handle = lib().ref_system_create_open(ham.handle, self.n, idx, a, b, int(bool(isSpinRestricted)),
-                                                       self.OCCUPANCY_TYPES[occupancyType], nf, fermiBroadening, densityTolerance,
+                                                       self.OCCUPANCY_TYPES[occupancyType], nf, fermiBroadening, int(qcmm), densityTolerance,
                                                        maximumSCFCycles, history, diisOnset, energyTolerance, int(useRCA))
             self.restricted = bool(isSpinRestricted)
         self.nbasis = lib().ref_system_nbasis(self.handle)

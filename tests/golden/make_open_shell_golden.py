@@ -2,7 +2,8 @@
 radical test set (pMolecule-1.9.0/tests/QCTestSystems.py:34-56, as pMolecule-1.9.0/tests/MNDOUHFEnergies.py runs it:
 converger densityTolerance 1e-8, maximumSCFCycles 500) for every restricted / unrestricted and occupancy-type
 combination listed there, computed by the reference's compiled C core (oracle/ref_shim.c: ref_system_create_open).
-Spin densities (alpha and beta, packed) are kept for the two small radicals.
+Spin densities (alpha and beta, packed) are kept for the two small radicals.  QC/MM cases: the three open-shell
+systems in the field of seeded point charges (their potentials at the QC atoms stored with the case).
 
 Run where the reference tree and the compiled reference core exist (``make -C oracle ref``):
 
@@ -53,6 +54,30 @@ def main(root):
             out["cases"].append(case)
             print(label, "restricted" if restricted else "unrestricted", occ, case["converged"], case["ncycles"],
                   "%.6f" % case["pure_qc_kj"])
+    # QC/MM: the radicals in the field of seeded point charges (potentials at the QC atoms in atomic units, the
+    # form the reference's QC model receives them, QCMMInteractionState.qcmmPotentials)
+    out["qcmm_cases"] = []
+    rng = np.random.default_rng(17)
+    bohr = 1.0e-10 / 5.291772083e-11
+    for label, name, sub, charge, mult in SYSTEMS[1:]:
+        Z, X = read_xyz(os.path.join(root, "pMolecule-1.9.0", "data", sub, name + ".xyz"))
+        X = np.array(X)
+        centre = X.mean(0)
+        d = rng.normal(size=(8, 3))
+        sites = centre + 5.0 * d / np.linalg.norm(d, axis=1)[:, None]
+        q = rng.uniform(-0.8, 0.8, size=8)
+        phi = [float(sum(qm / (np.linalg.norm(x - m) * bohr) for qm, m in zip(q, sites))) for x in X]
+        ham = R.RefHamiltonian("am1", Z)
+        occ = "Variable Fractional" if label == "Tyrosine Dipeptide Triplet" else "Cardinal"
+        s = R.RefSystem(ham, Z, charge=charge, qcmm=True, multiplicity=mult, isSpinRestricted=False, occupancyType=occ,
+                        densityTolerance=1.0e-8, maximumSCFCycles=500)
+        r = s.energy(X, phi=np.array(phi))
+        out["qcmm_cases"].append({"label": label, "atomic_numbers": Z, "xyz": X.tolist(), "charge": charge,
+                                  "multiplicity": mult, "isSpinRestricted": False, "occupancyType": occ, "phi": phi,
+                                  "converged": bool(r["converged"]), "ncycles": int(r["ncycles"]),
+                                  "total_electronic": float(r["total_electronic"]), "eqcmm": float(r["eqcmm"]),
+                                  "charges": r["charges"].tolist(), "gradients_hartree_per_bohr": r["gradients"].tolist()})
+        print("QC/MM", label, occ, r["converged"], r["ncycles"], "%.10f" % r["total_electronic"])
     json.dump(out, open(os.path.join(HERE, "open_shell_reference.json"), "w"), indent=0)
 
 

@@ -139,3 +139,17 @@ def test_open_shell_occupancy_checks():
         O.energy_open(ham, c["atomic_numbers"], c["xyz"], 0, 3, True, "Cardinal")
     with pytest.raises(ValueError):
         O.energy_open(ham, c["atomic_numbers"], c["xyz"], 0, 3, False, "Fixed Fractional", numberFractional=(1, 0, 0, 0, 1, 0))
+
+
+@pytest.mark.parametrize("case", _OPEN["qcmm_cases"], ids=[c["label"].replace(" ", "") for c in _OPEN["qcmm_cases"]])
+def test_open_shell_qcmm_oracle_matches_reference(case):
+    """Open-shell states embedded in point-charge potentials (QCModelMNDO_QCMMFockLowdin on both spins' Fock
+    matrices, Lowdin charges of the total density) against the reference core."""
+    ham = O.Hamiltonian("am1", case["atomic_numbers"])
+    r = O.energy_open(ham, case["atomic_numbers"], case["xyz"], case["charge"], case["multiplicity"], case["isSpinRestricted"],
+                      case["occupancyType"], phi=case["phi"])
+    assert r["converged"] and case["converged"] and abs(r["ncycles"] - case["ncycles"]) <= 20
+    assert abs(r["total_electronic"] - case["total_electronic"]) < 1e-6
+    assert abs(r["eqcmm"] - case["eqcmm"]) < 1e-6
+    np.testing.assert_allclose(r["charges"], case["charges"], rtol=0, atol=1e-6)
+    np.testing.assert_allclose(r["gradients"], case["gradients_hartree_per_bohr"], rtol=0, atol=1e-5)
