@@ -37,6 +37,9 @@ typedef struct {
     double po[9], ddp[6], dd, qq, am, ad, aq, alp, zcore, eheat, eisol, gss, gsp, gpp, gp2, hsp, hpp, gphot, pcore;
     double beta[4], uspd[4], fn1[4], fn2[4], fn3[4], pddgc[4], pddge[4], zetas, zetap;
     double exps[2][ORACLE_MAXPRIM], ccbf[2][ORACLE_MAXPRIM];
+    int ndiat;                                   /* PM6 diatomic core-core pairs, indexed by partner atomic number */
+    unsigned char diat_flag[ORACLE_MAXDIATOMIC];
+    double diat_a[ORACLE_MAXDIATOMIC], diat_x[ORACLE_MAXDIATOMIC];
 } Element;
 
 struct OracleHamiltonian { int n; Element *el; };
@@ -136,7 +139,8 @@ OracleHamiltonian *oracle_hamiltonian_create(int nElements, const int *atomicNum
                                              const double *raw, const int *nGaussians, const double *gaussians,
                                              const int *nPDDG, const double *pddg, const int *nShells,
                                              const int *shellTypes, const int *nPrimitives,
-                                             const double *exponents, const double *coefficients)
+                                             const double *exponents, const double *coefficients,
+                                             const int *nDiatomic, const double *diatomic)
 {
     OracleHamiltonian *h = (OracleHamiltonian *)calloc(1, sizeof(OracleHamiltonian));
     h->n = nElements;
@@ -166,6 +170,15 @@ OracleHamiltonian *oracle_hamiltonian_create(int nElements, const int *atomicNum
         for (int i = 0; i < e->npddg; i++) {
             const double *g = pddg + (k * ORACLE_MAXPDDG + i) * 2;
             e->pddgc[i] = g[0] / HARTREES_TO_EV; e->pddge[i] = g[1] / BOHRS_TO_ANGSTROMS;
+        }
+        /* PM6 diatomic pairs (pMolecule.MNDOParameters.pyx:259-276, units :358-363: a in bohr^-1 x 0.529..) */
+        e->ndiat = 0;
+        for (int i = 0; i < nDiatomic[k]; i++) {
+            const double *d = diatomic + (k * ORACLE_MAXDIATOMIC + i) * 3;
+            int j = (int)d[0];
+            if (j < 0 || j >= ORACLE_MAXDIATOMIC) continue;
+            e->diat_flag[j] = 1; e->diat_x[j] = d[1]; e->diat_a[j] = d[2] * BOHRS_TO_ANGSTROMS;
+            if (j + 1 > e->ndiat) e->ndiat = j + 1;
         }
         fill_ddp_po(e);
         e->nshell = nShells[k];
@@ -206,10 +219,68 @@ int oracle_element_derived(const OracleHamiltonian *h, int k, double *out)
 /* ================================================================================================ */
 /* Core-core repulsion and its r-derivative, non-diatomic branch: csource/MNDOIntegralUtilities.c:35-150
  * (CoreCore) and :152-281 (CoreCoreD).  The diatomic (PM6) branch is outside this path.           */
+/* PM6 diatomic core-core term and its r-derivative (csource/MNDOIntegralUtilities.c:45-96 energy, :164-218
+ * derivative): scale = 1 + x_ij exp(-a_ij r_A^2)-type pair terms (X-H with X = C, N, O) or
+ * x_ij exp(-a_ij r (1 + 0.0003 r_A^5)), the C-C and Si-O extra terms, times Z_a Z_b gamma, plus the
+ * unpolarisable core 1e-8 eV A^12 ((Z_a^1/3 + Z_b^1/3) / r_A)^12.                                   */
+#define PM6_UNPOLARIZABLE_CORE (1.0e-08 / 27.21)
+static double core_core_pm6(const Element *a, const Element *b, double r, double gam, double dgdr, double *scale_rest, double *dedr)
+{
+    double scale = 1.0, dscale = 0.0, rA = r * BOHRS_TO_ANGSTROMS;
+    if (b->Z < a->ndiat && a->diat_flag[b->Z]) {
+        double aij = a->diat_a[b->Z], xij = 2.0 * a->diat_x[b->Z];   /* factor 2 as the reference (Stewart's AM1/d) */
+        int xh = (a->Z == 1 && (b->Z == 6 || b->Z == 7 || b->Z == 8)) || (b->Z == 1 && (a->Z == 6 || a->Z == 7 || a->Z == 8));
+        if (xh) {
+            double f3 = xij * exp(-aij * r * r * BOHRS_TO_ANGSTROMS);
+            dscale -= 2.0 * aij * r * BOHRS_TO_ANGSTROMS * f3;
+            scale += f3;
+        } else {
+            double dd = 0.0003 * pow(rA, 5), f3 = xij * exp(-aij * r * (1.0 + dd));
+            dscale -= aij * (1.0 + 6.0 * dd) * f3;
+            scale += f3;
+        }
+    }
+    if (a->Z == 6 && b->Z == 6) {
+        double f3 = 9.28 * exp(-5.98 * rA);
+        dscale -= 5.98 * BOHRS_TO_ANGSTROMS * f3;
+        scale += f3;
+    }
+    if ((a->Z == 8 && b->Z == 14) || (a->Z == 14 && b->Z == 8)) {
+        double dd = rA - 2.9, f3 = -0.0007 * exp(-dd * dd);
+        dscale -= 2.0 * dd * BOHRS_TO_ANGSTROMS * f3;
+        scale += f3;
+    }
+    double zz = a->zcore * b->zcore;
+    double u = (pow(a->zcore, 1.0 / 3.0) + pow(b->zcore, 1.0 / 3.0)) / rA, u12 = pow(u, 12);
+    double enuc = zz * gam * scale + PM6_UNPOLARIZABLE_CORE * u12;
+    *dedr = zz * (dgdr * scale + gam * dscale) - 12.0 * PM6_UNPOLARIZABLE_CORE * u12 / r;
+    *scale_rest = 0.0;
+    return enuc;
+}
+
 static double core_core(const Element *a, const Element *b, double r, double *dedr)
 {
     double s8 = a->po[8] + b->po[8];
     double gam = 1.0 / sqrt(r * r + s8 * s8), dgdr = -r * gam * gam * gam;
+    if (a->ndiat > 0 && b->ndiat > 0) {
+        /* PM6: the diatomic term, then the AM1/PM3 Gaussian terms as for the other Hamiltonians */
+        double scale, de, enuc = core_core_pm6(a, b, r, gam, dgdr, &scale, &de);
+        double zz = a->zcore * b->zcore, an = 0.0;
+        const Element *e2[2] = { a, b };
+        for (int t = 0; t < 2; t++) {
+            const Element *e = e2[t];
+            for (int i = 0; i < e->ng; i++) {
+                double d = r - e->fn3[i], ax = e->fn2[i] * d * d;
+                if (ax <= EXPONENT_TOLERANCE) {
+                    scale += a->gphot * b->gphot * zz / r * e->fn1[i] * exp(-ax);
+                    an += e->fn1[i] * (1.0 / (r * r) + e->fn2[i] * 2.0 * d / r) * exp(-ax);
+                }
+            }
+        }
+        de -= an * a->gphot * b->gphot * zz;
+        if (dedr) *dedr = de;
+        return enuc + scale;
+    }
     double exi = exp(-a->alp * r), exj = exp(-b->alp * r);
     double scale = exi + exj;
     int nt = a->Z + b->Z;

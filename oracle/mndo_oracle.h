@@ -16,6 +16,7 @@
 #define ORACLE_MAXGAUSS 4
 #define ORACLE_MAXPDDG  4
 #define ORACLE_MAXPRIM  6
+#define ORACLE_MAXDIATOMIC 100   /* PM6 diatomic pairs per element, by partner atomic number */
 
 typedef struct {
     double densityTolerance;   /* DIISSCFConverger.c:27 default 1e-8 */
@@ -33,7 +34,8 @@ OracleHamiltonian *oracle_hamiltonian_create(int nElements, const int *atomicNum
                                              const double *raw, const int *nGaussians, const double *gaussians,
                                              const int *nPDDG, const double *pddg, const int *nShells,
                                              const int *shellTypes, const int *nPrimitives,
-                                             const double *exponents, const double *coefficients);
+                                             const double *exponents, const double *coefficients,
+                                             const int *nDiatomic, const double *diatomic);
 void oracle_hamiltonian_free(OracleHamiltonian *h);
 
 /* Derived per-element parameters, same layout as ref_element_derived in ref_shim.c. */

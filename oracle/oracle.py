@@ -36,7 +36,7 @@ def lib():
         pd = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
         pi = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
         L.oracle_hamiltonian_create.restype = P
-        L.oracle_hamiltonian_create.argtypes = [I, pi, pi, pd, pi, pd, pi, pd, pi, pi, pi, pd, pd]
+        L.oracle_hamiltonian_create.argtypes = [I, pi, pi, pd, pi, pd, pi, pd, pi, pi, pi, pd, pd, pi, pd]
         L.oracle_hamiltonian_free.argtypes = [P]
         L.oracle_element_derived.argtypes = [P, I, pd]
         L.oracle_energy.argtypes = [P, I, pi, pd, I, P, ctypes.POINTER(_Options), pd, I, pd, P, P,

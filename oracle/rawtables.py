@@ -17,6 +17,7 @@ RAW_FIELDS = ("iii", "iiid", "ir016", "ir066", "ir244", "ir266", "ir466", "qnd",
               "gpp", "gp2", "gsp", "gss", "g2sd", "hsp", "pcore", "qq", "udd", "upp", "uss", "zcore",
               "zetad", "zetap", "zetas", "zdn", "zpn", "zsn")
 MAXGAUSS, MAXPDDG, MAXPRIM = 4, 4, 6
+MAXDIATOMIC = 100   # PM6 diatomic core-core pairs per element (partner atomic numbers < 100)
 SHELL_TYPE = {"S": 0, "P": 1}
 _TABLE = None
 
@@ -29,7 +30,9 @@ def table():
 
 
 def raw_arrays(hamiltonian, elements):
-    """Arrays (Z, norb, raw, ng, gauss, npddg, pddg, nshell, stype, nprim, exps, coefs) for sorted elements."""
+    """Arrays (Z, norb, raw, ng, gauss, npddg, pddg, nshell, stype, nprim, exps, coefs, ndiatomic, diatomic) for
+    sorted elements; diatomic rows are (partner atomic number, coefficient x, exponent a in A^-1) as the PM6
+    files list them."""
     t = table()
     ne = len(elements)
     Z = np.array(elements, dtype=np.int32)
@@ -38,6 +41,7 @@ def raw_arrays(hamiltonian, elements):
     npd = np.zeros(ne, np.int32); pddg = np.zeros((ne, MAXPDDG, 2))
     nsh = np.zeros(ne, np.int32); stype = np.zeros((ne, 2), np.int32); nprim = np.zeros((ne, 2), np.int32)
     exps = np.zeros((ne, 2, MAXPRIM)); coefs = np.zeros((ne, 2, MAXPRIM))
+    nd = np.zeros(ne, np.int32); diat = np.zeros((ne, MAXDIATOMIC, 3))
     for e, z in enumerate(elements):
         el = t["hamiltonians"][hamiltonian][str(z)]
         norb[e] = el["orbitals"]
@@ -45,6 +49,8 @@ def raw_arrays(hamiltonian, elements):
         ng[e] = len(el["gaussians"]); npd[e] = len(el["pddg"])
         for i, g in enumerate(el["gaussians"]): gauss[e, i] = g
         for i, g in enumerate(el["pddg"]): pddg[e, i] = g
+        nd[e] = len(el.get("diatomic", []))
+        for i, g in enumerate(el.get("diatomic", [])): diat[e, i] = g
         lab = ("%ds" % el["qns"] if el["qns"] else "") + ("%dp" % el["qnp"] if el["qnp"] else "")
         shells = t["bases"][lab][: (1 if el["orbitals"] == 1 else 2)]
         nsh[e] = len(shells)
@@ -52,4 +58,4 @@ def raw_arrays(hamiltonian, elements):
             stype[e, s] = SHELL_TYPE[sh["type"]]; nprim[e, s] = len(sh["exponents"])
             exps[e, s, :nprim[e, s]] = sh["exponents"]; coefs[e, s, :nprim[e, s]] = sh["coefficients"]
     return (Z, norb, raw.ravel().copy(), ng, gauss.ravel().copy(), npd, pddg.ravel().copy(), nsh,
-            stype.ravel().copy(), nprim.ravel().copy(), exps.ravel().copy(), coefs.ravel().copy())
+            stype.ravel().copy(), nprim.ravel().copy(), exps.ravel().copy(), coefs.ravel().copy(), nd, diat.ravel().copy())

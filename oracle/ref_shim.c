@@ -63,6 +63,7 @@ enum { R_III, R_IIID, R_IR016, R_IR066, R_IR244, R_IR266, R_IR466, R_QND, R_QNP,
 # define MAXGAUSS 4
 # define MAXPDDG  4
 # define MAXPRIM  6
+# define MAXDIATOMIC 100
 
 typedef struct {
     int          nElements ;
@@ -84,7 +85,8 @@ typedef struct {
 
 /* . Unit conversion of one element, pMolecule.MNDOParameters.pyx:212-275 and 309-370. */
 static MNDOParameters *MakeElement ( const int atomicNumber, const int norbitals, const double *raw,
-                                     const int nGaussians, const double *gaussians, const int nPDDG, const double *pddg )
+                                     const int nGaussians, const double *gaussians, const int nPDDG, const double *pddg,
+                                     const int nDiatomic, const double *diatomic )
 {
     int i ;
     MNDOParameters *p = MNDOParameters_Allocate ( ) ;
@@ -120,6 +122,25 @@ static MNDOParameters *MakeElement ( const int atomicNumber, const int norbitals
         p->pddgc0 = ( Real * ) calloc ( nPDDG, sizeof ( Real ) ) ;
         p->pddge0 = ( Real * ) calloc ( nPDDG, sizeof ( Real ) ) ;
         for ( i = 0 ; i < nPDDG ; i++ ) { p->pddgc0[i] = pddg[2*i] ; p->pddge0[i] = pddg[2*i+1] ; }
+    }
+    /* . FillDiatomic (pMolecule.MNDOParameters.pyx:259-276): rows (partner atomic number, x, a), indexed by the
+         partner's atomic number up to the largest one. */
+    if ( nDiatomic > 0 )
+    {
+        int maxZ = 0 ;
+        for ( i = 0 ; i < nDiatomic ; i++ ) if ( ( int ) diatomic[3*i] > maxZ ) maxZ = ( int ) diatomic[3*i] ;
+        p->QDIATOMIC      = True ;
+        p->ndiatomic      = maxZ + 1 ;
+        p->QDIATOMICFLAGS = ( Boolean * ) calloc ( p->ndiatomic, sizeof ( Boolean ) ) ;
+        p->diatomica0     = ( Real    * ) calloc ( p->ndiatomic, sizeof ( Real    ) ) ;
+        p->diatomicx0     = ( Real    * ) calloc ( p->ndiatomic, sizeof ( Real    ) ) ;
+        for ( i = 0 ; i < nDiatomic ; i++ )
+        {
+            int j = ( int ) diatomic[3*i] ;
+            p->QDIATOMICFLAGS[j] = True ;
+            p->diatomicx0[j] = diatomic[3*i+1] ;
+            p->diatomica0[j] = diatomic[3*i+2] ;
+        }
     }
     /* . ToAtomicUnits. */
     p->ad    = p->ad0 ;
@@ -169,6 +190,12 @@ static MNDOParameters *MakeElement ( const int atomicNumber, const int norbitals
         p->pddge = ( Real * ) calloc ( p->npddg, sizeof ( Real ) ) ;
         for ( i = 0 ; i < p->npddg ; i++ ) { p->pddgc[i] = p->pddgc0[i] / HARTREES_TO_EV ; p->pddge[i] = p->pddge0[i] / BOHRS_TO_ANGSTROMS ; }
     }
+    if ( p->ndiatomic > 0 )   /* . pMolecule.MNDOParameters.pyx:358-363 */
+    {
+        p->diatomica = ( Real * ) calloc ( p->ndiatomic, sizeof ( Real ) ) ;
+        p->diatomicx = ( Real * ) calloc ( p->ndiatomic, sizeof ( Real ) ) ;
+        for ( i = 0 ; i < p->ndiatomic ; i++ ) { p->diatomica[i] = p->diatomica0[i] * BOHRS_TO_ANGSTROMS ; p->diatomicx[i] = p->diatomicx0[i] ; }
+    }
     MNDOParameters_CalculateOneCenterTEIs ( p ) ;
     return p ;
 }
@@ -201,7 +228,7 @@ static GaussianBasis *MakeBasis ( const int atomicNumber, const int nShells, con
 void *ref_hamiltonian_create ( const int nElements, const int *atomicNumbers, const int *norbitals, const double *raw,
                                const int *nGaussians, const double *gaussians, const int *nPDDG, const double *pddg,
                                const int *nShells, const int *shellTypes, const int *nPrimitives,
-                               const double *exponents, const double *coefficients )
+                               const double *exponents, const double *coefficients, const int *nDiatomic, const double *diatomic )
 {
     int e ;
     RefHamiltonian *h = ( RefHamiltonian * ) calloc ( 1, sizeof ( RefHamiltonian ) ) ;
@@ -212,7 +239,8 @@ void *ref_hamiltonian_create ( const int nElements, const int *atomicNumbers, co
     {
         MNDOParameters *p ;
         h->atomicNumbers[e] = atomicNumbers[e] ;
-        p = MakeElement ( atomicNumbers[e], norbitals[e], raw + e*NRAW, nGaussians[e], gaussians + e*MAXGAUSS*3, nPDDG[e], pddg + e*MAXPDDG*2 ) ;
+        p = MakeElement ( atomicNumbers[e], norbitals[e], raw + e*NRAW, nGaussians[e], gaussians + e*MAXGAUSS*3, nPDDG[e], pddg + e*MAXPDDG*2,
+                          nDiatomic[e], diatomic + e*MAXDIATOMIC*3 ) ;
         h->parameters->centers[e].atomicNumber   = atomicNumbers[e] ;
         h->parameters->centers[e].mndoparameters = p ;
         h->parameters->centers[e].orbitalbasis   = MakeBasis ( atomicNumbers[e], nShells[e], shellTypes + 2*e, nPrimitives + 2*e,

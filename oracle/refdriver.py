@@ -33,7 +33,7 @@ def lib():
         pd = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
         pi = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
         L.ref_hamiltonian_create.restype = P
-        L.ref_hamiltonian_create.argtypes = [I, pi, pi, pd, pi, pd, pi, pd, pi, pi, pi, pd, pd]
+        L.ref_hamiltonian_create.argtypes = [I, pi, pi, pd, pi, pd, pi, pd, pi, pi, pi, pd, pd, pi, pd]
         L.ref_element_derived.argtypes = [P, I, pd]
         L.ref_element_basis.argtypes = [P, I, pd, pd]
         L.ref_system_create.restype = P

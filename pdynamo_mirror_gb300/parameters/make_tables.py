@@ -13,6 +13,9 @@ Usage: python make_tables.py <pDynamo root> [output.json]
 import json, os, re, sys
 
 HAMILTONIANS = ("am1", "mndo", "pm3", "pddgmndo", "pddgpm3", "rm1")
+# tabulated as well (the checkers use them; the product's Hamiltonians are the list above): PM6 with its
+# diatomic core-core parameters, elements with s and p orbitals only
+TABLE_HAMILTONIANS = HAMILTONIANS + ("pm6",)
 SYMBOLS = ("H He Li Be B C N O F Ne Na Mg Al Si P S Cl Ar K Ca Sc Ti V Cr Mn Fe Co Ni Cu Zn Ga Ge As Se Br Kr "
            "Rb Sr Y Zr Nb Mo Tc Ru Rh Pd Ag Cd In Sn Sb Te I Xe Cs Ba La Ce Pr Nd Pm Sm Eu Gd Tb Dy Ho Er Tm "
            "Yb Lu Hf Ta W Re Os Ir Pt Au Hg Tl Pb Bi").split()
@@ -46,7 +49,7 @@ def read_element(path):
     out["gaussians"] = tables.get("gaussians", [])
     out["pddg"] = tables.get("pddg", [])
     if tables.get("diatomic"):
-        raise ValueError("diatomic core-core parameters are not supported: " + path)
+        out["diatomic"] = tables["diatomic"]   # [partner atomic number, coefficient, exponent (A^-1)], PM6
     return out
 
 
@@ -87,11 +90,13 @@ def main(root, output):
     base = os.path.join(root, "parameters", "mndoParameters")
     data = {"source": "pDynamo-1.9.0 parameters/mndoParameters", "hamiltonians": {}, "bases": {}}
     labels = set()
-    for h in HAMILTONIANS:
+    for h in TABLE_HAMILTONIANS:
         table = {}
         for fname in sorted(os.listdir(os.path.join(base, h))):
             if not fname.endswith(".yaml"): continue
             el = read_element(os.path.join(base, h, fname))
+            if "diatomic" in el and h not in ("pm6",):
+                raise ValueError("diatomic core-core parameters outside PM6: " + fname)
             if el["orbitals"] not in (1, 4):
                 continue  # d-orbital elements belong to the PM6 path
             table[str(el["atomicNumber"])] = el

@@ -153,3 +153,21 @@ def test_open_shell_qcmm_oracle_matches_reference(case):
     assert abs(r["eqcmm"] - case["eqcmm"]) < 1e-6
     np.testing.assert_allclose(r["charges"], case["charges"], rtol=0, atol=1e-6)
     np.testing.assert_allclose(r["gradients"], case["gradients_hartree_per_bohr"], rtol=0, atol=1e-5)
+
+
+_PM6 = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pm6_reference.json")))
+
+
+def test_pm6_oracle_matches_reference():
+    """PM6 for elements with s and p orbitals (the diatomic core-core term, MNDOIntegralUtilities.c:35-230) against
+    the reference core on the reference's closed-shell test molecules: energies and gradients."""
+    hams = {}
+    for name, m in sorted(_PM6["molecules"].items()):
+        key = tuple(sorted(set(m["Z"])))
+        if key not in hams:
+            hams[key] = O.Hamiltonian("pm6", m["Z"])
+        r = O.System(hams[key], m["Z"], m["charge"], maximumSCFCycles=500).energy(np.array(m["xyz"]))
+        assert r["converged"] and m["converged"], name
+        assert abs(r["pure_qc_kj"] - m["pure_qc_kj"]) < 1e-6 * 2625.5, name
+        np.testing.assert_allclose(r["gradients"], m["gradients_hartree_per_bohr"], rtol=0, atol=1e-5, err_msg=name)
+        assert abs(r["ncycles"] - m["ncycles"]) <= 10, name
