@@ -6,6 +6,8 @@ Only the closed-shell, spin-restricted, cardinal-occupancy case is on this path;
 spin options raise ValueError, as unknown options do in the reference.
 """
 
+import numpy as np
+
 from .converger import DIISSCFConverger
 from .parameters import HAMILTONIANS, available_elements
 
@@ -43,6 +45,20 @@ class QCModelMNDO:
             self.converger = DIISSCFConverger()
         if self.label is None:
             self.label = self.mndoModel.upper()
+
+    def IsSpinRestricted(self):
+        """The states on this path are closed-shell RHF (pMolecule.QCModel.pyx:298)."""
+        return True
+
+    def AtomicCharges(self, configuration, chargeModel=None, spinDensities=False):
+        """Lowdin charges of the QC atoms from the last energy on configuration (QCModelMNDO.AtomicCharges; the
+        NDDO basis is orthonormal, so Mulliken charges are the same); zeros for spin densities (closed shell)."""
+        if chargeModel not in (None, "Lowdin", "Mulliken"):
+            raise ValueError("Unknown QC charge model: " + str(chargeModel) + ".")
+        q = getattr(configuration, "qcCharges", None)
+        if q is None:
+            return None
+        return np.zeros(len(q)) if spinDensities else np.array(q, dtype=np.float64)
 
     def CheckElements(self, atomic_numbers):
         have = set(available_elements(self.mndoModel))

@@ -28,6 +28,7 @@ class Configuration:
         self.energyTerms = {}
         self.gradients3 = None
         self.qcState = None
+        self.qcCharges = None   # Lowdin charges of the QC atoms after Energy
 
 
 class SCFNotConverged(ValueError):
@@ -187,6 +188,8 @@ class System:
         if mmi is not None:
             Emm, Gmm = mmi.run(X, gradients=doGradients)
             small = torch.cat([small, Emm], 1)
+        nq = r["charges"].shape[1]
+        small = torch.cat([small, r["charges"]], 1)   # Lowdin charges of the QC atoms (QCModelMNDO_LowdinCharges)
         G = None
         if doGradients:
             qs, ms, _, _ = self._selections()
@@ -207,6 +210,7 @@ class System:
             G = Gh.numpy()
         E = small[:, :_native.NENERGY]
         st = small[:, _native.NENERGY].astype(np.int32)
+        self.qcChargesBatch = small[:, small.shape[1] - nq:].copy()
         pure = HARTREES_TO_KJ * (E[:, _native.EN_ELECTRONIC] + E[:, _native.EN_NUCLEAR] + E[:, _native.EN_BASELINE])
         qcmm = HARTREES_TO_KJ * E[:, _native.EN_QCMM]
         terms = {"Pure QC": pure, "QC/MM Elect.": qcmm, "SCF Cycles": small[:, _native.NENERGY + 1].astype(np.int32), "Status": st}
@@ -215,7 +219,7 @@ class System:
             raise SCFNotConverged("SCF procedure not converged.")
         total = pure + (qcmm if mm is not None else 0.0)
         if mmi is not None:
-            Emm = small[:, _native.NENERGY + 2:]
+            Emm = small[:, _native.NENERGY + 2:_native.NENERGY + 2 + len(_native.MM_TERMS)]
             for k, name in enumerate(_native.MM_TERMS):
                 if name in mmi.term_names():
                     terms[name] = Emm[:, k]
@@ -229,4 +233,24 @@ class System:
         if self.nbModel is None or not self.mm_indices():
             self.configuration.energyTerms.pop("QC/MM Elect.", None)
         self.configuration.gradients3 = None if G is None else G[0]
+        self.configuration.qcCharges = self.qcChargesBatch[0].copy()
         return float(total[0])
+
+    def AtomicCharges(self, qcChargeModel=None, qcAtomsOnly=False, spinDensities=False):
+        """Partial charges of the atoms after Energy (System.py:96-113): the MM point charges with the QC model's
+        Lowdin charges added at the QC atoms, or the QC atoms' charges alone (qcAtomsOnly, or no MM charges).
+        The closed-shell states here have no spin density, so spinDensities gives zeros.  Mulliken charges
+        equal Lowdin ones in the NDDO basis, which is orthonormal."""
+        if qcChargeModel not in (None, "Lowdin", "Mulliken"):
+            raise ValueError("Unknown QC charge model: " + str(qcChargeModel) + ".")
+        if self.qcModel is None:
+            return None
+        q = getattr(self.configuration, "qcCharges", None)
+        if q is None:
+            raise ValueError("No QC density: calculate an energy first.")
+        q = np.zeros_like(q) if spinDensities else np.array(q, dtype=np.float64)
+        if qcAtomsOnly or self.mmCharges is None:
+            return q
+        charges = np.zeros(len(self.atomicNumbers)) if spinDensities else np.array(self.mmCharges, dtype=np.float64)
+        charges[self.qcSelection] += q
+        return charges

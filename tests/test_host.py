@@ -98,3 +98,25 @@ def test_system_engine_follows_the_electronic_state(monkeypatch):
     s.electronicState.multiplicity = 3
     with pytest.raises(ValueError):
         s.engine()
+
+
+def test_atomic_charges_assembly():
+    """System.AtomicCharges / QCModelMNDO.AtomicCharges from the charges an energy leaves on the configuration
+    (System.py:96-113): MM point charges plus the QC atoms' Lowdin charges; QC atoms only; spin densities zero."""
+    import numpy as np
+    from pdynamo_mirror_gb300 import System
+    Z = [8, 1, 1, 8, 1, 1]
+    X = np.zeros((6, 3)); X[:, 0] = np.arange(6)
+    s = System(Z, X, mmCharges=[0.0, 0.0, 0.0, -0.834, 0.417, 0.417])
+    s.DefineQCModel(QCModelMNDO("am1"), qcSelection=[0, 1, 2])
+    with pytest.raises(ValueError):
+        s.AtomicCharges()
+    q = np.array([-0.4, 0.2, 0.2])
+    s.configuration.qcCharges = q
+    np.testing.assert_allclose(s.AtomicCharges(), [-0.4, 0.2, 0.2, -0.834, 0.417, 0.417])
+    np.testing.assert_allclose(s.AtomicCharges(qcAtomsOnly=True), q)
+    np.testing.assert_allclose(s.AtomicCharges(spinDensities=True), np.zeros(6))
+    np.testing.assert_allclose(s.qcModel.AtomicCharges(s.configuration, chargeModel="Mulliken"), q)
+    assert s.qcModel.IsSpinRestricted()
+    with pytest.raises(ValueError):
+        s.AtomicCharges(qcChargeModel="CM5")
