@@ -641,7 +641,7 @@ def main():
                        "scf_cta": scf_cta_layout(eng, T),
                        "l2": "working set > L2 (no flush needed)"},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(head["frames_h"].numel() * 8),
-                    "d2h_bytes_per_step": int(head["G"].nbytes + len(frames) * (_native.NENERGY + 2) * 8)},
+                    "d2h_bytes_per_step": int(head["G"].nbytes + len(frames) * (_native.NENERGY + 2 + len(sel)) * 8)},
             "gpu_launches": 8 * args.steps,
             "roofline": roofline(head, args.method != "fp64"),
             "clocks": clk}
