@@ -2,12 +2,15 @@
 the reference's compiled C core (oracle/ref_shim.c with the PM6 diatomic core-core parameters,
 pMolecule-1.9.0/extensions/csource/MNDOIntegralUtilities.c:35-230) for the reference's closed-shell test molecules
 (tests/golden/molecules.json) whose elements all have s and p orbitals only under PM6 and that have at most 30 atoms,
-converger as pMolecule-1.9.0/tests/MNDORHFEnergies.py runs it.  The reference stores no PM6 energies, so the core
-run here is the source.
+converger as pMolecule-1.9.0/tests/MNDORHFEnergies.py runs it.  The reference stores PM6 energies only (below), so
+the gradients and cycle counts come from the core run here; its energies equal the stored ones to 1e-8 kJ/mol.
 
 Run where the reference tree and the compiled reference core exist (``make -C oracle ref``):
 
-    python tests/golden/make_pm6_golden.py
+    python tests/golden/make_pm6_golden.py /root/reference
+
+It also writes pm6_pickle.json: the reference's stored PM6 "Pure QC" energies (kJ/mol, with their tolerance) from
+pMolecule-1.9.0/data/reference/MNDORHFEnergies.pkl, read as make_golden.py reads the other Hamiltonians'.
 """
 
 import json, os, sys
@@ -18,9 +21,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "..", ".."))
 from oracle import refdriver as R  # noqa: E402
 from oracle.rawtables import table  # noqa: E402
+sys.path.insert(0, HERE)
+from make_golden import load_pickle  # noqa: E402
 
 
-def main():
+def main(root):
+    pk = load_pickle(os.path.join(root, "pMolecule-1.9.0", "data", "reference", "MNDORHFEnergies.pkl"))
+    json.dump({"pm6": pk["pm6"]}, open(os.path.join(HERE, "pm6_pickle.json"), "w"), indent=1, sort_keys=True)
     mols = json.load(open(os.path.join(HERE, "molecules.json")))
     pm6 = table()["hamiltonians"]["pm6"]
     out = {"hamiltonian": "pm6", "converger": {"densityTolerance": 1.0e-8, "maximumSCFCycles": 500}, "molecules": {}}
@@ -41,4 +48,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -171,3 +171,21 @@ def test_pm6_oracle_matches_reference():
         assert abs(r["pure_qc_kj"] - m["pure_qc_kj"]) < 1e-6 * 2625.5, name
         np.testing.assert_allclose(r["gradients"], m["gradients_hartree_per_bohr"], rtol=0, atol=1e-5, err_msg=name)
         assert abs(r["ncycles"] - m["ncycles"]) <= 10, name
+
+
+def test_pm6_oracle_matches_the_references_stored_energies():
+    """The reference's own stored PM6 "Pure QC" energies (MNDORHFEnergies.pkl, tests/golden/pm6_pickle.json) within its
+    tolerance (1 kJ/mol), for the s/p molecules of the PM6 fixture."""
+    stored = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pm6_pickle.json")))["pm6"]
+    hams = {}
+    n = 0
+    for name, m in sorted(_PM6["molecules"].items()):
+        if name not in stored:
+            continue
+        key = tuple(sorted(set(m["Z"])))
+        if key not in hams:
+            hams[key] = O.Hamiltonian("pm6", m["Z"])
+        r = O.System(hams[key], m["Z"], m["charge"], maximumSCFCycles=500).energy(np.array(m["xyz"]), gradients=False)
+        assert abs(r["pure_qc_kj"] - stored[name]["value"]) <= stored[name]["tolerance"], name
+        n += 1
+    assert n >= 40
