@@ -46,6 +46,16 @@ class QCModelMNDO:
         if self.label is None:
             self.label = self.mndoModel.upper()
 
+    def GetOption(self, optionName):
+        """An option of the model (QCModelMNDO.GetOption, pMolecule.QCModelMNDO.pyx:306-318): the occupancy options
+        of the closed-shell cardinal states on this path; AttributeError for unknown names."""
+        values = {"isSpinRestricted": True, "occupancyType": "Cardinal", "numberFractionalHOOs": 1, "numberFractionalLUOs": 0,
+                  "numberFractionalAlphaHOOs": 1, "numberFractionalAlphaLUOs": 0, "numberFractionalBetaHOOs": 1,
+                  "numberFractionalBetaLUOs": 0}
+        if optionName not in values:
+            raise AttributeError("Unknown option: " + str(optionName) + ".")
+        return values[optionName]
+
     def IsSpinRestricted(self):
         """The states on this path are closed-shell RHF (pMolecule.QCModel.pyx:298)."""
         return True

@@ -117,6 +117,8 @@ def test_atomic_charges_assembly():
     np.testing.assert_allclose(s.AtomicCharges(qcAtomsOnly=True), q)
     np.testing.assert_allclose(s.AtomicCharges(spinDensities=True), np.zeros(6))
     np.testing.assert_allclose(s.qcModel.AtomicCharges(s.configuration, chargeModel="Mulliken"), q)
-    assert s.qcModel.IsSpinRestricted()
+    assert s.qcModel.IsSpinRestricted() and s.qcModel.GetOption("occupancyType") == "Cardinal"
+    with pytest.raises(AttributeError):
+        s.qcModel.GetOption("notAnOption")
     with pytest.raises(ValueError):
         s.AtomicCharges(qcChargeModel="CM5")
