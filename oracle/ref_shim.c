@@ -33,6 +33,7 @@
 # include "RegularGrid.h"
 # include "RegularGridOccupancy.h"
 # include "Selection.h"
+# include "Vector3.h"
 # include "DIISSCFConverger.h"
 # include "DIISSCFConvergerState.h"
 # include "GaussianBasis.h"
@@ -687,5 +688,35 @@ int ref_mmmm_energy ( const int nAtoms, const double *xyz, const double *charges
     PairListGenerator_Deallocate ( &g ) ; PairwiseInteractionABFS_Deallocate ( &p ) ;
     LJParameterContainer_Deallocate ( &lj ) ; LJParameterContainer_Deallocate ( &lj14 ) ; MMAtomContainer_Deallocate ( &mm ) ;
     Coordinates3_Deallocate ( &crd ) ; Coordinates3_Deallocate ( &grd ) ;
+    return 0 ;
+}
+
+/*----------------------------------------------------------------------------------------------------------------------------------
+! . Properties of the last energy's density: the dipole moment (Debye, about the origin; QCModelMNDO_DipoleMoment) and the
+! . Mayer bond orders with the charges, free and total valences QCModelMNDO_MayerBondOrders gives (QCModelMNDO.c).
+! . bondOrders: nAtoms x nAtoms (full).
+!---------------------------------------------------------------------------------------------------------------------------------*/
+int ref_system_properties ( void *vs, double *dipole, double *bondOrders, double *charges, double *freeValence, double *totalValence )
+{
+    RefSystem *s = ( RefSystem * ) vs ;
+    int i, j, n ;
+    Vector3 *d ;
+    SymmetricMatrix *b ;
+    Real1DArray *c, *f, *t ;
+    if ( s == NULL ) return 4 ;
+    n = s->nAtoms ;
+    d = QCModelMNDO_DipoleMoment ( s->model, s->state, s->coordinates3, NULL ) ;
+    for ( i = 0 ; i < 3 ; i++ ) dipole[i] = Vector3_Item ( d, i ) ;
+    Vector3_Deallocate ( &d ) ;
+    b = SymmetricMatrix_Allocate ( n ) ;
+    c = Real1DArray_Allocate ( n, NULL ) ; f = Real1DArray_Allocate ( n, NULL ) ; t = Real1DArray_Allocate ( n, NULL ) ;
+    QCModelMNDO_MayerBondOrders ( s->model, s->state, b, c, f, t ) ;
+    for ( i = 0 ; i < n ; i++ )
+    {
+        for ( j = 0 ; j < n ; j++ ) bondOrders[i*n+j] = SymmetricMatrix_Get_Component ( b, i, j ) ;
+        charges[i] = Real1DArray_Item ( c, i ) ; freeValence[i] = Real1DArray_Item ( f, i ) ; totalValence[i] = Real1DArray_Item ( t, i ) ;
+    }
+    SymmetricMatrix_Deallocate ( &b ) ;
+    Real1DArray_Deallocate ( &c ) ; Real1DArray_Deallocate ( &f ) ; Real1DArray_Deallocate ( &t ) ;
     return 0 ;
 }

@@ -52,6 +52,7 @@ def lib():
         L.ref_system_create_open.restype = P
         L.ref_system_create_open.argtypes = [P, I, pi, D, D, I, I, pi, D, I, D, I, I, D, D, I]
         L.ref_system_get_densities.argtypes = [P, pd, P]
+        L.ref_system_properties.argtypes = [P, pd, pd, pd, pd, pd]
         L.ref_mmmm_energy.argtypes = [I, pd, pd, pi, pi, I, pd, pd, pd, pd, I, I, pi, I, pi, D, D, D, D, D, D, pd, pd]
         _lib = L
     return _lib
@@ -156,6 +157,13 @@ class RefSystem:
         if not self.restricted:
             out["density"], out["density_alpha"], out["density_beta"] = P + Q, P, Q
         return out
+
+    def properties(self):
+        """Dipole (Debye) and Mayer bond orders, charges, free and total valences of the last energy's density."""
+        n = self.n
+        d, b, c, f, t = np.zeros(3), np.zeros(n * n), np.zeros(n), np.zeros(n), np.zeros(n)
+        lib().ref_system_properties(self.handle, d, b, c, f, t)
+        return {"dipole": d, "bond_orders": b.reshape(n, n), "charges": c, "free_valence": f, "total_valence": t}
 
     def set_density(self, P):
         lib().ref_system_set_density(self.handle, np.ascontiguousarray(P, dtype=np.float64))

@@ -70,6 +70,23 @@ class QCModelMNDO:
             return None
         return np.zeros(len(q)) if spinDensities else np.array(q, dtype=np.float64)
 
+    def DipoleMoment(self, configuration, center=None):
+        """Dipole moment (Debye) of the QC atoms from the last energy's density (QCModelMNDO_DipoleMoment)."""
+        from .properties import qc_dipole
+        st = getattr(configuration, "qcState", None)
+        if st is None:
+            return None
+        return qc_dipole(st.zcore, st.norbitals, st.ddp1, st.coordinates3, st.density(), center)
+
+    def BondOrders(self, configuration, chargeModel=None):
+        """(Mayer bond orders [n, n], charges, free valences, total valences) of the last energy's density
+        (QCModelMNDO.BondOrders, QCModelMNDO_MayerBondOrders)."""
+        from .properties import mayer
+        st = getattr(configuration, "qcState", None)
+        if st is None:
+            return None
+        return mayer(st.norbitals, st.density())
+
     def CheckElements(self, atomic_numbers):
         have = set(available_elements(self.mndoModel))
         missing = sorted(set(int(z) for z in atomic_numbers) - have)

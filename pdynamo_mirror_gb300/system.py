@@ -234,7 +234,24 @@ class System:
             self.configuration.energyTerms.pop("QC/MM Elect.", None)
         self.configuration.gradients3 = None if G is None else G[0]
         self.configuration.qcCharges = self.qcChargesBatch[0].copy()
+        from .properties import QCState
+        self.configuration.qcState = QCState(self._engine.density[0].clone(), self.qcModel.mndoModel,
+                                             [self.atomicNumbers[i] for i in self.qcSelection], self.coordinates3[self.qcSelection])
         return float(total[0])
+
+    def DipoleMoment(self, center=None):
+        """Dipole moment (Debye) after Energy (System.py:260-268): the MM point charges' part plus the QC model's."""
+        from .properties import mm_dipole
+        dipole = np.zeros(3)
+        mm = self.mm_indices() if self.qcModel is not None else list(range(len(self.atomicNumbers)))
+        if self.mmCharges is not None and mm:
+            dipole = dipole + mm_dipole(self.mmCharges[mm], self.coordinates3[mm], center)
+        if self.qcModel is not None:
+            qc = self.qcModel.DipoleMoment(self.configuration, center)
+            if qc is None:
+                raise ValueError("No QC density: calculate an energy first.")
+            dipole = dipole + qc
+        return dipole
 
     def AtomicCharges(self, qcChargeModel=None, qcAtomsOnly=False, spinDensities=False):
         """Partial charges of the atoms after Energy (System.py:96-113): the MM point charges with the QC model's

@@ -1,6 +1,6 @@
-"""Atomic charges after an energy (System.AtomicCharges, QCModelMNDO.AtomicCharges): the Lowdin charges of the
-converged density on the GPU against the oracle's, QC only and with MM point charges (NBModelFull).  Tolerance
-1e-6 e (two SCFs each stopping at the 1e-8 RMS density tolerance)."""
+"""Properties after an energy on the GPU: atomic charges (System.AtomicCharges, QCModelMNDO.AtomicCharges) against the
+oracle's Lowdin charges, QC only and with MM point charges (NBModelFull), 1e-6 e; dipole moments and Mayer bond orders
+against the reference core's.  The tolerances allow for two SCFs that each stop at the 1e-8 RMS density tolerance."""
 
 import numpy as np
 import pytest
@@ -44,3 +44,27 @@ def test_qcmm_charges_match_oracle():
     np.testing.assert_allclose(q[:len(Z)], r["charges"], rtol=0, atol=1e-6)
     np.testing.assert_allclose(q[len(Z):], mmq[len(Z):])
     np.testing.assert_allclose(s.AtomicCharges(qcAtomsOnly=True), q[:len(Z)])
+
+
+def test_dipoles_and_bond_orders_match_reference():
+    """System.DipoleMoment and QCModelMNDO.BondOrders after Energy against the reference core's
+    QCModelMNDO_DipoleMoment / QCModelMNDO_MayerBondOrders (tests/golden/properties_reference.json, closed-shell
+    cases): dipoles 1e-5 Debye, bond orders and valences 1e-6."""
+    import json, os
+    from pdynamo_mirror_gb300 import QCModelMNDO, System
+    cases = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "properties_reference.json")))["cases"]
+    n = 0
+    for c in cases:
+        if not c["isSpinRestricted"]:
+            continue
+        s = System(c["Z"], np.array(c["xyz"]))
+        s.electronicState.charge = c["charge"]
+        s.DefineQCModel(QCModelMNDO(c["hamiltonian"]))
+        s.Energy()
+        np.testing.assert_allclose(s.DipoleMoment(), c["dipole_debye"], rtol=0, atol=1e-5, err_msg=c["name"])
+        B, ch, fv, tv = s.qcModel.BondOrders(s.configuration)
+        np.testing.assert_allclose(B, c["bond_orders"], rtol=0, atol=1e-6, err_msg=c["name"])
+        np.testing.assert_allclose(ch, c["mayer_charges"], rtol=0, atol=1e-6, err_msg=c["name"])
+        np.testing.assert_allclose(tv, c["total_valence"], rtol=0, atol=1e-6, err_msg=c["name"])
+        n += 1
+    assert n == 5
