@@ -3,7 +3,8 @@ radical test set (pMolecule-1.9.0/tests/QCTestSystems.py:34-56, as pMolecule-1.9
 converger densityTolerance 1e-8, maximumSCFCycles 500) for every restricted / unrestricted and occupancy-type
 combination listed there, computed by the reference's compiled C core (oracle/ref_shim.c: ref_system_create_open).
 Spin densities (alpha and beta, packed) are kept for the two small radicals.  QC/MM cases: the three open-shell
-systems in the field of seeded point charges (their potentials at the QC atoms stored with the case).
+systems in the field of seeded point charges (their potentials at the QC atoms stored with the case).  PM6 cases:
+the allyl and methylene radicals, unrestricted.
 
 Run where the reference tree and the compiled reference core exist (``make -C oracle ref``):
 
@@ -78,6 +79,17 @@ def main(root):
                                   "total_electronic": float(r["total_electronic"]), "eqcmm": float(r["eqcmm"]),
                                   "charges": r["charges"].tolist(), "gradients_hartree_per_bohr": r["gradients"].tolist()})
         print("QC/MM", label, occ, r["converged"], r["ncycles"], "%.10f" % r["total_electronic"])
+    # PM6 (diatomic core-core term) for the two small radicals, unrestricted, cardinal occupancy
+    out["pm6_cases"] = []
+    for label, name, sub, charge, mult in SYSTEMS[2:]:
+        Z, X = read_xyz(os.path.join(root, "pMolecule-1.9.0", "data", sub, name + ".xyz"))
+        s = R.RefSystem(R.RefHamiltonian("pm6", Z), Z, charge=charge, multiplicity=mult, isSpinRestricted=False,
+                        occupancyType="Cardinal", densityTolerance=1.0e-8, maximumSCFCycles=500)
+        r = s.energy(np.array(X))
+        out["pm6_cases"].append({"label": label, "atomic_numbers": Z, "xyz": X, "charge": charge, "multiplicity": mult,
+                                 "converged": bool(r["converged"]), "ncycles": int(r["ncycles"]),
+                                 "pure_qc_kj": float(r["pure_qc_kj"]), "gradients_hartree_per_bohr": r["gradients"].tolist()})
+        print("PM6", label, r["converged"], r["ncycles"], "%.6f" % r["pure_qc_kj"])
     json.dump(out, open(os.path.join(HERE, "open_shell_reference.json"), "w"), indent=0)
 
 

@@ -189,3 +189,15 @@ def test_pm6_oracle_matches_the_references_stored_energies():
         assert abs(r["pure_qc_kj"] - stored[name]["value"]) <= stored[name]["tolerance"], name
         n += 1
     assert n >= 40
+
+
+@pytest.mark.parametrize("case", _OPEN_PM6 := json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                                                       "open_shell_reference.json")))["pm6_cases"],
+                         ids=[c["label"].replace(" ", "") for c in _OPEN_PM6])
+def test_open_shell_pm6_oracle_matches_reference(case):
+    """PM6 radicals, unrestricted: the open-shell restatement with the PM6 core-core term against the reference core."""
+    r = O.energy_open(O.Hamiltonian("pm6", case["atomic_numbers"]), case["atomic_numbers"], case["xyz"], case["charge"],
+                      case["multiplicity"], False, "Cardinal")
+    assert r["converged"] and case["converged"]
+    assert abs(r["pure_qc_kj"] - case["pure_qc_kj"]) < 1e-6 * 2625.5
+    np.testing.assert_allclose(r["gradients"], case["gradients_hartree_per_bohr"], rtol=0, atol=1e-5)
