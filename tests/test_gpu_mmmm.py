@@ -129,3 +129,43 @@ def test_bench_box_properties():
     assert np.abs(G.sum(1)).max() < 1e-8 * np.abs(G).max() * len(Z)
     np.testing.assert_allclose(E[3], E[0], rtol=1e-11, atol=1e-7)
     np.testing.assert_allclose(G[3], G[0], rtol=0, atol=1e-8)
+
+
+def test_water_dimer_binding_energies():
+    """Water dimer binding energies, the check of the reference's QCMMWaterDimerBinding.py (:11-12: within [-35, 5]
+    kJ/mol), for the models on this path: QC/QC (AM1) and QC/MM (AM1 water with a TIP3P water: NBModelABFS
+    electrostatics and the MM model's QC/MM LJ; the lone MM water has no MM/MM term).  Also against the oracle."""
+    from oracle import oracle as O
+    from pdynamo_mirror_gb300 import MMModel, NBModelABFS, QCModelMNDO, System
+    m = json.load(open(os.path.join(HERE, "golden", "molecules.json")))["waterDimer_Cs"]
+    Z, X = m["Z"], np.array(m["xyz"])
+
+    def qc(Zs, Xs):
+        s = System(Zs, Xs)
+        s.DefineQCModel(QCModelMNDO("am1"))
+        return s.Energy()
+
+    e1, e2, e12 = qc(Z[:3], X[:3]), qc(Z[3:], X[3:]), qc(Z, X)
+    qcqc = e12 - e1 - e2
+    s = System(Z, X)
+    s.DefineMMModel(MMModel.TIP3PWater(Z, X))
+    s.DefineQCModel(QCModelMNDO("am1"), qcSelection=[0, 1, 2])
+    s.DefineNBModel(NBModelABFS())
+    qcmm = s.Energy() - e1
+    assert -35.0 <= qcqc <= 5.0 and -35.0 <= qcmm <= 5.0
+    # the oracle: QC energies, ABFS QC/MM potentials and the QC/MM LJ term
+    ham, kj = O.Hamiltonian("am1", [1, 8]), 2625.5
+
+    def eo(Zs, Xs, phi=None):
+        r = O.System(ham, Zs, 0).energy(Xs, phi=phi, gradients=False)
+        return kj * (r["eelectronic"] + r["enuclear"] + r["baseline"] + r["eqcmm"])
+
+    q = s.mmModel.charges[3:]
+    phi, _, _ = O.qcmm("abfs", X[:3], X[3:], q, knots=O.abfs_knots(8.0, 12.0))
+    lj = s.mmModel.ljParameters
+    flags = np.array([mmmm.FLAG_QC_LJ] * 3 + [mmmm.FLAG_MM] * 3)
+    E, _ = mmmm.energies(X, s.mmModel.charges, s.mmModel.ljTypes, flags, lj.epsilon, lj.sigma, lj.epsilon, lj.sigma, True,
+                         s.mmModel.exclusions, [])
+    o1 = eo(Z[:3], X[:3])
+    assert abs(qcqc - (eo(Z, X) - o1 - eo(Z[3:], X[3:]))) < 1e-3
+    assert abs(qcmm - (eo(Z[:3], X[:3], phi) + E.sum() - o1)) < 1e-3
