@@ -11,23 +11,55 @@ e2e    the same through System.EnergyBatch with the frames in pinned host memory
 The working set per step (~4 MB per frame, >1 GB per batch) is far larger than L2, so no flush is needed.
 
 --impl reference times the CPU restatement of pDynamo's path (oracle/liboracle.so, built from mndo_oracle.c)
-on the host cores (one frame per process, all cores) on a bounded sample of the same frames.
+on every host core this process may use: a process pool made and warmed once, each worker holding its QC region
+and ABFS spline, each timed step a bounded sample of the same frames split evenly over the workers.
 """
 
-import argparse, json, os, subprocess, sys, threading, time
+import argparse, hashlib, json, os, subprocess, sys, threading, time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
 import numpy as np
 
-# DRAM bytes (read + write) of one k_scf launch on this workload (304 frames), from the ncu captures summarised
-# in profiles/k_scf_dram_304frames.md; per launch, like `achieved` (mixed: this build; plain: an earlier build).
-K_SCF_DRAM_BYTES_304 = {"mixed": 8.59e9 + 5.12e9, "fp64": 4.85e9 + 4.10e9}
+# ncu DRAM bytes of one k_scf launch on this workload, per method, with the source hash of the kernel build they were
+# captured on; roofline.traffic is reported only when the benched build has the same hash.
+SCF_TRAFFIC_PROFILE = os.path.join(HERE, "profiles", "k_scf_dram_qcmm_water_box_304frames.txt")
+SCF_SOURCES = ("pdynamo_mirror_gb300/csrc/scf.cu", "pdynamo_mirror_gb300/csrc/common.cuh", "pdynamo_mirror_gb300/csrc/tc.cuh",
+               "pdynamo_mirror_gb300/csrc/multipole.cuh", "include/pdg.h")
 
 METRIC = "QC/MM E+grad evals/s at |dE|<1e-6 Eh (AM1 RHF, 65 QC atoms in 4000 TIP3P waters, ABFS 8/12 A)"
 UNIT = "evals/s"
 KJ = 2625.5
+
+
+def scf_build_id():
+    """Hash of the sources of the SCF kernel's translation unit (what an ncu capture of it describes)."""
+    h = hashlib.sha256()
+    for rel in SCF_SOURCES:
+        with open(os.path.join(HERE, rel), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
+def scf_traffic(method, frames):
+    """(bytes, note): ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_scf launch of `method` on `frames`
+    frames, from the profile summary, when it was captured on this build; (None, why) otherwise."""
+    try:
+        rec = {}
+        with open(SCF_TRAFFIC_PROFILE) as f:
+            for line in f:
+                if line.strip() and not line.startswith("#"):
+                    k, v = line.split(None, 1)
+                    rec[k] = v.strip()
+    except OSError:
+        return None, "no ncu DRAM capture of k_scf"
+    if rec.get("build") != scf_build_id():
+        return None, "the ncu DRAM capture of k_scf (build %s) is of another build than this one (%s)" % (rec.get("build"), scf_build_id())
+    if int(rec.get("frames", 0)) != frames or method + "_dram_read_bytes" not in rec:
+        return None, "no ncu DRAM capture of k_scf for this method and batch size"
+    return (float(rec[method + "_dram_read_bytes"]) + float(rec[method + "_dram_write_bytes"]),
+            "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, this build (%s)" % rec["build"])
 
 
 def peaks():
@@ -157,55 +189,102 @@ def scf_cta_layout(eng, T):
 
 def workload(n_frames, seed=1):
     from pdynamo_mirror_gb300 import workloads
-    Z, X, Q, sel, charge = workloads.qcmm_water_box(seed=seed)
-    frames = workloads.perturbed_frames(X, n_frames, sigma=0.02, seed=11)
-    return Z, X, Q, sel, charge, frames
+    return workloads.qcmm_water_box_frames(n_frames, seed=seed)
 
 
-def cpu_reference_sample(Z, Q, sel, charge, frames, n_sample, processes):
-    """Oracle E+grad on n_sample frames, `processes` at a time (spawned workers). Returns (seconds, n)."""
-    import multiprocessing as mp
-    ctx = mp.get_context("spawn")
-    args = [(list(Z), Q, sel, charge, frames[f]) for f in range(n_sample)]
-    t0 = time.perf_counter()
-    if processes == 1:
-        for a in args:
-            _oracle_eval(a)
-    else:
-        with ctx.Pool(processes) as pool:
-            pool.map(_oracle_eval, args)
-    return time.perf_counter() - t0, n_sample
+def host_cores():
+    """Host cores this process may run on."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
 
 
-def _oracle_eval(args):
+# ---- CPU baseline: the oracle (the plain-C restatement of the reference's path), one frame after another per process
+_CPU = {}
+
+
+def _cpu_init(Z, Q, sel, charge):
+    """Per-process state, made once: the oracle library, the QC region and the ABFS spline knots."""
     sys.path.insert(0, HERE)
     from oracle import oracle as O
-    Z, Q, sel, charge, X = args
     nq = len(sel)
-    knots = O.abfs_knots(8.0, 12.0)
-    phi, _, _ = O.qcmm("abfs", X[:nq], X[nq:], Q[nq:], knots=knots)
-    r = O.System(O.Hamiltonian("am1", Z[:nq]), Z[:nq], charge=charge).energy(X[:nq], phi=phi)
-    O.qcmm("abfs", X[:nq], X[nq:], Q[nq:], qcq=r["charges"], knots=knots)
-    return r["eelectronic"]
+    Zq = [int(z) for z in Z[:nq]]
+    _CPU.update(O=O, nq=nq, Q=np.asarray(Q, dtype=np.float64), knots=O.abfs_knots(8.0, 12.0),
+                sys=O.System(O.Hamiltonian("am1", Zq), Zq, charge=charge))
+
+
+def _cpu_frames(frames):
+    """Cold energy + gradient of each frame as System.Energy(doGradients=True) computes it: QC/MM potentials, the
+    SCF from the diagonal guess, QC gradients, QC/MM gradients.  Returns (frames done, seconds)."""
+    O, nq, Q, kn, s = _CPU["O"], _CPU["nq"], _CPU["Q"], _CPU["knots"], _CPU["sys"]
+    t0 = time.perf_counter()
+    for X in frames:
+        phi, _, _ = O.qcmm("abfs", X[:nq], X[nq:], Q[nq:], knots=kn)
+        s.density = None
+        r = s.energy(X[:nq], phi=phi)
+        O.qcmm("abfs", X[:nq], X[nq:], Q[nq:], qcq=r["charges"], knots=kn)
+    return len(frames), time.perf_counter() - t0
+
+
+class CPUBaseline:
+    """The oracle on `processes` host cores: a spawned pool made and warmed once (or this process for one core)."""
+
+    def __init__(self, Z, Q, sel, charge, processes):
+        self.processes = processes
+        self.pool = None
+        init = (list(Z), np.asarray(Q), list(sel), int(charge))
+        if processes > 1:
+            import multiprocessing as mp
+            self.pool = mp.get_context("spawn").Pool(processes, initializer=_cpu_init, initargs=init)
+        else:
+            _cpu_init(*init)
+
+    def warm(self, frames):
+        """One frame per worker, outside any timed region."""
+        self.run(np.repeat(np.asarray(frames)[:1], self.processes, axis=0))
+
+    def run(self, frames):
+        """(wall seconds, frames done, per-worker seconds) for the frames split evenly over the workers."""
+        t0 = time.perf_counter()
+        if self.pool is None:
+            done = [_cpu_frames(frames)]
+        else:
+            chunks = [c for c in np.array_split(np.asarray(frames), self.processes) if len(c)]
+            done = self.pool.map(_cpu_frames, chunks, chunksize=1)
+        return time.perf_counter() - t0, sum(d[0] for d in done), [d[1] for d in done]
+
+    def close(self):
+        if self.pool is not None:
+            self.pool.close()
+            self.pool.join()
 
 
 def run_reference(args):
-    Z, X, Q, sel, charge, frames = workload(max(args.frames, args.reference_sample))
-    cores = os.cpu_count() or 1
-    n = min(len(frames), max(cores, args.reference_sample))
-    times = []
+    Z, X, Q, sel, charge, frames = workload(args.reference_sample)
+    cores = host_cores()
+    cpu = CPUBaseline(Z, Q, sel, charge, cores)
+    cpu.warm(frames)
+    times, worker_rates = [], []
     for s in range(args.warmup + args.steps):
-        t, k = cpu_reference_sample(Z, Q, sel, charge, frames, n, cores)
+        t, n, per = cpu.run(frames)
         if s >= args.warmup:
             times.append(t)
+            worker_rates.append(n / max(1, len(per)) / (sum(per) / len(per)))
+    cpu.close()
+    n = len(frames)
     value = n / (sum(times) / len(times))
+    per_core = float(np.mean(worker_rates))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded water box, perturbed frames)",
             "config": {"workload": "qcmm_water_box_am1_abfs", "qc_atoms": len(sel), "mm_atoms": len(Z) - len(sel),
                        "frames_per_step": n},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": "%d frames per step, one frame per process, oracle/mndo_oracle.c" % n},
+                             "per_core": per_core,
+                             "sample": "%d frames per step split evenly over %d worker processes (pool made and warmed once, "
+                                       "each worker holding its QC region and spline), cold E+grad per frame, oracle/mndo_oracle.c; "
+                                       "per_core = a worker's own frames / its own time, all workers busy" % (n, cores)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -224,8 +303,8 @@ def bench_clusters(args):
     mols = workloads.water_clusters(512, seed=2)
     b = MoleculeBatch("pm3", mols)
     xyz = b.coordinates(mols)
-    convs = {"fp64": DIISSCFConverger(),
-             "mixed": DIISSCFConverger(densityStep="purification", purificationProducts=6, purificationSwitch=1e-5)}
+    from pdynamo_mirror_gb300.converger import MIXED_METHOD
+    convs = {"fp64": DIISSCFConverger(), "mixed": DIISSCFConverger(**MIXED_METHOD)}
     res = {}
     for name in ("fp64", "mixed"):
         conv = convs[name]
@@ -330,7 +409,7 @@ def bench_md(args):
     rank = int(os.environ.get("RANK", "0"))
     Z, X, Q, sel, charge = workloads.qcmm_water_box(seed=1)
     R = args.frames
-    MIXED = dict(densityStep="purification", purificationProducts=6, purificationSwitch=1e-5)
+    from pdynamo_mirror_gb300.converger import MIXED_METHOD as MIXED
 
     def make(method):
         s = System(Z, X, mmCharges=Q)
@@ -482,26 +561,85 @@ def main():
             run_reference(args)
         return
 
+    bench_water_box(args, world, rank)
+
+
+def tei_count(Z):
+    """Two-centre TEIs of a QC region: per atom pair n_i(n_i+1)/2 x n_j(n_j+1)/2 (4 orbitals on heavy atoms, 1 on H)."""
+    t = np.array([1 if int(z) == 1 else 10 for z in Z], dtype=np.int64)
+    return int((t.sum() ** 2 - (t * t).sum()) // 2)
+
+
+def qcmm_pairs_in_cutoff(qc, mm, cutoff):
+    """QC/MM pairs within the outer cutoff over all frames (device tensors [F, n, 3], [F, m, 3] in A)."""
     import torch
-    from pdynamo_mirror_gb300 import NBModelABFS, QCModelMNDO, System, _native
+    n = 0
+    for f0 in range(0, qc.shape[0], 16):
+        d = torch.cdist(qc[f0:f0 + 16], mm[f0:f0 + 16])
+        n += int((d < cutoff).sum().item())
+    return n
+
+
+def single_frame_latency(Z, X, Q, sel, charge, method, repeats=5):
+    """Median wall time (ms) of one cold System.EnergyBatch(doGradients=True) of one frame, host coordinates in and
+    energy + gradients out: the drop-in call's latency."""
+    import torch
+    from pdynamo_mirror_gb300 import DIISSCFConverger, NBModelABFS, QCModelMNDO, System
+    from pdynamo_mirror_gb300.converger import MIXED_METHOD
+    s = System(Z, X, mmCharges=Q if Q is not None else None)
+    s.electronicState.charge = charge
+    s.DefineQCModel(QCModelMNDO("am1", converger=DIISSCFConverger(**(MIXED_METHOD if method == "mixed" else {}))), qcSelection=sel)
+    if Q is not None:
+        s.DefineNBModel(NBModelABFS(innerCutoff=8.0, outerCutoff=12.0))
+    t = []
+    for k in range(2 + repeats):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.EnergyBatch(X[None], doGradients=True, warmStart=False)
+        if k >= 2:
+            t.append(time.perf_counter() - t0)
+    return 1e3 * float(np.median(t))
+
+
+def cpu_single_frame(Z, X, Q, sel, charge, repeats=3):
+    """Median wall time (ms) of the oracle's cold E+grad of the same frame on one host core."""
+    from oracle import oracle as O
+    nq = len(sel)
+    Zq = [int(z) for z in Z[:nq]]
+    s = O.System(O.Hamiltonian("am1", Zq), Zq, charge=charge)
+    kn = O.abfs_knots(8.0, 12.0) if Q is not None else None
+    t = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        phi = O.qcmm("abfs", X[:nq], X[nq:], Q[nq:], knots=kn)[0] if Q is not None else None
+        s.density = None
+        r = s.energy(X[:nq], phi=phi)
+        if Q is not None:
+            O.qcmm("abfs", X[:nq], X[nq:], Q[nq:], qcq=r["charges"], knots=kn)
+        t.append(time.perf_counter() - t0)
+    return 1e3 * float(np.median(t))
+
+
+def bench_water_box(args, world, rank):
+    import torch
+    from pdynamo_mirror_gb300 import DIISSCFConverger, NBModelABFS, QCModelMNDO, System, _native, workloads
+    from pdynamo_mirror_gb300.converger import MIXED_METHOD
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     dev = torch.device("cuda")
     Z, X, Q, sel, charge, frames = workload(args.frames, seed=1 + rank)
-    from pdynamo_mirror_gb300 import DIISSCFConverger
-    METHODS = {"fp64": dict(densityStep="fp64"),
-               "mixed": dict(densityStep="purification", purificationProducts=6, purificationSwitch=1e-5)}
+    METHODS = {"fp64": dict(densityStep="fp64"), "mixed": dict(MIXED_METHOD)}
     METHODS["learned_mixed"] = METHODS["mixed"]
     guess_info = {}
+    nq = len(sel)
 
     def train_guess(s, eng):
         """The learned start density, trained on frames the SCF converges here (a seed apart from the timed
         frames); returns the model and what it achieved on held-out frames."""
         from pdynamo_mirror_gb300 import LearnedDensityGuess
         t0 = time.perf_counter()
-        from pdynamo_mirror_gb300 import workloads
         tr = workloads.perturbed_frames(X, 2048, sigma=0.02, seed=101 + rank)
         qc_t, mm_t, q_t, _ = s._device_inputs(tr)
         phis, dens = [], []
@@ -530,14 +668,13 @@ def main():
             guess, info = train_guess(s, eng)
             s.DefineDensityGuess(guess)
             # held-out validation (frames of their own seed): the guess stays on only if it saves SCF cycles
-            from pdynamo_mirror_gb300 import workloads
             qc_v, mm_v, q_v, _ = s._device_inputs(workloads.perturbed_frames(X, 256, sigma=0.02, seed=201 + rank))
             info.update(guess.validate(qc_v, conv, mm_v, q_v, nb))
             info["used_in_timed_steps"] = guess.enabled
             guess_info.update(info)
 
-        def step():
-            return eng.run(qc, conv, mm, q, nb, gradients=True, warm_start=False, guess=guess)
+        def step(events=False):
+            return eng.run(qc, conv, mm, q, nb, gradients=True, warm_start=False, guess=guess, events=events)
 
         for _ in range(args.warmup):
             r = step()
@@ -563,16 +700,19 @@ def main():
         ms = e0.elapsed_time(e1) / args.steps
         clk = clocks.stop() if clocks else None
         timers = eng.timings(len(frames))
-        # the dominant kernel alone: k_scf through pdg_scf on the integrals the last step left in the
-        # workspace (same frames, cold guess), CUDA events on the launching stream
-        k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        scf_times = []
+        # per-phase device times of further steps (not the timed ones): CUDA events around the QC/MM potentials,
+        # the integral kernels, the SCF kernel, the gradient kernels and the QC/MM gradients, median of 3
+        eng.phase_events(True)
+        phases = []
         for _ in range(3):
-            k0.record(stream)
-            eng.scf(conv, phi=r["phi"], use_density=False)
-            k1.record(stream)
-            torch.cuda.synchronize()
-            scf_times.append(k0.elapsed_time(k1))
+            rr = step(events=True)
+            pt = eng.phase_times()
+            ev = rr["events"]
+            pt.update(qcmm_potentials=ev[0].elapsed_time(ev[1]), qcmm_gradients=ev[2].elapsed_time(ev[3]),
+                      step=ev[0].elapsed_time(ev[3]))
+            phases.append(pt)
+        eng.phase_events(False)
+        phase_ms = {k: float(np.median([p[k] for p in phases])) for k in phases[0]}
         if world > 1:
             t = torch.tensor([ms], device=dev)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -587,8 +727,8 @@ def main():
             torch.cuda.synchronize()
             if k >= 2:
                 te.append(time.perf_counter() - t0)
-        return dict(ms=ms, clk=clk, scf_ms=float(np.median(scf_times)), e2e_s=sum(te) / len(te), E=E, G=G,
-                    ncyc=r["ncycles"].cpu().numpy(), timers=timers, eng=eng, conv=conv, frames_h=frames_h)
+        return dict(ms=ms, clk=clk, phase_ms=phase_ms, e2e_s=sum(te) / len(te), E=E, G=G,
+                    ncyc=r["ncycles"].cpu().numpy(), timers=timers, eng=eng, conv=conv, frames_h=frames_h, qc=qc, mm=mm)
 
     plain = measure("fp64", args.method == "fp64")
     mixed = None if args.method == "fp64" else (measure("mixed", args.method == "mixed"))
@@ -604,34 +744,82 @@ def main():
     ncyc_f = float(head["ncyc"].mean())
     fp64_peak = fp64_peak_tflops(dev)
     fp32_peak = fp32_peak_tflops(dev)
-    bf16_peak = peaks().get("bf16_tflops", 1925.7)
+    pk = peaks()
+    bf16_peak = pk.get("bf16_tflops", 1898.3)
+    hbm_peak = pk.get("hbm_gbs", 6790.0)
+    nF = len(frames)
 
     def roofline(h, mixed):
         """FP64 roofline of the method's k_scf (its FP64 algorithmic flops over the event-timed launch, against
         cuBLAS DGEMM measured here) and, for the mixed method, the composite: the time its FP64, FP32 and tensor work
         would take at the three measured peaks over the measured time."""
-        f64, f32, tc = scf_work(h["timers"], N, kv, len(frames), mixed)
-        t = h["scf_ms"] * 1e-3
+        f64, f32, tc = scf_work(h["timers"], N, kv, nF, mixed)
+        t_ms = h["phase_ms"]["scf"]
+        t = t_ms * 1e-3
+        traffic, tnote = scf_traffic("mixed" if mixed else "fp64", nF)
         r = {"bound": "fp64", "kernel": "k_scf", "achieved": f64 / t / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
-             "frac": f64 / t / 1e12 / fp64_peak,
-             "traffic": K_SCF_DRAM_BYTES_304["mixed" if mixed else "fp64"] if len(frames) == 304 else None,
-             "note": "FP64 algorithmic flops of the density steps over the k_scf launch (%.2f ms, %d frames); peak = cuBLAS DGEMM "
-                     "4096^3 measured in this run (of measured; MEASURED_PEAKS.json has no FP64 figure)" % (h["scf_ms"], len(frames))}
+             "frac": f64 / t / 1e12 / fp64_peak, "traffic": traffic, "traffic_note": tnote,
+             "note": "FP64 algorithmic flops of the density steps over the k_scf launch (%.2f ms, %d frames, CUDA events on its "
+                     "stream); peak = cuBLAS DGEMM 4096^3 measured in this run (of measured; MEASURED_PEAKS.json has no FP64 "
+                     "figure)" % (t_ms, nF)}
         if mixed:
             t_ideal = f64 / (fp64_peak * 1e12) + f32 / (fp32_peak * 1e12) + tc / (bf16_peak * 1e12)
-            r["composite"] = {"t_ideal_ms": t_ideal * 1e3, "t_measured_ms": h["scf_ms"], "frac": t_ideal / t,
+            r["composite"] = {"t_ideal_ms": t_ideal * 1e3, "t_measured_ms": t_ms, "frac": t_ideal / t,
                               "fp64_tflop": f64 / 1e12, "fp32_tflop": f32 / 1e12, "tensor_tflop": tc / 1e12,
                               "fp32_peak_tflops": fp32_peak, "bf16_peak_tflops": bf16_peak,
                               "note": "the mixed SCF spreads its work over the FP64 pipe (FP64 base steps), the FP32 pipe (perturbative "
                                       "steps, commutators) and the tensor cores (SP2): time at the three measured peaks (FP32: cuBLAS "
-                                      "SGEMM 4096^3 without TF32, measured here; BF16: MEASURED_PEAKS.json) over the measured launch"}
+                                      "SGEMM 4096^3 without TF32, measured here; BF16 burst: MEASURED_PEAKS.json) over the measured launch"}
         return r
+
+    def kernel_rooflines(h):
+        """Roofline of every kernel group of one step against the measured HBM copy bandwidth, from the algorithmic
+        bytes per unit of work: integrals 8 (n_TEI + N(N+1)/2 + 20 n_pairs) written + 24 N_A read per frame; Fock
+        builds 8 n_TEI + 24 N(N+1)/2 per build (their share of the SCF launch from its per-CTA phase cycles);
+        gradients 8 (n_TEI + N(N+1)/2) read + 24 N_A written per frame; QC/MM potentials and gradients 32 bytes per
+        QC/MM pair within the outer cutoff."""
+        ph, Th = h["phase_ms"], h["timers"]
+        n_tei, npk = tei_count(Z[:nq]), N * (N + 1) // 2
+        n_pairs = nq * (nq - 1) // 2
+        builds = float(Th["QC SCF Fock Builds"].mean())
+        fock_share = float(Th["QC Fock"].mean() / Th["QC SCF Total"].mean())
+        pairs = qcmm_pairs_in_cutoff(h["qc"], h["mm"], 12.0)
+
+        def row(kernels, nbytes, ms, unit_note):
+            gbs = nbytes / (ms * 1e-3) / 1e9
+            return {"kernels": kernels, "bound": "hbm", "bytes": nbytes, "ms": ms, "achieved": gbs, "peak": hbm_peak,
+                    "unit": "GB/s", "frac": gbs / hbm_peak, "count": unit_note}
+        return {
+            "pair_integrals": row("k_pair_integrals, _ss, _sps, k_assemble_h", nF * (8 * (n_tei + npk + 20 * n_pairs) + 24 * nq),
+                                  ph["integrals"], "n_TEI %d, N %d, %d pairs per frame" % (n_tei, N, n_pairs)),
+            "fock_build": row("k_scf (Fock build share %.3f of the launch)" % fock_share, nF * builds * (8 * n_tei + 24 * npk),
+                              fock_share * ph["scf"], "%.2f builds per frame" % builds),
+            "gradients": row("k_pair_gradients, _ss, _sps, k_reduce_gradients", nF * (8 * (n_tei + npk) + 24 * nq), ph["gradients"],
+                             "n_TEI %d per frame" % n_tei),
+            "qcmm_potentials": row("k_qcmm_potentials", 32 * pairs, ph["qcmm_potentials"], "%d QC/MM pairs within 12 A" % pairs),
+            "qcmm_gradients": row("k_qcmm_grad_qc, k_qcmm_grad_mm (FP32 pair terms in the mixed method)", 32 * pairs,
+                                  ph["qcmm_gradients"], "%d QC/MM pairs within 12 A" % pairs),
+            "phase_ms": ph,
+            "note": "CUDA events on the launching stream around each kernel group of one step (median of 3 steps after the "
+                    "timed ones); peak = MEASURED_PEAKS.json hbm_gbs (of measured)"}
+
     clk = head["clk"]
+    # one QC/MM E+grad (the drop-in call) and one 16-water AM1 E+grad: latency through System.EnergyBatch, and the oracle
+    # on one host core
+    Z0, X0 = workloads.water_cluster(16, seed=0)
+    single = {"qcmm_water_box": {"gpu_ms_plain_fp64": single_frame_latency(Z, X, Q, sel, charge, "fp64"),
+                                 "gpu_ms_mixed": single_frame_latency(Z, X, Q, sel, charge, "mixed"),
+                                 "cpu_ms_one_core": cpu_single_frame(Z, X, Q, sel, charge) if not args.no_cpu_baseline else None},
+              "water_cluster_16_am1": {"gpu_ms_plain_fp64": single_frame_latency(Z0, X0, None, list(range(len(Z0))), 0, "fp64"),
+                                       "gpu_ms_mixed": single_frame_latency(Z0, X0, None, list(range(len(Z0))), 0, "mixed"),
+                                       "cpu_ms_one_core": cpu_single_frame(Z0, X0, None, list(range(len(Z0))), 0) if not args.no_cpu_baseline else None},
+              "note": "median wall time of one cold System.EnergyBatch(doGradients=True) of one frame (host coordinates in, energy "
+                      "and gradients out; one SCF CTA on one SM), and of the oracle's cold E+grad of the same frame on one host core"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded water box, perturbed frames)",
-            "config": {"workload": "qcmm_water_box_am1_abfs", "qc_atoms": len(sel), "mm_atoms": len(Z) - len(sel),
-                       "basis_functions": N, "frames_per_step": len(frames),
+            "config": {"workload": "qcmm_water_box_am1_abfs", "qc_atoms": nq, "mm_atoms": len(Z) - nq,
+                       "basis_functions": N, "frames_per_step": nF,
                        "method": {"fp64": "plain FP64",
                                   "mixed": "mixed: split-BF16 SP2 purification on tcgen05 (6 partial products, FP32 accumulation) until the RMS density change < 1e-5, then FP64",
                                   "learned_mixed": "learned+mixed: per-pair MLP start density (kept only where held-out validation shows "
@@ -641,9 +829,13 @@ def main():
                        "scf_cta": scf_cta_layout(eng, T),
                        "l2": "working set > L2 (no flush needed)"},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(head["frames_h"].numel() * 8),
-                    "d2h_bytes_per_step": int(head["G"].nbytes + len(frames) * (_native.NENERGY + 2 + len(sel)) * 8)},
-            "gpu_launches": 8 * args.steps,
+                    "d2h_bytes_per_step": int(head["G"].nbytes + nF * (_native.NENERGY + 2 + nq) * 8)},
+            # per step: k_qcmm_potentials; k_pair_integrals, _ss, _sps, k_assemble_h; k_scf; k_pair_gradients, _ss, _sps,
+            # k_reduce_gradients; k_qcmm_grad_qc, k_qcmm_grad_mm (or their FP32-pair forms)
+            "gpu_launches": 12 * args.steps,
             "roofline": roofline(head, args.method != "fp64"),
+            "kernel_rooflines": kernel_rooflines(head),
+            "single_frame": single,
             "clocks": clk}
     if args.method != "fp64":
         # tensor-core part: SP2 iterations x k partial products x 2 N^3 algorithmic flops, over the purification
@@ -653,26 +845,31 @@ def main():
         mhz = (clk or {}).get("sm_mhz") or 2070.0
         t_pur = pur_cycles / (mhz * 1e6)
         tc_tf = (sp2 * 6 * 2.0 * N ** 3) / t_pur / 1e12 if t_pur > 0 else 0.0
-        pk = peaks()
-        bf16 = pk.get("bf16_tflops", 1900.0) / 152.0 / 2   # per SM, two SCF CTAs per SM share it
+        bf16 = bf16_peak / 152.0 / 2   # per SM, two SCF CTAs per SM share it
         line["roofline"]["tensor"] = {"achieved_per_cta": tc_tf, "unit": "TFLOP/s", "peak_per_cta": bf16,
                                       "frac": tc_tf / bf16 if bf16 else None,
                                       "note": "split-BF16 SP2 products of one frame's CTA (measured BF16 peak / 152 SMs / 2 CTAs per SM)"}
         dE = float(np.abs(head["E"] - plain["E"]).max()) / KJ
         dG = float(np.abs(head["G"] - plain["G"]).max()) / (KJ * 1.0e-10 / 5.291772083e-11)
         line["plain_fp64"] = {"value": n_total / (plain["ms"] * 1e-3), "ms_per_step": plain["ms"], "e2e": n_total / plain["e2e_s"],
-                              "mean_scf_cycles": float(plain["ncyc"].mean()), "roofline": roofline(plain, False)}
+                              "mean_scf_cycles": float(plain["ncyc"].mean()), "roofline": roofline(plain, False),
+                              "kernel_rooflines": kernel_rooflines(plain)}
         if args.method == "learned_mixed":
             line["mixed"] = {"value": n_total / (mixed["ms"] * 1e-3), "ms_per_step": mixed["ms"], "e2e": n_total / mixed["e2e_s"],
                              "mean_scf_cycles": float(mixed["ncyc"].mean())}
             line["learned_guess"] = guess_info
         line["accuracy_vs_plain_fp64"] = {"max_abs_dE_hartree": dE, "max_abs_dF_hartree_per_bohr": dG,
-                                          "gate": "|dE| < 1e-6 Eh, |dF| < 1e-5 Eh/Bohr", "pass": bool(dE < 1e-6 and dG < 1e-5)}
+                                          "gate": "|dE| < 1e-6 Eh, |dF| < 1e-5 Eh/Bohr", "pass": bool(dE < 1e-6 and dG < 1e-5),
+                                          "oracle": "each method's timed configuration is checked against the oracle frame by frame "
+                                                    "in tests/test_gpu_timed_config.py"}
     if rank == 0 and not args.no_cpu_baseline:
-        n = min(len(frames), 96)
-        t, k = cpu_reference_sample(list(Z), Q, sel, charge, frames, n, 1)
+        n = min(nF, 96)
+        cpu = CPUBaseline(Z, Q, sel, charge, 1)
+        cpu.warm(frames)
+        t, k, _ = cpu.run(frames[:n])
         line["cpu_baseline"] = {"value": k / t, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": "%d frames, serial, oracle/mndo_oracle.c (C restatement; pDynamo's own core is not buildable on the GPU host)" % n}
+                                "sample": "%d frames, serial, cold E+grad each, oracle/mndo_oracle.c (C restatement; pDynamo's own "
+                                          "core is not buildable on the GPU host)" % n}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -171,6 +171,15 @@ int pdg_gradients(pdg_system *sys, int n_frames, const double *d_xyz, const doub
 int pdg_gradients_static_scratch(pdg_system *sys, int n_frames, const double *d_xyz, const double *d_density,
                                  double *d_gradients, void *stream);
 
+/* Device time of each phase of pdg_energy_gradients, for profiling.  pdg_phase_events(sys, 1) makes every later
+ * pdg_energy_gradients call on sys record four CUDA events on its stream (before the integrals, after them, after
+ * the SCF kernel, after the gradient kernels; 0 stops it).  pdg_phase_times waits for the last call's events and
+ * writes h_ms[3]: the integral kernels, the SCF kernel and the gradient kernels, in milliseconds.  The device
+ * counterpart of the reference's per-phase timings (pMolecule.QCModel.pyx:208-275, EnergyWithTimings: QC
+ * Initialize, the converger, QC Gradients). */
+int pdg_phase_events(pdg_system *sys, int enable);
+int pdg_phase_times(const pdg_system *sys, float *h_ms);
+
 /* Per-phase SCF timings of the last pdg_energy_gradients call that used this workspace: for every frame
  * PDG_NTIMERS GPU clock-cycle counts (clock64 of the frame's CTA), the device counterpart of the phase
  * timings of pMolecule.QCModel.pyx:208-275 (EnergyWithTimings: QC Fock, QC Converger Iterate,
@@ -268,9 +277,12 @@ int pdg_guess_loss(pdg_system *sys, int n_frames, const double *d_xyz, const int
 
 /* Check of the tensor-core (tcgen05) split-BF16 product used by the purification density step:
  * d_c = X X for a symmetric n x n FP32 matrix d_x (n <= 144), with kprod = 1, 3 or 6 BF16 partial
- * products accumulated in FP32.  d_status (one int) is 0, or 1 when the tensor-core completion wait ran out.
+ * products accumulated in FP32.  d_status (one int) is 0, or 1 when the tensor-core completion wait ran out
+ * after wait_limit polls of its mbarrier (wait_limit <= 0: the limit the SCF kernel uses, 2^22).
+ * kprod = 0 checks that bounded wait alone: no tensor-core operation is issued (no allocation, no product), the
+ * kernel waits wait_limit polls on a barrier nothing arrives on and writes status 1; d_x and d_c may be NULL.
  * No counterpart in the reference (its density step is an FP64 eigensolve). */
-int pdg_tc_selftest(int n, int kprod, const float *d_x, float *d_c, int *d_status, void *stream);
+int pdg_tc_selftest(int n, int kprod, int wait_limit, const float *d_x, float *d_c, int *d_status, void *stream);
 
 /* Launch configuration of the SCF kernel for this system on the current device: threads per CTA (one CTA
  * per frame), dynamic shared memory per CTA, and the CUDA runtime's occupancy estimate in CTAs per SM (the

@@ -34,6 +34,10 @@ struct pdg_system {
     float *d_ovl32 = nullptr, *d_mpw32 = nullptr;
     int *d_ints = nullptr;
     void *d_mp = nullptr;
+    // phase events of pdg_energy_gradients (pdg_phase_events / pdg_phase_times): before the integrals, after them,
+    // after the SCF, after the gradients
+    cudaEvent_t ev[4] = { nullptr, nullptr, nullptr, nullptr };
+    int ev_on = 0, ev_recorded = 0;
 };
 
 extern "C" int pdg_version(void) { return 100; }
@@ -167,6 +171,8 @@ extern "C" int pdg_system_destroy(pdg_system *s)
     if (!s) return PDG_OK;
     cudaFree(s->d_elements); cudaFree(s->d_terms); cudaFree(s->d_ints); cudaFree(s->d_ovl); cudaFree(s->d_mp);
     cudaFree(s->d_ovl32); cudaFree(s->d_mpw32);
+    for (cudaEvent_t e : s->ev)
+        if (e) cudaEventDestroy(e);
     delete s;
     return PDG_OK;
 }
@@ -217,16 +223,43 @@ extern "C" int pdg_energy_gradients(pdg_system *s, int n_frames, const double *d
     cudaStream_t st = (cudaStream_t)stream;
     FramePlan p = plan_for(s, PDG_MAX_HISTORY);
     double *w = (double *)ws;
+    auto mark = [&](int k) { if (s->ev_on) cudaEventRecord(s->ev[k], st); };
+    s->ev_recorded = 0;
+    mark(0);
     if ((rc = integrals(s, p, n_frames, d_xyz, w, st))) return rc;
+    mark(1);
     launch_scf(s->d, p, n_frames, d_phi, *o, d_density, use_density, d_energies, d_charges, d_status, d_ncycles, w, 0, nullptr, st);
     if ((rc = cuda_check(cudaGetLastError(), "scf kernel"))) return rc;
+    mark(2);
     if (d_gradients) {
         // the mixed method takes the sp-sp pair gradient terms in FP32 (assembled and summed in FP64)
         launch_pair_gradients(s->d, p, n_frames, d_xyz, d_density, w, st, o->density_step != 0);
         launch_reduce_gradients(s->d, p, n_frames, w, d_gradients, st);
         if ((rc = cuda_check(cudaGetLastError(), "gradient kernels"))) return rc;
     }
+    mark(3);
+    s->ev_recorded = s->ev_on;
     return PDG_OK;
+}
+
+extern "C" int pdg_phase_events(pdg_system *s, int enable)
+{
+    if (!s) return fail(PDG_BAD_ARGUMENT, "null system");
+    if (enable && !s->ev[0])
+        for (cudaEvent_t &e : s->ev)
+            if ((e = nullptr, cudaEventCreate(&e)) != cudaSuccess) return cuda_check(cudaGetLastError(), "phase events");
+    s->ev_on = enable ? 1 : 0;
+    s->ev_recorded = 0;
+    return PDG_OK;
+}
+
+extern "C" int pdg_phase_times(const pdg_system *s, float *h_ms)
+{
+    if (!s || !h_ms) return fail(PDG_BAD_ARGUMENT, "null argument");
+    if (!s->ev_recorded) return fail(PDG_BAD_ARGUMENT, "pdg_phase_times: no pdg_energy_gradients call recorded phase events");
+    int rc = cuda_check(cudaEventSynchronize(s->ev[3]), "phase events");
+    for (int k = 0; k < 3 && !rc; k++) rc = cuda_check(cudaEventElapsedTime(h_ms + k, s->ev[k], s->ev[k + 1]), "phase events");
+    return rc;
 }
 
 extern "C" int pdg_scf(pdg_system *s, int n_frames, const double *d_phi, const pdg_scf_options *o, double *d_density,
@@ -369,12 +402,15 @@ extern "C" int pdg_gradients_static_scratch(pdg_system *s, int n_frames, const d
     return cuda_check(cudaGetLastError(), "gradient kernels (static scratch)");
 }
 
-extern "C" int pdg_tc_selftest(int n, int kprod, const float *d_x, float *d_c, int *d_status, void *stream)
+extern "C" int pdg_tc_selftest(int n, int kprod, int wait_limit, const float *d_x, float *d_c, int *d_status, void *stream)
 {
-    if (n < 1 || n > 144) return fail(PDG_TOO_LARGE, "pdg_tc_selftest: n must be 1..144");
-    if (kprod != 1 && kprod != 3 && kprod != 6) return fail(PDG_BAD_ARGUMENT, "pdg_tc_selftest: kprod must be 1, 3 or 6");
-    if (!d_x || !d_c || !d_status) return fail(PDG_BAD_ARGUMENT, "null argument");
-    launch_tc_selftest(n, kprod, d_x, d_c, d_status, (cudaStream_t)stream);
+    if (kprod != 0 && kprod != 1 && kprod != 3 && kprod != 6) return fail(PDG_BAD_ARGUMENT, "pdg_tc_selftest: kprod must be 0, 1, 3 or 6");
+    if (!d_status) return fail(PDG_BAD_ARGUMENT, "null argument");
+    if (kprod != 0) {
+        if (n < 1 || n > 144) return fail(PDG_TOO_LARGE, "pdg_tc_selftest: n must be 1..144");
+        if (!d_x || !d_c) return fail(PDG_BAD_ARGUMENT, "null argument");
+    }
+    launch_tc_selftest(n, kprod, wait_limit, d_x, d_c, d_status, (cudaStream_t)stream);
     return cuda_check(cudaGetLastError(), "tensor-core self-test kernel");
 }
 

@@ -254,7 +254,7 @@ int launch_qcmm_potentials(int model, int n_frames, int n_qc, int n_mm, const do
 int launch_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,
                           const double *q, const double *qcq, int n_knots, const double *knots, double cutoff,
                           double *gqc, double *gmm, cudaStream_t st);
-int launch_tc_selftest(int n, int kprod, const float *x, float *c, int *status, cudaStream_t st);
+int launch_tc_selftest(int n, int kprod, int wait_limit, const float *x, float *c, int *status, cudaStream_t st);
 
 // SCF kernels (scf.cu), in two compiled variants: scf_n (256 threads per CTA, tensor-core step) and scf_w
 // (scf_wide.cu: 512 threads per CTA, FP64 only).  The single-system entry points use scf_n.

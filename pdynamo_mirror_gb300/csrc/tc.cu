@@ -5,18 +5,31 @@
 // 0..127 come from one M = 128 tcgen05 tile; rows 128..n-1 are the transposed columns of that tile (X X is
 // symmetric) except the trailing 16 x 16 corner, which FP32 cores compute directly.  This is the product the
 // purification density step runs every iteration.
+//
+// kprod = 0 checks the bounded completion wait itself: the kernel initialises the barrier, issues no tcgen05
+// operation at all (no tensor-memory allocation, no product, no commit), waits wait_limit polls on the barrier
+// that nothing will ever arrive on, and reports status 1.  That is the path every tensor-core wait of the SCF
+// takes when a completion never comes: it gives up and reports, it does not hang.
 #include "tc.cuh"
 
 #define TC_THREADS 256
 #define TC_WAIT_LIMIT (1 << 22)
 
-__global__ void __launch_bounds__(TC_THREADS) k_tc_selftest(int n, int kprod, const float *__restrict__ X, float *__restrict__ C,
-                                                            int *__restrict__ status)
+__global__ void __launch_bounds__(TC_THREADS) k_tc_selftest(int n, int kprod, int wait_limit, const float *__restrict__ X,
+                                                            float *__restrict__ C, int *__restrict__ status)
 {
     extern __shared__ __align__(1024) unsigned char tsm[];
     __shared__ uint32_t taddr_s;
     __shared__ __align__(8) uint64_t bar_s;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (kprod == 0) {
+        if (tid == 0) {
+            const uint32_t bar = tc_smem_addr(&bar_s);
+            mbar_init(bar, 1);
+            *status = mbar_wait(bar, 0, wait_limit) ? 0 : 1;
+        }
+        return;
+    }
     const int Kp = (n + 15) & ~15, R = Kp > TC_M ? Kp : TC_M;
     const size_t part = (size_t)R * Kp * 2;
     unsigned char *ph = tsm, *pm = tsm + part, *pl = tsm + 2 * part;
@@ -42,7 +55,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_selftest(int n, int kprod, co
         for (int q = 0; q < kprod; q++) tc_product(taddr, pa[q], 0, pb[q], Kp, Kp, q > 0);
         tc_commit(bar);
     }
-    const bool ok = mbar_wait(bar, 0, TC_WAIT_LIMIT);
+    const bool ok = mbar_wait(bar, 0, wait_limit);
     tc_fence_after();
     // accumulator rows 0..127: lane quarter w % 4; warps 0-3 and 4-7 split the column chunks
     const int nch = Kp / 16, half = (nch + 1) / 2, c0 = w < 4 ? 0 : half, c1 = w < 4 ? half : nch;
@@ -70,11 +83,11 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_selftest(int n, int kprod, co
     if (tid == 0) *status = ok ? 0 : 1;
 }
 
-int launch_tc_selftest(int n, int kprod, const float *x, float *c, int *status, cudaStream_t st)
+int launch_tc_selftest(int n, int kprod, int wait_limit, const float *x, float *c, int *status, cudaStream_t st)
 {
     const int Kp = (n + 15) & ~15, R = Kp > TC_M ? Kp : TC_M;
-    const size_t sm = (size_t)3 * R * Kp * 2;
+    const size_t sm = kprod == 0 ? 0 : (size_t)3 * R * Kp * 2;
     cudaFuncSetAttribute(k_tc_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_tc_selftest<<<1, TC_THREADS, sm, st>>>(n, kprod, x, c, status);
+    k_tc_selftest<<<1, TC_THREADS, sm, st>>>(n, kprod, wait_limit > 0 ? wait_limit : TC_WAIT_LIMIT, x, c, status);
     return 0;
 }

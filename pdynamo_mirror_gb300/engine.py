@@ -69,11 +69,13 @@ class QCEngine:
         return self._knots[k]
 
     def run(self, qc_xyz, converger, mm_xyz=None, mm_charges=None, nbmodel=None, gradients=True, warm_start=True, guess=None,
-            mm_gradients=True):
+            mm_gradients=True, events=False):
         """qc_xyz [F, n, 3] and mm_xyz [F, m, 3] in Angstrom (device float64), mm_charges [m].  The SCF starts
         from the previous density (warm_start, same batch shape), else from guess.predict (a
         LearnedDensityGuess, unless its validation disabled it), else from the diagonal guess.  mm_gradients=False skips the
-        MM-side QC/MM gradients (fixed MM atoms).  Returns a dict of device tensors in Hartree / Hartree per Bohr."""
+        MM-side QC/MM gradients (fixed MM atoms).  Returns a dict of device tensors in Hartree / Hartree per Bohr.
+        events=True also returns "events": four CUDA events on the stream, before the QC/MM potentials, after them,
+        after pdg_energy_gradients and after the QC/MM gradients (for profiling)."""
         F = qc_xyz.shape[0]
         n, N = self.n_atoms, self.n_basis
         dev = self.device
@@ -81,8 +83,14 @@ class QCEngine:
         sh = _native.stream_handle(stream)
         ws = self.workspace(F)
         out = {}
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)] if events else None
+
+        def mark(k):
+            if ev:
+                ev[k].record(stream)
         phi = None
         qcmm = nbmodel is not None and mm_xyz is not None and mm_xyz.shape[1] > 0
+        mark(0)
         if qcmm:
             knots = self.knots(nbmodel) if nbmodel.model_id == 1 else None
             nk = 0 if knots is None else knots.numel() // 3
@@ -90,6 +98,7 @@ class QCEngine:
             _native.check(self.L.pdg_qcmm_potentials(nbmodel.model_id, F, n, mm_xyz.shape[1], _native.ptr(qc_xyz), _native.ptr(mm_xyz),
                                                      _native.ptr(mm_charges), nk, _native.ptr(knots), float(nbmodel.outerCutoff),
                                                      _native.ptr(phi), sh), "pdg_qcmm_potentials")
+        mark(1)
         xyz_bohr = (qc_xyz * ANGSTROMS_TO_BOHRS).contiguous()
         use = 1 if (warm_start and self.density is not None and self.density.shape[0] == F) else 0
         if not use and guess is not None and guess.enabled:
@@ -108,6 +117,7 @@ class QCEngine:
                                                   _native.ptr(charges), _native.ptr(status), _native.ptr(ncycles),
                                                   _native.ptr(ws), ws.numel(), sh), "pdg_energy_gradients")
         out.update(energies=energies, qc_gradients=grad, charges=charges, status=status, ncycles=ncycles, phi=phi)
+        mark(2)
         if qcmm and gradients:
             gqc = torch.empty((F, n, 3), dtype=torch.float64, device=dev)
             gmm = torch.empty((F, mm_xyz.shape[1], 3), dtype=torch.float64, device=dev) if mm_gradients else None
@@ -118,6 +128,9 @@ class QCEngine:
                                                     float(nbmodel.outerCutoff), _native.ptr(gqc), _native.ptr(gmm), sh),
                           "pdg_qcmm_gradients")
             out.update(qcmm_qc_gradients=gqc, qcmm_mm_gradients=gmm)
+        mark(3)
+        if ev:
+            out["events"] = ev
         return out
 
     def scf(self, converger, phi=None, use_density=False):
@@ -145,6 +158,16 @@ class QCEngine:
                                          _native.ptr(st), _native.ptr(ws), ws.numel(), _native.stream_handle(torch.cuda.current_stream(self.device))),
                       "pdg_density")
         return P, en, st
+
+    def phase_events(self, enable=True):
+        """Record CUDA events around the integral, SCF and gradient kernels of every later run (pdg_phase_events)."""
+        _native.check(self.L.pdg_phase_events(self.handle, 1 if enable else 0), "pdg_phase_events")
+
+    def phase_times(self):
+        """Device milliseconds of the last run's integrals, SCF and gradients (pdg_phase_times; waits for them)."""
+        out = (ctypes.c_float * 3)()
+        _native.check(self.L.pdg_phase_times(self.handle, out), "pdg_phase_times")
+        return {"integrals": out[0], "scf": out[1], "gradients": out[2]}
 
     def occupancy(self):
         """(threads per SCF CTA, dynamic shared bytes, resident SCF CTAs per SM)."""

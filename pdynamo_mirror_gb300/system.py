@@ -32,7 +32,24 @@ class Configuration:
 
 
 class SCFNotConverged(ValueError):
-    pass
+    """The reference raises ValueError when the SCF does not converge (pMolecule.QCModel.pyx:177); here also when a
+    frame's SCF stopped on a non-finite energy or a tensor-core wait that ran out."""
+
+
+def scf_failure_message(status):
+    """The message for the per-frame statuses of a batch that did not all converge."""
+    status = np.asarray(status)
+    parts = []
+    for code, what in ((_native.PDG_NOT_CONVERGED, "not converged"), (_native.PDG_NAN, "non-finite energy"),
+                       (_native.PDG_TENSOR_TIMEOUT, "tensor-core completion wait ran out")):
+        frames = np.nonzero(status == code)[0]
+        if len(frames):
+            parts.append("%s in frame%s %s" % (what, "s" if len(frames) > 1 else "", ", ".join(str(int(f)) for f in frames[:8])
+                                                + (", ..." if len(frames) > 8 else "")))
+    other = np.nonzero(~np.isin(status, [_native.PDG_OK, _native.PDG_NOT_CONVERGED, _native.PDG_NAN, _native.PDG_TENSOR_TIMEOUT]))[0]
+    if len(other):
+        parts.append("status %d in frame %d" % (int(status[other[0]]), int(other[0])))
+    return "SCF procedure not converged: " + "; ".join(parts) + "."
 
 
 class System:
@@ -216,7 +233,7 @@ class System:
         terms = {"Pure QC": pure, "QC/MM Elect.": qcmm, "SCF Cycles": small[:, _native.NENERGY + 1].astype(np.int32), "Status": st}
         if (st != _native.PDG_OK).any():
             self._engine.density = None
-            raise SCFNotConverged("SCF procedure not converged.")
+            raise SCFNotConverged(scf_failure_message(st))
         total = pure + (qcmm if mm is not None else 0.0)
         if mmi is not None:
             Emm = small[:, _native.NENERGY + 2:_native.NENERGY + 2 + len(_native.MM_TERMS)]
@@ -268,6 +285,9 @@ class System:
         q = np.zeros_like(q) if spinDensities else np.array(q, dtype=np.float64)
         if qcAtomsOnly or self.mmCharges is None:
             return q
+        # The QC atoms carry their QC charge only, as MMAtomContainer.AtomicCharges gives 0 for the atoms that
+        # DefineQCModel deactivated: whatever the order of DefineMMModel and DefineQCModel, and whatever the
+        # constructor's mmCharges held at those atoms.
         charges = np.zeros(len(self.atomicNumbers)) if spinDensities else np.array(self.mmCharges, dtype=np.float64)
-        charges[self.qcSelection] += q
+        charges[self.qcSelection] = q
         return charges

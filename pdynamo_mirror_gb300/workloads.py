@@ -8,6 +8,8 @@
   rejection with O-O >= 2.6 A to every oxygen already placed.  Non-periodic.
 * perturbed_frames(xyz, n, sigma, seed): n copies with independent Gaussian displacements, a stand-in for
   molecular-dynamics frames of one system.
+* qcmm_water_box_frames(n): the QC/MM water box (seed 1) and n of its perturbed frames (0.02 A, seed 11), the
+  benchmark's input.
 """
 
 import math
@@ -127,3 +129,9 @@ def water_clusters(n_clusters=512, smallest=4, largest=64, seed=2):
     rng = np.random.default_rng(seed)
     sizes = rng.integers(smallest, largest + 1, size=n_clusters)
     return [water_cluster(int(w), seed=seed * 1000003 + k) for k, w in enumerate(sizes)]
+
+
+def qcmm_water_box_frames(n_frames, seed=1, frame_seed=11, sigma=0.02):
+    """The QC/MM water box and n_frames perturbed copies of it: (Z, X, charges, qc_selection, qc_charge, frames)."""
+    Z, X, Q, sel, charge = qcmm_water_box(seed=seed)
+    return Z, X, Q, sel, charge, perturbed_frames(X, n_frames, sigma=sigma, seed=frame_seed)

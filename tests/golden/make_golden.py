@@ -3,7 +3,7 @@
 Run in a container that has the reference tree and the compiled reference core
 (``make -C oracle ref``):
 
-    python tests/golden/make_golden.py /root/reference
+    PDYNAMO_REFERENCE=<reference tree> python tests/golden/make_golden.py
 
 It writes
   mndo_rhf_pickle.json     the reference's stored "Pure QC" energies (kJ/mol) for every closed-shell test
@@ -80,6 +80,14 @@ def molecules(root):
             Z, xyz = read_xyz(path)
             out[label] = {"Z": Z, "xyz": xyz, "charge": CHARGES.get(label, 0)}
     return out
+
+
+def reference_root():
+    """The pDynamo 1.9.0 tree: the first argument, else $PDYNAMO_REFERENCE."""
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PDYNAMO_REFERENCE")
+    if not root:
+        raise SystemExit("usage: %s <reference tree>  (or set PDYNAMO_REFERENCE)" % sys.argv[0])
+    return root
 
 
 def main(root):
@@ -167,4 +175,4 @@ def qcmm_fixtures(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(reference_root())

@@ -8,7 +8,7 @@ the allyl and methylene radicals, unrestricted.
 
 Run where the reference tree and the compiled reference core exist (``make -C oracle ref``):
 
-    python tests/golden/make_open_shell_golden.py /root/reference
+    PDYNAMO_REFERENCE=<reference tree> python tests/golden/make_open_shell_golden.py
 """
 
 import json, os, sys
@@ -31,6 +31,14 @@ KEYWORDS = {"Tyrosine Dipeptide Singlet": [(True, "Cardinal"), (False, "Cardinal
                                            (False, "Fixed Fractional"), (True, "Variable Fractional"), (False, "Variable Fractional")],
             "Tyrosine Dipeptide Triplet": UNRESTRICTED, "Allyl Radical": UNRESTRICTED, "Methylene Radical": UNRESTRICTED}
 SMALL = ("Allyl Radical", "Methylene Radical")
+
+
+def reference_root():
+    """The pDynamo 1.9.0 tree: the first argument, else $PDYNAMO_REFERENCE."""
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PDYNAMO_REFERENCE")
+    if not root:
+        raise SystemExit("usage: %s <reference tree>  (or set PDYNAMO_REFERENCE)" % sys.argv[0])
+    return root
 
 
 def main(root):
@@ -94,4 +102,4 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(reference_root())

@@ -7,7 +7,7 @@ the gradients and cycle counts come from the core run here; its energies equal t
 
 Run where the reference tree and the compiled reference core exist (``make -C oracle ref``):
 
-    python tests/golden/make_pm6_golden.py /root/reference
+    PDYNAMO_REFERENCE=<reference tree> python tests/golden/make_pm6_golden.py
 
 It also writes pm6_pickle.json: the reference's stored PM6 "Pure QC" energies (kJ/mol, with their tolerance) from
 pMolecule-1.9.0/data/reference/MNDORHFEnergies.pkl, read as make_golden.py reads the other Hamiltonians'.
@@ -23,6 +23,14 @@ from oracle import refdriver as R  # noqa: E402
 from oracle.rawtables import table  # noqa: E402
 sys.path.insert(0, HERE)
 from make_golden import load_pickle  # noqa: E402
+
+
+def reference_root():
+    """The pDynamo 1.9.0 tree: the first argument, else $PDYNAMO_REFERENCE."""
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PDYNAMO_REFERENCE")
+    if not root:
+        raise SystemExit("usage: %s <reference tree>  (or set PDYNAMO_REFERENCE)" % sys.argv[0])
+    return root
 
 
 def main(root):
@@ -48,4 +56,4 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(reference_root())

@@ -6,7 +6,7 @@ radical (UHF, AM1).
 
 Run where the reference tree and the compiled reference core exist (``make -C oracle ref``):
 
-    python tests/golden/make_properties_golden.py /root/reference
+    PDYNAMO_REFERENCE=<reference tree> python tests/golden/make_properties_golden.py
 """
 
 import json, os, sys
@@ -20,6 +20,14 @@ from oracle import refdriver as R  # noqa: E402
 from make_golden import read_xyz  # noqa: E402
 
 CLOSED = (("water", "am1"), ("formaldehyde", "am1"), ("glycine", "am1"), ("pyridine", "pm3"), ("nitromethane", "pm3"))
+
+
+def reference_root():
+    """The pDynamo 1.9.0 tree: the first argument, else $PDYNAMO_REFERENCE."""
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PDYNAMO_REFERENCE")
+    if not root:
+        raise SystemExit("usage: %s <reference tree>  (or set PDYNAMO_REFERENCE)" % sys.argv[0])
+    return root
 
 
 def main(root):
@@ -47,4 +55,4 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(reference_root())

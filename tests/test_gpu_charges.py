@@ -46,6 +46,34 @@ def test_qcmm_charges_match_oracle():
     np.testing.assert_allclose(s.AtomicCharges(qcAtomsOnly=True), q[:len(Z)])
 
 
+@pytest.mark.parametrize("order", ["mm_first", "qc_first"])
+def test_qcmm_charges_ignore_mm_charges_at_qc_atoms(order):
+    """A TIP3P MM model puts non-zero charges on the QC atoms too.  Whichever of DefineMMModel and DefineQCModel
+    comes first, the QC atoms' charges are their Lowdin charges alone (MMAtomContainer.AtomicCharges gives 0 for
+    atoms that DefineQCModel deactivated) and the MM atoms keep their TIP3P charges."""
+    from oracle import oracle as O
+    from pdynamo_mirror_gb300 import MMModel, NBModelABFS, QCModelMNDO, System, workloads
+    Z, X, allZ, allX, _ = _water_trimer_with_mm()
+    nq = len(Z)
+    s = System(allZ, allX)
+    mm = MMModel.TIP3PWater(allZ, allX)
+    assert np.abs(np.asarray(mm.charges)[:nq]).min() > 0.4
+    if order == "mm_first":
+        s.DefineMMModel(mm)
+        s.DefineQCModel(QCModelMNDO("am1"), qcSelection=range(nq))
+    else:
+        s.DefineQCModel(QCModelMNDO("am1"), qcSelection=range(nq))
+        s.DefineMMModel(mm)
+    s.DefineNBModel(NBModelABFS())
+    s.Energy(doGradients=True)
+    mmq = np.asarray(mm.charges, dtype=np.float64)
+    phi, _, _ = O.qcmm("abfs", X, allX[nq:], mmq[nq:], knots=O.abfs_knots(8.0, 12.0))
+    r = O.System(O.Hamiltonian("am1", Z), Z).energy(X, phi=phi)
+    q = s.AtomicCharges()
+    np.testing.assert_allclose(q[:nq], r["charges"], rtol=0, atol=1e-6)
+    np.testing.assert_allclose(q[nq:], mmq[nq:])
+
+
 def test_dipoles_and_bond_orders_match_reference():
     """System.DipoleMoment and QCModelMNDO.BondOrders after Energy against the reference core's
     QCModelMNDO_DipoleMoment / QCModelMNDO_MayerBondOrders (tests/golden/properties_reference.json, closed-shell

@@ -21,7 +21,7 @@ def _product(X, k):
     x = torch.as_tensor(X, dtype=torch.float32, device="cuda").contiguous()
     c = torch.full_like(x, float("nan"))
     st = torch.full((1,), -1, dtype=torch.int32, device="cuda")
-    _native.check(L.pdg_tc_selftest(X.shape[0], k, _native.ptr(x), _native.ptr(c), _native.ptr(st),
+    _native.check(L.pdg_tc_selftest(X.shape[0], k, 0, _native.ptr(x), _native.ptr(c), _native.ptr(st),
                                     _native.stream_handle(torch.cuda.current_stream())), "pdg_tc_selftest")
     torch.cuda.synchronize()
     assert int(st.item()) == 0

@@ -120,3 +120,13 @@ def test_energy_path_with_mm_model_host_side(monkeypatch):
             assert abs(t[name] - Emm[k]) < 1e-9
     assert abs(e - (t["Pure QC"] + t["QC/MM Elect."] + Emm.sum())) < 1e-9
     assert s.configuration.qcCharges.shape == (len(sel),) and abs(s.configuration.qcCharges.sum() - charge) < 1e-8
+
+
+def test_scf_failure_message_names_each_status():
+    from pdynamo_mirror_gb300 import _native
+    from pdynamo_mirror_gb300.system import SCFNotConverged, scf_failure_message
+    assert issubclass(SCFNotConverged, ValueError)
+    m = scf_failure_message([_native.PDG_OK, _native.PDG_NAN, _native.PDG_NOT_CONVERGED, _native.PDG_TENSOR_TIMEOUT, _native.PDG_NAN])
+    assert "non-finite energy in frames 1, 4" in m
+    assert "not converged in frame 2" in m
+    assert "tensor-core completion wait ran out in frame 3" in m

@@ -35,6 +35,34 @@ def test_static_scratch_gradients_match_workspace_path_twice():
         np.testing.assert_allclose(g.cpu().numpy(), ref, rtol=0, atol=TOL)
 
 
+def test_static_scratch_call_leaves_free_device_memory_unchanged():
+    """The property the entry point exists for: once a first call on the device has loaded the kernels and looked
+    up the scratch's address, a further call allocates no device memory.  Every buffer of the call exists before
+    it, so torch's caching allocator stays idle, and the driver's free-memory count (cudaMemGetInfo) must be the
+    same before and after."""
+    import torch
+    from pdynamo_mirror_gb300 import _native
+    from pdynamo_mirror_gb300.engine import ANGSTROMS_TO_BOHRS
+    eng, qc, P = _engine_and_densities(16, 6, seed=12)
+    xyz = (qc * ANGSTROMS_TO_BOHRS).contiguous()
+    g = torch.empty((qc.shape[0], eng.n_atoms, 3), dtype=torch.float64, device="cuda")
+    stream = _native.stream_handle(torch.cuda.current_stream())
+
+    def call():
+        _native.check(eng.L.pdg_gradients_static_scratch(eng.handle, qc.shape[0], _native.ptr(xyz), _native.ptr(P),
+                                                         _native.ptr(g), stream), "pdg_gradients_static_scratch")
+        torch.cuda.synchronize()
+
+    call()                                     # first call: kernels loaded, scratch address looked up
+    ref = g.clone()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    call()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 == free0, "the call changed free device memory by %d bytes" % (free0 - free1)
+    np.testing.assert_allclose(g.cpu().numpy(), ref.cpu().numpy(), rtol=0, atol=TOL)
+
+
 def test_static_scratch_rejects_requests_beyond_its_size():
     import torch
     from pdynamo_mirror_gb300 import _native, workloads
