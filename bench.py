@@ -706,6 +706,7 @@ def bench_water_box(args, world, rank):
         phases = []
         for _ in range(3):
             rr = step(events=True)
+            torch.cuda.synchronize()
             pt = eng.phase_times()
             ev = rr["events"]
             pt.update(qcmm_potentials=ev[0].elapsed_time(ev[1]), qcmm_gradients=ev[2].elapsed_time(ev[3]),
