@@ -229,20 +229,25 @@ int pdg_scf_timings(const pdg_system *sys, int n_frames, const void *d_workspace
  *          the spline is given by n_knots knots d_knots = [x (A^2) | y (a.u.) | y'' (second derivatives)].
  * Coordinates here are in Angstrom, as the reference evaluates these pair terms in Angstrom.
  *   d_qc_xyz  n_frames * n_qc * 3,  d_mm_xyz n_frames * n_mm * 3,  d_mm_charges n_mm (shared by frames)
- *   d_phi     out n_frames * n_qc potentials (a.u.) */
+ *   d_phi     out n_frames * n_qc potentials (a.u.)
+ *   d_workspace  at least pdg_qcmm_workspace_bytes(n_frames, n_mm) bytes, 256-byte aligned: each call first lists,
+ *             per frame, the MM atoms within the cutoff of any QC atom (in MM index order; the pair-list step of the
+ *             reference, whose cell-grid lists, PairListGenerator.c:414, serve the same purpose), and the pair
+ *             kernels scan that list.  Nothing in it is read before it is written; it need not persist between calls. */
+size_t pdg_qcmm_workspace_bytes(int n_frames, int n_mm);
 int pdg_qcmm_potentials(int model, int n_frames, int n_qc, int n_mm, const double *d_qc_xyz,
                         const double *d_mm_xyz, const double *d_mm_charges, int n_knots, const double *d_knots,
-                        double outer_cutoff, double *d_phi, void *stream);
+                        double outer_cutoff, double *d_phi, void *d_workspace, size_t workspace_bytes, void *stream);
 /* Gradients (Eh/Bohr) of q_A phi_A with respect to QC and MM coordinates for given QC charges.
  * d_qc_grad (n_frames*n_qc*3) and d_mm_grad (n_frames*n_mm*3) are overwritten; d_mm_grad may be NULL, and the
  * MM-side gradients are then not computed (dynamics with the MM atoms fixed never uses them).
  * model | PDG_QCMM_FP32_PAIRS evaluates the pair terms in FP32 (per-atom sums in FP64; errors ~1e-7 Hartree/Bohr,
- * used by the mixed method; the reference's arithmetic is FP64, which is the default here). */
+ * used by the mixed method; the reference's arithmetic is FP64, which is the default here).  Workspace as above. */
 #define PDG_QCMM_FP32_PAIRS 0x100
 int pdg_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const double *d_qc_xyz,
                        const double *d_mm_xyz, const double *d_mm_charges, const double *d_qc_charges,
                        int n_knots, const double *d_knots, double outer_cutoff,
-                       double *d_qc_grad, double *d_mm_grad, void *stream);
+                       double *d_qc_grad, double *d_mm_grad, void *d_workspace, size_t workspace_bytes, void *stream);
 
 /* Learned start density (no counterpart in the reference, whose SCF starts from the diagonal guess,
  * QCOnePDM.c:280, or from the previous density).  A per-atom-pair MLP (64 features -> 256 -> 256 -> 16, SiLU,

@@ -24,7 +24,7 @@ EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system
            "pdg_batch_info", "pdg_batch_workspace_bytes", "pdg_batch_schedule", "pdg_batch_energy_gradients", "pdg_batch_timings",
            "pdg_batch_graph_create", "pdg_graph_launch", "pdg_graph_destroy", "pdg_langevin_positions", "pdg_langevin_velocities",
            "pdg_normal_deviates", "pdg_density_combine", "pdg_mm_create", "pdg_mm_destroy", "pdg_mm_workspace_bytes",
-           "pdg_mm_energy_gradients", "pdg_phase_events", "pdg_phase_times", "pdg_last_error")
+           "pdg_mm_energy_gradients", "pdg_phase_events", "pdg_phase_times", "pdg_qcmm_workspace_bytes", "pdg_last_error")
 TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densities Tridiagonal", "QC Densities Eigenvalues",
           "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds",
           "QC Densities Cluster Rounds", "QC Densities Steps", "QC Densities Purification",
@@ -87,8 +87,10 @@ def load(path=LIB_PATH):
     L.pdg_mlp_adam.argtypes = [I, I, I, P, F, P, P, P, P, P, F, F, F, I, P]
     L.pdg_guess_assemble.argtypes = [P, I, P, P, P, P, P, P]
     L.pdg_guess_loss.argtypes = [P, I, P, P, P, P, P, P, P, P]
-    L.pdg_qcmm_potentials.argtypes = [I, I, I, I, P, P, P, I, P, D, P, P]
-    L.pdg_qcmm_gradients.argtypes = [I, I, I, I, P, P, P, P, I, P, D, P, P, P]
+    L.pdg_qcmm_workspace_bytes.argtypes = [I, I]
+    L.pdg_qcmm_workspace_bytes.restype = S
+    L.pdg_qcmm_potentials.argtypes = [I, I, I, I, P, P, P, I, P, D, P, P, S, P]
+    L.pdg_qcmm_gradients.argtypes = [I, I, I, I, P, P, P, P, I, P, D, P, P, P, S, P]
     LL = ctypes.c_longlong
     L.pdg_batch_create.argtypes = [P, I, PP]
     L.pdg_batch_destroy.argtypes = [P]
@@ -131,3 +133,4 @@ def ptr(t):
 
 def stream_handle(torch_stream):
     return ctypes.c_void_p(torch_stream.cuda_stream)
+

@@ -333,26 +333,46 @@ extern "C" int pdg_scf_timings(const pdg_system *s, int n_frames, const void *ws
     return PDG_OK;
 }
 
+extern "C" size_t pdg_qcmm_workspace_bytes(int n_frames, int n_mm)
+{
+    if (n_frames <= 0 || n_mm < 0) return 0;
+    return qcmm_workspace_bytes(n_frames, n_mm);
+}
+
+static int check_qcmm_workspace(int n_frames, int n_mm, void *ws, size_t bytes)
+{
+    if (!ws || bytes < qcmm_workspace_bytes(n_frames, n_mm)) return fail(PDG_BAD_ARGUMENT, "QC/MM workspace missing or too small");
+    if ((uintptr_t)ws % 256) return fail(PDG_BAD_ARGUMENT, "QC/MM workspace must be 256-byte aligned");
+    return PDG_OK;
+}
+
 extern "C" int pdg_qcmm_potentials(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,
-                                   const double *q, int n_knots, const double *knots, double cutoff, double *phi, void *stream)
+                                   const double *q, int n_knots, const double *knots, double cutoff, double *phi,
+                                   void *ws, size_t bytes, void *stream)
 {
     if (model != 0 && model != 1) return fail(PDG_BAD_ARGUMENT, "model must be 0 (full) or 1 (ABFS)");
     if (n_frames <= 0 || n_qc <= 0 || n_mm < 0 || !qc || !phi || (n_mm > 0 && (!mm || !q))) return fail(PDG_BAD_ARGUMENT, "bad sizes or null pointers");
+    if (n_qc > PDG_MAX_ATOMS) return fail(PDG_TOO_LARGE, "more QC atoms than PDG_MAX_ATOMS");
     if (model == 1 && (n_knots < 2 || !knots || cutoff <= 0.0)) return fail(PDG_BAD_ARGUMENT, "ABFS needs spline knots and a cutoff");
-    launch_qcmm_potentials(model, n_frames, n_qc, n_mm, qc, mm, q, n_knots, knots, cutoff, phi, (cudaStream_t)stream);
+    int rc = check_qcmm_workspace(n_frames, n_mm, ws, bytes);
+    if (rc) return rc;
+    launch_qcmm_potentials(model, n_frames, n_qc, n_mm, qc, mm, q, n_knots, knots, cutoff, phi, ws, (cudaStream_t)stream);
     return cuda_check(cudaGetLastError(), "qcmm potentials");
 }
 
 extern "C" int pdg_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,
                                   const double *q, const double *qcq, int n_knots, const double *knots, double cutoff,
-                                  double *gqc, double *gmm, void *stream)
+                                  double *gqc, double *gmm, void *ws, size_t bytes, void *stream)
 {
     const int base_model = model & ~PDG_QCMM_FP32_PAIRS;
     if ((base_model != 0 && base_model != 1) || (model & ~(PDG_QCMM_FP32_PAIRS | 1))) return fail(PDG_BAD_ARGUMENT, "model must be 0 (full) or 1 (ABFS), optionally | PDG_QCMM_FP32_PAIRS");
     if (model & PDG_QCMM_FP32_PAIRS && base_model == 1 && n_knots > 1024) return fail(PDG_TOO_LARGE, "FP32 pair terms take at most 1024 spline knots");
     if (n_frames <= 0 || n_qc <= 0 || n_mm < 0 || !qc || !qcq || !gqc || (n_mm > 0 && (!mm || !q))) return fail(PDG_BAD_ARGUMENT, "bad sizes or null pointers");
+    if (n_qc > PDG_MAX_ATOMS) return fail(PDG_TOO_LARGE, "more QC atoms than PDG_MAX_ATOMS");
     if (base_model == 1 && (n_knots < 2 || !knots || cutoff <= 0.0)) return fail(PDG_BAD_ARGUMENT, "ABFS needs spline knots and a cutoff");
-    launch_qcmm_gradients(model, n_frames, n_qc, n_mm, qc, mm, q, qcq, n_knots, knots, cutoff, gqc, gmm, (cudaStream_t)stream);
+    int rc = check_qcmm_workspace(n_frames, n_mm, ws, bytes);
+    if (rc) return rc;
+    launch_qcmm_gradients(model, n_frames, n_qc, n_mm, qc, mm, q, qcq, n_knots, knots, cutoff, gqc, gmm, ws, (cudaStream_t)stream);
     return cuda_check(cudaGetLastError(), "qcmm gradients");
 }
 

@@ -249,11 +249,12 @@ void launch_batch_gradients(const Batch &b, const double *xyz, const double *den
                             bool fp32_terms = false);
 #define PDG_SMEM_LIMIT_1 (220 * 1024)   // shared-memory budget of one SCF CTA alone on its SM
 #define PDG_SMEM_LIMIT_2 (112 * 1024)   // ... of each of two
+size_t qcmm_workspace_bytes(int n_frames, int n_mm);
 int launch_qcmm_potentials(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,
-                           const double *q, int n_knots, const double *knots, double cutoff, double *phi, cudaStream_t st);
+                           const double *q, int n_knots, const double *knots, double cutoff, double *phi, void *ws, cudaStream_t st);
 int launch_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,
                           const double *q, const double *qcq, int n_knots, const double *knots, double cutoff,
-                          double *gqc, double *gmm, cudaStream_t st);
+                          double *gqc, double *gmm, void *ws, cudaStream_t st);
 int launch_tc_selftest(int n, int kprod, int wait_limit, const float *x, float *c, int *status, cudaStream_t st);
 
 // SCF kernels (scf.cu), in two compiled variants: scf_n (256 threads per CTA, tensor-core step) and scf_w

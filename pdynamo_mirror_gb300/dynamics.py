@@ -176,9 +176,11 @@ class LangevinDynamics:
                 phi = torch.empty((self.R, eng.n_atoms), dtype=torch.float64, device=self.dev)
                 knots = eng.knots(self.nb) if self.nb.model_id == 1 else None
                 nk = 0 if knots is None else knots.numel() // 3
+                qws, qwb = eng.qcmm_workspace(self.R, self.mm_xyz.shape[1])
                 _native.check(eng.L.pdg_qcmm_potentials(self.nb.model_id, self.R, eng.n_atoms, self.mm_xyz.shape[1], _native.ptr(self.xyz),
                                                         _native.ptr(self.mm_xyz), _native.ptr(self.mm_q), nk, _native.ptr(knots),
-                                                        float(self.nb.outerCutoff), _native.ptr(phi), self._sh()), "pdg_qcmm_potentials")
+                                                        float(self.nb.outerCutoff), _native.ptr(phi), _native.ptr(qws), qwb, self._sh()),
+                              "pdg_qcmm_potentials")
             self.model_history = (self.model_history + [self.guess.predict(self.xyz, phi)])[-3:]
         warm = False
         if self.mode != "diagonal" and self.history:

@@ -45,6 +45,7 @@ class QCEngine:
         _native.check(self.L.pdg_system_info(h, ctypes.byref(nb), ctypes.byref(no), ctypes.byref(npair)), "pdg_system_info")
         self.n_atoms, self.n_basis, self.n_occupied, self.n_pairs = len(self.atomic_numbers), nb.value, no.value, npair.value
         self._ws, self._ws_frames = None, 0
+        self._qcmm_ws = None
         self.density = None          # device [F, N, N], kept between calls as the reference keeps its state
         self._knots = {}
 
@@ -61,6 +62,14 @@ class QCEngine:
             self._ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
             self._ws_frames = n_frames
         return self._ws
+
+    def qcmm_workspace(self, n_frames, n_mm):
+        """The device workspace of pdg_qcmm_potentials / pdg_qcmm_gradients (the per-frame near lists), grown as
+        needed: (tensor, bytes)."""
+        need = int(self.L.pdg_qcmm_workspace_bytes(int(n_frames), int(n_mm)))
+        if self._qcmm_ws is None or self._qcmm_ws.numel() < need:
+            self._qcmm_ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+        return self._qcmm_ws, self._qcmm_ws.numel()
 
     def knots(self, nbmodel):
         k = id(nbmodel)
@@ -95,9 +104,10 @@ class QCEngine:
             knots = self.knots(nbmodel) if nbmodel.model_id == 1 else None
             nk = 0 if knots is None else knots.numel() // 3
             phi = torch.empty((F, n), dtype=torch.float64, device=dev)
+            qws, qwb = self.qcmm_workspace(F, mm_xyz.shape[1])
             _native.check(self.L.pdg_qcmm_potentials(nbmodel.model_id, F, n, mm_xyz.shape[1], _native.ptr(qc_xyz), _native.ptr(mm_xyz),
                                                      _native.ptr(mm_charges), nk, _native.ptr(knots), float(nbmodel.outerCutoff),
-                                                     _native.ptr(phi), sh), "pdg_qcmm_potentials")
+                                                     _native.ptr(phi), _native.ptr(qws), qwb, sh), "pdg_qcmm_potentials")
         mark(1)
         xyz_bohr = (qc_xyz * ANGSTROMS_TO_BOHRS).contiguous()
         use = 1 if (warm_start and self.density is not None and self.density.shape[0] == F) else 0
@@ -125,7 +135,7 @@ class QCEngine:
             gmodel = nbmodel.model_id | (_native.QCMM_FP32_PAIRS if opts.density_step != 0 else 0)
             _native.check(self.L.pdg_qcmm_gradients(gmodel, F, n, mm_xyz.shape[1], _native.ptr(qc_xyz), _native.ptr(mm_xyz),
                                                     _native.ptr(mm_charges), _native.ptr(charges), nk, _native.ptr(knots),
-                                                    float(nbmodel.outerCutoff), _native.ptr(gqc), _native.ptr(gmm), sh),
+                                                    float(nbmodel.outerCutoff), _native.ptr(gqc), _native.ptr(gmm), _native.ptr(qws), qwb, sh),
                           "pdg_qcmm_gradients")
             out.update(qcmm_qc_gradients=gqc, qcmm_mm_gradients=gmm)
         mark(3)

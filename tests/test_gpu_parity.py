@@ -182,13 +182,15 @@ def test_qcmm_potentials_and_gradients_match_oracle(model):
     nk = 0 if kn is None else kn.numel() // 3
     phi = torch.empty((1, nq), dtype=torch.float64, device="cuda")
     s = _native.stream_handle(torch.cuda.current_stream())
+    wb = int(L.pdg_qcmm_workspace_bytes(1, len(Q) - nq))
+    ws = torch.empty(wb, dtype=torch.uint8, device="cuda")
     _native.check(L.pdg_qcmm_potentials(nb.model_id, 1, nq, len(Q) - nq, _native.ptr(dq), _native.ptr(dm), _native.ptr(dc), nk,
-                                        _native.ptr(kn), float(nb.outerCutoff), _native.ptr(phi), s), "potentials")
+                                        _native.ptr(kn), float(nb.outerCutoff), _native.ptr(phi), _native.ptr(ws), wb, s), "potentials")
     gq = torch.empty((1, nq, 3), dtype=torch.float64, device="cuda")
     gm = torch.empty((1, len(Q) - nq, 3), dtype=torch.float64, device="cuda")
     _native.check(L.pdg_qcmm_gradients(nb.model_id, 1, nq, len(Q) - nq, _native.ptr(dq), _native.ptr(dm), _native.ptr(dc),
                                        _native.ptr(_dev(qcq[None])), nk, _native.ptr(kn), float(nb.outerCutoff),
-                                       _native.ptr(gq), _native.ptr(gm), s), "gradients")
+                                       _native.ptr(gq), _native.ptr(gm), _native.ptr(ws), wb, s), "gradients")
     np.testing.assert_allclose(phi[0].cpu().numpy(), phi_o, rtol=0, atol=1e-11)
     np.testing.assert_allclose(gq[0].cpu().numpy(), gq_o, rtol=0, atol=1e-11)
     np.testing.assert_allclose(gm[0].cpu().numpy(), gm_o, rtol=0, atol=1e-11)

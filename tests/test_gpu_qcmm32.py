@@ -25,12 +25,15 @@ def test_fp32_pair_gradients_match_fp64(model):
     knots = torch.as_tensor(NBModelABFS(innerCutoff=8.0, outerCutoff=12.0).knots(), dtype=torch.float64, device="cuda") if model == 1 else None
     nk = 0 if knots is None else knots.numel() // 3
     sh = _native.stream_handle(torch.cuda.current_stream())
+    wb = int(L.pdg_qcmm_workspace_bytes(4, mm.shape[1]))
+    ws = torch.empty(wb, dtype=torch.uint8, device="cuda")
     out = {}
     for flag in (0, _native.QCMM_FP32_PAIRS):
         gq = torch.empty((4, nq, 3), dtype=torch.float64, device="cuda")
         gm = torch.empty((4, mm.shape[1], 3), dtype=torch.float64, device="cuda")
         _native.check(L.pdg_qcmm_gradients(model | flag, 4, nq, mm.shape[1], _native.ptr(qc), _native.ptr(mm), _native.ptr(q), _native.ptr(qcq),
-                                           nk, _native.ptr(knots), 12.0, _native.ptr(gq), _native.ptr(gm), sh), "pdg_qcmm_gradients")
+                                           nk, _native.ptr(knots), 12.0, _native.ptr(gq), _native.ptr(gm), _native.ptr(ws), wb, sh),
+                      "pdg_qcmm_gradients")
         out[flag] = (gq.cpu().numpy(), gm.cpu().numpy())
     (gq64, gm64), (gq32, gm32) = out[0], out[_native.QCMM_FP32_PAIRS]
     assert np.abs(gq64).max() > 1e-3 and np.abs(gm64).max() > 1e-4
