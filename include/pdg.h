@@ -391,6 +391,29 @@ size_t pdg_mm_workspace_bytes(const pdg_mm_system *m, int n_frames);
 int pdg_mm_energy_gradients(const pdg_mm_system *m, int n_frames, const double *d_xyz, double *d_energies, double *d_gradients,
                             void *d_workspace, size_t workspace_bytes, void *stream);
 
+/* ---- One large QC region over the whole GPU ----
+ * pdg_energy_gradients gives each frame one CTA (one SM): the throughput form for many frames of a small region.  A
+ * single large region (hundreds of atoms, N up to PDG_MAX_BASIS) is computed here with every SCF phase spread over all
+ * SMs: the Fock build and the DIIS/ODA vector work as grid-wide kernels, the FP64 density step as a Householder
+ * tridiagonalisation of two grid-wide kernels per column (replayed from a CUDA graph), bisection and inverse iteration
+ * for the wanted eigenpairs, and a blocked compact-WY back-transformation and density by DGEMM; the integrals and
+ * gradients are the pair kernels of pdg_energy_gradients on this one frame.  The results are those of
+ * pdg_energy_gradients for the same frame (QCModel.Energy + EnergyGradients, pMolecule.QCModel.pyx:146-185), by the
+ * reference's FP64 method whatever options->density_step asks.
+ *   pdg_wide_create       a wide engine for sys (which must outlive it); holds a cuBLAS handle and, after the first
+ *                         call, the tridiagonalisation graph of the workspace it was given
+ *   pdg_wide_workspace_bytes   the workspace one call needs (256-byte aligned)
+ *   pdg_wide_energy_gradients  one frame, arguments as pdg_energy_gradients with n_frames = 1.  The call waits for the
+ *                         stream at every SCF cycle (the host reads the converger's state to decide whether to go on),
+ *                         so it returns after the work is done; do not capture it in a CUDA graph. */
+typedef struct pdg_wide pdg_wide;
+int pdg_wide_create(pdg_system *sys, pdg_wide **out);
+int pdg_wide_destroy(pdg_wide *wide);
+size_t pdg_wide_workspace_bytes(const pdg_system *sys);
+int pdg_wide_energy_gradients(pdg_wide *wide, const double *d_xyz, const double *d_phi, const pdg_scf_options *options,
+                              double *d_density, int use_density, double *d_energies, double *d_gradients, double *d_charges,
+                              int *d_status, int *d_ncycles, void *d_workspace, size_t workspace_bytes, void *stream);
+
 /* Text of the last error on this host thread (never NULL). */
 const char *pdg_last_error(void);
 

@@ -24,7 +24,8 @@ EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system
            "pdg_batch_info", "pdg_batch_workspace_bytes", "pdg_batch_schedule", "pdg_batch_energy_gradients", "pdg_batch_timings",
            "pdg_batch_graph_create", "pdg_graph_launch", "pdg_graph_destroy", "pdg_langevin_positions", "pdg_langevin_velocities",
            "pdg_normal_deviates", "pdg_density_combine", "pdg_mm_create", "pdg_mm_destroy", "pdg_mm_workspace_bytes",
-           "pdg_mm_energy_gradients", "pdg_phase_events", "pdg_phase_times", "pdg_qcmm_workspace_bytes", "pdg_last_error")
+           "pdg_mm_energy_gradients", "pdg_phase_events", "pdg_phase_times", "pdg_qcmm_workspace_bytes", "pdg_wide_create", "pdg_wide_destroy",
+           "pdg_wide_workspace_bytes", "pdg_wide_energy_gradients", "pdg_last_error")
 TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densities Tridiagonal", "QC Densities Eigenvalues",
           "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds",
           "QC Densities Cluster Rounds", "QC Densities Steps", "QC Densities Purification",
@@ -76,6 +77,11 @@ def load(path=LIB_PATH):
     L.pdg_gradients.argtypes = [P, I, P, P, P, P, S, P]
     L.pdg_scf_timings.argtypes = [P, I, P, S, P, P]
     L.pdg_phase_events.argtypes = [P, I]
+    L.pdg_wide_create.argtypes = [P, PP]
+    L.pdg_wide_destroy.argtypes = [P]
+    L.pdg_wide_workspace_bytes.argtypes = [P]
+    L.pdg_wide_workspace_bytes.restype = S
+    L.pdg_wide_energy_gradients.argtypes = [P, P, P, ctypes.POINTER(SCFOptions), P, I, P, P, P, P, P, P, S, P]
     L.pdg_phase_times.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
     L.pdg_gradients_static_scratch.argtypes = [P, I, P, P, P, P]
     L.pdg_tc_selftest.argtypes = [I, I, I, P, P, P, P]

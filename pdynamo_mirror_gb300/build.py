@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libpdg.so")
-UNITS = ("api.cu", "integrals.cu", "scf.cu", "scf_wide.cu", "qcmm.cu", "tc.cu", "guess.cu", "dynamics.cu", "mmmm.cu")
+UNITS = ("api.cu", "integrals.cu", "scf.cu", "scf_wide.cu", "qcmm.cu", "tc.cu", "guess.cu", "dynamics.cu", "mmmm.cu", "wide.cu")
 HEADERS = ("common.cuh", "multipole.cuh", "overlap.cuh", "tc.cuh")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-diag-suppress", "177"]
@@ -58,7 +58,7 @@ def build(force=False, verbose=False):
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         list(ex.map(compile_one, zip(UNITS, objs)))
     tmp = LIB + ".tmp"
-    r = subprocess.run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"], capture_output=True, text=True)
+    r = subprocess.run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lcublas"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
     os.replace(tmp, LIB)

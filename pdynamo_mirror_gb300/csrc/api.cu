@@ -262,6 +262,41 @@ extern "C" int pdg_phase_times(const pdg_system *s, float *h_ms)
     return rc;
 }
 
+extern "C" int pdg_wide_create(pdg_system *s, pdg_wide **out)
+{
+    if (!s || !out) return fail(PDG_BAD_ARGUMENT, "null argument");
+    if (s->d.n_basis < 3) return fail(PDG_BAD_ARGUMENT, "pdg_wide_create: the wide engine needs at least 3 basis functions");
+    int rc = wide_create(s->d, out);
+    if (rc) return fail(rc, "pdg_wide_create: cuBLAS handle");
+    return PDG_OK;
+}
+
+extern "C" int pdg_wide_destroy(pdg_wide *w)
+{
+    wide_destroy(w);
+    return PDG_OK;
+}
+
+extern "C" size_t pdg_wide_workspace_bytes(const pdg_system *s)
+{
+    return s ? wide_workspace_bytes(s->d) : 0;
+}
+
+extern "C" int pdg_wide_energy_gradients(pdg_wide *w, const double *d_xyz, const double *d_phi, const pdg_scf_options *o,
+                                         double *d_density, int use_density, double *d_energies, double *d_gradients, double *d_charges,
+                                         int *d_status, int *d_ncycles, void *ws, size_t bytes, void *stream)
+{
+    if (!w || !o || !d_xyz || !d_density || !d_energies || !d_status) return fail(PDG_BAD_ARGUMENT, "null argument");
+    if (o->history < 1 || o->history > PDG_MAX_HISTORY) return fail(PDG_BAD_ARGUMENT, "history must be 1..16");
+    if (o->maximum_scf_cycles < 0) return fail(PDG_BAD_ARGUMENT, "maximum_scf_cycles must be >= 0");
+    if (!ws || (uintptr_t)ws % 256) return fail(PDG_BAD_ARGUMENT, "wide workspace missing or not 256-byte aligned");
+    if (bytes < wide_workspace_size(w)) return fail(PDG_BAD_ARGUMENT, "wide workspace too small");
+    const int rc = wide_energy_gradients(w, d_xyz, d_phi, *o, d_density, use_density, d_energies, d_gradients, d_charges, d_status,
+                                         d_ncycles, (double *)ws, (cudaStream_t)stream);
+    if (rc) return fail(rc, "pdg_wide_energy_gradients: a kernel, a cuBLAS call or a stream wait failed");
+    return cuda_check(cudaGetLastError(), "wide SCF");
+}
+
 extern "C" int pdg_scf(pdg_system *s, int n_frames, const double *d_phi, const pdg_scf_options *o, double *d_density,
                        int use_density, double *d_energies, double *d_charges, int *d_status, int *d_ncycles,
                        void *ws, size_t bytes, void *stream)

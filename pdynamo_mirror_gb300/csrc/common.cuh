@@ -250,6 +250,13 @@ void launch_batch_gradients(const Batch &b, const double *xyz, const double *den
 #define PDG_SMEM_LIMIT_1 (220 * 1024)   // shared-memory budget of one SCF CTA alone on its SM
 #define PDG_SMEM_LIMIT_2 (112 * 1024)   // ... of each of two
 size_t qcmm_workspace_bytes(int n_frames, int n_mm);
+// One large QC region's SCF over the whole GPU (wide.cu).
+size_t wide_workspace_bytes(const DeviceSystem &s);
+int wide_create(const DeviceSystem &s, pdg_wide **out);
+size_t wide_workspace_size(const pdg_wide *W);
+void wide_destroy(pdg_wide *W);
+int wide_energy_gradients(pdg_wide *W, const double *xyz, const double *phi, const pdg_scf_options &o, double *P, int use_density,
+                          double *energies, double *gradients, double *charges, int *status, int *ncycles, double *ws, cudaStream_t st);
 int launch_qcmm_potentials(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,
                            const double *q, int n_knots, const double *knots, double cutoff, double *phi, void *ws, cudaStream_t st);
 int launch_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const double *qc, const double *mm,

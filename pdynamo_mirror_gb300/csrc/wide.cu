@@ -1,0 +1,970 @@
+// wide.cu - the SCF of ONE large QC region spread over the whole GPU (pdg_wide_*, include/pdg.h).
+//
+// The single-frame kernel of scf.cu gives one CTA to each frame: right for many small frames, but a 600-atom region
+// (N = 1200) would run its O(N^3) density steps on one SM.  Here every phase of one SCF cycle is a grid-wide
+// kernel (or a cuBLAS GEMM for the dense products), queued by the host on one stream; the converger's scalar state
+// lives on the device, and the host reads one small control record per cycle to decide whether to go on.
+//
+//   Fock build        F = H + G(P) (QCModelMNDO_Fock, QCModelMNDO.c:700; G of MNDOIntegrals_MakeFockG,
+//                     MNDOIntegrals.c:51, as J/K block contractions, one thread per output element), traces and the
+//                     Lowdin QC/MM term (QCModelMNDO_QCMMFockLowdin, :1808)
+//   DIIS / ODA        DIIS_Fock_Save (DIISSCFConverger.c:385: e = F P - P F by GEMMs on the last step's
+//                     eigenvectors), DIIS_Iterate (:530; bordered solve with drop-oldest), RCA_Iterate (:661), the mode
+//                     switching of IterateWithoutDensities (:147) and the convergence test (:116)
+//   density step      QCOnePDM_MakeFromFock (QCOnePDM.c:403) as in scf.cu but grid-wide: Householder
+//                     tridiagonalisation (two kernels per column, replayed from a CUDA graph), FP64 bisection for the
+//                     min(n_occ, N - n_occ) wanted eigenvalues, inverse iteration (one thread per vector,
+//                     re-orthogonalised inside clusters of close eigenvalues), blocked compact-WY back-transformation
+//                     and P = 2 Z Z^T or 2 (1 - Z Z^T) by DGEMM.
+// The integrals and the gradients are the batch kernels of integrals.cu run on this one frame (their grids span the
+// frame's atom pairs).  Reductions are taken in a fixed order, so results do not depend on timing.
+#include "common.cuh"
+#include "multipole.cuh"
+#include <cublas_v2.h>
+#include <vector>
+#include <cstring>
+
+namespace wide {
+
+#define WB 256                 // threads per block of the grid-wide kernels
+#define WW (WB / 32)
+#define WMAXH PDG_MAX_HISTORY
+#define WNB 32                 // reflectors per back-transformation block
+
+// Converger state on the device (one per wide object), read by the host after every cycle's control kernel.
+struct Ctl {
+    int iteration, converged, status, ncyc, valid, have_z, qdiis, qrca, matnum, newest, good, do_extrap, do_oda, done;
+    int slots[WMAXH];
+    double eold, deltaeold, rms, eel, e1, e2, eq, etemp, deltae, maxerr, mu, enuc, base;
+    double cf[WMAXH];
+    double B[WMAXH * WMAXH];
+};
+
+// Workspace plan (doubles from the base): the frame plan of the integral and gradient kernels first, then the
+// regions of the grid-wide SCF.
+struct WPlan {
+    FramePlan fp;   // only tei, pair_e, pair_g and H (the integral and gradient kernels' regions) are laid out
+    size_t F, A, C, rP, rF, hP, hF, hE, Zc, G, colbuf, vbuf, q, pk, part, d, e, tau, eig, cst, lu, y, vb, sb, tb, wb, ctl, total;
+    int kvp;   // vectors rounded up to 32 (interleaved inverse-iteration arrays)
+    int parts; // partial-sum slots per reduction
+};
+
+__host__ inline WPlan wide_plan(const DeviceSystem &s)
+{
+    WPlan w;
+    std::memset(&w, 0, sizeof(w));
+    const size_t N = s.n_basis, NN = N * N, kv = s.n_vec > 0 ? s.n_vec : 1;
+    w.kvp = (int)((kv + 31) & ~size_t(31));
+    w.parts = 1024;
+    size_t o = 0;
+    auto take = [&](size_t n) { size_t r = o; o += align32(n); return r; };
+    w.fp.tei = take(s.tei_total);
+    w.fp.pair_e = take((size_t)s.n_pairs * PDG_PAIR_E_STRIDE);
+    w.fp.pair_g = take((size_t)s.n_pairs * 3);
+    w.fp.H = take(NN);
+    w.fp.stride = o;
+    w.F = take(NN); w.A = take(NN); w.C = take(NN); w.rP = take(NN); w.rF = take(NN);
+    w.hP = take(WMAXH * NN); w.hF = take(WMAXH * NN); w.hE = take(WMAXH * NN);
+    w.Zc = take(N * kv); w.G = take(N * kv);
+    w.colbuf = take(N); w.vbuf = take(N); w.q = take(N); w.pk = take((size_t)s.n_cel + 1);
+    w.part = take((size_t)w.parts * 32);
+    w.d = take(N); w.e = take(N); w.tau = take(N); w.eig = take(N); w.cst = take(N / 2 + 2);
+    w.lu = take(5 * N * (size_t)w.kvp + (N * (size_t)w.kvp + 7) / 8);
+    w.y = take(N * (size_t)w.kvp);
+    w.vb = take(N * WNB); w.sb = take(WNB * WNB); w.tb = take(WNB * WNB); w.wb = take(WNB * kv);
+    w.ctl = take((sizeof(Ctl) + 7) / 8);
+    w.total = align32(o);
+    return w;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Deterministic partial sums: every block writes its partials to part[slot * parts + block]; single-block kernels sum
+// them in block order.
+__device__ __forceinline__ double block_reduce(double v, double *red)
+{
+    return block_sum(v, red);
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Fock build.  pk: one-centre densities of every atom with the off-diagonal factor 2 (the Coulomb right-hand sides).
+__global__ void __launch_bounds__(WB) k_pk(DeviceSystem s, const double *__restrict__ P, double *__restrict__ pk)
+{
+    const int N = s.n_basis;
+    for (int e = blockIdx.x * WB + threadIdx.x; e < s.n_cel; e += gridDim.x * WB) {
+        const int A = s.cel[e] >> 4, ab = s.cel[e] & 15, as = s.atom_start[A];
+        const int m = MP_DA[ab], n = MP_DB[ab];
+        pk[e] = (m == n ? 1.0 : 2.0) * P[(size_t)(as + m) * N + as + n];
+    }
+}
+
+__global__ void __launch_bounds__(WB) k_fock(DeviceSystem s, const double *__restrict__ H, const double *__restrict__ P,
+                                             const double *__restrict__ tei, const double *__restrict__ pk, double *__restrict__ F)
+{
+    const int N = s.n_basis, n_out = s.n_cel + s.n_xel;
+    for (int e = blockIdx.x * WB + threadIdx.x; e < n_out; e += gridDim.x * WB) {
+        if (e < s.n_cel) {
+            const int A = s.cel[e] >> 4, ab = s.cel[e] & 15;
+            const int no = s.atom_norb[A], as = s.atom_start[A], na = no * (no + 1) / 2;
+            const int m = MP_DA[ab], n = MP_DB[ab];
+            double acc = 0.0;
+            for (int B = 0; B < s.n_atoms; B++) {
+                if (B == A) continue;
+                const int hi = A > B ? A : B, lo = A > B ? B : A, pp = hi * (hi - 1) / 2 + lo;
+                const int k0 = s.atom_pk[B], nb = s.atom_pk[B + 1] - k0;
+                const double *blk = tei + s.pair_tei[pp], *pb = pk + k0;
+                if (A > B) for (int cd = 0; cd < nb; cd++) acc = fma(blk[ab * nb + cd], pb[cd], acc);
+                else       for (int cd = 0; cd < nb; cd++) acc = fma(blk[cd * na + ab], pb[cd], acc);
+            }
+            const double *E = elem(s, s.atom_elem[A]);
+            const double gss = E[PDG_E_GSS], gsp = E[PDG_E_GSP], gpp = E[PDG_E_GPP], gp2 = E[PDG_E_GP2], hsp = E[PDG_E_HSP], hpp = E[PDG_E_HPP];
+            const double *PA = P + (size_t)as * N + as;
+            double g = 0.0;
+            if (no == 1) g = 0.5 * PA[0] * gss;
+            else if (m == 0 && n == 0) { g = 0.5 * PA[0] * gss; for (int q = 1; q < 4; q++) g += PA[q * N + q] * (gsp - 0.5 * hsp); }
+            else if (m == n) {
+                g = PA[0] * (gsp - 0.5 * hsp) + 0.5 * PA[m * N + m] * gpp;
+                for (int q = 1; q < 4; q++) if (q != m) g += PA[q * N + q] * (gp2 - 0.5 * hpp);
+            } else if (n == 0) g = PA[m * N + n] * (1.5 * hsp - 0.5 * gsp);
+            else g = PA[m * N + n] * (1.5 * hpp - 0.5 * gp2);
+            const double v = H[(size_t)(as + m) * N + as + n] + g + acc;
+            F[(size_t)(as + m) * N + as + n] = v;
+            F[(size_t)(as + n) * N + as + m] = v;
+        } else {
+            const int x = s.xel[e - s.n_cel], pp = x >> 4, lid = x & 15;
+            const int i = s.pair_i[pp], j = s.pair_j[pp];
+            const int noi = s.atom_norb[i], noj = s.atom_norb[j], is = s.atom_start[i], js = s.atom_start[j];
+            const int nj = noj * (noj + 1) / 2, aa = lid / noj, c = lid % noj;
+            const double *blk = tei + s.pair_tei[pp];
+            double t = 0.0;
+            for (int b = 0; b < noi; b++) {
+                const int ab = aa >= b ? aa * (aa + 1) / 2 + b : b * (b + 1) / 2 + aa;
+                for (int d = 0; d < noj; d++) {
+                    const int cd = c >= d ? c * (c + 1) / 2 + d : d * (d + 1) / 2 + c;
+                    t = fma(blk[ab * nj + cd], P[(size_t)(is + b) * N + js + d], t);
+                }
+            }
+            const double v = fma(-0.5, t, H[(size_t)(is + aa) * N + js + c]);
+            F[(size_t)(is + aa) * N + js + c] = v;
+            F[(size_t)(js + c) * N + is + aa] = v;
+        }
+    }
+}
+
+// tr(P H) and tr(P F) over the lower triangle (off-diagonal and diagonal parts apart, as scf.cu), one warp per row;
+// block partials to part slots 0..3.
+__global__ void __launch_bounds__(WB) k_traces(int N, const double *__restrict__ P, const double *__restrict__ H,
+                                               const double *__restrict__ F, double *__restrict__ part, int parts)
+{
+    __shared__ double red[32];
+    const int lane = threadIdx.x & 31, gw = blockIdx.x * WW + (threadIdx.x >> 5), nw = gridDim.x * WW;
+    double th = 0.0, tf = 0.0, dh = 0.0, df = 0.0;
+    for (int i = gw; i < N; i += nw)
+        for (int j = lane; j <= i; j += 32) {
+            const size_t k = (size_t)i * N + j;
+            const double pv = P[k];
+            if (j < i) { th = fma(pv, H[k], th); tf = fma(pv, F[k], tf); }
+            else { dh = fma(pv, H[k], dh); df = fma(pv, F[k], df); }
+        }
+    th = block_reduce(th, red); tf = block_reduce(tf, red); dh = block_reduce(dh, red); df = block_reduce(df, red);
+    if (threadIdx.x == 0) {
+        part[0 * parts + blockIdx.x] = th; part[1 * parts + blockIdx.x] = tf;
+        part[2 * parts + blockIdx.x] = dh; part[3 * parts + blockIdx.x] = df;
+    }
+}
+
+// Lowdin charges q_A = Z_A - sum P_mm and the QC/MM term: F_mm -= phi_A, partial q . phi to part slot 4 (one block).
+__global__ void __launch_bounds__(WB) k_lowdin(DeviceSystem s, const double *__restrict__ P, const double *__restrict__ phi,
+                                               double *__restrict__ F, double *__restrict__ charges, double *__restrict__ part, int parts)
+{
+    __shared__ double red[32];
+    const int N = s.n_basis;
+    double tq = 0.0;
+    for (int A = threadIdx.x; A < s.n_atoms; A += WB) {
+        const int no = s.atom_norb[A], as = s.atom_start[A];
+        double ps = 0.0;
+        for (int m = 0; m < no; m++) ps += P[(size_t)(as + m) * N + as + m];
+        const double q = elem(s, s.atom_elem[A])[PDG_E_ZCORE] - ps;
+        if (charges) charges[A] = q;
+        if (phi) {
+            tq += q * phi[A];
+            for (int m = 0; m < no; m++) F[(size_t)(as + m) * N + as + m] -= phi[A];
+        }
+    }
+    tq = block_reduce(tq, red);
+    if (threadIdx.x == 0) part[4 * parts] = tq;
+}
+
+__device__ __forceinline__ double sum_parts(const double *part, int slot, int parts, int nb)
+{
+    double t = 0.0;
+    for (int b = 0; b < nb; b++) t += part[(size_t)slot * parts + b];
+    return t;
+}
+
+// Control after the Fock build (one thread): energies, the convergence test (DIISSCFConverger_Converged,
+// DIISSCFConverger.c:116-121, signed deltaeold), the DIIS slot of this cycle.
+__global__ void k_control_fock(Ctl *c, const double *__restrict__ part, int parts, int nb_traces, pdg_scf_options o, int hist)
+{
+    if (threadIdx.x != 0) return;
+    const double th = sum_parts(part, 0, parts, nb_traces), tf = sum_parts(part, 1, parts, nb_traces);
+    const double dh = sum_parts(part, 2, parts, nb_traces), df = sum_parts(part, 3, parts, nb_traces);
+    const double e1 = 2.0 * th + dh, e2 = 0.5 * ((2.0 * tf + df) - e1), eq = part[4 * parts];
+    c->e1 = e1; c->e2 = e2; c->eq = eq; c->eel = e1 + e2 + eq;
+    c->ncyc++;
+    if (!isfinite(c->eel)) { c->status = PDG_NAN; c->done = 1; return; }
+    c->converged = (c->iteration > 0) && (c->rms <= o.density_tolerance) && (c->deltaeold <= o.energy_tolerance);
+    if (c->converged) { c->status = PDG_OK; c->done = 1; return; }
+    c->deltae = c->eel - c->eold; c->etemp = c->eel;
+    if (c->valid) {
+        int mn = c->matnum, newest;
+        if (mn < hist) { mn++; newest = c->slots[mn - 1]; }
+        else { mn = hist; newest = c->slots[0]; for (int i = 0; i < hist - 1; i++) c->slots[i] = c->slots[i + 1]; c->slots[hist - 1] = newest; }
+        c->matnum = mn; c->newest = newest;
+    }
+}
+
+// DIIS history: P and F into the newest slot (dense).
+__global__ void __launch_bounds__(WB) k_pack(size_t NN, const Ctl *c, const double *__restrict__ P, const double *__restrict__ F,
+                                             double *__restrict__ hP, double *__restrict__ hF)
+{
+    const size_t off = (size_t)c->newest * NN;
+    for (size_t k = (size_t)blockIdx.x * WB + threadIdx.x; k < NN; k += (size_t)gridDim.x * WB) { hP[off + k] = P[k]; hF[off + k] = F[k]; }
+}
+
+// Error vector from C: e_ij = sg (C_ij - C_ji) for i > j (C = G Z^T with G = F Z, or C = F P), into the newest slot
+// (strict lower triangle, dense row-major positions); block maxima to part slot 5.
+__global__ void __launch_bounds__(WB) k_error(int N, const Ctl *c, const double *__restrict__ C, double sg, double *__restrict__ hE,
+                                              double *__restrict__ part, int parts)
+{
+    __shared__ double red[32];
+    double *he = hE + (size_t)c->newest * N * N;
+    const int lane = threadIdx.x & 31, gw = blockIdx.x * WW + (threadIdx.x >> 5), nw = gridDim.x * WW;
+    double mx = 0.0;
+    for (int i = gw; i < N; i += nw)
+        for (int j = lane; j < i; j += 32) {
+            const double ev = sg * (C[(size_t)i * N + j] - C[(size_t)j * N + i]);
+            he[(size_t)i * N + j] = ev;
+            mx = fmax(mx, fabs(ev));
+        }
+    mx = block_max(mx, red);
+    if (threadIdx.x == 0) part[5 * parts + blockIdx.x] = mx;
+}
+
+// B-matrix row: dots of the newest error vector with every stored one (strict lower triangles), block partials to
+// part slots 8 + m.
+__global__ void __launch_bounds__(WB) k_dots(int N, const Ctl *c, const double *__restrict__ hE, double *__restrict__ part, int parts)
+{
+    __shared__ double red[32];
+    const int lane = threadIdx.x & 31, gw = blockIdx.x * WW + (threadIdx.x >> 5), nw = gridDim.x * WW;
+    const size_t NN = (size_t)N * N;
+    const double *en = hE + (size_t)c->newest * NN;
+    const int mn = c->matnum;
+    double acc[WMAXH];
+    for (int m = 0; m < WMAXH; m++) acc[m] = 0.0;
+    for (int i = gw; i < N; i += nw)
+        for (int j = lane; j < i; j += 32) {
+            const size_t k = (size_t)i * N + j;
+            const double v = en[k];
+            for (int m = 0; m < mn; m++) acc[m] = fma(hE[(size_t)c->slots[m] * NN + k], v, acc[m]);
+        }
+    for (int m = 0; m < mn; m++) {
+        const double t = block_reduce(acc[m], red);
+        if (threadIdx.x == 0) part[(size_t)(8 + m) * parts + blockIdx.x] = t;
+    }
+}
+
+// ODA traces t1..t4 = F.P, F.rP, rF.P, rF.rP (full matrices), block partials to part slots 24..27.
+__global__ void __launch_bounds__(WB) k_oda_traces(size_t NN, const double *__restrict__ F, const double *__restrict__ P,
+                                                   const double *__restrict__ rF, const double *__restrict__ rP, double *__restrict__ part, int parts)
+{
+    __shared__ double red[32];
+    double t1 = 0, t2 = 0, t3 = 0, t4 = 0;
+    for (size_t k = (size_t)blockIdx.x * WB + threadIdx.x; k < NN; k += (size_t)gridDim.x * WB) {
+        t1 += F[k] * P[k]; t2 += F[k] * rP[k]; t3 += rF[k] * P[k]; t4 += rF[k] * rP[k];
+    }
+    t1 = block_reduce(t1, red); t2 = block_reduce(t2, red); t3 = block_reduce(t3, red); t4 = block_reduce(t4, red);
+    if (threadIdx.x == 0) {
+        part[24 * parts + blockIdx.x] = t1; part[25 * parts + blockIdx.x] = t2;
+        part[26 * parts + blockIdx.x] = t3; part[27 * parts + blockIdx.x] = t4;
+    }
+}
+
+// Small dense solve A x = b (n <= 17) by one warp: Gauss-Jordan with partial pivoting, rejecting a reciprocal
+// 1-norm condition below 1e-15 (SymmetricMatrix_SolveLinearEquations' test, SymmetricMatrix.c:1412-1450).
+__device__ bool warp_solve(int n, const double *Ain, const double *bin, double *M, double *x)
+{
+    const int lane = threadIdx.x & 31, w2 = 2 * n + 1;
+    for (int e = lane; e < n * w2; e += 32) {
+        const int i = e / w2, j = e % w2;
+        M[e] = j < n ? Ain[i * n + j] : (j < 2 * n ? (j - n == i ? 1.0 : 0.0) : bin[i]);
+    }
+    __syncwarp();
+    double cs = 0.0;
+    if (lane < n) for (int i = 0; i < n; i++) cs += fabs(M[i * w2 + lane]);
+    const double anorm = warp_max(cs);
+    for (int k = 0; k < n; k++) {
+        double v = (lane >= k && lane < n) ? fabs(M[lane * w2 + k]) : -1.0;
+        int iv = lane;
+        for (int off = 16; off > 0; off >>= 1) {
+            const double v2 = __shfl_xor_sync(0xffffffffu, v, off);
+            const int i2 = __shfl_xor_sync(0xffffffffu, iv, off);
+            if (v2 > v || (v2 == v && i2 < iv)) { v = v2; iv = i2; }
+        }
+        if (v == 0.0) return false;
+        if (iv != k)
+            for (int j = lane; j < w2; j += 32) { const double t = M[k * w2 + j]; M[k * w2 + j] = M[iv * w2 + j]; M[iv * w2 + j] = t; }
+        __syncwarp();
+        const double r = 1.0 / M[k * w2 + k];
+        const double fi = lane < n ? M[lane * w2 + k] * r : 0.0;
+        const double pk0 = lane < w2 ? M[k * w2 + lane] : 0.0, pk1 = lane + 32 < w2 ? M[k * w2 + lane + 32] : 0.0;
+        __syncwarp();
+        for (int i = 0; i < n; i++) {
+            const double f = __shfl_sync(0xffffffffu, fi, i);
+            if (i == k) continue;
+            if (lane < w2) M[i * w2 + lane] = fma(-f, pk0, M[i * w2 + lane]);
+            if (lane + 32 < w2) M[i * w2 + lane + 32] = fma(-f, pk1, M[i * w2 + lane + 32]);
+        }
+        __syncwarp();
+    }
+    double ci = 0.0;
+    if (lane < n) for (int i = 0; i < n; i++) ci += fabs(M[i * w2 + n + lane] / M[i * w2 + i]);
+    const double inorm = warp_max(ci);
+    if (lane < n) x[lane] = M[lane * w2 + 2 * n] / M[lane * w2 + lane];
+    __syncwarp();
+    return anorm * inorm < 1.0e15;
+}
+
+// Control after the DIIS save (one warp): the B-matrix row, the mode switch (RCA_ONSET 0.8, diisOnset), the DIIS
+// solve with drop-oldest, or the ODA step length from the four traces (DIISSCFConverger.c:661-760).
+__global__ void k_control_diis(Ctl *c, const double *__restrict__ part, int parts, int nb, int nb_oda, pdg_scf_options o, int hist)
+{
+    __shared__ double M[17 * 35], Ab[17 * 17], bb[17], x[17];
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x >= 32) return;
+    if (lane == 0) {
+        double mx = 0.0;
+        for (int b = 0; b < nb; b++) mx = fmax(mx, part[5 * parts + b]);
+        c->maxerr = mx;
+        for (int m = 0; m < c->matnum; m++) {
+            const double t = 2.0 * sum_parts(part, 8 + m, parts, nb);
+            const int n = c->slots[m];
+            c->B[n * WMAXH + c->newest] = t; c->B[c->newest * WMAXH + n] = t;
+        }
+        c->do_extrap = 0; c->do_oda = 0;
+        if (c->iteration > 0 && o.use_rca) {
+            if (c->qdiis && c->maxerr > 0.8) { c->qdiis = 0; c->qrca = 1; }
+            else if (c->iteration > 1 && c->qrca && c->maxerr < o.diis_onset) { c->qdiis = 1; c->qrca = 0; }
+        }
+    }
+    __syncwarp();
+    if (c->iteration > 0 && c->qdiis) {
+        int mn = c->matnum, good = 0;
+        while (mn > 1) {
+            const int n1 = mn + 1;
+            for (int e = lane; e < n1 * n1; e += 32) {
+                const int i = e / n1, j = e % n1;
+                Ab[e] = (i < mn && j < mn) ? c->B[c->slots[i] * WMAXH + c->slots[j]] : ((i == mn && j == mn) ? 0.0 : -1.0);
+            }
+            if (lane < n1) bb[lane] = lane == mn ? -1.0 : 0.0;
+            __syncwarp();
+            const bool ok = warp_solve(n1, Ab, bb, M, x);
+            double dev = -1.0;
+            for (int i = 0; i < mn; i++) dev += x[i];
+            if (ok && fabs(dev) < 1.0e-6) {
+                if (lane < mn) c->cf[lane] = x[lane];
+                good = 1;
+                break;
+            }
+            mn--;
+            __syncwarp();
+            if (lane == 0) {
+                for (int i = 0; i < mn; i++) c->slots[i] = c->slots[i + 1];
+                for (int i = mn; i < hist; i++) { c->slots[i] = c->slots[i - 1] + 1; if (c->slots[i] >= hist) c->slots[i] -= hist; }
+            }
+            __syncwarp();
+        }
+        if (lane == 0) { c->matnum = mn; c->good = good; c->do_extrap = good; }
+    } else if (c->iteration > 0 && o.use_rca && c->qrca && lane == 0) {
+        const double t1 = sum_parts(part, 24, parts, nb_oda), t2 = sum_parts(part, 25, parts, nb_oda);
+        const double t3 = sum_parts(part, 26, parts, nb_oda), t4 = sum_parts(part, 27, parts, nb_oda);
+        double ca = t1 - t2, cc = t3 - t4, dd = c->eold;
+        const double etemp = c->etemp;
+        ca += cc + 2.0 * (dd - etemp);
+        double cb = etemp - ca - cc - dd, fmin_ = etemp, mub = 1.0, mu;
+        if (c->eold < etemp) { fmin_ = c->eold; mub = 0.0; }
+        if (ca == 0.0) {
+            if (cb == 0.0) mu = mub;
+            else { double mt = -cc / (2.0 * cb); mu = (cb > 0.0 && mt > 0.0 && mt < 1.0) ? mt : mub; }
+        } else {
+            double fac = cb * cb - 3.0 * ca * cc;
+            if (fac >= 0.0) {
+                double m1 = (-cb + sqrt(fac)) / (3.0 * ca), m2 = (-cb - sqrt(fac)) / (3.0 * ca);
+                if (m1 > 0.0 && m1 < 1.0) { double fv = ((ca * m1 + cb) * m1 + cc) * m1 + dd; if (fv < fmin_) { fmin_ = fv; mub = m1; } }
+                if (m2 > 0.0 && m2 < 1.0) { double fv = ((ca * m2 + cb) * m2 + cc) * m2 + dd; if (fv < fmin_) { fmin_ = fv; mub = m2; } }
+            }
+            mu = mub;
+        }
+        mu = fmax(mu, 0.01);
+        c->mu = mu;
+        c->etemp = ((ca * mu + cb) * mu + cc) * mu + dd;
+        c->do_oda = 1;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        if (c->valid) c->iteration++;
+        c->deltaeold = c->deltae; c->eold = c->etemp;
+    }
+}
+
+// DIIS extrapolation P = sum c_m hP_m, F = sum c_m hF_m, or the ODA mixture; then the RCA copies.
+__global__ void __launch_bounds__(WB) k_iterate(size_t NN, const Ctl *c, const double *__restrict__ hP, const double *__restrict__ hF,
+                                                double *__restrict__ P, double *__restrict__ F, double *__restrict__ rP, double *__restrict__ rF,
+                                                int use_rca)
+{
+    const int ex = c->do_extrap, oda = c->do_oda, mn = c->matnum;
+    const double mu = c->mu, nu = 1.0 - c->mu;
+    for (size_t k = (size_t)blockIdx.x * WB + threadIdx.x; k < NN; k += (size_t)gridDim.x * WB) {
+        double p = P[k], f = F[k];
+        if (ex) {
+            double pp = 0.0, ff = 0.0;
+            for (int m = 0; m < mn; m++) {
+                const size_t off = (size_t)c->slots[m] * NN + k;
+                pp = fma(c->cf[m], hP[off], pp); ff = fma(c->cf[m], hF[off], ff);
+            }
+            p = pp; f = ff;
+        } else if (oda) {
+            p = mu * p + nu * rP[k]; f = mu * f + nu * rF[k];
+        }
+        P[k] = p; F[k] = f;
+        if (use_rca) { rP[k] = p; rF[k] = f; }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Householder tridiagonalisation of the dense symmetric A (N x N, both triangles kept), column k by two kernels:
+//   tri_a(k)  every block forms the reflector of column k (rows k+1 ..) from colbuf (dlarfg; identical in every
+//             block), block 0 publishes v, tau, e[k], d[k]; then q_i = sum_j A22[i][j] v_j, one warp per row, and the
+//             block partials of q . v.
+//   tri_b(k)  K = tau^2 (q . v) / 2, w = tau q - K v, and the rank-2 update A22 -= v w^T + w v^T, one warp per row;
+//             v is stored below the subdiagonal of column k (the back-transformation reads it) and the updated
+//             column k+1 goes to colbuf.
+__device__ void reflector(int m, const double *__restrict__ x, double *v, double *red, double *tau_out, double *e_out)
+{
+    const double alpha = x[0];
+    double part = 0.0;
+    for (int i = 1 + threadIdx.x; i < m; i += WB) part = fma(x[i], x[i], part);
+    const double xn2 = block_sum(part, red);
+    double tau = 0.0, e = alpha, scal = 0.0;
+    if (xn2 != 0.0) {
+        const double beta = -copysign(sqrt(fma(alpha, alpha, xn2)), alpha);
+        tau = (beta - alpha) / beta; e = beta; scal = 1.0 / (alpha - beta);
+    }
+    for (int i = threadIdx.x; i < m; i += WB) v[i] = (i == 0) ? 1.0 : (tau != 0.0 ? x[i] * scal : 0.0);
+    *tau_out = tau; *e_out = e;
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(WB) k_tri_a(int N, int k, double *__restrict__ A, const double *__restrict__ colbuf, double *__restrict__ vbuf,
+                                              double *__restrict__ q, double *__restrict__ d, double *__restrict__ e, double *__restrict__ tau,
+                                              double *__restrict__ part, int parts)
+{
+    extern __shared__ double sv[];
+    __shared__ double red[32];
+    const int m = N - k - 1, c0 = k + 1, lane = threadIdx.x & 31;
+    double t, ek;
+    reflector(m, colbuf + c0, sv, red, &t, &ek);
+    if (blockIdx.x == 0) {
+        for (int i = threadIdx.x; i < m; i += WB) vbuf[i] = sv[i];
+        if (threadIdx.x == 0) { tau[k] = t; e[k] = ek; d[k] = A[(size_t)k * N + k]; }
+    }
+    double pv = 0.0;
+    const int gw = blockIdx.x * WW + (threadIdx.x >> 5), nw = gridDim.x * WW;
+    for (int i = gw; i < m; i += nw) {
+        const double *row = A + (size_t)(c0 + i) * N + c0;
+        double s = 0.0;
+        for (int j = lane; j < m; j += 32) s = fma(row[j], sv[j], s);
+        s = warp_sum(s);
+        if (lane == 0) { q[i] = s; pv = fma(s, sv[i], pv); }
+    }
+    pv = block_sum(pv, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = pv;
+}
+
+__global__ void __launch_bounds__(WB) k_tri_b(int N, int k, double *__restrict__ A, double *__restrict__ colbuf, const double *__restrict__ vbuf,
+                                              const double *__restrict__ q, const double *__restrict__ tau, const double *__restrict__ part, int nb_a)
+{
+    extern __shared__ double sm[];
+    double *sv = sm, *sw = sm + N;
+    const int m = N - k - 1, c0 = k + 1, lane = threadIdx.x & 31;
+    const double t = tau[k];
+    double qv = 0.0;
+    for (int b = 0; b < nb_a; b++) qv += part[b];
+    const double K = 0.5 * t * t * qv;
+    for (int i = threadIdx.x; i < m; i += WB) { const double vi = vbuf[i]; sv[i] = vi; sw[i] = fma(-K, vi, t * q[i]); }
+    __syncthreads();
+    const int gw = blockIdx.x * WW + (threadIdx.x >> 5), nw = gridDim.x * WW;
+    for (int i = gw; i < m; i += nw) {
+        double *row = A + (size_t)(c0 + i) * N + c0;
+        const double vi = sv[i], wi = sw[i];
+        for (int j = lane; j < m; j += 32) row[j] = fma(-vi, sw[j], fma(-wi, sv[j], row[j]));
+        if (lane == 0) {
+            if (i >= 1) A[(size_t)(c0 + i) * N + k] = vi;   // the reflector, below the subdiagonal of column k
+            if (i >= 1) colbuf[c0 + i] = row[0];             // column c0 of the updated A22 (row c0 + i), next reflector's input
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) colbuf[c0] = A[(size_t)c0 * N + c0];
+}
+
+// Start: A = F, colbuf = column 0; end: the last two diagonal and the last subdiagonal elements.
+__global__ void __launch_bounds__(WB) k_tri_start(int N, const double *__restrict__ F, double *__restrict__ A, double *__restrict__ colbuf)
+{
+    const size_t NN = (size_t)N * N;
+    for (size_t k = (size_t)blockIdx.x * WB + threadIdx.x; k < NN; k += (size_t)gridDim.x * WB) A[k] = F[k];
+    for (int i = blockIdx.x * WB + threadIdx.x; i < N; i += gridDim.x * WB) colbuf[i] = F[(size_t)i * N];
+}
+
+__global__ void k_tri_end(int N, const double *__restrict__ A, double *__restrict__ d, double *__restrict__ e, double *__restrict__ tau)
+{
+    if (threadIdx.x || blockIdx.x) return;
+    if (N >= 2) { d[N - 2] = A[(size_t)(N - 2) * N + N - 2]; e[N - 2] = A[(size_t)(N - 1) * N + N - 2]; d[N - 1] = A[(size_t)(N - 1) * N + N - 1]; }
+    else d[0] = A[0];
+    if (N >= 2) tau[N - 2] = 0.0;
+    e[N - 1] = 0.0;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Eigenvalues of the tridiagonal T (d, e) by FP64 bisection on Sturm counts (as dstebz): eigenvalue of index
+// first + t, t < nv, one thread each; the result in eig[t].
+__device__ __forceinline__ int sturm(int N, const double *d, const double *e, double x, double pivmin)
+{
+    int c = 0;
+    double q = d[0] - x;
+    if (fabs(q) < pivmin) q = -pivmin;
+    c += (q < 0.0);
+    for (int i = 1; i < N; i++) {
+        q = (d[i] - x) - e[i - 1] * e[i - 1] / q;
+        if (fabs(q) < pivmin) q = -pivmin;
+        c += (q < 0.0);
+    }
+    return c;
+}
+
+__global__ void __launch_bounds__(WB) k_bisect(int N, int first, int nv, const double *__restrict__ d, const double *__restrict__ e,
+                                               double *__restrict__ eig)
+{
+    const int t = blockIdx.x * WB + threadIdx.x;
+    if (t >= nv) return;
+    double lo = 1e300, hi = -1e300, emax = 0.0;
+    for (int i = 0; i < N; i++) {
+        const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < N - 1 ? fabs(e[i]) : 0.0);
+        lo = fmin(lo, d[i] - r); hi = fmax(hi, d[i] + r);
+        if (i < N - 1) emax = fmax(emax, e[i] * e[i]);
+    }
+    const double tnorm = fmax(fabs(lo), fabs(hi));
+    const double pivmin = fmax(1e-300, 2.2250738585072014e-308 * fmax(1.0, emax));
+    lo -= 2.2e-16 * tnorm * N + 2.0 * pivmin; hi += 2.2e-16 * tnorm * N + 2.0 * pivmin;
+    const int idx = first + t;   // the eigenvalue with exactly idx eigenvalues below it
+    for (int it = 0; it < 200; it++) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi || hi - lo <= 2.2e-16 * fmax(fabs(lo), fabs(hi)) + pivmin) break;
+        if (sturm(N, d, e, mid, pivmin) > idx) hi = mid; else lo = mid;
+    }
+    eig[t] = 0.5 * (lo + hi);
+}
+
+// Inverse iteration for the nv wanted eigenvectors, one thread per vector: the LU factors of T - lambda I with row
+// interchanges (stored interleaved by vector), four solves from a hashed start vector, re-orthogonalisation after
+// every solve against the earlier vectors of the same cluster of close eigenvalues (as dstein), then normalisation.  Clusters run in rounds: round r handles the r-th member of every cluster, so every vector's cluster
+// predecessors are final.  Output: the vectors as columns of Zc (N x nv, column-major), in the tridiagonal basis.
+__device__ __forceinline__ unsigned int whash(unsigned int a, unsigned int b)
+{
+    unsigned int h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u + (a << 6) + (a >> 2));
+    h ^= h >> 16; h *= 0x85EBCA6Bu; h ^= h >> 13; h *= 0xC2B2AE35u; h ^= h >> 16;
+    return h;
+}
+
+__global__ void __launch_bounds__(WB) k_invit(int N, int nv, int ld, int round, const int *__restrict__ cstart, const double *__restrict__ d,
+                                              const double *__restrict__ e, const double *__restrict__ eig, double tnorm,
+                                              double *__restrict__ lu, unsigned char *__restrict__ pv, double *__restrict__ y,
+                                              double *__restrict__ Zc)
+{
+    const int t = blockIdx.x * WB + threadIdx.x;
+    if (t >= nv) return;
+    const int c0 = cstart[t];
+    if (t - c0 != round) return;
+    const double sigma = eig[t], tiny = 1e-14 * tnorm + 1e-300;
+    double *u0 = lu, *u1 = lu + (size_t)N * ld, *u2 = lu + 2 * (size_t)N * ld, *lm = lu + 3 * (size_t)N * ld;
+    double ak = d[0] - sigma, bk = N > 1 ? e[0] : 0.0;
+    for (int k = 0; k < N - 1; k++) {
+        const double ck = e[k], an = d[k + 1] - sigma, bn = k + 1 < N - 1 ? e[k + 1] : 0.0;
+        const bool sw = fabs(ak) < fabs(ck);
+        double piv = sw ? ck : ak;
+        if (fabs(piv) < tiny) piv = copysign(tiny, piv);
+        const double r = 1.0 / piv, l = (sw ? ak : ck) * r;
+        const double uu1 = sw ? an : bk, uu2 = sw ? bn : 0.0;
+        u0[(size_t)k * ld + t] = r; u1[(size_t)k * ld + t] = uu1; u2[(size_t)k * ld + t] = uu2; lm[(size_t)k * ld + t] = l;
+        pv[(size_t)k * ld + t] = sw;
+        ak = fma(-l, uu1, sw ? bk : an);
+        bk = fma(-l, uu2, sw ? 0.0 : bn);
+    }
+    if (fabs(ak) < tiny) ak = copysign(tiny, ak);
+    u0[(size_t)(N - 1) * ld + t] = 1.0 / ak;
+    for (int i = 0; i < N; i++) y[(size_t)i * ld + t] = ((whash(t * 2654435761u + 17u, i) >> 8) * (1.0 / 16777216.0)) * 2.0 - 1.0;
+    for (int it = 0; it < 4; it++) {
+        double c = y[t];
+        for (int k = 0; k < N - 1; k++) {
+            const double xn = y[(size_t)(k + 1) * ld + t], l = lm[(size_t)k * ld + t];
+            const bool sw = pv[(size_t)k * ld + t];
+            const double yk = sw ? xn : c, cn = sw ? c : xn;
+            y[(size_t)k * ld + t] = yk;
+            c = fma(-l, yk, cn);
+        }
+        double x1 = c * u0[(size_t)(N - 1) * ld + t], x2 = 0.0, mx = fabs(x1);
+        y[(size_t)(N - 1) * ld + t] = x1;
+        for (int k = N - 2; k >= 0; k--) {
+            const size_t o = (size_t)k * ld + t;
+            const double x0 = fma(-u2[o], x2, fma(-u1[o], x1, y[o])) * u0[o];
+            y[o] = x0; x2 = x1; x1 = x0; mx = fmax(mx, fabs(x0));
+        }
+        const double sc = mx > 0.0 ? 1.0 / mx : 1.0;
+        for (int i = 0; i < N; i++) y[(size_t)i * ld + t] *= sc;
+        for (int p = c0; p < t; p++) {
+            const double *zp = Zc + (size_t)p * N;
+            double dt = 0.0;
+            for (int i = 0; i < N; i++) dt = fma(y[(size_t)i * ld + t], zp[i], dt);
+            for (int i = 0; i < N; i++) y[(size_t)i * ld + t] = fma(-dt, zp[i], y[(size_t)i * ld + t]);
+        }
+    }
+    double nr = 0.0;
+    for (int i = 0; i < N; i++) { const double v = y[(size_t)i * ld + t]; nr = fma(v, v, nr); }
+    const double s = 1.0 / sqrt(nr);
+    double *z = Zc + (size_t)t * N;
+    for (int i = 0; i < N; i++) z[i] = y[(size_t)i * ld + t] * s;
+}
+
+// Cluster starts (one thread; nv <= N): cstart[t] = first index of t's cluster; returns the largest cluster size.
+__global__ void k_clusters(int nv, const double *__restrict__ eig, double gap, int *__restrict__ cstart, int *__restrict__ maxsize)
+{
+    if (threadIdx.x || blockIdx.x) return;
+    int s0 = 0, big = nv > 0 ? 1 : 0;
+    for (int t = 0; t < nv; t++) {
+        if (t > 0 && eig[t] - eig[t - 1] > gap) s0 = t;
+        cstart[t] = s0;
+        big = max(big, t - s0 + 1);
+    }
+    *maxsize = big;
+}
+
+// Back-transformation block: Vb (m x nb, column-major, unit diagonal at row j of column j, zeros above) from the
+// reflectors stored in A below the subdiagonal of columns k0 .. k0 + nb - 1; rows counted from k0 + 1.
+__global__ void __launch_bounds__(WB) k_vblock(int N, int k0, int nb, const double *__restrict__ A, double *__restrict__ Vb)
+{
+    const int m = N - k0 - 1;
+    for (int e = blockIdx.x * WB + threadIdx.x; e < m * nb; e += gridDim.x * WB) {
+        const int j = e / m, r = e % m;   // column j (reflector k0 + j), row r (matrix row k0 + 1 + r)
+        double v = 0.0;
+        if (r == j) v = 1.0;
+        else if (r > j) v = A[(size_t)(k0 + 1 + r) * N + k0 + j];
+        Vb[(size_t)j * m + r] = v;
+    }
+}
+
+// T of the compact WY form I - V T V^T (upper triangular, dlarft 'Forward' 'Columnwise') from S = V^T V and tau.
+__global__ void k_tblock(int nb, const double *__restrict__ S, const double *__restrict__ tau, int k0, double *__restrict__ T)
+{
+    if (threadIdx.x || blockIdx.x) return;
+    for (int j = 0; j < nb; j++) {
+        const double tj = tau[k0 + j];
+        T[j * WNB + j] = tj;
+        for (int i = 0; i < j; i++) {
+            double s = 0.0;
+            for (int l = i; l < j; l++) s += T[i * WNB + l] * S[j * nb + l];   // S column-major (nb x nb): S[l][j] = S[j * nb + l]
+            T[i * WNB + j] = -tj * s;
+        }
+        for (int i = j + 1; i < nb; i++) T[i * WNB + j] = 0.0;
+    }
+}
+
+// W2 = T W in place (T upper nb x nb, row-major with stride WNB; W nb x kv column-major with ld nb).
+__global__ void __launch_bounds__(WB) k_trmm(int nb, int kv, const double *__restrict__ T, double *__restrict__ W)
+{
+    for (int c = blockIdx.x * WB + threadIdx.x; c < kv; c += gridDim.x * WB) {
+        double col[WNB], out[WNB];
+        for (int i = 0; i < nb; i++) col[i] = W[(size_t)c * nb + i];
+        for (int i = 0; i < nb; i++) {
+            double s = 0.0;
+            for (int l = i; l < nb; l++) s = fma(T[i * WNB + l], col[l], s);
+            out[i] = s;
+        }
+        for (int i = 0; i < nb; i++) W[(size_t)c * nb + i] = out[i];
+    }
+}
+
+// P = 2 C (occupied vectors) or 2 (1 - C) (virtual), C = Zc Zc^T; block partials of the squared change to part slot 6.
+__global__ void __launch_bounds__(WB) k_density(int N, int occ, const double *__restrict__ C, double *__restrict__ P,
+                                                double *__restrict__ part, int parts)
+{
+    __shared__ double red[32];
+    const size_t NN = (size_t)N * N;
+    double r = 0.0;
+    for (size_t k = (size_t)blockIdx.x * WB + threadIdx.x; k < NN; k += (size_t)gridDim.x * WB) {
+        const int i = (int)(k / N), j = (int)(k % N);
+        const double v = C[(size_t)min(i, j) * N + max(i, j)];   // C symmetric; take one triangle for both entries
+        const double pn = occ ? 2.0 * v : ((i == j ? 2.0 : 0.0) - 2.0 * v);
+        const double dl = pn - P[k];
+        r = fma(dl, dl, r);
+        P[k] = pn;
+    }
+    r = block_reduce(r, red);
+    if (threadIdx.x == 0) part[6 * parts + blockIdx.x] = r;
+}
+
+__global__ void k_control_density(Ctl *c, const double *__restrict__ part, int parts, int nb, int N)
+{
+    if (threadIdx.x || blockIdx.x) return;
+    c->rms = sqrt(sum_parts(part, 6, parts, nb)) / (double)N;
+    c->valid = 1;
+    c->have_z = 1;
+}
+
+// Uniform diagonal guess (QCOnePDM.c:326-331).
+__global__ void __launch_bounds__(WB) k_guess(int N, double g, double *__restrict__ P)
+{
+    const size_t NN = (size_t)N * N;
+    for (size_t k = (size_t)blockIdx.x * WB + threadIdx.x; k < NN; k += (size_t)gridDim.x * WB) P[k] = (k / N == k % N) ? g : 0.0;
+}
+
+// Nuclear energy (pair terms in pair order) and the heat-of-formation baseline, one block.
+__global__ void __launch_bounds__(WB) k_init_ctl(DeviceSystem s, const double *__restrict__ pair_e, int valid, int hist, Ctl *c)
+{
+    __shared__ double red[32];
+    double en = 0.0;
+    for (int p = threadIdx.x; p < s.n_pairs; p += WB) en += pair_e[(size_t)p * PDG_PAIR_E_STRIDE + 20];
+    en = block_sum(en, red);
+    double base = 0.0;
+    for (int A = threadIdx.x; A < s.n_atoms; A += WB) { const double *E = elem(s, s.atom_elem[A]); base += E[PDG_E_EHEAT] - E[PDG_E_EISOL]; }
+    base = block_sum(base, red);
+    if (threadIdx.x == 0) {
+        memset(c, 0, sizeof(Ctl));
+        c->enuc = en; c->base = base; c->valid = valid; c->status = PDG_NOT_CONVERGED;
+        for (int i = 0; i < hist; i++) c->slots[i] = i;
+    }
+}
+
+__global__ void k_finish(const Ctl *c, double *__restrict__ energies, int *__restrict__ status, int *__restrict__ ncycles)
+{
+    if (threadIdx.x || blockIdx.x) return;
+    energies[0] = c->eel; energies[1] = c->e1 + c->e2; energies[2] = c->enuc; energies[3] = c->base; energies[4] = c->eq;
+    energies[5] = c->e1; energies[6] = c->e2; energies[7] = c->rms;
+    *status = c->status;
+    if (ncycles) *ncycles = c->iteration;
+}
+
+}  // namespace wide
+
+// =================================================================================================================
+// Host side.
+using namespace wide;
+
+struct pdg_wide {
+    DeviceSystem s;
+    WPlan w;
+    int grid;                      // blocks of the grid-wide kernels (the SM count)
+    cublasHandle_t blas = nullptr;
+    cudaGraphExec_t tri = nullptr; // the tridiagonalisation (2 (N - 2) kernels), replayed every density step
+    cudaStream_t tri_stream = nullptr;
+    double *tri_ws = nullptr;      // workspace base the graph was captured on
+    Ctl host;                      // last control record read back
+};
+
+static int cublas_ok(cublasStatus_t st, const char *what);
+
+size_t wide_workspace_bytes(const DeviceSystem &s) { return sizeof(double) * wide_plan(s).total; }
+size_t wide_workspace_size(const pdg_wide *W) { return sizeof(double) * W->w.total; }
+
+int wide_create(const DeviceSystem &s, pdg_wide **out)
+{
+    pdg_wide *W = new pdg_wide();
+    W->s = s;
+    W->w = wide_plan(s);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    W->grid = sms > 0 ? sms : 148;
+    if (W->grid > W->w.parts) W->grid = W->w.parts;
+    if (cublasCreate(&W->blas) != CUBLAS_STATUS_SUCCESS) { delete W; return PDG_CUDA_ERROR; }
+    cublasSetMathMode(W->blas, CUBLAS_DEFAULT_MATH);
+    *out = W;
+    return PDG_OK;
+}
+
+void wide_destroy(pdg_wide *W)
+{
+    if (!W) return;
+    if (W->tri) cudaGraphExecDestroy(W->tri);
+    if (W->blas) cublasDestroy(W->blas);
+    delete W;
+}
+
+// C (m x n, column-major, ld m) = op(A) op(B) + beta C with FP64 GEMM on the given stream.
+static cublasStatus_t dgemm(pdg_wide *W, cudaStream_t st, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
+                            double alpha, const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc)
+{
+    cublasSetStream(W->blas, st);
+    return cublasDgemm(W->blas, ta, tb, m, n, k, &alpha, A, lda, B, ldb, &beta, C, ldc);
+}
+
+// The tridiagonalisation of A (plan regions of this workspace) as one CUDA graph, captured on first use.
+static int tri_graph(pdg_wide *W, double *ws, cudaStream_t st)
+{
+    const int N = W->s.n_basis;
+    if (W->tri && W->tri_ws == ws) return PDG_OK;
+    if (W->tri) { cudaGraphExecDestroy(W->tri); W->tri = nullptr; }
+    cudaStream_t cap;
+    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return PDG_CUDA_ERROR;
+    const WPlan &p = W->w;
+    double *A = ws + p.A, *colbuf = ws + p.colbuf, *vbuf = ws + p.vbuf, *q = ws + p.q, *part = ws + p.part;
+    double *d = ws + p.d, *e = ws + p.e, *tau = ws + p.tau;
+    const size_t sm_a = sizeof(double) * (size_t)N, sm_b = 2 * sizeof(double) * (size_t)N;
+    cudaFuncSetAttribute(k_tri_a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_a);
+    cudaFuncSetAttribute(k_tri_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_b);
+    cudaGraph_t g;
+    cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    for (int k = 0; k + 2 < N; k++) {
+        k_tri_a<<<W->grid, WB, sm_a, cap>>>(N, k, A, colbuf, vbuf, q, d, e, tau, part, p.parts);
+        k_tri_b<<<W->grid, WB, sm_b, cap>>>(N, k, A, colbuf, vbuf, q, tau, part, W->grid);
+    }
+    k_tri_end<<<1, 32, 0, cap>>>(N, A, d, e, tau);
+    cudaError_t ce = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (ce != cudaSuccess) return PDG_CUDA_ERROR;
+    ce = cudaGraphInstantiate(&W->tri, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) { W->tri = nullptr; return PDG_CUDA_ERROR; }
+    W->tri_ws = ws;
+    return PDG_OK;
+}
+
+// One FP64 density step: P <- density of the wanted eigenvectors of F; the vectors stay in Zc for the DIIS save.
+static int wide_density_step(pdg_wide *W, double *ws, double *P, cudaStream_t st)
+{
+    const DeviceSystem &s = W->s;
+    const WPlan &p = W->w;
+    const int N = s.n_basis, kv = s.n_vec, G = W->grid;
+    double *F = ws + p.F, *A = ws + p.A, *C = ws + p.C, *Zc = ws + p.Zc, *part = ws + p.part;
+    k_tri_start<<<G, WB, 0, st>>>(N, F, A, ws + p.colbuf);
+    int rc = tri_graph(W, ws, st);
+    if (rc) return rc;
+    if (cudaGraphLaunch(W->tri, st) != cudaSuccess) return PDG_CUDA_ERROR;
+    // eigenvalues: the lowest n_occ (occupied) or the highest N - n_occ (virtual)
+    const int first = s.vec_occupied ? 0 : N - kv;
+    k_bisect<<<(kv + WB - 1) / WB, WB, 0, st>>>(N, first, kv, ws + p.d, ws + p.e, ws + p.eig);
+    // clusters of close eigenvalues, whose vectors are re-orthogonalised against each other
+    int *cstart = (int *)(ws + p.cst), *maxsize = cstart + N;
+    double bounds[2];
+    {
+        // Gershgorin bound of T, for the cluster gap and the pivot floor
+        std::vector<double> hd(N), he(N);
+        if (cudaMemcpyAsync(hd.data(), ws + p.d, sizeof(double) * N, cudaMemcpyDeviceToHost, st) != cudaSuccess) return PDG_CUDA_ERROR;
+        if (cudaMemcpyAsync(he.data(), ws + p.e, sizeof(double) * N, cudaMemcpyDeviceToHost, st) != cudaSuccess) return PDG_CUDA_ERROR;
+        if (cudaStreamSynchronize(st) != cudaSuccess) return PDG_CUDA_ERROR;
+        double lo = 1e300, hi = -1e300;
+        for (int i = 0; i < N; i++) {
+            const double r = (i > 0 ? fabs(he[i - 1]) : 0.0) + (i < N - 1 ? fabs(he[i]) : 0.0);
+            lo = fmin(lo, hd[i] - r); hi = fmax(hi, hd[i] + r);
+        }
+        bounds[0] = lo; bounds[1] = hi;
+    }
+    // Inverse iteration at an eigenvalue converged to round-off leaves a vector's overlap with another eigenvector at
+    // about eps ||T|| / gap: below 1e-11 for gaps above 1e-5 ||T||, so only closer eigenvalues form clusters.
+    const double tn = fmax(fabs(bounds[0]), fabs(bounds[1]));
+    k_clusters<<<1, 1, 0, st>>>(kv, ws + p.eig, 1.0e-5 * tn, cstart, maxsize);
+    int big = 0;
+    if (cudaMemcpyAsync(&big, maxsize, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return PDG_CUDA_ERROR;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return PDG_CUDA_ERROR;
+    double *lu = ws + p.lu;
+    unsigned char *pv = (unsigned char *)(lu + 5 * (size_t)N * p.kvp);
+    for (int r = 0; r < big; r++)
+        k_invit<<<(kv + WB - 1) / WB, WB, 0, st>>>(N, kv, p.kvp, r, cstart, ws + p.d, ws + p.e, ws + p.eig, tn, lu, pv, ws + p.y, Zc);
+    // back-transformation Zc <- Q Zc, blocks of WNB reflectors from the last to the first
+    const int nref = N - 2;
+    for (int k0 = ((nref - 1) / WNB) * WNB; k0 >= 0 && nref > 0; k0 -= WNB) {
+        const int nb = min(WNB, nref - k0), m = N - k0 - 1;
+        double *Vb = ws + p.vb, *S = ws + p.sb, *T = ws + p.tb, *Wm = ws + p.wb;
+        k_vblock<<<G, WB, 0, st>>>(N, k0, nb, A, Vb);
+        if (dgemm(W, st, CUBLAS_OP_T, CUBLAS_OP_N, nb, nb, m, 1.0, Vb, m, Vb, m, 0.0, S, nb) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
+        k_tblock<<<1, 1, 0, st>>>(nb, S, ws + p.tau, k0, T);
+        // W = V^T Zc[k0+1:, :]   (nb x kv)
+        if (dgemm(W, st, CUBLAS_OP_T, CUBLAS_OP_N, nb, kv, m, 1.0, Vb, m, Zc + k0 + 1, N, 0.0, Wm, nb) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
+        k_trmm<<<(kv + WB - 1) / WB, WB, 0, st>>>(nb, kv, T, Wm);
+        // Zc[k0+1:, :] -= V W2
+        if (dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_N, m, kv, nb, -1.0, Vb, m, Wm, nb, 1.0, Zc + k0 + 1, N) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
+    }
+    // C = Zc Zc^T (column-major N x N: symmetric, so also row-major), P from it
+    if (dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_T, N, N, kv, 1.0, Zc, N, Zc, N, 0.0, C, N) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
+    k_density<<<G, WB, 0, st>>>(N, s.vec_occupied, C, P, part, p.parts);
+    k_control_density<<<1, 1, 0, st>>>((Ctl *)(ws + p.ctl), part, p.parts, G, N);
+    return cudaGetLastError() == cudaSuccess ? PDG_OK : PDG_CUDA_ERROR;
+}
+
+int wide_energy_gradients(pdg_wide *W, const double *xyz, const double *phi, const pdg_scf_options &o, double *P, int use_density,
+                          double *energies, double *gradients, double *charges, int *status, int *ncycles, double *ws, cudaStream_t st)
+{
+    const DeviceSystem &s = W->s;
+    const WPlan &p = W->w;
+    const int N = s.n_basis, G = W->grid, hist = o.history;
+    const size_t NN = (size_t)N * N;
+    Ctl *ctl = (Ctl *)(ws + p.ctl);
+    double *F = ws + p.F, *H = ws + p.fp.H, *part = ws + p.part, *C = ws + p.C;
+    // integrals (the frame kernels of integrals.cu on this one frame)
+    launch_pair_integrals(s, p.fp, 1, xyz, ws, st);
+    launch_assemble_h(s, p.fp, 1, ws, st);
+    if (!use_density) k_guess<<<G, WB, 0, st>>>(N, (double)s.n_electrons / (double)N, P);
+    k_init_ctl<<<1, WB, 0, st>>>(s, ws + p.fp.pair_e, use_density ? 1 : 0, hist, ctl);
+    if (cudaGetLastError() != cudaSuccess) return PDG_CUDA_ERROR;
+    const int nb_tr = G;
+    for (int cycle = 0; cycle <= o.maximum_scf_cycles; cycle++) {
+        // Fock build, energies, convergence test
+        k_pk<<<G, WB, 0, st>>>(s, P, ws + p.pk);
+        k_fock<<<G * 4, WB, 0, st>>>(s, H, P, ws + p.fp.tei, ws + p.pk, F);
+        k_traces<<<nb_tr, WB, 0, st>>>(N, P, H, F, part, p.parts);
+        k_lowdin<<<1, WB, 0, st>>>(s, P, phi, F, charges, part, p.parts);
+        k_control_fock<<<1, 1, 0, st>>>(ctl, part, p.parts, nb_tr, o, hist);
+        if (cudaMemcpyAsync(&W->host, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st) != cudaSuccess) return PDG_CUDA_ERROR;
+        if (cudaStreamSynchronize(st) != cudaSuccess) return PDG_CUDA_ERROR;
+        if (W->host.done || W->host.iteration >= o.maximum_scf_cycles) break;
+        // DIIS save: history, error vector e = F P - P F, B-matrix row
+        if (W->host.valid) {
+            k_pack<<<G, WB, 0, st>>>(NN, ctl, P, F, ws + p.hP, ws + p.hF);
+            double sg = 1.0;
+            if (W->host.have_z) {
+                // P = 2 Zc Zc^T (or 2 (1 - Zc Zc^T)): F P - P F = sg (G Zc^T - Zc G^T), G = F Zc
+                if (dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_N, N, s.n_vec, N, 1.0, F, N, ws + p.Zc, N, 0.0, ws + p.G, N) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
+                // C (column-major) = G Zc^T, i.e. row-major C^T: the error kernel reads C_ij - C_ji, so the sign flips
+                if (dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_T, N, N, s.n_vec, 1.0, ws + p.G, N, ws + p.Zc, N, 0.0, C, N) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
+                sg = s.vec_occupied ? -2.0 : 2.0;
+            } else {
+                // C (column-major) = F P, row-major (F P)^T = P F: e = FP - PF = C^T - C, read as -(C_ij - C_ji)
+                if (dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_N, N, N, N, 1.0, F, N, P, N, 0.0, C, N) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
+                sg = -1.0;
+            }
+            k_error<<<G, WB, 0, st>>>(N, ctl, C, sg, ws + p.hE, part, p.parts);
+            k_dots<<<G, WB, 0, st>>>(N, ctl, ws + p.hE, part, p.parts);
+            if (o.use_rca) k_oda_traces<<<G, WB, 0, st>>>(NN, F, P, ws + p.rF, ws + p.rP, part, p.parts);
+            k_control_diis<<<1, 32, 0, st>>>(ctl, part, p.parts, G, G, o, hist);
+            k_iterate<<<G, WB, 0, st>>>(NN, ctl, ws + p.hP, ws + p.hF, P, F, ws + p.rP, ws + p.rF, o.use_rca);
+        } else {
+            // no valid density yet (the diagonal guess): nothing to save; the reference does not count this cycle
+            k_control_diis<<<1, 32, 0, st>>>(ctl, part, p.parts, 0, 0, o, hist);
+        }
+        int rc = wide_density_step(W, ws, P, st);
+        if (rc) return rc;
+    }
+    k_finish<<<1, 1, 0, st>>>(ctl, energies, status, ncycles);
+    if (gradients) {
+        launch_pair_gradients(s, p.fp, 1, xyz, P, ws, st, false);
+        launch_reduce_gradients(s, p.fp, 1, ws, gradients, st);
+    }
+    if (cudaGetLastError() != cudaSuccess) return PDG_CUDA_ERROR;
+    return PDG_OK;
+}

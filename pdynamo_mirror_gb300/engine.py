@@ -24,10 +24,18 @@ def require_cuda():
         raise _native.NativeError("a CUDA device is required: the GB300 kernels are the only compute path")
 
 
-class QCEngine:
-    """A pdg_system plus the device buffers of a batch."""
+# Basis size above which one frame's SCF is spread over the whole GPU (pdg_wide_*) instead of one CTA per frame.
+WIDE_BASIS = 384
 
-    def __init__(self, hamiltonian, atomic_numbers, charge, device=None):
+
+class QCEngine:
+    """A pdg_system plus the device buffers of a batch.
+
+    Regions of more than WIDE_BASIS basis functions (or wide=True) run every frame's SCF over the whole GPU
+    (pdg_wide_energy_gradients, one frame after another); smaller ones give each frame one CTA
+    (pdg_energy_gradients, all frames in one launch)."""
+
+    def __init__(self, hamiltonian, atomic_numbers, charge, device=None, wide=None):
         require_cuda()
         self.L = _native.load()
         self.device = torch.device(device or "cuda")
@@ -46,19 +54,30 @@ class QCEngine:
         self.n_atoms, self.n_basis, self.n_occupied, self.n_pairs = len(self.atomic_numbers), nb.value, no.value, npair.value
         self._ws, self._ws_frames = None, 0
         self._qcmm_ws = None
+        self.wide = (self.n_basis > WIDE_BASIS) if wide is None else bool(wide)
+        self._wide = None
+        if self.wide:
+            w = ctypes.c_void_p()
+            with torch.cuda.device(self.device):
+                _native.check(self.L.pdg_wide_create(h, ctypes.byref(w)), "pdg_wide_create")
+            self._wide = w
         self.density = None          # device [F, N, N], kept between calls as the reference keeps its state
         self._knots = {}
 
     def __del__(self):
         try:
+            if getattr(self, "_wide", None):
+                self.L.pdg_wide_destroy(self._wide)
             if getattr(self, "handle", None):
                 self.L.pdg_system_destroy(self.handle)
         except Exception:
             pass
 
     def workspace(self, n_frames):
+        if self.wide:
+            n_frames = 1   # the wide path computes one frame at a time
         if self._ws is None or self._ws_frames < n_frames:
-            nbytes = int(self.L.pdg_workspace_bytes(self.handle, n_frames))
+            nbytes = int(self.L.pdg_wide_workspace_bytes(self.handle)) if self.wide else int(self.L.pdg_workspace_bytes(self.handle, n_frames))
             self._ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
             self._ws_frames = n_frames
         return self._ws
@@ -122,10 +141,19 @@ class QCEngine:
         status = torch.empty(F, dtype=torch.int32, device=dev)
         ncycles = torch.empty(F, dtype=torch.int32, device=dev)
         opts = converger.options()
-        _native.check(self.L.pdg_energy_gradients(self.handle, F, _native.ptr(xyz_bohr), _native.ptr(phi), ctypes.byref(opts),
-                                                  _native.ptr(self.density), use, _native.ptr(energies), _native.ptr(grad),
-                                                  _native.ptr(charges), _native.ptr(status), _native.ptr(ncycles),
-                                                  _native.ptr(ws), ws.numel(), sh), "pdg_energy_gradients")
+        if self.wide:
+            # one frame after another, each over the whole GPU
+            for f in range(F):
+                _native.check(self.L.pdg_wide_energy_gradients(
+                    self._wide, _native.ptr(xyz_bohr[f]), _native.ptr(None if phi is None else phi[f]), ctypes.byref(opts),
+                    _native.ptr(self.density[f]), use, _native.ptr(energies[f]), _native.ptr(None if grad is None else grad[f]),
+                    _native.ptr(charges[f]), _native.ptr(status[f:f + 1]), _native.ptr(ncycles[f:f + 1]), _native.ptr(ws), ws.numel(), sh),
+                    "pdg_wide_energy_gradients")
+        else:
+            _native.check(self.L.pdg_energy_gradients(self.handle, F, _native.ptr(xyz_bohr), _native.ptr(phi), ctypes.byref(opts),
+                                                      _native.ptr(self.density), use, _native.ptr(energies), _native.ptr(grad),
+                                                      _native.ptr(charges), _native.ptr(status), _native.ptr(ncycles),
+                                                      _native.ptr(ws), ws.numel(), sh), "pdg_energy_gradients")
         out.update(energies=energies, qc_gradients=grad, charges=charges, status=status, ncycles=ncycles, phi=phi)
         mark(2)
         if qcmm and gradients:

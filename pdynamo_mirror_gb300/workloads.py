@@ -10,6 +10,7 @@
   molecular-dynamics frames of one system.
 * qcmm_water_box_frames(n): the QC/MM water box (seed 1) and n of its perturbed frames (0.02 A, seed 11), the
   benchmark's input.
+* large_qcmm(seed): 200 QC waters (600 atoms, N = 1200, neutral) in 20000 TIP3P waters in an 85 A cube, seed 4.
 """
 
 import math
@@ -92,10 +93,10 @@ def water_cluster(n, seed=0, centre=None, min_oo=2.6):
     return np.array(Z), np.array(X)
 
 
-def qcmm_water_box(seed=1, n_qc_waters=21, n_mm_waters=4000, box=50.0, min_oo=2.6):
+def qcmm_water_box(seed=1, n_qc_waters=21, n_mm_waters=4000, box=50.0, min_oo=2.6, hydroxide=True):
     """Returns (atomic numbers, coordinates, MM charges (0 on QC atoms), QC atom indices, QC charge)."""
     rng = np.random.default_rng(seed)
-    n_qc_mol = n_qc_waters + 1
+    n_qc_mol = n_qc_waters + (1 if hydroxide else 0)
     edge = 8.0 * (n_qc_mol / 16.0) ** (1.0 / 3.0)
     centre = np.full(3, 0.5 * box)
     grid = _Grid(np.zeros(3) - 5.0, box + 10.0, min_oo)
@@ -113,7 +114,13 @@ def qcmm_water_box(seed=1, n_qc_waters=21, n_mm_waters=4000, box=50.0, min_oo=2.
     for o in _place(rng, n_mm_waters, np.zeros(3), box, grid):
         R = _random_rotation(rng)
         X.extend(o + loc @ R.T); Z.extend([8, 1, 1]); Q.extend([TIP3P_O, TIP3P_H, TIP3P_H])
-    return np.array(Z), np.array(X), np.array(Q), list(range(n_qc)), -1
+    return np.array(Z), np.array(X), np.array(Q), list(range(n_qc)), (-1 if hydroxide else 0)
+
+
+def large_qcmm(seed=4, n_qc_waters=200, n_mm_waters=20000, box=85.0):
+    """The large QC/MM system: a 200-water QC region (600 atoms, 1200 basis functions, neutral) at the centre of an
+    85 A cube holding 20000 TIP3P waters, placed as qcmm_water_box.  Returns the same tuple."""
+    return qcmm_water_box(seed=seed, n_qc_waters=n_qc_waters, n_mm_waters=n_mm_waters, box=box, hydroxide=False)
 
 
 def perturbed_frames(xyz, n, sigma=0.02, seed=7):

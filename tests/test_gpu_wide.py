@@ -1,0 +1,97 @@
+"""One QC region's SCF over the whole GPU (pdg_wide_energy_gradients) against the oracle and against the one-CTA path.
+
+* the QC/MM water box (65 QC atoms, N = 131, ABFS) and a 60-water AM1 cluster (N = 360), with the wide engine forced,
+  against the oracle at the accuracy gate (|dE| < 1e-6 Hartree, max |dF| < 1e-5 Hartree/Bohr) and against the
+  one-CTA path (both converge the same FP64 SCF to the 1e-8 density tolerance: energies within 1e-9 Hartree);
+* a warm start from the converged density converges again in at most two cycles to the same energy;
+* the large QC/MM system (200 QC waters, 600 atoms, N = 1200, in 20000 TIP3P waters; the engine picks the wide path
+  by size) through System.Energy against the oracle's fixture (tests/golden/large_qcmm_reference.json): energy terms,
+  QC gradients, the MM gradients of the 400 MM atoms nearest the QC region and the sum of all MM gradients.
+"""
+import json, os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+KJ = 2625.5
+A2B = 1.0e-10 / 5.291772083e-11
+E_TOL, G_TOL = 1.0e-6, 1.0e-5
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _engine(h, Z, charge, wide):
+    from pdynamo_mirror_gb300.engine import QCEngine
+    return QCEngine(h, Z, charge, wide=wide)
+
+
+def test_wide_water_box_matches_oracle_and_one_cta_path():
+    import torch
+    from pdynamo_mirror_gb300 import DIISSCFConverger, NBModelABFS, workloads
+    Z, X, Q, sel, charge = workloads.qcmm_water_box(seed=1)
+    nq = len(sel)
+    nb = NBModelABFS(innerCutoff=8.0, outerCutoff=12.0)
+    qc = torch.as_tensor(X[None, :nq], device="cuda").contiguous()
+    mm = torch.as_tensor(X[None, nq:], device="cuda").contiguous()
+    q = torch.as_tensor(Q[nq:], device="cuda")
+    out = {}
+    for wide in (True, False):
+        eng = _engine("am1", Z[:nq], charge, wide)
+        assert eng.wide == wide
+        r = eng.run(qc, DIISSCFConverger(), mm, q, nb, gradients=True, warm_start=False)
+        assert int(r["status"][0]) == 0
+        out[wide] = (r["energies"][0].cpu().numpy(), (r["qc_gradients"] + r["qcmm_qc_gradients"])[0].cpu().numpy(),
+                     r["charges"][0].cpu().numpy(), int(r["ncycles"][0]))
+    (Ew, Gw, Cw, nw), (Ec, Gc, Cc, nc) = out[True], out[False]
+    knots = O.abfs_knots(8.0, 12.0)
+    phi, _, _ = O.qcmm("abfs", X[:nq], X[nq:], Q[nq:], knots=knots)
+    ref = O.System(O.Hamiltonian("am1", list(Z[:nq])), list(Z[:nq]), charge=charge).energy(X[:nq], phi=phi)
+    _, gq, _ = O.qcmm("abfs", X[:nq], X[nq:], Q[nq:], qcq=ref["charges"], knots=knots)
+    assert abs(Ew[1] + Ew[2] + Ew[3] - (ref["eelectronic"] + ref["enuclear"] + ref["baseline"])) < E_TOL
+    assert abs(Ew[4] - ref["eqcmm"]) < E_TOL
+    assert np.abs(Gw - (ref["gradients"] + gq)).max() < G_TOL
+    np.testing.assert_allclose(Ew[:7], Ec[:7], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(Gw, Gc, rtol=0, atol=1e-7)
+    np.testing.assert_allclose(Cw, Cc, rtol=0, atol=1e-7)
+    assert abs(nw - nc) <= 2
+
+
+def test_wide_cluster_matches_oracle_and_warm_start():
+    import torch
+    from pdynamo_mirror_gb300 import DIISSCFConverger, workloads
+    Z, X = workloads.water_cluster(60, seed=61)
+    eng = _engine("am1", Z, 0, True)
+    xyz = torch.as_tensor(X[None], device="cuda").contiguous()
+    r = eng.run(xyz, DIISSCFConverger(), gradients=True, warm_start=False)
+    assert int(r["status"][0]) == 0
+    E, G = r["energies"][0].cpu().numpy(), r["qc_gradients"][0].cpu().numpy()
+    ref = O.System(O.Hamiltonian("am1", list(Z)), list(Z)).energy(X)
+    assert abs(E[1] + E[2] + E[3] - (ref["eelectronic"] + ref["enuclear"] + ref["baseline"])) < E_TOL
+    assert np.abs(G - ref["gradients"]).max() < G_TOL
+    r2 = eng.run(xyz, DIISSCFConverger(), gradients=True, warm_start=True)
+    assert int(r2["status"][0]) == 0 and int(r2["ncycles"][0]) <= 2
+    assert abs(float(r2["energies"][0, 0]) - float(E[0])) < 1e-9
+
+
+def test_large_qcmm_system_matches_oracle_fixture():
+    from pdynamo_mirror_gb300 import NBModelABFS, QCModelMNDO, System, workloads
+    ref = json.load(open(os.path.join(HERE, "golden", "large_qcmm_reference.json")))
+    Z, X, Q, sel, charge = workloads.large_qcmm()
+    nq = len(sel)
+    s = System(Z, X, mmCharges=Q)
+    s.electronicState.charge = charge
+    s.DefineQCModel(QCModelMNDO("am1"), qcSelection=sel)
+    s.DefineNBModel(NBModelABFS(innerCutoff=8.0, outerCutoff=12.0))
+    assert s.engine().wide and s.engine().n_basis == 1200
+    s.Energy(doGradients=True)
+    t = s.configuration.energyTerms
+    assert abs(t["Pure QC"] / KJ - (ref["eelectronic"] + ref["enuclear"] + ref["baseline"])) < E_TOL
+    assert abs(t["QC/MM Elect."] / KJ - ref["eqcmm"]) < E_TOL
+    g = s.configuration.gradients3 / (A2B * KJ)
+    assert np.abs(g[:nq] - np.array(ref["qc_gradients"])).max() < G_TOL
+    mm = np.array(ref["mm_sample"]) + nq
+    assert np.abs(g[mm] - np.array(ref["mm_gradients_sample"])).max() < G_TOL
+    assert np.abs(g[nq:].sum(axis=0) - np.array(ref["mm_gradient_sum"])).max() < G_TOL
