@@ -413,6 +413,13 @@ size_t pdg_wide_workspace_bytes(const pdg_system *sys);
 int pdg_wide_energy_gradients(pdg_wide *wide, const double *d_xyz, const double *d_phi, const pdg_scf_options *options,
                               double *d_density, int use_density, double *d_energies, double *d_gradients, double *d_charges,
                               int *d_status, int *d_ncycles, void *d_workspace, size_t workspace_bytes, void *stream);
+/* Device time per phase of the last pdg_wide_energy_gradients call (after pdg_wide_phase_events(wide, 1)), in
+ * milliseconds, PDG_WIDE_NPHASES values: integrals, Fock builds (with the converger's energy test), DIIS/ODA,
+ * tridiagonalisation, eigenvalues and eigenvectors (with the host's waits for their sizes), back-transformation,
+ * density, gradients.  The counterpart of the reference's phase timings (pMolecule.QCModel.pyx:208-275). */
+#define PDG_WIDE_NPHASES 8
+int pdg_wide_phase_events(pdg_wide *wide, int enable);
+int pdg_wide_phase_times(pdg_wide *wide, float *h_ms);
 
 /* Text of the last error on this host thread (never NULL). */
 const char *pdg_last_error(void);

@@ -15,6 +15,7 @@ EN_TOTAL_ELECTRONIC, EN_ELECTRONIC, EN_NUCLEAR, EN_BASELINE, EN_QCMM, EN_ONE_ELE
 MAX_HISTORY = 16
 QCMM_FP32_PAIRS = 0x100   # pdg_qcmm_gradients model flag: FP32 pair terms (the mixed method)
 MM_FLAG_MM, MM_FLAG_QC_LJ, MM_FLAG_FIXED = 1, 2, 4   # pdg_mm_create atom flags
+WIDE_PHASES = ("integrals", "fock", "diis", "tridiagonal", "eigen", "backtransform", "density", "gradients")
 MM_TERMS = ("MM/MM Elect.", "MM/MM LJ", "MM/MM 1-4 Elect.", "MM/MM 1-4 LJ", "QC/MM LJ", "QC/MM 1-4 LJ")
 
 EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system_info", "pdg_workspace_bytes",
@@ -25,7 +26,8 @@ EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system
            "pdg_batch_graph_create", "pdg_graph_launch", "pdg_graph_destroy", "pdg_langevin_positions", "pdg_langevin_velocities",
            "pdg_normal_deviates", "pdg_density_combine", "pdg_mm_create", "pdg_mm_destroy", "pdg_mm_workspace_bytes",
            "pdg_mm_energy_gradients", "pdg_phase_events", "pdg_phase_times", "pdg_qcmm_workspace_bytes", "pdg_wide_create", "pdg_wide_destroy",
-           "pdg_wide_workspace_bytes", "pdg_wide_energy_gradients", "pdg_last_error")
+           "pdg_wide_workspace_bytes", "pdg_wide_energy_gradients", "pdg_wide_phase_events", "pdg_wide_phase_times",
+           "pdg_last_error")
 TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densities Tridiagonal", "QC Densities Eigenvalues",
           "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds",
           "QC Densities Cluster Rounds", "QC Densities Steps", "QC Densities Purification",
@@ -80,6 +82,8 @@ def load(path=LIB_PATH):
     L.pdg_wide_create.argtypes = [P, PP]
     L.pdg_wide_destroy.argtypes = [P]
     L.pdg_wide_workspace_bytes.argtypes = [P]
+    L.pdg_wide_phase_events.argtypes = [P, I]
+    L.pdg_wide_phase_times.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
     L.pdg_wide_workspace_bytes.restype = S
     L.pdg_wide_energy_gradients.argtypes = [P, P, P, ctypes.POINTER(SCFOptions), P, I, P, P, P, P, P, P, S, P]
     L.pdg_phase_times.argtypes = [P, ctypes.POINTER(ctypes.c_float)]

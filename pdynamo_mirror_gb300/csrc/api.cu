@@ -277,6 +277,18 @@ extern "C" int pdg_wide_destroy(pdg_wide *w)
     return PDG_OK;
 }
 
+extern "C" int pdg_wide_phase_events(pdg_wide *w, int enable)
+{
+    if (!w) return fail(PDG_BAD_ARGUMENT, "null argument");
+    return wide_timing(w, enable) ? fail(PDG_CUDA_ERROR, "pdg_wide_phase_events: event creation failed") : PDG_OK;
+}
+
+extern "C" int pdg_wide_phase_times(pdg_wide *w, float *h_ms)
+{
+    if (!w || !h_ms) return fail(PDG_BAD_ARGUMENT, "null argument");
+    return wide_phase_times(w, h_ms);
+}
+
 extern "C" size_t pdg_wide_workspace_bytes(const pdg_system *s)
 {
     return s ? wide_workspace_bytes(s->d) : 0;

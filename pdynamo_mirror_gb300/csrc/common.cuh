@@ -254,6 +254,8 @@ size_t qcmm_workspace_bytes(int n_frames, int n_mm);
 size_t wide_workspace_bytes(const DeviceSystem &s);
 int wide_create(const DeviceSystem &s, pdg_wide **out);
 size_t wide_workspace_size(const pdg_wide *W);
+int wide_timing(pdg_wide *W, int enable);
+int wide_phase_times(pdg_wide *W, float *ms);
 void wide_destroy(pdg_wide *W);
 int wide_energy_gradients(pdg_wide *W, const double *xyz, const double *phi, const pdg_scf_options &o, double *P, int use_density,
                           double *energies, double *gradients, double *charges, int *status, int *ncycles, double *ws, cudaStream_t st);

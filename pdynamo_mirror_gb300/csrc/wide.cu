@@ -669,20 +669,26 @@ __global__ void __launch_bounds__(WB) k_vblock(int N, int k0, int nb, const doub
     }
 }
 
-// T of the compact WY form I - V T V^T (upper triangular, dlarft 'Forward' 'Columnwise') from S = V^T V and tau.
+// T of the compact WY form I - V T V^T (upper triangular, dlarft 'Forward' 'Columnwise') from S = V^T V and tau: one
+// warp, column by column, lane i forming T[i][j] = -tau_j sum_{l=i}^{j-1} T[i][l] S[l][j] for i < j.
 __global__ void k_tblock(int nb, const double *__restrict__ S, const double *__restrict__ tau, int k0, double *__restrict__ T)
 {
-    if (threadIdx.x || blockIdx.x) return;
+    __shared__ double Ts[WNB * WNB];
+    const int i = threadIdx.x;
+    if (blockIdx.x || i >= 32) return;
+    for (int e = i; e < WNB * WNB; e += 32) Ts[e] = 0.0;
+    __syncwarp();
     for (int j = 0; j < nb; j++) {
         const double tj = tau[k0 + j];
-        T[j * WNB + j] = tj;
-        for (int i = 0; i < j; i++) {
-            double s = 0.0;
-            for (int l = i; l < j; l++) s += T[i * WNB + l] * S[j * nb + l];   // S column-major (nb x nb): S[l][j] = S[j * nb + l]
-            T[i * WNB + j] = -tj * s;
-        }
-        for (int i = j + 1; i < nb; i++) T[i * WNB + j] = 0.0;
+        double s = 0.0;
+        if (i < j)
+            for (int l = i; l < j; l++) s = fma(Ts[i * WNB + l], S[j * nb + l], s);   // S column-major: S[l][j] = S[j * nb + l]
+        __syncwarp();
+        if (i < j) Ts[i * WNB + j] = -tj * s;
+        if (i == j) Ts[j * WNB + j] = tj;
+        __syncwarp();
     }
+    for (int e = i; e < WNB * WNB; e += 32) T[e] = Ts[e];
 }
 
 // W2 = T W in place (T upper nb x nb, row-major with stride WNB; W nb x kv column-major with ld nb).
@@ -735,7 +741,7 @@ __global__ void __launch_bounds__(WB) k_guess(int N, double g, double *__restric
 }
 
 // Nuclear energy (pair terms in pair order) and the heat-of-formation baseline, one block.
-__global__ void __launch_bounds__(WB) k_init_ctl(DeviceSystem s, const double *__restrict__ pair_e, int valid, int hist, Ctl *c)
+__global__ void __launch_bounds__(WB) k_init_ctl(DeviceSystem s, const double *__restrict__ pair_e, int valid, int hist, int use_rca, Ctl *c)
 {
     __shared__ double red[32];
     double en = 0.0;
@@ -747,6 +753,7 @@ __global__ void __launch_bounds__(WB) k_init_ctl(DeviceSystem s, const double *_
     if (threadIdx.x == 0) {
         memset(c, 0, sizeof(Ctl));
         c->enuc = en; c->base = base; c->valid = valid; c->status = PDG_NOT_CONVERGED;
+        c->qrca = use_rca ? 1 : 0;   // ODA (RCA) until the DIIS onset, as the reference starts (DIISSCFConverger.c:147)
         for (int i = 0; i < hist; i++) c->slots[i] = i;
     }
 }
@@ -766,9 +773,17 @@ __global__ void k_finish(const Ctl *c, double *__restrict__ energies, int *__res
 // Host side.
 using namespace wide;
 
+// Phases of the per-call device timing (pdg_wide_phase_times).
+enum { WPH_INTEGRALS, WPH_FOCK, WPH_DIIS, WPH_TRIDIAGONAL, WPH_EIGEN, WPH_BACKTRANSFORM, WPH_DENSITY, WPH_GRADIENTS, WPH_N };
+
 struct pdg_wide {
     DeviceSystem s;
     WPlan w;
+    // phase timing: events recorded on the stream in order, each closing the phase it is tagged with
+    int timing = 0, n_marks = 0;
+    std::vector<cudaEvent_t> events;
+    std::vector<int> tags;
+    float phase_ms[WPH_N] = {};
     int grid;                      // blocks of the grid-wide kernels (the SM count)
     cublasHandle_t blas = nullptr;
     cudaGraphExec_t tri = nullptr; // the tridiagonalisation (2 (N - 2) kernels), replayed every density step
@@ -798,9 +813,48 @@ int wide_create(const DeviceSystem &s, pdg_wide **out)
     return PDG_OK;
 }
 
+static void mark(pdg_wide *W, cudaStream_t st, int phase)
+{
+    if (!W->timing || W->n_marks >= (int)W->events.size()) return;
+    cudaEventRecord(W->events[W->n_marks], st);
+    W->tags[W->n_marks++] = phase;
+}
+
+int wide_timing(pdg_wide *W, int enable)
+{
+    if (enable && W->events.empty()) {
+        W->events.resize(4096);
+        W->tags.resize(4096);
+        for (cudaEvent_t &e : W->events)
+            if (cudaEventCreate(&e) != cudaSuccess) return PDG_CUDA_ERROR;
+    }
+    W->timing = enable ? 1 : 0;
+    return PDG_OK;
+}
+
+int wide_phase_times(pdg_wide *W, float *ms)
+{
+    for (int k = 0; k < WPH_N; k++) ms[k] = W->phase_ms[k];
+    return PDG_OK;
+}
+
+// After a timed call: the device time between consecutive marks, summed per phase.
+static void collect(pdg_wide *W)
+{
+    for (int k = 0; k < WPH_N; k++) W->phase_ms[k] = 0.0f;
+    if (!W->timing || W->n_marks < 2) return;
+    cudaEventSynchronize(W->events[W->n_marks - 1]);
+    for (int k = 1; k < W->n_marks; k++) {
+        float t = 0.0f;
+        if (cudaEventElapsedTime(&t, W->events[k - 1], W->events[k]) == cudaSuccess) W->phase_ms[W->tags[k]] += t;
+    }
+}
+
 void wide_destroy(pdg_wide *W)
 {
     if (!W) return;
+    for (cudaEvent_t e : W->events)
+        if (e) cudaEventDestroy(e);
     if (W->tri) cudaGraphExecDestroy(W->tri);
     if (W->blas) cublasDestroy(W->blas);
     delete W;
@@ -856,6 +910,7 @@ static int wide_density_step(pdg_wide *W, double *ws, double *P, cudaStream_t st
     int rc = tri_graph(W, ws, st);
     if (rc) return rc;
     if (cudaGraphLaunch(W->tri, st) != cudaSuccess) return PDG_CUDA_ERROR;
+    mark(W, st, WPH_TRIDIAGONAL);
     // eigenvalues: the lowest n_occ (occupied) or the highest N - n_occ (virtual)
     const int first = s.vec_occupied ? 0 : N - kv;
     k_bisect<<<(kv + WB - 1) / WB, WB, 0, st>>>(N, first, kv, ws + p.d, ws + p.e, ws + p.eig);
@@ -886,6 +941,7 @@ static int wide_density_step(pdg_wide *W, double *ws, double *P, cudaStream_t st
     unsigned char *pv = (unsigned char *)(lu + 5 * (size_t)N * p.kvp);
     for (int r = 0; r < big; r++)
         k_invit<<<(kv + WB - 1) / WB, WB, 0, st>>>(N, kv, p.kvp, r, cstart, ws + p.d, ws + p.e, ws + p.eig, tn, lu, pv, ws + p.y, Zc);
+    mark(W, st, WPH_EIGEN);
     // back-transformation Zc <- Q Zc, blocks of WNB reflectors from the last to the first
     const int nref = N - 2;
     for (int k0 = ((nref - 1) / WNB) * WNB; k0 >= 0 && nref > 0; k0 -= WNB) {
@@ -893,17 +949,19 @@ static int wide_density_step(pdg_wide *W, double *ws, double *P, cudaStream_t st
         double *Vb = ws + p.vb, *S = ws + p.sb, *T = ws + p.tb, *Wm = ws + p.wb;
         k_vblock<<<G, WB, 0, st>>>(N, k0, nb, A, Vb);
         if (dgemm(W, st, CUBLAS_OP_T, CUBLAS_OP_N, nb, nb, m, 1.0, Vb, m, Vb, m, 0.0, S, nb) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
-        k_tblock<<<1, 1, 0, st>>>(nb, S, ws + p.tau, k0, T);
+        k_tblock<<<1, 32, 0, st>>>(nb, S, ws + p.tau, k0, T);
         // W = V^T Zc[k0+1:, :]   (nb x kv)
         if (dgemm(W, st, CUBLAS_OP_T, CUBLAS_OP_N, nb, kv, m, 1.0, Vb, m, Zc + k0 + 1, N, 0.0, Wm, nb) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
         k_trmm<<<(kv + WB - 1) / WB, WB, 0, st>>>(nb, kv, T, Wm);
         // Zc[k0+1:, :] -= V W2
         if (dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_N, m, kv, nb, -1.0, Vb, m, Wm, nb, 1.0, Zc + k0 + 1, N) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
     }
+    mark(W, st, WPH_BACKTRANSFORM);
     // C = Zc Zc^T (column-major N x N: symmetric, so also row-major), P from it
     if (dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_T, N, N, kv, 1.0, Zc, N, Zc, N, 0.0, C, N) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
     k_density<<<G, WB, 0, st>>>(N, s.vec_occupied, C, P, part, p.parts);
     k_control_density<<<1, 1, 0, st>>>((Ctl *)(ws + p.ctl), part, p.parts, G, N);
+    mark(W, st, WPH_DENSITY);
     return cudaGetLastError() == cudaSuccess ? PDG_OK : PDG_CUDA_ERROR;
 }
 
@@ -916,12 +974,15 @@ int wide_energy_gradients(pdg_wide *W, const double *xyz, const double *phi, con
     const size_t NN = (size_t)N * N;
     Ctl *ctl = (Ctl *)(ws + p.ctl);
     double *F = ws + p.F, *H = ws + p.fp.H, *part = ws + p.part, *C = ws + p.C;
+    W->n_marks = 0;
+    mark(W, st, WPH_INTEGRALS);
     // integrals (the frame kernels of integrals.cu on this one frame)
     launch_pair_integrals(s, p.fp, 1, xyz, ws, st);
     launch_assemble_h(s, p.fp, 1, ws, st);
     if (!use_density) k_guess<<<G, WB, 0, st>>>(N, (double)s.n_electrons / (double)N, P);
-    k_init_ctl<<<1, WB, 0, st>>>(s, ws + p.fp.pair_e, use_density ? 1 : 0, hist, ctl);
+    k_init_ctl<<<1, WB, 0, st>>>(s, ws + p.fp.pair_e, use_density ? 1 : 0, hist, o.use_rca, ctl);
     if (cudaGetLastError() != cudaSuccess) return PDG_CUDA_ERROR;
+    mark(W, st, WPH_INTEGRALS);
     const int nb_tr = G;
     for (int cycle = 0; cycle <= o.maximum_scf_cycles; cycle++) {
         // Fock build, energies, convergence test
@@ -930,6 +991,7 @@ int wide_energy_gradients(pdg_wide *W, const double *xyz, const double *phi, con
         k_traces<<<nb_tr, WB, 0, st>>>(N, P, H, F, part, p.parts);
         k_lowdin<<<1, WB, 0, st>>>(s, P, phi, F, charges, part, p.parts);
         k_control_fock<<<1, 1, 0, st>>>(ctl, part, p.parts, nb_tr, o, hist);
+        mark(W, st, WPH_FOCK);
         if (cudaMemcpyAsync(&W->host, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st) != cudaSuccess) return PDG_CUDA_ERROR;
         if (cudaStreamSynchronize(st) != cudaSuccess) return PDG_CUDA_ERROR;
         if (W->host.done || W->host.iteration >= o.maximum_scf_cycles) break;
@@ -957,6 +1019,7 @@ int wide_energy_gradients(pdg_wide *W, const double *xyz, const double *phi, con
             // no valid density yet (the diagonal guess): nothing to save; the reference does not count this cycle
             k_control_diis<<<1, 32, 0, st>>>(ctl, part, p.parts, 0, 0, o, hist);
         }
+        mark(W, st, WPH_DIIS);
         int rc = wide_density_step(W, ws, P, st);
         if (rc) return rc;
     }
@@ -965,6 +1028,8 @@ int wide_energy_gradients(pdg_wide *W, const double *xyz, const double *phi, con
         launch_pair_gradients(s, p.fp, 1, xyz, P, ws, st, false);
         launch_reduce_gradients(s, p.fp, 1, ws, gradients, st);
     }
+    mark(W, st, WPH_GRADIENTS);
     if (cudaGetLastError() != cudaSuccess) return PDG_CUDA_ERROR;
+    collect(W);
     return PDG_OK;
 }

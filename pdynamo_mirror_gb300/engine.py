@@ -207,6 +207,16 @@ class QCEngine:
         _native.check(self.L.pdg_phase_times(self.handle, out), "pdg_phase_times")
         return {"integrals": out[0], "scf": out[1], "gradients": out[2]}
 
+    def wide_phase_events(self, enable=True):
+        """Per-phase device timing of the wide path's later calls (pdg_wide_phase_events)."""
+        _native.check(self.L.pdg_wide_phase_events(self._wide, 1 if enable else 0), "pdg_wide_phase_events")
+
+    def wide_phase_times(self):
+        """Device milliseconds per phase of the last wide call (pdg_wide_phase_times), as {phase: ms}."""
+        out = (ctypes.c_float * len(_native.WIDE_PHASES))()
+        _native.check(self.L.pdg_wide_phase_times(self._wide, out), "pdg_wide_phase_times")
+        return dict(zip(_native.WIDE_PHASES, list(out)))
+
     def occupancy(self):
         """(threads per SCF CTA, dynamic shared bytes, resident SCF CTAs per SM)."""
         t, b, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
