@@ -398,8 +398,13 @@ int pdg_mm_energy_gradients(const pdg_mm_system *m, int n_frames, const double *
  * tridiagonalisation of two grid-wide kernels per column (replayed from a CUDA graph), bisection and inverse iteration
  * for the wanted eigenpairs, and a blocked compact-WY back-transformation and density by DGEMM; the integrals and
  * gradients are the pair kernels of pdg_energy_gradients on this one frame.  The results are those of
- * pdg_energy_gradients for the same frame (QCModel.Energy + EnergyGradients, pMolecule.QCModel.pyx:146-185), by the
- * reference's FP64 method whatever options->density_step asks.
+ * pdg_energy_gradients for the same frame (QCModel.Energy + EnergyGradients, pMolecule.QCModel.pyx:146-185).
+ * options->density_step 0 is the reference's FP64 method; 3 or 6 the mixed method of this path: every FP64 density step
+ * keeps a base (its matrix, density and all eigenpairs), and the following steps are perturbative ones around it in FP32
+ * products with small factors (scf.cu's perturbative step as SGEMMs), falling back to an FP64 step when the correction
+ * is not small; the DIIS error is formed in FP32 from the change of F; the sp-sp and sp-s pair gradient terms are FP32.
+ * The base stays with the wide engine and its workspace between calls, so a warm-started call (the next MD step) can run
+ * perturbative steps from its first cycle.
  *   pdg_wide_create       a wide engine for sys (which must outlive it); holds a cuBLAS handle and, after the first
  *                         call, the tridiagonalisation graph of the workspace it was given
  *   pdg_wide_workspace_bytes   the workspace one call needs (256-byte aligned)
@@ -414,10 +419,11 @@ int pdg_wide_energy_gradients(pdg_wide *wide, const double *d_xyz, const double 
                               double *d_density, int use_density, double *d_energies, double *d_gradients, double *d_charges,
                               int *d_status, int *d_ncycles, void *d_workspace, size_t workspace_bytes, void *stream);
 /* Device time per phase of the last pdg_wide_energy_gradients call (after pdg_wide_phase_events(wide, 1)), in
- * milliseconds, PDG_WIDE_NPHASES values: integrals, Fock builds (with the converger's energy test), DIIS/ODA,
- * tridiagonalisation, eigenvalues and eigenvectors (with the host's waits for their sizes), back-transformation,
- * density, gradients.  The counterpart of the reference's phase timings (pMolecule.QCModel.pyx:208-275). */
-#define PDG_WIDE_NPHASES 8
+ * milliseconds: integrals, Fock builds (with the converger's energy test), DIIS/ODA, tridiagonalisation, eigenvalues and
+ * eigenvectors (with the host's waits for their sizes), back-transformation, density (and the perturbative steps),
+ * gradients; then two counts: the call's FP64 density steps and its perturbative steps.  PDG_WIDE_NPHASES values in
+ * all.  The counterpart of the reference's phase timings (pMolecule.QCModel.pyx:208-275). */
+#define PDG_WIDE_NPHASES 10
 int pdg_wide_phase_events(pdg_wide *wide, int enable);
 int pdg_wide_phase_times(pdg_wide *wide, float *h_ms);
 

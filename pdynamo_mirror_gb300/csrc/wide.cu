@@ -44,8 +44,13 @@ struct Ctl {
 // regions of the grid-wide SCF.
 struct WPlan {
     FramePlan fp;   // only tei, pair_e, pair_g and H (the integral and gradient kernels' regions) are laid out
-    size_t F, A, C, rP, rF, hP, hF, hE, Zc, G, colbuf, vbuf, q, pk, part, d, e, tau, eig, cst, lu, y, vb, sb, tb, wb, ctl, total;
-    int kvp;   // vectors rounded up to 32 (interleaved inverse-iteration arrays)
+    size_t F, A, C, rP, rF, hP, hF, hE, Zc, G, colbuf, vbuf, q, pk, part, d, e, tau, eig, cst, lu, y, vb, sb, tb, wb, ctl;
+    // mixed method: the base of the perturbative steps (F0, P0, all eigenvalues, the complementary vectors in FP64), the
+    // matrix the last density step was applied to, and FP32 work (float offsets from f32)
+    size_t BF, BP, BL, Ft, Zcc, f32;
+    size_t D, ZY, V32, Gi, T1, E, Lp, T2, Mp, K, K2, R, EK, Am, U, Sm, WZ2, DQ, P32, f32_total;
+    size_t total;
+    int kvp;   // vectors rounded up to 32 (interleaved inverse-iteration arrays; wanted or complementary set)
     int parts; // partial-sum slots per reduction
 };
 
@@ -53,8 +58,8 @@ __host__ inline WPlan wide_plan(const DeviceSystem &s)
 {
     WPlan w;
     std::memset(&w, 0, sizeof(w));
-    const size_t N = s.n_basis, NN = N * N, kv = s.n_vec > 0 ? s.n_vec : 1;
-    w.kvp = (int)((kv + 31) & ~size_t(31));
+    const size_t N = s.n_basis, NN = N * N, kv = s.n_vec > 0 ? s.n_vec : 1, nc = N > kv ? N - kv : 1;
+    w.kvp = (int)((N + 31) & ~size_t(31));
     w.parts = 1024;
     size_t o = 0;
     auto take = [&](size_t n) { size_t r = o; o += align32(n); return r; };
@@ -73,6 +78,15 @@ __host__ inline WPlan wide_plan(const DeviceSystem &s)
     w.y = take(N * (size_t)w.kvp);
     w.vb = take(N * WNB); w.sb = take(WNB * WNB); w.tb = take(WNB * WNB); w.wb = take(WNB * kv);
     w.ctl = take((sizeof(Ctl) + 7) / 8);
+    w.BF = take(NN); w.BP = take(NN); w.BL = take(N); w.Ft = take(NN); w.Zcc = take(N * nc);
+    size_t f = 0;
+    auto tf = [&](size_t n) { size_t r = f; f += (n + 63) & ~size_t(63); return r; };
+    w.D = tf(NN); w.ZY = tf(2 * N * kv); w.V32 = tf(N * nc); w.Gi = tf(nc * kv); w.T1 = tf(N * kv); w.E = tf(nc * kv);
+    w.Lp = tf(kv * kv); w.T2 = tf(N * nc); w.Mp = tf(nc * nc); w.K = tf(nc * kv); w.K2 = tf(nc * kv); w.R = tf(nc * kv);
+    w.EK = tf(kv * kv); w.Am = tf(kv * kv); w.U = tf(kv * kv); w.Sm = tf(N * kv); w.WZ2 = tf(2 * N * kv); w.DQ = tf(NN);
+    w.P32 = tf(NN);
+    w.f32_total = f;
+    w.f32 = take((f + 1) / 2);
     w.total = align32(o);
     return w;
 }
@@ -233,7 +247,8 @@ __global__ void __launch_bounds__(WB) k_pack(size_t NN, const Ctl *c, const doub
 
 // Error vector from C: e_ij = sg (C_ij - C_ji) for i > j (C = G Z^T with G = F Z, or C = F P), into the newest slot
 // (strict lower triangle, dense row-major positions); block maxima to part slot 5.
-__global__ void __launch_bounds__(WB) k_error(int N, const Ctl *c, const double *__restrict__ C, double sg, double *__restrict__ hE,
+template <typename T>
+__global__ void __launch_bounds__(WB) k_error(int N, const Ctl *c, const T *__restrict__ C, double sg, double *__restrict__ hE,
                                               double *__restrict__ part, int parts)
 {
     __shared__ double red[32];
@@ -242,7 +257,7 @@ __global__ void __launch_bounds__(WB) k_error(int N, const Ctl *c, const double 
     double mx = 0.0;
     for (int i = gw; i < N; i += nw)
         for (int j = lane; j < i; j += 32) {
-            const double ev = sg * (C[(size_t)i * N + j] - C[(size_t)j * N + i]);
+            const double ev = sg * ((double)C[(size_t)i * N + j] - (double)C[(size_t)j * N + i]);
             he[(size_t)i * N + j] = ev;
             mx = fmax(mx, fabs(ev));
         }
@@ -573,9 +588,10 @@ __global__ void __launch_bounds__(WB) k_bisect(int N, int first, int nv, const d
 }
 
 // Inverse iteration for the nv wanted eigenvectors, one thread per vector: the LU factors of T - lambda I with row
-// interchanges (stored interleaved by vector), four solves from a hashed start vector, re-orthogonalisation after
-// every solve against the earlier vectors of the same cluster of close eigenvalues (as dstein), then normalisation.  Clusters run in rounds: round r handles the r-th member of every cluster, so every vector's cluster
-// predecessors are final.  Output: the vectors as columns of Zc (N x nv, column-major), in the tridiagonal basis.
+// interchanges (stored interleaved by vector, so the threads' accesses coalesce), four solves from a hashed start
+// vector with rescaling between them, then normalisation.  Output: the vectors as columns of Zc (N x nv, column-major),
+// in the tridiagonal basis.  Vectors of well-separated eigenvalues come out orthogonal to about eps ||T|| / gap; those of
+// close eigenvalues are orthonormalised afterwards within their cluster (k_cluster_mgs).
 __device__ __forceinline__ unsigned int whash(unsigned int a, unsigned int b)
 {
     unsigned int h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u + (a << 6) + (a >> 2));
@@ -583,15 +599,12 @@ __device__ __forceinline__ unsigned int whash(unsigned int a, unsigned int b)
     return h;
 }
 
-__global__ void __launch_bounds__(WB) k_invit(int N, int nv, int ld, int round, const int *__restrict__ cstart, const double *__restrict__ d,
-                                              const double *__restrict__ e, const double *__restrict__ eig, double tnorm,
-                                              double *__restrict__ lu, unsigned char *__restrict__ pv, double *__restrict__ y,
-                                              double *__restrict__ Zc)
+__global__ void __launch_bounds__(WB) k_invit(int N, int nv, int ld, const double *__restrict__ d, const double *__restrict__ e,
+                                              const double *__restrict__ eig, double tnorm, double *__restrict__ lu,
+                                              unsigned char *__restrict__ pv, double *__restrict__ y, double *__restrict__ Zc)
 {
     const int t = blockIdx.x * WB + threadIdx.x;
     if (t >= nv) return;
-    const int c0 = cstart[t];
-    if (t - c0 != round) return;
     const double sigma = eig[t], tiny = 1e-14 * tnorm + 1e-300;
     double *u0 = lu, *u1 = lu + (size_t)N * ld, *u2 = lu + 2 * (size_t)N * ld, *lm = lu + 3 * (size_t)N * ld;
     double ak = d[0] - sigma, bk = N > 1 ? e[0] : 0.0;
@@ -610,10 +623,11 @@ __global__ void __launch_bounds__(WB) k_invit(int N, int nv, int ld, int round, 
     if (fabs(ak) < tiny) ak = copysign(tiny, ak);
     u0[(size_t)(N - 1) * ld + t] = 1.0 / ak;
     for (int i = 0; i < N; i++) y[(size_t)i * ld + t] = ((whash(t * 2654435761u + 17u, i) >> 8) * (1.0 / 16777216.0)) * 2.0 - 1.0;
+    double sc = 1.0;
     for (int it = 0; it < 4; it++) {
-        double c = y[t];
+        double c = y[t] * sc;
         for (int k = 0; k < N - 1; k++) {
-            const double xn = y[(size_t)(k + 1) * ld + t], l = lm[(size_t)k * ld + t];
+            const double xn = y[(size_t)(k + 1) * ld + t] * sc, l = lm[(size_t)k * ld + t];
             const bool sw = pv[(size_t)k * ld + t];
             const double yk = sw ? xn : c, cn = sw ? c : xn;
             y[(size_t)k * ld + t] = yk;
@@ -626,20 +640,46 @@ __global__ void __launch_bounds__(WB) k_invit(int N, int nv, int ld, int round, 
             const double x0 = fma(-u2[o], x2, fma(-u1[o], x1, y[o])) * u0[o];
             y[o] = x0; x2 = x1; x1 = x0; mx = fmax(mx, fabs(x0));
         }
-        const double sc = mx > 0.0 ? 1.0 / mx : 1.0;
-        for (int i = 0; i < N; i++) y[(size_t)i * ld + t] *= sc;
-        for (int p = c0; p < t; p++) {
-            const double *zp = Zc + (size_t)p * N;
-            double dt = 0.0;
-            for (int i = 0; i < N; i++) dt = fma(y[(size_t)i * ld + t], zp[i], dt);
-            for (int i = 0; i < N; i++) y[(size_t)i * ld + t] = fma(-dt, zp[i], y[(size_t)i * ld + t]);
-        }
+        sc = mx > 0.0 ? 1.0 / mx : 1.0;   // folded into the next forward pass
     }
     double nr = 0.0;
-    for (int i = 0; i < N; i++) { const double v = y[(size_t)i * ld + t]; nr = fma(v, v, nr); }
-    const double s = 1.0 / sqrt(nr);
+    for (int i = 0; i < N; i++) { const double v = y[(size_t)i * ld + t] * sc; nr = fma(v, v, nr); }
+    const double s = sc / sqrt(nr);
     double *z = Zc + (size_t)t * N;
     for (int i = 0; i < N; i++) z[i] = y[(size_t)i * ld + t] * s;
+}
+
+// Modified Gram-Schmidt inside every cluster of close eigenvalues, one warp per cluster (lanes over the components):
+// each member is orthogonalised against the earlier ones (twice, for numerical safety) and normalised.  The span of a
+// cluster's vectors is its invariant subspace to within the contamination from farther eigenvalues, and the density
+// depends on the span only.
+__global__ void __launch_bounds__(WB) k_cluster_mgs(int N, int nv, const int *__restrict__ cstart, double *__restrict__ Zc)
+{
+    const int lane = threadIdx.x & 31, gw = blockIdx.x * WW + (threadIdx.x >> 5);
+    if (gw >= nv) return;
+    const int c0 = gw;
+    if (cstart[c0] != c0) return;   // warps start only at a cluster's first member
+    int c1 = c0 + 1;
+    while (c1 < nv && cstart[c1] == c0) c1++;
+    if (c1 - c0 < 2) return;
+    for (int t = c0; t < c1; t++) {
+        double *zt = Zc + (size_t)t * N;
+        for (int pass = 0; pass < 2; pass++)
+            for (int q = c0; q < t; q++) {
+                const double *zq = Zc + (size_t)q * N;
+                double dt = 0.0;
+                for (int i = lane; i < N; i += 32) dt = fma(zt[i], zq[i], dt);
+                dt = warp_sum(dt);
+                for (int i = lane; i < N; i += 32) zt[i] = fma(-dt, zq[i], zt[i]);
+                __syncwarp();
+            }
+        double nr = 0.0;
+        for (int i = lane; i < N; i += 32) nr = fma(zt[i], zt[i], nr);
+        nr = warp_sum(nr);
+        const double s = 1.0 / sqrt(nr);
+        for (int i = lane; i < N; i += 32) zt[i] *= s;
+        __syncwarp();
+    }
 }
 
 // Cluster starts (one thread; nv <= N): cstart[t] = first index of t's cluster; returns the largest cluster size.
@@ -767,6 +807,74 @@ __global__ void k_finish(const Ctl *c, double *__restrict__ energies, int *__res
     if (ncycles) *ncycles = c->iteration;
 }
 
+// ---------------------------------------------------------------------------------------------------------------
+// Mixed method (perturbative density steps; not in the reference).  FP32 elementwise helpers.
+__global__ void __launch_bounds__(WB) k_f32_diff(size_t n, const double *__restrict__ a, const double *__restrict__ b, float *__restrict__ out)
+{
+    for (size_t k = (size_t)blockIdx.x * WB + threadIdx.x; k < n; k += (size_t)gridDim.x * WB) out[k] = (float)(a[k] - (b ? b[k] : 0.0));
+}
+__global__ void __launch_bounds__(WB) k_f32_sum(size_t n, const float *__restrict__ a, const float *__restrict__ b, float *__restrict__ out)
+{
+    for (size_t k = (size_t)blockIdx.x * WB + threadIdx.x; k < n; k += (size_t)gridDim.x * WB) out[k] = a[k] + b[k];
+}
+// Gi (nc x kv, column-major) = 1 / (lambda_a - mu_i); BL = wanted eigenvalues, then the complementary ones
+__global__ void __launch_bounds__(WB) k_gaps(int kv, int nc, const double *__restrict__ BL, float *__restrict__ Gi)
+{
+    for (int e = blockIdx.x * WB + threadIdx.x; e < kv * nc; e += gridDim.x * WB) {
+        const int a = e / nc, i = e % nc;
+        Gi[e] = (float)(1.0 / (BL[a] - BL[kv + i]));
+    }
+}
+// K2 = (E + R) o Gi; block maxima of |K2 - K| and |K2| to part slots 28, 29
+__global__ void __launch_bounds__(WB) k_sweep(size_t n, const float *__restrict__ E, const float *__restrict__ R, const float *__restrict__ Gi,
+                                              const float *__restrict__ K, float *__restrict__ K2, int first, double *__restrict__ part, int parts)
+{
+    __shared__ double red[32];
+    float dm = 0.f, km = 0.f;
+    for (size_t k = (size_t)blockIdx.x * WB + threadIdx.x; k < n; k += (size_t)gridDim.x * WB) {
+        const float kn = (E[k] + (first ? 0.f : R[k])) * Gi[k];
+        dm = fmaxf(dm, fabsf(kn - (first ? 0.f : K[k]))); km = fmaxf(km, fabsf(kn));
+        K2[k] = kn;
+    }
+    const double d = block_max((double)dm, red), m = block_max((double)km, red);
+    if (threadIdx.x == 0) { part[28 * (size_t)parts + blockIdx.x] = d; part[29 * (size_t)parts + blockIdx.x] = m; }
+}
+__global__ void k_sweep_max(const double *__restrict__ part, int parts, int nb, double *__restrict__ out)
+{
+    if (threadIdx.x || blockIdx.x) return;
+    double d = 0.0, m = 0.0;
+    for (int b = 0; b < nb; b++) { d = fmax(d, part[28 * (size_t)parts + b]); m = fmax(m, part[29 * (size_t)parts + b]); }
+    out[0] = d; out[1] = m;
+}
+// y += alpha x (FP32)
+__global__ void __launch_bounds__(WB) k_f32_axpy(size_t n, float alpha, const float *__restrict__ x, float *__restrict__ y)
+{
+    for (size_t k = (size_t)blockIdx.x * WB + threadIdx.x; k < n; k += (size_t)gridDim.x * WB) y[k] = fmaf(alpha, x[k], y[k]);
+}
+// P = P0 + c dQ (dQ column-major N x N, taken from one triangle for both entries); block partials of the squared change
+__global__ void __launch_bounds__(WB) k_pert_density(int N, double c, const double *__restrict__ BP, const float *__restrict__ DQ,
+                                                     double *__restrict__ P, double *__restrict__ part, int parts)
+{
+    __shared__ double red[32];
+    const size_t NN = (size_t)N * N;
+    double r = 0.0;
+    for (size_t k = (size_t)blockIdx.x * WB + threadIdx.x; k < NN; k += (size_t)gridDim.x * WB) {
+        const int i = (int)(k / N), j = (int)(k % N);
+        const double v = (double)DQ[(size_t)min(i, j) * N + max(i, j)];
+        const double pn = BP[k] + c * v;
+        const double dl = pn - P[k];
+        r = fma(dl, dl, r);
+        P[k] = pn;
+    }
+    r = block_reduce(r, red);
+    if (threadIdx.x == 0) part[6 * (size_t)parts + blockIdx.x] = r;
+}
+__global__ void __launch_bounds__(WB) k_copy(size_t n, const double *__restrict__ a, double *__restrict__ b)
+{
+    for (size_t k = (size_t)blockIdx.x * WB + threadIdx.x; k < n; k += (size_t)gridDim.x * WB) b[k] = a[k];
+}
+__global__ void k_set_have_z(Ctl *c, int v) { if (threadIdx.x == 0 && blockIdx.x == 0) c->have_z = v; }
+
 }  // namespace wide
 
 // =================================================================================================================
@@ -790,6 +898,11 @@ struct pdg_wide {
     cudaStream_t tri_stream = nullptr;
     double *tri_ws = nullptr;      // workspace base the graph was captured on
     Ctl host;                      // last control record read back
+    // mixed method: the base of the perturbative steps is valid for this workspace
+    int base_ok = 0;
+    double *base_ws = nullptr;
+    double sweep[2];               // last perturbative sweep: max change of K, max |K|
+    int pert_steps = 0, fp64_steps = 0;   // density steps of the last call
 };
 
 static int cublas_ok(cublasStatus_t st, const char *what);
@@ -835,6 +948,8 @@ int wide_timing(pdg_wide *W, int enable)
 int wide_phase_times(pdg_wide *W, float *ms)
 {
     for (int k = 0; k < WPH_N; k++) ms[k] = W->phase_ms[k];
+    ms[WPH_N] = (float)W->fp64_steps;
+    ms[WPH_N + 1] = (float)W->pert_steps;
     return PDG_OK;
 }
 
@@ -868,6 +983,13 @@ static cublasStatus_t dgemm(pdg_wide *W, cudaStream_t st, cublasOperation_t ta, 
     return cublasDgemm(W->blas, ta, tb, m, n, k, &alpha, A, lda, B, ldb, &beta, C, ldc);
 }
 
+static cublasStatus_t sgemm(pdg_wide *W, cudaStream_t st, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
+                            float alpha, const float *A, int lda, const float *B, int ldb, float beta, float *C, int ldc)
+{
+    cublasSetStream(W->blas, st);
+    return cublasSgemm(W->blas, ta, tb, m, n, k, &alpha, A, lda, B, ldb, &beta, C, ldc);
+}
+
 // The tridiagonalisation of A (plan regions of this workspace) as one CUDA graph, captured on first use.
 static int tri_graph(pdg_wide *W, double *ws, cudaStream_t st)
 {
@@ -899,23 +1021,59 @@ static int tri_graph(pdg_wide *W, double *ws, cudaStream_t st)
     return PDG_OK;
 }
 
-// One FP64 density step: P <- density of the wanted eigenvectors of F; the vectors stay in Zc for the DIIS save.
-static int wide_density_step(pdg_wide *W, double *ws, double *P, cudaStream_t st)
+// Eigenpairs [first, first + nv) of the tridiagonal T in d, e (eigenvalues to eig_out): bisection, inverse iteration with
+// cluster re-orthogonalisation, and the blocked back-transformation by the reflectors stored in A; the vectors end as the
+// columns of Zout (N x nv, column-major).  tn: the Gershgorin bound of T.
+static int wide_eigenvectors(pdg_wide *W, double *ws, int first, int nv, double *Zout, double *eig_out, double tn, cudaStream_t st)
+{
+    const WPlan &p = W->w;
+    const int N = W->s.n_basis, G = W->grid;
+    double *A = ws + p.A;
+    k_bisect<<<(nv + WB - 1) / WB, WB, 0, st>>>(N, first, nv, ws + p.d, ws + p.e, eig_out);
+    // Inverse iteration at an eigenvalue converged to round-off leaves a vector's overlap with another eigenvector at
+    // about eps ||T|| / gap: below 1e-11 for gaps above 1e-5 ||T||, so only closer eigenvalues form clusters, whose
+    // vectors are orthonormalised after the iteration.
+    int *cstart = (int *)(ws + p.cst), *maxsize = cstart + N;
+    k_clusters<<<1, 1, 0, st>>>(nv, eig_out, 1.0e-5 * tn, cstart, maxsize);
+    double *lu = ws + p.lu;
+    unsigned char *pv = (unsigned char *)(lu + 5 * (size_t)N * p.kvp);
+    k_invit<<<(nv + WB - 1) / WB, WB, 0, st>>>(N, nv, p.kvp, ws + p.d, ws + p.e, eig_out, tn, lu, pv, ws + p.y, Zout);
+    k_cluster_mgs<<<(nv + WW - 1) / WW, WB, 0, st>>>(N, nv, cstart, Zout);
+    mark(W, st, WPH_EIGEN);
+    // back-transformation Zout <- Q Zout, blocks of WNB reflectors from the last to the first
+    const int nref = N - 2;
+    for (int k0 = ((nref - 1) / WNB) * WNB; k0 >= 0 && nref > 0; k0 -= WNB) {
+        const int nb = min(WNB, nref - k0), m = N - k0 - 1;
+        double *Vb = ws + p.vb, *S = ws + p.sb, *T = ws + p.tb, *Wm = ws + p.wb;
+        k_vblock<<<G, WB, 0, st>>>(N, k0, nb, A, Vb);
+        if (dgemm(W, st, CUBLAS_OP_T, CUBLAS_OP_N, nb, nb, m, 1.0, Vb, m, Vb, m, 0.0, S, nb) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
+        k_tblock<<<1, 32, 0, st>>>(nb, S, ws + p.tau, k0, T);
+        for (int c0 = 0; c0 < nv; c0 += N) {   // the W buffer holds WNB x N: columns in chunks of N
+            const int nvc = min(N, nv - c0);
+            if (dgemm(W, st, CUBLAS_OP_T, CUBLAS_OP_N, nb, nvc, m, 1.0, Vb, m, Zout + (size_t)c0 * N + k0 + 1, N, 0.0, Wm, nb) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
+            k_trmm<<<(nvc + WB - 1) / WB, WB, 0, st>>>(nb, nvc, T, Wm);
+            if (dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_N, m, nvc, nb, -1.0, Vb, m, Wm, nb, 1.0, Zout + (size_t)c0 * N + k0 + 1, N) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
+        }
+    }
+    mark(W, st, WPH_BACKTRANSFORM);
+    return cudaGetLastError() == cudaSuccess ? PDG_OK : PDG_CUDA_ERROR;
+}
+
+// One FP64 density step: P <- density of the wanted eigenvectors of F; the vectors stay in Zc for the DIIS save.  With
+// make_base (the mixed method) it also keeps the base of the following perturbative steps: F0 = F, P0 = P, the wanted
+// vectors in FP32, the complementary eigenpairs (from the same tridiagonal form, vectors rounded to FP32) and the
+// reciprocal gaps.
+static int wide_density_step(pdg_wide *W, double *ws, double *P, cudaStream_t st, bool make_base)
 {
     const DeviceSystem &s = W->s;
     const WPlan &p = W->w;
-    const int N = s.n_basis, kv = s.n_vec, G = W->grid;
+    const int N = s.n_basis, kv = s.n_vec, nc = N - kv, G = W->grid;
     double *F = ws + p.F, *A = ws + p.A, *C = ws + p.C, *Zc = ws + p.Zc, *part = ws + p.part;
     k_tri_start<<<G, WB, 0, st>>>(N, F, A, ws + p.colbuf);
     int rc = tri_graph(W, ws, st);
     if (rc) return rc;
     if (cudaGraphLaunch(W->tri, st) != cudaSuccess) return PDG_CUDA_ERROR;
     mark(W, st, WPH_TRIDIAGONAL);
-    // eigenvalues: the lowest n_occ (occupied) or the highest N - n_occ (virtual)
-    const int first = s.vec_occupied ? 0 : N - kv;
-    k_bisect<<<(kv + WB - 1) / WB, WB, 0, st>>>(N, first, kv, ws + p.d, ws + p.e, ws + p.eig);
-    // clusters of close eigenvalues, whose vectors are re-orthogonalised against each other
-    int *cstart = (int *)(ws + p.cst), *maxsize = cstart + N;
     double bounds[2];
     {
         // Gershgorin bound of T, for the cluster gap and the pivot floor
@@ -930,38 +1088,93 @@ static int wide_density_step(pdg_wide *W, double *ws, double *P, cudaStream_t st
         }
         bounds[0] = lo; bounds[1] = hi;
     }
-    // Inverse iteration at an eigenvalue converged to round-off leaves a vector's overlap with another eigenvector at
-    // about eps ||T|| / gap: below 1e-11 for gaps above 1e-5 ||T||, so only closer eigenvalues form clusters.
     const double tn = fmax(fabs(bounds[0]), fabs(bounds[1]));
-    k_clusters<<<1, 1, 0, st>>>(kv, ws + p.eig, 1.0e-5 * tn, cstart, maxsize);
-    int big = 0;
-    if (cudaMemcpyAsync(&big, maxsize, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return PDG_CUDA_ERROR;
-    if (cudaStreamSynchronize(st) != cudaSuccess) return PDG_CUDA_ERROR;
-    double *lu = ws + p.lu;
-    unsigned char *pv = (unsigned char *)(lu + 5 * (size_t)N * p.kvp);
-    for (int r = 0; r < big; r++)
-        k_invit<<<(kv + WB - 1) / WB, WB, 0, st>>>(N, kv, p.kvp, r, cstart, ws + p.d, ws + p.e, ws + p.eig, tn, lu, pv, ws + p.y, Zc);
-    mark(W, st, WPH_EIGEN);
-    // back-transformation Zc <- Q Zc, blocks of WNB reflectors from the last to the first
-    const int nref = N - 2;
-    for (int k0 = ((nref - 1) / WNB) * WNB; k0 >= 0 && nref > 0; k0 -= WNB) {
-        const int nb = min(WNB, nref - k0), m = N - k0 - 1;
-        double *Vb = ws + p.vb, *S = ws + p.sb, *T = ws + p.tb, *Wm = ws + p.wb;
-        k_vblock<<<G, WB, 0, st>>>(N, k0, nb, A, Vb);
-        if (dgemm(W, st, CUBLAS_OP_T, CUBLAS_OP_N, nb, nb, m, 1.0, Vb, m, Vb, m, 0.0, S, nb) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
-        k_tblock<<<1, 32, 0, st>>>(nb, S, ws + p.tau, k0, T);
-        // W = V^T Zc[k0+1:, :]   (nb x kv)
-        if (dgemm(W, st, CUBLAS_OP_T, CUBLAS_OP_N, nb, kv, m, 1.0, Vb, m, Zc + k0 + 1, N, 0.0, Wm, nb) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
-        k_trmm<<<(kv + WB - 1) / WB, WB, 0, st>>>(nb, kv, T, Wm);
-        // Zc[k0+1:, :] -= V W2
-        if (dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_N, m, kv, nb, -1.0, Vb, m, Wm, nb, 1.0, Zc + k0 + 1, N) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
-    }
-    mark(W, st, WPH_BACKTRANSFORM);
+    // the wanted eigenpairs: the lowest n_occ (occupied) or the highest N - n_occ (virtual)
+    if ((rc = wide_eigenvectors(W, ws, s.vec_occupied ? 0 : N - kv, kv, Zc, ws + p.eig, tn, st))) return rc;
     // C = Zc Zc^T (column-major N x N: symmetric, so also row-major), P from it
     if (dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_T, N, N, kv, 1.0, Zc, N, Zc, N, 0.0, C, N) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
     k_density<<<G, WB, 0, st>>>(N, s.vec_occupied, C, P, part, p.parts);
     k_control_density<<<1, 1, 0, st>>>((Ctl *)(ws + p.ctl), part, p.parts, G, N);
     mark(W, st, WPH_DENSITY);
+    if (make_base && nc > 0) {
+        float *f32 = (float *)(ws + p.f32);
+        const size_t NN = (size_t)N * N;
+        k_copy<<<G, WB, 0, st>>>(NN, F, ws + p.BF);
+        k_copy<<<G, WB, 0, st>>>(NN, P, ws + p.BP);
+        k_copy<<<1, WB, 0, st>>>((size_t)kv, ws + p.eig, ws + p.BL);
+        k_f32_diff<<<G, WB, 0, st>>>((size_t)N * kv, Zc, nullptr, f32 + p.ZY);
+        if ((rc = wide_eigenvectors(W, ws, s.vec_occupied ? kv : 0, nc, ws + p.Zcc, ws + p.BL + kv, tn, st))) return rc;
+        k_f32_diff<<<G, WB, 0, st>>>((size_t)N * nc, ws + p.Zcc, nullptr, f32 + p.V32);
+        k_gaps<<<G, WB, 0, st>>>(kv, nc, ws + p.BL, f32 + p.Gi);
+        W->base_ok = 1;
+        W->base_ws = ws;
+        mark(W, st, WPH_DENSITY);
+    }
+    return cudaGetLastError() == cudaSuccess ? PDG_OK : PDG_CUDA_ERROR;
+}
+
+// Perturbative density step around the base (the device counterpart of scf.cu's density_step_pert, every product a
+// cuBLAS SGEMM): for F = F0 + dF, the wanted invariant subspace is spanned by the columns of Z0 + V K, K (nc x kv)
+// solving E + M' K - K L' - K E^T K = (lambda_a - mu_i) K_ia with E = V^T dF Z0, L' = Z0^T dF Z0, M' = V^T dF V (fixed-
+// point sweeps from K = E / (lambda - mu)); the new projector differs from Z0 Z0^T by dQ = Z0 W^T + Y (Z0 + W)^T, Y = V K,
+// U = (1 + K^T K)^-1 - 1 = -A + A^2 (A = K^T K), W = Y + (Z0 + Y) U; P = P0 + 2 dQ (occupied) or P0 - 2 dQ.  Every FP32
+// product has a small factor (dF, K, Y, W).  Returns 1 when it produced P, 0 when the base does not carry the step (the
+// sweeps do not settle or |K| >= 2e-3: the caller runs an FP64 step, which makes a new base).
+static int wide_pert_step(pdg_wide *W, double *ws, double *P, cudaStream_t st, int *done)
+{
+    const DeviceSystem &s = W->s;
+    const WPlan &p = W->w;
+    const int N = s.n_basis, kv = s.n_vec, nc = N - kv, G = W->grid;
+    const size_t NN = (size_t)N * N;
+    float *f = (float *)(ws + p.f32);
+    float *D = f + p.D, *Z0 = f + p.ZY, *Yc = f + p.ZY + (size_t)N * kv, *V = f + p.V32, *Gi = f + p.Gi, *T1 = f + p.T1, *E = f + p.E;
+    float *Lp = f + p.Lp, *T2 = f + p.T2, *Mp = f + p.Mp, *K = f + p.K, *K2 = f + p.K2, *R = f + p.R, *EK = f + p.EK, *Am = f + p.Am;
+    float *U = f + p.U, *Sm = f + p.Sm, *Wc = f + p.WZ2, *WZ = f + p.WZ2 + (size_t)N * kv, *DQ = f + p.DQ;
+    double *part = ws + p.part, *mx = ws + p.part + 30 * (size_t)p.parts;
+    const cublasOperation_t Nn = CUBLAS_OP_N, Tt = CUBLAS_OP_T;
+    *done = 0;
+    if (nc <= 0) return PDG_OK;
+    k_f32_diff<<<G, WB, 0, st>>>(NN, ws + p.F, ws + p.BF, D);
+    if (sgemm(W, st, Nn, Nn, N, kv, N, 1.f, D, N, Z0, N, 0.f, T1, N) ||                 // T1 = dF Z0
+        sgemm(W, st, Tt, Nn, nc, kv, N, 1.f, V, N, T1, N, 0.f, E, nc) ||                // E = V^T T1
+        sgemm(W, st, Tt, Nn, kv, kv, N, 1.f, Z0, N, T1, N, 0.f, Lp, kv) ||              // L' = Z0^T T1
+        sgemm(W, st, Nn, Nn, N, nc, N, 1.f, D, N, V, N, 0.f, T2, N) ||                  // T2 = dF V
+        sgemm(W, st, Tt, Nn, nc, nc, N, 1.f, V, N, T2, N, 0.f, Mp, nc))                 // M' = V^T T2
+        return PDG_CUDA_ERROR;
+    k_sweep<<<G, WB, 0, st>>>((size_t)nc * kv, E, R, Gi, K, K, 1, part, p.parts);     // K = E / (lambda - mu)
+    bool settled = false;
+    double kmax = 0.0;
+    for (int it = 0; it < 12 && !settled; it++) {
+        if (sgemm(W, st, Tt, Nn, kv, kv, nc, 1.f, E, nc, K, nc, 0.f, EK, kv)) return PDG_CUDA_ERROR;   // E^T K
+        k_f32_axpy<<<1, WB, 0, st>>>((size_t)kv * kv, 1.f, Lp, EK);                                      // L' + E^T K
+        if (sgemm(W, st, Nn, Nn, nc, kv, nc, 1.f, Mp, nc, K, nc, 0.f, R, nc) ||                          // M' K
+            sgemm(W, st, Nn, Nn, nc, kv, kv, -1.f, K, nc, EK, kv, 1.f, R, nc))                           // - K (L' + E^T K)
+            return PDG_CUDA_ERROR;
+        k_sweep<<<G, WB, 0, st>>>((size_t)nc * kv, E, R, Gi, K, K2, 0, part, p.parts);
+        k_sweep_max<<<1, 1, 0, st>>>(part, p.parts, G, mx);
+        if (cudaMemcpyAsync(W->sweep, mx, 2 * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess) return PDG_CUDA_ERROR;
+        if (cudaStreamSynchronize(st) != cudaSuccess) return PDG_CUDA_ERROR;
+        float *tmp = K; K = K2; K2 = tmp;
+        kmax = W->sweep[1];
+        settled = W->sweep[0] <= 1.0e-5 * W->sweep[1] + 1.0e-30;
+    }
+    // |K| bounds the FP32 rounding carried into P (~1e-7 |K| per product): 2e-3 keeps it far below the 1e-8 tolerance
+    if (!settled || !(kmax < 2.0e-3)) return PDG_OK;
+    if (sgemm(W, st, Nn, Nn, N, kv, nc, 1.f, V, N, K, nc, 0.f, Yc, N) ||               // Y = V K
+        sgemm(W, st, Tt, Nn, kv, kv, nc, 1.f, K, nc, K, nc, 0.f, Am, kv) ||            // A = K^T K
+        sgemm(W, st, Nn, Nn, kv, kv, kv, 1.f, Am, kv, Am, kv, 0.f, U, kv))             // A^2
+        return PDG_CUDA_ERROR;
+    k_f32_axpy<<<1, WB, 0, st>>>((size_t)kv * kv, -1.f, Am, U);                          // U = A^2 - A
+    k_f32_sum<<<G, WB, 0, st>>>((size_t)N * kv, Z0, Yc, Sm);                             // S = Z0 + Y
+    if (cudaMemcpyAsync(Wc, Yc, sizeof(float) * (size_t)N * kv, cudaMemcpyDeviceToDevice, st) != cudaSuccess) return PDG_CUDA_ERROR;
+    if (sgemm(W, st, Nn, Nn, N, kv, kv, 1.f, Sm, N, U, kv, 1.f, Wc, N)) return PDG_CUDA_ERROR;   // W = Y + S U
+    k_f32_sum<<<G, WB, 0, st>>>((size_t)N * kv, Z0, Wc, WZ);                                       // Z0 + W
+    // dQ = [Z0 | Y] [W | Z0 + W]^T
+    if (sgemm(W, st, Nn, Tt, N, N, 2 * kv, 1.f, Z0, N, Wc, N, 0.f, DQ, N)) return PDG_CUDA_ERROR;
+    k_pert_density<<<G, WB, 0, st>>>(N, s.vec_occupied ? 2.0 : -2.0, ws + p.BP, DQ, P, part, p.parts);
+    k_control_density<<<1, 1, 0, st>>>((Ctl *)(ws + p.ctl), part, p.parts, G, N);
+    mark(W, st, WPH_DENSITY);
+    *done = 1;
     return cudaGetLastError() == cudaSuccess ? PDG_OK : PDG_CUDA_ERROR;
 }
 
@@ -984,6 +1197,9 @@ int wide_energy_gradients(pdg_wide *W, const double *xyz, const double *phi, con
     if (cudaGetLastError() != cudaSuccess) return PDG_CUDA_ERROR;
     mark(W, st, WPH_INTEGRALS);
     const int nb_tr = G;
+    const bool mixed = o.density_step != 0;
+    bool have_ft = false;   // F~ of the last density step is in the workspace (mixed method)
+    W->pert_steps = W->fp64_steps = 0;
     for (int cycle = 0; cycle <= o.maximum_scf_cycles; cycle++) {
         // Fock build, energies, convergence test
         k_pk<<<G, WB, 0, st>>>(s, P, ws + p.pk);
@@ -999,7 +1215,15 @@ int wide_energy_gradients(pdg_wide *W, const double *xyz, const double *phi, con
         if (W->host.valid) {
             k_pack<<<G, WB, 0, st>>>(NN, ctl, P, F, ws + p.hP, ws + p.hF);
             double sg = 1.0;
-            if (W->host.have_z) {
+            if (have_ft) {
+                // mixed method: P is the projector of F~ (the matrix its density step was applied to), so F P - P F =
+                // dF P - P dF with dF = F - F~, small once the SCF settles: its FP32 product carries ~1e-7 |dF|
+                float *f32 = (float *)(ws + p.f32);
+                k_f32_diff<<<G, WB, 0, st>>>(NN, F, ws + p.Ft, f32 + p.D);
+                k_f32_diff<<<G, WB, 0, st>>>(NN, P, nullptr, f32 + p.P32);
+                if (sgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_N, N, N, N, 1.f, f32 + p.D, N, f32 + p.P32, N, 0.f, f32 + p.DQ, N) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
+                k_error<float><<<G, WB, 0, st>>>(N, ctl, f32 + p.DQ, -1.0, ws + p.hE, part, p.parts);
+            } else if (W->host.have_z) {
                 // P = 2 Zc Zc^T (or 2 (1 - Zc Zc^T)): F P - P F = sg (G Zc^T - Zc G^T), G = F Zc
                 if (dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_N, N, s.n_vec, N, 1.0, F, N, ws + p.Zc, N, 0.0, ws + p.G, N) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
                 // C (column-major) = G Zc^T, i.e. row-major C^T: the error kernel reads C_ij - C_ji, so the sign flips
@@ -1010,7 +1234,7 @@ int wide_energy_gradients(pdg_wide *W, const double *xyz, const double *phi, con
                 if (dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_N, N, N, N, 1.0, F, N, P, N, 0.0, C, N) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
                 sg = -1.0;
             }
-            k_error<<<G, WB, 0, st>>>(N, ctl, C, sg, ws + p.hE, part, p.parts);
+            if (!have_ft) k_error<double><<<G, WB, 0, st>>>(N, ctl, C, sg, ws + p.hE, part, p.parts);
             k_dots<<<G, WB, 0, st>>>(N, ctl, ws + p.hE, part, p.parts);
             if (o.use_rca) k_oda_traces<<<G, WB, 0, st>>>(NN, F, P, ws + p.rF, ws + p.rP, part, p.parts);
             k_control_diis<<<1, 32, 0, st>>>(ctl, part, p.parts, G, G, o, hist);
@@ -1020,12 +1244,23 @@ int wide_energy_gradients(pdg_wide *W, const double *xyz, const double *phi, con
             k_control_diis<<<1, 32, 0, st>>>(ctl, part, p.parts, 0, 0, o, hist);
         }
         mark(W, st, WPH_DIIS);
-        int rc = wide_density_step(W, ws, P, st);
-        if (rc) return rc;
+        int rc;
+        if (mixed) {
+            k_copy<<<G, WB, 0, st>>>(NN, F, ws + p.Ft);
+            int done = 0;
+            if (W->base_ok && W->base_ws == ws && (rc = wide_pert_step(W, ws, P, st, &done))) return rc;
+            if (!done && (rc = wide_density_step(W, ws, P, st, true))) return rc;
+            have_ft = true;
+            if (done) W->pert_steps++; else W->fp64_steps++;
+        } else {
+            if ((rc = wide_density_step(W, ws, P, st, false))) return rc;
+            W->fp64_steps++;
+        }
     }
     k_finish<<<1, 1, 0, st>>>(ctl, energies, status, ncycles);
     if (gradients) {
-        launch_pair_gradients(s, p.fp, 1, xyz, P, ws, st, false);
+        // the mixed method takes the sp-sp and sp-s pair gradient terms in FP32 (assembled and summed in FP64)
+        launch_pair_gradients(s, p.fp, 1, xyz, P, ws, st, mixed);
         launch_reduce_gradients(s, p.fp, 1, ws, gradients, st);
     }
     mark(W, st, WPH_GRADIENTS);

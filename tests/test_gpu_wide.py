@@ -7,7 +7,10 @@
 * a warm start from the converged density converges again in at most two cycles to the same energy;
 * the large QC/MM system (200 QC waters, 600 atoms, N = 1200, in 20000 TIP3P waters; the engine picks the wide path
   by size) through System.Energy against the oracle's fixture (tests/golden/large_qcmm_reference.json): energy terms,
-  QC gradients, the MM gradients of the 400 MM atoms nearest the QC region and the sum of all MM gradients.
+  QC gradients, the MM gradients of the 400 MM atoms nearest the QC region and the sum of all MM gradients; with the
+  plain FP64 method and with the mixed method (perturbative density steps around an FP64 base, FP32 DIIS errors and
+  pair-gradient terms), and the mixed method again on a displaced geometry warm-started from the first (an MD step:
+  its density steps are all perturbative ones around the kept base) against the plain method on that geometry.
 """
 import json, os
 
@@ -80,14 +83,42 @@ def test_wide_cluster_matches_oracle_and_warm_start():
     assert abs(float(r2["energies"][0, 0]) - float(E[0])) < 1e-9
 
 
-def test_large_qcmm_system_matches_oracle_fixture():
-    from pdynamo_mirror_gb300 import NBModelABFS, QCModelMNDO, System, workloads
+@pytest.mark.parametrize("method", ["fp64", "mixed"])
+def test_wide_mixed_water_box_matches_oracle(method):
+    from pdynamo_mirror_gb300 import DIISSCFConverger, NBModelABFS, QCModelMNDO, System, workloads
+    from pdynamo_mirror_gb300.converger import MIXED_METHOD
+    from pdynamo_mirror_gb300.engine import QCEngine
+    Z, X, Q, sel, charge, frames = workloads.qcmm_water_box_frames(2)
+    nq = len(sel)
+    s = System(Z, X, mmCharges=Q)
+    s.electronicState.charge = charge
+    s.DefineQCModel(QCModelMNDO("am1", converger=DIISSCFConverger(**(MIXED_METHOD if method == "mixed" else {}))), qcSelection=sel)
+    s.DefineNBModel(NBModelABFS(innerCutoff=8.0, outerCutoff=12.0))
+    s._engine, s._engine_charge = QCEngine("am1", list(Z[:nq]), charge, wide=True), charge
+    E, G, terms = s.EnergyBatch(frames, doGradients=True, warmStart=False)
+    knots = O.abfs_knots(8.0, 12.0)
+    for f in range(2):
+        X_ = frames[f]
+        phi, _, _ = O.qcmm("abfs", X_[:nq], X_[nq:], Q[nq:], knots=knots)
+        r = O.System(O.Hamiltonian("am1", list(Z[:nq])), list(Z[:nq]), charge=charge).energy(X_[:nq], phi=phi)
+        _, gq, gm = O.qcmm("abfs", X_[:nq], X_[nq:], Q[nq:], qcq=r["charges"], knots=knots)
+        assert abs(terms["Pure QC"][f] / KJ - (r["eelectronic"] + r["enuclear"] + r["baseline"])) < E_TOL
+        assert abs(terms["QC/MM Elect."][f] / KJ - r["eqcmm"]) < E_TOL
+        g = G[f] / (A2B * KJ)
+        assert np.abs(g[:nq] - (r["gradients"] + gq)).max() < G_TOL
+        assert np.abs(g[nq:] - gm).max() < G_TOL
+
+
+@pytest.mark.parametrize("method", ["fp64", "mixed"])
+def test_large_qcmm_system_matches_oracle_fixture(method):
+    from pdynamo_mirror_gb300 import DIISSCFConverger, NBModelABFS, QCModelMNDO, System, workloads
+    from pdynamo_mirror_gb300.converger import MIXED_METHOD
     ref = json.load(open(os.path.join(HERE, "golden", "large_qcmm_reference.json")))
     Z, X, Q, sel, charge = workloads.large_qcmm()
     nq = len(sel)
     s = System(Z, X, mmCharges=Q)
     s.electronicState.charge = charge
-    s.DefineQCModel(QCModelMNDO("am1"), qcSelection=sel)
+    s.DefineQCModel(QCModelMNDO("am1", converger=DIISSCFConverger(**(MIXED_METHOD if method == "mixed" else {}))), qcSelection=sel)
     s.DefineNBModel(NBModelABFS(innerCutoff=8.0, outerCutoff=12.0))
     assert s.engine().wide and s.engine().n_basis == 1200
     s.Energy(doGradients=True)
@@ -99,3 +130,21 @@ def test_large_qcmm_system_matches_oracle_fixture():
     mm = np.array(ref["mm_sample"]) + nq
     assert np.abs(g[mm] - np.array(ref["mm_gradients_sample"])).max() < G_TOL
     assert np.abs(g[nq:].sum(axis=0) - np.array(ref["mm_gradient_sum"])).max() < G_TOL
+    if method == "mixed":
+        # an MD-like step: every atom displaced by up to 0.005 A, warm start from the converged density; the kept base
+        # carries every density step, and the result agrees with the plain method on the new geometry
+        eng = s.engine()
+        eng.wide_phase_events(True)
+        X2 = X + np.random.default_rng(7).uniform(-0.005, 0.005, size=X.shape)
+        s.coordinates3 = X2
+        e_mixed = s.Energy(doGradients=True)
+        g_mixed = s.configuration.gradients3.copy()
+        steps = eng.wide_phase_times()
+        assert steps["fp64_steps"] == 0 and steps["perturbative_steps"] >= 1
+        p = System(Z, X2, mmCharges=Q)
+        p.electronicState.charge = charge
+        p.DefineQCModel(QCModelMNDO("am1"), qcSelection=sel)
+        p.DefineNBModel(NBModelABFS(innerCutoff=8.0, outerCutoff=12.0))
+        e_plain = p.Energy(doGradients=True)
+        assert abs(e_mixed - e_plain) / KJ < E_TOL
+        assert np.abs(g_mixed - p.configuration.gradients3).max() / (A2B * KJ) < G_TOL
