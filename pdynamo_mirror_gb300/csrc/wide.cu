@@ -29,7 +29,7 @@ namespace wide {
 #define WB 256                 // threads per block of the grid-wide kernels
 #define WW (WB / 32)
 #define WMAXH PDG_MAX_HISTORY
-#define WNB 32                 // reflectors per back-transformation block
+#define WNB 64                 // reflectors per back-transformation block
 
 // Converger state on the device (one per wide object), read by the host after every cycle's control kernel.
 struct Ctl {
@@ -44,7 +44,7 @@ struct Ctl {
 // regions of the grid-wide SCF.
 struct WPlan {
     FramePlan fp;   // only tei, pair_e, pair_g and H (the integral and gradient kernels' regions) are laid out
-    size_t F, A, C, rP, rF, hP, hF, hE, Zc, G, colbuf, vbuf, q, pk, part, d, e, tau, eig, cst, lu, y, vb, sb, tb, wb, ctl;
+    size_t F, A, C, rP, rF, hP, hF, hE, Zc, G, colbuf, vbuf, q, tpart, pk, part, d, e, tau, eig, cst, lu, y, vb, sb, tb, wb, ctl;
     // mixed method: the base of the perturbative steps (F0, P0, all eigenvalues, the complementary vectors in FP64), the
     // matrix the last density step was applied to, and FP32 work (float offsets from f32)
     size_t BF, BP, BL, Ft, Zcc, f32;
@@ -71,12 +71,12 @@ __host__ inline WPlan wide_plan(const DeviceSystem &s)
     w.F = take(NN); w.A = take(NN); w.C = take(NN); w.rP = take(NN); w.rF = take(NN);
     w.hP = take(WMAXH * NN); w.hF = take(WMAXH * NN); w.hE = take(WMAXH * NN);
     w.Zc = take(N * kv); w.G = take(N * kv);
-    w.colbuf = take(N); w.vbuf = take(N); w.q = take(N); w.pk = take((size_t)s.n_cel + 1);
+    w.colbuf = take(2 * N); w.vbuf = take(2 * N); w.q = take(2 * N); w.tpart = take(2 * (size_t)w.parts); w.pk = take((size_t)s.n_cel + 1);
     w.part = take((size_t)w.parts * 32);
     w.d = take(N); w.e = take(N); w.tau = take(N); w.eig = take(N); w.cst = take(N / 2 + 2);
     w.lu = take(5 * N * (size_t)w.kvp + (N * (size_t)w.kvp + 7) / 8);
     w.y = take(N * (size_t)w.kvp);
-    w.vb = take(N * WNB); w.sb = take(WNB * WNB); w.tb = take(WNB * WNB); w.wb = take(WNB * kv);
+    w.vb = take(N * WNB); w.sb = take(WNB * WNB); w.tb = take(WNB * WNB); w.wb = take(2 * WNB * N);   // W and T W: WNB x (up to N columns) each
     w.ctl = take((sizeof(Ctl) + 7) / 8);
     w.BF = take(NN); w.BP = take(NN); w.BL = take(N); w.Ft = take(NN); w.Zcc = take(N * nc);
     size_t f = 0;
@@ -456,13 +456,19 @@ __global__ void __launch_bounds__(WB) k_iterate(size_t NN, const Ctl *c, const d
 }
 
 // ---------------------------------------------------------------------------------------------------------------
-// Householder tridiagonalisation of the dense symmetric A (N x N, both triangles kept), column k by two kernels:
-//   tri_a(k)  every block forms the reflector of column k (rows k+1 ..) from colbuf (dlarfg; identical in every
-//             block), block 0 publishes v, tau, e[k], d[k]; then q_i = sum_j A22[i][j] v_j, one warp per row, and the
-//             block partials of q . v.
-//   tri_b(k)  K = tau^2 (q . v) / 2, w = tau q - K v, and the rank-2 update A22 -= v w^T + w v^T, one warp per row;
-//             v is stored below the subdiagonal of column k (the back-transformation reads it) and the updated
-//             column k+1 goes to colbuf.
+// Householder tridiagonalisation of the dense symmetric A (N x N, both triangles kept; dsytd2 'L'), one grid-wide
+// kernel per column.  With A(k) the matrix after k steps, step k forms the reflector v_k, tau_k from column k of A(k)
+// (rows k+1 ..), the product q_k = A(k)22 v_k over rows and columns k+1 .., w_k = tau_k q_k - K_k v_k with
+// K_k = tau_k^2 (q_k . v_k) / 2, and A(k+1)22 = A(k)22 - v_k w_k^T - w_k v_k^T.  Launch k finishes step k - 1 and
+// starts step k in one pass over the rows:
+//   * every block forms w_{k-1} from q_{k-1} (and the block partials of q_{k-1} . v_{k-1}) of launch k - 1, then
+//     column k of A(k) from the copy of column k of A(k-1) that launch k - 1 left (its rows k ..) minus the rank-2
+//     terms of step k - 1, and from it the reflector v_k (dlarfg; identical in every block);
+//   * one warp per row i > k: the row's columns > k are updated by step k - 1 and, in the same pass, multiplied by
+//     v_k (q_k, and the block partials of q_k . v_k); the row's column k takes v_k (the back-transformation reads the
+//     reflectors there); row k + 1, updated, is copied out as the next launch's column.
+// q, the reflector, the column copy and the partials are double-buffered by the parity of k, since launch k reads
+// launch k - 1's and writes its own.
 __device__ void reflector(int m, const double *__restrict__ x, double *v, double *red, double *tau_out, double *e_out)
 {
     const double alpha = x[0];
@@ -479,72 +485,91 @@ __device__ void reflector(int m, const double *__restrict__ x, double *v, double
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(WB) k_tri_a(int N, int k, double *__restrict__ A, const double *__restrict__ colbuf, double *__restrict__ vbuf,
-                                              double *__restrict__ q, double *__restrict__ d, double *__restrict__ e, double *__restrict__ tau,
-                                              double *__restrict__ part, int parts)
+// v_{k-1} and w_{k-1} (N - k entries each, indexed from row k) into shared memory; false for k = 0.
+__device__ bool previous_step(int N, int k, const double *__restrict__ vbuf, const double *__restrict__ qbuf, const double *__restrict__ tau,
+                              const double *__restrict__ tpart, int parts, int nb, double *vp, double *wp)
 {
-    extern __shared__ double sv[];
+    if (k == 0) return false;
+    const int pp = (k - 1) & 1, mp = N - k;
+    const double t = tau[k - 1];
+    double qv = 0.0;
+    for (int b = 0; b < nb; b++) qv += tpart[pp * parts + b];
+    const double K = 0.5 * t * t * qv;
+    for (int i = threadIdx.x; i < mp; i += WB) { const double vi = vbuf[pp * N + i]; vp[i] = vi; wp[i] = fma(-K, vi, t * qbuf[pp * N + i]); }
+    __syncthreads();
+    return true;
+}
+
+__global__ void __launch_bounds__(WB) k_tri_step(int N, int k, double *__restrict__ A, double *__restrict__ colbuf, double *__restrict__ vbuf,
+                                                 double *__restrict__ qbuf, double *__restrict__ d, double *__restrict__ e,
+                                                 double *__restrict__ tau, double *__restrict__ tpart, int parts, int nb)
+{
+    extern __shared__ double sm[];
     __shared__ double red[32];
-    const int m = N - k - 1, c0 = k + 1, lane = threadIdx.x & 31;
-    double t, ek;
-    reflector(m, colbuf + c0, sv, red, &t, &ek);
+    double *vp = sm, *wp = sm + N, *c = sm + 2 * N, *vk = sm + 3 * N;
+    const int lane = threadIdx.x & 31, par = k & 1, mp = N - k, m = N - k - 1, c0 = k + 1;
+    const bool upd = previous_step(N, k, vbuf, qbuf, tau, tpart, parts, nb, vp, wp);
+    // column k of A(k), rows k .. N-1 (index r = row - k)
+    const double *cb = colbuf + par * N + k;
+    for (int r = threadIdx.x; r < mp; r += WB) c[r] = upd ? fma(-vp[r], wp[0], fma(-wp[r], vp[0], cb[r])) : cb[r];
+    __syncthreads();
+    double tk, ek;
+    reflector(m, c + 1, vk, red, &tk, &ek);
     if (blockIdx.x == 0) {
-        for (int i = threadIdx.x; i < m; i += WB) vbuf[i] = sv[i];
-        if (threadIdx.x == 0) { tau[k] = t; e[k] = ek; d[k] = A[(size_t)k * N + k]; }
+        for (int i = threadIdx.x; i < m; i += WB) vbuf[par * N + i] = vk[i];
+        if (threadIdx.x == 0) { tau[k] = tk; e[k] = ek; d[k] = c[0]; }
     }
     double pv = 0.0;
     const int gw = blockIdx.x * WW + (threadIdx.x >> 5), nw = gridDim.x * WW;
-    for (int i = gw; i < m; i += nw) {
-        const double *row = A + (size_t)(c0 + i) * N + c0;
-        double s = 0.0;
-        for (int j = lane; j < m; j += 32) s = fma(row[j], sv[j], s);
-        s = warp_sum(s);
-        if (lane == 0) { q[i] = s; pv = fma(s, sv[i], pv); }
-    }
-    pv = block_sum(pv, red);
-    if (threadIdx.x == 0) part[blockIdx.x] = pv;
-}
-
-__global__ void __launch_bounds__(WB) k_tri_b(int N, int k, double *__restrict__ A, double *__restrict__ colbuf, const double *__restrict__ vbuf,
-                                              const double *__restrict__ q, const double *__restrict__ tau, const double *__restrict__ part, int nb_a)
-{
-    extern __shared__ double sm[];
-    double *sv = sm, *sw = sm + N;
-    const int m = N - k - 1, c0 = k + 1, lane = threadIdx.x & 31;
-    const double t = tau[k];
-    double qv = 0.0;
-    for (int b = 0; b < nb_a; b++) qv += part[b];
-    const double K = 0.5 * t * t * qv;
-    for (int i = threadIdx.x; i < m; i += WB) { const double vi = vbuf[i]; sv[i] = vi; sw[i] = fma(-K, vi, t * q[i]); }
-    __syncthreads();
-    const int gw = blockIdx.x * WW + (threadIdx.x >> 5), nw = gridDim.x * WW;
+    double *next = colbuf + (1 - par) * N + c0;   // row k+1 of A(k+1)... of A(k) from column k+1 on: launch k+1's column
     for (int i = gw; i < m; i += nw) {
         double *row = A + (size_t)(c0 + i) * N + c0;
-        const double vi = sv[i], wi = sw[i];
-        for (int j = lane; j < m; j += 32) row[j] = fma(-vi, sw[j], fma(-wi, sv[j], row[j]));
+        const double vi = upd ? vp[i + 1] : 0.0, wi = upd ? wp[i + 1] : 0.0;   // row c0 + i is entry i + 1 of step k - 1
+        double sacc = 0.0;
+        for (int j = lane; j < m; j += 32) {
+            double a = row[j];
+            if (upd) { a = fma(-vi, wp[j + 1], fma(-wi, vp[j + 1], a)); row[j] = a; }
+            if (i == 0) next[j] = a;
+            sacc = fma(a, vk[j], sacc);
+        }
+        sacc = warp_sum(sacc);
         if (lane == 0) {
-            if (i >= 1) A[(size_t)(c0 + i) * N + k] = vi;   // the reflector, below the subdiagonal of column k
-            if (i >= 1) colbuf[c0 + i] = row[0];             // column c0 of the updated A22 (row c0 + i), next reflector's input
+            qbuf[par * N + i] = sacc;
+            pv = fma(sacc, vk[i], pv);
+            if (i >= 1) A[(size_t)(c0 + i) * N + k] = vk[i];   // the reflector, below the subdiagonal of column k
         }
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) colbuf[c0] = A[(size_t)c0 * N + c0];
+    pv = block_sum(pv, red);
+    if (threadIdx.x == 0) tpart[par * parts + blockIdx.x] = pv;
 }
 
-// Start: A = F, colbuf = column 0; end: the last two diagonal and the last subdiagonal elements.
+// After the last step (k = N - 3): step N - 3's update of the trailing 2 x 2 block gives d[N-2], e[N-2], d[N-1].
+__global__ void __launch_bounds__(WB) k_tri_last(int N, const double *__restrict__ A, const double *__restrict__ colbuf,
+                                                 const double *__restrict__ vbuf, const double *__restrict__ qbuf, double *__restrict__ d,
+                                                 double *__restrict__ e, double *__restrict__ tau, const double *__restrict__ tpart, int parts, int nb)
+{
+    extern __shared__ double sm[];
+    double *vp = sm, *wp = sm + N;
+    if (blockIdx.x) return;
+    const int k = N - 2;
+    const bool upd = previous_step(N, k, vbuf, qbuf, tau, tpart, parts, nb, vp, wp);
+    if (threadIdx.x == 0) {
+        const double *cb = colbuf + (k & 1) * N + k;
+        const double a00 = cb[0], a10 = cb[1], a11 = A[(size_t)(N - 1) * N + N - 1];
+        d[N - 2] = upd ? a00 - 2.0 * vp[0] * wp[0] : a00;
+        e[N - 2] = upd ? a10 - vp[1] * wp[0] - wp[1] * vp[0] : a10;
+        d[N - 1] = upd ? a11 - 2.0 * vp[1] * wp[1] : a11;
+        tau[N - 2] = 0.0;
+        e[N - 1] = 0.0;
+    }
+}
+
+// Start: A = F and the first column (row 0 of the symmetric F).
 __global__ void __launch_bounds__(WB) k_tri_start(int N, const double *__restrict__ F, double *__restrict__ A, double *__restrict__ colbuf)
 {
     const size_t NN = (size_t)N * N;
     for (size_t k = (size_t)blockIdx.x * WB + threadIdx.x; k < NN; k += (size_t)gridDim.x * WB) A[k] = F[k];
-    for (int i = blockIdx.x * WB + threadIdx.x; i < N; i += gridDim.x * WB) colbuf[i] = F[(size_t)i * N];
-}
-
-__global__ void k_tri_end(int N, const double *__restrict__ A, double *__restrict__ d, double *__restrict__ e, double *__restrict__ tau)
-{
-    if (threadIdx.x || blockIdx.x) return;
-    if (N >= 2) { d[N - 2] = A[(size_t)(N - 2) * N + N - 2]; e[N - 2] = A[(size_t)(N - 1) * N + N - 2]; d[N - 1] = A[(size_t)(N - 1) * N + N - 1]; }
-    else d[0] = A[0];
-    if (N >= 2) tau[N - 2] = 0.0;
-    e[N - 1] = 0.0;
+    for (int i = blockIdx.x * WB + threadIdx.x; i < N; i += gridDim.x * WB) colbuf[i] = F[i];
 }
 
 // ---------------------------------------------------------------------------------------------------------------
@@ -564,10 +589,10 @@ __device__ __forceinline__ int sturm(int N, const double *d, const double *e, do
     return c;
 }
 
-__global__ void __launch_bounds__(WB) k_bisect(int N, int first, int nv, const double *__restrict__ d, const double *__restrict__ e,
+__global__ void __launch_bounds__(32) k_bisect(int N, int first, int nv, const double *__restrict__ d, const double *__restrict__ e,
                                                double *__restrict__ eig)
 {
-    const int t = blockIdx.x * WB + threadIdx.x;
+    const int t = blockIdx.x * 32 + threadIdx.x;
     if (t >= nv) return;
     double lo = 1e300, hi = -1e300, emax = 0.0;
     for (int i = 0; i < N; i++) {
@@ -591,7 +616,7 @@ __global__ void __launch_bounds__(WB) k_bisect(int N, int first, int nv, const d
 // interchanges (stored interleaved by vector, so the threads' accesses coalesce), four solves from a hashed start
 // vector with rescaling between them, then normalisation.  Output: the vectors as columns of Zc (N x nv, column-major),
 // in the tridiagonal basis.  Vectors of well-separated eigenvalues come out orthogonal to about eps ||T|| / gap; those of
-// close eigenvalues are orthonormalised afterwards within their cluster (k_cluster_mgs).
+// close eigenvalues are orthonormalised afterwards within their cluster (k_cluster_gs).
 __device__ __forceinline__ unsigned int whash(unsigned int a, unsigned int b)
 {
     unsigned int h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u + (a << 6) + (a >> 2));
@@ -599,11 +624,11 @@ __device__ __forceinline__ unsigned int whash(unsigned int a, unsigned int b)
     return h;
 }
 
-__global__ void __launch_bounds__(WB) k_invit(int N, int nv, int ld, const double *__restrict__ d, const double *__restrict__ e,
+__global__ void __launch_bounds__(32) k_invit(int N, int nv, int ld, const double *__restrict__ d, const double *__restrict__ e,
                                               const double *__restrict__ eig, double tnorm, double *__restrict__ lu,
                                               unsigned char *__restrict__ pv, double *__restrict__ y, double *__restrict__ Zc)
 {
-    const int t = blockIdx.x * WB + threadIdx.x;
+    const int t = blockIdx.x * 32 + threadIdx.x;
     if (t >= nv) return;
     const double sigma = eig[t], tiny = 1e-14 * tnorm + 1e-300;
     double *u0 = lu, *u1 = lu + (size_t)N * ld, *u2 = lu + 2 * (size_t)N * ld, *lm = lu + 3 * (size_t)N * ld;
@@ -649,36 +674,45 @@ __global__ void __launch_bounds__(WB) k_invit(int N, int nv, int ld, const doubl
     for (int i = 0; i < N; i++) z[i] = y[(size_t)i * ld + t] * s;
 }
 
-// Modified Gram-Schmidt inside every cluster of close eigenvalues, one warp per cluster (lanes over the components):
-// each member is orthogonalised against the earlier ones (twice, for numerical safety) and normalised.  The span of a
-// cluster's vectors is its invariant subspace to within the contamination from farther eigenvalues, and the density
-// depends on the span only.
-__global__ void __launch_bounds__(WB) k_cluster_mgs(int N, int nv, const int *__restrict__ cstart, double *__restrict__ Zc)
+// Gram-Schmidt inside every cluster of close eigenvalues, one block per cluster: each member in turn is
+// orthogonalised against the cluster's earlier members by classical Gram-Schmidt done twice (the dots of a pass in
+// parallel over the warps, then one combined update over the components) and normalised.  The span of a cluster's
+// vectors is its invariant subspace to within the contamination from farther eigenvalues, and the density depends on
+// the span only.  Blocks whose index is not a cluster start return at once.
+__global__ void __launch_bounds__(WB) k_cluster_gs(int N, int nv, const int *__restrict__ cstart, double *__restrict__ Zc)
 {
-    const int lane = threadIdx.x & 31, gw = blockIdx.x * WW + (threadIdx.x >> 5);
-    if (gw >= nv) return;
-    const int c0 = gw;
-    if (cstart[c0] != c0) return;   // warps start only at a cluster's first member
+    extern __shared__ double dots[];   // one per earlier member
+    __shared__ double red[32];
+    const int c0 = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (c0 >= nv || cstart[c0] != c0) return;
     int c1 = c0 + 1;
     while (c1 < nv && cstart[c1] == c0) c1++;
     if (c1 - c0 < 2) return;
-    for (int t = c0; t < c1; t++) {
+    for (int t = c0 + 1; t < c1; t++) {
         double *zt = Zc + (size_t)t * N;
-        for (int pass = 0; pass < 2; pass++)
-            for (int q = c0; q < t; q++) {
-                const double *zq = Zc + (size_t)q * N;
+        const int nq = t - c0;
+        for (int pass = 0; pass < 2; pass++) {
+            for (int q = w; q < nq; q += WW) {
+                const double *zq = Zc + (size_t)(c0 + q) * N;
                 double dt = 0.0;
                 for (int i = lane; i < N; i += 32) dt = fma(zt[i], zq[i], dt);
                 dt = warp_sum(dt);
-                for (int i = lane; i < N; i += 32) zt[i] = fma(-dt, zq[i], zt[i]);
-                __syncwarp();
+                if (lane == 0) dots[q] = dt;
             }
+            __syncthreads();
+            for (int i = threadIdx.x; i < N; i += WB) {
+                double v = zt[i];
+                for (int q = 0; q < nq; q++) v = fma(-dots[q], Zc[(size_t)(c0 + q) * N + i], v);
+                zt[i] = v;
+            }
+            __syncthreads();
+        }
         double nr = 0.0;
-        for (int i = lane; i < N; i += 32) nr = fma(zt[i], zt[i], nr);
-        nr = warp_sum(nr);
-        const double s = 1.0 / sqrt(nr);
-        for (int i = lane; i < N; i += 32) zt[i] *= s;
-        __syncwarp();
+        for (int i = threadIdx.x; i < N; i += WB) nr = fma(zt[i], zt[i], nr);
+        nr = block_sum(nr, red);
+        const double sc = 1.0 / sqrt(nr);
+        for (int i = threadIdx.x; i < N; i += WB) zt[i] *= sc;
+        __syncthreads();
     }
 }
 
@@ -710,40 +744,26 @@ __global__ void __launch_bounds__(WB) k_vblock(int N, int k0, int nb, const doub
 }
 
 // T of the compact WY form I - V T V^T (upper triangular, dlarft 'Forward' 'Columnwise') from S = V^T V and tau: one
-// warp, column by column, lane i forming T[i][j] = -tau_j sum_{l=i}^{j-1} T[i][l] S[l][j] for i < j.
-__global__ void k_tblock(int nb, const double *__restrict__ S, const double *__restrict__ tau, int k0, double *__restrict__ T)
+// block of WNB threads, column by column, thread i forming T[i][j] = -tau_j sum_{l=i}^{j-1} T[i][l] S[l][j] for i < j.
+// T is written column-major (WNB x WNB, zeros below the diagonal), ready for DGEMM.
+__global__ void __launch_bounds__(WNB) k_tblock(int nb, const double *__restrict__ S, const double *__restrict__ tau, int k0, double *__restrict__ T)
 {
-    __shared__ double Ts[WNB * WNB];
+    __shared__ double Ts[WNB * WNB];   // row-major
     const int i = threadIdx.x;
-    if (blockIdx.x || i >= 32) return;
-    for (int e = i; e < WNB * WNB; e += 32) Ts[e] = 0.0;
-    __syncwarp();
+    if (blockIdx.x) return;
+    for (int e = i; e < WNB * WNB; e += WNB) Ts[e] = 0.0;
+    __syncthreads();
     for (int j = 0; j < nb; j++) {
         const double tj = tau[k0 + j];
         double s = 0.0;
         if (i < j)
             for (int l = i; l < j; l++) s = fma(Ts[i * WNB + l], S[j * nb + l], s);   // S column-major: S[l][j] = S[j * nb + l]
-        __syncwarp();
+        __syncthreads();
         if (i < j) Ts[i * WNB + j] = -tj * s;
         if (i == j) Ts[j * WNB + j] = tj;
-        __syncwarp();
+        __syncthreads();
     }
-    for (int e = i; e < WNB * WNB; e += 32) T[e] = Ts[e];
-}
-
-// W2 = T W in place (T upper nb x nb, row-major with stride WNB; W nb x kv column-major with ld nb).
-__global__ void __launch_bounds__(WB) k_trmm(int nb, int kv, const double *__restrict__ T, double *__restrict__ W)
-{
-    for (int c = blockIdx.x * WB + threadIdx.x; c < kv; c += gridDim.x * WB) {
-        double col[WNB], out[WNB];
-        for (int i = 0; i < nb; i++) col[i] = W[(size_t)c * nb + i];
-        for (int i = 0; i < nb; i++) {
-            double s = 0.0;
-            for (int l = i; l < nb; l++) s = fma(T[i * WNB + l], col[l], s);
-            out[i] = s;
-        }
-        for (int i = 0; i < nb; i++) W[(size_t)c * nb + i] = out[i];
-    }
+    for (int e = i; e < nb * nb; e += WNB) { const int r = e % nb, c = e / nb; T[e] = Ts[r * WNB + c]; }   // column-major, ld nb
 }
 
 // P = 2 C (occupied vectors) or 2 (1 - C) (virtual), C = Zc Zc^T; block partials of the squared change to part slot 6.
@@ -999,18 +1019,16 @@ static int tri_graph(pdg_wide *W, double *ws, cudaStream_t st)
     cudaStream_t cap;
     if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return PDG_CUDA_ERROR;
     const WPlan &p = W->w;
-    double *A = ws + p.A, *colbuf = ws + p.colbuf, *vbuf = ws + p.vbuf, *q = ws + p.q, *part = ws + p.part;
+    double *A = ws + p.A, *colbuf = ws + p.colbuf, *vbuf = ws + p.vbuf, *q = ws + p.q, *tpart = ws + p.tpart;
     double *d = ws + p.d, *e = ws + p.e, *tau = ws + p.tau;
-    const size_t sm_a = sizeof(double) * (size_t)N, sm_b = 2 * sizeof(double) * (size_t)N;
-    cudaFuncSetAttribute(k_tri_a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_a);
-    cudaFuncSetAttribute(k_tri_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_b);
+    const size_t sm_step = 4 * sizeof(double) * (size_t)N, sm_last = 2 * sizeof(double) * (size_t)N;
+    cudaFuncSetAttribute(k_tri_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_step);
+    cudaFuncSetAttribute(k_tri_last, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_last);
     cudaGraph_t g;
     cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-    for (int k = 0; k + 2 < N; k++) {
-        k_tri_a<<<W->grid, WB, sm_a, cap>>>(N, k, A, colbuf, vbuf, q, d, e, tau, part, p.parts);
-        k_tri_b<<<W->grid, WB, sm_b, cap>>>(N, k, A, colbuf, vbuf, q, tau, part, W->grid);
-    }
-    k_tri_end<<<1, 32, 0, cap>>>(N, A, d, e, tau);
+    for (int k = 0; k + 2 < N; k++)
+        k_tri_step<<<W->grid, WB, sm_step, cap>>>(N, k, A, colbuf, vbuf, q, d, e, tau, tpart, p.parts, W->grid);
+    k_tri_last<<<1, WB, sm_last, cap>>>(N, A, colbuf, vbuf, q, d, e, tau, tpart, p.parts, W->grid);
     cudaError_t ce = cudaStreamEndCapture(cap, &g);
     cudaStreamDestroy(cap);
     if (ce != cudaSuccess) return PDG_CUDA_ERROR;
@@ -1029,16 +1047,16 @@ static int wide_eigenvectors(pdg_wide *W, double *ws, int first, int nv, double 
     const WPlan &p = W->w;
     const int N = W->s.n_basis, G = W->grid;
     double *A = ws + p.A;
-    k_bisect<<<(nv + WB - 1) / WB, WB, 0, st>>>(N, first, nv, ws + p.d, ws + p.e, eig_out);
+    k_bisect<<<(nv + 31) / 32, 32, 0, st>>>(N, first, nv, ws + p.d, ws + p.e, eig_out);
     // Inverse iteration at an eigenvalue converged to round-off leaves a vector's overlap with another eigenvector at
-    // about eps ||T|| / gap: below 1e-11 for gaps above 1e-5 ||T||, so only closer eigenvalues form clusters, whose
+    // about eps ||T|| / gap: below 3e-10 for gaps above 1e-6 ||T||, so only closer eigenvalues form clusters, whose
     // vectors are orthonormalised after the iteration.
     int *cstart = (int *)(ws + p.cst), *maxsize = cstart + N;
-    k_clusters<<<1, 1, 0, st>>>(nv, eig_out, 1.0e-5 * tn, cstart, maxsize);
+    k_clusters<<<1, 1, 0, st>>>(nv, eig_out, 1.0e-6 * tn, cstart, maxsize);
     double *lu = ws + p.lu;
     unsigned char *pv = (unsigned char *)(lu + 5 * (size_t)N * p.kvp);
-    k_invit<<<(nv + WB - 1) / WB, WB, 0, st>>>(N, nv, p.kvp, ws + p.d, ws + p.e, eig_out, tn, lu, pv, ws + p.y, Zout);
-    k_cluster_mgs<<<(nv + WW - 1) / WW, WB, 0, st>>>(N, nv, cstart, Zout);
+    k_invit<<<(nv + 31) / 32, 32, 0, st>>>(N, nv, p.kvp, ws + p.d, ws + p.e, eig_out, tn, lu, pv, ws + p.y, Zout);
+    k_cluster_gs<<<nv, WB, sizeof(double) * (size_t)nv, st>>>(N, nv, cstart, Zout);
     mark(W, st, WPH_EIGEN);
     // back-transformation Zout <- Q Zout, blocks of WNB reflectors from the last to the first
     const int nref = N - 2;
@@ -1047,12 +1065,14 @@ static int wide_eigenvectors(pdg_wide *W, double *ws, int first, int nv, double 
         double *Vb = ws + p.vb, *S = ws + p.sb, *T = ws + p.tb, *Wm = ws + p.wb;
         k_vblock<<<G, WB, 0, st>>>(N, k0, nb, A, Vb);
         if (dgemm(W, st, CUBLAS_OP_T, CUBLAS_OP_N, nb, nb, m, 1.0, Vb, m, Vb, m, 0.0, S, nb) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
-        k_tblock<<<1, 32, 0, st>>>(nb, S, ws + p.tau, k0, T);
-        for (int c0 = 0; c0 < nv; c0 += N) {   // the W buffer holds WNB x N: columns in chunks of N
+        k_tblock<<<1, WNB, 0, st>>>(nb, S, ws + p.tau, k0, T);
+        double *W2 = Wm + (size_t)WNB * N;
+        for (int c0 = 0; c0 < nv; c0 += N) {   // the W buffers hold WNB x N: columns in chunks of N
             const int nvc = min(N, nv - c0);
-            if (dgemm(W, st, CUBLAS_OP_T, CUBLAS_OP_N, nb, nvc, m, 1.0, Vb, m, Zout + (size_t)c0 * N + k0 + 1, N, 0.0, Wm, nb) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
-            k_trmm<<<(nvc + WB - 1) / WB, WB, 0, st>>>(nb, nvc, T, Wm);
-            if (dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_N, m, nvc, nb, -1.0, Vb, m, Wm, nb, 1.0, Zout + (size_t)c0 * N + k0 + 1, N) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
+            if (dgemm(W, st, CUBLAS_OP_T, CUBLAS_OP_N, nb, nvc, m, 1.0, Vb, m, Zout + (size_t)c0 * N + k0 + 1, N, 0.0, Wm, nb) != CUBLAS_STATUS_SUCCESS ||
+                dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_N, nb, nvc, nb, 1.0, T, nb, Wm, nb, 0.0, W2, nb) != CUBLAS_STATUS_SUCCESS ||
+                dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_N, m, nvc, nb, -1.0, Vb, m, W2, nb, 1.0, Zout + (size_t)c0 * N + k0 + 1, N) != CUBLAS_STATUS_SUCCESS)
+                return PDG_CUDA_ERROR;
         }
     }
     mark(W, st, WPH_BACKTRANSFORM);
