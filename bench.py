@@ -528,6 +528,112 @@ def bench_md(args):
     print(json.dumps(line))
 
 
+LARGE_METRIC = ("QC/MM E+grad per MD step, evals/s (AM1, 200 QC waters = 600 atoms, N = 1200, in 20000 fixed TIP3P waters, "
+                "ABFS 8/12 A, 300 K Langevin, 0.5 fs)")
+
+
+def large_cpu_sample(Z, Q, sel, charge, X):
+    """The oracle on one host core for the large frame, bounded: integrals + SCF cycles + gradients cost T(c) for c
+    SCF cycles; runs with c = 1 and c = 2 give the fixed cost and the cost per cycle (seconds)."""
+    from oracle import oracle as O
+    nq = len(sel)
+    Zq = [int(z) for z in Z[:nq]]
+    ham = O.Hamiltonian("am1", Zq)
+    kn = O.abfs_knots(8.0, 12.0)
+    t = {}
+    for c in (1, 2):
+        s = O.System(ham, Zq, charge=charge, maximumSCFCycles=c)
+        t0 = time.perf_counter()
+        phi = O.qcmm("abfs", X[:nq], X[nq:], Q[nq:], knots=kn)[0]
+        r = s.energy(X[:nq], phi=phi)
+        O.qcmm("abfs", X[:nq], X[nq:], Q[nq:], qcq=r["charges"], knots=kn)
+        t[c] = time.perf_counter() - t0
+    per_cycle = t[2] - t[1]
+    return t[1] - per_cycle, per_cycle
+
+
+def bench_large(args, md_steps=None, md_warmup=None, cpu=True):
+    """The large QC/MM system: Langevin dynamics (300 K, 0.5 fs, 25 ps^-1) of its 600 QC atoms in the fixed MM waters,
+    every step one E+grad with the previous step's density as the start (the reference's warm start), each SCF over the
+    whole GPU (the wide engine).  Plain FP64 against the mixed method (FP64 base steps, perturbative steps around the
+    base kept across MD steps, FP32 DIIS errors and pair-gradient terms) from the same start; ms per MD step by CUDA
+    events over the timed steps.  Accuracy: plain FP64 cold E+grad at the last geometry of the mixed trajectory."""
+    import torch
+    from pdynamo_mirror_gb300 import DIISSCFConverger, LangevinDynamics, NBModelABFS, QCModelMNDO, System, workloads
+    from pdynamo_mirror_gb300.converger import MIXED_METHOD
+    steps = args.steps if md_steps is None else md_steps
+    warm = max(3, args.warmup if md_warmup is None else md_warmup)
+    Z, X, Q, sel, charge = workloads.large_qcmm()
+    nq = len(sel)
+
+    def make(method):
+        s = System(Z, X, mmCharges=Q)
+        s.electronicState.charge = charge
+        s.DefineQCModel(QCModelMNDO("am1", converger=DIISSCFConverger(**(MIXED_METHOD if method == "mixed" else {}))), qcSelection=sel)
+        s.DefineNBModel(NBModelABFS(innerCutoff=8.0, outerCutoff=12.0))
+        s.DefineFixedAtoms(range(nq, len(Z)))
+        return s
+
+    res = {}
+    for method in ("fp64", "mixed"):
+        s = make(method)
+        eng = s.engine()
+        eng.wide_phase_events(True)
+        md = LangevinDynamics(s, replicas=1, timeStep=0.0005, seed=404, densityGuess="previous")
+        t0 = time.perf_counter()
+        md.run(1)
+        torch.cuda.synchronize()
+        cold_ms = 1e3 * (time.perf_counter() - t0)
+        md.run(warm - 1)
+        torch.cuda.synchronize()
+        clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) if method == "mixed" else None
+        if clocks:
+            clocks.start()
+        st = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        phases = []
+        e0.record(st)
+        cyc = []
+        for _ in range(steps):
+            cyc += md.run(1)
+            phases.append(eng.wide_phase_times())
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        res[method] = dict(ms=ms, cold_ms=cold_ms, clk=clocks.stop() if clocks else None,
+                           cycles=float(np.mean([int(c[0]) for c in cyc])),
+                           phases={k: float(np.mean([p[k] for p in phases])) for k in phases[0]},
+                           E=float(md.last["energies"][0, 0]), G=(md.last["qc_gradients"] + md.last["qcmm_qc_gradients"])[0].cpu().numpy(),
+                           xyz=md.xyz.clone(), mm=(md.mm_xyz, md.mm_q), nb=s.nbModel)
+    head, plain = res["mixed"], res["fp64"]
+    ref = make("fp64")
+    r = ref.engine().run(head["xyz"], ref.qcModel.converger, head["mm"][0], head["mm"][1], head["nb"], gradients=True,
+                         warm_start=False, mm_gradients=False)
+    dE = abs(head["E"] - float(r["energies"][0, 0]))
+    dG = float(np.abs(head["G"] - (r["qc_gradients"] + r["qcmm_qc_gradients"])[0].cpu().numpy()).max())
+    out = {"metric": LARGE_METRIC, "value": 1e3 / head["ms"], "unit": UNIT, "ms_per_md_step": head["ms"], "md_steps": steps,
+           "warmup_md_steps": warm, "higher_is_better": True,
+           "config": {"workload": "large_qcmm_am1_abfs_langevin", "qc_atoms": nq, "basis_functions": ref.engine().n_basis,
+                      "mm_atoms": len(Z) - nq, "time_step_fs": 0.5, "temperature_k": 300.0, "start_density": "previous step (warm)",
+                      "engine": "wide (one frame over all SMs)", "method": "mixed: FP64 base steps + perturbative steps around the "
+                      "base kept across MD steps (no purification beyond 144 basis functions; no learned start density)"},
+           "mean_scf_cycles": head["cycles"], "cold_first_step_ms": head["cold_ms"], "phase_ms_per_md_step": head["phases"],
+           "plain_fp64": {"value": 1e3 / plain["ms"], "ms_per_md_step": plain["ms"], "mean_scf_cycles": plain["cycles"],
+                          "cold_first_step_ms": plain["cold_ms"], "phase_ms_per_md_step": plain["phases"]},
+           "accuracy_vs_plain_fp64": {"where": "last geometry of the timed mixed trajectory, plain FP64 cold", "max_abs_dE_hartree": dE,
+                                      "max_abs_dF_hartree_per_bohr": dG, "gate": "|dE| < 1e-6 Eh, |dF| < 1e-5 Eh/Bohr",
+                                      "pass": bool(dE < 1e-6 and dG < 1e-5)},
+           "clocks": head["clk"]}
+    if cpu:
+        fixed, per_cycle = large_cpu_sample(Z, Q, sel, charge, X)
+        est = fixed + plain["cycles"] * per_cycle
+        out["cpu_baseline"] = {"value": 1.0 / est, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": "oracle/mndo_oracle.c on the 600-atom frame with 1 and 2 SCF cycles (fixed cost %.1f s, "
+                                         "%.1f s per cycle), taken at the plain GPU path's %.2f warm cycles per MD step"
+                                         % (fixed, per_cycle, plain["cycles"])}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -540,7 +646,7 @@ def main():
     ap.add_argument("--method", default="learned_mixed", choices=["learned_mixed", "mixed", "fp64"],
                     help="learned start density + purification cycles (the metric's learned+mixed), purification cycles "
                          "from the diagonal guess (mixed), or FP64 throughout")
-    ap.add_argument("--workload", default="qcmm_water_box", choices=["qcmm_water_box", "water_clusters", "qcmm_md"],
+    ap.add_argument("--workload", default="qcmm_water_box", choices=["qcmm_water_box", "water_clusters", "qcmm_md", "large_qcmm"],
                     help="the QC/MM water box (the headline metric), 512 independent PM3 water clusters in one launch, or "
                          "Langevin dynamics of water-box replicas with the learned start density trained on trajectories")
     ap.add_argument("--md-equilibration", type=int, default=150)
@@ -554,6 +660,9 @@ def main():
         return bench_clusters(args)
     if args.workload == "qcmm_md" and args.impl == "gb300":
         return bench_md(args)
+    if args.workload == "large_qcmm" and args.impl == "gb300":
+        print(json.dumps(bench_large(args, cpu=not args.no_cpu_baseline)))
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

@@ -402,7 +402,7 @@ int pdg_mm_energy_gradients(const pdg_mm_system *m, int n_frames, const double *
  * options->density_step 0 is the reference's FP64 method; 3 or 6 the mixed method of this path: every FP64 density step
  * keeps a base (its matrix, density and all eigenpairs), and the following steps are perturbative ones around it in FP32
  * products with small factors (scf.cu's perturbative step as SGEMMs), falling back to an FP64 step when the correction
- * is not small; the DIIS error is formed in FP32 from the change of F; the sp-sp and sp-s pair gradient terms are FP32.
+ * is not small (|K| >= 1e-2); the DIIS error is formed in FP32 from the change of F; the sp-sp and sp-s pair gradient terms are FP32.
  * The base stays with the wide engine and its workspace between calls, so a warm-started call (the next MD step) can run
  * perturbative steps from its first cycle.
  *   pdg_wide_create       a wide engine for sys (which must outlive it); holds a cuBLAS handle and, after the first
@@ -419,11 +419,11 @@ int pdg_wide_energy_gradients(pdg_wide *wide, const double *d_xyz, const double 
                               double *d_density, int use_density, double *d_energies, double *d_gradients, double *d_charges,
                               int *d_status, int *d_ncycles, void *d_workspace, size_t workspace_bytes, void *stream);
 /* Device time per phase of the last pdg_wide_energy_gradients call (after pdg_wide_phase_events(wide, 1)), in
- * milliseconds: integrals, Fock builds (with the converger's energy test), DIIS/ODA, tridiagonalisation, eigenvalues and
- * eigenvectors (with the host's waits for their sizes), back-transformation, density (and the perturbative steps),
+ * milliseconds: integrals, Fock builds (with the converger's energy test), DIIS/ODA, tridiagonalisation (with the
+ * host's read of its bounds), eigenvalues, eigenvectors, back-transformation, density (and the perturbative steps),
  * gradients; then two counts: the call's FP64 density steps and its perturbative steps.  PDG_WIDE_NPHASES values in
  * all.  The counterpart of the reference's phase timings (pMolecule.QCModel.pyx:208-275). */
-#define PDG_WIDE_NPHASES 10
+#define PDG_WIDE_NPHASES 11
 int pdg_wide_phase_events(pdg_wide *wide, int enable);
 int pdg_wide_phase_times(pdg_wide *wide, float *h_ms);
 

@@ -15,8 +15,8 @@ EN_TOTAL_ELECTRONIC, EN_ELECTRONIC, EN_NUCLEAR, EN_BASELINE, EN_QCMM, EN_ONE_ELE
 MAX_HISTORY = 16
 QCMM_FP32_PAIRS = 0x100   # pdg_qcmm_gradients model flag: FP32 pair terms (the mixed method)
 MM_FLAG_MM, MM_FLAG_QC_LJ, MM_FLAG_FIXED = 1, 2, 4   # pdg_mm_create atom flags
-WIDE_PHASES = ("integrals", "fock", "diis", "tridiagonal", "eigen", "backtransform", "density", "gradients", "fp64_steps",
-               "perturbative_steps")
+WIDE_PHASES = ("integrals", "fock", "diis", "tridiagonal", "eigenvalues", "eigenvectors", "backtransform", "density", "gradients",
+               "fp64_steps", "perturbative_steps")
 MM_TERMS = ("MM/MM Elect.", "MM/MM LJ", "MM/MM 1-4 Elect.", "MM/MM 1-4 LJ", "QC/MM LJ", "QC/MM 1-4 LJ")
 
 EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system_info", "pdg_workspace_bytes",

@@ -526,11 +526,21 @@ __global__ void __launch_bounds__(WB) k_tri_step(int N, int k, double *__restric
         double *row = A + (size_t)(c0 + i) * N + c0;
         const double vi = upd ? vp[i + 1] : 0.0, wi = upd ? wp[i + 1] : 0.0;   // row c0 + i is entry i + 1 of step k - 1
         double sacc = 0.0;
-        for (int j = lane; j < m; j += 32) {
-            double a = row[j];
-            if (upd) { a = fma(-vi, wp[j + 1], fma(-wi, vp[j + 1], a)); row[j] = a; }
-            if (i == 0) next[j] = a;
-            sacc = fma(a, vk[j], sacc);
+        // eight loads of the row in flight per lane before the arithmetic that uses them
+        for (int j0 = lane; j0 < m; j0 += 256) {
+            double a[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) { const int j = j0 + 32 * u; a[u] = j < m ? row[j] : 0.0; }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int j = j0 + 32 * u;
+                if (j < m) {
+                    double av = a[u];
+                    if (upd) { av = fma(-vi, wp[j + 1], fma(-wi, vp[j + 1], av)); row[j] = av; }
+                    if (i == 0) next[j] = av;
+                    sacc = fma(av, vk[j], sacc);
+                }
+            }
         }
         sacc = warp_sum(sacc);
         if (lane == 0) {
@@ -589,27 +599,41 @@ __device__ __forceinline__ int sturm(int N, const double *d, const double *e, do
     return c;
 }
 
-__global__ void __launch_bounds__(32) k_bisect(int N, int first, int nv, const double *__restrict__ d, const double *__restrict__ e,
-                                               double *__restrict__ eig)
+// One warp per eigenvalue: multisection instead of bisection.  An FP64 warp instruction costs the same however many
+// lanes are active, so the 32 lanes evaluate 31 interior points of the bracket at once (the cost of one bisection
+// step) and the bracket shrinks 32-fold per round: about 11 rounds to round-off instead of 55 bisection steps.
+#define MS_WARPS 4
+__global__ void __launch_bounds__(32 * MS_WARPS) k_bisect(int N, int first, int nv, const double *__restrict__ d,
+                                                          const double *__restrict__ e, double *__restrict__ eig)
 {
-    const int t = blockIdx.x * 32 + threadIdx.x;
+    const int lane = threadIdx.x & 31, t = blockIdx.x * MS_WARPS + (threadIdx.x >> 5);
     if (t >= nv) return;
     double lo = 1e300, hi = -1e300, emax = 0.0;
-    for (int i = 0; i < N; i++) {
+    for (int i = lane; i < N; i += 32) {
         const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < N - 1 ? fabs(e[i]) : 0.0);
         lo = fmin(lo, d[i] - r); hi = fmax(hi, d[i] + r);
         if (i < N - 1) emax = fmax(emax, e[i] * e[i]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, o));
     }
     const double tnorm = fmax(fabs(lo), fabs(hi));
     const double pivmin = fmax(1e-300, 2.2250738585072014e-308 * fmax(1.0, emax));
     lo -= 2.2e-16 * tnorm * N + 2.0 * pivmin; hi += 2.2e-16 * tnorm * N + 2.0 * pivmin;
     const int idx = first + t;   // the eigenvalue with exactly idx eigenvalues below it
-    for (int it = 0; it < 200; it++) {
-        const double mid = 0.5 * (lo + hi);
-        if (mid <= lo || mid >= hi || hi - lo <= 2.2e-16 * fmax(fabs(lo), fabs(hi)) + pivmin) break;
-        if (sturm(N, d, e, mid, pivmin) > idx) hi = mid; else lo = mid;
+    for (int round = 0; round < 40; round++) {
+        if (hi - lo <= 2.2e-16 * fmax(fabs(lo), fabs(hi)) + pivmin) break;
+        const double x = lo + (hi - lo) * (double)(lane + 1) * (1.0 / 32.0);   // lane 31: hi itself
+        const bool above = lane == 31 ? true : sturm(N, d, e, x, pivmin) > idx;
+        const unsigned b = __ballot_sync(0xffffffffu, above);
+        const int l = __ffs(b) - 1;   // first point with more than idx eigenvalues below it
+        const double xl = __shfl_sync(0xffffffffu, x, l), xp = l > 0 ? __shfl_sync(0xffffffffu, x, max(l - 1, 0)) : lo;
+        if (xl >= hi && xp <= lo) break;   // no progress (round-off)
+        hi = xl; lo = xp;
     }
-    eig[t] = 0.5 * (lo + hi);
+    if (lane == 0) eig[t] = 0.5 * (lo + hi);
 }
 
 // Inverse iteration for the nv wanted eigenvectors, one thread per vector: the LU factors of T - lambda I with row
@@ -650,17 +674,47 @@ __global__ void __launch_bounds__(32) k_invit(int N, int nv, int ld, const doubl
     for (int i = 0; i < N; i++) y[(size_t)i * ld + t] = ((whash(t * 2654435761u + 17u, i) >> 8) * (1.0 / 16777216.0)) * 2.0 - 1.0;
     double sc = 1.0;
     for (int it = 0; it < 4; it++) {
+        // forward: interchanges and L; the operands of eight steps are loaded ahead of the dependent recurrence
         double c = y[t] * sc;
-        for (int k = 0; k < N - 1; k++) {
+        int k = 0;
+        for (; k + 8 <= N - 1; k += 8) {
+            double xn[8], l[8]; bool sw[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                xn[u] = y[(size_t)(k + 1 + u) * ld + t] * sc; l[u] = lm[(size_t)(k + u) * ld + t]; sw[u] = pv[(size_t)(k + u) * ld + t];
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const double yk = sw[u] ? xn[u] : c, cn = sw[u] ? c : xn[u];
+                y[(size_t)(k + u) * ld + t] = yk;
+                c = fma(-l[u], yk, cn);
+            }
+        }
+        for (; k < N - 1; k++) {
             const double xn = y[(size_t)(k + 1) * ld + t] * sc, l = lm[(size_t)k * ld + t];
             const bool sw = pv[(size_t)k * ld + t];
             const double yk = sw ? xn : c, cn = sw ? c : xn;
             y[(size_t)k * ld + t] = yk;
             c = fma(-l, yk, cn);
         }
+        // back substitution with U, eight rows loaded ahead
         double x1 = c * u0[(size_t)(N - 1) * ld + t], x2 = 0.0, mx = fabs(x1);
         y[(size_t)(N - 1) * ld + t] = x1;
-        for (int k = N - 2; k >= 0; k--) {
+        k = N - 2;
+        for (; k - 7 >= 0; k -= 8) {
+            double yy[8], a0[8], a1[8], a2[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const size_t o = (size_t)(k - u) * ld + t;
+                yy[u] = y[o]; a0[u] = u0[o]; a1[u] = u1[o]; a2[u] = u2[o];
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const double x0 = fma(-a2[u], x2, fma(-a1[u], x1, yy[u])) * a0[u];
+                y[(size_t)(k - u) * ld + t] = x0; x2 = x1; x1 = x0; mx = fmax(mx, fabs(x0));
+            }
+        }
+        for (; k >= 0; k--) {
             const size_t o = (size_t)k * ld + t;
             const double x0 = fma(-u2[o], x2, fma(-u1[o], x1, y[o])) * u0[o];
             y[o] = x0; x2 = x1; x1 = x0; mx = fmax(mx, fabs(x0));
@@ -902,7 +956,8 @@ __global__ void k_set_have_z(Ctl *c, int v) { if (threadIdx.x == 0 && blockIdx.x
 using namespace wide;
 
 // Phases of the per-call device timing (pdg_wide_phase_times).
-enum { WPH_INTEGRALS, WPH_FOCK, WPH_DIIS, WPH_TRIDIAGONAL, WPH_EIGEN, WPH_BACKTRANSFORM, WPH_DENSITY, WPH_GRADIENTS, WPH_N };
+enum { WPH_INTEGRALS, WPH_FOCK, WPH_DIIS, WPH_TRIDIAGONAL, WPH_EIGENVALUES, WPH_EIGENVECTORS, WPH_BACKTRANSFORM, WPH_DENSITY,
+       WPH_GRADIENTS, WPH_N };
 
 struct pdg_wide {
     DeviceSystem s;
@@ -1047,7 +1102,8 @@ static int wide_eigenvectors(pdg_wide *W, double *ws, int first, int nv, double 
     const WPlan &p = W->w;
     const int N = W->s.n_basis, G = W->grid;
     double *A = ws + p.A;
-    k_bisect<<<(nv + 31) / 32, 32, 0, st>>>(N, first, nv, ws + p.d, ws + p.e, eig_out);
+    k_bisect<<<(nv + MS_WARPS - 1) / MS_WARPS, 32 * MS_WARPS, 0, st>>>(N, first, nv, ws + p.d, ws + p.e, eig_out);
+    mark(W, st, WPH_EIGENVALUES);
     // Inverse iteration at an eigenvalue converged to round-off leaves a vector's overlap with another eigenvector at
     // about eps ||T|| / gap: below 3e-10 for gaps above 1e-6 ||T||, so only closer eigenvalues form clusters, whose
     // vectors are orthonormalised after the iteration.
@@ -1057,7 +1113,7 @@ static int wide_eigenvectors(pdg_wide *W, double *ws, int first, int nv, double 
     unsigned char *pv = (unsigned char *)(lu + 5 * (size_t)N * p.kvp);
     k_invit<<<(nv + 31) / 32, 32, 0, st>>>(N, nv, p.kvp, ws + p.d, ws + p.e, eig_out, tn, lu, pv, ws + p.y, Zout);
     k_cluster_gs<<<nv, WB, sizeof(double) * (size_t)nv, st>>>(N, nv, cstart, Zout);
-    mark(W, st, WPH_EIGEN);
+    mark(W, st, WPH_EIGENVECTORS);
     // back-transformation Zout <- Q Zout, blocks of WNB reflectors from the last to the first
     const int nref = N - 2;
     for (int k0 = ((nref - 1) / WNB) * WNB; k0 >= 0 && nref > 0; k0 -= WNB) {
@@ -1178,8 +1234,9 @@ static int wide_pert_step(pdg_wide *W, double *ws, double *P, cudaStream_t st, i
         kmax = W->sweep[1];
         settled = W->sweep[0] <= 1.0e-5 * W->sweep[1] + 1.0e-30;
     }
-    // |K| bounds the FP32 rounding carried into P (~1e-7 |K| per product): 2e-3 keeps it far below the 1e-8 tolerance
-    if (!settled || !(kmax < 2.0e-3)) return PDG_OK;
+    // |K| bounds the FP32 rounding carried into P (~1e-7 |K| per product) and the error of U = -A + A^2 (|K|^6): 1e-2
+    // keeps both far below the 1e-8 tolerance, and lets a step cover the change of geometry of an MD step
+    if (!settled || !(kmax < 1.0e-2)) return PDG_OK;
     if (sgemm(W, st, Nn, Nn, N, kv, nc, 1.f, V, N, K, nc, 0.f, Yc, N) ||               // Y = V K
         sgemm(W, st, Tt, Nn, kv, kv, nc, 1.f, K, nc, K, nc, 0.f, Am, kv) ||            // A = K^T K
         sgemm(W, st, Nn, Nn, kv, kv, kv, 1.f, Am, kv, Am, kv, 0.f, U, kv))             // A^2
