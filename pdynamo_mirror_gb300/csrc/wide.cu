@@ -215,13 +215,24 @@ __device__ __forceinline__ double sum_parts(const double *part, int slot, int pa
     return t;
 }
 
+// The same sum by one warp: lane l adds blocks l, l + 32, ... (loads in flight together), then the fixed shuffle tree;
+// every lane gets the result, and every block that calls it gets the same value.
+__device__ __forceinline__ double warp_sum_parts(const double *part, int nb)
+{
+    const int lane = threadIdx.x & 31;
+    double t = 0.0;
+    for (int b = lane; b < nb; b += 32) t += part[b];
+    return warp_sum(t);
+}
+
 // Control after the Fock build (one thread): energies, the convergence test (DIISSCFConverger_Converged,
 // DIISSCFConverger.c:116-121, signed deltaeold), the DIIS slot of this cycle.
 __global__ void k_control_fock(Ctl *c, const double *__restrict__ part, int parts, int nb_traces, pdg_scf_options o, int hist)
 {
+    if (threadIdx.x >= 32) return;
+    const double th = warp_sum_parts(part, nb_traces), tf = warp_sum_parts(part + parts, nb_traces);
+    const double dh = warp_sum_parts(part + 2 * (size_t)parts, nb_traces), df = warp_sum_parts(part + 3 * (size_t)parts, nb_traces);
     if (threadIdx.x != 0) return;
-    const double th = sum_parts(part, 0, parts, nb_traces), tf = sum_parts(part, 1, parts, nb_traces);
-    const double dh = sum_parts(part, 2, parts, nb_traces), df = sum_parts(part, 3, parts, nb_traces);
     const double e1 = 2.0 * th + dh, e2 = 0.5 * ((2.0 * tf + df) - e1), eq = part[4 * parts];
     c->e1 = e1; c->e2 = e2; c->eq = eq; c->eel = e1 + e2 + eq;
     c->ncyc++;
@@ -356,15 +367,22 @@ __global__ void k_control_diis(Ctl *c, const double *__restrict__ part, int part
     __shared__ double M[17 * 35], Ab[17 * 17], bb[17], x[17];
     const int lane = threadIdx.x & 31;
     if (threadIdx.x >= 32) return;
-    if (lane == 0) {
-        double mx = 0.0;
-        for (int b = 0; b < nb; b++) mx = fmax(mx, part[5 * parts + b]);
-        c->maxerr = mx;
-        for (int m = 0; m < c->matnum; m++) {
-            const double t = 2.0 * sum_parts(part, 8 + m, parts, nb);
+    double mx = 0.0;
+    for (int b = lane; b < nb; b += 32) mx = fmax(mx, part[5 * (size_t)parts + b]);
+    mx = warp_max(mx);
+    const int matnum = c->matnum;
+    for (int m = 0; m < matnum; m++) {
+        const double t = 2.0 * warp_sum_parts(part + (size_t)(8 + m) * parts, nb);
+        if (lane == 0) {
             const int n = c->slots[m];
             c->B[n * WMAXH + c->newest] = t; c->B[c->newest * WMAXH + n] = t;
         }
+    }
+    const double t1 = warp_sum_parts(part + 24 * (size_t)parts, nb_oda), t2 = warp_sum_parts(part + 25 * (size_t)parts, nb_oda);
+    const double t3 = warp_sum_parts(part + 26 * (size_t)parts, nb_oda), t4 = warp_sum_parts(part + 27 * (size_t)parts, nb_oda);
+    __syncwarp();
+    if (lane == 0) {
+        c->maxerr = mx;
         c->do_extrap = 0; c->do_oda = 0;
         if (c->iteration > 0 && o.use_rca) {
             if (c->qdiis && c->maxerr > 0.8) { c->qdiis = 0; c->qrca = 1; }
@@ -400,8 +418,6 @@ __global__ void k_control_diis(Ctl *c, const double *__restrict__ part, int part
         }
         if (lane == 0) { c->matnum = mn; c->good = good; c->do_extrap = good; }
     } else if (c->iteration > 0 && o.use_rca && c->qrca && lane == 0) {
-        const double t1 = sum_parts(part, 24, parts, nb_oda), t2 = sum_parts(part, 25, parts, nb_oda);
-        const double t3 = sum_parts(part, 26, parts, nb_oda), t4 = sum_parts(part, 27, parts, nb_oda);
         double ca = t1 - t2, cc = t3 - t4, dd = c->eold;
         const double etemp = c->etemp;
         ca += cc + 2.0 * (dd - etemp);
@@ -492,9 +508,13 @@ __device__ bool previous_step(int N, int k, const double *__restrict__ vbuf, con
     if (k == 0) return false;
     const int pp = (k - 1) & 1, mp = N - k;
     const double t = tau[k - 1];
-    double qv = 0.0;
-    for (int b = 0; b < nb; b++) qv += tpart[pp * parts + b];
-    const double K = 0.5 * t * t * qv;
+    __shared__ double qv_s;
+    if (threadIdx.x < 32) {
+        const double qv = warp_sum_parts(tpart + pp * parts, nb);
+        if (threadIdx.x == 0) qv_s = qv;
+    }
+    __syncthreads();
+    const double K = 0.5 * t * t * qv_s;
     for (int i = threadIdx.x; i < mp; i += WB) { const double vi = vbuf[pp * N + i]; vp[i] = vi; wp[i] = fma(-K, vi, t * qbuf[pp * N + i]); }
     __syncthreads();
     return true;
@@ -592,9 +612,37 @@ __device__ __forceinline__ int sturm(int N, const double *d, const double *e, do
     if (fabs(q) < pivmin) q = -pivmin;
     c += (q < 0.0);
     for (int i = 1; i < N; i++) {
-        q = (d[i] - x) - e[i - 1] * e[i - 1] / q;
+        // e^2 / q with the reciprocal from an FP32 seed and two FP64 Newton steps (relative error ~1e-16; only the sign
+        // of each pivot counts): a fraction of the FP64 instructions of a division.  Pivots outside the float range
+        // take the division.
+        double r;
+        const double aq = fabs(q);
+        if (aq > 1.0e-30 && aq < 1.0e30) {
+            r = (double)__frcp_rn((float)q);
+            r = r * fma(-q, r, 2.0);
+            r = r * fma(-q, r, 2.0);
+        } else r = 1.0 / q;
+        q = (d[i] - x) - e[i - 1] * e[i - 1] * r;
         if (fabs(q) < pivmin) q = -pivmin;
         c += (q < 0.0);
+    }
+    return c;
+}
+
+// The Sturm count in FP32, for the multisection rounds whose bracket is still wide (the count is exact wherever x is
+// farther than ~1e-6 ||T|| from every eigenvalue).
+__device__ __forceinline__ int sturm32(int N, const double *d, const double *e, double x, float pivmin)
+{
+    int c = 0;
+    const float xf = (float)x;
+    float q = (float)d[0] - xf;
+    if (fabsf(q) < pivmin) q = -pivmin;
+    c += (q < 0.0f);
+    for (int i = 1; i < N; i++) {
+        const float ef = (float)e[i - 1];
+        q = ((float)d[i] - xf) - __fdividef(ef * ef, q);
+        if (fabsf(q) < pivmin) q = -pivmin;
+        c += (q < 0.0f);
     }
     return c;
 }
@@ -623,6 +671,24 @@ __global__ void __launch_bounds__(32 * MS_WARPS) k_bisect(int N, int first, int 
     const double pivmin = fmax(1e-300, 2.2250738585072014e-308 * fmax(1.0, emax));
     lo -= 2.2e-16 * tnorm * N + 2.0 * pivmin; hi += 2.2e-16 * tnorm * N + 2.0 * pivmin;
     const int idx = first + t;   // the eigenvalue with exactly idx eigenvalues below it
+    // FP32 counts while the bracket is wider than 1e-4 ||T|| (its interior points stay far from the eigenvalue in
+    // FP32 terms only then), with a margin of 1e-5 ||T|| kept on both sides of the FP32 bracket; FP64 after that
+    const float piv32 = 1.0e-30f;
+    for (int round = 0; round < 8 && hi - lo > 1.0e-4 * tnorm; round++) {
+        const double x = lo + (hi - lo) * (double)(lane + 1) * (1.0 / 32.0);
+        const bool above = lane == 31 ? true : sturm32(N, d, e, x, piv32) > idx;
+        const unsigned b = __ballot_sync(0xffffffffu, above);
+        const int l = __ffs(b) - 1;
+        const double xl = __shfl_sync(0xffffffffu, x, l), xp = l > 0 ? __shfl_sync(0xffffffffu, x, max(l - 1, 0)) : lo;
+        hi = fmin(hi, xl + 1.0e-5 * tnorm); lo = fmax(lo, xp - 1.0e-5 * tnorm);
+    }
+    // the FP64 counts at the widened bracket's ends confirm it; if not, the whole Gershgorin interval again
+    {
+        const bool ok_lo = lane != 0 || sturm(N, d, e, lo, pivmin) <= idx, ok_hi = lane != 1 || sturm(N, d, e, hi, pivmin) > idx;
+        if (!__all_sync(0xffffffffu, ok_lo && ok_hi)) {
+            lo = -tnorm - 2.2e-16 * tnorm * N - 2.0 * pivmin; hi = tnorm + 2.2e-16 * tnorm * N + 2.0 * pivmin;
+        }
+    }
     for (int round = 0; round < 40; round++) {
         if (hi - lo <= 2.2e-16 * fmax(fabs(lo), fabs(hi)) + pivmin) break;
         const double x = lo + (hi - lo) * (double)(lane + 1) * (1.0 / 32.0);   // lane 31: hi itself
@@ -841,8 +907,10 @@ __global__ void __launch_bounds__(WB) k_density(int N, int occ, const double *__
 
 __global__ void k_control_density(Ctl *c, const double *__restrict__ part, int parts, int nb, int N)
 {
-    if (threadIdx.x || blockIdx.x) return;
-    c->rms = sqrt(sum_parts(part, 6, parts, nb)) / (double)N;
+    if (threadIdx.x >= 32 || blockIdx.x) return;
+    const double r = warp_sum_parts(part + 6 * (size_t)parts, nb);
+    if (threadIdx.x) return;
+    c->rms = sqrt(r) / (double)N;
     c->valid = 1;
     c->have_z = 1;
 }
@@ -915,10 +983,11 @@ __global__ void __launch_bounds__(WB) k_sweep(size_t n, const float *__restrict_
 }
 __global__ void k_sweep_max(const double *__restrict__ part, int parts, int nb, double *__restrict__ out)
 {
-    if (threadIdx.x || blockIdx.x) return;
+    if (threadIdx.x >= 32 || blockIdx.x) return;
     double d = 0.0, m = 0.0;
-    for (int b = 0; b < nb; b++) { d = fmax(d, part[28 * (size_t)parts + b]); m = fmax(m, part[29 * (size_t)parts + b]); }
-    out[0] = d; out[1] = m;
+    for (int b = threadIdx.x; b < nb; b += 32) { d = fmax(d, part[28 * (size_t)parts + b]); m = fmax(m, part[29 * (size_t)parts + b]); }
+    d = warp_max(d); m = warp_max(m);
+    if (threadIdx.x == 0) { out[0] = d; out[1] = m; }
 }
 // y += alpha x (FP32)
 __global__ void __launch_bounds__(WB) k_f32_axpy(size_t n, float alpha, const float *__restrict__ x, float *__restrict__ y)
@@ -1170,7 +1239,7 @@ static int wide_density_step(pdg_wide *W, double *ws, double *P, cudaStream_t st
     // C = Zc Zc^T (column-major N x N: symmetric, so also row-major), P from it
     if (dgemm(W, st, CUBLAS_OP_N, CUBLAS_OP_T, N, N, kv, 1.0, Zc, N, Zc, N, 0.0, C, N) != CUBLAS_STATUS_SUCCESS) return PDG_CUDA_ERROR;
     k_density<<<G, WB, 0, st>>>(N, s.vec_occupied, C, P, part, p.parts);
-    k_control_density<<<1, 1, 0, st>>>((Ctl *)(ws + p.ctl), part, p.parts, G, N);
+    k_control_density<<<1, 32, 0, st>>>((Ctl *)(ws + p.ctl), part, p.parts, G, N);
     mark(W, st, WPH_DENSITY);
     if (make_base && nc > 0) {
         float *f32 = (float *)(ws + p.f32);
@@ -1227,7 +1296,7 @@ static int wide_pert_step(pdg_wide *W, double *ws, double *P, cudaStream_t st, i
             sgemm(W, st, Nn, Nn, nc, kv, kv, -1.f, K, nc, EK, kv, 1.f, R, nc))                           // - K (L' + E^T K)
             return PDG_CUDA_ERROR;
         k_sweep<<<G, WB, 0, st>>>((size_t)nc * kv, E, R, Gi, K, K2, 0, part, p.parts);
-        k_sweep_max<<<1, 1, 0, st>>>(part, p.parts, G, mx);
+        k_sweep_max<<<1, 32, 0, st>>>(part, p.parts, G, mx);
         if (cudaMemcpyAsync(W->sweep, mx, 2 * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess) return PDG_CUDA_ERROR;
         if (cudaStreamSynchronize(st) != cudaSuccess) return PDG_CUDA_ERROR;
         float *tmp = K; K = K2; K2 = tmp;
@@ -1249,7 +1318,7 @@ static int wide_pert_step(pdg_wide *W, double *ws, double *P, cudaStream_t st, i
     // dQ = [Z0 | Y] [W | Z0 + W]^T
     if (sgemm(W, st, Nn, Tt, N, N, 2 * kv, 1.f, Z0, N, Wc, N, 0.f, DQ, N)) return PDG_CUDA_ERROR;
     k_pert_density<<<G, WB, 0, st>>>(N, s.vec_occupied ? 2.0 : -2.0, ws + p.BP, DQ, P, part, p.parts);
-    k_control_density<<<1, 1, 0, st>>>((Ctl *)(ws + p.ctl), part, p.parts, G, N);
+    k_control_density<<<1, 32, 0, st>>>((Ctl *)(ws + p.ctl), part, p.parts, G, N);
     mark(W, st, WPH_DENSITY);
     *done = 1;
     return cudaGetLastError() == cudaSuccess ? PDG_OK : PDG_CUDA_ERROR;
@@ -1283,7 +1352,7 @@ int wide_energy_gradients(pdg_wide *W, const double *xyz, const double *phi, con
         k_fock<<<G * 4, WB, 0, st>>>(s, H, P, ws + p.fp.tei, ws + p.pk, F);
         k_traces<<<nb_tr, WB, 0, st>>>(N, P, H, F, part, p.parts);
         k_lowdin<<<1, WB, 0, st>>>(s, P, phi, F, charges, part, p.parts);
-        k_control_fock<<<1, 1, 0, st>>>(ctl, part, p.parts, nb_tr, o, hist);
+        k_control_fock<<<1, 32, 0, st>>>(ctl, part, p.parts, nb_tr, o, hist);
         mark(W, st, WPH_FOCK);
         if (cudaMemcpyAsync(&W->host, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st) != cudaSuccess) return PDG_CUDA_ERROR;
         if (cudaStreamSynchronize(st) != cudaSuccess) return PDG_CUDA_ERROR;
