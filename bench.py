@@ -649,6 +649,8 @@ def main():
     ap.add_argument("--workload", default="qcmm_water_box", choices=["qcmm_water_box", "water_clusters", "qcmm_md", "large_qcmm"],
                     help="the QC/MM water box (the headline metric), 512 independent PM3 water clusters in one launch, or "
                          "Langevin dynamics of water-box replicas with the learned start density trained on trajectories")
+    ap.add_argument("--no-large", action="store_true", help="leave out the large QC/MM sub-line of the default workload")
+    ap.add_argument("--large-steps", type=int, default=10, help="timed MD steps per method of the large QC/MM sub-line")
     ap.add_argument("--md-equilibration", type=int, default=150)
     ap.add_argument("--md-training-steps", type=int, default=66, help="training densities = replicas x this")
     ap.add_argument("--md-epochs", type=int, default=6)
@@ -972,6 +974,9 @@ def bench_water_box(args, world, rank):
                                           "gate": "|dE| < 1e-6 Eh, |dF| < 1e-5 Eh/Bohr", "pass": bool(dE < 1e-6 and dG < 1e-5),
                                           "oracle": "each method's timed configuration is checked against the oracle frame by frame "
                                                     "in tests/test_gpu_timed_config.py"}
+    if rank == 0 and not args.no_large:
+        # config 4, the large QC/MM system over the whole GPU: a short Langevin trajectory per method
+        line["large_qcmm"] = bench_large(args, md_steps=args.large_steps, md_warmup=3, cpu=not args.no_cpu_baseline)
     if rank == 0 and not args.no_cpu_baseline:
         n = min(nF, 96)
         cpu = CPUBaseline(Z, Q, sel, charge, 1)

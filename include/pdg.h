@@ -391,6 +391,21 @@ size_t pdg_mm_workspace_bytes(const pdg_mm_system *m, int n_frames);
 int pdg_mm_energy_gradients(const pdg_mm_system *m, int n_frames, const double *d_xyz, double *d_energies, double *d_gradients,
                             void *d_workspace, size_t workspace_bytes, void *stream);
 
+/* ---- Harmonic bond and angle terms of an MM model ----
+ * Replace HarmonicBondContainer_Energy and HarmonicAngleContainer_Energy (pMolecule-1.9.0/extensions/csource/
+ * HarmonicBondContainer.c:149, HarmonicAngleContainer.c:157): E = k (r - r0)^2 per bond and k (theta - theta0)^2 per angle
+ * (theta at the middle atom, its cosine clamped to +-0.999999 as the reference does), for many frames.  kJ/mol, Angstrom,
+ * radians.  For the flexible waters of MM models that move in dynamics.
+ *   pdg_mm_bonded_create   n_atoms; bonds (i, j) with (r0, k); angles (i, j, k), j the apex, with (theta0, k)
+ *   pdg_mm_bonded_energy_gradients  for n_frames frames of d_xyz (n_frames x n_atoms x 3): d_energies n_frames x 2 (bond,
+ *                          angle), and unless NULL the gradients ADDED to d_gradients (n_frames x n_atoms x 3, kJ/mol/A) */
+typedef struct pdg_mm_bonded pdg_mm_bonded;
+int pdg_mm_bonded_create(int n_atoms, int n_bonds, const int *h_bonds, const double *h_bond_params, int n_angles,
+                         const int *h_angles, const double *h_angle_params, pdg_mm_bonded **out);
+int pdg_mm_bonded_destroy(pdg_mm_bonded *bonded);
+int pdg_mm_bonded_energy_gradients(const pdg_mm_bonded *bonded, int n_frames, const double *d_xyz, double *d_energies,
+                                   double *d_gradients, void *stream);
+
 /* ---- One large QC region over the whole GPU ----
  * pdg_energy_gradients gives each frame one CTA (one SM): the throughput form for many frames of a small region.  A
  * single large region (hundreds of atoms, N up to PDG_MAX_BASIS) is computed here with every SCF phase spread over all
@@ -402,7 +417,7 @@ int pdg_mm_energy_gradients(const pdg_mm_system *m, int n_frames, const double *
  * options->density_step 0 is the reference's FP64 method; 3 or 6 the mixed method of this path: every FP64 density step
  * keeps a base (its matrix, density and all eigenpairs), and the following steps are perturbative ones around it in FP32
  * products with small factors (scf.cu's perturbative step as SGEMMs), falling back to an FP64 step when the correction
- * is not small (|K| >= 1e-2); the DIIS error is formed in FP32 from the change of F; the sp-sp and sp-s pair gradient terms are FP32.
+ * is not small (|K| >= 3e-2); the DIIS error is formed in FP32 from the change of F; the sp-sp and sp-s pair gradient terms are FP32.
  * The base stays with the wide engine and its workspace between calls, so a warm-started call (the next MD step) can run
  * perturbative steps from its first cycle.
  *   pdg_wide_create       a wide engine for sys (which must outlive it); holds a cuBLAS handle and, after the first

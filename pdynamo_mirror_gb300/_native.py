@@ -28,7 +28,7 @@ EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system
            "pdg_normal_deviates", "pdg_density_combine", "pdg_mm_create", "pdg_mm_destroy", "pdg_mm_workspace_bytes",
            "pdg_mm_energy_gradients", "pdg_phase_events", "pdg_phase_times", "pdg_qcmm_workspace_bytes", "pdg_wide_create", "pdg_wide_destroy",
            "pdg_wide_workspace_bytes", "pdg_wide_energy_gradients", "pdg_wide_phase_events", "pdg_wide_phase_times",
-           "pdg_last_error")
+           "pdg_mm_bonded_create", "pdg_mm_bonded_destroy", "pdg_mm_bonded_energy_gradients", "pdg_last_error")
 TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densities Tridiagonal", "QC Densities Eigenvalues",
           "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds",
           "QC Densities Cluster Rounds", "QC Densities Steps", "QC Densities Purification",
@@ -122,6 +122,9 @@ def load(path=LIB_PATH):
     L.pdg_density_combine.argtypes = [LL, I, P, P, P, P]
     L.pdg_mm_create.argtypes = [I, P, P, P, I, P, P, P, P, I, P, I, P, D, D, D, D, D, PP]
     L.pdg_mm_destroy.argtypes = [P]
+    L.pdg_mm_bonded_create.argtypes = [I, I, P, P, I, P, P, PP]
+    L.pdg_mm_bonded_destroy.argtypes = [P]
+    L.pdg_mm_bonded_energy_gradients.argtypes = [P, I, P, P, P, P]
     L.pdg_mm_workspace_bytes.argtypes = [P, I]
     L.pdg_mm_workspace_bytes.restype = S
     L.pdg_mm_energy_gradients.argtypes = [P, I, P, P, P, P, S, P]

@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libpdg.so")
-UNITS = ("api.cu", "integrals.cu", "scf.cu", "scf_wide.cu", "qcmm.cu", "tc.cu", "guess.cu", "dynamics.cu", "mmmm.cu", "wide.cu")
+UNITS = ("api.cu", "integrals.cu", "scf.cu", "scf_wide.cu", "qcmm.cu", "tc.cu", "guess.cu", "dynamics.cu", "mmmm.cu", "wide.cu", "bonded.cu")
 HEADERS = ("common.cuh", "multipole.cuh", "overlap.cuh", "tc.cuh")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-diag-suppress", "177"]

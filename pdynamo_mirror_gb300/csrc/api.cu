@@ -42,6 +42,8 @@ struct pdg_system {
 
 extern "C" int pdg_version(void) { return 100; }
 
+int bonded_fail(int code, const char *msg) { return fail(code, msg); }
+
 extern "C" const char *pdg_last_error(void) { return g_error.c_str(); }
 
 extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n_atoms, const int *h_atom_element,
