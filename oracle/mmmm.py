@@ -155,3 +155,32 @@ def energies(xyz, charges, lj_types, flags, epsilon, sigma, epsilon14, sigma14, 
         s = ((qcp[i] & mm[j]) | (mm[i] & qcp[j])) & f2
         add(i[s], j[s], np.zeros(int(s.sum())), A14[t[i[s]], t[j[s]]], B14[t[i[s]], t[j[s]]], 2, 5, False)
     return E, G
+
+
+def harmonic_terms(X, bonds, bond_params, angles, angle_params):
+    """Harmonic bonds and angles, as HarmonicBondContainer_Energy (pMolecule-1.9.0/extensions/csource/
+    HarmonicBondContainer.c:149-181: E = k (r - r0)^2) and HarmonicAngleContainer_Energy (HarmonicAngleContainer.c:157-200:
+    E = k (theta - theta0)^2 at the middle atom, cosine clamped to +-0.999999).  X [n, 3] (A); bonds [nb, 2] with
+    (r0, k); angles [na, 3] with (theta0 rad, k).  Returns (E_bond, E_angle) in kJ/mol and the gradients [n, 3]."""
+    X = np.asarray(X, dtype=np.float64)
+    G = np.zeros_like(X)
+    eb = ea = 0.0
+    for (i, j), (r0, k) in zip(np.asarray(bonds, dtype=np.int64).reshape(-1, 2), np.asarray(bond_params, dtype=np.float64).reshape(-1, 2)):
+        d = X[i] - X[j]
+        r = np.sqrt(d @ d)
+        df = k * (r - r0)
+        eb += df * (r - r0)
+        g = (2.0 * df / r) * d
+        G[i] += g; G[j] -= g
+    for (i, j, l), (t0, k) in zip(np.asarray(angles, dtype=np.int64).reshape(-1, 3), np.asarray(angle_params, dtype=np.float64).reshape(-1, 2)):
+        a, c = X[i] - X[j], X[l] - X[j]
+        ra, rc = np.sqrt(a @ a), np.sqrt(c @ c)
+        a, c = a / ra, c / rc
+        dot = min(0.999999, max(-0.999999, a @ c))
+        theta = np.arccos(dot)
+        df = k * (theta - t0)
+        ea += df * (theta - t0)
+        d2 = 2.0 * df * (-1.0 / np.sqrt(1.0 - dot * dot))
+        gi, gk = d2 * (c - dot * a) / ra, d2 * (a - dot * c) / rc
+        G[i] += gi; G[l] += gk; G[j] -= gi + gk
+    return eb, ea, G

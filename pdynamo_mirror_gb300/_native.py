@@ -17,7 +17,7 @@ QCMM_FP32_PAIRS = 0x100   # pdg_qcmm_gradients model flag: FP32 pair terms (the 
 MM_FLAG_MM, MM_FLAG_QC_LJ, MM_FLAG_FIXED = 1, 2, 4   # pdg_mm_create atom flags
 WIDE_PHASES = ("integrals", "fock", "diis", "tridiagonal", "eigenvalues", "eigenvectors", "backtransform", "density", "gradients",
                "fp64_steps", "perturbative_steps")
-MM_TERMS = ("MM/MM Elect.", "MM/MM LJ", "MM/MM 1-4 Elect.", "MM/MM 1-4 LJ", "QC/MM LJ", "QC/MM 1-4 LJ")
+MM_TERMS = ("MM/MM Elect.", "MM/MM LJ", "MM/MM 1-4 Elect.", "MM/MM 1-4 LJ", "QC/MM LJ", "QC/MM 1-4 LJ", "Harmonic Bond", "Harmonic Angle")
 
 EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system_info", "pdg_workspace_bytes",
            "pdg_energy_gradients", "pdg_scf", "pdg_density", "pdg_one_electron", "pdg_fock", "pdg_gradients", "pdg_qcmm_potentials",

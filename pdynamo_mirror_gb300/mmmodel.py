@@ -11,7 +11,10 @@ connectivity); here the caller supplies what the energy needs, in the reference'
   the 1-4 pairs (the reference's MMAtomContainer, ljParameters, ljParameters14, exclusions, interactions14 handed to
   NBModelABFS.SetUp, pMolecule.NBModelABFS.pyx:181).  ``MMModel.TIP3PWater`` builds one for systems of waters.
 * ``MMInteractions``  the device evaluation through pdg_mm_create / pdg_mm_energy_gradients (MM/MM Elect., MM/MM LJ,
-  their 1-4 terms, QC/MM LJ and its 1-4 term, labelled as NBModelABFSState.GetEnergies does).
+  their 1-4 terms, QC/MM LJ and its 1-4 term, labelled as NBModelABFSState.GetEnergies does) and, when the model has
+  them, the harmonic bond and angle terms through pdg_mm_bonded_* (HarmonicBondContainer_Energy,
+  HarmonicAngleContainer_Energy; "Harmonic Bond", "Harmonic Angle"), with the terms among QC atoms only or fixed atoms
+  only left out as the reference deactivates them (pMolecule-1.9.0/pMolecule/EnergyModel.py:118-143).
 """
 
 import ctypes
@@ -25,6 +28,12 @@ from . import _native
 # LJ parameters (epsilon 0.1521 kcal/mol, sigma 3.15061 A); hydrogens carry no LJ term.
 TIP3P_CHARGE_O, TIP3P_CHARGE_H = -0.834, 0.417
 TIP3P_EPSILON_O, TIP3P_SIGMA_O = 0.1521 * 4.184, 3.15061
+# The flexible water of the reference's OPLS files (parameters/forceFields/opls/protein/harmonicBondParameters.yaml:359,
+# harmonicAngleParameters.yaml:988): HW-OW 0.9572 A with 529.60 kcal/mol/A^2, HW-OW-HW 104.52 deg with 34.05
+# kcal/mol/rad^2, E = k (x - x0)^2, converted to kJ/mol and radians as HarmonicBondParameterContainer /
+# HarmonicAngleParameterContainer.ProcessRawItems do (1 kcal = 4.184 kJ).
+WATER_OH_R0, WATER_OH_K = 0.9572, 529.60 * 4.184
+WATER_HOH_THETA0, WATER_HOH_K = np.radians(104.52), 34.05 * 4.184
 
 
 class LJParameterContainer:
@@ -73,7 +82,8 @@ def _pairs(p, n):
 class MMModel:
     """Charges (e) and LJ types of every atom, LJ parameters, exclusions and 1-4 pairs."""
 
-    def __init__(self, charges, ljTypes, ljParameters, ljParameters14=None, exclusions=None, interactions14=None):
+    def __init__(self, charges, ljTypes, ljParameters, ljParameters14=None, exclusions=None, interactions14=None, bonds=None,
+                 angles=None):
         self.charges = np.array(charges, dtype=np.float64).ravel()
         self.ljTypes = np.array(ljTypes, dtype=np.int64).ravel()
         n = len(self.charges)
@@ -87,16 +97,25 @@ class MMModel:
             raise ValueError("LJ type out of range.")
         self.exclusions = _pairs(exclusions, n)
         self.interactions14 = _pairs(interactions14, n)
+        # harmonic terms: bonds (i, j, r0 A, k kJ/mol/A^2), angles (i, j apex, k, theta0 rad, k kJ/mol/rad^2)
+        b = np.array(bonds if bonds is not None else [], dtype=np.float64).reshape(-1, 4)
+        a = np.array(angles if angles is not None else [], dtype=np.float64).reshape(-1, 5)
+        self.bonds, self.bondParameters = b[:, :2].astype(np.int64), b[:, 2:].copy()
+        self.angles, self.angleParameters = a[:, :3].astype(np.int64), a[:, 3:].copy()
+        for idx in (self.bonds, self.angles):
+            if idx.size and (idx.min() < 0 or idx.max() >= n):
+                raise ValueError("Bond or angle atom out of range.")
 
     @property
     def natoms(self):
         return len(self.charges)
 
     @classmethod
-    def TIP3PWater(cls, atomicNumbers, coordinates3, bondCutoff=1.25):
+    def TIP3PWater(cls, atomicNumbers, coordinates3, bondCutoff=1.25, flexible=False):
         """Waters (and hydroxides): each hydrogen bonds to the nearest oxygen within bondCutoff (A); TIP3P charges
         and oxygen LJ (hydroxide O-H pairs take the water charges of their atoms); exclusions within each
-        molecule (O-H and H-H); no 1-4 pairs."""
+        molecule (O-H and H-H); no 1-4 pairs.  flexible adds the O-H bonds and H-O-H angles of the reference's OPLS
+        water, so that MM waters can move in dynamics."""
         Z = np.asarray(atomicNumbers)
         X = np.asarray(coordinates3, dtype=np.float64).reshape(len(Z), 3)
         if not set(np.unique(Z)) <= {1, 8}:
@@ -115,7 +134,14 @@ class MMModel:
             excl += [(hs[a], hs[b]) for a in range(len(hs)) for b in range(a + 1, len(hs))]
         charges = np.where(Z == 8, TIP3P_CHARGE_O, TIP3P_CHARGE_H)
         lj = LJParameterContainer([TIP3P_EPSILON_O, 0.0], [TIP3P_SIGMA_O, 0.0], rule="OPLS")
-        return cls(charges, np.where(Z == 8, 0, 1), lj, exclusions=excl)
+        bonds, angles = [], []
+        if flexible:
+            for o in sorted(owner):
+                hs = owner[o]
+                bonds += [(o, h, WATER_OH_R0, WATER_OH_K) for h in hs]
+                if len(hs) == 2:
+                    angles.append((hs[0], o, hs[1], WATER_HOH_THETA0, WATER_HOH_K))
+        return cls(charges, np.where(Z == 8, 0, 1), lj, exclusions=excl, bonds=bonds, angles=angles)
 
 
 class MMInteractions:
@@ -150,6 +176,21 @@ class MMInteractions:
                                       nbModel.electrostaticScale14, ctypes.byref(h)), "pdg_mm_create")
         self.handle, self.n, self.device = h, n, device
         self._ws = None
+        # harmonic terms, those among QC atoms only or among fixed atoms only left out (EnergyModel.py:118-143)
+        qcset, fixset = set(qc.tolist()), set(fixedAtoms or [])
+
+        def active(atoms):
+            return not (all(a in qcset for a in atoms) or all(a in fixset for a in atoms))
+        kb = [t for t in range(len(mmModel.bonds)) if active(mmModel.bonds[t].tolist())]
+        ka = [t for t in range(len(mmModel.angles)) if active(mmModel.angles[t].tolist())]
+        self.has_bonds, self.has_angles = len(kb) > 0, len(ka) > 0
+        self.bonded = None
+        if kb or ka:
+            bi = c(mmModel.bonds[kb].ravel(), np.int32); bp = c(mmModel.bondParameters[kb][:, [0, 1]].ravel(), np.float64)
+            ai = c(mmModel.angles[ka].ravel(), np.int32); ap = c(mmModel.angleParameters[ka][:, [0, 1]].ravel(), np.float64)
+            hb = ctypes.c_void_p()
+            _native.check(L.pdg_mm_bonded_create(n, len(kb), p(bi), p(bp), len(ka), p(ai), p(ap), ctypes.byref(hb)), "pdg_mm_bonded_create")
+            self.bonded = hb
 
     def __del__(self):
         if getattr(self, "handle", None):
@@ -158,9 +199,15 @@ class MMInteractions:
             except Exception:
                 pass
             self.handle = None
+        if getattr(self, "bonded", None):
+            try:
+                _native.load().pdg_mm_bonded_destroy(self.bonded)
+            except Exception:
+                pass
+            self.bonded = None
 
     def run(self, frames, gradients=True):
-        """frames: device tensor [F, n, 3] (A).  Returns (energies [F, 6] kJ/mol in the order of _native.MM_TERMS,
+        """frames: device tensor [F, n, 3] (A).  Returns (energies [F, 8] kJ/mol in the order of _native.MM_TERMS,
         gradients [F, n, 3] kJ/mol/A or None)."""
         F = frames.shape[0]
         L = _native.load()
@@ -168,11 +215,18 @@ class MMInteractions:
         if self._ws is None or self._ws.numel() < need:
             self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
         X = frames.contiguous()
-        E = torch.empty((F, 6), dtype=torch.float64, device=self.device)
+        E = torch.zeros((F, len(_native.MM_TERMS)), dtype=torch.float64, device=self.device)
         G = torch.empty((F, self.n, 3), dtype=torch.float64, device=self.device) if gradients else None
         st = _native.stream_handle(torch.cuda.current_stream(self.device))
-        _native.check(L.pdg_mm_energy_gradients(self.handle, F, _native.ptr(X), _native.ptr(E), _native.ptr(G), _native.ptr(self._ws),
+        E6 = torch.empty((F, 6), dtype=torch.float64, device=self.device)
+        _native.check(L.pdg_mm_energy_gradients(self.handle, F, _native.ptr(X), _native.ptr(E6), _native.ptr(G), _native.ptr(self._ws),
                                                 self._ws.numel(), st), "pdg_mm_energy_gradients")
+        E[:, :6] = E6
+        if self.bonded is not None:
+            Eb = torch.empty((F, 2), dtype=torch.float64, device=self.device)
+            _native.check(L.pdg_mm_bonded_energy_gradients(self.bonded, F, _native.ptr(X), _native.ptr(Eb), _native.ptr(G), st),
+                          "pdg_mm_bonded_energy_gradients")
+            E[:, 6:] = Eb
         return E, G
 
     def term_names(self):
@@ -182,4 +236,5 @@ class MMInteractions:
             names += ["MM/MM 1-4 Elect.", "MM/MM 1-4 LJ"]
         if self.has_qc:
             names += ["QC/MM LJ"] + (["QC/MM 1-4 LJ"] if self.has14 else [])
+        names += (["Harmonic Bond"] if self.has_bonds else []) + (["Harmonic Angle"] if self.has_angles else [])
         return names

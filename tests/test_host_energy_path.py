@@ -92,7 +92,10 @@ class _OracleMM:
         out = [self.mmmm.energies(x.numpy(), m.charges, m.ljTypes, self.flags, lj.epsilon, lj.sigma, lj.epsilon, lj.sigma, True,
                                   m.exclusions, m.interactions14, self.nb.innerCutoff, self.nb.outerCutoff, self.nb.dampingCutoff)
                for x in frames]
-        return torch.tensor(np.array([o[0] for o in out])), (torch.tensor(np.array([o[1] for o in out])) if gradients else None)
+        E = np.array([o[0] for o in out])
+        # the MMInteractions contract: one column per _native.MM_TERMS entry (no bonded terms in this model)
+        E = np.concatenate([E, np.zeros((len(out), 2))], axis=1)
+        return torch.tensor(E), (torch.tensor(np.array([o[1] for o in out])) if gradients else None)
 
     def term_names(self):
         return ["MM/MM Elect.", "MM/MM LJ", "QC/MM LJ"]

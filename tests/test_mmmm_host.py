@@ -117,3 +117,28 @@ def test_c_abi_rejects_bad_arguments():
     rc = L.pdg_mm_create(2, p(q), p(t), p(fl), 1, p(tab), p(tab), p(tab), p(tab), 0, None, 0, None, 12.0, 8.0, 0.5, 1.0, 1.0,
                          ctypes.byref(h))
     assert rc == _native.PDG_BAD_ARGUMENT
+
+
+def test_harmonic_terms_match_finite_differences_and_tip3p_geometry():
+    """The oracle's harmonic bond and angle terms: zero at the TIP3P geometry, analytic gradients against central
+    differences on a distorted water pair, and the flexible TIP3P model's terms (two bonds and one angle per water)."""
+    import numpy as np
+    from oracle import mmmm
+    from pdynamo_mirror_gb300 import MMModel, workloads
+    Z, X = workloads.water_cluster(2, seed=5)
+    m = MMModel.TIP3PWater(Z, X, flexible=True)
+    assert len(m.bonds) == 4 and len(m.angles) == 2
+    eb, ea, G = mmmm.harmonic_terms(X, m.bonds, m.bondParameters, m.angles, m.angleParameters)
+    assert abs(eb) < 1e-10 and abs(ea) < 1e-10
+    Xd = X + np.random.default_rng(2).normal(scale=0.05, size=X.shape)
+    eb, ea, G = mmmm.harmonic_terms(Xd, m.bonds, m.bondParameters, m.angles, m.angleParameters)
+    assert eb > 0 and ea > 0
+    h = 1e-6
+    for a in range(len(Z)):
+        for c in range(3):
+            Xp, Xm = Xd.copy(), Xd.copy()
+            Xp[a, c] += h; Xm[a, c] -= h
+            ep = sum(mmmm.harmonic_terms(Xp, m.bonds, m.bondParameters, m.angles, m.angleParameters)[:2])
+            em = sum(mmmm.harmonic_terms(Xm, m.bonds, m.bondParameters, m.angles, m.angleParameters)[:2])
+            assert abs((ep - em) / (2 * h) - G[a, c]) < 1e-5 * max(1.0, abs(G[a, c]))
+    assert len(MMModel.TIP3PWater(Z, X).bonds) == 0
