@@ -450,7 +450,7 @@ def bench_md(args):
     s_ho = make("fp64")
     ho = LangevinDynamics(s_ho, replicas=R, timeStep=0.0005, seed=202 + rank, densityGuess="extrapolate")
     equilibrate(ho)
-    snap = dict(xyz=ho.xyz.clone(), vel=ho.vel.clone(), acc=ho.acc.clone(), hist=[h.clone() for h in ho.history], n=ho.n_step)
+    snap = dict(X=ho.X.clone(), vel=ho.vel.clone(), acc=ho.acc.clone(), hist=[h.clone() for h in ho.history], n=ho.n_step)
     # (a) cold start on held-out frames: learned guess against the diagonal guess
     cold = LearnedDensityGuess(s_ho.engine(), seed=0)
     cold.load_state_dict(g.state_dict())
@@ -463,7 +463,7 @@ def bench_md(args):
             guess = LearnedDensityGuess(s.engine(), seed=0)
             guess.load_state_dict(g.state_dict())
         m = LangevinDynamics(s, replicas=R, timeStep=0.0005, seed=202 + rank, densityGuess=guess)
-        m.xyz.copy_(snap["xyz"]); m.vel.copy_(snap["vel"]); m.acc.copy_(snap["acc"]); m.n_step = snap["n"]
+        m.X.copy_(snap["X"]); m.vel.copy_(snap["vel"]); m.acc.copy_(snap["acc"]); m.n_step = snap["n"]
         m.history = [h.clone() for h in snap["hist"]]
         m.last = {}
         m.run(warm)

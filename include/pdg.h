@@ -342,7 +342,8 @@ int pdg_graph_destroy(pdg_graph *graph);
  *   pdg_langevin_positions   the first half of Iteration (:126-137 and RandomForces :147-157): positions, half
  *                            velocities, random forces from Philox4x32-10 normal deviates for (seed, element,
  *                            step); d_deviates (NULL or n_replicas x n_free x 3 x 2) receives (w1, w2) per element.
- *                            random = 0 applies no random forces.
+ *                            random = 0 applies no random forces; random = 2 reads the deviates from d_deviates
+ *                            instead (deviates with the linear constraints projected out, below).
  *   pdg_langevin_velocities  the second half (:139-144): accelerations a = -100 grad_scale (g_a + g_b) / m from the
  *                            gradients at the new point (rows d_grad_rows[f] of n_replicas x n_rows x 3 arrays;
  *                            d_grad_b may be NULL; grad_scale converts them to kJ/mol/A), v += facV3 a, and per
@@ -354,6 +355,16 @@ int pdg_langevin_positions(int n_replicas, int n_atoms, int n_free, const int *d
 int pdg_langevin_velocities(int n_replicas, int n_free, int n_rows, const int *d_grad_rows, const double *d_mass,
                             const double *d_grad_a, const double *d_grad_b, double grad_scale, double facV3,
                             double *d_velocities, double *d_accelerations, double *d_mv2, void *stream);
+/* Linear constraints of the dynamics (SystemGeometryObjectiveFunction.ApplyLinearConstraints / GradientsGet /
+ * VelocitiesAssign, pMolecule-1.9.0/pMolecule/SystemGeometryObjectiveFunction.py:99-101, :177-183, :317-345, through
+ * Real2DArray.ProjectOutOfArray): for each replica, x_w -= V (V^T x_w) where x_w = s x is the mass-weighted form of
+ * the array and V the replica's n_vectors (1..6) orthonormal rotation and translation vectors
+ * (Coordinates3_RotationTranslationVectors, pCore-1.9.0/extensions/csource/Coordinates3.c:1315; d_vectors
+ * n_replicas x n_vectors x n_free x 3).  d_scale: s per free atom (sqrt(m) for velocities, 1/sqrt(m) for
+ * gradients, NULL for 1: the deviates).  Element (fa, k, c) of replica r is d_array[((r n_rows + row) 3 + k) width
+ * + c], row = d_rows[fa] (d_rows NULL: row fa, n_rows = n_free); width 1 or 2 (the two deviate vectors). */
+int pdg_linear_constraints_project(int n_replicas, int n_free, int n_rows, const int *d_rows, int n_vectors, const double *d_vectors,
+                                   const double *d_scale, int width, double *d_array, void *stream);
 /* n_pairs pairs of standard normal deviates for counters (pair index, step, stream_id) under key seed, the
  * generator pdg_langevin_positions uses (stream_id 0); for tests and for velocity assignment. */
 int pdg_normal_deviates(long long n_pairs, unsigned long long seed, unsigned int step, unsigned int stream_id, double *d_out,

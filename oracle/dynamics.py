@@ -116,3 +116,39 @@ def assign_velocities(masses, temperature_k, rng):
     v = rng.standard_normal((len(masses), 3)) * sigma / np.sqrt(masses)[:, None]
     _, t = temperature(v, masses, 3 * len(masses))
     return v * math.sqrt(temperature_k / t)
+
+
+def rotation_translation_vectors(x, masses):
+    """Mass-weighted rotation and translation vectors (Coordinates3_RotationTranslationVectors,
+    pCore-1.9.0/extensions/csource/Coordinates3.c:1315-1385, weights = masses): columns Tx, Ty, Tz, Rx, Ry, Rz of a
+    3n x 6 matrix, sqrt(m) weights and rotations about the centre of mass, orthonormalised by one Gram-Schmidt pass
+    that drops columns whose norm falls to 1e-10 sqrt(3n) or below (Real2DArray.c:487-545).  Returns [K, n, 3]."""
+    x = np.asarray(x, dtype=np.float64).reshape(-1, 3)
+    m = np.asarray(masses, dtype=np.float64)
+    n = len(m)
+    sw = np.sqrt(m)
+    c = x - np.average(x, axis=0, weights=m)
+    M = np.zeros((3 * n, 6))
+    for a in range(3):
+        M[a::3, a] = sw
+    # rotation about axis a: sqrt(m) (e_a x (x - c))
+    for a in range(3):
+        e = np.zeros(3); e[a] = 1.0
+        M[:, 3 + a] = (sw[:, None] * np.cross(e, c)).ravel()
+    kept = []
+    for col in range(6):
+        v = M[:, col].copy()
+        for u in kept:
+            v = v - np.dot(v, u) * u
+        if np.linalg.norm(v) > 1.0e-10 * math.sqrt(3 * n):
+            kept.append(v / np.linalg.norm(v))
+    return np.array(kept).reshape(-1, n, 3)
+
+
+def project(a, vectors, weights):
+    """Removes the vectors (orthonormal in the weighted space) from a [n, 3] whose weighted form is weights[:, None] a
+    (ProjectOutOfArray on the objective function's mass-weighted variables)."""
+    aw = (np.asarray(weights, dtype=np.float64)[:, None] * a).ravel()
+    V = np.asarray(vectors, dtype=np.float64).reshape(len(vectors), -1)
+    aw = aw - V.T @ (V @ aw)
+    return aw.reshape(-1, 3) / np.asarray(weights, dtype=np.float64)[:, None]

@@ -25,7 +25,7 @@ EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system
            "pdg_mlp_backward", "pdg_mlp_adam", "pdg_guess_assemble", "pdg_guess_loss", "pdg_batch_create", "pdg_batch_destroy",
            "pdg_batch_info", "pdg_batch_workspace_bytes", "pdg_batch_schedule", "pdg_batch_energy_gradients", "pdg_batch_timings",
            "pdg_batch_graph_create", "pdg_graph_launch", "pdg_graph_destroy", "pdg_langevin_positions", "pdg_langevin_velocities",
-           "pdg_normal_deviates", "pdg_density_combine", "pdg_mm_create", "pdg_mm_destroy", "pdg_mm_workspace_bytes",
+           "pdg_normal_deviates", "pdg_linear_constraints_project", "pdg_density_combine", "pdg_mm_create", "pdg_mm_destroy", "pdg_mm_workspace_bytes",
            "pdg_mm_energy_gradients", "pdg_phase_events", "pdg_phase_times", "pdg_qcmm_workspace_bytes", "pdg_wide_create", "pdg_wide_destroy",
            "pdg_wide_workspace_bytes", "pdg_wide_energy_gradients", "pdg_wide_phase_events", "pdg_wide_phase_times",
            "pdg_mm_bonded_create", "pdg_mm_bonded_destroy", "pdg_mm_bonded_energy_gradients", "pdg_last_error")
@@ -119,6 +119,7 @@ def load(path=LIB_PATH):
     L.pdg_langevin_positions.argtypes = [I, I, I, P, P, P, P, P, P, I, U64, U32, P, P]
     L.pdg_langevin_velocities.argtypes = [I, I, I, P, P, P, P, D, D, P, P, P, P]
     L.pdg_normal_deviates.argtypes = [LL, U64, U32, U32, P, P]
+    L.pdg_linear_constraints_project.argtypes = [I, I, I, P, I, P, P, I, P, P]
     L.pdg_density_combine.argtypes = [LL, I, P, P, P, P]
     L.pdg_mm_create.argtypes = [I, P, P, P, I, P, P, P, P, I, P, I, P, D, D, D, D, D, PP]
     L.pdg_mm_destroy.argtypes = [P]

@@ -795,7 +795,8 @@ extern "C" int pdg_langevin_positions(int n_replicas, int n_atoms, int n_free, c
     LangevinFactors f;
     f.facR1 = h_factors[0]; f.facR2 = h_factors[1]; f.facV1 = h_factors[2]; f.facV2 = h_factors[3];
     f.sdR = h_factors[4]; f.sdV1 = h_factors[5]; f.sdV2 = h_factors[6];
-    f.random = random ? 1 : 0;
+    if (random < 0 || random > 2 || (random == 2 && !d_deviates)) return fail(PDG_BAD_ARGUMENT, "pdg_langevin_positions: bad random mode");
+    f.random = random;
     launch_langevin_positions(n_replicas, n_atoms, n_free, d_free_atoms, d_inv_sqrt_mass, d_xyz, d_velocities, d_accelerations, f,
                               (uint64_t)seed, (uint32_t)step, d_deviates, (cudaStream_t)stream);
     return cuda_check(cudaGetLastError(), "langevin positions kernel");
@@ -810,6 +811,16 @@ extern "C" int pdg_langevin_velocities(int n_replicas, int n_free, int n_rows, c
     launch_langevin_velocities(n_replicas, n_free, n_rows, d_grad_rows, d_mass, d_grad_a, d_grad_b, grad_scale, facV3, d_velocities,
                                d_accelerations, d_mv2, (cudaStream_t)stream);
     return cuda_check(cudaGetLastError(), "langevin velocities kernel");
+}
+
+extern "C" int pdg_linear_constraints_project(int n_replicas, int n_free, int n_rows, const int *d_rows, int n_vectors,
+                                              const double *d_vectors, const double *d_scale, int width, double *d_array, void *stream)
+{
+    if (n_replicas <= 0 || n_free <= 0 || n_rows < n_free || n_vectors < 1 || n_vectors > 6 || !d_vectors ||
+        width < 1 || width > 2 || !d_array || (!d_rows && n_rows != n_free))
+        return fail(PDG_BAD_ARGUMENT, "pdg_linear_constraints_project: bad argument");
+    launch_linear_project(n_replicas, n_free, n_rows, d_rows, n_vectors, d_vectors, d_scale, width, d_array, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "linear constraints kernel");
 }
 
 extern "C" int pdg_normal_deviates(long long n_pairs, unsigned long long seed, unsigned int step, unsigned int stream_id, double *d_out,

@@ -300,7 +300,7 @@ void launch_guess_loss(const DeviceSystem &s, int n_frames, const double *xyz, c
 // carry the temperature factor.
 struct LangevinFactors {
     double facR1, facR2, facV1, facV2, sdR, sdV1, sdV2;
-    int random;   // 0: no random forces (plain velocity Verlet with friction), for tests
+    int random;   // 0: no random forces (plain velocity Verlet with friction), 1: generated deviates, 2: given deviates
 };
 #define PDG_MAX_DENSITY_TERMS 8
 struct DensityTerms {
@@ -316,6 +316,8 @@ void launch_langevin_velocities(int n_replicas, int n_free, int n_rows, const in
                                 cudaStream_t st);
 void launch_density_combine(long long n, const DensityTerms &t, double *out, cudaStream_t st);
 void launch_normal_deviates(long long n_pairs, uint64_t seed, uint32_t step, uint32_t stream, double *out, cudaStream_t st);
+void launch_linear_project(int n_replicas, int n_free, int n_rows, const int *rows, int n_vectors, const double *vectors,
+                           const double *scale, int width, double *arr, cudaStream_t st);
 
 // ---- MM/MM and QC/MM Lennard-Jones energies (mmmm.cu) ----
 // Per-atom flags: an active MM atom, a QC atom with LJ interactions (the reference's qcpSelection), a fixed atom.

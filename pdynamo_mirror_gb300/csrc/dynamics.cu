@@ -12,7 +12,12 @@
 // x += sdR w1 / sqrt(m), v += (sdV1 w1 + sdV2 w2) / sqrt(m), a = -100 g / m.  Only free atoms move; fixed atoms
 // (System.DefineFixedAtoms) keep their coordinates, as the objective function's freeAtoms selection does
 // (SystemGeometryObjectiveFunction.py:138-152).  With fixed atoms the reference removes no rotation or
-// translation (:213-222), so no linear constraints are applied.
+// translation (:213-222).  Without them its LangevinDynamics_SystemGeometry removes both
+// (MolecularDynamics.py:27-32): orthonormal mass-weighted rotation and translation vectors V, made once from the
+// starting coordinates (Coordinates3_RotationTranslationVectors), are projected out of the assigned velocities,
+// of both deviate vectors (RandomForces, LangevinVelocityVerletIntegrator.py:147-157) and of the gradients
+// (GradientsGet, :177-183).  k_linear_project does that projection for any array whose weighted form is
+// x_w = s x: x_w -= V (V^T x_w), with s = sqrt(m) for velocities, 1 for the deviates, 1 / sqrt(m) for gradients.
 //
 // Normal deviates come from a counter-based generator, so a replica's stream depends only on (seed, replica,
 // element, step) and not on launch shape: Philox4x32-10 (Salmon, Moraes, Dror and Shaw, "Parallel random
@@ -73,14 +78,81 @@ __global__ void k_langevin_positions(int n_replicas, int n_atoms, int n_free, co
     double xv = *x + f.facR1 * v + f.facR2 * a;
     v = f.facV1 * v + f.facV2 * a;
     double w1 = 0.0, w2 = 0.0;
-    if (f.random) {
+    if (f.random == 1) {
         normal_pair((uint64_t)g, step, 0u, seed, w1, w2);
+    } else if (f.random == 2) {                 // given (e.g. projected) deviates
+        w1 = deviates[2 * g];
+        w2 = deviates[2 * g + 1];
+    }
+    if (f.random) {
         xv += f.sdR * s * w1;
         v += (f.sdV1 * w1 + f.sdV2 * w2) * s;
     }
     *x = xv;
     vel[g] = v;
-    if (deviates) { deviates[2 * g] = w1; deviates[2 * g + 1] = w2; }
+    if (deviates && f.random != 2) { deviates[2 * g] = w1; deviates[2 * g + 1] = w2; }
+}
+
+// Linear constraints (see the header): one block per replica.  Element (fa, k, c) of replica r sits at
+// arr[((r n_rows + row(fa)) 3 + k) width + c] with row(fa) = rows[fa] (fa when rows is NULL); each of the width
+// components is a vector of its own.  vec: n_replicas x n_vectors x n_free x 3, orthonormal; scale: s per free atom
+// (NULL: 1).  Dot products in a fixed order: per thread over its strided elements, then lanes, then warps.
+constexpr int LP_T = 256, LP_MAXV = 6, LP_MAXW = 2;
+__global__ void __launch_bounds__(LP_T) k_linear_project(int n_free, int n_rows, const int *__restrict__ rows, int nv,
+                                                         const double *__restrict__ vec, const double *__restrict__ scale, int width,
+                                                         double *__restrict__ arr)
+{
+    __shared__ double part[LP_T / 32][LP_MAXV * LP_MAXW];
+    __shared__ double dots[LP_MAXV * LP_MAXW];
+    const int r = blockIdx.x;
+    const int ne = 3 * n_free;
+    const double *V = vec + (size_t)r * nv * ne;
+    double acc[LP_MAXV * LP_MAXW];
+#pragma unroll
+    for (int i = 0; i < LP_MAXV * LP_MAXW; i++) acc[i] = 0.0;
+    for (int e = threadIdx.x; e < ne; e += LP_T) {
+        const int fa = e / 3, k = e - 3 * fa;
+        const double s = scale ? scale[fa] : 1.0;
+        const double *x = arr + (((size_t)r * n_rows + (rows ? rows[fa] : fa)) * 3 + k) * width;
+#pragma unroll
+        for (int c = 0; c < LP_MAXW; c++) {
+            if (c < width) {
+                const double xw = s * x[c];
+#pragma unroll
+                for (int v = 0; v < LP_MAXV; v++)
+                    if (v < nv) acc[v * LP_MAXW + c] += V[(size_t)v * ne + e] * xw;
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < LP_MAXV * LP_MAXW; i++) {
+        double t = acc[i];
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) part[w][i] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < LP_MAXV * LP_MAXW) {
+        double t = 0.0;
+        for (int q = 0; q < LP_T / 32; q++) t += part[q][threadIdx.x];
+        dots[threadIdx.x] = t;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < ne; e += LP_T) {
+        const int fa = e / 3, k = e - 3 * fa;
+        const double s = scale ? scale[fa] : 1.0;
+        double *x = arr + (((size_t)r * n_rows + (rows ? rows[fa] : fa)) * 3 + k) * width;
+#pragma unroll
+        for (int c = 0; c < LP_MAXW; c++) {
+            if (c < width) {
+                double p = 0.0;
+#pragma unroll
+                for (int v = 0; v < LP_MAXV; v++)
+                    if (v < nv) p += dots[v * LP_MAXW + c] * V[(size_t)v * ne + e];
+                x[c] -= p / s;
+            }
+        }
+    }
 }
 
 // Second half: accelerations from the gradients at the new point and the velocity completion, one block per
@@ -177,4 +249,10 @@ void launch_normal_deviates(long long n_pairs, uint64_t seed, uint32_t step, uin
 {
     const int threads = 256;
     k_normal_deviates<<<(unsigned)((n_pairs + threads - 1) / threads), threads, 0, st>>>(n_pairs, seed, step, stream, out);
+}
+
+void launch_linear_project(int n_replicas, int n_free, int n_rows, const int *rows, int n_vectors, const double *vectors,
+                           const double *scale, int width, double *arr, cudaStream_t st)
+{
+    k_linear_project<<<n_replicas, LP_T, 0, st>>>(n_free, n_rows, rows, n_vectors, vectors, scale, width, arr);
 }

@@ -72,23 +72,42 @@ def test_masses_are_pdynamos():
         atomic_mass(0)
 
 
-def test_dynamics_requires_fixed_mm_atoms():
+def test_dynamics_needs_free_atoms():
     Z, X = workloads.water_cluster(2, seed=1)
-    allZ = np.concatenate([Z, [8, 1, 1]])
-    allX = np.concatenate([X, X[:3] + 6.0])
-    s = System(allZ, allX, mmCharges=[0.0] * len(Z) + [workloads.TIP3P_O, workloads.TIP3P_H, workloads.TIP3P_H])
-    s.DefineQCModel(QCModelMNDO("am1"), qcSelection=range(len(Z)))
-    s.DefineNBModel(NBModelFull())
-    with pytest.raises(ValueError):
+    s = System(Z, X)
+    s.DefineQCModel(QCModelMNDO("am1"))
+    s.DefineFixedAtoms(range(len(Z)))
+    with pytest.raises(ValueError, match="No free atoms"):
         LangevinDynamics(s)
-    with pytest.raises(ValueError):
-        s.DefineFixedAtoms([len(allZ)])
-    # an MM model's LJ terms are not in the dynamics driver: refused rather than left out
-    from pdynamo_mirror_gb300 import MMModel
-    s.DefineFixedAtoms(range(len(Z), len(allZ)))
-    s.DefineMMModel(MMModel.TIP3PWater(allZ, allX))
-    with pytest.raises(ValueError, match="LJ"):
-        LangevinDynamics(s)
+    s.DefineFixedAtoms(None)
+    with pytest.raises(ValueError, match="densityGuess"):
+        LangevinDynamics(s, densityGuess="guess")
+
+
+def test_rotation_translation_vectors_match_oracle():
+    """The host vectors against the oracle's restatement of Coordinates3_RotationTranslationVectors: six for a bent
+    molecule, five for a linear one, three for one atom; orthonormal; and projecting them out of a velocity field
+    leaves no linear or angular momentum."""
+    from pdynamo_mirror_gb300.dynamics import rotation_translation_vectors
+    from pdynamo_mirror_gb300.parameters import atomic_mass
+    Z, X = workloads.water_cluster(3, seed=2)
+    m = np.array([atomic_mass(z) for z in Z])
+    V = rotation_translation_vectors(X, m)
+    Vo = D.rotation_translation_vectors(X, m)
+    assert V.shape == (6, len(Z), 3)
+    np.testing.assert_allclose(V, Vo, rtol=0, atol=1e-12)
+    F = V.reshape(6, -1)
+    np.testing.assert_allclose(F @ F.T, np.eye(6), rtol=0, atol=1e-12)
+    v = np.random.default_rng(0).normal(size=X.shape)
+    vp = D.project(v, V, np.sqrt(m))
+    c = X - np.average(X, axis=0, weights=m)
+    np.testing.assert_allclose((m[:, None] * vp).sum(0), 0.0, atol=1e-12)
+    np.testing.assert_allclose((m[:, None] * np.cross(c, vp)).sum(0), 0.0, atol=1e-11)
+    lin = np.array([[0.0, 0.0, 0.0], [0.0, 0.0, 1.16], [0.0, 0.0, -1.16]])
+    ml = np.array([12.011, 15.9994, 15.9994])
+    assert rotation_translation_vectors(lin, ml).shape == (5, 3, 3)
+    np.testing.assert_allclose(rotation_translation_vectors(lin, ml), D.rotation_translation_vectors(lin, ml), atol=1e-12)
+    assert rotation_translation_vectors(np.zeros((1, 3)), [1.00794]).shape == (3, 1, 3)
 
 
 def test_oracle_velocity_assignment_hits_the_temperature():
