@@ -72,8 +72,9 @@ typedef struct {
                                    change falls below mixed_switch, then the FP64 eigensolve to convergence
                                    (N <= 144; larger systems use the FP64 step throughout). Not in the reference.
                                    3 and 6 (the mixed method) also turn on: perturbative density steps after the
-                                   first FP64 step, FP32 DIIS commutators, and FP32 sp-sp pair gradient terms
-                                   (assembled and summed in FP64) in pdg_energy_gradients / pdg_batch_*. */
+                                   first FP64 step (or from the start, around a shared base: pdg_set_shared_base),
+                                   FP32 DIIS commutators, and FP32 sp-sp pair gradient terms (assembled and summed
+                                   in FP64) in pdg_energy_gradients / pdg_batch_*. */
     double mixed_switch;        /* RMS density change that ends the purification cycles (e.g. 1e-4) */
 } pdg_scf_options;
 
@@ -138,6 +139,24 @@ int pdg_scf(pdg_system *sys, int n_frames, const double *d_phi, const pdg_scf_op
             int use_density, double *d_energies, double *d_charges, int *d_status, int *d_ncycles,
             void *d_workspace, size_t workspace_bytes, void *stream);
 
+/* Shared base of the mixed method's perturbative density steps (no counterpart in the reference; it stands where
+ * the reference would call the FP64 eigensolver, QCOnePDM_MakeFromFock, QCOnePDM.c:403, for every frame).
+ * Every FP64 density step of the mixed method leaves a base in its frame's workspace: the Fock matrix F0 and
+ * density P0 it was made from, its wanted eigenvectors and their complement (FP32) and the reciprocal eigenvalue
+ * gaps.  A perturbative step solves the block-diagonalisation (Riccati) equation for a nearby Fock matrix in the
+ * basis of those vectors, in FP32 products whose factors are small, and falls back to an FP64 step when |K|
+ * reaches 0.15 around a shared base (2e-3 around a frame's own).  pdg_base_capture copies frame `frame`'s base (pdg_base_bytes bytes, 16-byte aligned) out of the
+ * workspace of the last mixed-method call; pdg_set_shared_base(sys, d_base) makes later mixed-method calls on
+ * this system (pdg_energy_gradients, pdg_scf) start every frame from it: the start density is P0 (when
+ * use_density is 0) and every density step is a perturbative step around it (no purification, no FP64 step)
+ * until one fails, after which that frame takes FP64 steps and bases of its own.  The base must come from the
+ * same QC region (basis, electron count) and stay valid until the calls that use it have run; NULL detaches it.
+ * The converged results do not depend on the base: it changes the path, not the fixed point. */
+size_t pdg_base_bytes(pdg_system *sys);
+int pdg_base_capture(pdg_system *sys, int n_frames, int frame, const void *d_workspace, size_t workspace_bytes, void *d_base,
+                     void *stream);
+int pdg_set_shared_base(pdg_system *sys, const void *d_base);
+
 /* One density step for given Fock matrices d_fock (n_frames * N * N): d_density (in: the previous density,
  * out: the density of the n_occ lowest eigenvectors) by the FP64 eigensolve (density_step 0) or by split-BF16
  * purification (3 or 6 partial products; N <= 144).  d_energies[PDG_EN_RMS_DENSITY] gets the RMS change. */
@@ -185,7 +204,7 @@ int pdg_phase_times(const pdg_system *sys, float *h_ms);
  * timings of pMolecule.QCModel.pyx:208-275 (EnergyWithTimings: QC Fock, QC Converger Iterate,
  * QC Converger Densities), with the density step split into its parts.  d_out: n_frames * PDG_NTIMERS. */
 #define PDG_RMS_HISTORY 40
-#define PDG_NTIMERS (37 + PDG_RMS_HISTORY)
+#define PDG_NTIMERS (39 + PDG_RMS_HISTORY)
 enum {
     PDG_T_FOCK = 0, PDG_T_DIIS_SAVE = 1, PDG_T_ITERATE = 2, PDG_T_TRIDIAGONAL = 3, PDG_T_EIGENVALUES = 4,
     PDG_T_EIGENVECTORS = 5, PDG_T_BACKTRANSFORM = 6, PDG_T_DENSITY = 7, PDG_T_TOTAL = 8, PDG_T_CYCLES = 9,
@@ -217,8 +236,11 @@ enum {
     PDG_T_ITER_RCA = 35,       /* the ODA (RCA) step and the copies of P and F it keeps */
     PDG_T_DIIS_COMMUTATOR_FULL = 36, /* the part of PDG_T_DIIS_COMMUTATOR spent on full products F P (after a
                                   purification step, or from a caller's start density) */
-    PDG_T_RMS_HISTORY = 37     /* PDG_RMS_HISTORY entries: RMS density change of each density step, in SCF cycle
+    PDG_T_RMS_HISTORY = 37,    /* PDG_RMS_HISTORY entries: RMS density change of each density step, in SCF cycle
                                   order, negative for purification steps, 0 beyond the last */
+    PDG_T_PERT_KMAX = 37 + PDG_RMS_HISTORY,       /* largest max |K| of a perturbative step that was taken */
+    PDG_T_PERT_FAIL_K = 38 + PDG_RMS_HISTORY      /* max |K| of the last perturbative step that handed over (negative
+                                                     when its fixed-point sweeps had not settled), 0 if none */
 };
 int pdg_scf_timings(const pdg_system *sys, int n_frames, const void *d_workspace, size_t workspace_bytes,
                     double *d_out, void *stream);

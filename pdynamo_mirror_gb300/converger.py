@@ -6,10 +6,16 @@ The iteration itself runs on the device inside the SCF kernel (csrc/scf.cu).
 
 from . import _native
 
-# The mixed method as the benchmark runs it (the metric's "mixed"): split-BF16 purification with six partial
-# products until the RMS density change falls below 1e-5, then FP64 and perturbative density steps to the
-# reference's convergence test.  DIISSCFConverger(**MIXED_METHOD).
+# The mixed method (the metric's "mixed"): split-BF16 purification with six partial products until the RMS
+# density change falls below 1e-5, then FP64 and perturbative density steps to the reference's convergence test.
+# DIISSCFConverger(**MIXED_METHOD).
 MIXED_METHOD = {"densityStep": "purification", "purificationProducts": 6, "purificationSwitch": 1.0e-5}
+
+# The mixed method with a shared base, as the benchmark times it for batches of frames of one QC region: the first
+# batch runs MIXED_METHOD and leaves the base of one frame's FP64 step; every later batch starts each frame from
+# that base's density and takes perturbative density steps around it (no purification, no FP64 eigensolve) until
+# the reference's convergence test, falling back to FP64 steps for a frame the base no longer carries.
+SHARED_BASE_METHOD = dict(MIXED_METHOD, sharedBase=True)
 
 
 class DIISSCFConverger:
@@ -20,11 +26,14 @@ class DIISSCFConverger:
     (split-BF16 SP2 purification on the tensor cores until the RMS density change falls below
     purificationSwitch, then the FP64 eigensolve to convergence); purificationProducts 3 or 6 is the
     number of BF16 partial products accumulated in FP32.  The converged result is that of the FP64 step.
+    sharedBase (with "purification", one CTA per frame) keeps the base of the perturbative steps of one frame
+    of the first call and starts every frame of later calls from it (pdg_set_shared_base): the same fixed
+    point by a path of perturbative steps only.
     """
 
     _DEFAULTS = {"densityTolerance": 1.0e-8, "diisOnset": 0.2, "energyTolerance": 2.0e-4, "history": 10,
                  "maximumSCFCycles": 100, "useRCA": True, "densityStep": "fp64", "purificationSwitch": 1.0e-4,
-                 "purificationProducts": 3}
+                 "purificationProducts": 3, "sharedBase": False}
 
     def __init__(self, **options):
         for k, v in self._DEFAULTS.items():
@@ -43,6 +52,8 @@ class DIISSCFConverger:
             raise ValueError("densityStep must be 'fp64' or 'purification'.")
         if int(self.purificationProducts) not in (3, 6):
             raise ValueError("purificationProducts must be 3 or 6.")
+        if self.sharedBase and self.densityStep != "purification":
+            raise ValueError("sharedBase needs the mixed method (densityStep 'purification').")
 
     def options(self):
         step = 0 if self.densityStep == "fp64" else int(self.purificationProducts)

@@ -38,6 +38,8 @@ struct pdg_system {
     // after the SCF, after the gradients
     cudaEvent_t ev[4] = { nullptr, nullptr, nullptr, nullptr };
     int ev_on = 0, ev_recorded = 0;
+    // shared base of the mixed method's perturbative density steps (caller-owned device memory, pdg_set_shared_base)
+    const double *shared_base = nullptr;
 };
 
 extern "C" int pdg_version(void) { return 100; }
@@ -230,7 +232,8 @@ extern "C" int pdg_energy_gradients(pdg_system *s, int n_frames, const double *d
     mark(0);
     if ((rc = integrals(s, p, n_frames, d_xyz, w, st))) return rc;
     mark(1);
-    launch_scf(s->d, p, n_frames, d_phi, *o, d_density, use_density, d_energies, d_charges, d_status, d_ncycles, w, 0, nullptr, st);
+    launch_scf(s->d, p, n_frames, d_phi, *o, d_density, use_density, d_energies, d_charges, d_status, d_ncycles, w, 0, nullptr, st,
+               o->density_step != 0 ? s->shared_base : nullptr);
     if ((rc = cuda_check(cudaGetLastError(), "scf kernel"))) return rc;
     mark(2);
     if (d_gradients) {
@@ -323,8 +326,36 @@ extern "C" int pdg_scf(pdg_system *s, int n_frames, const double *d_phi, const p
     if (o->density_step != 0 && o->density_step != 3 && o->density_step != 6) return fail(PDG_BAD_ARGUMENT, "density_step must be 0, 3 or 6");
     FramePlan p = plan_for(s, PDG_MAX_HISTORY);
     launch_scf(s->d, p, n_frames, d_phi, *o, d_density, use_density, d_energies, d_charges, d_status, d_ncycles, (double *)ws, 0,
-               nullptr, (cudaStream_t)stream);
+               nullptr, (cudaStream_t)stream, o->density_step != 0 ? s->shared_base : nullptr);
     return cuda_check(cudaGetLastError(), "scf kernel");
+}
+
+// ---- shared base of the mixed method's perturbative density steps
+extern "C" size_t pdg_base_bytes(pdg_system *s)
+{
+    if (!s) return 0;
+    const FramePlan p = plan_for(s, PDG_MAX_HISTORY);
+    return (p.stride - p.BF) * sizeof(double);
+}
+
+extern "C" int pdg_base_capture(pdg_system *s, int n_frames, int frame, const void *ws, size_t bytes, void *d_base, void *stream)
+{
+    int rc = check_workspace(s, n_frames, const_cast<void *>(ws), bytes);
+    if (rc) return rc;
+    if (frame < 0 || frame >= n_frames || !d_base) return fail(PDG_BAD_ARGUMENT, "pdg_base_capture: bad argument");
+    if ((uintptr_t)d_base % 16) return fail(PDG_BAD_ARGUMENT, "pdg_base_capture: base not 16-byte aligned");
+    const FramePlan p = plan_for(s, PDG_MAX_HISTORY);
+    const double *src = (const double *)ws + (size_t)frame * p.stride + p.BF;
+    return cuda_check(cudaMemcpyAsync(d_base, src, (p.stride - p.BF) * sizeof(double), cudaMemcpyDeviceToDevice, (cudaStream_t)stream),
+                      "pdg_base_capture copy");
+}
+
+extern "C" int pdg_set_shared_base(pdg_system *s, const void *d_base)
+{
+    if (!s) return fail(PDG_BAD_ARGUMENT, "null system");
+    if ((uintptr_t)d_base % 16) return fail(PDG_BAD_ARGUMENT, "pdg_set_shared_base: base not 16-byte aligned");
+    s->shared_base = (const double *)d_base;
+    return PDG_OK;
 }
 
 extern "C" int pdg_one_electron(pdg_system *s, int n_frames, const double *d_xyz, double *d_h, void *ws, size_t bytes, void *stream)

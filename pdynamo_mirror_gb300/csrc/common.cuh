@@ -271,7 +271,7 @@ int launch_tc_selftest(int n, int kprod, int wait_limit, const float *x, float *
 #define PDG_SCF_LAUNCHERS                                                                                                   \
     void launch_scf(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *phi, const pdg_scf_options &o, \
                     double *density, int use_density, double *energies, double *charges, int *status, int *ncycles,      \
-                    double *ws, int fock_only, double *fock_out, cudaStream_t st);                                        \
+                    double *ws, int fock_only, double *fock_out, cudaStream_t st, const double *base = nullptr);          \
     int scf_occupancy(const DeviceSystem &s, int *threads, int *smem_bytes, int *ctas_per_sm);                           \
     void launch_batch_scf(const Batch &b, const int *order, int *queue, int grid, int smem_limit, size_t smem_bytes,     \
                           int tensor_items, const double *phi, const pdg_scf_options &o, double *density, int use_density, \

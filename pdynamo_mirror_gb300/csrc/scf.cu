@@ -32,6 +32,7 @@ struct SCFArgs {
     double *energies, *charges; int *status, *ncycles;
     double *ws; int fock_only; double *fock_out;
     int smem_limit;   // bytes of shared memory one CTA may plan for (the launch provides the plan's bytes)
+    const double *base;   // shared base of the perturbative density steps (the mixed method), or null
 };
 
 struct Smem {
@@ -872,6 +873,36 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
 }
 
 // ----------------------------------------------------------------------------------------------------
+// Base of the perturbative density steps: the block from FramePlan::BF to the end of a frame's workspace, either the
+// frame's own (left by its last FP64 step) or a shared copy of another frame's (pdg_base_capture), read-only here.
+struct PertBase { const double *BF, *BP; const float *Z32, *V32, *Gi; };
+
+__device__ __forceinline__ PertBase pert_base(const double *blk, const FramePlan &pl, int N, int kv)
+{
+    PertBase b;
+    b.BF = blk;
+    b.BP = blk + (pl.BP - pl.BF);
+    const float *bw = (const float *)(blk + (pl.BW - pl.BF));
+    b.Z32 = bw + pert_dq_offset(N, kv) + 2 * (size_t)N * N;
+    b.V32 = b.Z32 + (size_t)kv * N;
+    b.Gi = b.V32 + (size_t)(N - kv) * N;
+    return b;
+}
+
+// Largest |K| the perturbative step takes around a shared base.  It bounds the FP32 rounding carried into P (~1e-7
+// |K| per product, 1.5e-8 at 0.15) and the truncation of U = -A + A^2 - A^3 + A^4 - A^5 (|K|^12, 1.3e-10); frames
+// 0.03 A from the base geometry (RMS per coordinate) reach |K| ~ 0.1 with energies within 1e-7 Hartree of the FP64
+// method's.
+#ifndef PDG_PERT_KMAX_SHARED
+#define PDG_PERT_KMAX_SHARED 0.15f
+#endif
+// Around a frame's own base (made by its FP64 step from a Fock matrix of the same geometry) the steps stay small:
+// the limit keeps their rounding at ~2e-10, so that the mixed method reproduces the FP64 energies to 1e-8.
+#ifndef PDG_PERT_KMAX
+#define PDG_PERT_KMAX 2.0e-3f
+#endif
+
+// ----------------------------------------------------------------------------------------------------
 // Perturbative density step (mixed method; no counterpart in the reference).  The last FP64 step left a base:
 // its matrix F0, density P0, wanted eigenvectors Z0 (kv rows) with eigenvalues lambda, and the complementary
 // eigenvectors V (nc = N - kv rows) with eigenvalues mu, all exact to FP64 round-off.  For the new matrix
@@ -879,18 +910,19 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
 // Riccati equation of block diagonalisation in the basis [Z0; V]:
 //     E + M' K - K L' - K (E^T K) = (lambda_a - mu_i) K_ia,   E = V dF Z0^T,  M' = V dF V^T,  L' = Z0 dF Z0^T,
 // solved by fixed-point iteration from K = E / (lambda_a - mu_i) (first-order perturbation theory).  The new
-// projector differs from Z0^T Z0 by dQ = Z0^T W + Y^T (Z0 + W), with Y = K^T V, U = -K^T K ((1 + K^T K)^-1 to
-// second order) and W = Y + U (Z0 + Y); P = P0 + 2 dQ (occupied vectors) or P0 - 2 dQ (virtual).  Every FP32
+// projector differs from Z0^T Z0 by dQ = Z0^T W + Y^T (Z0 + W), with Y = K^T V, U = (1 + A)^-1 - 1 = -A + A^2 - A^3
+// (A = K^T K) and W = Y + U (Z0 + Y); P = P0 + 2 dQ (occupied vectors) or P0 - 2 dQ (virtual).  Every FP32
 // product here has a small factor (dF, K, Y, W), so its rounding error is ~1e-7 of a small quantity; only P0
 // (FP64) carries the full magnitude.  Returns the RMS change of P, or -1 without touching P when the base no
 // longer carries the step (the iteration does not settle, or K is not small): the caller then runs an FP64 step,
 // which makes a new base.
-__device__ double density_step_pert(const SCFArgs &a, double *wsf, const double *F, double *P, Smem &sm, Timer &tm)
+__device__ double density_step_pert(const SCFArgs &a, double *wsf, const double *F, double *P, Smem &sm, Timer &tm, const PertBase &pb,
+                                   bool warm_k, float kmax_limit)
 {
     const DeviceSystem &s = a.s;
     const FramePlan &pl = a.plan;
-    const int N = s.n_basis, kv = s.n_vec, nc = N - kv, ldz = sm.ldz, tid = threadIdx.x;
-    const double *BF = wsf + pl.BF, *BP = wsf + pl.BP, *BZ = wsf + pl.BZ, *BL = wsf + pl.BL;
+    const int N = s.n_basis, kv = s.n_vec, nc = N - kv, tid = threadIdx.x;
+    const double *BF = pb.BF, *BP = pb.BP;
     float *D = (float *)(wsf + pl.BW), *T1 = D + (size_t)N * N, *E = T1 + (size_t)N * kv, *Lp = E + (size_t)nc * kv;
     float *T2 = Lp + (size_t)kv * kv, *Mp = T2 + (size_t)N * nc, *K = Mp + (size_t)nc * nc, *K2 = K + (size_t)nc * kv;
     float *EK = K2 + (size_t)nc * kv, *U = EK + (size_t)kv * kv, *Y = U + (size_t)kv * kv, *Wz = Y + (size_t)kv * N;
@@ -899,36 +931,40 @@ __device__ double density_step_pert(const SCFArgs &a, double *wsf, const double 
     const long long t_coupling = tm.now();
     for (size_t k = tid; k < (size_t)N * N; k += PDG_BLOCK) D[k] = (float)(F[k] - BF[k]);
     __syncthreads();
-    const float *Z32 = DQ + 2 * (size_t)N * N, *V32 = Z32 + (size_t)kv * N, *Gi = V32 + (size_t)nc * N;
+    const float *Z32 = pb.Z32, *V32 = pb.V32, *Gi = pb.Gi;
     auto Zf = [&](int t, int i) { return Z32[(size_t)t * N + i]; };
     auto Vf = [&](int j, int i) { return V32[(size_t)j * N + i]; };
     // T1 = dF Z0^T (N x kv);  E = V T1 (nc x kv);  L' = Z0 T1 (kv x kv)
     tgemm32<true, true>(N, kv, N, [&](int i, int k) { return D[(size_t)i * N + k]; }, [&](int k, int t) { return Zf(t, k); }, false, sm,
-                      [&](int i, int t, double v) { T1[(size_t)i * kv + t] = (float)v; });
+                       [&](int i, int t, double v) { T1[(size_t)i * kv + t] = (float)v; });
     tgemm32<true, false>(nc, kv, N, [&](int j, int k) { return Vf(j, k); }, [&](int k, int t) { return T1[(size_t)k * kv + t]; }, false, sm,
-                       [&](int j, int t, double v) { E[(size_t)j * kv + t] = (float)v; });
+                        [&](int j, int t, double v) { E[(size_t)j * kv + t] = (float)v; });
     tgemm32<true, false>(kv, kv, N, [&](int b, int k) { return Zf(b, k); }, [&](int k, int t) { return T1[(size_t)k * kv + t]; }, false, sm,
-                       [&](int b, int t, double v) { Lp[(size_t)b * kv + t] = (float)v; });
+                        [&](int b, int t, double v) { Lp[(size_t)b * kv + t] = (float)v; });
     // T2 = dF V^T (N x nc);  M' = V T2 (nc x nc)
     tgemm32<true, true>(N, nc, N, [&](int i, int k) { return D[(size_t)i * N + k]; }, [&](int k, int j) { return Vf(j, k); }, false, sm,
-                      [&](int i, int j, double v) { T2[(size_t)i * nc + j] = (float)v; });
+                       [&](int i, int j, double v) { T2[(size_t)i * nc + j] = (float)v; });
     tgemm32<true, false>(nc, nc, N, [&](int j, int k) { return Vf(j, k); }, [&](int k, int l) { return T2[(size_t)k * nc + l]; }, false, sm,
-                       [&](int j, int l, double v) { Mp[(size_t)j * nc + l] = (float)v; });
+                        [&](int j, int l, double v) { Mp[(size_t)j * nc + l] = (float)v; });
     tm.add(PDG_T_PERT_COUPLING, t_coupling);
     const long long t_solve = tm.now();
-    // K from first-order theory, then the fixed-point iteration (each sweep one GEMM over [M' | -K] [K ; L' + E^T K])
-    for (int e = tid; e < nc * kv; e += PDG_BLOCK) K[e] = E[e] * Gi[e];
-    __syncthreads();
+    // K from first-order theory, or the previous step's K around the same base (warm_k), then the fixed-point
+    // iteration (each sweep one GEMM over [M' | -K] [K ; L' + E^T K]); the last iterate goes back to the first buffer
+    float *const K0 = K;
+    if (!warm_k) {
+        for (int e = tid; e < nc * kv; e += PDG_BLOCK) K[e] = E[e] * Gi[e];
+        __syncthreads();
+    }
     bool settled = false;
     float kmax = 0.f;
     for (int it = 0; it < 12 && !settled; it++) {
         tgemm32<false, false>(kv, kv, nc, [&](int b, int j) { return E[(size_t)j * kv + b]; }, [&](int j, int t) { return K[(size_t)j * kv + t]; },
-                            false, sm, [&](int b, int t, double v) { EK[(size_t)b * kv + t] = (float)v; });
+                      false, sm, [&](int b, int t, double v) { EK[(size_t)b * kv + t] = (float)v; });
         float dmax = 0.f, km = 0.f;
         tgemm32<true, false>(nc, kv, nc + kv,
             [&](int j, int k) { return k < nc ? Mp[(size_t)j * nc + k] : -K[(size_t)j * kv + (k - nc)]; },
             [&](int k, int t) { return k < nc ? K[(size_t)k * kv + t] : Lp[(size_t)(k - nc) * kv + t] + EK[(size_t)(k - nc) * kv + t]; },
-            false, sm, [&](int j, int t, double v) {
+     false, sm, [&](int j, int t, double v) {
                 const size_t e = (size_t)j * kv + t;
                 const float kn = (E[e] + (float)v) * Gi[e];
                 K2[e] = kn;
@@ -941,27 +977,45 @@ __device__ double density_step_pert(const SCFArgs &a, double *wsf, const double 
         settled = dmax <= 1.0e-5f * km + 1.0e-30f;   // remaining error ~ (contraction) x this change
         if (tid == 0) tm.slot[PDG_T_PERT_SWEEPS] += 1.0;
     }
+    if (K != K0) {
+        for (int e = tid; e < nc * kv; e += PDG_BLOCK) K0[e] = K[e];
+        __syncthreads();
+        K2 = K;
+        K = K0;
+    }
     tm.add(PDG_T_PERT_SOLVE, t_solve);
     const long long t_density = tm.now();
-    // |K| bounds the FP32 rounding carried into P (~1e-7 |K| per product): 2e-3 keeps it far below the SCF's
-    // 1e-8 density tolerance
-    if (!settled || !(kmax < 2.0e-3f)) {
-        if (tid == 0) tm.slot[PDG_T_PERT_FALLBACKS] += 1.0;
+    if (!settled || !(kmax < kmax_limit)) {
+        if (tid == 0) { tm.slot[PDG_T_PERT_FALLBACKS] += 1.0; tm.slot[PDG_T_PERT_FAIL_K] = settled ? (double)kmax : -(double)kmax; }
         tm.lap(PDG_T_PERT);
         return -1.0;
     }
     // Y = K^T V (kv x N);  U = -K^T K (kv x kv)
-    tgemm32<false, false>(kv, N, nc, [&](int t, int j) { return K[(size_t)j * kv + t]; }, [&](int j, int i) { return Vf(j, i); }, false, sm,
-                        [&](int t, int i, double v) { Y[(size_t)t * N + i] = (float)v; });
-    // U = (1 + K^T K)^-1 - 1 = -A + A^2 + O(|K|^6), A = K^T K (kv x kv; EK holds A)
-    tgemm32<false, false>(kv, kv, nc, [&](int t, int j) { return K[(size_t)j * kv + t]; }, [&](int j, int b) { return K[(size_t)j * kv + b]; },
-                        false, sm, [&](int t, int b, double v) { EK[(size_t)t * kv + b] = (float)v; });
-    tgemm32<true, false>(kv, kv, kv, [&](int t, int j) { return EK[(size_t)t * kv + j]; }, [&](int j, int b) { return EK[(size_t)j * kv + b]; },
-                         false, sm, [&](int t, int b, double v) { U[(size_t)t * kv + b] = (float)(v - (double)EK[(size_t)t * kv + b]); });
+    tgemm32<false, false>(N, kv, nc, [&](int i, int j) { return Vf(j, i); }, [&](int j, int t) { return K[(size_t)j * kv + t]; }, false, sm,
+                         [&](int i, int t, double v) { Y[(size_t)t * N + i] = (float)v; });   // Y^T = V^T K
+    if (tid == 0) tm.slot[PDG_T_PERT_KMAX] = fmax(tm.slot[PDG_T_PERT_KMAX], (double)kmax);
+    // U = (1 + K^T K)^-1 - 1 = -A S4 + O(|K|^12), A = K^T K, by Horner: S1 = 1 - A, S(r+1) = 1 - A S(r) (kv x kv;
+    // EK holds A, Lp and U (free after the sweeps) take the S in turn, and Lp the result)
+    tgemm32<false, false>(kv, kv, nc, [&](int t, int j) { return K[(size_t)j * kv + t]; }, [&](int j, int c) { return K[(size_t)j * kv + c]; },
+                  false, sm, [&](int t, int c, double v) { EK[(size_t)t * kv + c] = (float)v; });
+    for (int e = tid; e < kv * kv; e += PDG_BLOCK) Lp[e] = (e / kv == e % kv ? 1.f : 0.f) - EK[e];
+    __syncthreads();
+    {
+        float *Sa = Lp, *Sb = U;
+        for (int r = 0; r < 3; r++) {
+            tgemm32<true, false>(kv, kv, kv, [&](int t, int j) { return EK[(size_t)t * kv + j]; }, [&](int j, int c) { return Sa[(size_t)j * kv + c]; },
+                           false, sm, [&](int t, int c, double v) { Sb[(size_t)t * kv + c] = (float)((t == c ? 1.0 : 0.0) - v); });
+            float *tmp = Sa; Sa = Sb; Sb = tmp;
+        }
+        // Sa = S4 (in U); the result into Lp
+        tgemm32<true, false>(kv, kv, kv, [&](int t, int j) { return EK[(size_t)t * kv + j]; }, [&](int j, int c) { return Sa[(size_t)j * kv + c]; },
+                       false, sm, [&](int t, int c, double v) { Sb[(size_t)t * kv + c] = (float)(-v); });
+        U = Sb;
+    }
     // W = Y + U (Z0 + Y)
-    tgemm32<true, false>(kv, N, 2 * kv, [&](int t, int k) { return U[(size_t)t * kv + (k < kv ? k : k - kv)]; },
-                       [&](int k, int i) { return k < kv ? Zf(k, i) : Y[(size_t)(k - kv) * N + i]; }, false, sm,
-                       [&](int t, int i, double v) { Wz[(size_t)t * N + i] = (float)((double)Y[(size_t)t * N + i] + v); });
+    tgemm32<false, true>(N, kv, 2 * kv, [&](int i, int k) { return k < kv ? Zf(k, i) : Y[(size_t)(k - kv) * N + i]; },
+                        [&](int k, int t) { return U[(size_t)t * kv + (k < kv ? k : k - kv)]; }, false, sm,
+                        [&](int i, int t, double v) { Wz[(size_t)t * N + i] = (float)((double)Y[(size_t)t * N + i] + v); });   // W^T
     // dQ = Z0^T W + Y^T (Z0 + W) (symmetric; lower triangle) and P = P0 +- 2 dQ
     const double c = s.vec_occupied ? 2.0 : -2.0;
     double rms = 0.0;
@@ -1326,6 +1380,24 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
     // comes round), kept so that the next DIIS save can form its commutator from the small difference F - F~
     double *Ft = wsf + pl.A;
     const bool delta_commutator = o.density_step != 0;
+    // A shared base (mixed method): every density step is a perturbative step around it, with no purification, until
+    // one fails (K not small); that frame then takes an FP64 step, which makes its own base.  Without a start
+    // density the SCF starts from the base's density P0 = 2 Z0^T Z0, which commutes with F0: F = F0 stands for the
+    // matrix it was made from, so the first DIIS save already takes the difference commutator.
+    bool use_shared = delta_commutator && a.base != nullptr;
+    bool warm_k = false;   // the perturbative step's K buffer holds the last solution around the current base
+    auto cur_base = [&]() { return pert_base(use_shared ? a.base : wsf + pl.BF, pl, N, s.n_vec); };
+    if (use_shared) {
+        mixed = false;
+        base_ok = true;
+        if (!a.use_density) {
+            const PertBase b0 = cur_base();
+            for (size_t k = tid; k < NN; k += PDG_BLOCK) { P[k] = b0.BP[k]; F[k] = b0.BF[k]; }
+            valid = true;
+            have_z = true;
+        }
+        __syncthreads();
+    }
     while (iteration < o.maximum_scf_cycles && !converged) {
         if (delta_commutator && (have_z || have_pert)) {
             for (size_t k = tid; k < NN; k += PDG_BLOCK) Ft[k] = F[k];
@@ -1382,15 +1454,15 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
                     // FP64 step of the mixed method keeps a base, so Z is the base's vectors, also held in FP32.
                     float *G32 = (float *)(wsf + pl.G);
                     float *DF = (float *)(wsf + pl.BW) + pert_dq_offset(N, kv) + (size_t)N * N;
-                    const float *Z32 = DF + (size_t)N * N;
+                    const float *Z32 = cur_base().Z32;
                     for (size_t k = tid; k < NN; k += PDG_BLOCK) DF[k] = (float)(F[k] - Ft[k]);
                     __syncthreads();
                     // S = Z0 (+ Y after a perturbative step), T = Z0 (+ W); both kv x N in FP32
                     const float *Yp = (const float *)(wsf + pl.BW) + pert_y_offset(N, kv), *Wp = Yp + (size_t)kv * N;
                     auto Sv = [&](int t, int k) { return have_pert ? Z32[(size_t)t * N + k] + Yp[(size_t)t * N + k] : Z32[(size_t)t * N + k]; };
                     auto Tv = [&](int t, int k) { return have_pert ? Z32[(size_t)t * N + k] + Wp[(size_t)t * N + k] : Z32[(size_t)t * N + k]; };
-                    tgemm32<true, false>(kv, N, N, Sv, [&](int k, int i) { return DF[(size_t)k * N + i]; },
-                                       false, sm, [&](int t, int i, double v) { G32[(size_t)t * N + i] = (float)v; });
+                    tgemm32<false, true>(N, kv, N, [&](int i, int k) { return DF[(size_t)k * N + i]; }, [&](int k, int t) { return Sv(t, k); },
+                                 false, sm, [&](int i, int t, double v) { G32[(size_t)t * N + i] = (float)v; });   // G^T = DF S^T
                     tgemm32<false, false>(N, N, 2 * kv,
                         [&](int i, int k) { return k < kv ? G32[(size_t)k * N + i] : Tv(k - kv, i); },
                         [&](int k, int j) { return k < kv ? Tv(k, j) : -G32[(size_t)(k - kv) * N + j]; },
@@ -1592,15 +1664,29 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
             if (rms < o.mixed_switch || n_mixed >= 20) mixed = false;
         } else {
             double r = -1.0;
-            if (base_ok) r = density_step_pert(a, wsf, F, P, sm, tm);
+            if (base_ok) r = density_step_pert(a, wsf, F, P, sm, tm, cur_base(), warm_k, use_shared ? PDG_PERT_KMAX_SHARED : PDG_PERT_KMAX);
+            warm_k = r >= 0.0;
             if (r >= 0.0) {
                 rms = r;
                 have_z = false; have_pert = true;
+            } else if (use_shared && ncyc == 1 && !a.use_density) {
+                // the shared base does not carry this frame from its first step: its density is no start either, so
+                // the frame starts again as a cold one (the diagonal guess, then the per-frame mixed path)
+                const double g = (double)s.n_electrons / (double)N;
+                for (size_t k = tid; k < NN; k += PDG_BLOCK) P[k] = ((k / N) == (k % N)) ? g : 0.0;
+                if (tid == 0) ctl[1] = 0;
+                valid = false; have_z = false; have_pert = false; base_ok = false; use_shared = false;
+                mixed = want_mixed; n_mixed = 0; last_mixed = false;
+                iteration = 0; qdiis = 0; qrca = o.use_rca ? 1 : 0;
+                eold = 0.0; deltaeold = 0.0; rms = 0.0;
+                __syncthreads();
+                continue;
             } else {
                 // FP64 step; in the mixed method it also keeps the base of the following perturbative steps
                 rms = density_step(a, wsf, F, P, sm, tm, delta_commutator);
                 have_z = true; have_pert = false;
                 base_ok = delta_commutator;
+                use_shared = false;
             }
             last_mixed = false;
         }
@@ -1727,13 +1813,14 @@ int scf_occupancy(const DeviceSystem &s, int *threads, int *smem_bytes, int *cta
 
 void launch_scf(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *phi, const pdg_scf_options &o,
                 double *density, int use_density, double *energies, double *charges, int *status, int *ncycles,
-                double *ws, int fock_only, double *fock_out, cudaStream_t st)
+                double *ws, int fock_only, double *fock_out, cudaStream_t st, const double *base)
 {
     SCFArgs a;
     a.s = s; a.plan = p; a.n_frames = n_frames; a.phi = phi; a.o = o; a.density = density; a.use_density = use_density;
     a.energies = energies; a.charges = charges; a.status = status; a.ncycles = ncycles; a.ws = ws;
     a.fock_only = fock_only; a.fock_out = fock_out;
     a.smem_limit = PDG_SMEM_LIMIT;
+    a.base = fock_only ? nullptr : base;
     size_t sm = scf_smem_bytes(s.n_basis, s.n_vec);
     static size_t configured = 0;
     if (sm > 48 * 1024 && sm > configured) {

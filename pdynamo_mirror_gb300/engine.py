@@ -63,6 +63,7 @@ class QCEngine:
             self._wide = w
         self.density = None          # device [F, N, N], kept between calls as the reference keeps its state
         self._knots = {}
+        self._base, self._base_on = None, False   # shared base of the mixed method's perturbative steps
 
     def __del__(self):
         try:
@@ -150,10 +151,14 @@ class QCEngine:
                     _native.ptr(charges[f]), _native.ptr(status[f:f + 1]), _native.ptr(ncycles[f:f + 1]), _native.ptr(ws), ws.numel(), sh),
                     "pdg_wide_energy_gradients")
         else:
+            shared = opts.density_step != 0 and bool(getattr(converger, "sharedBase", False))
+            self._attach_base(shared and self._base is not None)
             _native.check(self.L.pdg_energy_gradients(self.handle, F, _native.ptr(xyz_bohr), _native.ptr(phi), ctypes.byref(opts),
                                                       _native.ptr(self.density), use, _native.ptr(energies), _native.ptr(grad),
                                                       _native.ptr(charges), _native.ptr(status), _native.ptr(ncycles),
                                                       _native.ptr(ws), ws.numel(), sh), "pdg_energy_gradients")
+            if shared and self._base is None:
+                self.capture_base(F, 0)
         out.update(energies=energies, qc_gradients=grad, charges=charges, status=status, ncycles=ncycles, phi=phi)
         mark(2)
         if qcmm and gradients:
@@ -171,6 +176,25 @@ class QCEngine:
             out["events"] = ev
         return out
 
+    def _attach_base(self, on):
+        if on != self._base_on:
+            _native.check(self.L.pdg_set_shared_base(self.handle, _native.ptr(self._base) if on else None), "pdg_set_shared_base")
+            self._base_on = on
+
+    def capture_base(self, n_frames, frame=0):
+        """Keep frame `frame`'s perturbative base from the last mixed-method run of n_frames frames
+        (pdg_base_capture) as the shared base of later runs with a sharedBase converger."""
+        if self._base is None:
+            self._base = torch.empty(int(self.L.pdg_base_bytes(self.handle)), dtype=torch.uint8, device=self.device)
+        ws = self.workspace(n_frames)
+        _native.check(self.L.pdg_base_capture(self.handle, int(n_frames), int(frame), _native.ptr(ws), ws.numel(), _native.ptr(self._base),
+                                              _native.stream_handle(torch.cuda.current_stream(self.device))), "pdg_base_capture")
+
+    def reset_base(self):
+        """Forget the shared base: the next sharedBase run takes the full mixed path and captures a new one."""
+        self._attach_base(False)
+        self._base = None
+
     def scf(self, converger, phi=None, use_density=False):
         """pdg_scf: the SCF alone on the integrals of the last run (same frames); returns (energies, status,
         ncycles) device tensors and updates self.density."""
@@ -180,6 +204,7 @@ class QCEngine:
         status = torch.empty(F, dtype=torch.int32, device=self.device)
         ncycles = torch.empty(F, dtype=torch.int32, device=self.device)
         opts = converger.options()
+        self._attach_base(opts.density_step != 0 and bool(getattr(converger, "sharedBase", False)) and self._base is not None)
         _native.check(self.L.pdg_scf(self.handle, F, _native.ptr(phi), ctypes.byref(opts), _native.ptr(self.density), 1 if use_density else 0,
                                      _native.ptr(energies), None, _native.ptr(status), _native.ptr(ncycles), _native.ptr(ws), ws.numel(),
                                      _native.stream_handle(torch.cuda.current_stream(self.device))), "pdg_scf")

@@ -132,9 +132,11 @@ class LearnedDensityGuess:
         return hist
 
     def validate(self, qc_xyz, converger, mm_xyz=None, mm_charges=None, nbmodel=None):
-        """Held-out check, the converged SCF deciding: run the frames [F, n, 3] cold from the diagonal
-        guess and from this guess, compare the mean SCF cycles and the energies, and keep the guess enabled
-        only if it saved cycles (else the standard guess is the fallback).  Returns the figures as a dict."""
+        """Held-out check, the converged SCF deciding: run the frames [F, n, 3] cold from the standard start (the
+        diagonal guess, or the shared base's density with a sharedBase converger whose base exists; the
+        "diagonal_guess" figures then describe that start) and from this guess, compare the mean SCF cycles and the
+        energies, and keep the guess enabled only if it saved cycles (else the standard start is the fallback).
+        Returns the figures as a dict."""
         eng = self.eng
         self.enabled = True
         std = eng.run(qc_xyz, converger, mm_xyz, mm_charges, nbmodel, gradients=False, warm_start=False)
@@ -149,7 +151,9 @@ class LearnedDensityGuess:
         c_lrn = float(lrn["ncycles"].double().mean())
         ok = bool((std["status"] == 0).all()) and bool((lrn["status"] == 0).all())
         self.enabled = ok and c_lrn < c_std
-        self.validation = {"frames": int(qc_xyz.shape[0]), "rms_error_learned": err(P_g), "rms_error_diagonal": err(diag),
+        shared = bool(getattr(converger, "sharedBase", False)) and getattr(eng, "_base", None) is not None
+        self.validation = {"frames": int(qc_xyz.shape[0]), "standard_start": "shared base density" if shared else "diagonal guess",
+                           "rms_error_learned": err(P_g), "rms_error_diagonal": err(diag),
                            "mean_scf_cycles_diagonal_guess": c_std, "mean_scf_cycles_learned_guess": c_lrn,
                            "iterations_saved": c_std - c_lrn,
                            "max_abs_dE_hartree": float((lrn["energies"].sum(1) - e_std).abs().max()),

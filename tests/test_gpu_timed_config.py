@@ -71,3 +71,63 @@ def test_large_water_clusters_batch_match_oracle(method):
         e = E[k, 1] + E[k, 2] + E[k, 3]
         assert abs(e - (ref["eelectronic"] + ref["enuclear"] + ref["baseline"])) < E_TOL, k
         assert np.abs(G[b.atom_offsets[k]:b.atom_offsets[k + 1]] - ref["gradients"]).max() < G_TOL, k
+
+
+def test_shared_base_water_box_frames_match_oracle():
+    """The mixed method with a shared base, as timed: a first batch of frames (their own seed) leaves the base of
+    frame 0's FP64 step; the benchmark's frames then start from its density and converge by perturbative density
+    steps around it alone.  Every frame against the oracle at the gate; the per-frame SCF timers show that no frame
+    needed purification and (nearly) none an FP64 step."""
+    import torch
+    from pdynamo_mirror_gb300 import DIISSCFConverger, NBModelABFS, QCModelMNDO, System, workloads
+    from pdynamo_mirror_gb300.converger import SHARED_BASE_METHOD
+    Z, X, Q, sel, charge, frames = workloads.qcmm_water_box_frames(N_FRAMES)
+    s = System(Z, X, mmCharges=Q)
+    s.electronicState.charge = charge
+    s.DefineQCModel(QCModelMNDO("am1", converger=DIISSCFConverger(**SHARED_BASE_METHOD)), qcSelection=sel)
+    s.DefineNBModel(NBModelABFS(innerCutoff=8.0, outerCutoff=12.0))
+    first = workloads.perturbed_frames(X, N_FRAMES, sigma=0.02, seed=99)
+    s.EnergyBatch(first, doGradients=True, warmStart=False)
+    eng = s.engine()
+    assert eng._base is not None
+    E, G, terms = s.EnergyBatch(frames, doGradients=True, warmStart=False)
+    assert (terms["Status"] == 0).all()
+    T = eng.timings(N_FRAMES)
+    assert T["QC Densities Purification Steps"].max() == 0
+    assert T["QC Densities Perturbative Steps"].min() >= 3
+    assert T["QC Densities Steps"].mean() <= 0.25
+    nq = len(sel)
+    knots = O.abfs_knots(8.0, 12.0)
+    for f in range(N_FRAMES):
+        r, gq, gm = _oracle_qcmm(Z, Q, sel, charge, frames[f], knots)
+        assert abs(terms["Pure QC"][f] / KJ - (r["eelectronic"] + r["enuclear"] + r["baseline"])) < E_TOL, f
+        assert abs(terms["QC/MM Elect."][f] / KJ - r["eqcmm"]) < E_TOL, f
+        g = G[f] / (A2B * KJ)
+        assert np.abs(g[:nq] - (r["gradients"] + gq)).max() < G_TOL, f
+        assert np.abs(g[nq:] - gm).max() < G_TOL, f
+
+
+def test_shared_base_from_a_distant_geometry_falls_back_and_converges():
+    """A base from frames 0.08 A (RMS per coordinate) away cannot carry the first step for most frames (K is not
+    small): those frames start again cold (the diagonal guess and the per-frame mixed path: purification, an FP64 step, perturbative steps
+    around their own base) and still converge to the plain FP64 results."""
+    from pdynamo_mirror_gb300 import DIISSCFConverger, NBModelABFS, QCModelMNDO, System, workloads
+    from pdynamo_mirror_gb300.converger import SHARED_BASE_METHOD
+    Z, X, Q, sel, charge, frames = workloads.qcmm_water_box_frames(4)
+    res = {}
+    for method in ("shared", "fp64"):
+        s = System(Z, X, mmCharges=Q)
+        s.electronicState.charge = charge
+        s.DefineQCModel(QCModelMNDO("am1", converger=DIISSCFConverger(**(SHARED_BASE_METHOD if method == "shared" else {}))),
+                        qcSelection=sel)
+        s.DefineNBModel(NBModelABFS(innerCutoff=8.0, outerCutoff=12.0))
+        if method == "shared":
+            s.EnergyBatch(workloads.perturbed_frames(X, 4, sigma=0.08, seed=98), doGradients=True, warmStart=False)
+        res[method] = s.EnergyBatch(frames, doGradients=True, warmStart=False)
+        if method == "shared":
+            T = s.engine().timings(4)
+            assert (T["QC Densities Steps"] >= 1).any() and (T["QC Densities Purification Steps"] >= 1).any()
+    (Es, Gs, ts), (Ep, Gp, tp) = res["shared"], res["fp64"]
+    assert (ts["Status"] == 0).all()
+    assert np.abs(Es - Ep).max() / KJ < E_TOL
+    assert np.abs(Gs - Gp).max() / (A2B * KJ) < G_TOL
