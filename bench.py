@@ -753,24 +753,20 @@ def bench_water_box(args, world, rank):
     nq = len(sel)
 
     def train_guess(s, eng):
-        """The learned start density, trained on frames the SCF converges here (a seed apart from the timed
-        frames); returns the model and what it achieved on held-out frames."""
-        from pdynamo_mirror_gb300 import LearnedDensityGuess
+        """The learned start density (LinearResponseGuess), fitted to the densities the SCF converges here on 2048
+        frames of their own seed (the first of those batches also leaves the shared base); returns the model."""
+        from pdynamo_mirror_gb300 import LinearResponseGuess
         t0 = time.perf_counter()
         tr = workloads.perturbed_frames(X, 2048, sigma=0.02, seed=101 + rank)
         qc_t, mm_t, q_t, _ = s._device_inputs(tr)
-        phis, dens = [], []
+        g = LinearResponseGuess(eng)
         for s0 in range(0, len(tr), 256):
             r = eng.run(qc_t[s0:s0 + 256].contiguous(), s.qcModel.converger, mm_t[s0:s0 + 256].contiguous(), q_t, s.nbModel,
                         gradients=False, warm_start=False)
-            phis.append(r["phi"].clone()); dens.append(eng.density.clone())
-        phi, P = torch.cat(phis), torch.cat(dens)
-        g = LearnedDensityGuess(eng, seed=0)
-        hist = g.fit(qc_t, phi, P, epochs=40, batch=32, lr=1e-3, seed=0)
-        hist += g.fit(qc_t, phi, P, epochs=20, batch=32, lr=2e-4, seed=1)
+            g.fit(qc_t[s0:s0 + 256], r["phi"], eng.density)
+        del qc_t, mm_t
         torch.cuda.synchronize()
-        return g, {"training_frames": len(tr), "epochs": 60, "train_seconds": time.perf_counter() - t0,
-                   "loss_first_last": [hist[0], hist[-1]]}
+        return g, {"training_frames": len(tr), "train_seconds": time.perf_counter() - t0}
 
     def measure(method, timed_clocks):
         s = System(Z, X, mmCharges=Q)
@@ -950,8 +946,10 @@ def bench_water_box(args, world, rank):
                                                    "starts from the density of a base kept from an earlier batch (the first warm-up "
                                                    "step, frames no timed step evaluates) and converges by FP32 perturbative density "
                                                    "steps around it (Riccati solve for |K| < 3e-2; no purification, no FP64 "
-                                                   "eigensolve unless a frame falls back); a per-pair MLP start density is trained "
-                                                   "and kept only where held-out validation shows SCF cycles saved"}[args.method],
+                                                   "eigensolve unless a frame falls back); the start density of every frame is the "
+                                                   "learned linear response of the density to the QC coordinates and QC/MM "
+                                                   "potentials (LinearResponseGuess, fitted to 2048 converged frames of another "
+                                                   "seed), kept only where held-out validation shows SCF cycles saved"}[args.method],
                        "frame_sets": "a fresh seeded set of %d perturbed frames (sigma 0.02 A) per warm-up and timed step, the same "
                                      "sets for every method" % nF,
                        "perturbative_steps_per_frame": float(T["QC Densities Perturbative Steps"].mean()),

@@ -120,7 +120,10 @@ size_t pdg_workspace_bytes(const pdg_system *sys, int n_frames);
  *   d_phi        n_frames * n_atoms QC/MM potentials at the QC atoms, or NULL (no QC/MM)
  *   d_density    n_frames * N * N: in = start density when use_density != 0 (the reference keeps the
  *                previous density on the configuration, pMolecule.QCModel.pyx:153), else the diagonal
- *                guess (QCOnePDM.c:280); out = converged density
+ *                guess (QCOnePDM.c:280); out = converged density.  use_density 1: a density the converger
+ *                takes into its DIIS history at once (the previous converged one); 2: a start guess (a
+ *                predicted density, not idempotent), from which the first Fock matrix is built and which the
+ *                first density step replaces before DIIS starts, as the diagonal guess is
  *   d_energies   n_frames * PDG_NENERGY
  *   d_gradients  n_frames * n_atoms * 3 (Eh/Bohr) or NULL
  *   d_charges    n_frames * n_atoms Lowdin charges of the final density, or NULL

@@ -224,6 +224,7 @@ extern "C" int pdg_energy_gradients(pdg_system *s, int n_frames, const double *d
     if (o->history < 1 || o->history > PDG_MAX_HISTORY) return fail(PDG_BAD_ARGUMENT, "history must be 1..16");
     if (o->maximum_scf_cycles < 0) return fail(PDG_BAD_ARGUMENT, "maximum_scf_cycles must be >= 0");
     if (o->density_step != 0 && o->density_step != 3 && o->density_step != 6) return fail(PDG_BAD_ARGUMENT, "density_step must be 0, 3 or 6");
+    if (use_density < 0 || use_density > 2) return fail(PDG_BAD_ARGUMENT, "use_density must be 0, 1 or 2");
     cudaStream_t st = (cudaStream_t)stream;
     FramePlan p = plan_for(s, PDG_MAX_HISTORY);
     double *w = (double *)ws;
@@ -324,6 +325,7 @@ extern "C" int pdg_scf(pdg_system *s, int n_frames, const double *d_phi, const p
     if (o->history < 1 || o->history > PDG_MAX_HISTORY) return fail(PDG_BAD_ARGUMENT, "history must be 1..16");
     if (o->maximum_scf_cycles < 0) return fail(PDG_BAD_ARGUMENT, "maximum_scf_cycles must be >= 0");
     if (o->density_step != 0 && o->density_step != 3 && o->density_step != 6) return fail(PDG_BAD_ARGUMENT, "density_step must be 0, 3 or 6");
+    if (use_density < 0 || use_density > 2) return fail(PDG_BAD_ARGUMENT, "use_density must be 0, 1 or 2");
     FramePlan p = plan_for(s, PDG_MAX_HISTORY);
     launch_scf(s->d, p, n_frames, d_phi, *o, d_density, use_density, d_energies, d_charges, d_status, d_ncycles, (double *)ws, 0,
                nullptr, (cudaStream_t)stream, o->density_step != 0 ? s->shared_base : nullptr);

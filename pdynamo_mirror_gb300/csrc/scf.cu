@@ -257,15 +257,28 @@ __device__ void fock_build(const SCFArgs &a, int f, const double *H, const doubl
             const int A = s.cel[e] >> 4, ab = s.cel[e] & 15;
             const int no = s.atom_norb[A], as = s.atom_start[A], na = no * (no + 1) / 2;
             const int m = MP_DA[ab], n = MP_DB[ab];   // m >= n
-            double acc = 0.0;
-            for (int B = 0; B < s.n_atoms; B++) {
-                if (B == A) continue;
-                const int hi = A > B ? A : B, lo = A > B ? B : A, pp = hi * (hi - 1) / 2 + lo;
-                const int k0 = s.atom_pk[B], nb = s.atom_pk[B + 1] - k0;
-                const double *blk = tei + s.pair_tei[pp], *pb = pk + k0;
-                if (A > B) for (int cd = 0; cd < nb; cd++) acc = fma(blk[ab * nb + cd], pb[cd], acc);
-                else       for (int cd = 0; cd < nb; cd++) acc = fma(blk[cd * na + ab], pb[cd], acc);
+            // the partners in two interleaved halves with their own accumulators, so that the loads of one
+            // partner's block overlap those of the other (summed in a fixed order)
+            double acc = 0.0, acc2 = 0.0;
+            const int half = (s.n_atoms + 1) >> 1;
+            for (int B0 = 0; B0 < half; B0++) {
+                const int B1 = B0 + half;
+                if (B0 != A) {
+                    const int hi = A > B0 ? A : B0, lo = A > B0 ? B0 : A, pp = hi * (hi - 1) / 2 + lo;
+                    const int k0 = s.atom_pk[B0], nb = s.atom_pk[B0 + 1] - k0;
+                    const double *blk = tei + s.pair_tei[pp], *pb = pk + k0;
+                    if (A > B0) for (int cd = 0; cd < nb; cd++) acc = fma(blk[ab * nb + cd], pb[cd], acc);
+                    else        for (int cd = 0; cd < nb; cd++) acc = fma(blk[cd * na + ab], pb[cd], acc);
+                }
+                if (B1 < s.n_atoms && B1 != A) {
+                    const int hi = A > B1 ? A : B1, lo = A > B1 ? B1 : A, pp = hi * (hi - 1) / 2 + lo;
+                    const int k0 = s.atom_pk[B1], nb = s.atom_pk[B1 + 1] - k0;
+                    const double *blk = tei + s.pair_tei[pp], *pb = pk + k0;
+                    if (A > B1) for (int cd = 0; cd < nb; cd++) acc2 = fma(blk[ab * nb + cd], pb[cd], acc2);
+                    else        for (int cd = 0; cd < nb; cd++) acc2 = fma(blk[cd * na + ab], pb[cd], acc2);
+                }
             }
+            acc += acc2;
             const double *E = elem(s, s.atom_elem[A]);
             const double gss = E[PDG_E_GSS], gsp = E[PDG_E_GSP], gpp = E[PDG_E_GPP], gp2 = E[PDG_E_GP2], hsp = E[PDG_E_HSP], hpp = E[PDG_E_HPP];
             const double *PA = P + (size_t)as * N + as;
@@ -1337,7 +1350,7 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
 #endif
     bool mixed = want_mixed, last_mixed = false;
     int n_mixed = 0;
-    bool valid = a.use_density != 0;
+    bool valid = a.use_density == 1;   // 2: a start guess, which the first density step replaces before DIIS sees it
     if (!valid) {   // uniform diagonal guess (QCOnePDM.c:326-331)
         double g = (double)s.n_electrons / (double)N;
         for (size_t k = tid; k < NN; k += PDG_BLOCK) P[k] = ((k / N) == (k % N)) ? g : 0.0;
@@ -1385,12 +1398,24 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
     // density the SCF starts from the base's density P0 = 2 Z0^T Z0, which commutes with F0: F = F0 stands for the
     // matrix it was made from, so the first DIIS save already takes the difference commutator.
     bool use_shared = delta_commutator && a.base != nullptr;
+    // The mixed method forms the first DIIS error of a caller's start density (a learned guess, a previous step's
+    // density) in FP32 as well, from an FP32 copy of P: no FP64 N^3 product for a vector that only steers DIIS
+    bool fp32_start = delta_commutator && a.use_density == 1;
+    if (fp32_start) {
+        const int N4 = (N + 3) & ~3;
+        float *P32 = (float *)(wsf + pl.A) + 2 * ((NN + 3) & ~size_t(3));
+        for (int e = tid; e < N * N4; e += PDG_BLOCK) {
+            const int i = e / N4, j = e % N4;
+            P32[e] = j < N ? (float)P[(size_t)i * N + j] : 0.0f;
+        }
+        __syncthreads();
+    }
     bool warm_k = false;   // the perturbative step's K buffer holds the last solution around the current base
     auto cur_base = [&]() { return pert_base(use_shared ? a.base : wsf + pl.BF, pl, N, s.n_vec); };
     if (use_shared) {
         mixed = false;
         base_ok = true;
-        if (!a.use_density) {
+        if (a.use_density == 0) {
             const PertBase b0 = cur_base();
             for (size_t k = tid; k < NN; k += PDG_BLOCK) { P[k] = b0.BP[k]; F[k] = b0.BF[k]; }
             valid = true;
@@ -1481,7 +1506,7 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
                 // errors anyway)
                 double *FP = wsf + pl.A;
                 const long long t_pur = tm.now();
-                if (last_mixed) {
+                if (last_mixed || fp32_start) {
                     // FP32 outer products over k: thread block (i0..i0+3, j0..j0+3) += F[k][i0..] (x) P[k][j0..]
                     // (F symmetric), operands read as float4 rows with no shared-memory staging or barriers
                     const int N4 = (N + 3) & ~3;
@@ -1650,6 +1675,7 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
             }
             tm.add(PDG_T_ITER_RCA, t_sub);
             iteration++;
+            fp32_start = false;
         }
         deltaeold = deltae; eold = etemp;
         __syncthreads();
@@ -1669,7 +1695,7 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
             if (r >= 0.0) {
                 rms = r;
                 have_z = false; have_pert = true;
-            } else if (use_shared && ncyc == 1 && !a.use_density) {
+            } else if (use_shared && ncyc == 1 && a.use_density != 1) {
                 // the shared base does not carry this frame from its first step: its density is no start either, so
                 // the frame starts again as a cold one (the diagonal guess, then the per-frame mixed path)
                 const double g = (double)s.n_electrons / (double)N;

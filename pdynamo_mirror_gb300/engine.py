@@ -133,7 +133,7 @@ class QCEngine:
         use = 1 if (warm_start and self.density is not None and self.density.shape[0] == F) else 0
         if not use and guess is not None and guess.enabled:
             self.density = guess.predict(qc_xyz, phi)
-            use = 1
+            use = getattr(guess, "start_mode", 1)
         if not use:
             self.density = torch.empty((F, N, N), dtype=torch.float64, device=dev)
         energies = torch.empty((F, _native.NENERGY), dtype=torch.float64, device=dev)

@@ -169,3 +169,99 @@ class LearnedDensityGuess:
             p["wm"].copy_(torch.as_tensor(d["w%d" % i]))
             p["bm"].copy_(torch.as_tensor(d["b%d" % i]))
             p["w"].copy_(p["wm"].to(torch.bfloat16))
+
+
+class LinearResponseGuess:
+    """Start density from a linear model of the converged density in the geometry and the environment (not in the
+    reference): P(x, phi) ~ P_mean + (f - f_mean) J over the packed lower triangle of P, with features f = the QC
+    atoms' Cartesian coordinates (A) and the QC/MM potentials at them (a.u.), J by ridge regression on standardised
+    features over densities the SCF itself converged.  It learns the density's linear response to the displacements
+    and to the MM field around the frames it was trained on (MD or sampled frames of one QC region in a fixed
+    frame of reference).  The sums of the normal equations stay on the device in FP64, so that training can go on
+    batch by batch; prediction is one FP32 GEMM (features x J) and the unpacking.  The prediction enters the SCF as
+    a start density (use_density 1), DIIS history included.  validate() keeps it on only where it saves SCF cycles."""
+
+    start_mode = 1
+
+    def __init__(self, engine, ridge=1.0):
+        self.eng = engine
+        self.ridge = float(ridge)
+        dev = engine.device
+        N = engine.n_basis
+        self.N = N
+        il = torch.tril_indices(N, N, device=dev)
+        self._lower, self._upper = il[0] * N + il[1], il[1] * N + il[0]
+        nf = 4 * engine.n_atoms
+        self.nf, self.npk = nf, il.shape[1]
+        self.n = 0
+        self._sf = torch.zeros(nf, dtype=torch.float64, device=dev)
+        self._sp = torch.zeros(self.npk, dtype=torch.float64, device=dev)
+        self._sff = torch.zeros((nf, nf), dtype=torch.float64, device=dev)
+        self._sfp = torch.zeros((nf, self.npk), dtype=torch.float64, device=dev)
+        self.J = self.f_mean = self.p_mean = None
+        self.enabled = False
+        self.validation = None
+
+    def _features(self, qc_xyz, phi):
+        F = qc_xyz.shape[0]
+        x = qc_xyz.reshape(F, -1).to(torch.float64)
+        p = phi.to(torch.float64) if phi is not None else torch.zeros((F, self.eng.n_atoms), dtype=torch.float64, device=x.device)
+        return torch.cat([x, p], 1)
+
+    def fit(self, qc_xyz, phi, P):
+        """Add frames (qc_xyz [F, n, 3] A, phi [F, n] or None, converged densities P [F, N, N]) to the normal
+        equations and solve them; the model is then enabled until validate() says otherwise."""
+        f = self._features(qc_xyz, phi)
+        p = P.reshape(P.shape[0], -1)[:, self._lower].to(torch.float64)
+        self.n += f.shape[0]
+        self._sf += f.sum(0)
+        self._sp += p.sum(0)
+        self._sff += f.T @ f
+        self._sfp += f.T @ p
+        n = float(self.n)
+        fm, pm = self._sf / n, self._sp / n
+        C = self._sff / n - torch.outer(fm, fm)
+        S = self._sfp / n - torch.outer(fm, pm)
+        sd = torch.sqrt(torch.clamp(torch.diagonal(C), min=1e-30))
+        Cs = C / torch.outer(sd, sd) + (self.ridge / n) * torch.eye(self.nf, dtype=torch.float64, device=C.device)
+        Js = torch.linalg.solve(Cs, S / sd[:, None])
+        self.J = (Js / sd[:, None]).to(torch.float32).contiguous()
+        self.f_mean, self.p_mean = fm, pm
+        self.enabled = True
+        return self
+
+    def predict(self, qc_xyz, phi=None):
+        """Start densities [F, N, N] (FP64) for frames qc_xyz [F, n, 3] (A) with potentials phi [F, n]."""
+        F = qc_xyz.shape[0]
+        d = (self._features(qc_xyz, phi) - self.f_mean).to(torch.float32)
+        pk = torch.mm(d, self.J).to(torch.float64) + self.p_mean
+        P = torch.empty((F, self.N * self.N), dtype=torch.float64, device=pk.device)
+        P[:, self._lower] = pk
+        P[:, self._upper] = pk
+        return P.view(F, self.N, self.N)
+
+    def validate(self, qc_xyz, converger, mm_xyz=None, mm_charges=None, nbmodel=None):
+        """Held-out check, the converged SCF deciding: the frames from the standard start (the diagonal guess, or
+        the shared base's density with a sharedBase converger whose base exists) and from this guess; the guess
+        stays enabled only if it saves SCF cycles.  Returns the figures as a dict."""
+        eng = self.eng
+        self.enabled = True
+        std = eng.run(qc_xyz, converger, mm_xyz, mm_charges, nbmodel, gradients=False, warm_start=False)
+        e_std, c_std = std["energies"].sum(1).clone(), float(std["ncycles"].double().mean())
+        P_std, phi = eng.density.clone(), std["phi"]
+        N = eng.n_basis
+        P_g = self.predict(qc_xyz, phi)
+        err = lambda A: float(((A - P_std) ** 2).sum(dim=(1, 2)).sqrt().mean()) / N
+        lrn = eng.run(qc_xyz, converger, mm_xyz, mm_charges, nbmodel, gradients=False, warm_start=False, guess=self)
+        c_lrn = float(lrn["ncycles"].double().mean())
+        ok = bool((std["status"] == 0).all()) and bool((lrn["status"] == 0).all())
+        self.enabled = ok and c_lrn < c_std
+        shared = bool(getattr(converger, "sharedBase", False)) and getattr(eng, "_base", None) is not None
+        self.validation = {"model": "linear response (ridge regression on QC coordinates and QC/MM potentials)",
+                           "training_frames": self.n, "frames": int(qc_xyz.shape[0]),
+                           "standard_start": "shared base density" if shared else "diagonal guess",
+                           "rms_error_learned": err(P_g), "mean_scf_cycles_standard_start": c_std,
+                           "mean_scf_cycles_learned_guess": c_lrn, "iterations_saved": c_std - c_lrn,
+                           "max_abs_dE_hartree": float((lrn["energies"].sum(1) - e_std).abs().max()),
+                           "enabled": self.enabled}
+        return self.validation
