@@ -846,7 +846,7 @@ def bench_water_box(args, world, rank):
             if k >= 2:
                 te.append(time.perf_counter() - t0)
         qc, mm = dev_sets[0]
-        return dict(ms=ms, clk=clk, phase_ms=phase_ms, e2e_s=sum(te) / len(te), E=E, G=G,
+        return dict(ms=ms, clk=clk, phase_ms=phase_ms, e2e_s=sum(te) / len(te), e2e_ms_each=[1e3 * t for t in te], E=E, G=G,
                     ncyc=r["ncycles"].cpu().numpy(), timers=timers, eng=eng, conv=conv, frames_h=sets_h[0], qc=qc, mm=mm)
 
     plain = measure("fp64", args.method == "fp64")
@@ -957,7 +957,7 @@ def bench_water_box(args, world, rank):
                        "purification_steps_per_frame": pur_steps, "fp64_density_steps_per_frame": fp64_steps,
                        "scf_cta": scf_cta_layout(eng, T),
                        "l2": "working set > L2 (no flush needed)"},
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(head["frames_h"].numel() * 8),
+            "e2e": {"value": e2e, "unit": UNIT, "ms_each": head["e2e_ms_each"], "h2d_bytes_per_step": int(head["frames_h"].numel() * 8),
                     "d2h_bytes_per_step": int(head["G"].nbytes + nF * (_native.NENERGY + 2 + nq) * 8)},
             # per step: k_qcmm_potentials; k_pair_integrals, _ss, _sps, k_assemble_h; k_scf; k_pair_gradients, _ss, _sps,
             # k_reduce_gradients; k_qcmm_grad_qc, k_qcmm_grad_mm (or their FP32-pair forms)

@@ -155,6 +155,12 @@ int pdg_scf(pdg_system *sys, int n_frames, const double *d_phi, const pdg_scf_op
  * until one fails, after which that frame takes FP64 steps and bases of its own.  The base must come from the
  * same QC region (basis, electron count) and stay valid until the calls that use it have run; NULL detaches it.
  * The converged results do not depend on the base: it changes the path, not the fixed point. */
+/* A side stream for pdg_energy_gradients (NULL detaches it): work the caller queued on it before the call (the
+ * QC/MM potentials) overlaps the integrals and the SCF waits for it; work queued on it after the call (the QC/MM
+ * gradients) waits for the SCF and overlaps the pair gradients.  The caller makes its main stream wait for the
+ * side stream before using those results.  System.Energy's order (QC/MM potentials, integrals, SCF, gradients,
+ * QC/MM gradients; pMolecule/System.py:309-312) is kept for every data dependence. */
+int pdg_set_side_stream(pdg_system *sys, void *side_stream);
 size_t pdg_base_bytes(pdg_system *sys);
 int pdg_base_capture(pdg_system *sys, int n_frames, int frame, const void *d_workspace, size_t workspace_bytes, void *d_base,
                      void *stream);

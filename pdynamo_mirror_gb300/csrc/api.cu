@@ -40,6 +40,9 @@ struct pdg_system {
     int ev_on = 0, ev_recorded = 0;
     // shared base of the mixed method's perturbative density steps (caller-owned device memory, pdg_set_shared_base)
     const double *shared_base = nullptr;
+    // side stream of pdg_set_side_stream and the two events that order it against the SCF
+    cudaStream_t side = nullptr;
+    cudaEvent_t side_in = nullptr, scf_out = nullptr;
 };
 
 extern "C" int pdg_version(void) { return 100; }
@@ -177,6 +180,8 @@ extern "C" int pdg_system_destroy(pdg_system *s)
     cudaFree(s->d_ovl32); cudaFree(s->d_mpw32);
     for (cudaEvent_t e : s->ev)
         if (e) cudaEventDestroy(e);
+    if (s->side_in) cudaEventDestroy(s->side_in);
+    if (s->scf_out) cudaEventDestroy(s->scf_out);
     delete s;
     return PDG_OK;
 }
@@ -231,11 +236,19 @@ extern "C" int pdg_energy_gradients(pdg_system *s, int n_frames, const double *d
     auto mark = [&](int k) { if (s->ev_on) cudaEventRecord(s->ev[k], st); };
     s->ev_recorded = 0;
     mark(0);
+    // with a side stream: what it holds so far (the QC/MM potentials) runs beside the integrals, the SCF waits for
+    // it, and what the caller queues on it next (the QC/MM gradients) waits for the SCF
+    if (s->side && (rc = cuda_check(cudaEventRecord(s->side_in, s->side), "side stream event"))) return rc;
     if ((rc = integrals(s, p, n_frames, d_xyz, w, st))) return rc;
     mark(1);
+    if (s->side && (rc = cuda_check(cudaStreamWaitEvent(st, s->side_in, 0), "side stream wait"))) return rc;
     launch_scf(s->d, p, n_frames, d_phi, *o, d_density, use_density, d_energies, d_charges, d_status, d_ncycles, w, 0, nullptr, st,
                o->density_step != 0 ? s->shared_base : nullptr);
     if ((rc = cuda_check(cudaGetLastError(), "scf kernel"))) return rc;
+    if (s->side) {
+        if ((rc = cuda_check(cudaEventRecord(s->scf_out, st), "side stream event"))) return rc;
+        if ((rc = cuda_check(cudaStreamWaitEvent(s->side, s->scf_out, 0), "side stream wait"))) return rc;
+    }
     mark(2);
     if (d_gradients) {
         // the mixed method takes the sp-sp pair gradient terms in FP32 (assembled and summed in FP64)
@@ -350,6 +363,18 @@ extern "C" int pdg_base_capture(pdg_system *s, int n_frames, int frame, const vo
     const double *src = (const double *)ws + (size_t)frame * p.stride + p.BF;
     return cuda_check(cudaMemcpyAsync(d_base, src, (p.stride - p.BF) * sizeof(double), cudaMemcpyDeviceToDevice, (cudaStream_t)stream),
                       "pdg_base_capture copy");
+}
+
+extern "C" int pdg_set_side_stream(pdg_system *s, void *side_stream)
+{
+    if (!s) return fail(PDG_BAD_ARGUMENT, "null system");
+    if (side_stream && !s->side_in) {
+        if (cudaEventCreateWithFlags(&s->side_in, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->scf_out, cudaEventDisableTiming) != cudaSuccess)
+            return cuda_check(cudaGetLastError(), "side stream events");
+    }
+    s->side = (cudaStream_t)side_stream;
+    return PDG_OK;
 }
 
 extern "C" int pdg_set_shared_base(pdg_system *s, const void *d_base)

@@ -8,7 +8,7 @@ CUDA stream:
 (pMolecule/System.py:309-312).  Torch supplies device memory and the stream only.
 """
 
-import ctypes
+import contextlib, ctypes
 
 import numpy as np
 import torch
@@ -119,20 +119,34 @@ class QCEngine:
                 ev[k].record(stream)
         phi = None
         qcmm = nbmodel is not None and mm_xyz is not None and mm_xyz.shape[1] > 0
+        # the QC/MM kernels on a side stream, beside the integrals and the pair gradients (pdg_set_side_stream),
+        # except when phase events are wanted (their intervals assume one stream) and on the wide path
+        side = self._side_stream() if (qcmm and not events and not self.wide) else None
+        qsh = sh
+        if side is not None:
+            side.wait_stream(stream)
+            qsh = _native.stream_handle(side)
+
+        def on_side():
+            # tensors the side stream writes come from its own pool
+            return torch.cuda.stream(side) if side is not None else contextlib.nullcontext()
         mark(0)
         if qcmm:
             knots = self.knots(nbmodel) if nbmodel.model_id == 1 else None
             nk = 0 if knots is None else knots.numel() // 3
-            phi = torch.empty((F, n), dtype=torch.float64, device=dev)
+            with on_side():
+                phi = torch.empty((F, n), dtype=torch.float64, device=dev)
             qws, qwb = self.qcmm_workspace(F, mm_xyz.shape[1])
             _native.check(self.L.pdg_qcmm_potentials(nbmodel.model_id, F, n, mm_xyz.shape[1], _native.ptr(qc_xyz), _native.ptr(mm_xyz),
                                                      _native.ptr(mm_charges), nk, _native.ptr(knots), float(nbmodel.outerCutoff),
-                                                     _native.ptr(phi), _native.ptr(qws), qwb, sh), "pdg_qcmm_potentials")
+                                                     _native.ptr(phi), _native.ptr(qws), qwb, qsh), "pdg_qcmm_potentials")
         mark(1)
         xyz_bohr = (qc_xyz * ANGSTROMS_TO_BOHRS).contiguous()
         use = 1 if (warm_start and self.density is not None and self.density.shape[0] == F) else 0
         if not use and guess is not None and guess.enabled:
-            self.density = guess.predict(qc_xyz, phi)
+            # the prediction reads the QC/MM potentials: on the side stream too, before the SCF's wait
+            with on_side():
+                self.density = guess.predict(qc_xyz, phi)
             use = getattr(guess, "start_mode", 1)
         if not use:
             self.density = torch.empty((F, N, N), dtype=torch.float64, device=dev)
@@ -153,6 +167,7 @@ class QCEngine:
         else:
             shared = opts.density_step != 0 and bool(getattr(converger, "sharedBase", False))
             self._attach_base(shared and self._base is not None)
+            self._attach_side(side)
             _native.check(self.L.pdg_energy_gradients(self.handle, F, _native.ptr(xyz_bohr), _native.ptr(phi), ctypes.byref(opts),
                                                       _native.ptr(self.density), use, _native.ptr(energies), _native.ptr(grad),
                                                       _native.ptr(charges), _native.ptr(status), _native.ptr(ncycles),
@@ -162,19 +177,33 @@ class QCEngine:
         out.update(energies=energies, qc_gradients=grad, charges=charges, status=status, ncycles=ncycles, phi=phi)
         mark(2)
         if qcmm and gradients:
-            gqc = torch.empty((F, n, 3), dtype=torch.float64, device=dev)
-            gmm = torch.empty((F, mm_xyz.shape[1], 3), dtype=torch.float64, device=dev) if mm_gradients else None
+            with on_side():
+                gqc = torch.empty((F, n, 3), dtype=torch.float64, device=dev)
+                gmm = torch.empty((F, mm_xyz.shape[1], 3), dtype=torch.float64, device=dev) if mm_gradients else None
             # the mixed method takes the QC/MM gradient pair terms in FP32 (per-atom sums in FP64); plain FP64 keeps FP64
             gmodel = nbmodel.model_id | (_native.QCMM_FP32_PAIRS if opts.density_step != 0 else 0)
             _native.check(self.L.pdg_qcmm_gradients(gmodel, F, n, mm_xyz.shape[1], _native.ptr(qc_xyz), _native.ptr(mm_xyz),
                                                     _native.ptr(mm_charges), _native.ptr(charges), nk, _native.ptr(knots),
-                                                    float(nbmodel.outerCutoff), _native.ptr(gqc), _native.ptr(gmm), _native.ptr(qws), qwb, sh),
+                                                    float(nbmodel.outerCutoff), _native.ptr(gqc), _native.ptr(gmm), _native.ptr(qws), qwb, qsh),
                           "pdg_qcmm_gradients")
             out.update(qcmm_qc_gradients=gqc, qcmm_mm_gradients=gmm)
+        if side is not None:
+            stream.wait_stream(side)
         mark(3)
         if ev:
             out["events"] = ev
         return out
+
+    def _side_stream(self):
+        if getattr(self, "_side", None) is None:
+            self._side = torch.cuda.Stream(device=self.device)
+        return self._side
+
+    def _attach_side(self, side):
+        h = None if side is None else side.cuda_stream
+        if h != getattr(self, "_side_on", None):
+            _native.check(self.L.pdg_set_side_stream(self.handle, None if h is None else ctypes.c_void_p(h)), "pdg_set_side_stream")
+            self._side_on = h
 
     def _attach_base(self, on):
         if on != self._base_on:
