@@ -650,6 +650,9 @@ def main():
                     help="the QC/MM water box (the headline metric), 512 independent PM3 water clusters in one launch, or "
                          "Langevin dynamics of water-box replicas with the learned start density trained on trajectories")
     ap.add_argument("--no-large", action="store_true", help="leave out the large QC/MM sub-line of the default workload")
+    ap.add_argument("--profile-region", action="store_true",
+                    help="bracket the reported method's timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off) "
+                         "and time only that method")
     ap.add_argument("--large-steps", type=int, default=10, help="timed MD steps per method of the large QC/MM sub-line")
     ap.add_argument("--md-equilibration", type=int, default=150)
     ap.add_argument("--md-training-steps", type=int, default=66, help="training densities = replicas x this")
@@ -807,11 +810,16 @@ def bench_water_box(args, world, rank):
         if clocks:
             clocks.start()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        profiled = args.profile_region and timed_clocks
+        if profiled:
+            torch.cuda.profiler.start()
         e0.record(stream)
         for k in range(args.steps):
             r = step(args.warmup + k)
         e1.record(stream)
         torch.cuda.synchronize()
+        if profiled:
+            torch.cuda.profiler.stop()
         if world > 1:
             torch.distributed.barrier()
         ms = e0.elapsed_time(e1) / args.steps
@@ -849,6 +857,12 @@ def bench_water_box(args, world, rank):
         return dict(ms=ms, clk=clk, phase_ms=phase_ms, e2e_s=sum(te) / len(te), e2e_ms_each=[1e3 * t for t in te], E=E, G=G,
                     ncyc=r["ncycles"].cpu().numpy(), timers=timers, eng=eng, conv=conv, frames_h=sets_h[0], qc=qc, mm=mm)
 
+    if args.profile_region:
+        # only the reported method, its timed steps inside the profiler range
+        h = measure(args.method, True)
+        if rank == 0:
+            print(json.dumps({"profile_region": args.method, "frames": len(frames), "steps": args.steps, "ms_per_step": h["ms"]}))
+        return
     plain = measure("fp64", args.method == "fp64")
     mixed = None if args.method == "fp64" else (measure("mixed", args.method == "mixed"))
     head = plain if args.method == "fp64" else (mixed if args.method == "mixed" else measure(args.method, True))

@@ -257,28 +257,15 @@ __device__ void fock_build(const SCFArgs &a, int f, const double *H, const doubl
             const int A = s.cel[e] >> 4, ab = s.cel[e] & 15;
             const int no = s.atom_norb[A], as = s.atom_start[A], na = no * (no + 1) / 2;
             const int m = MP_DA[ab], n = MP_DB[ab];   // m >= n
-            // the partners in two interleaved halves with their own accumulators, so that the loads of one
-            // partner's block overlap those of the other (summed in a fixed order)
-            double acc = 0.0, acc2 = 0.0;
-            const int half = (s.n_atoms + 1) >> 1;
-            for (int B0 = 0; B0 < half; B0++) {
-                const int B1 = B0 + half;
-                if (B0 != A) {
-                    const int hi = A > B0 ? A : B0, lo = A > B0 ? B0 : A, pp = hi * (hi - 1) / 2 + lo;
-                    const int k0 = s.atom_pk[B0], nb = s.atom_pk[B0 + 1] - k0;
-                    const double *blk = tei + s.pair_tei[pp], *pb = pk + k0;
-                    if (A > B0) for (int cd = 0; cd < nb; cd++) acc = fma(blk[ab * nb + cd], pb[cd], acc);
-                    else        for (int cd = 0; cd < nb; cd++) acc = fma(blk[cd * na + ab], pb[cd], acc);
-                }
-                if (B1 < s.n_atoms && B1 != A) {
-                    const int hi = A > B1 ? A : B1, lo = A > B1 ? B1 : A, pp = hi * (hi - 1) / 2 + lo;
-                    const int k0 = s.atom_pk[B1], nb = s.atom_pk[B1 + 1] - k0;
-                    const double *blk = tei + s.pair_tei[pp], *pb = pk + k0;
-                    if (A > B1) for (int cd = 0; cd < nb; cd++) acc2 = fma(blk[ab * nb + cd], pb[cd], acc2);
-                    else        for (int cd = 0; cd < nb; cd++) acc2 = fma(blk[cd * na + ab], pb[cd], acc2);
-                }
+            double acc = 0.0;
+            for (int B = 0; B < s.n_atoms; B++) {
+                if (B == A) continue;
+                const int hi = A > B ? A : B, lo = A > B ? B : A, pp = hi * (hi - 1) / 2 + lo;
+                const int k0 = s.atom_pk[B], nb = s.atom_pk[B + 1] - k0;
+                const double *blk = tei + s.pair_tei[pp], *pb = pk + k0;
+                if (A > B) for (int cd = 0; cd < nb; cd++) acc = fma(blk[ab * nb + cd], pb[cd], acc);
+                else       for (int cd = 0; cd < nb; cd++) acc = fma(blk[cd * na + ab], pb[cd], acc);
             }
-            acc += acc2;
             const double *E = elem(s, s.atom_elem[A]);
             const double gss = E[PDG_E_GSS], gsp = E[PDG_E_GSP], gpp = E[PDG_E_GPP], gp2 = E[PDG_E_GP2], hsp = E[PDG_E_HSP], hpp = E[PDG_E_HPP];
             const double *PA = P + (size_t)as * N + as;
@@ -1384,6 +1371,7 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
     double *cf = sm.small + 32;   // DIIS coefficients
     if (tid == 0) { ctl[1] = 0; for (int i = 0; i < hist; i++) ctl[2 + i] = i; }
     int iteration = 0, converged = 0, qdiis = 0, qrca = o.use_rca ? 1 : 0, st = PDG_NOT_CONVERGED;
+    bool rca_prev = false;   // rP, rF hold the last cycle's P, F (RCA_Save)
     double eold = 0.0, deltaeold = 0.0, rms = 0.0, eel = 0.0;
     __syncthreads();
     int ncyc = 0;
@@ -1639,7 +1627,7 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
                     }
                     tm.add(PDG_T_ITER_EXTRAPOLATE, t_sub);
                     t_sub = tm.now();
-                } else if (o.use_rca && qrca) {
+                } else if (o.use_rca && qrca && rca_prev) {
                     // RCA_Iterate: cubic in mu from four traces (DIISSCFConverger.c:661-760)
                     const double *rP = wsf + pl.rP, *rF = wsf + pl.rF;
                     double t1 = 0, t2 = 0, t3 = 0, t4 = 0;
@@ -1668,10 +1656,15 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
                     __syncthreads();
                 }
             }
-            if (o.use_rca) {
+            // RCA_Save (DIISSCFConverger.c:231-235) every cycle in ODA mode; in DIIS mode the copies would only serve a
+            // switch back to ODA (an error above 0.8 while extrapolating), which then skips one ODA interpolation
+            // instead and saves from there
+            rca_prev = false;
+            if (o.use_rca && !qdiis) {
                 double *rP = wsf + pl.rP, *rF = wsf + pl.rF;
                 for (size_t k = tid; k < NN; k += PDG_BLOCK) { rP[k] = P[k]; rF[k] = F[k]; }
                 __syncthreads();
+                rca_prev = true;
             }
             tm.add(PDG_T_ITER_RCA, t_sub);
             iteration++;
