@@ -769,6 +769,7 @@ def bench_water_box(args, world, rank):
             g.fit(qc_t[s0:s0 + 256], r["phi"], eng.density)
         del qc_t, mm_t
         torch.cuda.synchronize()
+        torch.cuda.empty_cache()
         return g, {"training_frames": len(tr), "train_seconds": time.perf_counter() - t0}
 
     def measure(method, timed_clocks):

@@ -30,7 +30,8 @@ struct pdg_system {
     std::vector<double> elements;
     int charge;
     // device allocations owned by the system (tables only; no per-frame data)
-    double *d_elements = nullptr, *d_terms = nullptr, *d_ovl = nullptr;
+    double *d_elements = nullptr, *d_terms = nullptr, *d_ovl = nullptr, *d_ovl_tab = nullptr;
+    int *d_ovl_tab_idx = nullptr;   // per ordered element pair: table offset, then node count
     float *d_ovl32 = nullptr, *d_mpw32 = nullptr;
     int *d_ints = nullptr;
     void *d_mp = nullptr;
@@ -97,6 +98,13 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
             ovl_n[a * n_elements + b] = (int)(ovl.size() / OV_REC - before);
         }
     if (ovl.empty()) ovl.assign(OV_REC, 0.0);
+    // the same sums tabulated against R (the mixed method's integrals)
+    std::vector<double> ovl_tab;
+    std::vector<int> ovl_tab_idx(2 * n_elements * n_elements);
+    for (int e = 0; e < n_elements * n_elements; e++) {
+        ovl_tab_idx[e] = (int)ovl_tab.size();
+        ovl_tab_idx[n_elements * n_elements + e] = overlap_table(ovl.data() + (size_t)ovl_off[e] * OV_REC, ovl_n[e], ovl_tab);
+    }
     pdg_system *s = new pdg_system();
     s->elements.assign(h_elements, h_elements + (size_t)n_elements * PDG_ELEMENT_STRIDE);
     s->charge = charge;
@@ -149,7 +157,12 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
         (rc = cuda_check(cudaMemcpy(s->d_mpw32, mpw32.data(), sizeof(float) * mpw32.size(), cudaMemcpyHostToDevice), "copy FP32 multipole weights")) ||
         (rc = cuda_check(cudaMemcpy(s->d_elements, s->elements.data(), sizeof(double) * s->elements.size(), cudaMemcpyHostToDevice), "copy elements")) ||
         (rc = cuda_check(cudaMemcpy(s->d_terms, terms.data(), sizeof(double) * terms.size(), cudaMemcpyHostToDevice), "copy terms")) ||
-        (rc = cuda_check(cudaMemcpy(s->d_ints, ints.data(), sizeof(int) * ints.size(), cudaMemcpyHostToDevice), "copy tables"))) {
+        (rc = cuda_check(cudaMemcpy(s->d_ints, ints.data(), sizeof(int) * ints.size(), cudaMemcpyHostToDevice), "copy tables")) ||
+        (rc = cuda_check(cudaMalloc(&s->d_ovl_tab, sizeof(double) * ovl_tab.size()), "cudaMalloc overlap table")) ||
+        (rc = cuda_check(cudaMemcpy(s->d_ovl_tab, ovl_tab.data(), sizeof(double) * ovl_tab.size(), cudaMemcpyHostToDevice), "copy overlap table")) ||
+        (rc = cuda_check(cudaMalloc(&s->d_ovl_tab_idx, sizeof(int) * ovl_tab_idx.size()), "cudaMalloc overlap table index")) ||
+        (rc = cuda_check(cudaMemcpy(s->d_ovl_tab_idx, ovl_tab_idx.data(), sizeof(int) * ovl_tab_idx.size(), cudaMemcpyHostToDevice),
+                         "copy overlap table index"))) {
         pdg_system_destroy(s);
         return rc;
     }
@@ -169,6 +182,9 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     d.mp_map = s->d_mp;
     d.atom_pk = b + pk_at;
     d.ovl32 = s->d_ovl32; d.mp_w32 = s->d_mpw32;
+    d.ovl_tab = nullptr;   // attached per call for the mixed method (mixed_view)
+    d.ovl_tab_off = s->d_ovl_tab_idx; d.ovl_tab_n = s->d_ovl_tab_idx + n_elements * n_elements;
+    d.ovl_tab_inv_h = 1.0 / OV_TAB_H;
     *out = s;
     return PDG_OK;
 }
@@ -177,7 +193,7 @@ extern "C" int pdg_system_destroy(pdg_system *s)
 {
     if (!s) return PDG_OK;
     cudaFree(s->d_elements); cudaFree(s->d_terms); cudaFree(s->d_ints); cudaFree(s->d_ovl); cudaFree(s->d_mp);
-    cudaFree(s->d_ovl32); cudaFree(s->d_mpw32);
+    cudaFree(s->d_ovl32); cudaFree(s->d_mpw32); cudaFree(s->d_ovl_tab); cudaFree(s->d_ovl_tab_idx);
     for (cudaEvent_t e : s->ev)
         if (e) cudaEventDestroy(e);
     if (s->side_in) cudaEventDestroy(s->side_in);
@@ -211,11 +227,19 @@ static int check_workspace(const pdg_system *s, int n_frames, void *ws, size_t b
     return PDG_OK;
 }
 
-static int integrals(pdg_system *s, const FramePlan &p, int n_frames, const double *xyz, double *ws, cudaStream_t st)
+static int integrals(const DeviceSystem &d, const FramePlan &p, int n_frames, const double *xyz, double *ws, cudaStream_t st)
 {
-    launch_pair_integrals(s->d, p, n_frames, xyz, ws, st);
-    launch_assemble_h(s->d, p, n_frames, ws, st);
+    launch_pair_integrals(d, p, n_frames, xyz, ws, st);
+    launch_assemble_h(d, p, n_frames, ws, st);
     return cuda_check(cudaGetLastError(), "integral kernels");
+}
+
+// The system as the mixed method's kernels see it: with the tabulated overlap sums attached.
+static DeviceSystem mixed_view(const pdg_system *s, bool mixed)
+{
+    DeviceSystem d = s->d;
+    if (mixed) d.ovl_tab = s->d_ovl_tab;
+    return d;
 }
 
 extern "C" int pdg_energy_gradients(pdg_system *s, int n_frames, const double *d_xyz, const double *d_phi,
@@ -239,7 +263,7 @@ extern "C" int pdg_energy_gradients(pdg_system *s, int n_frames, const double *d
     // with a side stream: what it holds so far (the QC/MM potentials) runs beside the integrals, the SCF waits for
     // it, and what the caller queues on it next (the QC/MM gradients) waits for the SCF
     if (s->side && (rc = cuda_check(cudaEventRecord(s->side_in, s->side), "side stream event"))) return rc;
-    if ((rc = integrals(s, p, n_frames, d_xyz, w, st))) return rc;
+    if ((rc = integrals(mixed_view(s, o->density_step != 0), p, n_frames, d_xyz, w, st))) return rc;
     mark(1);
     if (s->side && (rc = cuda_check(cudaStreamWaitEvent(st, s->side_in, 0), "side stream wait"))) return rc;
     launch_scf(s->d, p, n_frames, d_phi, *o, d_density, use_density, d_energies, d_charges, d_status, d_ncycles, w, 0, nullptr, st,
@@ -252,7 +276,7 @@ extern "C" int pdg_energy_gradients(pdg_system *s, int n_frames, const double *d
     mark(2);
     if (d_gradients) {
         // the mixed method takes the sp-sp pair gradient terms in FP32 (assembled and summed in FP64)
-        launch_pair_gradients(s->d, p, n_frames, d_xyz, d_density, w, st, o->density_step != 0);
+        launch_pair_gradients(mixed_view(s, o->density_step != 0), p, n_frames, d_xyz, d_density, w, st, o->density_step != 0);
         launch_reduce_gradients(s->d, p, n_frames, w, d_gradients, st);
         if ((rc = cuda_check(cudaGetLastError(), "gradient kernels"))) return rc;
     }
@@ -392,7 +416,7 @@ extern "C" int pdg_one_electron(pdg_system *s, int n_frames, const double *d_xyz
     cudaStream_t st = (cudaStream_t)stream;
     FramePlan p = plan_for(s, PDG_MAX_HISTORY);
     double *w = (double *)ws;
-    if ((rc = integrals(s, p, n_frames, d_xyz, w, st))) return rc;
+    if ((rc = integrals(s->d, p, n_frames, d_xyz, w, st))) return rc;
     size_t NN = (size_t)s->d.n_basis * s->d.n_basis;
     for (int f = 0; f < n_frames; f++)
         if ((rc = cuda_check(cudaMemcpyAsync(d_h + f * NN, w + f * p.stride + p.H, sizeof(double) * NN, cudaMemcpyDeviceToDevice, st), "copy H"))) return rc;
@@ -407,7 +431,7 @@ extern "C" int pdg_fock(pdg_system *s, int n_frames, const double *d_xyz, const 
     cudaStream_t st = (cudaStream_t)stream;
     FramePlan p = plan_for(s, PDG_MAX_HISTORY);
     double *w = (double *)ws;
-    if ((rc = integrals(s, p, n_frames, d_xyz, w, st))) return rc;
+    if ((rc = integrals(s->d, p, n_frames, d_xyz, w, st))) return rc;
     pdg_scf_options o = { 1e-8, 2e-4, 0.2, 0, 10, 1, 0, 1e-4 };
     launch_scf(s->d, p, n_frames, d_phi, o, const_cast<double *>(d_density), 1, d_energies, nullptr, nullptr, nullptr, w, 1, d_fock, st);
     return cuda_check(cudaGetLastError(), "fock kernel");

@@ -41,6 +41,11 @@ struct DeviceSystem {
     const int *atom_pk;                // n_atoms + 1: first entry of each atom's one-centre block in the cel order
     const float *ovl32;                // the overlap primitive records rounded to FP32 (the mixed method's gradients)
     const float *mp_w32;               // the multipole map's weights rounded to FP32 (same layout as MultipoleMap::w)
+    // The overlap radial sums tabulated against R (overlap.cuh, overlap_table), for the mixed method only: null in
+    // every call of the FP64 method, which sums the primitives
+    const double *ovl_tab;
+    const int *ovl_tab_off, *ovl_tab_n;   // per ordered element pair: first double, node count
+    double ovl_tab_inv_h;
 };
 
 // Per-frame workspace plan (all offsets in doubles from the frame's base).

@@ -178,7 +178,8 @@ k_pair_integrals(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, con
         // resonance integrals H_ab = S_ab (beta_a + beta_b) / 2 (QCModelMNDO.c:1075-1092)
         const int eo = eli * s.n_elements + elj;
         double Fo[5], Do[5];
-        overlap_sums(s.ovl + (size_t)s.ovl_off[eo] * OV_REC, s.ovl_n[eo], x * x + y * y + z * z, false, overlap_used(noi, noj), Fo, Do);
+        if (s.ovl_tab) overlap_sums_table(s, eo, sqrt(x * x + y * y + z * z), Fo, nullptr);
+        else overlap_sums(s.ovl + (size_t)s.ovl_off[eo] * OV_REC, s.ovl_n[eo], x * x + y * y + z * z, false, overlap_used(noi, noj), Fo, Do);
         const int is = s.atom_start[i], js = s.atom_start[j];
         if (lane < noi * noj) {
             const int a = lane / noj, b = lane % noj;
@@ -222,11 +223,17 @@ __global__ void __launch_bounds__(256) k_pair_integrals_ss(DeviceSystem sys0, Fr
     pe[10] = -Ei[PDG_E_ZCORE] * cj;
     pe[20] = core_core(Ei, Ej, r, nullptr);
     const int eo = eli * s.n_elements + elj;
-    const double *rec = s.ovl + (size_t)s.ovl_off[eo] * OV_REC;
     double S = 0.0;
-    for (int t = 0; t < s.ovl_n[eo]; t++) {
-        const double fac = rec[OV_REC * t] * R2;
-        if (fac <= PRIMITIVE_OVERLAP_TOLERANCE) S = fma(rec[OV_REC * t + 1], exp(-fac), S);
+    if (s.ovl_tab) {
+        double Fo[5];
+        overlap_sums_table(s, eo, r, Fo, nullptr);
+        S = Fo[0];
+    } else {
+        const double *rec = s.ovl + (size_t)s.ovl_off[eo] * OV_REC;
+        for (int t = 0; t < s.ovl_n[eo]; t++) {
+            const double fac = rec[OV_REC * t] * R2;
+            if (fac <= PRIMITIVE_OVERLAP_TOLERANCE) S = fma(rec[OV_REC * t + 1], exp(-fac), S);
+        }
     }
     const int N = s.n_basis, is = s.atom_start[i], js = s.atom_start[j];
     const double v = S * 0.5 * (Ei[PDG_E_BETA] + Ej[PDG_E_BETA]);
@@ -342,7 +349,8 @@ __global__ void __launch_bounds__(128) k_pair_integrals_sps(DeviceSystem sys0, F
     // resonance integrals H_ab = S_ab (beta_a + beta_b) / 2
     const int eo = eli * s.n_elements + elj;
     double Fo[5], Do[5];
-    overlap_sums_thread(s.ovl + (size_t)s.ovl_off[eo] * OV_REC, s.ovl_n[eo], R2, false, Fo, Do);
+    if (s.ovl_tab) overlap_sums_table(s, eo, r, Fo, nullptr);
+    else overlap_sums_thread(s.ovl + (size_t)s.ovl_off[eo] * OV_REC, s.ovl_n[eo], R2, false, Fo, Do);
     const double AB[3] = { x, y, z };
     const int N = s.n_basis, is = s.atom_start[i], js = s.atom_start[j];
     double *H = wsf + plan.H;
@@ -631,11 +639,17 @@ __global__ void __launch_bounds__(256) k_pair_gradients_ss(DeviceSystem sys0, Fr
         }
     }
     const int eo = eli * s.n_elements + elj;
-    const double *rec = s.ovl + (size_t)s.ovl_off[eo] * OV_REC;
     double D = 0.0;
-    for (int t = 0; t < s.ovl_n[eo]; t++) {
-        const double abg = rec[OV_REC * t], fac = abg * R2;
-        if (fac <= PRIMITIVE_OVERLAP_TOLERANCE) D = fma((abg + abg) * rec[OV_REC * t + 1], exp(-fac), D);
+    if (s.ovl_tab) {
+        double Fo[5], Do[5];
+        overlap_sums_table(s, eo, r, Fo, Do);
+        D = Do[0];
+    } else {
+        const double *rec = s.ovl + (size_t)s.ovl_off[eo] * OV_REC;
+        for (int t = 0; t < s.ovl_n[eo]; t++) {
+            const double abg = rec[OV_REC * t], fac = abg * R2;
+            if (fac <= PRIMITIVE_OVERLAP_TOLERANCE) D = fma((abg + abg) * rec[OV_REC * t + 1], exp(-fac), D);
+        }
     }
     const double w = (Ei[PDG_E_BETA] + Ej[PDG_E_BETA]) * pij;
     double *pg = ws + fv.ws + plan.pair_g + (size_t)p * 3;

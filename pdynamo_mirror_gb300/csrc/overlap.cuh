@@ -9,6 +9,7 @@
 // tabulated per ordered element pair on the host; on the device one exp per primitive pair remains.
 // Primitive pairs with (ab/g)|AB|^2 above 18 ln 10 are skipped, as the reference does (GaussianBasis.h:43).
 #pragma once
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -121,4 +122,63 @@ __device__ __forceinline__ void overlap_gradient(const Real *W, int noi, int noj
         radial += -q * D[3] + tr * D[4];
     }
     for (int k = 0; k < 3; k++) g[k] = AB[k] * radial - wps[k] * F[1] + wsp[k] * F[2] + (u[k] + v[k]) * F[3];
+}
+
+// ---- Tabulated radial sums (the mixed method).  The five sums F_k(R) = sum_t w_kt exp(-(ab/g)_t R^2) of an ordered
+// element pair are smooth in R, so they are tabulated once per system at nodes R_n = n h (h = 0.005 Bohr, out to the
+// distance at which every primitive pair falls below the tolerance) with their exact derivatives, and evaluated by
+// cubic Hermite interpolation: error <= h^4 max|F''''| / 384 (~1e-11 of the sums at bonding distances; the derivative
+// ~1e-8), against 36-144 FP64 exponentials per pair.  Node layout: F_0..F_4, dF_0/dR..dF_4/dR (10 doubles).
+#define OV_TAB_H 0.005
+#define OV_TAB_NODE 10
+
+// Host: append the table of records rec[0 .. nrec) (OV_REC each); returns the node count.
+inline int overlap_table(const double *rec, int nrec, std::vector<double> &out)
+{
+    double abg_min = 1e300;
+    for (int t = 0; t < nrec; t++) abg_min = std::min(abg_min, rec[OV_REC * t]);
+    if (nrec == 0) abg_min = 1.0;
+    const double rmax = std::sqrt(PRIMITIVE_OVERLAP_TOLERANCE / abg_min);
+    const int n = (int)std::ceil(rmax / OV_TAB_H) + 2;
+    for (int i = 0; i < n; i++) {
+        const double R = i * OV_TAB_H, R2 = R * R;
+        double F[5] = { 0, 0, 0, 0, 0 }, G[5] = { 0, 0, 0, 0, 0 };
+        for (int t = 0; t < nrec; t++) {
+            const double *q = rec + OV_REC * t;
+            const double fac = q[0] * R2;
+            if (fac > PRIMITIVE_OVERLAP_TOLERANCE) continue;
+            const double e = std::exp(-fac), d = -2.0 * q[0] * R * e;
+            const int ty = (int)q[3];
+            F[ty] += q[1] * e;  G[ty] += q[1] * d;
+            F[4] += q[2] * e;   G[4] += q[2] * d;
+        }
+        for (int k = 0; k < 5; k++) out.push_back(F[k]);
+        for (int k = 0; k < 5; k++) out.push_back(G[k]);
+    }
+    return n;
+}
+
+// Device: F[0..4] and D[0..4] (D_k = sum 2 (ab/g) w e = -(dF_k/dR) / R; D may be null) of ordered element pair eo at
+// distance R from the table; zero beyond it.
+__device__ __forceinline__ void overlap_sums_table(const DeviceSystem &s, int eo, double R, double *F, double *D)
+{
+    const double u = R * s.ovl_tab_inv_h;
+    const int i = (int)u, n = s.ovl_tab_n[eo];
+    if (i >= n - 1) {
+        for (int k = 0; k < 5; k++) { F[k] = 0.0; if (D) D[k] = 0.0; }
+        return;
+    }
+    const double t = u - (double)i, t2 = t * t, t3 = t2 * t;
+    const double h00 = 2.0 * t3 - 3.0 * t2 + 1.0, h10 = (t3 - 2.0 * t2 + t) * OV_TAB_H;
+    const double h01 = 3.0 * t2 - 2.0 * t3, h11 = (t3 - t2) * OV_TAB_H;
+    const double *a = s.ovl_tab + s.ovl_tab_off[eo] + (size_t)OV_TAB_NODE * i, *b = a + OV_TAB_NODE;
+#pragma unroll
+    for (int k = 0; k < 5; k++) F[k] = h00 * a[k] + h10 * a[5 + k] + h01 * b[k] + h11 * b[5 + k];
+    if (D) {
+        const double g00 = (6.0 * t2 - 6.0 * t) * s.ovl_tab_inv_h, g10 = 3.0 * t2 - 4.0 * t + 1.0;
+        const double g01 = (6.0 * t - 6.0 * t2) * s.ovl_tab_inv_h, g11 = 3.0 * t2 - 2.0 * t;
+        const double ir = 1.0 / R;
+#pragma unroll
+        for (int k = 0; k < 5; k++) D[k] = -(g00 * a[k] + g10 * a[5 + k] + g01 * b[k] + g11 * b[5 + k]) * ir;
+    }
 }

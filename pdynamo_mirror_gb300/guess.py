@@ -224,8 +224,9 @@ class LinearResponseGuess:
         S = self._sfp / n - torch.outer(fm, pm)
         sd = torch.sqrt(torch.clamp(torch.diagonal(C), min=1e-30))
         Cs = C / torch.outer(sd, sd) + (self.ridge / n) * torch.eye(self.nf, dtype=torch.float64, device=C.device)
-        Js = torch.linalg.solve(Cs, S / sd[:, None])
-        self.J = (Js / sd[:, None]).to(torch.float32).contiguous()
+        # the (4 N_A)^2 system is solved on the host (training only; no device solver library needed)
+        Js = np.linalg.solve(Cs.cpu().numpy(), (S / sd[:, None]).cpu().numpy())
+        self.J = (torch.from_numpy(Js).to(C.device) / sd[:, None]).to(torch.float32).contiguous()
         self.f_mean, self.p_mean = fm, pm
         self.enabled = True
         return self
