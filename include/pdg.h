@@ -142,6 +142,24 @@ int pdg_scf(pdg_system *sys, int n_frames, const double *d_phi, const pdg_scf_op
             int use_density, double *d_energies, double *d_charges, int *d_status, int *d_ncycles,
             void *d_workspace, size_t workspace_bytes, void *stream);
 
+/* Spin-unrestricted (UHF) energies and gradients, cardinal occupancies, the FP64 method (density_step 0):
+ * QCModelMNDO with isSpinRestricted False (pMolecule.QCModelMNDO.pyx; QCModelMNDO_Fock over the alpha and beta
+ * density sets, QCModelMNDO.c:700-730, MakeFockG with each spin's density for the exchange, MNDOIntegrals.c:51-143;
+ * DIISSCFConverger.c:385-760 over both sets; QCModelMNDO_Gradients with the spin density's exchange terms,
+ * QCModelMNDOState.c:178-260).  n_alpha + n_beta = the system's electrons, n_alpha >= n_beta.
+ *   d_density     n_frames * 2 * N * N: alpha then beta of each frame (in: start densities when use_density != 0;
+ *                 out: converged)
+ *   d_total_spin  n_frames * N * N total densities, then n_frames * N * N spin densities (alpha - beta) of the
+ *                 converged states (written when d_gradients is given)
+ *   d_energies    as pdg_energy_gradients ([5] tr(P H) and [6] the two-electron energy summed over the spins)
+ *   workspace     pdg_uhf_workspace_bytes(sys, n_frames, n_alpha, n_beta)
+ * Other arguments as pdg_energy_gradients. */
+size_t pdg_uhf_workspace_bytes(pdg_system *sys, int n_frames, int n_alpha, int n_beta);
+int pdg_energy_gradients_uhf(pdg_system *sys, int n_frames, const double *d_xyz, const double *d_phi, const pdg_scf_options *options,
+                             int n_alpha, int n_beta, double *d_density, int use_density, double *d_energies, double *d_gradients,
+                             double *d_charges, int *d_status, int *d_ncycles, double *d_total_spin, void *d_workspace,
+                             size_t workspace_bytes, void *stream);
+
 /* Shared base of the mixed method's perturbative density steps (no counterpart in the reference; it stands where
  * the reference would call the FP64 eigensolver, QCOnePDM_MakeFromFock, QCOnePDM.c:403, for every frame).
  * Every FP64 density step of the mixed method leaves a base in its frame's workspace: the Fock matrix F0 and

@@ -1474,7 +1474,8 @@ static void rca2_iterate(DIIS2 *d, int N, double **P, double **F, double eold, d
 int oracle_energy_open(const OracleHamiltonian *h, int nAtoms, const int *elementIndex, const double *xyz,
                        double alphaCharge, double betaCharge, int restricted, int occupancyType, const int *nFractional,
                        double fermiBroadening, const double *phi, const OracleSCFOptions *o, double *energies, double *grad,
-                       double *charges, double *densityA, double *densityB, int *ncycles)
+                       double *charges, double *densityA, double *densityB, int *ncycles, const double *startA,
+                       const double *startB)
 {
     if (!h || nAtoms <= 0 || !o || !nFractional || occupancyType < 0 || occupancyType > 2) return 4;
     Config c;
@@ -1494,6 +1495,15 @@ int oracle_energy_open(const OracleHamiltonian *h, int nAtoms, const int *elemen
         P[s] = (double *)calloc((size_t)N * N, sizeof(double)); F[s] = (double *)calloc((size_t)N * N, sizeof(double));
         for (int i = 0; i < N; i++) P[s][i * N + i] = occ[s].charge / (double)N;   /* diagonal guess (QCOnePDM.c:330) */
     }
+    /* given start densities (packed; total density when restricted): used as a valid density, whose Fock matrices
+       enter the DIIS history from the first cycle */
+    const double *start[2] = { startA, startB };
+    int valid = 0;
+    if (startA && (restricted || startB)) {
+        for (int s = 0; s < ns; s++)
+            for (int i = 0; i < N; i++) for (int j = 0; j <= i; j++) P[s][i * N + j] = P[s][j * N + i] = start[s][PK(i, j)];
+        valid = 1;
+    }
     DIIS2 d; memset(&d, 0, sizeof(d));
     d.ndiis = o->history; d.nsets = ns;
     for (int i = 0; i < d.ndiis; i++) {
@@ -1505,7 +1515,7 @@ int oracle_energy_open(const OracleHamiltonian *h, int nAtoms, const int *elemen
         }
     }
     for (int s = 0; s < ns; s++) { d.rP[s] = (double *)calloc((size_t)N * N, sizeof(double)); d.rF[s] = (double *)calloc((size_t)N * N, sizeof(double)); }
-    int iteration = 0, converged = 0, qdiis = 0, qrca = o->useRCA ? 1 : 0, valid = 0;
+    int iteration = 0, converged = 0, qdiis = 0, qrca = o->useRCA ? 1 : 0;
     double eold = 0.0, deltaeold = 0.0, rms = 0.0, eqc = 0.0, eoei = 0.0, etei = 0.0, eocc = 0.0, eqcmm = 0.0;
     while (iteration < o->maximumSCFCycles && !converged) {
         /* Fock matrices and energies (QCModelMNDO_Fock) */
@@ -1576,7 +1586,7 @@ int oracle_fock(const OracleHamiltonian *h, int nAtoms, const int *elementIndex,
     config_init(&c, h, nAtoms, elementIndex, xyz);
     integrals(&c);
     int N = c.nBasis;
-    double *P = (double *)malloc(sizeof(double) * N * N), *F = (double *)malloc(sizeof(double) * N * N), eqc;
+    double *P = (double *)calloc((size_t)N * N, sizeof(double)), *F = (double *)calloc((size_t)N * N, sizeof(double)), eqc;
     for (int i = 0; i < N; i++) for (int j = 0; j <= i; j++) P[i * N + j] = P[j * N + i] = density[PK(i, j)];
     double eq = build_fock(&c, P, F, phi, NULL, &eqc, NULL, NULL);
     for (int i = 0; i < N; i++) for (int j = 0; j <= i; j++) fock[PK(i, j)] = F[i * N + j];

@@ -57,11 +57,14 @@ int oracle_energy(const OracleHamiltonian *h, int nAtoms, const int *elementInde
 /* Open-shell and fractional-occupancy states (QC only): restricted (total density) or unrestricted (alpha, beta)
  * densities, occupancyType 0 cardinal, 1 fixed fractional, 2 variable fractional (Fermi), nFractional = (HOOs,
  * LUOs, alpha HOOs, alpha LUOs, beta HOOs, beta LUOs).  energies[5] = occupancy energy.  phi (nullable): QC/MM
- * potentials at the QC atoms (a.u.), charges (nullable): the Lowdin charges of the last Fock build. */
+ * potentials at the QC atoms (a.u.), charges (nullable): the Lowdin charges of the last Fock build.  startA / startB
+ * (nullable, packed): start densities in place of the diagonal guess (alpha and beta; startA alone, the total density,
+ * when restricted), valid for the DIIS history from the first cycle. */
 int oracle_energy_open(const OracleHamiltonian *h, int nAtoms, const int *elementIndex, const double *xyz,
                        double alphaCharge, double betaCharge, int restricted, int occupancyType, const int *nFractional,
                        double fermiBroadening, const double *phi, const OracleSCFOptions *o, double *energies, double *grad,
-                       double *charges, double *densityA, double *densityB, int *ncycles);
+                       double *charges, double *densityA, double *densityB, int *ncycles, const double *startA,
+                       const double *startB);
 int oracle_fock(const OracleHamiltonian *h, int nAtoms, const int *elementIndex, const double *xyz,
                 const double *phi, const double *density, double *fock, double *energies);
 

@@ -42,7 +42,7 @@ def lib():
         L.oracle_energy.argtypes = [P, I, pi, pd, I, P, ctypes.POINTER(_Options), pd, I, pd, P, P,
                                     ctypes.POINTER(I), P]
         L.oracle_energy_open.argtypes = [P, I, pi, pd, D, D, I, I, pi, D, P, ctypes.POINTER(_Options), pd, P, P, pd, P,
-                                         ctypes.POINTER(I)]
+                                         ctypes.POINTER(I), P, P]
         L.oracle_fock.argtypes = [P, I, pi, pd, P, pd, pd, pd]
         L.oracle_gradients.argtypes = [P, I, pi, pd, pd, pd]
         L.oracle_abfs_knots.argtypes = [D, D, D, I, I, pd, pd]
@@ -158,9 +158,11 @@ OCCUPANCY_TYPES = {"Cardinal": 0, "Fixed Fractional": 1, "Variable Fractional": 
 
 def energy_open(ham, atomic_numbers, xyz_angstrom, charge=0, multiplicity=1, isSpinRestricted=True, occupancyType="Cardinal",
                 numberFractional=(1, 0, 1, 0, 1, 0), fermiBroadening=1.0e3, densityTolerance=1.0e-8, maximumSCFCycles=500,
-                history=10, diisOnset=0.2, energyTolerance=2.0e-4, useRCA=True, gradients=True, phi=None):
+                history=10, diisOnset=0.2, energyTolerance=2.0e-4, useRCA=True, gradients=True, phi=None, start=None):
     """Open-shell / fractional-occupancy QC energy (pMolecule.QCModelMNDO keywords isSpinRestricted, occupancyType),
-    alpha and beta charges as QCModel.CrossCheckModelAndState (pMolecule.QCModel.pyx:91-140) forms them."""
+    alpha and beta charges as QCModel.CrossCheckModelAndState (pMolecule.QCModel.pyx:91-140) forms them.  start: packed
+    start densities, (alpha, beta) when unrestricted or the total density when restricted, in place of the diagonal
+    guess."""
     Z = [int(z) for z in atomic_numbers]
     idx = np.array([ham.elements.index(z) for z in Z], dtype=np.int32)
     n = len(Z)
@@ -178,10 +180,19 @@ def energy_open(ham, atomic_numbers, xyz_angstrom, charge=0, multiplicity=1, isS
     nc = ctypes.c_int(0)
     ph = None if phi is None else np.ascontiguousarray(phi, dtype=np.float64)
     q = np.zeros(n)
+    if start is None:
+        sa = sb = None
+    elif isSpinRestricted:
+        sa, sb = np.ascontiguousarray(start, dtype=np.float64), None
+    else:
+        sa, sb = (np.ascontiguousarray(x, dtype=np.float64) for x in start)
+    for x in (sa, sb):
+        if x is not None and x.shape != (nb * (nb + 1) // 2,):
+            raise ValueError("start densities must be packed lower triangles of %d elements" % (nb * (nb + 1) // 2))
     rc = lib().oracle_energy_open(ham.handle, n, idx, np.ascontiguousarray(xyz_angstrom, dtype=np.float64).ravel(), a, b,
                                   int(bool(isSpinRestricted)), OCCUPANCY_TYPES[occupancyType],
                                   np.ascontiguousarray(numberFractional, dtype=np.int32), fermiBroadening, _ptr(ph),
-                                  ctypes.byref(opts), en, _ptr(g), _ptr(q), PA, _ptr(PB), ctypes.byref(nc))
+                                  ctypes.byref(opts), en, _ptr(g), _ptr(q), PA, _ptr(PB), ctypes.byref(nc), _ptr(sa), _ptr(sb))
     if rc == 4:
         raise ValueError("invalid occupancy settings")
     out = {"total_electronic": en[0], "eelectronic": en[1], "enuclear": en[2], "baseline": en[3], "eqcmm": en[4],

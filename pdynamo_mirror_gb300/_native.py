@@ -29,7 +29,8 @@ EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system
            "pdg_mm_energy_gradients", "pdg_phase_events", "pdg_phase_times", "pdg_qcmm_workspace_bytes", "pdg_wide_create", "pdg_wide_destroy",
            "pdg_wide_workspace_bytes", "pdg_wide_energy_gradients", "pdg_wide_phase_events", "pdg_wide_phase_times",
            "pdg_mm_bonded_create", "pdg_mm_bonded_destroy", "pdg_mm_bonded_energy_gradients", "pdg_base_bytes",
-           "pdg_base_capture", "pdg_set_shared_base", "pdg_set_side_stream", "pdg_last_error")
+           "pdg_base_capture", "pdg_set_shared_base", "pdg_set_side_stream", "pdg_uhf_workspace_bytes",
+           "pdg_energy_gradients_uhf", "pdg_last_error")
 TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densities Tridiagonal", "QC Densities Eigenvalues",
           "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds",
           "QC Densities Cluster Rounds", "QC Densities Steps", "QC Densities Purification",
@@ -132,6 +133,8 @@ def load(path=LIB_PATH):
     L.pdg_base_capture.argtypes = [P, I, I, P, S, P, P]
     L.pdg_set_shared_base.argtypes = [P, P]
     L.pdg_set_side_stream.argtypes = [P, P]
+    L.pdg_uhf_workspace_bytes.argtypes = [P, I, I, I]; L.pdg_uhf_workspace_bytes.restype = S
+    L.pdg_energy_gradients_uhf.argtypes = [P, I, P, P, ctypes.POINTER(SCFOptions), I, I, P, I, P, P, P, P, P, P, P, S, P]
     L.pdg_mm_workspace_bytes.argtypes = [P, I]
     L.pdg_mm_workspace_bytes.restype = S
     L.pdg_mm_energy_gradients.argtypes = [P, I, P, P, P, P, S, P]

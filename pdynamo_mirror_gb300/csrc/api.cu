@@ -71,7 +71,7 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     }
     if (nb > PDG_MAX_BASIS) return fail(PDG_TOO_LARGE, "more than 2048 basis functions");
     int nel = zsum - charge;
-    if (nel < 0 || nel % 2 != 0 || nel / 2 > nb) return fail(PDG_BAD_ARGUMENT, "closed-shell RHF needs an even electron count that fits the basis");
+    if (nel < 0 || nel > 2 * nb) return fail(PDG_BAD_ARGUMENT, "the electron count does not fit the basis");
     int npairs = n_atoms * (n_atoms - 1) / 2;
     std::vector<int> pi(npairs), pj(npairs), pt(npairs);
     int tei = 0;
@@ -222,6 +222,7 @@ extern "C" size_t pdg_workspace_bytes(const pdg_system *s, int n_frames)
 static int check_workspace(const pdg_system *s, int n_frames, void *ws, size_t bytes)
 {
     if (!s) return fail(PDG_BAD_ARGUMENT, "null system");
+    if (s->d.n_electrons % 2) return fail(PDG_BAD_ARGUMENT, "closed-shell RHF needs an even electron count (odd counts: pdg_energy_gradients_uhf)");
     if (n_frames <= 0) return fail(PDG_BAD_ARGUMENT, "n_frames must be positive");
     if (!ws || bytes < pdg_workspace_bytes(s, n_frames)) return fail(PDG_BAD_ARGUMENT, "workspace missing or too small");
     return PDG_OK;
@@ -307,6 +308,7 @@ extern "C" int pdg_phase_times(const pdg_system *s, float *h_ms)
 
 extern "C" int pdg_wide_create(pdg_system *s, pdg_wide **out)
 {
+    if (s && s->d.n_electrons % 2) return fail(PDG_BAD_ARGUMENT, "closed-shell RHF needs an even electron count");
     if (!s || !out) return fail(PDG_BAD_ARGUMENT, "null argument");
     if (s->d.n_basis < 3) return fail(PDG_BAD_ARGUMENT, "pdg_wide_create: the wide engine needs at least 3 basis functions");
     int rc = wide_create(s->d, out);
@@ -367,6 +369,56 @@ extern "C" int pdg_scf(pdg_system *s, int n_frames, const double *d_phi, const p
     launch_scf(s->d, p, n_frames, d_phi, *o, d_density, use_density, d_energies, d_charges, d_status, d_ncycles, (double *)ws, 0,
                nullptr, (cudaStream_t)stream, o->density_step != 0 ? s->shared_base : nullptr);
     return cuda_check(cudaGetLastError(), "scf kernel");
+}
+
+// ---- spin-unrestricted (UHF) energies and gradients
+// The frame plan of the spin-unrestricted SCF: room for every eigenpair of a spin's matrix.
+static FramePlan uhf_plan(const pdg_system *s, int n_alpha, int n_beta)
+{
+    DeviceSystem d = s->d;
+    d.n_vec = d.n_basis;   // every eigenpair of each spin's matrix
+    (void)n_alpha; (void)n_beta;
+    return make_plan(d, PDG_MAX_HISTORY);
+}
+
+extern "C" size_t pdg_uhf_workspace_bytes(pdg_system *s, int n_frames, int n_alpha, int n_beta)
+{
+    if (!s || n_frames <= 0) return 0;
+    return 2 * (size_t)n_frames * uhf_plan(s, n_alpha, n_beta).stride * sizeof(double);
+}
+
+extern "C" int pdg_energy_gradients_uhf(pdg_system *s, int n_frames, const double *d_xyz, const double *d_phi, const pdg_scf_options *o,
+                                        int n_alpha, int n_beta, double *d_density, int use_density, double *d_energies,
+                                        double *d_gradients, double *d_charges, int *d_status, int *d_ncycles, double *d_total_spin,
+                                        void *ws, size_t bytes, void *stream)
+{
+    if (!s || n_frames <= 0) return fail(PDG_BAD_ARGUMENT, "pdg_energy_gradients_uhf: bad argument");
+    if (!o || !d_xyz || !d_density || !d_energies || !d_status || (d_gradients && !d_total_spin))
+        return fail(PDG_BAD_ARGUMENT, "pdg_energy_gradients_uhf: null argument");
+    if (o->history < 1 || o->history > PDG_MAX_HISTORY) return fail(PDG_BAD_ARGUMENT, "history must be 1..16");
+    if (o->maximum_scf_cycles < 0) return fail(PDG_BAD_ARGUMENT, "maximum_scf_cycles must be >= 0");
+    if (o->density_step != 0) return fail(PDG_BAD_ARGUMENT, "pdg_energy_gradients_uhf: the FP64 density step only (density_step 0)");
+    if (use_density < 0 || use_density > 2) return fail(PDG_BAD_ARGUMENT, "use_density must be 0, 1 or 2");
+    const int N = s->d.n_basis;
+    if (n_alpha < n_beta || n_beta < 0 || n_alpha > N || n_alpha + n_beta != s->d.n_electrons)
+        return fail(PDG_BAD_ARGUMENT, "pdg_energy_gradients_uhf: n_alpha >= n_beta >= 0, n_alpha <= N and n_alpha + n_beta = the electrons");
+    if (!ws || bytes < pdg_uhf_workspace_bytes(s, n_frames, n_alpha, n_beta)) return fail(PDG_BAD_ARGUMENT, "workspace missing or too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    const FramePlan p = uhf_plan(s, n_alpha, n_beta);
+    double *w = (double *)ws;
+    int rc;
+    if ((rc = integrals(s->d, p, n_frames, d_xyz, w, st))) return rc;
+    launch_scf_uhf(s->d, p, n_frames, d_phi, *o, n_alpha, n_beta, d_density, use_density, d_energies, d_charges, d_status, d_ncycles, w, st);
+    if ((rc = cuda_check(cudaGetLastError(), "spin-unrestricted scf kernel"))) return rc;
+    if (d_gradients) {
+        launch_uhf_densities(n_frames, N, d_density, d_total_spin, st);
+        DeviceSystem dg = s->d;
+        dg.spin = d_total_spin + (size_t)n_frames * N * N;
+        launch_pair_gradients(dg, p, n_frames, d_xyz, d_total_spin, w, st, false);
+        launch_reduce_gradients(s->d, p, n_frames, w, d_gradients, st);
+        if ((rc = cuda_check(cudaGetLastError(), "gradient kernels"))) return rc;
+    }
+    return PDG_OK;
 }
 
 // ---- shared base of the mixed method's perturbative density steps
@@ -640,6 +692,7 @@ extern "C" int pdg_batch_create(pdg_system *const *systems, int n_items, pdg_bat
     long long ws = 0, dens = 0, atom = 0, work[PDG_WORK_KINDS] = {};
     for (int k = 0; k < n_items; k++) {
         if (!systems[k]) { delete bt; return fail(PDG_BAD_ARGUMENT, "null system in batch"); }
+        if (systems[k]->d.n_electrons % 2) { delete bt; return fail(PDG_BAD_ARGUMENT, "closed-shell RHF needs an even electron count"); }
         BatchItem it = {};
         it.s = systems[k]->d;
         it.plan = plan_for(systems[k], PDG_MAX_HISTORY);

@@ -46,6 +46,9 @@ struct DeviceSystem {
     const double *ovl_tab;
     const int *ovl_tab_off, *ovl_tab_n;   // per ordered element pair: first double, node count
     double ovl_tab_inv_h;
+    // spin density (alpha - beta) per frame, at the same offsets as the total density, for the spin-unrestricted
+    // gradients; null for closed shells
+    const double *spin;
 };
 
 // Per-frame workspace plan (all offsets in doubles from the frame's base).
@@ -94,7 +97,7 @@ __host__ inline FramePlan make_plan(const DeviceSystem &s, int history)
     p.A = o;      o += align32(2 * NN + 4 * N);  // work matrix: F P product, packed tridiagonal matrix, or the FP32
                                                  // purification iterates (two N x N) and P in FP32 (N x round4(N))
     const size_t kv = s.n_vec > 0 ? s.n_vec : 1, nc = N > kv ? N - kv : 1;
-    const size_t kvp = (nc + 31) & ~size_t(31);   // inverse iteration of the wanted vectors or of their complement
+    const size_t kvp = ((nc > kv ? nc : kv) + 31) & ~size_t(31);   // inverse iteration of the wanted vectors or of their complement
     p.G = o;      o += align32(kv * N);      // DIIS: the vectors times F
     p.Z = o;      o += align32(kv * (N | 1)); // wanted eigenvectors when they do not fit in shared memory
     p.LU = o;     o += align32(5 * N * kvp + (N * kvp + 7) / 8);   // inverse iteration factors + iterates
@@ -277,6 +280,10 @@ int launch_tc_selftest(int n, int kprod, int wait_limit, const float *x, float *
     void launch_scf(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *phi, const pdg_scf_options &o, \
                     double *density, int use_density, double *energies, double *charges, int *status, int *ncycles,      \
                     double *ws, int fock_only, double *fock_out, cudaStream_t st, const double *base = nullptr);          \
+    void launch_scf_uhf(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *phi, const pdg_scf_options &o,  \
+                        int n_alpha, int n_beta, double *density, int use_density, double *energies, double *charges,       \
+                        int *status, int *ncycles, double *ws, cudaStream_t st);                                              \
+    void launch_uhf_densities(int n_frames, int N, const double *P, double *out, cudaStream_t st);                       \
     int scf_occupancy(const DeviceSystem &s, int *threads, int *smem_bytes, int *ctas_per_sm);                           \
     void launch_batch_scf(const Batch &b, const int *order, int *queue, int grid, int smem_limit, size_t smem_bytes,     \
                           int tensor_items, const double *phi, const pdg_scf_options &o, double *density, int use_density, \
@@ -286,6 +293,8 @@ int launch_tc_selftest(int n, int kprod, int wait_limit, const float *x, float *
 namespace scf_n { PDG_SCF_LAUNCHERS }
 namespace scf_w { PDG_SCF_LAUNCHERS }
 using scf_n::launch_scf;
+using scf_n::launch_scf_uhf;
+using scf_n::launch_uhf_densities;
 using scf_n::scf_occupancy;
 void launch_guess_features(const DeviceSystem &s, int n_frames, const double *xyz, const double *phi, float *env, int *count,
                            int *offsets, float *X, int *row_frame, int *row_pair, cudaStream_t st);

@@ -455,6 +455,7 @@ k_pair_gradients(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, con
     const int N = s.n_basis;
     const double *R = xyz + 3 * fv.atom;
     const double *P = density + fv.dens;
+    const double *Sp = s.spin ? s.spin + fv.dens : nullptr;   // spin density (spin-unrestricted states)
     // one thread per pair: geometry, core-core derivative, direction cosines and their derivatives
     int mi = 0, mj = 0;
     double mx = 0.0, my = 0.0, mz = 0.0, mr = 1.0, mdc = 0.0;
@@ -495,7 +496,9 @@ k_pair_gradients(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, con
             const int l = MP_DA[kl], kk = MP_DB[kl], n = MP_DA[mn], m = MP_DB[mn];   // kl = (l >= kk), mn = (n >= m)
             const double aa = (kk == l) ? 1.0 : 2.0, bb = (m == n) ? 1.0 : 2.0;
             const int K = is + kk, Lx = is + l, M = js + m, Nn = js + n;
-            const double fv = P[(size_t)M * N + K] * P[(size_t)Nn * N + Lx] + P[(size_t)Nn * N + K] * P[(size_t)M * N + Lx];
+            double fv = P[(size_t)M * N + K] * P[(size_t)Nn * N + Lx] + P[(size_t)Nn * N + K] * P[(size_t)M * N + Lx];
+            // open shells: the spin density's products join the exchange part (QCModelMNDOState.c:178-260)
+            if (Sp) fv += Sp[(size_t)M * N + K] * Sp[(size_t)Nn * N + Lx] + Sp[(size_t)Nn * N + K] * Sp[(size_t)M * N + Lx];
             G[k] = (Real)(0.25 * aa * bb * fv) - oneI[kl] * oneJ[mn];
         }
         if (r >= 5.0e-3) {
@@ -622,6 +625,7 @@ __global__ void __launch_bounds__(256) k_pair_gradients_ss(DeviceSystem sys0, Fr
     const int N = s.n_basis, is = s.atom_start[i], js = s.atom_start[j];
     const double *P = density + fv.dens;
     const double pii = P[(size_t)is * N + is], pjj = P[(size_t)js * N + js], pij = P[(size_t)is * N + js];
+    const double sij = s.spin ? s.spin[fv.dens + (size_t)is * N + js] : 0.0;   // spin density (open shells)
     double eng[3] = { 0.0, 0.0, 0.0 };
     if (r >= 5.0e-3) {
         double dcore = 0.0;
@@ -630,7 +634,7 @@ __global__ void __launch_bounds__(256) k_pair_gradients_ss(DeviceSystem sys0, Fr
         const double ro = r + to[0], sv = rsqrt(ro * ro + ta[0]), ds0 = -ro * sv * sv * sv;
         const double roi = r + to[MP_CORE_I], svi = rsqrt(roi * roi + ta[MP_CORE_I]), dci = -roi * svi * svi * svi;
         const double roj = r + to[MP_CORE_J], svj = rsqrt(roj * roj + ta[MP_CORE_J]), dcj = -roj * svj * svj * svj;
-        const double gam = 0.5 * pij * pij - pii * pjj;
+        const double gam = 0.5 * (pij * pij + sij * sij) - pii * pjj;
         const double t0 = gam * ds0;
         const double o0 = pii * dci * (-Ej[PDG_E_ZCORE]) + pjj * dcj * (-Ei[PDG_E_ZCORE]);
         for (int x = 0; x < 3; x++) {
@@ -684,13 +688,16 @@ __global__ void __launch_bounds__(128) k_pair_gradients_sps(DeviceSystem sys0, F
     // one-centre densities (off-diagonal elements doubled) and Gamma over the sp atom's distributions:
     // Gamma_ab = 1/4 aa (P_{s,a} P_{s,b} + P_{s,b} P_{s,a}) - one_sp[ab] one_s  (QCModelMNDOState.c:196-250)
     const double one_s = P[(size_t)bs * N + bs];
+    const double *Sp = s.spin ? s.spin + fv.dens : nullptr;   // spin density (open shells)
     Real one_sp[10], gam[10];
 #pragma unroll
     for (int ab = 0; ab < 10; ab++) {
         const int a = MP_DA[ab], b = MP_DB[ab];
         const double f = (a == b) ? 1.0 : 2.0, o = f * P[(size_t)(as + a) * N + as + b];
         one_sp[ab] = (Real)o;
-        gam[ab] = (Real)(0.5 * f * P[(size_t)bs * N + as + a] * P[(size_t)bs * N + as + b] - o * one_s);
+        double x = P[(size_t)bs * N + as + a] * P[(size_t)bs * N + as + b];
+        if (Sp) x += Sp[(size_t)bs * N + as + a] * Sp[(size_t)bs * N + as + b];
+        gam[ab] = (Real)(0.5 * f * x - o * one_s);
     }
     double eng[3] = { 0.0, 0.0, 0.0 };
     if (r >= 5.0e-3) {

@@ -33,6 +33,7 @@ struct SCFArgs {
     double *ws; int fock_only; double *fock_out;
     int smem_limit;   // bytes of shared memory one CTA may plan for (the launch provides the plan's bytes)
     const double *base;   // shared base of the perturbative density steps (the mixed method), or null
+    int n_alpha, n_beta;  // spin-unrestricted SCF (k_scf_uhf): electrons of each spin
 };
 
 struct Smem {
@@ -743,7 +744,8 @@ __device__ void tridiag_vectors(const SCFArgs &a, double *wsf, const double *A, 
     }
 }
 
-__device__ double density_step(const SCFArgs &a, double *wsf, const double *F, double *P, Smem &sm, Timer &tm, bool make_base = false)
+__device__ double density_step(const SCFArgs &a, double *wsf, const double *F, double *P, Smem &sm, Timer &tm, bool make_base = false,
+                               int n_use = -1)
 {
     const DeviceSystem &s = a.s;
     const FramePlan &pl = a.plan;
@@ -830,10 +832,12 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
     tm.lap(PDG_T_TRIDIAGONAL);
     tridiag_vectors<double>(a, wsf, A, sm, tm, s.vec_occupied ? 0 : N - kv, kv, Z, ldz, sm.zs != nullptr);
     tm.lap(PDG_T_BACKTRANSFORM);
-    // --- P = 2 Z^T Z (occupied) or 2 (1 - Z^T Z) (virtual); lower triangle then mirrored
+    // --- P = 2 Z^T Z (occupied) or 2 (1 - Z^T Z) (virtual); lower triangle then mirrored.  n_use >= 0: the
+    //     leading n_use of the (occupied-side) vectors only, when all eigenpairs were computed
     const bool occ = s.vec_occupied;
+    const int kuse = (n_use >= 0 && occ) ? n_use : kv;
     double rms = 0.0;
-    tgemm<false, false>(N, N, kv, [&](int i, int k) { return Z[(size_t)k * ldz + i]; }, [&](int k, int j) { return Z[(size_t)k * ldz + j]; },
+    tgemm<false, false>(N, N, kuse, [&](int i, int k) { return Z[(size_t)k * ldz + i]; }, [&](int k, int j) { return Z[(size_t)k * ldz + j]; },
                         true, sm, [&](int i, int j, double v) {
         if (j > i) return;
         const double pn = occ ? 2.0 * v : ((i == j ? 2.0 : 0.0) - 2.0 * v);
@@ -1726,6 +1730,362 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
     }
 }
 
+// ----------------------------------------------------------------------------------------------------
+// Spin-unrestricted SCF (UHF, cardinal occupancies; the FP64 method).  Restates the reference's open-shell path:
+// QCModelMNDO_Fock with two density sets (QCModelMNDO.c:700-730; MakeFockG with the density of the spin for the
+// exchange, MNDOIntegrals.c:51-143), the converger over both sets (DIISSCFConverger.c:385-521: one B matrix summed
+// over the sets, the largest error doubled; :530-650 the same coefficients for both; :661-760 ODA traces summed) and
+// one density step per spin (QCOnePDM_MakeFromFock, QCOnePDM.c:403, occupancy 1).  A frame's alpha data use the
+// workspace slot of the frame (integrals included), its beta data slot n_frames + f; densities alpha then beta.
+
+// F = H + J(Pt) - K(Ps) without the QC/MM term: Coulomb from the total density, exchange from the spin's, the
+// one-centre terms split by spin as MakeFockG does (gss, gsp, gpp, gp2, hsp, hpp).
+__device__ void fock_build_spin(const SCFArgs &a, const double *H, const double *Pt, const double *Ps, double *F, const double *tei,
+                                Smem &sm, double *scratch)
+{
+    const DeviceSystem &s = a.s;
+    const int N = s.n_basis;
+    double *pk = s.n_cel <= GK * (GA_LD + GB_LD) ? sm.ta : scratch;
+    for (int e = threadIdx.x; e < s.n_cel; e += PDG_BLOCK) {
+        const int A = s.cel[e] >> 4, ab = s.cel[e] & 15, as = s.atom_start[A];
+        const int m = MP_DA[ab], n = MP_DB[ab];
+        pk[e] = (m == n ? 1.0 : 2.0) * Pt[(size_t)(as + m) * N + as + n];
+    }
+    __syncthreads();
+    const int n_out = s.n_cel + s.n_xel;
+    for (int e = threadIdx.x; e < n_out; e += PDG_BLOCK) {
+        if (e < s.n_cel) {
+            const int A = s.cel[e] >> 4, ab = s.cel[e] & 15;
+            const int no = s.atom_norb[A], as = s.atom_start[A], na = no * (no + 1) / 2;
+            const int m = MP_DA[ab], n = MP_DB[ab];
+            double acc = 0.0;
+            for (int B = 0; B < s.n_atoms; B++) {
+                if (B == A) continue;
+                const int hi = A > B ? A : B, lo = A > B ? B : A, pp = hi * (hi - 1) / 2 + lo;
+                const int k0 = s.atom_pk[B], nb = s.atom_pk[B + 1] - k0;
+                const double *blk = tei + s.pair_tei[pp], *pb = pk + k0;
+                if (A > B) for (int cd = 0; cd < nb; cd++) acc = fma(blk[ab * nb + cd], pb[cd], acc);
+                else       for (int cd = 0; cd < nb; cd++) acc = fma(blk[cd * na + ab], pb[cd], acc);
+            }
+            const double *E = elem(s, s.atom_elem[A]);
+            const double gss = E[PDG_E_GSS], gsp = E[PDG_E_GSP], gpp = E[PDG_E_GPP], gp2 = E[PDG_E_GP2], hsp = E[PDG_E_HSP], hpp = E[PDG_E_HPP];
+            const double *T = Pt + (size_t)as * N + as, *S = Ps + (size_t)as * N + as;
+            double g = 0.0;
+            if (m == 0 && n == 0) {
+                g = (T[0] - S[0]) * gss;
+                for (int q = 1; q < no; q++) g += T[q * N + q] * gsp - S[q * N + q] * hsp;
+            } else if (m == n) {
+                g = T[0] * gsp - S[0] * hsp + (T[m * N + m] - S[m * N + m]) * gpp;
+                for (int q = 1; q < no; q++) if (q != m) g += T[q * N + q] * gp2 - S[q * N + q] * hpp;
+            } else if (n == 0) g = 2.0 * T[m * N] * hsp - S[m * N] * (hsp + gsp);
+            else g = 2.0 * T[m * N + n] * hpp - S[m * N + n] * (hpp + gp2);
+            const double v = H[(size_t)(as + m) * N + as + n] + g + acc;
+            F[(size_t)(as + m) * N + as + n] = v;
+            F[(size_t)(as + n) * N + as + m] = v;
+        } else {
+            const int x = s.xel[e - s.n_cel], pp = x >> 4, lid = x & 15;
+            const int i = s.pair_i[pp], j = s.pair_j[pp];
+            const int noi = s.atom_norb[i], noj = s.atom_norb[j], is = s.atom_start[i], js = s.atom_start[j];
+            const int nj = noj * (noj + 1) / 2, aa = lid / noj, c = lid % noj;
+            const double *blk = tei + s.pair_tei[pp];
+            double t = 0.0;
+            for (int b = 0; b < noi; b++) {
+                const int ab = aa >= b ? aa * (aa + 1) / 2 + b : b * (b + 1) / 2 + aa;
+                for (int d = 0; d < noj; d++) {
+                    const int cd = c >= d ? c * (c + 1) / 2 + d : d * (d + 1) / 2 + c;
+                    t = fma(blk[ab * nj + cd], Ps[(size_t)(is + b) * N + js + d], t);
+                }
+            }
+            const double v = H[(size_t)(is + aa) * N + js + c] - t;
+            F[(size_t)(is + aa) * N + js + c] = v;
+            F[(size_t)(js + c) * N + is + aa] = v;
+        }
+    }
+    __syncthreads();
+}
+
+// tr(X Y) of two symmetric N x N matrices (lower triangle, warp per row).
+__device__ double sym_trace(int N, const double *X, const double *Y, Smem &sm)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double off = 0.0, dg = 0.0;
+    for (int i = w; i < N; i += PDG_WARPS)
+        for (int j = lane; j <= i; j += 32) {
+            const size_t k = (size_t)i * N + j;
+            if (j < i) off = fma(X[k], Y[k], off); else dg = fma(X[k], Y[k], dg);
+        }
+    const double2 t = block_sum2(off, dg, sm.red);
+    return 2.0 * t.x + t.y;
+}
+
+__device__ void scf_frame_uhf(const SCFArgs &a, const int f, double *shm)
+{
+    const DeviceSystem &s = a.s;
+    const FramePlan &pl = a.plan;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, N = s.n_basis;
+    const size_t NN = (size_t)N * N;
+    const int nsp[2] = { a.n_alpha, a.n_beta };
+    Smem sm = carve(shm, N, N, a.smem_limit);
+    double *wsp[2] = { a.ws + (size_t)f * pl.stride, a.ws + (size_t)(a.n_frames + f) * pl.stride };
+    double *H = wsp[0] + pl.H;
+    const double *tei = wsp[0] + pl.tei;
+    double *Fs[2] = { wsp[0] + pl.F, wsp[1] + pl.F };
+    double *Ps[2] = { a.density + (size_t)(2 * f) * NN, a.density + (size_t)(2 * f + 1) * NN };
+    double *Pt = wsp[1] + pl.P0;
+    double *Bm = wsp[0] + pl.misc;
+    Timer tm;
+    tm.slot = wsp[0] + pl.misc + PDG_MAX_HISTORY * PDG_MAX_HISTORY;
+    const long long t_begin = clock64();
+    if (tid < PDG_NTIMERS) tm.slot[tid] = 0.0;
+    __syncthreads();
+    tm.start();
+    double en = 0.0;
+    for (int p = tid; p < s.n_pairs; p += PDG_BLOCK) en += wsp[0][pl.pair_e + (size_t)p * PDG_PAIR_E_STRIDE + 20];
+    en = block_sum(en, sm.red);
+    double base = 0.0;
+    for (int A = tid; A < s.n_atoms; A += PDG_BLOCK) { const double *E = elem(s, s.atom_elem[A]); base += E[PDG_E_EHEAT] - E[PDG_E_EISOL]; }
+    base = block_sum(base, sm.red);
+    // the density steps compute every eigenpair of each spin's matrix (the occupied/virtual boundary then lies
+    // inside the vectors the inverse iteration orthogonalises, so a near-degenerate pair across it cannot mix) and
+    // form the density from the n_s lowest (occupancy 1: the step's 2 Z^T Z halved)
+    SCFArgs as = a;
+    as.s.vec_occupied = 1;
+    as.s.n_vec = N;
+    bool valid = a.use_density == 1;
+    if (a.use_density != 1)
+        for (int q = 0; q < 2; q++) {   // uniform diagonal guess per spin (QCOnePDM.c:326-331)
+            const double g = (double)nsp[q] / (double)N;
+            for (size_t k = tid; k < NN; k += PDG_BLOCK) Ps[q][k] = ((k / N) == (k % N)) ? g : 0.0;
+        }
+    __syncthreads();
+    const pdg_scf_options &o = a.o;
+    const int hist = o.history, hl = pl.hist_len;
+    int *ctl = sm.iv;
+    double *cf = sm.small + 32;
+    if (tid == 0) { ctl[1] = 0; for (int i = 0; i < hist; i++) ctl[2 + i] = i; }
+    int iteration = 0, converged = 0, qdiis = 0, qrca = o.use_rca ? 1 : 0, st = PDG_NOT_CONVERGED;
+    bool rca_prev = false;
+    double eold = 0.0, deltaeold = 0.0, rms = 0.0, eel = 0.0, e1 = 0.0, e2 = 0.0, eq = 0.0;
+    const double *phi = a.phi ? a.phi + (size_t)f * s.n_atoms : nullptr;
+    __syncthreads();
+    while (iteration < o.maximum_scf_cycles && !converged) {
+        for (size_t k = tid; k < NN; k += PDG_BLOCK) Pt[k] = Ps[0][k] + Ps[1][k];
+        __syncthreads();
+        e1 = e2 = 0.0;
+        for (int q = 0; q < 2; q++) {
+            fock_build_spin(a, H, Pt, Ps[q], Fs[q], tei, sm, wsp[q] + pl.G);
+            const double th = sym_trace(N, Ps[q], H, sm), tf = sym_trace(N, Ps[q], Fs[q], sm);
+            e1 += th;
+            e2 += 0.5 * (tf - th);
+        }
+        // QC/MM: Lowdin charges of the total density, -phi on the diagonal of both spins' matrices
+        double tq = 0.0;
+        for (int A = tid; A < s.n_atoms; A += PDG_BLOCK) {
+            const int no = s.atom_norb[A], as0 = s.atom_start[A];
+            double ps = 0.0;
+            for (int m = 0; m < no; m++) ps += Pt[(size_t)(as0 + m) * N + as0 + m];
+            const double q = elem(s, s.atom_elem[A])[PDG_E_ZCORE] - ps;
+            if (a.charges) a.charges[(size_t)f * s.n_atoms + A] = q;
+            if (phi) {
+                tq += q * phi[A];
+                for (int m = 0; m < no; m++) { Fs[0][(size_t)(as0 + m) * N + as0 + m] -= phi[A]; Fs[1][(size_t)(as0 + m) * N + as0 + m] -= phi[A]; }
+            }
+        }
+        eq = block_sum(tq, sm.red);
+        tm.lap(PDG_T_FOCK);
+        eel = e1 + e2 + eq;
+        if (!isfinite(eel)) { st = PDG_NAN; break; }
+        converged = (iteration > 0) && (rms <= o.density_tolerance) && (deltaeold <= o.energy_tolerance);
+        if (converged) break;
+        double deltae = eel - eold, etemp = eel;
+        if (valid) {
+            if (tid == 0) {
+                int mn = ctl[1], newest;
+                if (mn < hist) { mn++; newest = ctl[2 + mn - 1]; }
+                else { mn = hist; newest = ctl[2]; for (int i = 0; i < hist - 1; i++) ctl[2 + i] = ctl[3 + i]; ctl[2 + hist - 1] = newest; }
+                ctl[1] = mn; ctl[20] = newest;
+            }
+            __syncthreads();
+            const int newest = ctl[20], matnum = ctl[1];
+            double emx = 0.0, dots[PDG_MAX_HISTORY];
+            for (int m = 0; m < PDG_MAX_HISTORY; m++) dots[m] = 0.0;
+            for (int q = 0; q < 2; q++) {
+                double *wq = wsp[q];
+                double *hp = wq + pl.hP + (size_t)newest * hl, *hf = wq + pl.hF + (size_t)newest * hl, *he = wq + pl.hE + (size_t)newest * hl;
+                for (int i = w; i < N; i += PDG_WARPS)
+                    for (int j = lane; j <= i; j += 32) { hp[i * (i + 1) / 2 + j] = Ps[q][(size_t)i * N + j]; hf[i * (i + 1) / 2 + j] = Fs[q][(size_t)i * N + j]; }
+                double *FP = wq + pl.A;
+                const double *Fq = Fs[q], *Pq = Ps[q];
+                tgemm<true, false>(N, N, N, [&](int i, int k) { return Fq[(size_t)i * N + k]; }, [&](int k, int j) { return Pq[(size_t)k * N + j]; },
+                                   false, sm, [&](int i, int j, double v) { FP[(size_t)i * N + j] = v; });
+                for (int i = w; i < N; i += PDG_WARPS)
+                    for (int j = lane; j < i; j += 32) {
+                        const double ev = FP[(size_t)i * N + j] - FP[(size_t)j * N + i];
+                        he[i * (i - 1) / 2 + j] = ev;
+                        emx = fmax(emx, fabs(ev));
+                    }
+                __syncthreads();
+                const int ne = N * (N - 1) / 2;
+                for (int k = tid; k < ne; k += PDG_BLOCK) {
+                    const double en_ = he[k];
+                    for (int m = 0; m < matnum; m++) dots[m] += wq[pl.hE + (size_t)ctl[2 + m] * hl + k] * en_;
+                }
+            }
+            const double maxerr = 2.0 * block_max(emx, sm.red);   // two density sets: the largest error doubled
+            {
+                double *rs = sm.ta;
+                for (int m = 0; m < matnum; m++) {
+                    const double v = warp_sum(dots[m]);
+                    if (lane == 0) rs[w * PDG_MAX_HISTORY + m] = v;
+                }
+                __syncthreads();
+                if (tid < matnum) {
+                    double t = 0.0;
+                    for (int q = 0; q < PDG_WARPS; q++) t += rs[q * PDG_MAX_HISTORY + tid];
+                    const double b = 2.0 * t;
+                    const int n = ctl[2 + tid];
+                    Bm[n * PDG_MAX_HISTORY + newest] = b; Bm[newest * PDG_MAX_HISTORY + n] = b;
+                }
+            }
+            __syncthreads();
+            tm.lap(PDG_T_DIIS_SAVE);
+            if (iteration > 0) {
+                if (o.use_rca) {
+                    if (qdiis && maxerr > 0.8) { qdiis = 0; qrca = 1; }
+                    else if (iteration > 1 && qrca && maxerr < o.diis_onset) { qdiis = 1; qrca = 0; }
+                }
+                if (qdiis) {
+                    if (w == 0) {
+                        int mn = ctl[1], good = 0;
+                        while (mn > 1) {
+                            const int n1 = mn + 1;
+                            double *x = sm.small + 64;
+                            const bool okk = warp_small_solve(n1,
+                                [&](int i, int j) { return (i < mn && j < mn) ? Bm[ctl[2 + i] * PDG_MAX_HISTORY + ctl[2 + j]] : ((i == mn && j == mn) ? 0.0 : -1.0); },
+                                [&](int i) { return i == mn ? -1.0 : 0.0; }, sm.ta, x);
+                            double dev = 0.0;
+                            for (int i = 0; i < mn; i++) dev += x[i];
+                            dev += -1.0;
+                            if (okk && fabs(dev) < 1.0e-6) {
+                                if (lane < mn) cf[lane] = x[lane];
+                                good = 1;
+                                break;
+                            }
+                            mn--;
+                            __syncwarp();
+                            if (lane == 0) {
+                                for (int i = 0; i < mn; i++) ctl[2 + i] = ctl[3 + i];
+                                for (int i = mn; i < hist; i++) { ctl[2 + i] = ctl[2 + i - 1] + 1; if (ctl[2 + i] >= hist) ctl[2 + i] -= hist; }
+                            }
+                            __syncwarp();
+                        }
+                        if (lane == 0) { ctl[1] = mn; ctl[21] = good; }
+                    }
+                    __syncthreads();
+                    if (ctl[21]) {
+                        const int mn = ctl[1];
+                        for (int q = 0; q < 2; q++)
+                            for (int e = tid; e < hl; e += PDG_BLOCK) {
+                                int i = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+                                while ((i + 1) * (i + 2) / 2 <= e) i++;
+                                while (i * (i + 1) / 2 > e) i--;
+                                const int j = e - i * (i + 1) / 2;
+                                double pp = 0.0, ff = 0.0;
+                                for (int m = 0; m < mn; m++) {
+                                    const size_t off = (size_t)ctl[2 + m] * hl + e;
+                                    pp = fma(cf[m], wsp[q][pl.hP + off], pp); ff = fma(cf[m], wsp[q][pl.hF + off], ff);
+                                }
+                                Ps[q][(size_t)i * N + j] = pp; Fs[q][(size_t)i * N + j] = ff;
+                                Ps[q][(size_t)j * N + i] = pp; Fs[q][(size_t)j * N + i] = ff;
+                            }
+                        __syncthreads();
+                    }
+                } else if (o.use_rca && qrca && rca_prev) {
+                    // RCA_Iterate over both sets: the four traces summed (DIISSCFConverger.c:661-760)
+                    double t1 = 0, t2 = 0, t3 = 0, t4 = 0;
+                    for (int q = 0; q < 2; q++) {
+                        const double *rP = wsp[q] + pl.rP, *rF = wsp[q] + pl.rF;
+                        for (size_t k = tid; k < NN; k += PDG_BLOCK) {
+                            t1 += Fs[q][k] * Ps[q][k]; t2 += Fs[q][k] * rP[k]; t3 += rF[k] * Ps[q][k]; t4 += rF[k] * rP[k];
+                        }
+                    }
+                    t1 = block_sum(t1, sm.red); t2 = block_sum(t2, sm.red); t3 = block_sum(t3, sm.red); t4 = block_sum(t4, sm.red);
+                    double ca = t1 - t2, cc = t3 - t4, dd = eold;
+                    ca += cc + 2.0 * (dd - etemp);
+                    double cb = etemp - ca - cc - dd, fmin_ = etemp, mub = 1.0, mu;
+                    if (eold < etemp) { fmin_ = eold; mub = 0.0; }
+                    if (ca == 0.0) {
+                        if (cb == 0.0) mu = mub;
+                        else { double mt = -cc / (2.0 * cb); mu = (cb > 0.0 && mt > 0.0 && mt < 1.0) ? mt : mub; }
+                    } else {
+                        double fac = cb * cb - 3.0 * ca * cc;
+                        if (fac >= 0.0) {
+                            double m1 = (-cb + sqrt(fac)) / (3.0 * ca), m2 = (-cb - sqrt(fac)) / (3.0 * ca);
+                            if (m1 > 0.0 && m1 < 1.0) { double fv = ((ca * m1 + cb) * m1 + cc) * m1 + dd; if (fv < fmin_) { fmin_ = fv; mub = m1; } }
+                            if (m2 > 0.0 && m2 < 1.0) { double fv = ((ca * m2 + cb) * m2 + cc) * m2 + dd; if (fv < fmin_) { fmin_ = fv; mub = m2; } }
+                        }
+                        mu = mub;
+                    }
+                    mu = fmax(mu, 0.01);
+                    const double nu = 1.0 - mu;
+                    for (int q = 0; q < 2; q++) {
+                        const double *rP = wsp[q] + pl.rP, *rF = wsp[q] + pl.rF;
+                        for (size_t k = tid; k < NN; k += PDG_BLOCK) { Ps[q][k] = mu * Ps[q][k] + nu * rP[k]; Fs[q][k] = mu * Fs[q][k] + nu * rF[k]; }
+                    }
+                    etemp = ((ca * mu + cb) * mu + cc) * mu + dd;
+                    __syncthreads();
+                }
+            }
+            rca_prev = false;
+            if (o.use_rca) {   // RCA_Save every cycle, as the reference does (DIISSCFConverger.c:231-235)
+                for (int q = 0; q < 2; q++) {
+                    double *rP = wsp[q] + pl.rP, *rF = wsp[q] + pl.rF;
+                    for (size_t k = tid; k < NN; k += PDG_BLOCK) { rP[k] = Ps[q][k]; rF[k] = Fs[q][k]; }
+                }
+                __syncthreads();
+                rca_prev = true;
+            }
+            iteration++;
+        }
+        deltaeold = deltae; eold = etemp;
+        __syncthreads();
+        tm.lap(PDG_T_ITERATE);
+        // one density step per spin (the step builds 2 Z^T Z: the spin's density is doubled before and halved after)
+        rms = 0.0;
+        for (int q = 0; q < 2; q++) {
+            double *P = Ps[q];
+            if (nsp[q] == 0) {
+                double d2 = 0.0;
+                for (size_t k = tid; k < NN; k += PDG_BLOCK) { d2 += P[k] * P[k]; P[k] = 0.0; }
+                rms = fmax(rms, sqrt(block_sum(d2, sm.red)) / (double)N);
+                continue;
+            }
+            for (size_t k = tid; k < NN; k += PDG_BLOCK) P[k] *= 2.0;
+            __syncthreads();
+            as.s.n_occ = nsp[q];
+            const double r = density_step(as, wsp[q], Fs[q], P, sm, tm, false, nsp[q]);
+            for (size_t k = tid; k < NN; k += PDG_BLOCK) P[k] *= 0.5;
+            __syncthreads();
+            rms = fmax(rms, 0.5 * r);
+        }
+        valid = true;
+    }
+    if (converged) st = PDG_OK;
+    if (tid == 0) {
+        double *E = a.energies + (size_t)f * PDG_NENERGY;
+        E[0] = eel; E[1] = e1 + e2; E[2] = en; E[3] = base; E[4] = eq; E[5] = e1; E[6] = e2; E[7] = rms;
+        a.status[f] = st;
+        if (a.ncycles) a.ncycles[f] = iteration;
+        tm.slot[PDG_T_TOTAL] = (double)(clock64() - t_begin);
+    }
+}
+
+__global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf_uhf(SCFArgs a)
+{
+    extern __shared__ __align__(128) double shm[];
+    scf_frame_uhf(a, blockIdx.x, shm);
+}
+
 // Tensor memory (256 columns) and the completion mbarrier of the purification density step, for CTAs that may
 // run it.  A CTA of a kernel that contains tcgen05 code holds the tensor-memory allocation permit until it
 // allocates and relinquishes it (or exits), and no other such CTA is placed on its SM meanwhile: CTAs that
@@ -1849,6 +2209,40 @@ void launch_scf(const DeviceSystem &s, const FramePlan &p, int n_frames, const d
         configured = sm;
     }
     k_scf<<<n_frames, PDG_BLOCK, sm, st>>>(a);
+}
+
+__global__ void k_uhf_densities(long long n, size_t NN, const double *__restrict__ P, double *__restrict__ out)
+{
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const long long f = g / (long long)NN, k = g % (long long)NN;
+    const double a = P[(2 * f) * NN + k], b = P[(2 * f + 1) * NN + k];
+    out[g] = a + b;       // total densities, n_frames x N x N
+    out[n + g] = a - b;   // spin densities after them
+}
+
+void launch_uhf_densities(int n_frames, int N, const double *P, double *out, cudaStream_t st)
+{
+    const long long n = (long long)n_frames * N * N;
+    k_uhf_densities<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, (size_t)N * N, P, out);
+}
+
+void launch_scf_uhf(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *phi, const pdg_scf_options &o, int n_alpha,
+                    int n_beta, double *density, int use_density, double *energies, double *charges, int *status, int *ncycles, double *ws,
+                    cudaStream_t st)
+{
+    SCFArgs a = {};
+    a.s = s; a.plan = p; a.n_frames = n_frames; a.phi = phi; a.o = o; a.density = density; a.use_density = use_density;
+    a.energies = energies; a.charges = charges; a.status = status; a.ncycles = ncycles; a.ws = ws;
+    a.fock_only = 0; a.fock_out = nullptr; a.smem_limit = PDG_SMEM_LIMIT; a.base = nullptr;
+    a.n_alpha = n_alpha; a.n_beta = n_beta;
+    const int N = s.n_basis;
+    const size_t sm = scf_smem_bytes(N, N);   // every eigenpair (scf_frame_uhf)
+    if (sm > 48 * 1024) {
+        cudaFuncSetAttribute(k_scf_uhf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_scf_uhf, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    }
+    k_scf_uhf<<<n_frames, PDG_BLOCK, sm, st>>>(a);
 }
 
 void launch_batch_scf(const Batch &b, const int *order, int *queue, int grid, int smem_limit, size_t smem_bytes, int tensor_items,

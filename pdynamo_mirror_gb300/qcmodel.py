@@ -1,9 +1,10 @@
-"""QCModelMNDO: closed-shell RHF MNDO-family QC model on the GB300 path.
+"""QCModelMNDO: the MNDO-family QC model on the GB300 path.
 
 Mirrors the keyword surface of pDynamo's QCModelMNDO (pMolecule.QCModelMNDO.pyx:511-621): the first
 positional argument or ``mndoModel`` names the Hamiltonian; ``converger`` takes a DIISSCFConverger.
-Only the closed-shell, spin-restricted, cardinal-occupancy case is on this path; other occupancy or
-spin options raise ValueError, as unknown options do in the reference.
+Spin-restricted closed shells (RHF) and spin-unrestricted states (UHF, ``isSpinRestricted=False``; with the
+ElectronicState's multiplicity) with cardinal occupancies are on this path; fractional occupancies raise
+ValueError, as unknown options do in the reference.
 """
 
 import numpy as np
@@ -30,9 +31,7 @@ class QCModelMNDO:
         if "mndoModel" in options: self.mndoModel = options.pop("mndoModel")
         if "label" in options: self.label = options.pop("label")
         if "keepOrbitalData" in options: self.keepOrbitalData = bool(options.pop("keepOrbitalData"))
-        if "isSpinRestricted" in options:
-            if not options.pop("isSpinRestricted"):
-                raise ValueError("Only spin-restricted (RHF) models are on this path.")
+        if "isSpinRestricted" in options: self.isSpinRestricted = bool(options.pop("isSpinRestricted"))
         if "occupancyType" in options:
             if options.pop("occupancyType") != "Cardinal":
                 raise ValueError("Only cardinal occupancies are on this path.")
@@ -49,7 +48,7 @@ class QCModelMNDO:
     def GetOption(self, optionName):
         """An option of the model (QCModelMNDO.GetOption, pMolecule.QCModelMNDO.pyx:306-318): the occupancy options
         of the closed-shell cardinal states on this path; AttributeError for unknown names."""
-        values = {"isSpinRestricted": True, "occupancyType": "Cardinal", "numberFractionalHOOs": 1, "numberFractionalLUOs": 0,
+        values = {"isSpinRestricted": self.isSpinRestricted, "occupancyType": "Cardinal", "numberFractionalHOOs": 1, "numberFractionalLUOs": 0,
                   "numberFractionalAlphaHOOs": 1, "numberFractionalAlphaLUOs": 0, "numberFractionalBetaHOOs": 1,
                   "numberFractionalBetaLUOs": 0}
         if optionName not in values:
@@ -57,8 +56,8 @@ class QCModelMNDO:
         return values[optionName]
 
     def IsSpinRestricted(self):
-        """The states on this path are closed-shell RHF (pMolecule.QCModel.pyx:298)."""
-        return True
+        """Whether the model is spin-restricted (pMolecule.QCModel.pyx:298)."""
+        return self.isSpinRestricted
 
     def AtomicCharges(self, configuration, chargeModel=None, spinDensities=False):
         """Lowdin charges of the QC atoms from the last energy on configuration (QCModelMNDO.AtomicCharges; the

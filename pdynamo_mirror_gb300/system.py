@@ -18,8 +18,8 @@ from .engine import GRADIENT_TO_KJ_PER_A, HARTREES_TO_KJ, QCEngine
 
 class ElectronicState:
     def __init__(self, charge=0, multiplicity=1):
-        if multiplicity != 1:
-            raise ValueError("Only singlet (closed-shell) states are on this path.")
+        if int(multiplicity) < 1:
+            raise ValueError("Invalid multiplicity.")
         self.charge, self.multiplicity = int(charge), int(multiplicity)
 
 
@@ -131,10 +131,21 @@ class System:
         qc = set(self.qcSelection or [])
         return [i for i in range(len(self.atomicNumbers)) if i not in qc]
 
+    def spin_occupancies(self):
+        """(n_alpha, n_beta) of a spin-unrestricted model, None for a spin-restricted one; the checks of
+        QCModel.CrossCheckModelAndState (pMolecule.QCModel.pyx:91-140) for cardinal occupancies."""
+        mult = int(self.electronicState.multiplicity)
+        if self.qcModel.isSpinRestricted:
+            if mult != 1:
+                raise ValueError("A spin-unrestricted calculation is required for non-singlet states with cardinal occupancy.")
+            return None
+        ne = self.engine().n_electrons
+        if (ne + mult - 1) % 2 or mult - 1 > ne:
+            raise ValueError("The multiplicity is incompatible with the number of electrons.")
+        return (ne + mult - 1) // 2, (ne - mult + 1) // 2
+
     def engine(self):
         """The device engine of the QC region, rebuilt when the electronic state's charge changes."""
-        if self.electronicState.multiplicity != 1:
-            raise ValueError("Only singlet (closed-shell) states are on this path.")
         charge = int(self.electronicState.charge)
         if self._engine is None or getattr(self, "_engine_charge", None) != charge:
             qcZ = [self.atomicNumbers[i] for i in self.qcSelection]
@@ -197,8 +208,13 @@ class System:
         X = self._device_frames(frames)
         qc, mm, q, mm_idx = self._device_inputs(None, X)
         mmi = self._mm_interactions() if self.mmModel is not None else None
-        r = eng.run(qc, self.qcModel.converger, mm, q, self.nbModel if mm is not None else None, gradients=doGradients,
-                    warm_start=warmStart, guess=self.densityGuess)
+        spins = self.spin_occupancies()
+        if spins is None:
+            r = eng.run(qc, self.qcModel.converger, mm, q, self.nbModel if mm is not None else None, gradients=doGradients,
+                        warm_start=warmStart, guess=self.densityGuess)
+        else:
+            r = eng.run_uhf(qc, self.qcModel.converger, spins[0], spins[1], mm, q, self.nbModel if mm is not None else None,
+                            gradients=doGradients, warm_start=warmStart)
         F = qc.shape[0]
         # one device -> host copy of the small per-frame results
         small = torch.cat([r["energies"], r["status"].to(torch.float64)[:, None], r["ncycles"].to(torch.float64)[:, None]], 1)
@@ -233,7 +249,10 @@ class System:
         terms = {"Pure QC": pure, "QC/MM Elect.": qcmm, "SCF Cycles": small[:, _native.NENERGY + 1].astype(np.int32), "Status": st}
         if (st != _native.PDG_OK).any():
             self._engine.density = None
+            self._engine.density_uhf = None
             raise SCFNotConverged(scf_failure_message(st))
+        # the QC density of each frame (the total density of a spin-unrestricted state) for the properties
+        self._qc_density = (r["density_alpha"] + r["density_beta"]) if spins is not None else self._engine.density
         total = pure + (qcmm if mm is not None else 0.0)
         if mmi is not None:
             Emm = small[:, _native.NENERGY + 2:_native.NENERGY + 2 + len(_native.MM_TERMS)]
@@ -252,7 +271,7 @@ class System:
         self.configuration.gradients3 = None if G is None else G[0]
         self.configuration.qcCharges = self.qcChargesBatch[0].copy()
         from .properties import QCState
-        self.configuration.qcState = QCState(self._engine.density[0].clone(), self.qcModel.mndoModel,
+        self.configuration.qcState = QCState(self._qc_density[0].clone(), self.qcModel.mndoModel,
                                              [self.atomicNumbers[i] for i in self.qcSelection], self.coordinates3[self.qcSelection])
         return float(total[0])
 

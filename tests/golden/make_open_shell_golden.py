@@ -2,7 +2,8 @@
 radical test set (pMolecule-1.9.0/tests/QCTestSystems.py:34-56, as pMolecule-1.9.0/tests/MNDOUHFEnergies.py runs it:
 converger densityTolerance 1e-8, maximumSCFCycles 500) for every restricted / unrestricted and occupancy-type
 combination listed there, computed by the reference's compiled C core (oracle/ref_shim.c: ref_system_create_open).
-Spin densities (alpha and beta, packed) are kept for the two small radicals.  QC/MM cases: the three open-shell
+Spin densities (alpha and beta, packed) are kept for the two small radicals and for the tyrosine dipeptide triplet
+(unrestricted, cardinal occupancies: the start density of the converged-state test).  QC/MM cases: the three open-shell
 systems in the field of seeded point charges (their potentials at the QC atoms stored with the case).  PM6 cases:
 the allyl and methylene radicals, unrestricted.
 
@@ -55,7 +56,7 @@ def main(root):
                     "ncycles": int(r["ncycles"]), "pure_qc_kj": float(r["pure_qc_kj"]),
                     "eelectronic": float(r["eelectronic"]), "enuclear": float(r["enuclear"]),
                     "gradients_hartree_per_bohr": r["gradients"].tolist()}
-            if label in SMALL:
+            if label in SMALL or (label == "Tyrosine Dipeptide Triplet" and occ == "Cardinal"):
                 if restricted:
                     case["density"] = r["density"].tolist()
                 else:

@@ -58,7 +58,8 @@ def test_option_errors_match_reference_behaviour():
     with pytest.raises(ValueError):
         DIISSCFConverger(notAnOption=1)
     with pytest.raises(ValueError):
-        QCModelMNDO("am1", isSpinRestricted=False)
+        QCModelMNDO("am1", occupancyType="Fixed Fractional")
+    assert not QCModelMNDO("am1", isSpinRestricted=False).IsSpinRestricted()
     with pytest.raises(ValueError):
         QCModelMNDO("pm6")
     with pytest.raises(ValueError):
@@ -77,7 +78,8 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_system_engine_follows_the_electronic_state(monkeypatch):
-    """The device engine is rebuilt when the charge changes and non-singlet states are refused (host logic; the
+    """The device engine is rebuilt when the charge changes; non-singlet states need a spin-unrestricted model, whose
+    alpha and beta electron counts follow from the multiplicity (QCModel.CrossCheckModelAndState; host logic, the
     engine itself is replaced by a stand-in, as it needs a GPU)."""
     import pdynamo_mirror_gb300.system as S
     made = []
@@ -86,6 +88,7 @@ def test_system_engine_follows_the_electronic_state(monkeypatch):
         def __init__(self, hamiltonian, atomic_numbers, charge):
             made.append(charge)
             self.device = "cpu"
+            self.n_electrons = 8 - charge
 
     monkeypatch.setattr(S, "QCEngine", Stand)
     s = S.System([8, 1, 1], [[0.0, 0.0, 0.0], [0.96, 0.0, 0.0], [-0.24, 0.93, 0.0]])
@@ -96,8 +99,15 @@ def test_system_engine_follows_the_electronic_state(monkeypatch):
     e2 = s.engine()
     assert e2 is not e1 and made == [0, 2]
     s.electronicState.multiplicity = 3
-    with pytest.raises(ValueError):
-        s.engine()
+    with pytest.raises(ValueError, match="spin-unrestricted"):
+        s.spin_occupancies()
+    s.DefineQCModel(QCModelMNDO("am1", isSpinRestricted=False))
+    assert s.spin_occupancies() == (4, 2)
+    s.electronicState.multiplicity = 2
+    with pytest.raises(ValueError, match="incompatible"):
+        s.spin_occupancies()
+    s.electronicState.multiplicity = 1
+    assert s.spin_occupancies() == (3, 3)
 
 
 def test_atomic_charges_assembly():
