@@ -42,7 +42,7 @@ typedef enum {
 /* Per-element parameter record: PDG_ELEMENT_STRIDE doubles, all in atomic units, filled by the host
  * from pDynamo's parameter files (restating pMolecule.MNDOParameters.pyx:309-370 and
  * MNDOParameters.c:155-930).  Offsets: */
-#define PDG_ELEMENT_STRIDE 96
+#define PDG_ELEMENT_STRIDE 128
 enum {
     PDG_E_Z = 0, PDG_E_NORB = 1, PDG_E_ZCORE = 2, PDG_E_ALP = 3, PDG_E_GPHOT = 4, PDG_E_NG = 5, PDG_E_NPDDG = 6,
     PDG_E_DD = 7, PDG_E_QQ = 8, PDG_E_PO = 9 /* 9 values */, PDG_E_GSS = 18, PDG_E_GSP = 19, PDG_E_GPP = 20,
@@ -50,7 +50,10 @@ enum {
     PDG_E_FN1 = 32 /* 4 */, PDG_E_FN2 = 36 /* 4 */, PDG_E_FN3 = 40 /* 4 */, PDG_E_PDDGC = 44 /* 4 */,
     PDG_E_PDDGE = 48 /* 4 */, PDG_E_EHEAT = 52, PDG_E_EISOL = 53, PDG_E_NSHELL = 54, PDG_E_NPRIM_S = 55,
     PDG_E_NPRIM_P = 56, PDG_E_EXP_S = 57 /* 6 */, PDG_E_CCBF_S = 63 /* 6 */, PDG_E_EXP_P = 69 /* 6 */,
-    PDG_E_CCBF_P = 75 /* 6 */
+    PDG_E_CCBF_P = 75 /* 6 */,
+    /* PM6: 1 when the element has diatomic core-core pairs; the element's index in the system's element list; the
+     * pairs' exponent a (1/bohr) and coefficient x by partner index (0 where the pair has no parameters) */
+    PDG_E_DIAT = 81, PDG_E_INDEX = 82, PDG_E_DIAT_A = 84 /* PDG_MAX_ELEMENTS */, PDG_E_DIAT_X = 100 /* PDG_MAX_ELEMENTS */
 };
 
 #define PDG_MAX_ELEMENTS 16
@@ -155,6 +158,35 @@ int pdg_scf(pdg_system *sys, int n_frames, const double *d_phi, const pdg_scf_op
  *   workspace     pdg_uhf_workspace_bytes(sys, n_frames, n_alpha, n_beta)
  * Other arguments as pdg_energy_gradients. */
 size_t pdg_uhf_workspace_bytes(pdg_system *sys, int n_frames, int n_alpha, int n_beta);
+
+/* Occupancies of the open-shell / fractional-occupancy SCF (QCModelMNDO's isSpinRestricted, occupancyType,
+ * numberFractional*HOOs / LUOs and fermiBroadening options; the alpha and beta charges as
+ * QCModel.CrossCheckModelAndState forms them, pMolecule.QCModel.pyx:91-140). */
+enum { PDG_OCC_CARDINAL = 0, PDG_OCC_FIXED_FRACTIONAL = 1, PDG_OCC_VARIABLE_FRACTIONAL = 2 };
+typedef struct {
+    int spin_restricted;       /* 1: one density set (the total density, occupancy 2 per orbital); 0: alpha and beta */
+    int occupancy_type;        /* PDG_OCC_* */
+    double alpha_charge;       /* electrons of each spin; alpha + beta = the system's electrons */
+    double beta_charge;
+    int n_fractional[6];       /* fixed fractional: HOOs, LUOs (restricted), alpha HOOs, alpha LUOs, beta HOOs, beta LUOs */
+    double fermi_broadening;   /* variable fractional: beta of the Fermi-Dirac occupancies (1 / Hartree) */
+} pdg_occupancy;
+
+/* Open-shell and fractional-occupancy energies and gradients (QCModelMNDO with isSpinRestricted and occupancyType;
+ * QCOnePDM_MakeFromFock with the occupancies, QCOnePDM.c:403-460 and :505-599), the FP64 method: spin-restricted or
+ * unrestricted, cardinal, fixed fractional or variable fractional occupancies.  The electronic energy includes the
+ * occupancy energy of variable fractional occupancies, d_energies[1] - [5] - [6].
+ *   d_density     n_frames * n_sets * N * N (n_sets 1 when spin_restricted: the total density; else alpha then beta)
+ *   d_total_spin  unrestricted: as pdg_energy_gradients_uhf; restricted: unused
+ *   workspace     pdg_open_workspace_bytes(sys, n_frames)
+ * Invalid occupancies (a cardinal count that is not whole, fractional orbitals outside 1..occupied and 0..virtual,
+ * charges that do not add up to the electrons or exceed the orbitals) return PDG_BAD_ARGUMENT.  Other arguments as
+ * pdg_energy_gradients_uhf, which is this call with unrestricted cardinal occupancies. */
+size_t pdg_open_workspace_bytes(pdg_system *sys, int n_frames);
+int pdg_energy_gradients_open(pdg_system *sys, int n_frames, const double *d_xyz, const double *d_phi, const pdg_scf_options *options,
+                              const pdg_occupancy *occupancy, double *d_density, int use_density, double *d_energies,
+                              double *d_gradients, double *d_charges, int *d_status, int *d_ncycles, double *d_total_spin,
+                              void *d_workspace, size_t workspace_bytes, void *stream);
 int pdg_energy_gradients_uhf(pdg_system *sys, int n_frames, const double *d_xyz, const double *d_phi, const pdg_scf_options *options,
                              int n_alpha, int n_beta, double *d_density, int use_density, double *d_energies, double *d_gradients,
                              double *d_charges, int *d_status, int *d_ncycles, double *d_total_spin, void *d_workspace,

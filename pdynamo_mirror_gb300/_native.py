@@ -30,7 +30,7 @@ EXPORTS = ("pdg_version", "pdg_system_create", "pdg_system_destroy", "pdg_system
            "pdg_wide_workspace_bytes", "pdg_wide_energy_gradients", "pdg_wide_phase_events", "pdg_wide_phase_times",
            "pdg_mm_bonded_create", "pdg_mm_bonded_destroy", "pdg_mm_bonded_energy_gradients", "pdg_base_bytes",
            "pdg_base_capture", "pdg_set_shared_base", "pdg_set_side_stream", "pdg_uhf_workspace_bytes",
-           "pdg_energy_gradients_uhf", "pdg_last_error")
+           "pdg_energy_gradients_uhf", "pdg_open_workspace_bytes", "pdg_energy_gradients_open", "pdg_last_error")
 TIMERS = ("QC Fock", "QC Converger DIIS Save", "QC Converger Iterate", "QC Densities Tridiagonal", "QC Densities Eigenvalues",
           "QC Densities Eigenvectors", "QC Densities Back-transform", "QC Densities Density", "QC SCF Total", "QC SCF Fock Builds",
           "QC Densities Cluster Rounds", "QC Densities Steps", "QC Densities Purification",
@@ -49,6 +49,15 @@ class SCFOptions(ctypes.Structure):
                 ("diis_onset", ctypes.c_double), ("maximum_scf_cycles", ctypes.c_int),
                 ("history", ctypes.c_int), ("use_rca", ctypes.c_int), ("density_step", ctypes.c_int),
                 ("mixed_switch", ctypes.c_double)]
+
+
+OCC_TYPES = {"Cardinal": 0, "Fixed Fractional": 1, "Variable Fractional": 2}
+
+
+class Occupancy(ctypes.Structure):
+    """pdg_occupancy: density sets and occupancies of pdg_energy_gradients_open."""
+    _fields_ = [("spin_restricted", ctypes.c_int), ("occupancy_type", ctypes.c_int), ("alpha_charge", ctypes.c_double),
+                ("beta_charge", ctypes.c_double), ("n_fractional", ctypes.c_int * 6), ("fermi_broadening", ctypes.c_double)]
 
 
 class NativeError(RuntimeError):
@@ -135,6 +144,9 @@ def load(path=LIB_PATH):
     L.pdg_set_side_stream.argtypes = [P, P]
     L.pdg_uhf_workspace_bytes.argtypes = [P, I, I, I]; L.pdg_uhf_workspace_bytes.restype = S
     L.pdg_energy_gradients_uhf.argtypes = [P, I, P, P, ctypes.POINTER(SCFOptions), I, I, P, I, P, P, P, P, P, P, P, S, P]
+    L.pdg_open_workspace_bytes.argtypes = [P, I]; L.pdg_open_workspace_bytes.restype = S
+    L.pdg_energy_gradients_open.argtypes = [P, I, P, P, ctypes.POINTER(SCFOptions), ctypes.POINTER(Occupancy), P, I, P, P, P, P, P, P,
+                                            P, S, P]
     L.pdg_mm_workspace_bytes.argtypes = [P, I]
     L.pdg_mm_workspace_bytes.restype = S
     L.pdg_mm_energy_gradients.argtypes = [P, I, P, P, P, P, S, P]

@@ -59,6 +59,9 @@ extern "C" int pdg_system_create(const double *h_elements, int n_elements, int n
     *out = nullptr;
     if (n_elements <= 0 || n_elements > PDG_MAX_ELEMENTS) return fail(PDG_TOO_LARGE, "element count outside 1..16");
     if (n_atoms <= 0 || n_atoms > PDG_MAX_ATOMS) return fail(PDG_TOO_LARGE, "atom count outside 1..1024");
+    for (int e = 0; e < n_elements; e++)   // PM6 records index their diatomic pairs by the partner's place in this list
+        if (h_elements[e * PDG_ELEMENT_STRIDE + PDG_E_DIAT] != 0.0 && (int)h_elements[e * PDG_ELEMENT_STRIDE + PDG_E_INDEX] != e)
+            return fail(PDG_BAD_ARGUMENT, "PM6 element record whose index is not its place in the element list");
     std::vector<int> elem(n_atoms), start(n_atoms), norb(n_atoms);
     int nb = 0, zsum = 0;
     for (int a = 0; a < n_atoms; a++) {
@@ -371,20 +374,102 @@ extern "C" int pdg_scf(pdg_system *s, int n_frames, const double *d_phi, const p
     return cuda_check(cudaGetLastError(), "scf kernel");
 }
 
-// ---- spin-unrestricted (UHF) energies and gradients
-// The frame plan of the spin-unrestricted SCF: room for every eigenpair of a spin's matrix.
-static FramePlan uhf_plan(const pdg_system *s, int n_alpha, int n_beta)
+// ---- open-shell (UHF) and fractional-occupancy energies and gradients
+// The frame plan of the open-shell / fractional-occupancy SCF: room for every eigenpair of a set's matrix.
+static FramePlan open_plan(const pdg_system *s)
 {
     DeviceSystem d = s->d;
-    d.n_vec = d.n_basis;   // every eigenpair of each spin's matrix
-    (void)n_alpha; (void)n_beta;
+    d.n_vec = d.n_basis;
     return make_plan(d, PDG_MAX_HISTORY);
+}
+
+extern "C" size_t pdg_open_workspace_bytes(pdg_system *s, int n_frames)
+{
+    if (!s || n_frames <= 0) return 0;
+    return 2 * (size_t)n_frames * open_plan(s).stride * sizeof(double);
 }
 
 extern "C" size_t pdg_uhf_workspace_bytes(pdg_system *s, int n_frames, int n_alpha, int n_beta)
 {
-    if (!s || n_frames <= 0) return 0;
-    return 2 * (size_t)n_frames * uhf_plan(s, n_alpha, n_beta).stride * sizeof(double);
+    (void)n_alpha; (void)n_beta;
+    return pdg_open_workspace_bytes(s, n_frames);
+}
+
+// One density set's occupancies by occupancy_init's rules (QCOnePDM.c:290-330, with the orbital checks of
+// QCModel.CrossCheckModelAndState, pMolecule.QCModel.pyx:119-135): cardinal needs a whole number of full orbitals;
+// fixed fractional spreads the charge left over by the nOcc - nHOO full orbitals evenly over nHOO + nLUO orbitals.
+static bool occupancy_set(int type, double factor, double charge, int nHOO, int nLUO, int N, OpenOccupancy &oc, int q)
+{
+    if (!(charge >= 0.0)) return false;
+    const int nocc = (int)std::lround(std::ceil(charge / factor));
+    if (nocc > N) return false;
+    int ncard = 0, nfrac = 0;
+    double frac = 0.0;
+    bool ok = true;
+    if (type == PDG_OCC_CARDINAL) { ok = std::fabs(nocc * factor - charge) < 1.0e-10; ncard = nocc; }
+    else if (type == PDG_OCC_FIXED_FRACTIONAL) {
+        ncard = nocc - nHOO; nfrac = nHOO + nLUO;
+        frac = (charge / factor - ncard) / (double)std::max(nfrac, 1);
+        ok = nHOO > 0 && nLUO >= 0 && ncard >= 0 && ncard + nfrac <= N && frac >= 0.0 && frac <= 1.0;
+    }
+    oc.charge[q] = charge; oc.ncard[q] = ncard; oc.nfrac[q] = nfrac; oc.frac[q] = frac;
+    return ok;
+}
+
+extern "C" int pdg_energy_gradients_open(pdg_system *s, int n_frames, const double *d_xyz, const double *d_phi, const pdg_scf_options *o,
+                                         const pdg_occupancy *occ, double *d_density, int use_density, double *d_energies,
+                                         double *d_gradients, double *d_charges, int *d_status, int *d_ncycles, double *d_total_spin,
+                                         void *ws, size_t bytes, void *stream)
+{
+    if (!s || n_frames <= 0) return fail(PDG_BAD_ARGUMENT, "pdg_energy_gradients_open: bad argument");
+    if (!o || !occ || !d_xyz || !d_density || !d_energies || !d_status)
+        return fail(PDG_BAD_ARGUMENT, "pdg_energy_gradients_open: null argument");
+    if (o->history < 1 || o->history > PDG_MAX_HISTORY) return fail(PDG_BAD_ARGUMENT, "history must be 1..16");
+    if (o->maximum_scf_cycles < 0) return fail(PDG_BAD_ARGUMENT, "maximum_scf_cycles must be >= 0");
+    if (o->density_step != 0) return fail(PDG_BAD_ARGUMENT, "pdg_energy_gradients_open: the FP64 density step only (density_step 0)");
+    if (use_density < 0 || use_density > 2) return fail(PDG_BAD_ARGUMENT, "use_density must be 0, 1 or 2");
+    const int N = s->d.n_basis;
+    OpenOccupancy oc = {};
+    oc.type = occ->occupancy_type;
+    if (oc.type < PDG_OCC_CARDINAL || oc.type > PDG_OCC_VARIABLE_FRACTIONAL) return fail(PDG_BAD_ARGUMENT, "unknown occupancy type");
+    const double a = occ->alpha_charge, b = occ->beta_charge;
+    if (!(a >= 0.0) || !(b >= 0.0) || std::fabs(a + b - (double)s->d.n_electrons) > 1.0e-10)
+        return fail(PDG_BAD_ARGUMENT, "alpha and beta charges must be >= 0 and add up to the electrons");
+    if (oc.type == PDG_OCC_VARIABLE_FRACTIONAL && !(occ->fermi_broadening > 0.0))
+        return fail(PDG_BAD_ARGUMENT, "the Fermi broadening must be > 0");
+    oc.beta = occ->fermi_broadening;
+    const int *nf = occ->n_fractional;
+    bool ok;
+    if (occ->spin_restricted) {
+        oc.n_sets = 1; oc.factor = 2.0;
+        ok = occupancy_set(oc.type, 2.0, a + b, nf[0], nf[1], N, oc, 0);
+    } else {
+        oc.n_sets = 2; oc.factor = 1.0;
+        ok = occupancy_set(oc.type, 1.0, a, nf[2], nf[3], N, oc, 0) && occupancy_set(oc.type, 1.0, b, nf[4], nf[5], N, oc, 1);
+    }
+    if (!ok) return fail(PDG_BAD_ARGUMENT, "invalid occupancies (orbital counts, fractional orbital specification or charges)");
+    if (d_gradients && oc.n_sets == 2 && !d_total_spin) return fail(PDG_BAD_ARGUMENT, "pdg_energy_gradients_open: null d_total_spin");
+    if (!ws || bytes < pdg_open_workspace_bytes(s, n_frames)) return fail(PDG_BAD_ARGUMENT, "workspace missing or too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    const FramePlan p = open_plan(s);
+    double *w = (double *)ws;
+    int rc;
+    if ((rc = integrals(s->d, p, n_frames, d_xyz, w, st))) return rc;
+    launch_scf_open(s->d, p, n_frames, d_phi, *o, oc, d_density, use_density, d_energies, d_charges, d_status, d_ncycles, w, st);
+    if ((rc = cuda_check(cudaGetLastError(), "open-shell scf kernel"))) return rc;
+    if (d_gradients) {
+        if (oc.n_sets == 2) {
+            launch_uhf_densities(n_frames, N, d_density, d_total_spin, st);
+            DeviceSystem dg = s->d;
+            dg.spin = d_total_spin + (size_t)n_frames * N * N;
+            launch_pair_gradients(dg, p, n_frames, d_xyz, d_total_spin, w, st, false);
+        } else {
+            launch_pair_gradients(s->d, p, n_frames, d_xyz, d_density, w, st, false);
+        }
+        launch_reduce_gradients(s->d, p, n_frames, w, d_gradients, st);
+        if ((rc = cuda_check(cudaGetLastError(), "gradient kernels"))) return rc;
+    }
+    return PDG_OK;
 }
 
 extern "C" int pdg_energy_gradients_uhf(pdg_system *s, int n_frames, const double *d_xyz, const double *d_phi, const pdg_scf_options *o,
@@ -392,33 +477,14 @@ extern "C" int pdg_energy_gradients_uhf(pdg_system *s, int n_frames, const doubl
                                         double *d_gradients, double *d_charges, int *d_status, int *d_ncycles, double *d_total_spin,
                                         void *ws, size_t bytes, void *stream)
 {
-    if (!s || n_frames <= 0) return fail(PDG_BAD_ARGUMENT, "pdg_energy_gradients_uhf: bad argument");
-    if (!o || !d_xyz || !d_density || !d_energies || !d_status || (d_gradients && !d_total_spin))
-        return fail(PDG_BAD_ARGUMENT, "pdg_energy_gradients_uhf: null argument");
-    if (o->history < 1 || o->history > PDG_MAX_HISTORY) return fail(PDG_BAD_ARGUMENT, "history must be 1..16");
-    if (o->maximum_scf_cycles < 0) return fail(PDG_BAD_ARGUMENT, "maximum_scf_cycles must be >= 0");
-    if (o->density_step != 0) return fail(PDG_BAD_ARGUMENT, "pdg_energy_gradients_uhf: the FP64 density step only (density_step 0)");
-    if (use_density < 0 || use_density > 2) return fail(PDG_BAD_ARGUMENT, "use_density must be 0, 1 or 2");
-    const int N = s->d.n_basis;
-    if (n_alpha < n_beta || n_beta < 0 || n_alpha > N || n_alpha + n_beta != s->d.n_electrons)
+    if (!s) return fail(PDG_BAD_ARGUMENT, "pdg_energy_gradients_uhf: bad argument");
+    if (n_alpha < n_beta || n_beta < 0 || n_alpha > s->d.n_basis || n_alpha + n_beta != s->d.n_electrons)
         return fail(PDG_BAD_ARGUMENT, "pdg_energy_gradients_uhf: n_alpha >= n_beta >= 0, n_alpha <= N and n_alpha + n_beta = the electrons");
-    if (!ws || bytes < pdg_uhf_workspace_bytes(s, n_frames, n_alpha, n_beta)) return fail(PDG_BAD_ARGUMENT, "workspace missing or too small");
-    cudaStream_t st = (cudaStream_t)stream;
-    const FramePlan p = uhf_plan(s, n_alpha, n_beta);
-    double *w = (double *)ws;
-    int rc;
-    if ((rc = integrals(s->d, p, n_frames, d_xyz, w, st))) return rc;
-    launch_scf_uhf(s->d, p, n_frames, d_phi, *o, n_alpha, n_beta, d_density, use_density, d_energies, d_charges, d_status, d_ncycles, w, st);
-    if ((rc = cuda_check(cudaGetLastError(), "spin-unrestricted scf kernel"))) return rc;
-    if (d_gradients) {
-        launch_uhf_densities(n_frames, N, d_density, d_total_spin, st);
-        DeviceSystem dg = s->d;
-        dg.spin = d_total_spin + (size_t)n_frames * N * N;
-        launch_pair_gradients(dg, p, n_frames, d_xyz, d_total_spin, w, st, false);
-        launch_reduce_gradients(s->d, p, n_frames, w, d_gradients, st);
-        if ((rc = cuda_check(cudaGetLastError(), "gradient kernels"))) return rc;
-    }
-    return PDG_OK;
+    pdg_occupancy occ = {};
+    occ.spin_restricted = 0; occ.occupancy_type = PDG_OCC_CARDINAL;
+    occ.alpha_charge = n_alpha; occ.beta_charge = n_beta;
+    return pdg_energy_gradients_open(s, n_frames, d_xyz, d_phi, o, &occ, d_density, use_density, d_energies, d_gradients, d_charges,
+                                     d_status, d_ncycles, d_total_spin, ws, bytes, stream);
 }
 
 // ---- shared base of the mixed method's perturbative density steps

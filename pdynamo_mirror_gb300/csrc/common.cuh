@@ -274,15 +274,26 @@ int launch_qcmm_gradients(int model, int n_frames, int n_qc, int n_mm, const dou
                           double *gqc, double *gmm, void *ws, cudaStream_t st);
 int launch_tc_selftest(int n, int kprod, int wait_limit, const float *x, float *c, int *status, cudaStream_t st);
 
+// Density sets and occupancies of the open-shell / fractional-occupancy SCF (k_scf_open): from pdg_occupancy by
+// occupancy_init's rules (QCOnePDM.c:290-330; host side, api.cu).
+struct OpenOccupancy {
+    int n_sets, type;        // 1 (restricted) or 2 sets; PDG_OCC_*
+    double factor;           // 2 (restricted) or 1
+    double charge[2];        // electrons of each set
+    int ncard[2], nfrac[2];  // full and fractional orbitals (cardinal, fixed fractional)
+    double frac[2];          // fraction of a full occupancy on each fractional orbital
+    double beta;             // Fermi broadening (variable fractional)
+};
+
 // SCF kernels (scf.cu), in two compiled variants: scf_n (256 threads per CTA, tensor-core step) and scf_w
 // (scf_wide.cu: 512 threads per CTA, FP64 only).  The single-system entry points use scf_n.
 #define PDG_SCF_LAUNCHERS                                                                                                   \
     void launch_scf(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *phi, const pdg_scf_options &o, \
                     double *density, int use_density, double *energies, double *charges, int *status, int *ncycles,      \
                     double *ws, int fock_only, double *fock_out, cudaStream_t st, const double *base = nullptr);          \
-    void launch_scf_uhf(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *phi, const pdg_scf_options &o,  \
-                        int n_alpha, int n_beta, double *density, int use_density, double *energies, double *charges,       \
-                        int *status, int *ncycles, double *ws, cudaStream_t st);                                              \
+    void launch_scf_open(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *phi, const pdg_scf_options &o, \
+                         const OpenOccupancy &oc, double *density, int use_density, double *energies, double *charges,       \
+                         int *status, int *ncycles, double *ws, cudaStream_t st);                                             \
     void launch_uhf_densities(int n_frames, int N, const double *P, double *out, cudaStream_t st);                       \
     int scf_occupancy(const DeviceSystem &s, int *threads, int *smem_bytes, int *ctas_per_sm);                           \
     void launch_batch_scf(const Batch &b, const int *order, int *queue, int grid, int smem_limit, size_t smem_bytes,     \
@@ -293,7 +304,7 @@ int launch_tc_selftest(int n, int kprod, int wait_limit, const float *x, float *
 namespace scf_n { PDG_SCF_LAUNCHERS }
 namespace scf_w { PDG_SCF_LAUNCHERS }
 using scf_n::launch_scf;
-using scf_n::launch_scf_uhf;
+using scf_n::launch_scf_open;
 using scf_n::launch_uhf_densities;
 using scf_n::scf_occupancy;
 void launch_guess_features(const DeviceSystem &s, int n_frames, const double *xyz, const double *phi, float *env, int *count,

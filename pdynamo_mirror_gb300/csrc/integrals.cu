@@ -17,13 +17,71 @@
 #define PI_D 3.14159265358979323846
 #define EXPONENT_TOLERANCE 25.0
 
-// Core-core repulsion and d/dr, non-diatomic branch (MNDOIntegralUtilities.c:35-150, :152-281).
+// PM6's diatomic core-core term and d/dr (MNDOIntegralUtilities.c:45-96 energy, :164-218 derivative): Z_a Z_b gamma
+// times 1 + 2 x_ab exp(-a_ab r_A r) for X-H pairs (X = C, N, O) or 1 + 2 x_ab exp(-a_ab r (1 + 0.0003 r_A^5)) for the
+// others, plus 9.28 exp(-5.98 r_A) for C-C and -0.0007 exp(-(r_A - 2.9)^2) for Si-O, plus the unpolarisable core
+// 1e-8 eV ((Z_a^1/3 + Z_b^1/3) / r_A)^12 (r_A: r in Angstroms).
+__device__ double core_core_pm6(const double *a, const double *b, int za, int zb, double r, double gam, double dgdr, double *dedr)
+{
+    const double B2A = PDG_BOHRS_TO_ANGSTROMS, rA = r * B2A;
+    const int kb = (int)b[PDG_E_INDEX];
+    double scale = 1.0, dscale = 0.0;
+    const double xij = 2.0 * a[PDG_E_DIAT_X + kb], aij = a[PDG_E_DIAT_A + kb];
+    if (xij != 0.0) {
+        const bool xh = (za == 1 && (zb == 6 || zb == 7 || zb == 8)) || (zb == 1 && (za == 6 || za == 7 || za == 8));
+        if (xh) {
+            const double f3 = xij * exp(-aij * r * r * B2A);
+            dscale -= 2.0 * aij * r * B2A * f3;
+            scale += f3;
+        } else {
+            const double r2 = rA * rA, dd = 0.0003 * r2 * r2 * rA, f3 = xij * exp(-aij * r * (1.0 + dd));
+            dscale -= aij * (1.0 + 6.0 * dd) * f3;
+            scale += f3;
+        }
+    }
+    if (za == 6 && zb == 6) {
+        const double f3 = 9.28 * exp(-5.98 * rA);
+        dscale -= 5.98 * B2A * f3;
+        scale += f3;
+    }
+    if ((za == 8 && zb == 14) || (za == 14 && zb == 8)) {
+        const double dd = rA - 2.9, f3 = -0.0007 * exp(-dd * dd);
+        dscale -= 2.0 * dd * B2A * f3;
+        scale += f3;
+    }
+    const double zz = a[PDG_E_ZCORE] * b[PDG_E_ZCORE];
+    const double UNPOLARIZABLE_CORE = 1.0e-08 / 27.21;   // 1e-8 eV in Hartree, as the reference writes it
+    const double u = (cbrt(a[PDG_E_ZCORE]) + cbrt(b[PDG_E_ZCORE])) / rA, u2 = u * u, u4 = u2 * u2, u12 = u4 * u4 * u4;
+    *dedr = zz * (dgdr * scale + gam * dscale) - 12.0 * UNPOLARIZABLE_CORE * u12 / r;
+    return zz * gam * scale + UNPOLARIZABLE_CORE * u12;
+}
+
+// Core-core repulsion and d/dr (MNDOIntegralUtilities.c:35-150, :152-281): the diatomic branch for PM6 elements,
+// else the exponential one; then the AM1/PM3 Gaussians and the PDDG terms.
 __device__ double core_core(const double *a, const double *b, double r, double *dedr)
 {
     const double B2A = PDG_BOHRS_TO_ANGSTROMS;
     int za = (int)a[PDG_E_Z], zb = (int)b[PDG_E_Z];
     double s8 = a[PDG_E_PO + 8] + b[PDG_E_PO + 8];
     double gam = rsqrt(r * r + s8 * s8), dgdr = -r * gam * gam * gam;
+    if (a[PDG_E_DIAT] != 0.0 && b[PDG_E_DIAT] != 0.0) {
+        double de, enuc = core_core_pm6(a, b, za, zb, r, gam, dgdr, &de), scale = 0.0, an = 0.0;
+        const double zz = a[PDG_E_ZCORE] * b[PDG_E_ZCORE], gg = a[PDG_E_GPHOT] * b[PDG_E_GPHOT];
+        for (int t = 0; t < 2; t++) {
+            const double *e = t ? b : a;
+            const int ng = (int)e[PDG_E_NG];
+            for (int i = 0; i < ng; i++) {
+                const double d = r - e[PDG_E_FN3 + i], ax = e[PDG_E_FN2 + i] * d * d;
+                if (ax <= EXPONENT_TOLERANCE) {
+                    const double ex = exp(-ax);
+                    scale += gg * zz / r * e[PDG_E_FN1 + i] * ex;
+                    an += e[PDG_E_FN1 + i] * (1.0 / (r * r) + e[PDG_E_FN2 + i] * 2.0 * d / r) * ex;
+                }
+            }
+        }
+        if (dedr) *dedr = de - an * gg * zz;
+        return enuc + scale;
+    }
     double alpa = a[PDG_E_ALP], alpb = b[PDG_E_ALP];
     double exi = exp(-alpa * r), exj = exp(-alpb * r);
     double scale = exi + exj;

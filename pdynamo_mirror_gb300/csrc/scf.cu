@@ -33,7 +33,14 @@ struct SCFArgs {
     double *ws; int fock_only; double *fock_out;
     int smem_limit;   // bytes of shared memory one CTA may plan for (the launch provides the plan's bytes)
     const double *base;   // shared base of the perturbative density steps (the mixed method), or null
-    int n_alpha, n_beta;  // spin-unrestricted SCF (k_scf_uhf): electrons of each spin
+    // open-shell and fractional-occupancy SCF (k_scf_open): the density sets and their occupancies
+    int n_sets;                      // 1: spin-restricted (the total density), 2: alpha and beta
+    int occ_type;                    // PDG_OCC_CARDINAL, PDG_OCC_FIXED_FRACTIONAL or PDG_OCC_VARIABLE_FRACTIONAL
+    double occ_factor;               // occupancy of a full orbital: 2 (restricted) or 1
+    double occ_charge[2];            // electrons of each set
+    int occ_ncard[2], occ_nfrac[2];  // fully and fractionally occupied orbitals (cardinal, fixed fractional)
+    double occ_frac[2];              // the fraction of occ_factor on each of the occ_nfrac orbitals
+    double fermi_beta;               // variable fractional: the Fermi broadening (1 / Hartree)
 };
 
 struct Smem {
@@ -597,7 +604,7 @@ __device__ void back_transform32(int N, float *work, const double *A, Smem &sm, 
 // (kv rows of ldz; z_in_smem when Z is the shared-memory slot).  The eigenvalues are left in sm.eig[0 .. kv).
 template <typename R>
 __device__ void tridiag_vectors(const SCFArgs &a, double *wsf, const double *A, Smem &sm, Timer &tm, int first, int kv, R *Z, int ldz,
-                                bool z_in_smem, bool count_step = true)
+                                bool z_in_smem, bool count_step = true, bool refine = false)
 {
     constexpr bool F32 = sizeof(R) == 4;
     const DeviceSystem &s = a.s;
@@ -678,6 +685,22 @@ __device__ void tridiag_vectors(const SCFArgs &a, double *wsf, const double *A, 
             __syncthreads();
         }
     }
+    if (refine) {
+        // eigenvalues to FP64 accuracy: the Rayleigh quotients z^T T z / z^T z of the inverse-iteration vectors (the
+        // multisection's shifts carry FP32 resolution, enough for the vectors but not for Fermi occupancies)
+        for (int t = tid; t < kv; t += PDG_BLOCK) {
+            const R *z = Z + (size_t)t * ldz;
+            double num = 0.0, den = 0.0;
+            for (int i = 0; i < N; i++) {
+                const double zi = (double)z[i];
+                den = fma(zi, zi, den);
+                num = fma(sm.d[i] * zi, zi, num);
+                if (i + 1 < N) num = fma(2.0 * sm.e[i] * zi, (double)z[i + 1], num);
+            }
+            sm.eig[t] = num / den;
+        }
+        __syncthreads();
+    }
     tm.lap(PDG_T_EIGENVECTORS);
     // --- back-transformation Z <- Q Z, Q = H_0 H_1 ... H_{N-3} with the reflectors stored in A
     if constexpr (F32) {
@@ -744,8 +767,14 @@ __device__ void tridiag_vectors(const SCFArgs &a, double *wsf, const double *A, 
     }
 }
 
+__device__ int occupancy_weights(const SCFArgs &a, int q, Smem &sm, double *wt);
+
+// One density step.  W false: P = 2 Z^T Z over the wanted vectors (closed shell).  W true (every eigenpair computed,
+// vec_occupied): P = sum_k w_k z_k z_k^T with the weights of density set occ_set's occupancies (occupancy_weights),
+// whose occupancy energy is left in sm.small[128].
+template <bool W = false>
 __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, double *P, Smem &sm, Timer &tm, bool make_base = false,
-                               int n_use = -1)
+                               int occ_set = 0)
 {
     const DeviceSystem &s = a.s;
     const FramePlan &pl = a.plan;
@@ -830,17 +859,21 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
     }
     __syncthreads();
     tm.lap(PDG_T_TRIDIAGONAL);
-    tridiag_vectors<double>(a, wsf, A, sm, tm, s.vec_occupied ? 0 : N - kv, kv, Z, ldz, sm.zs != nullptr);
+    tridiag_vectors<double>(a, wsf, A, sm, tm, s.vec_occupied ? 0 : N - kv, kv, Z, ldz, sm.zs != nullptr, true,
+                            W && a.occ_type == PDG_OCC_VARIABLE_FRACTIONAL);
     tm.lap(PDG_T_BACKTRANSFORM);
-    // --- P = 2 Z^T Z (occupied) or 2 (1 - Z^T Z) (virtual); lower triangle then mirrored.  n_use >= 0: the
-    //     leading n_use of the (occupied-side) vectors only, when all eigenpairs were computed
+    // --- P = 2 Z^T Z (occupied) or 2 (1 - Z^T Z) (virtual), or sum_k w_k z_k z_k^T; lower triangle then mirrored
     const bool occ = s.vec_occupied;
-    const int kuse = (n_use >= 0 && occ) ? n_use : kv;
+    double *wt = sm.part;   // per-vector weights (the tridiagonalisation's partial sums are dead here)
+    int kuse = kv;
+    if constexpr (W) kuse = occupancy_weights(a, occ_set, sm, wt);
     double rms = 0.0;
-    tgemm<false, false>(N, N, kuse, [&](int i, int k) { return Z[(size_t)k * ldz + i]; }, [&](int k, int j) { return Z[(size_t)k * ldz + j]; },
-                        true, sm, [&](int i, int j, double v) {
+    tgemm<false, false>(N, N, kuse, [&](int i, int k) { if constexpr (W) return wt[k] * Z[(size_t)k * ldz + i]; else return Z[(size_t)k * ldz + i]; },
+                        [&](int k, int j) { return Z[(size_t)k * ldz + j]; }, true, sm, [&](int i, int j, double v) {
         if (j > i) return;
-        const double pn = occ ? 2.0 * v : ((i == j ? 2.0 : 0.0) - 2.0 * v);
+        double pn;
+        if constexpr (W) pn = v;
+        else pn = occ ? 2.0 * v : ((i == j ? 2.0 : 0.0) - 2.0 * v);
         const double dlt = pn - P[(size_t)i * N + j];
         rms += (i == j) ? dlt * dlt : 2.0 * dlt * dlt;
         P[(size_t)i * N + j] = pn;
@@ -1818,20 +1851,84 @@ __device__ double sym_trace(int N, const double *X, const double *Y, Smem &sm)
     return 2.0 * t.x + t.y;
 }
 
-__device__ void scf_frame_uhf(const SCFArgs &a, const int f, double *shm)
+// Occupancy weights of density set q from the eigenvalues in sm.eig (every eigenpair, ascending), as
+// QCOnePDM_MakeFromFock forms the density (QCOnePDM.c:403-460, occupancies :505-599): cardinal and fixed-fractional
+// weights are fixed (occ_ncard full orbitals, then occ_nfrac at occ_frac); variable-fractional ones are Fermi-Dirac
+// occupancies at the Fermi energy of the reference's bisection (from [-1000, 1000] Hartree, only the lower bound
+// moves, until the electron count is within 1e-12), the orbitals above 1e-10 kept, with the occupancy energy
+// sum(p ln p + (1 - p) ln(1 - p)) / beta.  Weights (times occ_factor) go to wt; returns the number of weighted vectors
+// (the leading ones); the occupancy energy goes to sm.small[128].
+__device__ int occupancy_weights(const SCFArgs &a, int q, Smem &sm, double *wt)
+{
+    const int N = a.s.n_basis, tid = threadIdx.x, lane = tid & 31;
+    const double fac = a.occ_factor;
+    if (a.occ_type != PDG_OCC_VARIABLE_FRACTIONAL) {
+        const int nc = a.occ_ncard[q], nf = a.occ_nfrac[q];
+        const double fr = a.occ_frac[q] * fac;
+        for (int k = tid; k < N; k += PDG_BLOCK) wt[k] = k < nc ? fac : (k < nc + nf ? fr : 0.0);
+        if (tid == 0) sm.small[128] = 0.0;
+        __syncthreads();
+        return nc + nf;
+    }
+    if (tid < 32) {
+        const double target = a.occ_charge[q] / fac, beta = a.fermi_beta;
+        const double *ev = sm.eig;
+        auto fermi = [&](double ef, int k) {
+            const double e = -beta * (ef - ev[k]);
+            return e > 500.0 ? 0.0 : (e < -500.0 ? 1.0 : 1.0 / (1.0 + exp(e)));
+        };
+        double ef = 0.0;
+        if (target > 0.0) {
+            double lo = -1000.0, dx = 2000.0;
+            for (int it = 0; it < 500; it++) {
+                dx *= 0.5;
+                ef = lo + dx;
+                double t = 0.0;
+                for (int k = lane; k < N; k += 32) t += fermi(ef, k);
+                const double fm = warp_sum(t) - target;
+                if (fm <= 0.0) lo = ef;
+                if (fabs(fm) <= 1.0e-12) break;
+            }
+        }
+        int cnt = 0;
+        double e = 0.0;
+        for (int k = lane; k < N; k += 32) {
+            const double p = target > 0.0 ? fermi(ef, k) : 0.0, r = 1.0 - p;
+            wt[k] = p;
+            if (p > 1.0e-10) { cnt++; e += p * log(p); if (r > 1.0e-10) e += r * log(r); }
+        }
+        cnt = __reduce_add_sync(0xffffffffu, cnt);
+        e = warp_sum(e);
+        for (int k = lane; k < N; k += 32) wt[k] = k < cnt ? wt[k] * fac : 0.0;
+        if (lane == 0) { sm.small[128] = e / beta * fac; sm.iv[40] = cnt; }
+    }
+    __syncthreads();
+    return sm.iv[40];
+}
+
+// The open-shell and fractional-occupancy SCF of frame f (QCModelMNDO_Fock over the density sets, QCOnePDM_MakeFromFock
+// with the sets' occupancies, DIISSCFConverger over the sets): one set (spin-restricted, the total density, occupancy
+// factor 2) or two (alpha and beta, factor 1).  The sets' Fock matrices are J(P_total) - K(P_spin) + H (the restricted
+// set's with P_spin = P / 2); the electronic energy adds the occupancy energy of the densities in use (zero but for
+// variable fractional occupancies).  DIIS B entries and ODA traces are summed over the sets, the largest DIIS error is
+// doubled for two sets, both sets are extrapolated or mixed with the same coefficients (DIISSCFConverger.c:385-528,
+// 661-760).  The workspace holds two frame slots per frame: slot f has the integrals and set 0's matrices, slot
+// n_frames + f set 1's (or the restricted set's P / 2).  Densities: n_sets per frame, N x N each.
+__device__ void scf_frame_open(const SCFArgs &a, const int f, double *shm)
 {
     const DeviceSystem &s = a.s;
     const FramePlan &pl = a.plan;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, N = s.n_basis;
     const size_t NN = (size_t)N * N;
-    const int nsp[2] = { a.n_alpha, a.n_beta };
+    const int ns = a.n_sets;
     Smem sm = carve(shm, N, N, a.smem_limit);
     double *wsp[2] = { a.ws + (size_t)f * pl.stride, a.ws + (size_t)(a.n_frames + f) * pl.stride };
     double *H = wsp[0] + pl.H;
     const double *tei = wsp[0] + pl.tei;
     double *Fs[2] = { wsp[0] + pl.F, wsp[1] + pl.F };
-    double *Ps[2] = { a.density + (size_t)(2 * f) * NN, a.density + (size_t)(2 * f + 1) * NN };
-    double *Pt = wsp[1] + pl.P0;
+    double *Ps[2] = { a.density + (size_t)(ns * f) * NN, a.density + (size_t)(ns * f + ns - 1) * NN };
+    double *Pt = wsp[1] + pl.P0;   // the total density (two sets) or half the density (one set)
+    const double *Ptot = ns == 2 ? Pt : Ps[0];
     double *Bm = wsp[0] + pl.misc;
     Timer tm;
     tm.slot = wsp[0] + pl.misc + PDG_MAX_HISTORY * PDG_MAX_HISTORY;
@@ -1845,19 +1942,20 @@ __device__ void scf_frame_uhf(const SCFArgs &a, const int f, double *shm)
     double base = 0.0;
     for (int A = tid; A < s.n_atoms; A += PDG_BLOCK) { const double *E = elem(s, s.atom_elem[A]); base += E[PDG_E_EHEAT] - E[PDG_E_EISOL]; }
     base = block_sum(base, sm.red);
-    // the density steps compute every eigenpair of each spin's matrix (the occupied/virtual boundary then lies
-    // inside the vectors the inverse iteration orthogonalises, so a near-degenerate pair across it cannot mix) and
-    // form the density from the n_s lowest (occupancy 1: the step's 2 Z^T Z halved)
+    // the density steps compute every eigenpair of each set's matrix (the occupied/virtual boundary then lies
+    // inside the vectors the inverse iteration orthogonalises, so a near-degenerate pair across it cannot mix, and
+    // fractional occupancies need the orbitals on both sides of it) and weight them with the set's occupancies
     SCFArgs as = a;
     as.s.vec_occupied = 1;
     as.s.n_vec = N;
     bool valid = a.use_density == 1;
     if (a.use_density != 1)
-        for (int q = 0; q < 2; q++) {   // uniform diagonal guess per spin (QCOnePDM.c:326-331)
-            const double g = (double)nsp[q] / (double)N;
+        for (int q = 0; q < ns; q++) {   // uniform diagonal guess per set (QCOnePDM.c:326-331)
+            const double g = a.occ_charge[q] / (double)N;
             for (size_t k = tid; k < NN; k += PDG_BLOCK) Ps[q][k] = ((k / N) == (k % N)) ? g : 0.0;
         }
     __syncthreads();
+    double eocc[2] = { 0.0, 0.0 };   // occupancy energies of the densities in use (none for a start density)
     const pdg_scf_options &o = a.o;
     const int hist = o.history, hl = pl.hist_len;
     int *ctl = sm.iv;
@@ -1869,11 +1967,12 @@ __device__ void scf_frame_uhf(const SCFArgs &a, const int f, double *shm)
     const double *phi = a.phi ? a.phi + (size_t)f * s.n_atoms : nullptr;
     __syncthreads();
     while (iteration < o.maximum_scf_cycles && !converged) {
-        for (size_t k = tid; k < NN; k += PDG_BLOCK) Pt[k] = Ps[0][k] + Ps[1][k];
+        for (size_t k = tid; k < NN; k += PDG_BLOCK) Pt[k] = ns == 2 ? Ps[0][k] + Ps[1][k] : 0.5 * Ps[0][k];
         __syncthreads();
         e1 = e2 = 0.0;
-        for (int q = 0; q < 2; q++) {
-            fock_build_spin(a, H, Pt, Ps[q], Fs[q], tei, sm, wsp[q] + pl.G);
+        for (int q = 0; q < ns; q++) {
+            if (ns == 2) fock_build_spin(a, H, Pt, Ps[q], Fs[q], tei, sm, wsp[q] + pl.G);
+            else fock_build_spin(a, H, Ps[0], Pt, Fs[0], tei, sm, wsp[0] + pl.G);
             const double th = sym_trace(N, Ps[q], H, sm), tf = sym_trace(N, Ps[q], Fs[q], sm);
             e1 += th;
             e2 += 0.5 * (tf - th);
@@ -1883,17 +1982,18 @@ __device__ void scf_frame_uhf(const SCFArgs &a, const int f, double *shm)
         for (int A = tid; A < s.n_atoms; A += PDG_BLOCK) {
             const int no = s.atom_norb[A], as0 = s.atom_start[A];
             double ps = 0.0;
-            for (int m = 0; m < no; m++) ps += Pt[(size_t)(as0 + m) * N + as0 + m];
+            for (int m = 0; m < no; m++) ps += Ptot[(size_t)(as0 + m) * N + as0 + m];
             const double q = elem(s, s.atom_elem[A])[PDG_E_ZCORE] - ps;
             if (a.charges) a.charges[(size_t)f * s.n_atoms + A] = q;
             if (phi) {
                 tq += q * phi[A];
-                for (int m = 0; m < no; m++) { Fs[0][(size_t)(as0 + m) * N + as0 + m] -= phi[A]; Fs[1][(size_t)(as0 + m) * N + as0 + m] -= phi[A]; }
+                for (int m = 0; m < no; m++)
+                    for (int r = 0; r < ns; r++) Fs[r][(size_t)(as0 + m) * N + as0 + m] -= phi[A];
             }
         }
         eq = block_sum(tq, sm.red);
         tm.lap(PDG_T_FOCK);
-        eel = e1 + e2 + eq;
+        eel = eocc[0] + eocc[1] + e1 + e2 + eq;
         if (!isfinite(eel)) { st = PDG_NAN; break; }
         converged = (iteration > 0) && (rms <= o.density_tolerance) && (deltaeold <= o.energy_tolerance);
         if (converged) break;
@@ -1909,7 +2009,7 @@ __device__ void scf_frame_uhf(const SCFArgs &a, const int f, double *shm)
             const int newest = ctl[20], matnum = ctl[1];
             double emx = 0.0, dots[PDG_MAX_HISTORY];
             for (int m = 0; m < PDG_MAX_HISTORY; m++) dots[m] = 0.0;
-            for (int q = 0; q < 2; q++) {
+            for (int q = 0; q < ns; q++) {
                 double *wq = wsp[q];
                 double *hp = wq + pl.hP + (size_t)newest * hl, *hf = wq + pl.hF + (size_t)newest * hl, *he = wq + pl.hE + (size_t)newest * hl;
                 for (int i = w; i < N; i += PDG_WARPS)
@@ -1931,7 +2031,7 @@ __device__ void scf_frame_uhf(const SCFArgs &a, const int f, double *shm)
                     for (int m = 0; m < matnum; m++) dots[m] += wq[pl.hE + (size_t)ctl[2 + m] * hl + k] * en_;
                 }
             }
-            const double maxerr = 2.0 * block_max(emx, sm.red);   // two density sets: the largest error doubled
+            const double maxerr = (ns == 2 ? 2.0 : 1.0) * block_max(emx, sm.red);   // two density sets: the largest error doubled
             {
                 double *rs = sm.ta;
                 for (int m = 0; m < matnum; m++) {
@@ -1984,7 +2084,7 @@ __device__ void scf_frame_uhf(const SCFArgs &a, const int f, double *shm)
                     __syncthreads();
                     if (ctl[21]) {
                         const int mn = ctl[1];
-                        for (int q = 0; q < 2; q++)
+                        for (int q = 0; q < ns; q++)
                             for (int e = tid; e < hl; e += PDG_BLOCK) {
                                 int i = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
                                 while ((i + 1) * (i + 2) / 2 <= e) i++;
@@ -2001,9 +2101,9 @@ __device__ void scf_frame_uhf(const SCFArgs &a, const int f, double *shm)
                         __syncthreads();
                     }
                 } else if (o.use_rca && qrca && rca_prev) {
-                    // RCA_Iterate over both sets: the four traces summed (DIISSCFConverger.c:661-760)
+                    // RCA_Iterate over the sets: the four traces summed (DIISSCFConverger.c:661-760)
                     double t1 = 0, t2 = 0, t3 = 0, t4 = 0;
-                    for (int q = 0; q < 2; q++) {
+                    for (int q = 0; q < ns; q++) {
                         const double *rP = wsp[q] + pl.rP, *rF = wsp[q] + pl.rF;
                         for (size_t k = tid; k < NN; k += PDG_BLOCK) {
                             t1 += Fs[q][k] * Ps[q][k]; t2 += Fs[q][k] * rP[k]; t3 += rF[k] * Ps[q][k]; t4 += rF[k] * rP[k];
@@ -2028,7 +2128,7 @@ __device__ void scf_frame_uhf(const SCFArgs &a, const int f, double *shm)
                     }
                     mu = fmax(mu, 0.01);
                     const double nu = 1.0 - mu;
-                    for (int q = 0; q < 2; q++) {
+                    for (int q = 0; q < ns; q++) {
                         const double *rP = wsp[q] + pl.rP, *rF = wsp[q] + pl.rF;
                         for (size_t k = tid; k < NN; k += PDG_BLOCK) { Ps[q][k] = mu * Ps[q][k] + nu * rP[k]; Fs[q][k] = mu * Fs[q][k] + nu * rF[k]; }
                     }
@@ -2038,7 +2138,7 @@ __device__ void scf_frame_uhf(const SCFArgs &a, const int f, double *shm)
             }
             rca_prev = false;
             if (o.use_rca) {   // RCA_Save every cycle, as the reference does (DIISSCFConverger.c:231-235)
-                for (int q = 0; q < 2; q++) {
+                for (int q = 0; q < ns; q++) {
                     double *rP = wsp[q] + pl.rP, *rF = wsp[q] + pl.rF;
                     for (size_t k = tid; k < NN; k += PDG_BLOCK) { rP[k] = Ps[q][k]; rF[k] = Fs[q][k]; }
                 }
@@ -2050,40 +2150,29 @@ __device__ void scf_frame_uhf(const SCFArgs &a, const int f, double *shm)
         deltaeold = deltae; eold = etemp;
         __syncthreads();
         tm.lap(PDG_T_ITERATE);
-        // one density step per spin (the step builds 2 Z^T Z: the spin's density is doubled before and halved after)
+        // one density step per set, with its occupancies
         rms = 0.0;
-        for (int q = 0; q < 2; q++) {
-            double *P = Ps[q];
-            if (nsp[q] == 0) {
-                double d2 = 0.0;
-                for (size_t k = tid; k < NN; k += PDG_BLOCK) { d2 += P[k] * P[k]; P[k] = 0.0; }
-                rms = fmax(rms, sqrt(block_sum(d2, sm.red)) / (double)N);
-                continue;
-            }
-            for (size_t k = tid; k < NN; k += PDG_BLOCK) P[k] *= 2.0;
+        for (int q = 0; q < ns; q++) {
+            rms = fmax(rms, density_step<true>(as, wsp[q], Fs[q], Ps[q], sm, tm, false, q));
+            eocc[q] = sm.small[128];
             __syncthreads();
-            as.s.n_occ = nsp[q];
-            const double r = density_step(as, wsp[q], Fs[q], P, sm, tm, false, nsp[q]);
-            for (size_t k = tid; k < NN; k += PDG_BLOCK) P[k] *= 0.5;
-            __syncthreads();
-            rms = fmax(rms, 0.5 * r);
         }
         valid = true;
     }
     if (converged) st = PDG_OK;
     if (tid == 0) {
         double *E = a.energies + (size_t)f * PDG_NENERGY;
-        E[0] = eel; E[1] = e1 + e2; E[2] = en; E[3] = base; E[4] = eq; E[5] = e1; E[6] = e2; E[7] = rms;
+        E[0] = eel; E[1] = eel - eq; E[2] = en; E[3] = base; E[4] = eq; E[5] = e1; E[6] = e2; E[7] = rms;
         a.status[f] = st;
         if (a.ncycles) a.ncycles[f] = iteration;
         tm.slot[PDG_T_TOTAL] = (double)(clock64() - t_begin);
     }
 }
 
-__global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf_uhf(SCFArgs a)
+__global__ void __launch_bounds__(PDG_BLOCK, PDG_SCF_CTAS_PER_SM) k_scf_open(SCFArgs a)
 {
     extern __shared__ __align__(128) double shm[];
-    scf_frame_uhf(a, blockIdx.x, shm);
+    scf_frame_open(a, blockIdx.x, shm);
 }
 
 // Tensor memory (256 columns) and the completion mbarrier of the purification density step, for CTAs that may
@@ -2227,22 +2316,25 @@ void launch_uhf_densities(int n_frames, int N, const double *P, double *out, cud
     k_uhf_densities<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, (size_t)N * N, P, out);
 }
 
-void launch_scf_uhf(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *phi, const pdg_scf_options &o, int n_alpha,
-                    int n_beta, double *density, int use_density, double *energies, double *charges, int *status, int *ncycles, double *ws,
-                    cudaStream_t st)
+void launch_scf_open(const DeviceSystem &s, const FramePlan &p, int n_frames, const double *phi, const pdg_scf_options &o,
+                     const OpenOccupancy &oc, double *density, int use_density, double *energies, double *charges, int *status,
+                     int *ncycles, double *ws, cudaStream_t st)
 {
     SCFArgs a = {};
     a.s = s; a.plan = p; a.n_frames = n_frames; a.phi = phi; a.o = o; a.density = density; a.use_density = use_density;
     a.energies = energies; a.charges = charges; a.status = status; a.ncycles = ncycles; a.ws = ws;
     a.fock_only = 0; a.fock_out = nullptr; a.smem_limit = PDG_SMEM_LIMIT; a.base = nullptr;
-    a.n_alpha = n_alpha; a.n_beta = n_beta;
-    const int N = s.n_basis;
-    const size_t sm = scf_smem_bytes(N, N);   // every eigenpair (scf_frame_uhf)
-    if (sm > 48 * 1024) {
-        cudaFuncSetAttribute(k_scf_uhf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        cudaFuncSetAttribute(k_scf_uhf, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    a.n_sets = oc.n_sets; a.occ_type = oc.type; a.occ_factor = oc.factor; a.fermi_beta = oc.beta;
+    for (int q = 0; q < 2; q++) {
+        a.occ_charge[q] = oc.charge[q]; a.occ_ncard[q] = oc.ncard[q]; a.occ_nfrac[q] = oc.nfrac[q]; a.occ_frac[q] = oc.frac[q];
     }
-    k_scf_uhf<<<n_frames, PDG_BLOCK, sm, st>>>(a);
+    const int N = s.n_basis;
+    const size_t sm = scf_smem_bytes(N, N);   // every eigenpair (scf_frame_open)
+    if (sm > 48 * 1024) {
+        cudaFuncSetAttribute(k_scf_open, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_scf_open, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    }
+    k_scf_open<<<n_frames, PDG_BLOCK, sm, st>>>(a);
 }
 
 void launch_batch_scf(const Batch &b, const int *order, int *queue, int grid, int smem_limit, size_t smem_bytes, int tensor_items,

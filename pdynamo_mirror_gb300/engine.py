@@ -54,7 +54,7 @@ class QCEngine:
         self.n_atoms, self.n_basis, self.n_occupied, self.n_pairs = len(self.atomic_numbers), nb.value, no.value, npair.value
         from .parameters import E_ZCORE
         self.n_electrons = int(round(sum(self._records[k][E_ZCORE] for k in self._index))) - int(charge)
-        self.density_uhf = None      # device [F, 2, N, N] (alpha, beta) of the last spin-unrestricted run
+        self.density_open = None     # device [F, n_sets, N, N] of the last open-shell / fractional-occupancy run
         self._ws, self._ws_frames = None, 0
         self._qcmm_ws = None
         self.wide = (self.n_basis > WIDE_BASIS) if wide is None else bool(wide)
@@ -199,20 +199,28 @@ class QCEngine:
 
     def run_uhf(self, qc_xyz, converger, n_alpha, n_beta, mm_xyz=None, mm_charges=None, nbmodel=None, gradients=True, warm_start=True,
                 mm_gradients=True):
-        """The spin-unrestricted E + gradient of frames qc_xyz [F, n, 3] (A) with n_alpha and n_beta electrons
-        (pdg_energy_gradients_uhf; the FP64 method), starting from the previous run's alpha and beta densities when
-        warm_start and the shapes match, else from the diagonal guess.  Returns run()'s dict plus "density_alpha",
-        "density_beta", "density" (total) and "spin_density" (device, [F, N, N]; the last two with gradients)."""
+        """The spin-unrestricted E + gradient with n_alpha and n_beta electrons in cardinal occupancies: run_open."""
+        occ = _native.Occupancy(spin_restricted=0, occupancy_type=0, alpha_charge=float(n_alpha), beta_charge=float(n_beta))
+        return self.run_open(qc_xyz, converger, occ, mm_xyz, mm_charges, nbmodel, gradients, warm_start, mm_gradients)
+
+    def run_open(self, qc_xyz, converger, occupancy, mm_xyz=None, mm_charges=None, nbmodel=None, gradients=True, warm_start=True,
+                 mm_gradients=True):
+        """The open-shell or fractional-occupancy E + gradient of frames qc_xyz [F, n, 3] (A) with the density sets and
+        occupancies of occupancy (a _native.Occupancy; pdg_energy_gradients_open, the FP64 method), starting from the
+        previous run's densities when warm_start and the shapes match, else from the diagonal guess.  Returns run()'s
+        dict plus "density_sets" (device [F, n_sets, N, N]: the total density, or alpha and beta), "density" (total)
+        and, for two sets, "density_alpha", "density_beta" and "spin_density" (the last with gradients)."""
         F = qc_xyz.shape[0]
         n, N = self.n_atoms, self.n_basis
+        ns = 1 if occupancy.spin_restricted else 2
         dev = self.device
         stream = torch.cuda.current_stream(dev)
         sh = _native.stream_handle(stream)
         opts = converger.options()
         if opts.density_step != 0:
-            raise ValueError("The spin-unrestricted method runs the FP64 density step (densityStep 'fp64').")
+            raise ValueError("Open-shell and fractional-occupancy states run the FP64 density step (densityStep 'fp64').")
         if self.wide:
-            raise ValueError("The spin-unrestricted method runs one CTA per frame (at most %d basis functions)." % WIDE_BASIS)
+            raise ValueError("Open-shell and fractional-occupancy states run one CTA per frame (at most %d basis functions)." % WIDE_BASIS)
         phi = None
         qcmm = nbmodel is not None and mm_xyz is not None and mm_xyz.shape[1] > 0
         if qcmm:
@@ -223,29 +231,35 @@ class QCEngine:
             _native.check(self.L.pdg_qcmm_potentials(nbmodel.model_id, F, n, mm_xyz.shape[1], _native.ptr(qc_xyz), _native.ptr(mm_xyz),
                                                      _native.ptr(mm_charges), nk, _native.ptr(knots), float(nbmodel.outerCutoff),
                                                      _native.ptr(phi), _native.ptr(qws), qwb, sh), "pdg_qcmm_potentials")
-        need = int(self.L.pdg_uhf_workspace_bytes(self.handle, F, int(n_alpha), int(n_beta)))
-        if getattr(self, "_uhf_ws", None) is None or self._uhf_ws.numel() < need:
-            self._uhf_ws = torch.empty(need, dtype=torch.uint8, device=dev)
-        ws = self._uhf_ws
-        use = 1 if (warm_start and self.density_uhf is not None and self.density_uhf.shape[0] == F) else 0
+        need = int(self.L.pdg_open_workspace_bytes(self.handle, F))
+        if getattr(self, "_open_ws", None) is None or self._open_ws.numel() < need:
+            self._open_ws = torch.empty(need, dtype=torch.uint8, device=dev)
+        ws = self._open_ws
+        use = 1 if (warm_start and self.density_open is not None and tuple(self.density_open.shape[:2]) == (F, ns)) else 0
         if not use:
-            self.density_uhf = torch.empty((F, 2, N, N), dtype=torch.float64, device=dev)
+            self.density_open = torch.empty((F, ns, N, N), dtype=torch.float64, device=dev)
         xyz_bohr = (qc_xyz * ANGSTROMS_TO_BOHRS).contiguous()
         energies = torch.empty((F, _native.NENERGY), dtype=torch.float64, device=dev)
         grad = torch.empty((F, n, 3), dtype=torch.float64, device=dev) if gradients else None
-        ts = torch.empty((2, F, N, N), dtype=torch.float64, device=dev) if gradients else None
+        ts = torch.empty((2, F, N, N), dtype=torch.float64, device=dev) if (gradients and ns == 2) else None
         charges = torch.empty((F, n), dtype=torch.float64, device=dev)
         status = torch.empty(F, dtype=torch.int32, device=dev)
         ncycles = torch.empty(F, dtype=torch.int32, device=dev)
         self._attach_side(None)
-        _native.check(self.L.pdg_energy_gradients_uhf(self.handle, F, _native.ptr(xyz_bohr), _native.ptr(phi), ctypes.byref(opts),
-                                                      int(n_alpha), int(n_beta), _native.ptr(self.density_uhf), use, _native.ptr(energies),
-                                                      _native.ptr(grad), _native.ptr(charges), _native.ptr(status), _native.ptr(ncycles),
-                                                      _native.ptr(ts), _native.ptr(ws), ws.numel(), sh), "pdg_energy_gradients_uhf")
-        out = dict(energies=energies, qc_gradients=grad, charges=charges, status=status, ncycles=ncycles, phi=phi,
-                   density_alpha=self.density_uhf[:, 0], density_beta=self.density_uhf[:, 1])
-        if gradients:
-            out.update(density=ts[0], spin_density=ts[1])
+        _native.check(self.L.pdg_energy_gradients_open(self.handle, F, _native.ptr(xyz_bohr), _native.ptr(phi), ctypes.byref(opts),
+                                                       ctypes.byref(occupancy), _native.ptr(self.density_open), use, _native.ptr(energies),
+                                                       _native.ptr(grad), _native.ptr(charges), _native.ptr(status), _native.ptr(ncycles),
+                                                       _native.ptr(ts), _native.ptr(ws), ws.numel(), sh), "pdg_energy_gradients_open")
+        D = self.density_open
+        out = dict(energies=energies, qc_gradients=grad, charges=charges, status=status, ncycles=ncycles, phi=phi, density_sets=D)
+        if ns == 1:
+            out.update(density=D[:, 0])
+        else:
+            out.update(density_alpha=D[:, 0], density_beta=D[:, 1])
+            if gradients:
+                out.update(density=ts[0], spin_density=ts[1])
+            else:
+                out.update(density=D[:, 0] + D[:, 1])
         if qcmm and gradients:
             gqc = torch.empty((F, n, 3), dtype=torch.float64, device=dev)
             gmm = torch.empty((F, mm_xyz.shape[1], 3), dtype=torch.float64, device=dev) if mm_gradients else None

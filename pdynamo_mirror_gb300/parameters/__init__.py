@@ -9,7 +9,9 @@ The numbers come from ``mndo_parameters.json`` (generated from pDynamo's YAML fi
   ``MNDOParameters.c:762-875``, with ``AIJL`` :726 and ``POIJ`` :880),
 * STO-6G orbital shells: primitive unnormalisation, exponent scaling by zeta^2 and renormalisation of
   the contracted function (``GaussianBasis_UnnormalizePrimitives`` / ``_ScaleExponents`` /
-  ``_Normalize``, ``GaussianBasisCore.c:221,280,309``; ``pMolecule.QCParameters.pyx:131-140``).
+  ``_Normalize``, ``GaussianBasisCore.c:221,280,309``; ``pMolecule.QCParameters.pyx:131-140``),
+* PM6's diatomic core-core pairs (``pMolecule.MNDOParameters.pyx:259-276``, exponents to bohr^-1 :358-363),
+  stored per partner by the partner's index in the system's element list (``element_table``).
 
 The output record layout is ``PDG_ELEMENT_STRIDE`` doubles per element as declared in ``include/pdg.h``.
 """
@@ -21,7 +23,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 TABLE_PATH = os.path.join(HERE, "mndo_parameters.json")
 
-HAMILTONIANS = ("am1", "mndo", "pm3", "pddgmndo", "pddgpm3", "rm1")
+HAMILTONIANS = ("am1", "mndo", "pm3", "pddgmndo", "pddgpm3", "rm1", "pm6")
 
 # pCore Units (pCore/Units.py:43-44) and pMolecule.MNDOParameters.pyx:18-21.
 BOHRS_TO_ANGSTROMS = 5.291772083e-11 / 1.0e-10
@@ -31,11 +33,13 @@ HARTREES_TO_KCAL = 27.2113834 * 23.060529
 HARTREES_TO_KJ = 2625.5
 
 # Record offsets (include/pdg.h).
-STRIDE = 96
+STRIDE = 128
 E_Z, E_NORB, E_ZCORE, E_ALP, E_GPHOT, E_NG, E_NPDDG, E_DD, E_QQ, E_PO = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9
 E_GSS, E_GSP, E_GPP, E_GP2, E_HSP, E_HPP = 18, 19, 20, 21, 22, 23
 E_BETA, E_USPD, E_FN1, E_FN2, E_FN3, E_PDDGC, E_PDDGE = 24, 28, 32, 36, 40, 44, 48
 E_EHEAT, E_EISOL, E_NSHELL, E_NPRIM_S, E_NPRIM_P, E_EXP_S, E_CCBF_S, E_EXP_P, E_CCBF_P = 52, 53, 54, 55, 56, 57, 63, 69, 75
+E_DIAT, E_INDEX, E_DIAT_A, E_DIAT_X = 81, 82, 84, 100
+MAX_ELEMENTS = 16
 
 _TABLE = None
 
@@ -125,6 +129,8 @@ class ElementParameters:
         self.fn3 = [x[2] / BOHRS_TO_ANGSTROMS for x in raw["gaussians"]]
         self.pddgc = [x[0] / HARTREES_TO_EV for x in raw["pddg"]]
         self.pddge = [x[1] / BOHRS_TO_ANGSTROMS for x in raw["pddg"]]
+        # PM6 diatomic pairs: partner atomic number -> (coefficient x, exponent a in bohr^-1)
+        self.diatomic = {int(d[0]): (float(d[1]), float(d[2]) * BOHRS_TO_ANGSTROMS) for d in raw.get("diatomic", [])}
         self._fill_ddp_po()
         label = ("%ds" % raw["qns"] if raw["qns"] else "") + ("%dp" % raw["qnp"] if raw["qnp"] else "")
         if label not in t["bases"]:
@@ -175,7 +181,9 @@ class ElementParameters:
             c = c / math.sqrt(float(c @ ov @ c))
             self.shells.append((l, e, c))
 
-    def record(self):
+    def record(self, elements=None):
+        """The device record; elements (the system's sorted element list) places the element's own index and its
+        PM6 diatomic pairs by partner index."""
         r = np.zeros(STRIDE, dtype=np.float64)
         r[E_Z], r[E_NORB], r[E_ZCORE], r[E_ALP], r[E_GPHOT] = self.Z, self.norbitals, self.zcore, self.alp, self.gphot
         r[E_NG], r[E_NPDDG], r[E_DD], r[E_QQ] = len(self.fn1), len(self.pddgc), self.dd, self.qq
@@ -193,12 +201,20 @@ class ElementParameters:
             r[on] = n
             r[oe:oe + n] = e
             r[oc:oc + n] = c
+        if elements is not None:
+            if len(elements) > MAX_ELEMENTS:
+                raise ValueError("more than %d elements in one QC region" % MAX_ELEMENTS)
+            r[E_INDEX] = elements.index(self.Z)
+            r[E_DIAT] = 1.0 if self.diatomic else 0.0
+            for k, z in enumerate(elements):
+                x, a = self.diatomic.get(int(z), (0.0, 0.0))
+                r[E_DIAT_X + k], r[E_DIAT_A + k] = x, a
         return r
 
 
 def element_table(hamiltonian, atomic_numbers):
     """Sorted distinct elements, their stacked records, and the per-atom element index."""
     elements = sorted(set(int(z) for z in atomic_numbers))
-    records = np.stack([ElementParameters(hamiltonian, z).record() for z in elements])
+    records = np.stack([ElementParameters(hamiltonian, z).record(elements) for z in elements])
     index = np.array([elements.index(int(z)) for z in atomic_numbers], dtype=np.int32)
     return elements, records, index

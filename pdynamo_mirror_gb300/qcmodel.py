@@ -2,9 +2,10 @@
 
 Mirrors the keyword surface of pDynamo's QCModelMNDO (pMolecule.QCModelMNDO.pyx:511-621): the first
 positional argument or ``mndoModel`` names the Hamiltonian; ``converger`` takes a DIISSCFConverger.
-Spin-restricted closed shells (RHF) and spin-unrestricted states (UHF, ``isSpinRestricted=False``; with the
-ElectronicState's multiplicity) with cardinal occupancies are on this path; fractional occupancies raise
-ValueError, as unknown options do in the reference.
+Spin-restricted closed shells (RHF), spin-unrestricted states (UHF, ``isSpinRestricted=False``; with the
+ElectronicState's multiplicity) and the fractional occupancies (``occupancyType`` "Fixed Fractional" with the
+``numberFractional*HOOs`` / ``LUOs`` options, "Variable Fractional" with ``fermiBroadening``) are on this path;
+unknown options raise ValueError, as in the reference.
 """
 
 import numpy as np
@@ -20,6 +21,11 @@ class QCModelMNDO:
         self.label = None
         self.isSpinRestricted = True
         self.keepOrbitalData = False
+        # occupancy options and their defaults (QCModelMNDO_Allocate in the reference's C core)
+        self.occupancyType = "Cardinal"
+        self.fermiBroadening = 1.0e3
+        self.numberFractional = {"numberFractionalHOOs": 1, "numberFractionalLUOs": 0, "numberFractionalAlphaHOOs": 1,
+                                 "numberFractionalAlphaLUOs": 0, "numberFractionalBetaHOOs": 1, "numberFractionalBetaLUOs": 0}
         if len(arguments) > 1:
             raise ValueError("QCModelMNDO takes at most one positional argument.")
         if arguments:
@@ -33,8 +39,13 @@ class QCModelMNDO:
         if "keepOrbitalData" in options: self.keepOrbitalData = bool(options.pop("keepOrbitalData"))
         if "isSpinRestricted" in options: self.isSpinRestricted = bool(options.pop("isSpinRestricted"))
         if "occupancyType" in options:
-            if options.pop("occupancyType") != "Cardinal":
-                raise ValueError("Only cardinal occupancies are on this path.")
+            t = options.pop("occupancyType")
+            if t not in ("Cardinal", "Fixed Fractional", "Variable Fractional"):
+                raise ValueError("Unknown occupancy type: " + str(t) + ".")
+            self.occupancyType = t
+        if "fermiBroadening" in options: self.fermiBroadening = float(options.pop("fermiBroadening"))
+        for k in list(self.numberFractional):
+            if k in options: self.numberFractional[k] = int(options.pop(k))
         if options:
             raise ValueError("Invalid options: " + ", ".join(sorted(options)) + ".")
         self.mndoModel = str(self.mndoModel).lower()
@@ -46,11 +57,10 @@ class QCModelMNDO:
             self.label = self.mndoModel.upper()
 
     def GetOption(self, optionName):
-        """An option of the model (QCModelMNDO.GetOption, pMolecule.QCModelMNDO.pyx:306-318): the occupancy options
-        of the closed-shell cardinal states on this path; AttributeError for unknown names."""
-        values = {"isSpinRestricted": self.isSpinRestricted, "occupancyType": "Cardinal", "numberFractionalHOOs": 1, "numberFractionalLUOs": 0,
-                  "numberFractionalAlphaHOOs": 1, "numberFractionalAlphaLUOs": 0, "numberFractionalBetaHOOs": 1,
-                  "numberFractionalBetaLUOs": 0}
+        """An option of the model (QCModelMNDO.GetOption, pMolecule.QCModelMNDO.pyx:306-318): the occupancy options;
+        AttributeError for unknown names."""
+        values = dict(self.numberFractional, isSpinRestricted=self.isSpinRestricted, occupancyType=self.occupancyType,
+                      fermiBroadening=self.fermiBroadening)
         if optionName not in values:
             raise AttributeError("Unknown option: " + str(optionName) + ".")
         return values[optionName]

@@ -9,6 +9,8 @@ pMolecule/System.py:182-318: energies are returned in kJ/mol, gradients are left
 is the throughput form of the same computation.
 """
 
+import math
+
 import numpy as np
 import torch
 
@@ -132,17 +134,50 @@ class System:
         return [i for i in range(len(self.atomicNumbers)) if i not in qc]
 
     def spin_occupancies(self):
-        """(n_alpha, n_beta) of a spin-unrestricted model, None for a spin-restricted one; the checks of
-        QCModel.CrossCheckModelAndState (pMolecule.QCModel.pyx:91-140) for cardinal occupancies."""
+        """(alpha, beta) electron counts of an open-shell or fractional-occupancy model, None for the closed-shell
+        cardinal (RHF) path: QCModel.CrossCheckModelAndState (pMolecule.QCModel.pyx:91-140).  Cardinal counts are
+        whole numbers (ints); fractional ones are the floats (n +- (multiplicity - 1)) / 2."""
         mult = int(self.electronicState.multiplicity)
-        if self.qcModel.isSpinRestricted:
-            if mult != 1:
-                raise ValueError("A spin-unrestricted calculation is required for non-singlet states with cardinal occupancy.")
+        m = self.qcModel
+        fractional = m.occupancyType != "Cardinal"
+        if m.isSpinRestricted and mult != 1:
+            raise ValueError("A spin-unrestricted calculation is required for non-singlet states with %s occupancy."
+                             % ("fractional" if fractional else "cardinal"))
+        if m.isSpinRestricted and not fractional:
             return None
-        ne = self.engine().n_electrons
-        if (ne + mult - 1) % 2 or mult - 1 > ne:
-            raise ValueError("The multiplicity is incompatible with the number of electrons.")
-        return (ne + mult - 1) // 2, (ne - mult + 1) // 2
+        eng = self.engine()
+        ne = eng.n_electrons
+        if not fractional:
+            if (ne + mult - 1) % 2 or mult - 1 > ne:
+                raise ValueError("The multiplicity is incompatible with the number of electrons.")
+            return (ne + mult - 1) // 2, (ne - mult + 1) // 2
+        N = eng.n_basis
+        a, b = (ne + (mult - 1.0)) / 2.0, (ne - (mult - 1.0)) / 2.0
+        na, nb = int(math.ceil(a)), int(math.ceil(b))
+        if a < 0.0 or b < 0.0 or na > N or nb > N:
+            raise ValueError("Invalid alpha or beta electronic charge (< 0 or > number of available orbitals).")
+        if m.occupancyType == "Fixed Fractional":
+            f = m.numberFractional
+            sets = [("", na)] if m.isSpinRestricted else [("Alpha", na), ("Beta", nb)]
+            for tag, nocc in sets:
+                hoo, luo = f["numberFractional%sHOOs" % tag], f["numberFractional%sLUOs" % tag]
+                if not (1 <= hoo <= nocc and 0 <= luo <= N - nocc):
+                    raise ValueError("Invalid fixed fractional occupancy orbital specification.")
+        return a, b
+
+    def occupancy(self):
+        """The pdg_occupancy of an open-shell or fractional-occupancy model (None for the RHF path)."""
+        spins = self.spin_occupancies()
+        if spins is None:
+            return None
+        m = self.qcModel
+        f = m.numberFractional
+        occ = _native.Occupancy(spin_restricted=1 if m.isSpinRestricted else 0, occupancy_type=_native.OCC_TYPES[m.occupancyType],
+                                alpha_charge=float(spins[0]), beta_charge=float(spins[1]), fermi_broadening=float(m.fermiBroadening))
+        for k, name in enumerate(("", "Alpha", "Beta")):
+            occ.n_fractional[2 * k] = f["numberFractional%sHOOs" % name]
+            occ.n_fractional[2 * k + 1] = f["numberFractional%sLUOs" % name]
+        return occ
 
     def engine(self):
         """The device engine of the QC region, rebuilt when the electronic state's charge changes."""
@@ -208,13 +243,13 @@ class System:
         X = self._device_frames(frames)
         qc, mm, q, mm_idx = self._device_inputs(None, X)
         mmi = self._mm_interactions() if self.mmModel is not None else None
-        spins = self.spin_occupancies()
-        if spins is None:
+        occ = self.occupancy()
+        if occ is None:
             r = eng.run(qc, self.qcModel.converger, mm, q, self.nbModel if mm is not None else None, gradients=doGradients,
                         warm_start=warmStart, guess=self.densityGuess)
         else:
-            r = eng.run_uhf(qc, self.qcModel.converger, spins[0], spins[1], mm, q, self.nbModel if mm is not None else None,
-                            gradients=doGradients, warm_start=warmStart)
+            r = eng.run_open(qc, self.qcModel.converger, occ, mm, q, self.nbModel if mm is not None else None,
+                             gradients=doGradients, warm_start=warmStart)
         F = qc.shape[0]
         # one device -> host copy of the small per-frame results
         small = torch.cat([r["energies"], r["status"].to(torch.float64)[:, None], r["ncycles"].to(torch.float64)[:, None]], 1)
@@ -249,10 +284,10 @@ class System:
         terms = {"Pure QC": pure, "QC/MM Elect.": qcmm, "SCF Cycles": small[:, _native.NENERGY + 1].astype(np.int32), "Status": st}
         if (st != _native.PDG_OK).any():
             self._engine.density = None
-            self._engine.density_uhf = None
+            self._engine.density_open = None
             raise SCFNotConverged(scf_failure_message(st))
-        # the QC density of each frame (the total density of a spin-unrestricted state) for the properties
-        self._qc_density = (r["density_alpha"] + r["density_beta"]) if spins is not None else self._engine.density
+        # the QC density of each frame (the total density of an open-shell state) for the properties
+        self._qc_density = r["density"] if occ is not None else self._engine.density
         total = pure + (qcmm if mm is not None else 0.0)
         if mmi is not None:
             Emm = small[:, _native.NENERGY + 2:_native.NENERGY + 2 + len(_native.MM_TERMS)]

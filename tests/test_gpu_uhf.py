@@ -1,8 +1,10 @@
-"""Spin-unrestricted (UHF) states on the GPU (pdg_energy_gradients_uhf; QCModelMNDO(isSpinRestricted=False)) against
-the reference core's open-shell fixtures (tests/golden/open_shell_reference.json: the radicals and the tyrosine
-dipeptide triplet and singlet, AM1, cardinal occupancies): energies 1e-6 Hartree, gradients 1e-5 Hartree/Bohr,
-alpha and beta densities 1e-6; the QC/MM cases (given potentials) including the QC/MM energy and the Lowdin charges;
-a batch of displaced frames against the oracle frame by frame; and the closed-shell singlet equal to RHF.
+"""Open-shell (UHF) and fractional-occupancy states on the GPU (pdg_energy_gradients_uhf, pdg_energy_gradients_open;
+QCModelMNDO(isSpinRestricted=..., occupancyType=...)) against the reference core's open-shell fixtures
+(tests/golden/open_shell_reference.json: the radicals and the tyrosine dipeptide triplet and singlet, AM1; cardinal,
+fixed fractional and variable fractional occupancies, spin-restricted and unrestricted): energies 1e-6 Hartree,
+gradients 1e-5 Hartree/Bohr, alpha and beta densities 1e-6; the QC/MM cases (given potentials; the triplet with
+variable fractional occupancies) including the QC/MM energy and the Lowdin charges; a batch of displaced frames
+against the oracle frame by frame; and the closed-shell singlet equal to RHF.
 
 The tyrosine dipeptide triplet from the diagonal guess is path-dependent in the reference itself: the first ODA step
 (DIISSCFConverger.c:661-760) fits a cubic to two energies and two slopes of an energy that is quadratic in the
@@ -26,7 +28,7 @@ _OPEN = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), 
 CASES = [c for c in _OPEN["cases"] if not c["isSpinRestricted"] and c["occupancyType"] == "Cardinal"]
 TRIPLET = next(c for c in CASES if c["label"] == "Tyrosine Dipeptide Triplet")
 PATH_CASES = [c for c in CASES if c is not TRIPLET]
-QCMM = [c for c in _OPEN["qcmm_cases"] if not c["isSpinRestricted"] and c["occupancyType"] == "Cardinal"]
+QCMM = _OPEN["qcmm_cases"]
 
 
 def _converger():
@@ -52,7 +54,7 @@ def test_uhf_matches_reference_core(case):
     g = s.configuration.gradients3 / (KJ * A2B)
     np.testing.assert_allclose(g, case["gradients_hartree_per_bohr"], rtol=0, atol=1e-5)
     if "density_alpha" in case:
-        D = s.engine().density_uhf[0].cpu().numpy()
+        D = s.engine().density_open[0].cpu().numpy()
         np.testing.assert_allclose(_packed(D[0]), case["density_alpha"], rtol=0, atol=1e-6)
         np.testing.assert_allclose(_packed(D[1]), case["density_beta"], rtol=0, atol=1e-6)
 
@@ -66,8 +68,9 @@ def _unpacked(v, N):
 
 
 def _uhf_call(case, phi=None, start=None):
-    """One frame through pdg_energy_gradients_uhf: from the diagonal guess, or (use_density 1) from the packed alpha
-    and beta densities start."""
+    """One frame through pdg_energy_gradients_uhf (cardinal occupancies) or, for a fractional-occupancy case,
+    pdg_energy_gradients_open: from the diagonal guess, or (use_density 1) from the packed alpha and beta densities
+    start."""
     import ctypes
     import torch
     from pdynamo_mirror_gb300 import _native
@@ -77,11 +80,13 @@ def _uhf_call(case, phi=None, start=None):
     ne, m = eng.n_electrons, case["multiplicity"]
     na, nb = (ne + m - 1) // 2, (ne - m + 1) // 2
     N, n = eng.n_basis, len(Z)
+    restricted = case.get("isSpinRestricted", False)
+    ns = 1 if restricted else 2
     dev = torch.device("cuda")
     xyz = torch.as_tensor(np.array(case["xyz"])[None] * A2B, dtype=torch.float64, device=dev)
     ph = None if phi is None else torch.as_tensor(np.array(phi)[None], dtype=torch.float64, device=dev)
     if start is None:
-        P = torch.empty((1, 2, N, N), dtype=torch.float64, device=dev)
+        P = torch.empty((1, ns, N, N), dtype=torch.float64, device=dev)
     else:
         P = torch.as_tensor(np.stack([_unpacked(np.array(x), N) for x in start])[None], device=dev)
     E = torch.empty((1, _native.NENERGY), dtype=torch.float64, device=dev)
@@ -92,14 +97,66 @@ def _uhf_call(case, phi=None, start=None):
     TS = torch.empty((2, 1, N, N), dtype=torch.float64, device=dev)
     ws = torch.empty(int(eng.L.pdg_uhf_workspace_bytes(eng.handle, 1, na, nb)), dtype=torch.uint8, device=dev)
     opts = _converger().options()
-    _native.check(eng.L.pdg_energy_gradients_uhf(eng.handle, 1, _native.ptr(xyz), _native.ptr(ph), ctypes.byref(opts), na, nb,
-                                                 _native.ptr(P), 0 if start is None else 1, _native.ptr(E), _native.ptr(G),
-                                                 _native.ptr(q), _native.ptr(st), _native.ptr(nc), _native.ptr(TS),
-                                                 _native.ptr(ws), ws.numel(), _native.stream_handle(torch.cuda.current_stream())),
-                  "pdg_energy_gradients_uhf")
+    sh = _native.stream_handle(torch.cuda.current_stream())
+    occ_type = case.get("occupancyType", "Cardinal")
+    if occ_type == "Cardinal" and not restricted:
+        _native.check(eng.L.pdg_energy_gradients_uhf(eng.handle, 1, _native.ptr(xyz), _native.ptr(ph), ctypes.byref(opts), na, nb,
+                                                     _native.ptr(P), 0 if start is None else 1, _native.ptr(E), _native.ptr(G),
+                                                     _native.ptr(q), _native.ptr(st), _native.ptr(nc), _native.ptr(TS),
+                                                     _native.ptr(ws), ws.numel(), sh), "pdg_energy_gradients_uhf")
+    else:
+        occ = _native.Occupancy(spin_restricted=int(restricted), occupancy_type=_native.OCC_TYPES[occ_type],
+                                alpha_charge=(ne + m - 1) / 2.0, beta_charge=(ne - m + 1) / 2.0, fermi_broadening=1.0e3)
+        for k, v in enumerate((1, 0, 1, 0, 1, 0)):
+            occ.n_fractional[k] = v
+        _native.check(eng.L.pdg_energy_gradients_open(eng.handle, 1, _native.ptr(xyz), _native.ptr(ph), ctypes.byref(opts),
+                                                      ctypes.byref(occ), _native.ptr(P), 0 if start is None else 1, _native.ptr(E),
+                                                      _native.ptr(G), _native.ptr(q), _native.ptr(st), _native.ptr(nc),
+                                                      _native.ptr(TS), _native.ptr(ws), ws.numel(), sh), "pdg_energy_gradients_open")
     torch.cuda.synchronize()
     return {"status": int(st[0]), "ncycles": int(nc[0]), "energies": E.cpu().numpy()[0], "gradients": G.cpu().numpy()[0],
             "charges": q.cpu().numpy()[0], "density": P.cpu().numpy()[0], "total_spin": TS.cpu().numpy()[:, 0]}
+
+
+# the triplet's fixed fractional case with the default one fractional HOO and no LUO has cardinal occupancies: it
+# shares the cardinal case's path dependence and is checked against that case
+TRIPLET_FF = next(c for c in _OPEN["cases"] if c["label"] == TRIPLET["label"] and c["occupancyType"] == "Fixed Fractional")
+FRACTIONAL = [c for c in _OPEN["cases"] if c["occupancyType"] != "Cardinal" and c is not TRIPLET_FF]
+
+
+@pytest.mark.parametrize("case", FRACTIONAL, ids=["%s-%s-%s" % (c["label"].replace(" ", ""), "R" if c["isSpinRestricted"] else "U",
+                                                                c["occupancyType"].replace(" ", "")) for c in FRACTIONAL])
+def test_fractional_occupancies_match_reference_core(case):
+    """Fixed and variable fractional occupancies, spin-restricted and unrestricted (System.Energy with
+    QCModelMNDO(occupancyType=...), the reference's default one fractional HOO, no LUO and Fermi broadening 1000):
+    energies (with the occupancy energy), gradients and, for the radicals, the alpha and beta densities."""
+    from pdynamo_mirror_gb300 import QCModelMNDO, System
+    s = System(case["atomic_numbers"], np.array(case["xyz"]))
+    s.electronicState.charge = case["charge"]
+    s.electronicState.multiplicity = case["multiplicity"]
+    s.DefineQCModel(QCModelMNDO("am1", isSpinRestricted=case["isSpinRestricted"], occupancyType=case["occupancyType"],
+                                converger=_converger()))
+    s.Energy(doGradients=True)
+    assert abs(s.configuration.energyTerms["Pure QC"] - case["pure_qc_kj"]) / KJ < 1e-6
+    np.testing.assert_allclose(s.configuration.gradients3 / (KJ * A2B), case["gradients_hartree_per_bohr"], rtol=0, atol=1e-5)
+    if "density_alpha" in case:
+        D = s.engine().density_open[0].cpu().numpy()
+        np.testing.assert_allclose(_packed(D[0]), case["density_alpha"], rtol=0, atol=1e-6)
+        np.testing.assert_allclose(_packed(D[1]), case["density_beta"], rtol=0, atol=1e-6)
+
+
+def test_triplet_fixed_fractional_with_one_hoo_is_the_cardinal_state():
+    """One fractional HOO and no LUO per spin is a cardinal occupancy: from the reference's densities the fixed
+    fractional SCF stays at the reference's state, and from the diagonal guess it reaches the cardinal SCF's state."""
+    r = _uhf_call(TRIPLET_FF, start=(TRIPLET["density_alpha"], TRIPLET["density_beta"]))
+    assert r["status"] == 0 and r["ncycles"] <= 3
+    e = r["energies"]
+    assert abs(KJ * (e[1] + e[2] + e[3]) - TRIPLET_FF["pure_qc_kj"]) / KJ < 1e-6
+    np.testing.assert_allclose(r["gradients"], TRIPLET_FF["gradients_hartree_per_bohr"], rtol=0, atol=1e-5)
+    a, b = _uhf_call(TRIPLET_FF), _uhf_call(TRIPLET)
+    assert a["status"] == 0 and b["status"] == 0
+    assert abs(a["energies"][0] - b["energies"][0]) < 1e-9
+    np.testing.assert_allclose(a["gradients"], b["gradients"], rtol=0, atol=1e-8)
 
 
 @pytest.mark.parametrize("case", QCMM, ids=[c["label"].replace(" ", "") for c in QCMM])
@@ -144,7 +201,7 @@ def test_uhf_triplet_from_diagonal_guess_reaches_a_fixed_point_of_the_oracle():
     s.Energy(doGradients=True)
     e = s.configuration.energyTerms["Pure QC"]
     g = s.configuration.gradients3 / (KJ * A2B)
-    D = s.engine().density_uhf[0].cpu().numpy()
+    D = s.engine().density_open[0].cpu().numpy()
     np.testing.assert_allclose(np.trace(D[0]), 47.0, rtol=0, atol=1e-9)
     np.testing.assert_allclose(np.trace(D[1]), 45.0, rtol=0, atol=1e-9)
     r = O.energy_open(O.Hamiltonian("am1", c["atomic_numbers"]), c["atomic_numbers"], c["xyz"], 0, 3, False, "Cardinal",

@@ -45,6 +45,25 @@ def test_parameters_match_reference_core():
                 np.testing.assert_allclose(c, cc[s, :len(c)], rtol=1e-12)
 
 
+def test_pm6_records_carry_the_diatomic_pairs_by_partner_index():
+    """PM6 element records (pMolecule.MNDOParameters.pyx:259-276): each record knows its place in the system's element
+    list and holds the diatomic pairs' coefficient x and exponent a (bohr^-1) by partner index; the other
+    Hamiltonians have none."""
+    els, rec, idx = parameters.element_table("pm6", [8, 1, 1, 6, 9])
+    assert els == [1, 6, 8, 9] and list(idx) == [2, 0, 0, 1, 3]
+    P = parameters
+    for k, z in enumerate(els):
+        r = rec[k]
+        assert r[P.E_INDEX] == k and r[P.E_DIAT] == 1.0
+        d = parameters.table()["hamiltonians"]["pm6"][str(z)]["diatomic"]
+        pairs = {int(p[0]): (p[1], p[2] * P.BOHRS_TO_ANGSTROMS) for p in d}
+        for j, zj in enumerate(els):
+            assert (r[P.E_DIAT_X + j], r[P.E_DIAT_A + j]) == pytest.approx(pairs[zj], rel=1e-15)
+        assert not r[P.E_DIAT_X + len(els):P.E_DIAT_X + P.MAX_ELEMENTS].any()
+    _, rec, _ = parameters.element_table("am1", [8, 1, 1])
+    assert not rec[:, P.E_DIAT].any() and not rec[:, P.E_DIAT_X:P.E_DIAT_X + P.MAX_ELEMENTS].any()
+
+
 def test_abfs_knots_match_oracle():
     x, y = nbmodel.abfs_knots(8.0, 12.0)
     ox, oy = O.abfs_knots(8.0, 12.0)
@@ -58,10 +77,13 @@ def test_option_errors_match_reference_behaviour():
     with pytest.raises(ValueError):
         DIISSCFConverger(notAnOption=1)
     with pytest.raises(ValueError):
-        QCModelMNDO("am1", occupancyType="Fixed Fractional")
+        QCModelMNDO("am1", occupancyType="Partial")
+    m = QCModelMNDO("am1", occupancyType="Variable Fractional", fermiBroadening=500.0, numberFractionalBetaLUOs=2)
+    assert m.GetOption("occupancyType") == "Variable Fractional" and m.GetOption("fermiBroadening") == 500.0
+    assert m.GetOption("numberFractionalBetaLUOs") == 2 and m.GetOption("numberFractionalHOOs") == 1
     assert not QCModelMNDO("am1", isSpinRestricted=False).IsSpinRestricted()
     with pytest.raises(ValueError):
-        QCModelMNDO("pm6")
+        QCModelMNDO("pm7")
     with pytest.raises(ValueError):
         NBModelABFS(innerCutoff=12.0, outerCutoff=8.0)
 
@@ -89,6 +111,7 @@ def test_system_engine_follows_the_electronic_state(monkeypatch):
             made.append(charge)
             self.device = "cpu"
             self.n_electrons = 8 - charge
+            self.n_basis = 6
 
     monkeypatch.setattr(S, "QCEngine", Stand)
     s = S.System([8, 1, 1], [[0.0, 0.0, 0.0], [0.96, 0.0, 0.0], [-0.24, 0.93, 0.0]])
@@ -108,6 +131,23 @@ def test_system_engine_follows_the_electronic_state(monkeypatch):
         s.spin_occupancies()
     s.electronicState.multiplicity = 1
     assert s.spin_occupancies() == (3, 3)
+    # fractional occupancies (QCModel.CrossCheckModelAndState): restricted needs a singlet; counts as floats; the
+    # fixed fractional orbitals within 1..occupied and 0..virtual
+    s.DefineQCModel(QCModelMNDO("am1", occupancyType="Fixed Fractional", numberFractionalLUOs=1))
+    assert s.spin_occupancies() == (3.0, 3.0) and s.occupancy() is not None
+    o = s.occupancy()
+    assert o.spin_restricted == 1 and o.occupancy_type == 1 and list(o.n_fractional) == [1, 1, 1, 0, 1, 0]
+    s.electronicState.multiplicity = 3
+    with pytest.raises(ValueError, match="fractional occupancy"):
+        s.spin_occupancies()
+    s.DefineQCModel(QCModelMNDO("am1", isSpinRestricted=False, occupancyType="Fixed Fractional", numberFractionalBetaHOOs=3))
+    with pytest.raises(ValueError, match="fixed fractional"):
+        s.spin_occupancies()
+    s.DefineQCModel(QCModelMNDO("am1", isSpinRestricted=False, occupancyType="Variable Fractional"))
+    assert s.spin_occupancies() == (4.0, 2.0)
+    s.electronicState.multiplicity = 1
+    s.DefineQCModel(QCModelMNDO("am1"))
+    assert s.occupancy() is None
 
 
 def test_atomic_charges_assembly():
