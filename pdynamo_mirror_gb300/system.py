@@ -251,6 +251,7 @@ class System:
             r = eng.run_open(qc, self.qcModel.converger, occ, mm, q, self.nbModel if mm is not None else None,
                              gradients=doGradients, warm_start=warmStart)
         F = qc.shape[0]
+        on_gpu = torch.device(eng.device).type == "cuda"
         # one device -> host copy of the small per-frame results
         small = torch.cat([r["energies"], r["status"].to(torch.float64)[:, None], r["ncycles"].to(torch.float64)[:, None]], 1)
         if mmi is not None:
@@ -270,11 +271,15 @@ class System:
             Gd *= GRADIENT_TO_KJ_PER_A
             if mmi is not None:
                 Gd += Gmm
-            Gh = torch.empty(Gd.shape, dtype=torch.float64, pin_memory=True)
-            Gh.copy_(Gd, non_blocking=True)
-        small = small.cpu().numpy()
-        if doGradients:
+            Gh = torch.empty(Gd.shape, dtype=torch.float64, pin_memory=on_gpu)
+            Gh.copy_(Gd, non_blocking=on_gpu)
+        # both results come back on the stream with one host wait
+        small_h = torch.empty(small.shape, dtype=torch.float64, pin_memory=on_gpu)
+        small_h.copy_(small, non_blocking=on_gpu)
+        if on_gpu:
             torch.cuda.current_stream(eng.device).synchronize()
+        small = small_h.numpy()
+        if doGradients:
             G = Gh.numpy()
         E = small[:, :_native.NENERGY]
         st = small[:, _native.NENERGY].astype(np.int32)
