@@ -253,9 +253,12 @@ class QCEngine:
         D = self.density_open
         out = dict(energies=energies, qc_gradients=grad, charges=charges, status=status, ncycles=ncycles, phi=phi, density_sets=D)
         if ns == 1:
-            out.update(density=D[:, 0])
+            out.update(density=D[:, 0], spin_populations=torch.zeros((F, n), dtype=torch.float64, device=dev))
         else:
-            out.update(density_alpha=D[:, 0], density_beta=D[:, 1])
+            # Lowdin spin populations of the QC atoms: sum over each atom's orbitals of (P_alpha - P_beta)_mm
+            sd = D[:, 0].diagonal(dim1=-2, dim2=-1) - D[:, 1].diagonal(dim1=-2, dim2=-1)
+            out.update(density_alpha=D[:, 0], density_beta=D[:, 1],
+                       spin_populations=torch.zeros((F, n), dtype=torch.float64, device=dev).index_add_(1, self.basis_atom(), sd))
             if gradients:
                 out.update(density=ts[0], spin_density=ts[1])
             else:
@@ -269,6 +272,14 @@ class QCEngine:
                           "pdg_qcmm_gradients")
             out.update(qcmm_qc_gradients=gqc, qcmm_mm_gradients=gmm)
         return out
+
+    def basis_atom(self):
+        """Device index of the atom of every basis function (the atoms' orbitals in atom order)."""
+        if getattr(self, "_basis_atom", None) is None:
+            from .parameters import E_NORB
+            norb = [int(self._records[k][E_NORB]) for k in self._index]
+            self._basis_atom = torch.as_tensor(np.repeat(np.arange(self.n_atoms), norb), dtype=torch.long, device=self.device)
+        return self._basis_atom
 
     def _side_stream(self):
         if getattr(self, "_side", None) is None:

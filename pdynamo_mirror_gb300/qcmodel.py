@@ -71,13 +71,17 @@ class QCModelMNDO:
 
     def AtomicCharges(self, configuration, chargeModel=None, spinDensities=False):
         """Lowdin charges of the QC atoms from the last energy on configuration (QCModelMNDO.AtomicCharges; the
-        NDDO basis is orthonormal, so Mulliken charges are the same); zeros for spin densities (closed shell)."""
+        NDDO basis is orthonormal, so Mulliken charges are the same); with spinDensities their Lowdin spin populations
+        (sum over each atom's orbitals of P_alpha - P_beta; zeros for closed shells and spin-restricted states)."""
         if chargeModel not in (None, "Lowdin", "Mulliken"):
             raise ValueError("Unknown QC charge model: " + str(chargeModel) + ".")
         q = getattr(configuration, "qcCharges", None)
         if q is None:
             return None
-        return np.zeros(len(q)) if spinDensities else np.array(q, dtype=np.float64)
+        if spinDensities:
+            sp = getattr(configuration, "qcSpinDensities", None)
+            return np.zeros(len(q)) if sp is None else np.array(sp, dtype=np.float64)
+        return np.array(q, dtype=np.float64)
 
     def DipoleMoment(self, configuration, center=None):
         """Dipole moment (Debye) of the QC atoms from the last energy's density (QCModelMNDO_DipoleMoment)."""

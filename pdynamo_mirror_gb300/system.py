@@ -259,6 +259,8 @@ class System:
             small = torch.cat([small, Emm], 1)
         nq = r["charges"].shape[1]
         small = torch.cat([small, r["charges"]], 1)   # Lowdin charges of the QC atoms (QCModelMNDO_LowdinCharges)
+        if "spin_populations" in r:                   # and, for open-shell states, their Lowdin spin populations
+            small = torch.cat([small, r["spin_populations"]], 1)
         G = None
         if doGradients:
             qs, ms, _, _ = self._selections()
@@ -283,7 +285,12 @@ class System:
             G = Gh.numpy()
         E = small[:, :_native.NENERGY]
         st = small[:, _native.NENERGY].astype(np.int32)
-        self.qcChargesBatch = small[:, small.shape[1] - nq:].copy()
+        if "spin_populations" in r:
+            self.qcSpinBatch = small[:, small.shape[1] - nq:].copy()
+            self.qcChargesBatch = small[:, small.shape[1] - 2 * nq:small.shape[1] - nq].copy()
+        else:
+            self.qcSpinBatch = None
+            self.qcChargesBatch = small[:, small.shape[1] - nq:].copy()
         pure = HARTREES_TO_KJ * (E[:, _native.EN_ELECTRONIC] + E[:, _native.EN_NUCLEAR] + E[:, _native.EN_BASELINE])
         qcmm = HARTREES_TO_KJ * E[:, _native.EN_QCMM]
         terms = {"Pure QC": pure, "QC/MM Elect.": qcmm, "SCF Cycles": small[:, _native.NENERGY + 1].astype(np.int32), "Status": st}
@@ -310,6 +317,7 @@ class System:
             self.configuration.energyTerms.pop("QC/MM Elect.", None)
         self.configuration.gradients3 = None if G is None else G[0]
         self.configuration.qcCharges = self.qcChargesBatch[0].copy()
+        self.configuration.qcSpinDensities = None if self.qcSpinBatch is None else self.qcSpinBatch[0].copy()
         from .properties import QCState
         self.configuration.qcState = QCState(self._qc_density[0].clone(), self.qcModel.mndoModel,
                                              [self.atomicNumbers[i] for i in self.qcSelection], self.coordinates3[self.qcSelection])
@@ -332,8 +340,8 @@ class System:
     def AtomicCharges(self, qcChargeModel=None, qcAtomsOnly=False, spinDensities=False):
         """Partial charges of the atoms after Energy (System.py:96-113): the MM point charges with the QC model's
         Lowdin charges added at the QC atoms, or the QC atoms' charges alone (qcAtomsOnly, or no MM charges).
-        The closed-shell states here have no spin density, so spinDensities gives zeros.  Mulliken charges
-        equal Lowdin ones in the NDDO basis, which is orthonormal."""
+        spinDensities: the QC atoms' Lowdin spin populations (zero for closed shells and spin-restricted states),
+        zero at the MM atoms.  Mulliken charges equal Lowdin ones in the NDDO basis, which is orthonormal."""
         if qcChargeModel not in (None, "Lowdin", "Mulliken"):
             raise ValueError("Unknown QC charge model: " + str(qcChargeModel) + ".")
         if self.qcModel is None:
@@ -341,7 +349,11 @@ class System:
         q = getattr(self.configuration, "qcCharges", None)
         if q is None:
             raise ValueError("No QC density: calculate an energy first.")
-        q = np.zeros_like(q) if spinDensities else np.array(q, dtype=np.float64)
+        if spinDensities:
+            sp = getattr(self.configuration, "qcSpinDensities", None)
+            q = np.zeros_like(q) if sp is None else np.array(sp, dtype=np.float64)
+        else:
+            q = np.array(q, dtype=np.float64)
         if qcAtomsOnly or self.mmCharges is None:
             return q
         # The QC atoms carry their QC charge only, as MMAtomContainer.AtomicCharges gives 0 for the atoms that

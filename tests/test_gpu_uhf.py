@@ -57,6 +57,20 @@ def test_uhf_matches_reference_core(case):
         D = s.engine().density_open[0].cpu().numpy()
         np.testing.assert_allclose(_packed(D[0]), case["density_alpha"], rtol=0, atol=1e-6)
         np.testing.assert_allclose(_packed(D[1]), case["density_beta"], rtol=0, atol=1e-6)
+        _check_spin_populations(s, case)
+
+
+def _check_spin_populations(s, case):
+    """Lowdin spin populations (System.AtomicCharges / QCModelMNDO.AtomicCharges with spinDensities) against the
+    reference's alpha and beta densities; they add up to the unpaired electrons (fractional: their expectation)."""
+    N = int(round(np.sqrt(2 * len(case["density_alpha"]))))
+    Sd = np.diag(_unpacked(np.array(case["density_alpha"]), N) - _unpacked(np.array(case["density_beta"]), N))
+    norb = [1 if z == 1 else 4 for z in case["atomic_numbers"]]
+    want = np.add.reduceat(Sd, np.cumsum([0] + norb[:-1]))
+    sp = s.AtomicCharges(spinDensities=True)
+    np.testing.assert_allclose(sp, want, rtol=0, atol=5e-6)
+    np.testing.assert_allclose(s.qcModel.AtomicCharges(s.configuration, spinDensities=True), want, rtol=0, atol=5e-6)
+    assert abs(sp.sum() - Sd.sum()) < 1e-6
 
 
 def _unpacked(v, N):
@@ -143,6 +157,7 @@ def test_fractional_occupancies_match_reference_core(case):
         D = s.engine().density_open[0].cpu().numpy()
         np.testing.assert_allclose(_packed(D[0]), case["density_alpha"], rtol=0, atol=1e-6)
         np.testing.assert_allclose(_packed(D[1]), case["density_beta"], rtol=0, atol=1e-6)
+        _check_spin_populations(s, case)
 
 
 def test_triplet_fixed_fractional_with_one_hoo_is_the_cardinal_state():

@@ -166,6 +166,11 @@ def test_atomic_charges_assembly():
     np.testing.assert_allclose(s.AtomicCharges(), [-0.4, 0.2, 0.2, -0.834, 0.417, 0.417])
     np.testing.assert_allclose(s.AtomicCharges(qcAtomsOnly=True), q)
     np.testing.assert_allclose(s.AtomicCharges(spinDensities=True), np.zeros(6))
+    s.configuration.qcSpinDensities = np.array([0.1, 0.45, 0.45])   # an open-shell state's Lowdin spin populations
+    np.testing.assert_allclose(s.AtomicCharges(spinDensities=True), [0.1, 0.45, 0.45, 0.0, 0.0, 0.0])
+    np.testing.assert_allclose(s.AtomicCharges(qcAtomsOnly=True, spinDensities=True), [0.1, 0.45, 0.45])
+    np.testing.assert_allclose(s.qcModel.AtomicCharges(s.configuration, spinDensities=True), [0.1, 0.45, 0.45])
+    s.configuration.qcSpinDensities = None
     np.testing.assert_allclose(s.qcModel.AtomicCharges(s.configuration, chargeModel="Mulliken"), q)
     assert s.qcModel.IsSpinRestricted() and s.qcModel.GetOption("occupancyType") == "Cardinal"
     with pytest.raises(AttributeError):
