@@ -490,14 +490,19 @@ void launch_batch_integrals(const Batch &b, const double *xyz, double *ws, cudaS
 #define PG_SM 1408
 
 // Real = double: the reference's FP64 arithmetic.  Real = float (the mixed method): the pair's multipole terms,
-// rotation, density terms, contractions and overlap sums in FP32, the core-core term and the assembly of the
-// pair gradient in FP64 (per-pair errors ~1e-7 Hartree/Bohr, summed per atom in FP64).
+// rotation, density products, contractions, overlap sums and the lane sums in FP32, the core-core term and the
+// assembly of the pair gradient in FP64 (per-pair errors ~1e-7 Hartree/Bohr, summed per atom in FP64).  The FP32
+// variant over frames asks for four blocks per SM, so that a 304-frame batch of the water box (2432 warps) runs in
+// one wave (the batch variant, with its larger per-item bookkeeping, three).
+template <bool BATCH, typename Real> struct PairGradOcc { static constexpr int blocks = sizeof(Real) == 4 ? (BATCH ? 3 : 4) : 1; };
+
 template <bool BATCH, typename Real>
-__global__ void __launch_bounds__(PG_WARPS * 32)
+__global__ void __launch_bounds__(PG_WARPS * 32, PairGradOcc<BATCH, Real>::blocks)
 k_pair_gradients(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, const double *__restrict__ xyz,
                  const double *__restrict__ density, double *__restrict__ ws)
 {
-    __shared__ double smem[PG_WARPS][PG_SM];
+    __shared__ Real smem[PG_WARPS][PG_SM];
+    constexpr bool F32 = sizeof(Real) == 4;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     FrameView fv;
     int ub;
@@ -506,11 +511,16 @@ k_pair_gradients(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, con
     const FramePlan &plan = BATCH ? fv.plan : plan0;
     const double *terms = s.terms;
     const int b0 = ub * 32, nb = min(32, s.n_gen - b0);
-    Real *W = (Real *)smem[w];
+    Real *W = smem[w];
     Real *St = W, *dSt = W + 96, *L = W + 192, *dL = W + 292, *ci = W + 392, *cj = W + 402, *dci = W + 412, *dcj = W + 422;
     Real *C = W + 432, *CD = W + 532, *G = W + 832, *W1 = W + 932, *W2 = W + 1032, *W3 = W + 1132;
     Real *oneI = W + 1232, *oneJ = W + 1242, *Wres = W + 1252;
     const int N = s.n_basis;
+    // lane sums: in FP64 for the FP64 variant, in FP32 (then widened) for the FP32 one
+    auto lane_sum = [](Real v) -> double {
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        return (double)v;
+    };
     const double *R = xyz + 3 * fv.atom;
     const double *P = density + fv.dens;
     const double *Sp = s.spin ? s.spin + fv.dens : nullptr;   // spin density (spin-unrestricted states)
@@ -554,10 +564,19 @@ k_pair_gradients(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, con
             const int l = MP_DA[kl], kk = MP_DB[kl], n = MP_DA[mn], m = MP_DB[mn];   // kl = (l >= kk), mn = (n >= m)
             const double aa = (kk == l) ? 1.0 : 2.0, bb = (m == n) ? 1.0 : 2.0;
             const int K = is + kk, Lx = is + l, M = js + m, Nn = js + n;
-            double fv = P[(size_t)M * N + K] * P[(size_t)Nn * N + Lx] + P[(size_t)Nn * N + K] * P[(size_t)M * N + Lx];
-            // open shells: the spin density's products join the exchange part (QCModelMNDOState.c:178-260)
-            if (Sp) fv += Sp[(size_t)M * N + K] * Sp[(size_t)Nn * N + Lx] + Sp[(size_t)Nn * N + K] * Sp[(size_t)M * N + Lx];
-            G[k] = (Real)(0.25 * aa * bb * fv) - oneI[kl] * oneJ[mn];
+            if constexpr (F32) {
+                const float pa = (float)P[(size_t)M * N + K], pb = (float)P[(size_t)Nn * N + Lx];
+                const float pc = (float)P[(size_t)Nn * N + K], pd = (float)P[(size_t)M * N + Lx];
+                float fv = pa * pb + pc * pd;
+                // open shells: the spin density's products join the exchange part (QCModelMNDOState.c:178-260)
+                if (Sp) fv += (float)Sp[(size_t)M * N + K] * (float)Sp[(size_t)Nn * N + Lx] + (float)Sp[(size_t)Nn * N + K] * (float)Sp[(size_t)M * N + Lx];
+                G[k] = 0.25f * (float)(aa * bb) * fv - oneI[kl] * oneJ[mn];
+            } else {
+                double fv = P[(size_t)M * N + K] * P[(size_t)Nn * N + Lx] + P[(size_t)Nn * N + K] * P[(size_t)M * N + Lx];
+                // open shells: the spin density's products join the exchange part (QCModelMNDOState.c:178-260)
+                if (Sp) fv += Sp[(size_t)M * N + K] * Sp[(size_t)Nn * N + Lx] + Sp[(size_t)Nn * N + K] * Sp[(size_t)M * N + Lx];
+                G[k] = (Real)(0.25 * aa * bb * fv) - oneI[kl] * oneJ[mn];
+            }
         }
         if (r >= 5.0e-3) {
             const double *to = terms + (size_t)(eli * s.n_elements + elj) * 2 * MP_NTERMS, *ta = to + MP_NTERMS;
@@ -635,10 +654,9 @@ k_pair_gradients(DeviceSystem sys0, FramePlan plan0, int n_frames, Batch bt, con
                 o0 += oneJ[cd] * u * (-zi);
                 for (int xx = 0; xx < 3; xx++) oi[xx] += oneJ[cd] * ux[xx] * (-zi);
             }
-            // lane sums in FP64 whatever Real is
-            const double T0 = warp_sum((double)t0), O0 = warp_sum((double)o0);
+            const double T0 = lane_sum(t0), O0 = lane_sum(o0);
             double TI[3], TJ[3], OI[3];
-            for (int xx = 0; xx < 3; xx++) { TI[xx] = warp_sum((double)ti[xx]); TJ[xx] = warp_sum((double)tj[xx]); OI[xx] = warp_sum((double)oi[xx]); }
+            for (int xx = 0; xx < 3; xx++) { TI[xx] = lane_sum(ti[xx]); TJ[xx] = lane_sum(tj[xx]); OI[xx] = lane_sum(oi[xx]); }
             // eng = -s (dcore + doei0f + dtei0f) + doei1 + dtei1   (MNDOIntegrals.c:392-418)
             for (int xx = 0; xx < 3; xx++) {
                 const double sx = v3[xx] / r;
