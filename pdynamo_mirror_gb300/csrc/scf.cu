@@ -914,6 +914,82 @@ __device__ double density_step(const SCFArgs &a, double *wsf, const double *F, d
 // frame's own (left by its last FP64 step) or a shared copy of another frame's (pdg_base_capture), read-only here.
 struct PertBase { const double *BF, *BP; const float *Z32, *V32, *Gi; };
 
+// Tensor memory (columns from tmem), the completion mbarrier and its phase of a CTA that may use tcgen05.
+struct TCState { uint32_t tmem, bar, phase; };
+
+// C[0:128, 0:Kp] = A[0:128, 0:K] B[0:Kp, 0:K]^T on the tensor cores (accumulator in tensor memory at tc.tmem, Kp
+// columns), FP32 operands given by accessors (zero outside rows < ma / nb and K), each split into BF16 hi + mid + lo
+// and multiplied as hi.hi + hi.mid + mid.hi + hi.lo + lo.hi + mid.mid (the FP32 value to ~2^-24; the three dropped
+// products are below that).  K is staged in chunks of 32 columns through `stage` (shared memory, 16-byte aligned,
+// 3 * (128 + Kp) * 64 bytes), one commit and bounded wait per chunk.  False when a wait ran out.
+template <typename FA, typename FB>
+__device__ bool tc_product_f32(TCState &tc, unsigned char *stage, int ma, int nb, int K, int Kp, FA fa, FB fb)
+{
+    const int tid = threadIdx.x;
+    constexpr int KC = 32;
+    const size_t pa = (size_t)TC_M * KC * 2, pbs = (size_t)Kp * KC * 2;   // bytes of one part of A and of B
+    unsigned char *A0 = stage, *B0 = stage + 3 * pa;
+    for (int k0 = 0; k0 < K; k0 += KC) {
+        for (int e = tid; e < TC_M * KC; e += PDG_BLOCK) {
+            const int r = e / KC, c = e % KC, k = k0 + c;
+            const float x = (r < ma && k < K) ? fa(r, k) : 0.0f;
+            __nv_bfloat16 h, m, l;
+            bf16_split3(x, h, m, l);
+            const uint32_t o = tc_offset(r, c, KC);
+            *(__nv_bfloat16 *)(A0 + o) = h; *(__nv_bfloat16 *)(A0 + pa + o) = m; *(__nv_bfloat16 *)(A0 + 2 * pa + o) = l;
+        }
+        for (int e = tid; e < Kp * KC; e += PDG_BLOCK) {
+            const int r = e / KC, c = e % KC, k = k0 + c;
+            const float x = (r < nb && k < K) ? fb(r, k) : 0.0f;
+            __nv_bfloat16 h, m, l;
+            bf16_split3(x, h, m, l);
+            const uint32_t o = tc_offset(r, c, KC);
+            *(__nv_bfloat16 *)(B0 + o) = h; *(__nv_bfloat16 *)(B0 + pbs + o) = m; *(__nv_bfloat16 *)(B0 + 2 * pbs + o) = l;
+        }
+        tc_fence_proxy();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            const uint32_t a = tc_smem_addr(A0), b = tc_smem_addr(B0);
+            const uint32_t ah = a, am = a + (uint32_t)pa, al = a + 2 * (uint32_t)pa;
+            const uint32_t bh = b, bm = b + (uint32_t)pbs, bl = b + 2 * (uint32_t)pbs;
+            tc_product(tc.tmem, ah, 0, bh, Kp, KC, k0 > 0);
+            tc_product(tc.tmem, ah, 0, bm, Kp, KC, true);
+            tc_product(tc.tmem, am, 0, bh, Kp, KC, true);
+            tc_product(tc.tmem, ah, 0, bl, Kp, KC, true);
+            tc_product(tc.tmem, al, 0, bh, Kp, KC, true);
+            tc_product(tc.tmem, am, 0, bm, Kp, KC, true);
+            tc_commit(tc.bar);
+        }
+        const bool ok = mbar_wait(tc.bar, tc.phase, 1 << 22);
+        tc.phase ^= 1u;
+        if (__syncthreads_or(!ok)) return false;
+    }
+    tc_fence_after();
+    return true;
+}
+
+// Thread (row r = 32 (warp % 4) + lane of the accumulator) reads its columns of C: warps 0-3 the first half of the
+// 16-column chunks, warps 4-7 the rest; put(r, c, v) for r < 128, c < n.
+template <typename Put>
+__device__ void tc_readout(const TCState &tc, int Kp, int n, Put put)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int rr = 32 * (w & 3) + lane, nch = Kp / 16, half = (nch + 1) / 2, c0 = w < 4 ? 0 : half, c1 = w < 4 ? half : nch;
+    for (int ch = c0; ch < c1; ch++) {
+        float v[16];
+        tc_ld16(tc.tmem + ((uint32_t)(32 * (w & 3)) << 16) + (uint32_t)(ch * 16), v);
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+            const int c = ch * 16 + j;
+            if (c < n) put(rr, c, v[j]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+}
+
 __device__ __forceinline__ PertBase pert_base(const double *blk, const FramePlan &pl, int N, int kv)
 {
     PertBase b;
@@ -954,7 +1030,7 @@ __device__ __forceinline__ PertBase pert_base(const double *blk, const FramePlan
 // longer carries the step (the iteration does not settle, or K is not small): the caller then runs an FP64 step,
 // which makes a new base.
 __device__ double density_step_pert(const SCFArgs &a, double *wsf, const double *F, double *P, Smem &sm, Timer &tm, const PertBase &pb,
-                                   bool warm_k, float kmax_limit)
+                                   bool warm_k, float kmax_limit, TCState *tc = nullptr)
 {
     const DeviceSystem &s = a.s;
     const FramePlan &pl = a.plan;
@@ -971,6 +1047,49 @@ __device__ double density_step_pert(const SCFArgs &a, double *wsf, const double 
     const float *Z32 = pb.Z32, *V32 = pb.V32, *Gi = pb.Gi;
     auto Zf = [&](int t, int i) { return Z32[(size_t)t * N + i]; };
     auto Vf = [&](int j, int i) { return V32[(size_t)j * N + i]; };
+#ifndef PDG_SCF_NO_TENSOR
+    const int Kp = (N + 15) & ~15;
+    if (tc && N <= 144 && N > kv && sm.amat && smem_plan(N, kv, a.smem_limit).amat * 8 >= (size_t)3 * (TC_M + Kp) * 64) {
+        // On the tensor cores: with Q = [Z0; V] (the base's orthonormal basis, Z32 and V32 contiguous: N rows of N),
+        // C = Q dF Q^T holds L' (rows, columns < kv), E (rows >= kv, columns < kv) and M' (both >= kv).  R = Q dF and
+        // C's first 128 rows come from two tensor-core products; C is symmetric, so its columns >= 128 give rows
+        // >= 128 (the mirror); the corner of rows and columns >= 128 (N - 128 <= 16) is summed on the FP32 cores
+        // from R's rows >= 128.  R lives where the DIIS save later puts dF (free here).  The staging chunks use the
+        // shared-memory slot of the packed matrix (free between FP64 steps; large enough from N = 65 on).
+        float *R32 = (float *)(wsf + pl.BW) + pert_dq_offset(N, kv) + (size_t)N * N;
+        unsigned char *stage = (unsigned char *)sm.amat;
+        auto Qf = [&](int t, int k) { return Z32[(size_t)t * N + k]; };
+        auto put_c = [&](int r, int c, float v) {
+            if (r >= N) return;
+            if (r < kv) { if (c < kv) Lp[(size_t)r * kv + c] = v; }
+            else if (c < kv) E[(size_t)(r - kv) * kv + c] = v;
+            else Mp[(size_t)(r - kv) * nc + (c - kv)] = v;
+        };
+        if (!tc_product_f32(*tc, stage, min(N, TC_M), N, N, Kp, Qf, [&](int n, int k) { return D[(size_t)n * N + k]; })) return -2.0;
+        tc_readout(*tc, Kp, N, [&](int r, int c, float v) { if (r < N) R32[(size_t)r * N + c] = v; });
+        for (int e = tid; e < (N - TC_M) * N; e += PDG_BLOCK) {   // R's rows >= 128
+            const int r = TC_M + e / N, c = e % N;
+            float acc = 0.0f;
+            for (int k = 0; k < N; k++) acc = fmaf(Qf(r, k), D[(size_t)c * N + k], acc);
+            R32[(size_t)r * N + c] = acc;
+        }
+        __syncthreads();
+        if (!tc_product_f32(*tc, stage, min(N, TC_M), N, N, Kp, [&](int r, int k) { return R32[(size_t)r * N + k]; }, Qf)) return -2.0;
+        tc_readout(*tc, Kp, N, [&](int r, int c, float v) {
+            if (r >= N) return;
+            put_c(r, c, v);
+            if (c >= TC_M) put_c(c, r, v);
+        });
+        for (int e = tid; e < (N - TC_M) * (N - TC_M); e += PDG_BLOCK) {   // the corner
+            const int r = TC_M + e / (N - TC_M), c = TC_M + e % (N - TC_M);
+            float acc = 0.0f;
+            for (int k = 0; k < N; k++) acc = fmaf(R32[(size_t)r * N + k], Qf(c, k), acc);
+            put_c(r, c, acc);
+        }
+        __syncthreads();
+    } else
+#endif
+    {
     // T1 = dF Z0^T (N x kv);  E = V T1 (nc x kv);  L' = Z0 T1 (kv x kv)
     tgemm32<true, true>(N, kv, N, [&](int i, int k) { return D[(size_t)i * N + k]; }, [&](int k, int t) { return Zf(t, k); }, false, sm,
                        [&](int i, int t, double v) { T1[(size_t)i * kv + t] = (float)v; });
@@ -983,6 +1102,7 @@ __device__ double density_step_pert(const SCFArgs &a, double *wsf, const double 
                        [&](int i, int j, double v) { T2[(size_t)i * nc + j] = (float)v; });
     tgemm32<true, false>(nc, nc, N, [&](int j, int k) { return Vf(j, k); }, [&](int k, int l) { return T2[(size_t)k * nc + l]; }, false, sm,
                         [&](int j, int l, double v) { Mp[(size_t)j * nc + l] = (float)v; });
+    }
     tm.add(PDG_T_PERT_COUPLING, t_coupling);
     const long long t_solve = tm.now();
     // K from first-order theory, or the previous step's K around the same base (warm_k), then the fixed-point
@@ -1085,7 +1205,6 @@ __device__ double density_step_pert(const SCFArgs &a, double *wsf, const double 
 // (closed shell, symmetrised).  The FP32 iterate lives in the workspace matrix A; the BF16 parts in the
 // shared-memory slot of the packed matrix.  Returns the RMS change of P, or -1 when a tensor-core wait ran
 // out (P is then left unchanged).
-struct TCState { uint32_t tmem, bar, phase; };
 
 // Sum of the BF16 parts of eight consecutive iterate elements (16 bytes of each part array).
 __device__ __forceinline__ void bf16_sum8(const uint4 &a, const uint4 &b, const uint4 &c, float *x)
@@ -1368,9 +1487,10 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
     for (int A = tid; A < s.n_atoms; A += PDG_BLOCK) { const double *E = elem(s, s.atom_elem[A]); base += E[PDG_E_EHEAT] - E[PDG_E_EISOL]; }
     base = block_sum(base, sm.red);
 #ifdef PDG_SCF_NO_TENSOR
-    const bool want_mixed = false;
+    const bool want_mixed = false, tc_pert = false;
 #else
     const bool want_mixed = tc_ok && a.fock_only != 1 && a.o.density_step != 0 && N <= 144 && sm.amat != nullptr;
+    const bool tc_pert = tc_ok && N <= 144 && sm.amat != nullptr;   // the perturbative steps' coupling products
 #endif
     bool mixed = want_mixed, last_mixed = false;
     int n_mixed = 0;
@@ -1720,7 +1840,9 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
             if (rms < o.mixed_switch || n_mixed >= 20) mixed = false;
         } else {
             double r = -1.0;
-            if (base_ok) r = density_step_pert(a, wsf, F, P, sm, tm, cur_base(), warm_k, use_shared ? PDG_PERT_KMAX_SHARED : PDG_PERT_KMAX);
+            if (base_ok) r = density_step_pert(a, wsf, F, P, sm, tm, cur_base(), warm_k, use_shared ? PDG_PERT_KMAX_SHARED : PDG_PERT_KMAX,
+                                               tc_pert ? &tc : nullptr);
+            if (r == -2.0) { st = PDG_TENSOR_TIMEOUT; break; }   // a tensor-core wait ran out
             warm_k = r >= 0.0;
             if (r >= 0.0) {
                 rms = r;
