@@ -929,21 +929,37 @@ __device__ bool tc_product_f32(TCState &tc, unsigned char *stage, int ma, int nb
     constexpr int KC = 32;
     const size_t pa = (size_t)TC_M * KC * 2, pbs = (size_t)Kp * KC * 2;   // bytes of one part of A and of B
     unsigned char *A0 = stage, *B0 = stage + 3 * pa;
+    // each thread's elements of a chunk: all loads first (independent, in flight together), then the splits and
+    // the shared-memory stores
+    constexpr int UA = TC_M * KC / PDG_BLOCK, UB = 144 * KC / PDG_BLOCK;
+    static_assert(TC_M * KC % PDG_BLOCK == 0 && 144 * KC % PDG_BLOCK == 0, "chunk elements per thread");
     for (int k0 = 0; k0 < K; k0 += KC) {
-        for (int e = tid; e < TC_M * KC; e += PDG_BLOCK) {
-            const int r = e / KC, c = e % KC, k = k0 + c;
-            const float x = (r < ma && k < K) ? fa(r, k) : 0.0f;
+        float va[UA], vb[UB];
+#pragma unroll
+        for (int u = 0; u < UA; u++) {
+            const int e = tid + u * PDG_BLOCK, r = e / KC, k = k0 + e % KC;
+            va[u] = (r < ma && k < K) ? fa(r, k) : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < UB; u++) {
+            const int e = tid + u * PDG_BLOCK, r = e / KC, k = k0 + e % KC;
+            vb[u] = (r < nb && r < Kp && k < K) ? fb(r, k) : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < UA; u++) {
+            const int e = tid + u * PDG_BLOCK;
             __nv_bfloat16 h, m, l;
-            bf16_split3(x, h, m, l);
-            const uint32_t o = tc_offset(r, c, KC);
+            bf16_split3(va[u], h, m, l);
+            const uint32_t o = tc_offset(e / KC, e % KC, KC);
             *(__nv_bfloat16 *)(A0 + o) = h; *(__nv_bfloat16 *)(A0 + pa + o) = m; *(__nv_bfloat16 *)(A0 + 2 * pa + o) = l;
         }
-        for (int e = tid; e < Kp * KC; e += PDG_BLOCK) {
-            const int r = e / KC, c = e % KC, k = k0 + c;
-            const float x = (r < nb && k < K) ? fb(r, k) : 0.0f;
+#pragma unroll
+        for (int u = 0; u < UB; u++) {
+            const int e = tid + u * PDG_BLOCK;
+            if (e >= Kp * KC) break;
             __nv_bfloat16 h, m, l;
-            bf16_split3(x, h, m, l);
-            const uint32_t o = tc_offset(r, c, KC);
+            bf16_split3(vb[u], h, m, l);
+            const uint32_t o = tc_offset(e / KC, e % KC, KC);
             *(__nv_bfloat16 *)(B0 + o) = h; *(__nv_bfloat16 *)(B0 + pbs + o) = m; *(__nv_bfloat16 *)(B0 + 2 * pbs + o) = l;
         }
         tc_fence_proxy();
@@ -1067,10 +1083,11 @@ __device__ double density_step_pert(const SCFArgs &a, double *wsf, const double 
         };
         if (!tc_product_f32(*tc, stage, min(N, TC_M), N, N, Kp, Qf, [&](int n, int k) { return D[(size_t)n * N + k]; })) return -2.0;
         tc_readout(*tc, Kp, N, [&](int r, int c, float v) { if (r < N) R32[(size_t)r * N + c] = v; });
-        for (int e = tid; e < (N - TC_M) * N; e += PDG_BLOCK) {   // R's rows >= 128
-            const int r = TC_M + e / N, c = e % N;
+        for (int e = tid; e < (N - TC_M) * N; e += PDG_BLOCK) {   // R's rows >= 128 (dF symmetric: column c of dF
+            const int r = TC_M + e / N, c = e % N;                // read along its rows, coalesced over c)
             float acc = 0.0f;
-            for (int k = 0; k < N; k++) acc = fmaf(Qf(r, k), D[(size_t)c * N + k], acc);
+#pragma unroll 4
+            for (int k = 0; k < N; k++) acc = fmaf(Qf(r, k), D[(size_t)k * N + c], acc);
             R32[(size_t)r * N + c] = acc;
         }
         __syncthreads();
@@ -1631,12 +1648,47 @@ __device__ __forceinline__ void scf_frame(const SCFArgs &a, const int f, double 
                     const float *Yp = (const float *)(wsf + pl.BW) + pert_y_offset(N, kv), *Wp = Yp + (size_t)kv * N;
                     auto Sv = [&](int t, int k) { return have_pert ? Z32[(size_t)t * N + k] + Yp[(size_t)t * N + k] : Z32[(size_t)t * N + k]; };
                     auto Tv = [&](int t, int k) { return have_pert ? Z32[(size_t)t * N + k] + Wp[(size_t)t * N + k] : Z32[(size_t)t * N + k]; };
-                    tgemm32<false, true>(N, kv, N, [&](int i, int k) { return DF[(size_t)k * N + i]; }, [&](int k, int t) { return Sv(t, k); },
-                                 false, sm, [&](int i, int t, double v) { G32[(size_t)t * N + i] = (float)v; });   // G^T = DF S^T
-                    tgemm32<false, false>(N, N, 2 * kv,
-                        [&](int i, int k) { return k < kv ? G32[(size_t)k * N + i] : Tv(k - kv, i); },
-                        [&](int k, int j) { return k < kv ? Tv(k, j) : -G32[(size_t)(k - kv) * N + j]; },
-                        true, sm, store);
+                    auto fa2 = [&](int i, int k) { return k < kv ? G32[(size_t)k * N + i] : Tv(k - kv, i); };
+                    auto fb2 = [&](int j, int k) { return k < kv ? Tv(k, j) : -G32[(size_t)(k - kv) * N + j]; };
+                    bool on_tc = false;
+#ifndef PDG_SCF_NO_TENSOR
+                    const int Kp = (N + 15) & ~15;
+                    if (tc_pert && kv <= TC_M && smem_plan(N, kv, a.smem_limit).amat * 8 >= (size_t)3 * (TC_M + Kp) * 64) {
+                        // on the tensor cores (the perturbative step's split-BF16 products): G = S dF (kv x N, dF
+                        // symmetric), then C = G^T T - T^T G, antisymmetric: its first 128 rows from the tensor cores,
+                        // the lower elements of rows >= 128 from their columns there (C(c, r) = -C(r, c)), the corner
+                        // of rows and columns >= 128 (N - 128 <= 16) on the FP32 cores
+                        on_tc = true;
+                        unsigned char *stage = (unsigned char *)sm.amat;
+                        if (!tc_product_f32(tc, stage, kv, N, N, Kp, Sv, [&](int i, int k) { return DF[(size_t)i * N + k]; })) {
+                            st = PDG_TENSOR_TIMEOUT;
+                            break;
+                        }
+                        tc_readout(tc, Kp, N, [&](int r, int c, float v) { if (r < kv) G32[(size_t)r * N + c] = v; });
+                        if (!tc_product_f32(tc, stage, min(N, TC_M), N, 2 * kv, Kp, fa2, fb2)) {
+                            st = PDG_TENSOR_TIMEOUT;
+                            break;
+                        }
+                        tc_readout(tc, Kp, N, [&](int r, int c, float v) {
+                            if (r >= N) return;
+                            if (c < r) store(r, c, (double)v);
+                            else if (c >= TC_M && c > r) store(c, r, -(double)v);
+                        });
+                        for (int e = tid; e < (N - TC_M) * (N - TC_M); e += PDG_BLOCK) {
+                            const int i = TC_M + e / (N - TC_M), j = TC_M + e % (N - TC_M);
+                            if (j >= i) continue;
+                            float acc = 0.0f;
+                            for (int k = 0; k < 2 * kv; k++) acc = fmaf(fa2(i, k), fb2(j, k), acc);
+                            store(i, j, (double)acc);
+                        }
+                        __syncthreads();
+                    }
+#endif
+                    if (!on_tc) {
+                        tgemm32<false, true>(N, kv, N, [&](int i, int k) { return DF[(size_t)k * N + i]; }, [&](int k, int t) { return Sv(t, k); },
+                                     false, sm, [&](int i, int t, double v) { G32[(size_t)t * N + i] = (float)v; });   // G^T = DF S^T
+                        tgemm32<false, false>(N, N, 2 * kv, fa2, [&](int k, int j) { return fb2(j, k); }, true, sm, store);
+                    }
                 } else {
                     double *G = wsf + pl.G;
                     tgemm<true, false>(kv, N, N, [&](int t, int k) { return Zc[(size_t)t * ldz + k]; }, [&](int k, int i) { return F[(size_t)k * N + i]; },
