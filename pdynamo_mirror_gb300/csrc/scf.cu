@@ -922,7 +922,9 @@ struct TCState { uint32_t tmem, bar, phase; };
 // and multiplied as hi.hi + hi.mid + mid.hi + hi.lo + lo.hi + mid.mid (the FP32 value to ~2^-24; the three dropped
 // products are below that).  K is staged in chunks of 32 columns through `stage` (shared memory, 16-byte aligned,
 // 3 * (128 + Kp) * 64 bytes), one commit and bounded wait per chunk.  False when a wait ran out.
-template <typename FA, typename FB>
+// AT / BT: the operand is stored with K as its slow index (a transposed accessor), so a chunk is read with
+// consecutive threads on consecutive rows (coalesced) instead of consecutive K.
+template <bool AT = false, bool BT = false, typename FA, typename FB>
 __device__ bool tc_product_f32(TCState &tc, unsigned char *stage, int ma, int nb, int K, int Kp, FA fa, FB fb)
 {
     const int tid = threadIdx.x;
@@ -935,22 +937,27 @@ __device__ bool tc_product_f32(TCState &tc, unsigned char *stage, int ma, int nb
     static_assert(TC_M * KC % PDG_BLOCK == 0 && 144 * KC % PDG_BLOCK == 0, "chunk elements per thread");
     for (int k0 = 0; k0 < K; k0 += KC) {
         float va[UA], vb[UB];
+        // element e of a chunk: row e / KC, column e % KC (K fastest), or row e % rows, column e / rows (transposed)
+        auto arow = [&](int e) { return AT ? e % TC_M : e / KC; };
+        auto acol = [&](int e) { return AT ? e / TC_M : e % KC; };
+        auto brow = [&](int e) { return BT ? e % Kp : e / KC; };
+        auto bcol = [&](int e) { return BT ? e / Kp : e % KC; };
 #pragma unroll
         for (int u = 0; u < UA; u++) {
-            const int e = tid + u * PDG_BLOCK, r = e / KC, k = k0 + e % KC;
+            const int e = tid + u * PDG_BLOCK, r = arow(e), k = k0 + acol(e);
             va[u] = (r < ma && k < K) ? fa(r, k) : 0.0f;
         }
 #pragma unroll
         for (int u = 0; u < UB; u++) {
-            const int e = tid + u * PDG_BLOCK, r = e / KC, k = k0 + e % KC;
-            vb[u] = (r < nb && r < Kp && k < K) ? fb(r, k) : 0.0f;
+            const int e = tid + u * PDG_BLOCK, r = brow(e), k = k0 + bcol(e);
+            vb[u] = (e < Kp * KC && r < nb && k < K) ? fb(r, k) : 0.0f;
         }
 #pragma unroll
         for (int u = 0; u < UA; u++) {
             const int e = tid + u * PDG_BLOCK;
             __nv_bfloat16 h, m, l;
             bf16_split3(va[u], h, m, l);
-            const uint32_t o = tc_offset(e / KC, e % KC, KC);
+            const uint32_t o = tc_offset(arow(e), acol(e), KC);
             *(__nv_bfloat16 *)(A0 + o) = h; *(__nv_bfloat16 *)(A0 + pa + o) = m; *(__nv_bfloat16 *)(A0 + 2 * pa + o) = l;
         }
 #pragma unroll
@@ -959,7 +966,7 @@ __device__ bool tc_product_f32(TCState &tc, unsigned char *stage, int ma, int nb
             if (e >= Kp * KC) break;
             __nv_bfloat16 h, m, l;
             bf16_split3(vb[u], h, m, l);
-            const uint32_t o = tc_offset(e / KC, e % KC, KC);
+            const uint32_t o = tc_offset(brow(e), bcol(e), KC);
             *(__nv_bfloat16 *)(B0 + o) = h; *(__nv_bfloat16 *)(B0 + pbs + o) = m; *(__nv_bfloat16 *)(B0 + 2 * pbs + o) = l;
         }
         tc_fence_proxy();
@@ -1193,19 +1200,23 @@ __device__ double density_step_pert(const SCFArgs &a, double *wsf, const double 
     // dQ = Z0^T W + Y^T (Z0 + W) (symmetric; lower triangle) and P = P0 +- 2 dQ
     const double c = s.vec_occupied ? 2.0 : -2.0;
     double rms = 0.0;
-    tgemm32<false, false>(N, N, 2 * kv,
-        [&](int i, int k) { return k < kv ? Zf(k, i) : Y[(size_t)(k - kv) * N + i]; },
-        [&](int k, int j) { return k < kv ? Wz[(size_t)k * N + j] : Zf(k - kv, j) + Wz[(size_t)(k - kv) * N + j]; },
-        true, sm, [&](int i, int j, double v) {
-            if (j > i) return;
-            const double pn = BP[(size_t)i * N + j] + c * v;
-            const double dlt = pn - P[(size_t)i * N + j];
-            rms += (i == j) ? dlt * dlt : 2.0 * dlt * dlt;
-            P[(size_t)i * N + j] = pn;
-            P[(size_t)j * N + i] = pn;
-            DQ[(size_t)i * N + j] = (float)v;
-            DQ[(size_t)j * N + i] = (float)v;
-        });
+    auto dqa = [&](int i, int k) { return k < kv ? Zf(k, i) : Y[(size_t)(k - kv) * N + i]; };
+    auto dqb = [&](int j, int k) { return k < kv ? Wz[(size_t)k * N + j] : Zf(k - kv, j) + Wz[(size_t)(k - kv) * N + j]; };
+    auto dq_put = [&](int i, int j, double v) {   // i >= j
+        const double pn = BP[(size_t)i * N + j] + c * v;
+        const double dlt = pn - P[(size_t)i * N + j];
+        rms += (i == j) ? dlt * dlt : 2.0 * dlt * dlt;
+        P[(size_t)i * N + j] = pn;
+        P[(size_t)j * N + i] = pn;
+        DQ[(size_t)i * N + j] = (float)v;
+        DQ[(size_t)j * N + i] = (float)v;
+    };
+    // (on the FP32 cores: P takes dQ at full weight, and around a frame's own base the steps need its rounding at
+    // ~1e-10, which the tensor-core products' FP32 accumulation does not keep)
+    tgemm32<false, false>(N, N, 2 * kv, dqa, [&](int k, int j) { return dqb(j, k); }, true, sm, [&](int i, int j, double v) {
+        if (j > i) return;
+        dq_put(i, j, v);
+    });
     const double out = sqrt(block_sum(rms, sm.red)) / (double)N;
     tm.add(PDG_T_PERT_DENSITY, t_density);
     if (tid == 0) tm.slot[PDG_T_PERT_STEPS] += 1.0;
